@@ -1,0 +1,210 @@
+/*
+ * uwg.h -- C ABI of libuwg, the GB300 (sm_103a) particle-in-cell Stokes path.
+ *
+ * Conventions
+ *   - Every array argument is a DEVICE pointer unless its name ends in _h.
+ *   - The caller owns particle arrays; a context owns the mesh geometry, the
+ *     assembled operators and the solver workspaces.
+ *   - Every call is ordered on the context's stream (uwg_set_stream) and
+ *     returns UWG_OK (0) or a negative UWG_ERR_* code; uwg_last_error()
+ *     gives the message.  Calls that return values to the host
+ *     (statistics, counts, dt) synchronise the stream before returning.
+ *   - No exception or device trap crosses this boundary.
+ *
+ * Each entry point names the reference native call it replaces; the Python
+ * layer in underworld2_gb300/ calls them where underworld2's Python layer
+ * calls those functions through SWIG.  Citations:
+ *   L/ = src/underworld/libUnderworld/,  P/ = src/underworld/
+ */
+#ifndef UWG_H
+#define UWG_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define UWG_OK 0
+#define UWG_ERR_ARG (-1)            /* invalid argument */
+#define UWG_ERR_CUDA (-2)           /* CUDA runtime failure */
+#define UWG_ERR_STATE (-3)          /* call out of order (e.g. solve before assemble) */
+#define UWG_ERR_EMPTY_CELL (-4)     /* an element holds no particle (DVC needs >= 1) */
+#define UWG_ERR_CELL_FULL (-5)      /* more particles in one element than the kernels hold */
+#define UWG_ERR_NOT_CONVERGED (-6)  /* a Krylov solve hit its iteration cap */
+#define UWG_ERR_NAN (-7)            /* non-finite value met in a solve */
+#define UWG_ERR_PARTICLE_LOST (-8)  /* particles left the domain */
+
+typedef struct uwg_ctx uwg_ctx;
+
+/* Mesh description: regular Cartesian box, Q1 (order 1) or Q2 (order 2)
+ * velocity elements, dQ0 (porder 0) or dPc1 (porder 1) pressure.
+ * Replaces FeMesh_Cartesian construction (P/mesh/_mesh.py:1105-1160) over
+ * CartesianGenerator / C2Generator (L/StgDomain/Mesh/src/CartesianGenerator.c,
+ * L/StgFEM/Discretisation/src/C2Generator.c). */
+typedef struct {
+    int dim;
+    int order;
+    int porder;
+    int res[3];
+    double minc[3];
+    double maxc[3];
+} uwg_mesh_desc;
+
+int uwg_ctx_create(const uwg_mesh_desc* desc, uwg_ctx** out);
+void uwg_ctx_destroy(uwg_ctx* ctx);
+const char* uwg_last_error(const uwg_ctx* ctx);
+int uwg_set_stream(uwg_ctx* ctx, void* cuda_stream);
+int uwg_sync(uwg_ctx* ctx);
+/* sizes: n_el, n_nodes (velocity), n_vdof, n_pdof, nen, npn */
+int uwg_mesh_sizes(const uwg_ctx* ctx, int64_t* sizes_h);
+/* node coordinates per axis, copied to host arrays of length res*order+1 */
+int uwg_mesh_axis(const uwg_ctx* ctx, int axis, double* coords_h);
+
+/* Seeded per-cell uniform-random particle layout: cells in order, particles
+ * in order, dims in order, one Park-Miller stream seeded with seed^123459876.
+ * Writes x[n_el*ppc][dim], owner[n_el*ppc] and the cell tables
+ * (cell_offsets[n_el+1], cell_list[n_el*ppc]).  *rng_state_h is the stream
+ * state before the first draw and is advanced past the last one.
+ * Replaces ParticleLayout_InitialiseParticles for PerCellRandomLayout
+ * (L/StgFEM/Utils/src/MeshParticleLayout.c:194-230,
+ *  L/StgDomain/Swarm/src/Random.c:23-53, P/swarm/layouts.py:186-231). */
+int uwg_layout_random(uwg_ctx* ctx, int ppc, int64_t* rng_state_h, double* x, int32_t* owner,
+                      int32_t* cell_offsets, int32_t* cell_list);
+
+/* Element that owns each particle (n_el when outside the mesh), no table
+ * edits.  Replaces CellLayout_CellOf / _ElementCellLayout_CellOf
+ * (L/StgDomain/Swarm/src/ElementCellLayout.c:291-320) over
+ * Mesh_RegularAlgorithms_SearchElements (L/StgDomain/Mesh/src/Mesh_RegularAlgorithms.c:174-205). */
+int uwg_locate(uwg_ctx* ctx, int64_t np, const double* x, int32_t* owner);
+
+/* Owner update with the reference's cell-table semantics: particles are
+ * visited in index order, a leaver is removed from its old cell by
+ * swap-with-last, an arrival is appended.  cell_offsets/cell_list are
+ * rewritten in place.  *n_lost_h = particles now outside the mesh (their
+ * owner is n_el).  Replaces Swarm_UpdateAllParticleOwners
+ * (L/StgDomain/Swarm/src/SwarmClass.c:947-1015). */
+int uwg_update_owners(uwg_ctx* ctx, int64_t np, const double* x, int32_t* owner,
+                      int32_t* cell_offsets, int32_t* cell_list, int64_t* n_lost_h);
+
+/* Coincident mapping: the local coordinate of every particle in its element,
+ * by the Newton iteration of _ElementType_ConvertGlobalCoordToElLocal.
+ * ip_xi is written in cell-table slot order: [cell_offsets[e]+k][dim] is
+ * particle cell_list[cell_offsets[e]+k].  Replaces _CoincidentMapper_Map
+ * (L/PICellerator/MaterialPoints/src/CoincidentMapper.c:76-125,
+ *  L/StgFEM/Discretisation/src/ElementType.c:177-301). */
+int uwg_pic_map(uwg_ctx* ctx, int64_t np, const double* x, const int32_t* cell_offsets,
+                const int32_t* cell_list, double* ip_xi);
+
+/* Discrete Voronoi cell weights on a res^dim grid per element: ip_xi is
+ * replaced by the centroid of each particle's cells, ip_w = cells * cell
+ * volume.  Slot order as uwg_pic_map.  Replaces WeightsCalculator_CalculateAll
+ * with DVCWeights (L/PICellerator/Weights/src/DVCWeights.c:772-927). */
+int uwg_dvc_weights(uwg_ctx* ctx, int res, const int32_t* cell_offsets, double* ip_xi,
+                    double* ip_w);
+
+/* Dirichlet conditions: bc_mask[n_vdof] (1 = fixed), values[n_vdof].
+ * Replaces FeVariable_SetBC + SystemLinearEquations_BC_Setup
+ * (P/systems/_stokes.py:194-204, L/StgFEM/SLE/SystemSetup/src/SystemLinearEquations.c:521). */
+int uwg_set_bcs(uwg_ctx* ctx, const uint8_t* bc_mask, const double* values);
+
+/* Assembly of the Stokes operators from the PIC integration swarm:
+ *  - viscous operator K from the points (ip_xi, ip_w) with per-particle
+ *    viscosity eta_p (stored as exact equivalent-quadrature weights per element);
+ *  - f from the body force body_p[np][dim] at the points;
+ *  - G from Gauss quadrature (geometry only);
+ *  - the Schur preconditioner S_e = G_e^T diag(K_e)^-1 G_e;
+ *  - optional compressibility (pressure mass) from lambda_p (may be NULL);
+ *  - Dirichlet lifting of f and h.
+ * Replaces SystemLinearEquations_MatrixSetup / VectorSetup
+ * (L/StgFEM/SLE/SystemSetup/src/StiffnessMatrix.c:552-744, ForceVector.c:231-361)
+ * with the terms ConstitutiveMatrixCartesian (L/Underworld/Rheology/src/
+ * ConstitutiveMatrixCartesian.cpp:238-429), GradientStiffnessMatrixTerm
+ * (L/StgFEM/Assembly/src/GradientStiffnessMatrixTerm.c:129-219),
+ * UzawaPreconditionerTerm (L/StgFEM/SLE/ProvidedSystems/StokesFlow/src/
+ * UzawaPreconditionerTerm.c:124-207), VectorAssemblyTerm_NA__Fn and
+ * MatrixAssemblyTerm_NA__NB__Fn (L/Underworld/Utils/src/). */
+int uwg_assemble(uwg_ctx* ctx, int64_t np, const int32_t* cell_offsets, const int32_t* cell_list,
+                 const double* ip_xi, const double* ip_w, const double* eta_p,
+                 const double* body_p, const double* lambda_p);
+
+/* Element matrices of one element as assembled (host outputs, for checks):
+ * Ke_h[(dim*nen)^2], fe_h[dim*nen], Ge_h[dim*nen*npn], Se_h[npn*npn]. */
+int uwg_element_matrices(uwg_ctx* ctx, int64_t el, double* Ke_h, double* fe_h, double* Ge_h,
+                         double* Se_h);
+
+typedef struct {
+    int mixed;             /* 0: plain FP64 inner solves, 1: FP32 inner solves with FP64 refinement */
+    double rtol;           /* target ||[f-Ku-Gp ; h-G^T u]|| / ||[f;h]|| */
+    double inner_rtol;     /* relative tolerance of each velocity solve */
+    double outer_rtol;     /* relative tolerance of the Schur solve */
+    int max_inner;
+    int max_outer;
+    int mg_levels;         /* 0 = reference rule (halvings + 1) */
+    int smooth_steps;      /* Chebyshev degree per smoothing */
+    int restart;           /* FGMRES restart length */
+    int zero_guess;        /* 1: start from u=p=0, else from the given u, p */
+} uwg_solve_opts;
+
+typedef struct {
+    int pressure_its;
+    int velocity_presolve_its;
+    int velocity_pressuresolve_its;
+    int velocity_backsolve_its;
+    int velocity_total_its;
+    int refinement_steps;
+    double setup_time, presolve_time, pressure_time, backsolve_time, total_time;
+    double residual;       /* final relative residual of the full system, FP64 */
+    double vmin, vmax, pmin, pmax;
+    int fhat_reason, outer_reason, backsolve_reason; /* >0 converged, <0 not */
+} uwg_solve_stats;
+
+void uwg_solve_opts_default(uwg_solve_opts* o);
+
+/* BSSCR Schur-complement solve: f~ = K^-1 f, h^ = h - G^T f~, solve
+ * (G^T K^-1 G) p = -h^ with the Schur preconditioner, then K u = f - G p.
+ * u[n_vdof] (node-major, dof-minor, Dirichlet dofs carry their values) and
+ * p[n_pdof] in/out.  Replaces SystemLinearEquations_ExecuteSolver ->
+ * _StokesBlockKSPInterface_Solve -> KSPSolve_BSSCR -> BSSCR_DRIVER_auglag
+ * (L/Solvers/KSPSolvers/src/StokesBlockKSPInterface.c:275-448,
+ *  L/Solvers/KSPSolvers/src/BSSCR/BSSCR.c:163-247,
+ *  L/Solvers/KSPSolvers/src/BSSCR/auglag-driver-DGTGD.c:64-578). */
+int uwg_stokes_solve(uwg_ctx* ctx, const uwg_solve_opts* opts, double* u, double* p,
+                     uwg_solve_stats* stats_h);
+
+/* Residual norms ||f - K u - G p|| and ||h - G^T u|| (free dofs), FP64.
+ * Replaces Stokes_MomentumResidual / Stokes_ContinuityResidual
+ * (L/StgFEM/SLE/ProvidedSystems/StokesFlow/src/Stokes_SLE.c:204-256). */
+int uwg_stokes_residuals(uwg_ctx* ctx, const double* u, const double* p, double* res_h);
+
+/* Operator applications on full node-major vectors (Dirichlet dofs masked),
+ * for tests and the benchmark: y = K x (FP64 or FP32), y = G p, q = G^T u. */
+int uwg_apply_K64(uwg_ctx* ctx, int level, const double* x, double* y);
+int uwg_apply_K32(uwg_ctx* ctx, int level, const float* x, float* y);
+int uwg_apply_G(uwg_ctx* ctx, const double* p, double* y);
+int uwg_apply_Gt(uwg_ctx* ctx, const double* u, double* q);
+
+/* Midpoint RK2 advection of every particle through the velocity field
+ * vel[n_nodes][dim], with the first-order fallback when the midpoint
+ * evaluation fails.  *n_fallback_h / *n_failed_h count fallbacks and
+ * particles whose first evaluation failed (left untouched).
+ * Replaces _TimeIntegrator_Execute -> _TimeIntegrator_ExecuteRK2 ->
+ * TimeIntegrand_SecondOrder with _SwarmAdvector_TimeDeriv
+ * (L/StgDomain/Utils/src/TimeIntegrator.c:292-329,
+ *  L/StgDomain/Utils/src/TimeIntegrand.c:249-319,441-468,
+ *  L/PICellerator/MaterialPoints/src/SwarmAdvector.c:238-312). */
+int uwg_rk2_advect(uwg_ctx* ctx, int64_t np, double dt, const double* vel, double* x,
+                   int64_t* n_fallback_h, int64_t* n_failed_h);
+
+/* Velocity at arbitrary points (Mesh_SearchElements + Newton + basis);
+ * points outside get NaN.  Replaces FieldVariable_InterpolateValueAt
+ * (L/StgFEM/Discretisation/src/FeVariable.c:389-403). */
+int uwg_interpolate(uwg_ctx* ctx, int64_t n, const double* pts, const double* vel, double* out);
+
+/* dt = 0.5 * minimum node separation / max |v|.  Replaces SwarmAdvector_MaxDt
+ * (L/PICellerator/MaterialPoints/src/SwarmAdvector.c:370-387). */
+int uwg_max_dt(uwg_ctx* ctx, const double* vel, double* dt_h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,206 @@
+"""GPU parity of the PIC Stokes path against the CPU oracle (through the C ABI).
+
+Bit-exact: particle layout, element ownership, Newton local coordinates, DVC
+centroids and weights, RK2 positions, owner update and cell tables.
+Tolerance: element matrices 1e-10 relative (FP64), operator applies 1e-12,
+solutions 1e-7 relative to the field scale (both sides converged to 1e-10).
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from tests import oracle_system
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    (2, (8, 8), 5),
+    (2, (7, 5), 3),
+    (3, (4, 4, 4), 4),
+    (3, (3, 2, 5), 6),
+]
+
+
+def _ctx(dim, res):
+    from underworld2_gb300._core import Context
+    return Context(dim, res, (0.0,) * dim, (1.0,) * dim)
+
+
+def _oracle_mesh(dim, res):
+    return oracle.Mesh(dim, 1, res, (0.0,) * dim, (1.0,) * dim)
+
+
+@pytest.mark.parametrize("dim,res,ppc", CASES)
+def test_layout_locate_map_dvc_bit_exact(gpu, dim, res, ppc):
+    from underworld2_gb300._core import rng_seed
+    c = _ctx(dim, res)
+    m = _oracle_mesh(dim, res)
+    x, owner, off, lst, st = c.layout_random(ppc, rng_seed(13))
+    xo, sto = m.layout_random(ppc, 13)
+    assert st == sto
+    np.testing.assert_array_equal(x.cpu().numpy(), xo)
+    np.testing.assert_array_equal(c.locate(x).cpu().numpy(), m.cell_of(xo))
+    ip_xi = c.pic_map(x, off, lst)
+    tbl, cnt, _ = m.initial_tables(ppc, ppc)
+    ref_xi = np.stack([m.global_to_local(e, xo[p])[0] for e in range(m.n_el) for p in tbl[e]])
+    np.testing.assert_array_equal(ip_xi.cpu().numpy(), ref_xi)
+    ip_w = c.dvc_weights(off, ip_xi)
+    oxi, ow = m.pic_map(xo, tbl, cnt)
+    slots = np.concatenate([tbl[e, : cnt[e]] for e in range(m.n_el)])
+    np.testing.assert_array_equal(ip_xi.cpu().numpy(), oxi[slots])
+    np.testing.assert_array_equal(ip_w.cpu().numpy(), ow[slots])
+
+
+def test_dvc_golden_suite(gpu):
+    """The reference's DVC suite particle sets (10 particles, 10^d grid), one element."""
+    import json, os
+    g = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "golden.json")))["dvc_suite"]
+    for dim in (2, 3):
+        p = np.array(g["particles_%dd" % dim])
+        c = _ctx(dim, (1,) * dim)
+        off = torch.tensor([0, len(p)], dtype=torch.int32, device="cuda")
+        xi = torch.tensor(p, dtype=torch.float64, device="cuda")
+        w = c.dvc_weights(off, xi, res=10)
+        np.testing.assert_allclose(xi.cpu().numpy(), np.array(g["centroids_%dd" % dim]), atol=1e-6)
+        np.testing.assert_allclose(w.cpu().numpy(), np.array(g["weights_%dd" % dim]), atol=1e-12)
+        cx, wo, _ = oracle.dvc_element(dim, 10, p)
+        np.testing.assert_array_equal(xi.cpu().numpy(), cx)
+
+
+def _circle_problem(dim, res, ppc):
+    """Sinker: circle/sphere of radius 0.1 at (0.5, 0.6[, 0.5]), eta 100, rho 1."""
+    from underworld2_gb300._core import rng_seed
+    c = _ctx(dim, res)
+    m = _oracle_mesh(dim, res)
+    x, owner, off, lst, _ = c.layout_random(ppc, rng_seed(13))
+    xo, _ = m.layout_random(ppc, 13)
+    centre = np.array([0.5, 0.6, 0.5][:dim])
+    inside = np.sum((xo - centre) ** 2, axis=1) < 0.1 ** 2
+    eta = np.where(inside, 100.0, 1.0)
+    body = np.zeros((len(xo), dim))
+    body[:, 1] = np.where(inside, -1.0, 0.0)
+    # free-slip walls
+    nodes = m.node_coords()
+    mask = np.zeros((m.n_nodes, dim), np.uint8)
+    for d in range(dim):
+        mask[:, d] = (np.isclose(nodes[:, d], 0.0) | np.isclose(nodes[:, d], 1.0)).astype(np.uint8)
+    return c, m, (x, owner, off, lst), xo, eta, body, mask.ravel()
+
+
+@pytest.mark.parametrize("dim,res,ppc", [(2, (8, 8), 20), (3, (4, 4, 4), 8)])
+def test_assembly_and_operators(gpu, dim, res, ppc):
+    c, m, (x, owner, off, lst), xo, eta, body, mask = _circle_problem(dim, res, ppc)
+    ip_xi = c.pic_map(x, off, lst)
+    ip_w = c.dvc_weights(off, ip_xi)
+    c.set_bcs(torch.tensor(mask, device="cuda"))
+    eta_t = torch.tensor(eta, device="cuda")
+    body_t = torch.tensor(body, device="cuda")
+    c.assemble(off, lst, ip_xi, ip_w, eta_t, body_t)
+    tbl, cnt, _ = m.initial_tables(ppc, ppc)
+    oxi, ow = m.pic_map(xo, tbl, cnt)
+    pts = oracle_system.pic_points_by_element(tbl, cnt, oxi, ow)
+    for e in [0, m.n_el // 2, m.n_el - 1]:
+        Ke, Ge, Se = c.element_matrices(e)
+        ps, xi, w = pts[e]
+        Ko = m.element_K(e, xi, w, eta[ps])
+        assert np.abs(Ke - Ko).max() <= 1e-10 * np.abs(Ko).max()
+        gxi, gw = m.gauss_points()
+        Go = m.element_G(e, gxi, gw)
+        assert np.abs(Ge - Go).max() <= 1e-12 * np.abs(Go).max()
+        So = m.element_S(Ko, Go)
+        assert abs(Se[0, 0] - So[0, 0]) <= 1e-10 * abs(So[0, 0])
+    sysd = oracle_system.assemble(m, pts, eta, body, mask, np.zeros(len(mask)))
+    rng = np.random.default_rng(0)
+    xv = rng.standard_normal(m.n_nodes * dim) * (mask == 0)
+    y = c.apply_K(torch.tensor(xv, device="cuda")).cpu().numpy()
+    yo = sysd["K"] @ xv
+    free = mask == 0
+    assert np.abs(y[free] - yo[free]).max() <= 1e-12 * np.abs(yo).max()
+    y32 = c.apply_K(torch.tensor(xv, device="cuda", dtype=torch.float32)).cpu().numpy()
+    assert np.abs(y32[free] - yo[free]).max() <= 1e-5 * np.abs(yo).max()
+    pv = rng.standard_normal(m.n_el)
+    yg = c.apply_G(torch.tensor(pv, device="cuda")).cpu().numpy()
+    assert np.abs(yg[free] - (sysd["G"] @ pv)[free]).max() <= 1e-12 * np.abs(yg).max()
+    q = c.apply_Gt(torch.tensor(xv, device="cuda")).cpu().numpy()
+    assert np.abs(q - sysd["G"].T @ xv).max() <= 1e-12 * np.abs(q).max()
+
+
+@pytest.mark.parametrize("mixed", [0, 1])
+@pytest.mark.parametrize("dim,res,ppc", [(2, (16, 16), 20), (3, (4, 4, 4), 8)])
+def test_solve_matches_direct(gpu, dim, res, ppc, mixed):
+    c, m, (x, owner, off, lst), xo, eta, body, mask = _circle_problem(dim, res, ppc)
+    ip_xi = c.pic_map(x, off, lst)
+    ip_w = c.dvc_weights(off, ip_xi)
+    c.set_bcs(torch.tensor(mask, device="cuda"))
+    c.assemble(off, lst, ip_xi, ip_w, torch.tensor(eta, device="cuda"), torch.tensor(body, device="cuda"))
+    u = c.zeros(m.n_nodes * dim)
+    p = c.zeros(m.n_el)
+    st = c.solve(u, p, mixed=mixed, rtol=1e-8, inner_rtol=1e-11, outer_rtol=1e-10)
+    assert st["residual"] <= 1e-8, st
+    tbl, cnt, _ = m.initial_tables(ppc, ppc)
+    oxi, ow = m.pic_map(xo, tbl, cnt)
+    pts = oracle_system.pic_points_by_element(tbl, cnt, oxi, ow)
+    sysd = oracle_system.assemble(m, pts, eta, body, mask, np.zeros(len(mask)))
+    uo, po = oracle_system.solve(sysd, m.n_nodes * dim)
+    ug = u.cpu().numpy()
+    pg = p.cpu().numpy()
+    pg = pg - pg.mean()
+    assert np.abs(ug - uo).max() <= 1e-7 * np.abs(uo).max()
+    assert np.abs(pg - po).max() <= 1e-7 * np.abs(po).max()
+    # advection: velocity field from the solve, one RK2 step at the reference's max dt
+    vel = u.view(-1, dim)
+    dt = c.max_dt(u)
+    vmax = np.sqrt((uo.reshape(-1, dim) ** 2).sum(1)).max()
+    assert abs(dt - 0.5 * (1.0 / max(res)) / vmax) <= 1e-6 * dt
+    x_gpu = x.clone()
+    fb, failed = c.rk2(x_gpu, u, dt)
+    x_or, counts = m.rk2(ug, dt, xo.copy())
+    assert failed == counts[0] and fb == counts[1]
+    np.testing.assert_array_equal(x_gpu.cpu().numpy(), x_or)
+
+
+@pytest.mark.parametrize("dim,res", [(2, (6, 6)), (3, (3, 3, 3))])
+def test_owner_update_tables(gpu, dim, res):
+    """Random moves; owners and cell tables equal the sequential reference semantics."""
+    from underworld2_gb300._core import rng_seed
+    c = _ctx(dim, res)
+    m = _oracle_mesh(dim, res)
+    ppc = 6
+    x, owner, off, lst, _ = c.layout_random(ppc, rng_seed(7))
+    xo, _ = m.layout_random(ppc, 7)
+    tbl, cnt, own_o = m.initial_tables(ppc, 64)
+    rng = np.random.default_rng(3)
+    for step in range(4):
+        delta = rng.uniform(-0.3, 0.3, xo.shape) / max(res)
+        xo = np.clip(xo + delta, 0.0, 1.0)
+        if step == 2:
+            xo[5] = [1.2] + [0.5] * (dim - 1)     # leaves the domain
+        x = torch.tensor(xo, device="cuda")
+        lost = c.update_owners(x, owner, off, lst)
+        lost_o = m.update_owners(xo, own_o, tbl, cnt)
+        assert lost == lost_o
+        np.testing.assert_array_equal(owner.cpu().numpy(), own_o)
+        offn = off.cpu().numpy()
+        lstn = lst.cpu().numpy()
+        for e in range(m.n_el):
+            np.testing.assert_array_equal(lstn[offn[e]: offn[e + 1]], tbl[e, : cnt[e]])
+
+
+def test_golden_known_answers(gpu):
+    import json, os
+    g = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "golden.json")))
+    from underworld2_gb300._core import rng_seed
+    c = _ctx(2, (1, 1))
+    x, *_ = c.layout_random(4, rng_seed(13))
+    np.testing.assert_allclose(x.cpu().numpy(), np.array(g["layout_seed13_1x1_ppc4"]), atol=5e-9)
+    from underworld2_gb300._core import Context
+    c = Context(2, (9, 9), (-1.0, -1.0), (1.0, 1.0))
+    vel = torch.ones(c.n_nodes * 2, dtype=torch.float64, device="cuda")
+    dt = c.max_dt(vel)
+    pts = torch.tensor([g["rk2_9x9"]["start"]], dtype=torch.float64, device="cuda")
+    c.rk2(pts, vel, dt)
+    np.testing.assert_allclose(pts.cpu().numpy()[0], g["rk2_9x9"]["end"], atol=5e-9)
+    c = Context(2, (16, 16), (0.0, 0.0), (1.0, 1.0))
+    own = c.locate(torch.tensor([g["owner_16x16"]["point"]], dtype=torch.float64, device="cuda"))
+    assert int(own.cpu()[0]) == g["owner_16x16"]["cell"]

@@ -1,0 +1,182 @@
+"""Device-side state and thin wrappers over the libuwg C ABI.
+
+``Context`` owns one libuwg context (mesh geometry, assembled operators,
+solver workspaces) and ``SwarmState`` the particle arrays of one swarm.
+PyTorch is used only to hold device memory and to name the CUDA stream.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _native
+
+_MASK = 123459876
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _require_cuda():
+    if not torch.cuda.is_available():
+        raise RuntimeError("underworld2_gb300 needs a CUDA GPU (sm_103a); none is visible")
+
+
+class Context:
+    """One regular Cartesian Q1/dQ0 mesh on the current CUDA device."""
+
+    def __init__(self, dim, res, minc, maxc, order=1, porder=0, device=None):
+        _require_cuda()
+        self.L = _native.load()
+        self.device = torch.device(device or "cuda")
+        d = _native.MeshDesc()
+        d.dim, d.order, d.porder = dim, order, porder
+        for i in range(3):
+            d.res[i] = int(res[i]) if i < dim else 1
+            d.minc[i] = float(minc[i]) if i < dim else 0.0
+            d.maxc[i] = float(maxc[i]) if i < dim else 1.0
+        self.desc = d
+        self.dim, self.order, self.porder = dim, order, porder
+        self.res = tuple(int(r) for r in res[:dim])
+        self.minc = tuple(float(v) for v in minc[:dim])
+        self.maxc = tuple(float(v) for v in maxc[:dim])
+        with torch.cuda.device(self.device):
+            torch.cuda.current_stream().synchronize()
+            h = _native._CTX()
+            rc = self.L.uwg_ctx_create(ctypes.byref(d), ctypes.byref(h))
+            if rc != 0:
+                raise _native.UwgError(rc, "uwg_ctx_create failed (dim=%d order=%d porder=%d res=%s)"
+                                       % (dim, order, porder, self.res))
+            self.h = h
+        sizes = np.zeros(8, np.int64)
+        self.L.uwg_mesh_sizes(self.h, ctypes.c_void_p(sizes.ctypes.data))
+        self.n_el, self.n_nodes, self.n_vdof, self.n_pdof, self.nen, self.npn, self.nlev = (int(v) for v in sizes[:7])
+        self.axes = []
+        for a in range(dim):
+            buf = np.zeros(self.res[a] * order + 1)
+            self.L.uwg_mesh_axis(self.h, a, ctypes.c_void_p(buf.ctypes.data))
+            self.axes.append(buf)
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                self.L.uwg_ctx_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+    # -- helpers -------------------------------------------------------------
+    def _stream(self):
+        s = torch.cuda.current_stream(self.device).cuda_stream
+        self.L.uwg_set_stream(self.h, ctypes.c_void_p(s))
+
+    def _call(self, name, *args):
+        self._stream()
+        return _native.check(self.h, getattr(self.L, name)(self.h, *args))
+
+    def zeros(self, *shape, dtype=torch.float64):
+        return torch.zeros(*shape, dtype=dtype, device=self.device)
+
+    # -- particles -----------------------------------------------------------
+    def layout_random(self, ppc, rng_state):
+        np_ = self.n_el * ppc
+        x = self.zeros(np_, self.dim)
+        owner = self.zeros(np_, dtype=torch.int32)
+        off = self.zeros(self.n_el + 1, dtype=torch.int32)
+        lst = self.zeros(np_, dtype=torch.int32)
+        st = ctypes.c_int64(rng_state)
+        self._call("uwg_layout_random", int(ppc), ctypes.byref(st), _ptr(x), _ptr(owner), _ptr(off), _ptr(lst))
+        return x, owner, off, lst, st.value
+
+    def locate(self, x):
+        owner = self.zeros(x.shape[0], dtype=torch.int32)
+        self._call("uwg_locate", x.shape[0], _ptr(x), _ptr(owner))
+        return owner
+
+    def update_owners(self, x, owner, off, lst):
+        lost = ctypes.c_int64(0)
+        self._call("uwg_update_owners", x.shape[0], _ptr(x), _ptr(owner), _ptr(off), _ptr(lst), ctypes.byref(lost))
+        return lost.value
+
+    def pic_map(self, x, off, lst):
+        ip_xi = self.zeros(x.shape[0], self.dim)
+        self._call("uwg_pic_map", x.shape[0], _ptr(x), _ptr(off), _ptr(lst), _ptr(ip_xi))
+        return ip_xi
+
+    def dvc_weights(self, off, ip_xi, res=15):
+        ip_w = self.zeros(ip_xi.shape[0])
+        self._call("uwg_dvc_weights", int(res), _ptr(off), _ptr(ip_xi), _ptr(ip_w))
+        return ip_w
+
+    # -- assembly and solve ----------------------------------------------------
+    def set_bcs(self, mask, values=None):
+        mask = mask.to(self.device, torch.uint8).contiguous()
+        values = None if values is None else values.to(self.device, torch.float64).contiguous()
+        self._call("uwg_set_bcs", _ptr(mask), _ptr(values))
+
+    def assemble(self, off, lst, ip_xi, ip_w, eta, body=None, one_on_lambda=None):
+        self._call("uwg_assemble", lst.shape[0], _ptr(off), _ptr(lst), _ptr(ip_xi), _ptr(ip_w), _ptr(eta),
+                   _ptr(body), _ptr(one_on_lambda))
+
+    def element_matrices(self, el):
+        nd = self.dim * self.nen
+        Ke = np.zeros((nd, nd))
+        fe = np.zeros(nd)
+        Ge = np.zeros((nd, self.npn))
+        Se = np.zeros((self.npn, self.npn))
+        p = lambda a: ctypes.c_void_p(a.ctypes.data)
+        self._call("uwg_element_matrices", int(el), p(Ke), p(fe), p(Ge), p(Se))
+        return Ke, Ge, Se
+
+    def solve(self, u, p, **opts):
+        o = _native.SolveOpts()
+        self.L.uwg_solve_opts_default(ctypes.byref(o))
+        for k, v in opts.items():
+            if not hasattr(o, k):
+                raise ValueError("unknown solver option %r" % k)
+            setattr(o, k, v)
+        st = _native.SolveStats()
+        self._call("uwg_stokes_solve", ctypes.byref(o), _ptr(u), _ptr(p), ctypes.byref(st))
+        return st.as_dict()
+
+    def residuals(self, u, p):
+        out = np.zeros(2)
+        self._call("uwg_stokes_residuals", _ptr(u), _ptr(p), ctypes.c_void_p(out.ctypes.data))
+        return out
+
+    def apply_K(self, x, level=0):
+        y = torch.empty_like(x)
+        self._call("uwg_apply_K64" if x.dtype == torch.float64 else "uwg_apply_K32", int(level), _ptr(x), _ptr(y))
+        return y
+
+    def apply_G(self, p):
+        y = self.zeros(self.n_vdof)
+        self._call("uwg_apply_G", _ptr(p), _ptr(y))
+        return y
+
+    def apply_Gt(self, u):
+        q = self.zeros(self.n_pdof)
+        self._call("uwg_apply_Gt", _ptr(u), _ptr(q))
+        return q
+
+    # -- advection -------------------------------------------------------------
+    def rk2(self, x, vel, dt):
+        fb, failed = ctypes.c_int64(0), ctypes.c_int64(0)
+        self._call("uwg_rk2_advect", x.shape[0], float(dt), _ptr(vel), _ptr(x), ctypes.byref(fb), ctypes.byref(failed))
+        return fb.value, failed.value
+
+    def interpolate(self, pts, vel):
+        out = torch.empty_like(pts)
+        self._call("uwg_interpolate", pts.shape[0], _ptr(pts), _ptr(vel), _ptr(out))
+        return out
+
+    def max_dt(self, vel):
+        dt = ctypes.c_double(0.0)
+        self._call("uwg_max_dt", _ptr(vel), ctypes.byref(dt))
+        return dt.value
+
+
+def rng_seed(seed):
+    """Park-Miller state after Swarm_Random_Seed (L/StgDomain/Swarm/src/Random.c:37-40)."""
+    return int(seed) ^ _MASK

@@ -1,0 +1,273 @@
+// Context management and the remaining extern "C" entry points of libuwg.
+//
+//   L/ = src/underworld/libUnderworld/
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "uwg_ops.cuh"
+
+int uwg_set_error(uwg_ctx* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+extern "C" const char* uwg_last_error(const uwg_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+static void* dmalloc(size_t bytes, bool* ok) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, bytes ? bytes : 8) != cudaSuccess) { *ok = false; return nullptr; }
+    return p;
+}
+
+extern "C" void uwg_ctx_destroy(uwg_ctx* c) {
+    if (!c) return;
+    cudaDeviceSynchronize();
+    for (int d = 0; d < 3; d++) if (c->ax[d]) cudaFree(c->ax[d]);
+    for (int l = 0; l < c->nlev; l++) {
+        uwg_level& L = c->lev[l];
+        if (l > 0) for (int d = 0; d < 3; d++) if (L.ax[d]) cudaFree(L.ax[d]);
+        cudaFree(L.W64); cudaFree(L.W32); cudaFree(L.bc); cudaFree(L.diag64); cudaFree(L.diag32);
+        if (L.cinv64) cudaFree(L.cinv64);
+        if (L.cinv32) cudaFree(L.cinv32);
+    }
+    cudaFree(c->f); cudaFree(c->h); cudaFree(c->Shat); cudaFree(c->Mp); cudaFree(c->bcval);
+    cudaFree(c->red);
+    if (c->red_host) cudaFreeHost(c->red_host);
+    uwg_solver_free(c);
+    delete c;
+}
+
+// Node coordinates per axis, CartesianGenerator_CalcGeom
+// (L/StgDomain/Mesh/src/CartesianGenerator.c:2003-2036, contact depth 0).
+static std::vector<double> axis_coords(int n_el_axis, int order, double mn, double mx) {
+    int n = n_el_axis * order + 1;
+    std::vector<double> v(n);
+    double steps = mx - mn;
+    for (int i = 0; i < n; i++) {
+        if (i <= 0) v[i] = mn;
+        else if (i >= n - 1) v[i] = mx;
+        else v[i] = mn + ((double)i / (double)(n - 1)) * steps;
+    }
+    return v;
+}
+
+extern "C" int uwg_ctx_create(const uwg_mesh_desc* d, uwg_ctx** out) {
+    if (!d || !out) return UWG_ERR_ARG;
+    *out = nullptr;
+    if (d->dim != 2 && d->dim != 3) return UWG_ERR_ARG;
+    if (d->order != 1 || d->porder != 0) return UWG_ERR_ARG;   // Q1/dQ0 operators
+    for (int i = 0; i < d->dim; i++)
+        if (d->res[i] < 1 || !(d->maxc[i] > d->minc[i])) return UWG_ERR_ARG;
+    int dev_count = 0;
+    if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count < 1) return UWG_ERR_CUDA;
+    uwg_ctx* c = new uwg_ctx();
+    memset(c->lev, 0, sizeof(c->lev));
+    c->dim = d->dim;
+    c->order = d->order;
+    c->porder = d->porder;
+    for (int i = 0; i < 3; i++) {
+        c->res[i] = i < d->dim ? d->res[i] : 1;
+        c->minc[i] = i < d->dim ? d->minc[i] : 0.0;
+        c->maxc[i] = i < d->dim ? d->maxc[i] : 1.0;
+        c->ax[i] = nullptr;
+    }
+    c->stream = 0;
+    c->n_el = (int64_t)c->res[0] * c->res[1] * c->res[2];
+    int64_t nn = 1;
+    for (int i = 0; i < c->dim; i++) nn *= (int64_t)c->res[i] * c->order + 1;
+    c->n_nodes = nn;
+    c->n_vdof = nn * c->dim;
+    c->nen = c->dim == 3 ? 8 : 4;
+    c->npn = 1;
+    c->n_pdof = c->n_el * c->npn;
+    c->nq = c->dim == 3 ? 27 : 9;
+    c->dvc_res = 15;
+    c->assembled = false;
+    c->red_host = nullptr;
+    bool ok = true;
+    // finest axes and minimum separation (Mesh_HexType_GetMinimumSeparationGeneral,
+    // L/StgDomain/Mesh/src/Mesh_HexType.c:275-332: the closest node pair of any
+    // element; on a regular mesh an adjacent pair along one axis)
+    double minsep = HUGE_VAL;
+    std::vector<double> hax[3];
+    for (int i = 0; i < c->dim; i++) {
+        hax[i] = axis_coords(c->res[i], c->order, c->minc[i], c->maxc[i]);
+        for (size_t k = 0; k + 1 < hax[i].size(); k++) {
+            double dd = hax[i][k] - hax[i][k + 1];
+            double m = std::sqrt(dd * dd);
+            if (m < minsep) minsep = m;
+        }
+        c->ax[i] = (double*)dmalloc(sizeof(double) * hax[i].size(), &ok);
+        if (ok) cudaMemcpy(c->ax[i], hax[i].data(), sizeof(double) * hax[i].size(), cudaMemcpyHostToDevice);
+    }
+    c->min_sep = minsep;
+    // multigrid levels: halve while every axis is even (reference rule, L/.../_bsscr.py:73-91)
+    int nlev = 1;
+    {
+        int r[3] = {c->res[0], c->res[1], c->res[2]};
+        while (nlev < UWG_MAXLEV) {
+            bool even = true;
+            for (int i = 0; i < c->dim; i++) even = even && (r[i] % 2 == 0);
+            if (!even) break;
+            for (int i = 0; i < c->dim; i++) r[i] /= 2;
+            nlev++;
+        }
+    }
+    c->nlev = nlev;
+    for (int l = 0; l < nlev && ok; l++) {
+        uwg_level& L = c->lev[l];
+        int64_t ne = 1, nnod = 1;
+        for (int i = 0; i < 3; i++) {
+            L.res[i] = i < c->dim ? (c->res[i] >> l) : 1;
+            ne *= L.res[i];
+            if (i < c->dim) nnod *= L.res[i] + 1;
+        }
+        L.n_el = ne;
+        L.n_nodes = nnod;
+        L.n_dof = nnod * c->dim;
+        for (int i = 0; i < 3; i++) {
+            if (i >= c->dim) { L.ax[i] = nullptr; continue; }
+            if (l == 0) { L.ax[i] = c->ax[i]; continue; }
+            std::vector<double> v(L.res[i] + 1);
+            for (int k = 0; k <= L.res[i]; k++) v[k] = hax[i][(size_t)k << l];
+            L.ax[i] = (double*)dmalloc(sizeof(double) * v.size(), &ok);
+            if (ok) cudaMemcpy(L.ax[i], v.data(), sizeof(double) * v.size(), cudaMemcpyHostToDevice);
+        }
+        L.W64 = (double*)dmalloc(sizeof(double) * c->nq * ne, &ok);
+        L.W32 = (float*)dmalloc(sizeof(float) * c->nq * ne, &ok);
+        L.bc = (uint8_t*)dmalloc(L.n_dof, &ok);
+        L.diag64 = (double*)dmalloc(sizeof(double) * L.n_dof, &ok);
+        L.diag32 = (float*)dmalloc(sizeof(float) * L.n_dof, &ok);
+        if (ok) cudaMemset(L.bc, 0, L.n_dof);
+        L.lmax64 = L.lmax32 = 1.0;
+        L.cinv64 = nullptr;
+        L.cinv32 = nullptr;
+        if (l == nlev - 1) {
+            if (L.n_dof > 4096) {
+                ok = false;
+            } else {
+                L.cinv64 = (double*)dmalloc(sizeof(double) * L.n_dof * L.n_dof, &ok);
+                L.cinv32 = (float*)dmalloc(sizeof(float) * L.n_dof * L.n_dof, &ok);
+            }
+        }
+    }
+    c->bc = c->lev[0].bc;
+    c->f = (double*)dmalloc(sizeof(double) * c->n_vdof, &ok);
+    c->bcval = (double*)dmalloc(sizeof(double) * c->n_vdof, &ok);
+    c->h = (double*)dmalloc(sizeof(double) * c->n_pdof, &ok);
+    c->Shat = (double*)dmalloc(sizeof(double) * c->n_pdof, &ok);
+    c->Mp = (double*)dmalloc(sizeof(double) * c->n_pdof, &ok);
+    c->red = dmalloc(4096 * sizeof(double), &ok);
+    if (ok && cudaMallocHost((void**)&c->red_host, 4096 * sizeof(double)) != cudaSuccess) ok = false;
+    if (ok) {
+        cudaMemset(c->bcval, 0, sizeof(double) * c->n_vdof);
+        cudaMemset(c->h, 0, sizeof(double) * c->n_pdof);
+        cudaMemset(c->Mp, 0, sizeof(double) * c->n_pdof);
+        cudaMemset(c->f, 0, sizeof(double) * c->n_vdof);
+    }
+    if (!ok || cudaDeviceSynchronize() != cudaSuccess) {
+        uwg_ctx_destroy(c);
+        return UWG_ERR_CUDA;
+    }
+    *out = c;
+    return UWG_OK;
+}
+
+extern "C" int uwg_set_stream(uwg_ctx* c, void* s) {
+    if (!c) return UWG_ERR_ARG;
+    c->stream = (cudaStream_t)s;
+    return UWG_OK;
+}
+
+extern "C" int uwg_sync(uwg_ctx* c) {
+    if (!c) return UWG_ERR_ARG;
+    UWG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return UWG_OK;
+}
+
+extern "C" int uwg_mesh_sizes(const uwg_ctx* c, int64_t* s) {
+    if (!c || !s) return UWG_ERR_ARG;
+    s[0] = c->n_el; s[1] = c->n_nodes; s[2] = c->n_vdof; s[3] = c->n_pdof; s[4] = c->nen; s[5] = c->npn;
+    s[6] = c->nlev;
+    return UWG_OK;
+}
+
+extern "C" int uwg_mesh_axis(const uwg_ctx* c, int axis, double* out) {
+    if (!c || !out || axis < 0 || axis >= c->dim) return UWG_ERR_ARG;
+    size_t n = (size_t)c->res[axis] * c->order + 1;
+    if (cudaMemcpy(out, c->ax[axis], sizeof(double) * n, cudaMemcpyDeviceToHost) != cudaSuccess) return UWG_ERR_CUDA;
+    return UWG_OK;
+}
+
+extern "C" int uwg_set_bcs(uwg_ctx* c, const uint8_t* mask, const double* values) {
+    if (!c || !mask) return uwg_set_error(c, UWG_ERR_ARG, "uwg_set_bcs: bad argument");
+    UWG_CUDA(c, cudaMemcpyAsync(c->lev[0].bc, mask, c->n_vdof, cudaMemcpyDeviceToDevice, c->stream));
+    if (values) {
+        UWG_CUDA(c, cudaMemcpyAsync(c->bcval, values, sizeof(double) * c->n_vdof, cudaMemcpyDeviceToDevice, c->stream));
+    } else {
+        UWG_CUDA(c, cudaMemsetAsync(c->bcval, 0, sizeof(double) * c->n_vdof, c->stream));
+    }
+    for (int l = 0; l + 1 < c->nlev; l++) {
+        int rc = uwg_ops_bc_coarsen(c, l);
+        if (rc) return rc;
+    }
+    c->assembled = false;
+    return UWG_OK;
+}
+
+__global__ void k_keep_bc(int64_t n, const uint8_t* bc, double* v) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n && !bc[i]) v[i] = 0.0;
+}
+
+extern "C" int uwg_assemble(uwg_ctx* c, int64_t np, const int32_t* off, const int32_t* list, const double* ip_xi,
+                            const double* ip_w, const double* eta_p, const double* body_p, const double* lambda_p) {
+    if (!c || !off || (np && (!list || !ip_xi || !ip_w || !eta_p)))
+        return uwg_set_error(c, UWG_ERR_ARG, "uwg_assemble: bad argument");
+    int rc = uwg_ops_assemble(c, off, list, ip_xi, ip_w, eta_p, body_p, lambda_p);
+    if (rc) return rc;
+    if (!lambda_p) UWG_CUDA(c, cudaMemsetAsync(c->Mp, 0, sizeof(double) * c->n_pdof, c->stream));
+    UWG_CUDA(c, cudaMemsetAsync(c->h, 0, sizeof(double) * c->n_pdof, c->stream));
+    // Dirichlet lifting: f -= K_fb g, h -= G_b^T g  (StiffnessMatrix.c:627-678)
+    k_keep_bc<<<(unsigned)((c->n_vdof + 255) / 256), 256, 0, c->stream>>>(c->n_vdof, c->bc, c->bcval);
+    UWG_CUDA(c, cudaGetLastError());
+    if ((rc = uwg_ops_applyK_lift(c, c->bcval, c->lev[0].diag64))) return rc;   // diag64 as scratch
+    vk_axpy<double>(c->stream, c->n_vdof, -1.0, c->lev[0].diag64, c->f);
+    vk_mask<double>(c->stream, c->n_vdof, c->bc, c->f);
+    if ((rc = uwg_ops_applyGt_mode(c, c->bcval, c->Shat, 1))) return rc;           // Shat as scratch
+    vk_axpy<double>(c->stream, c->n_pdof, -1.0, c->Shat, c->h);
+    if ((rc = uwg_solver_setup(c))) return rc;
+    UWG_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->assembled = true;
+    return UWG_OK;
+}
+
+extern "C" int uwg_element_matrices(uwg_ctx* c, int64_t el, double* Ke, double* fe, double* Ge, double* Se) {
+    if (!c || el < 0 || el >= c->n_el) return uwg_set_error(c, UWG_ERR_ARG, "uwg_element_matrices: bad element");
+    if (!c->assembled) return uwg_set_error(c, UWG_ERR_STATE, "element matrices before uwg_assemble");
+    return uwg_ops_element_matrices(c, el, Ke, fe, Ge, Se);
+}
+
+extern "C" int uwg_apply_K64(uwg_ctx* c, int level, const double* x, double* y) {
+    if (!c || !x || !y || level < 0 || level >= c->nlev) return uwg_set_error(c, UWG_ERR_ARG, "uwg_apply_K64: bad argument");
+    if (!c->assembled) return uwg_set_error(c, UWG_ERR_STATE, "apply before uwg_assemble");
+    return uwg_ops_applyK<double>(c, level, x, y);
+}
+
+extern "C" int uwg_apply_K32(uwg_ctx* c, int level, const float* x, float* y) {
+    if (!c || !x || !y || level < 0 || level >= c->nlev) return uwg_set_error(c, UWG_ERR_ARG, "uwg_apply_K32: bad argument");
+    if (!c->assembled) return uwg_set_error(c, UWG_ERR_STATE, "apply before uwg_assemble");
+    return uwg_ops_applyK<float>(c, level, x, y);
+}
+
+extern "C" int uwg_apply_G(uwg_ctx* c, const double* p, double* y) {
+    if (!c || !p || !y) return uwg_set_error(c, UWG_ERR_ARG, "uwg_apply_G: bad argument");
+    return uwg_ops_applyG(c, p, y);
+}
+
+extern "C" int uwg_apply_Gt(uwg_ctx* c, const double* u, double* q) {
+    if (!c || !u || !q) return uwg_set_error(c, UWG_ERR_ARG, "uwg_apply_Gt: bad argument");
+    return uwg_ops_applyGt(c, u, q);
+}

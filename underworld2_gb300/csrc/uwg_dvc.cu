@@ -1,0 +1,271 @@
+// Discrete Voronoi cell (DVC) integration weights, one warp per element.
+//
+// The reference grows every particle's region on a res^dim grid over the
+// element, particle by particle and round by round
+// (L/PICellerator/Weights/src/DVCWeights.c:676-770): a particle first claims
+// cells of its boundary list (free cells, or cells whose owner is strictly
+// farther away, :256-365), then rebuilds its boundary list from the cells it
+// just claimed (neighbours in the order S, N, E, W, U, D that it does not own,
+// each once, :388-486).  Within one particle's step the claims touch distinct
+// cells and are independent, and the boundary rebuild is an ordered,
+// de-duplicated expansion, so the warp performs each step in parallel with
+// ballots and prefix counts while keeping the reference's sequential order:
+// results are identical to the sequential algorithm.
+//
+// Per warp: owner/done bytes and particle coordinates in shared memory,
+// boundary lists (double-buffered per round) in a per-warp global scratch.
+// Built with -fmad=false (the distance test must round like the reference).
+#include <algorithm>
+
+#include "uwg_internal.cuh"
+
+#define DVC_NMAX 128     // particles per element handled by the kernel
+#define DVC_WARPS 4      // warps per block
+
+struct dvc_args {
+    int64_t n_el;
+    int R;               // grid cells per axis
+    const int32_t* off;
+    double* ip_xi;       // in: local coords, out: centroids (slot order)
+    double* ip_w;
+    int16_t* scratch;    // per warp: claimed[RC] + pool0[PCAP] + pool1[PCAP]
+    int64_t pcap;
+    int32_t* status;     // [0] = first error code, [1] = element
+};
+
+__device__ __forceinline__ void dvc_fail(int32_t* status, int code, int64_t el) {
+    if (atomicCAS(&status[0], 0, code) == 0) status[1] = (int32_t)el;
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(32 * DVC_WARPS) k_dvc(dvc_args a) {
+    extern __shared__ unsigned char smem[];
+    const int R = a.R;
+    const int RC = DIM == 3 ? R * R * R : R * R;
+    const int NNB = 2 * DIM;
+    int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    // per-block cell centre table (accumulated exactly as _DVCWeights_ConstructGrid)
+    double* cen = (double*)smem;                       // [16]
+    size_t per_warp = (size_t)RC * 2 + (size_t)DVC_NMAX * 3 * 8 + (size_t)DVC_NMAX * 4 * 4;
+    per_warp = (per_warp + 15) & ~(size_t)15;
+    unsigned char* wbase = smem + 128 + per_warp * wib;
+    double* xs = (double*)wbase;                       // [NMAX][3]
+    int32_t* hdr = (int32_t*)(xs + DVC_NMAX * 3);      // [2][NMAX][2] (offset, length) per pool
+    uint8_t* owner = (uint8_t*)(hdr + DVC_NMAX * 4);   // [RC]
+    uint8_t* done = owner + RC;                        // [RC]
+    if (threadIdx.x == 0) {
+        double dx = (1.0 - -1.0) / R;
+        double X = -1.0 - dx / 2.0;
+        for (int i = 0; i < R; i++) { X = X + dx; cen[i] = X; }
+    }
+    __syncthreads();
+    const double dx = (1.0 - -1.0) / R;
+    const double da = DIM == 3 ? dx * dx * dx : dx * dx;
+
+    int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    int16_t* claimed = a.scratch + gw * (RC + 2 * a.pcap);
+    int16_t* pool[2] = {claimed + RC, claimed + RC + a.pcap};
+    unsigned lt = (1u << lane) - 1u;
+
+    for (int64_t el = gw; el < a.n_el; el += nw) {
+        int32_t o0 = a.off[el];
+        int n = a.off[el + 1] - o0;
+        if (n == 0) { if (lane == 0) dvc_fail(a.status, UWG_ERR_EMPTY_CELL, el); continue; }
+        if (n > DVC_NMAX) { if (lane == 0) dvc_fail(a.status, UWG_ERR_CELL_FULL, el); continue; }
+        for (int k = lane; k < n; k += 32) {
+            xs[k * 3 + 0] = a.ip_xi[(int64_t)(o0 + k) * DIM + 0];
+            xs[k * 3 + 1] = a.ip_xi[(int64_t)(o0 + k) * DIM + 1];
+            xs[k * 3 + 2] = DIM == 3 ? a.ip_xi[(int64_t)(o0 + k) * DIM + DIM - 1] : 0.0;
+        }
+        for (int c = lane; c < RC; c += 32) { owner[c] = 0xFF; done[c] = 0; }
+        __syncwarp();
+
+        int cur = 0;
+        int64_t bump = 0;
+        bool overflow = false;
+
+        // Boundary rebuild for particle i from claimed[0..ncl) into pool[dst].
+        auto update = [&](int i, int ncl, int dst) {
+            int64_t start = bump;
+            int total = ncl * NNB, cnt = 0;
+            for (int base = 0; base < total; base += 32) {
+                int t = base + lane;
+                int c1 = -1;
+                bool ok = false;
+                if (t < total) {
+                    int c0 = claimed[t / NNB], k = t % NNB;
+                    int ci = c0 % R, cj = (c0 / R) % R, ck = DIM == 3 ? c0 / (R * R) : 0;
+                    switch (k) {   // S, N, E, W, U, D
+                        case 0: c1 = cj > 0 ? c0 - R : -1; break;
+                        case 1: c1 = cj < R - 1 ? c0 + R : -1; break;
+                        case 2: c1 = ci < R - 1 ? c0 + 1 : -1; break;
+                        case 3: c1 = ci > 0 ? c0 - 1 : -1; break;
+                        case 4: c1 = ck < R - 1 ? c0 + R * R : -1; break;
+                        default: c1 = ck > 0 ? c0 - R * R : -1; break;
+                    }
+                    ok = c1 >= 0 && owner[c1] != i && done[c1] == 0;
+                }
+                unsigned m = __match_any_sync(0xffffffffu, ok ? c1 : -2 - lane);
+                bool keep = ok && (__ffs(m) - 1 == lane);
+                unsigned kb = __ballot_sync(0xffffffffu, keep);
+                if (keep) {
+                    done[c1] = 1;
+                    int64_t pos = start + cnt + __popc(kb & lt);
+                    if (pos < a.pcap) pool[dst][pos] = (int16_t)c1;
+                }
+                cnt += __popc(kb);
+                __syncwarp();
+            }
+            if (start + cnt > a.pcap) overflow = true;
+            for (int k = lane; k < cnt && start + k < a.pcap; k += 32) done[pool[dst][start + k]] = 0;
+            if (lane == 0) {
+                hdr[(dst * DVC_NMAX + i) * 2 + 0] = (int32_t)start;
+                hdr[(dst * DVC_NMAX + i) * 2 + 1] = cnt;
+            }
+            bump = start + cnt;
+            __syncwarp();
+        };
+
+        // seeding (:687-705 / :735-756)
+        for (int i = 0; i < n; i++) {
+            int k = (int)((xs[i * 3 + 0] - -1.0) / dx);
+            int j = (int)((xs[i * 3 + 1] - -1.0) / dx);
+            int l = DIM == 3 ? (int)((xs[i * 3 + 2] - -1.0) / dx) : 0;
+            if (k == R) k--;
+            if (j == R) j--;
+            if (DIM == 3 && l == R) l--;
+            int c = k + j * R + l * R * R;
+            if (lane == 0) { owner[c] = (uint8_t)i; claimed[0] = (int16_t)c; }
+            __syncwarp();
+            update(i, 1, 0);
+        }
+
+        // growth rounds (:707-720 / :758-769)
+        int rounds = 0;
+        while (true) {
+            int nxt = cur ^ 1;
+            bump = 0;
+            int claimed_total = 0;
+            for (int i = 0; i < n; i++) {
+                int bo = hdr[(cur * DVC_NMAX + i) * 2 + 0], bl = hdr[(cur * DVC_NMAX + i) * 2 + 1];
+                int ncl = 0;
+                const double px = xs[i * 3 + 0], py = xs[i * 3 + 1], pz = xs[i * 3 + 2];
+                for (int base = 0; base < bl; base += 32) {
+                    int t = base + lane;
+                    bool take = false;
+                    int c0 = 0;
+                    if (t < bl) {
+                        c0 = pool[cur][bo + t];
+                        int o = owner[c0];
+                        if (o == 0xFF) take = true;
+                        else if (o != i) {
+                            double x0 = cen[c0 % R], y0 = cen[(c0 / R) % R];
+                            double x1 = xs[o * 3 + 0], y1 = xs[o * 3 + 1];
+                            double dist;
+                            if (DIM == 2) {
+                                dist = (x1 + px - x0 - x0) * (x1 - px) + (y1 + py - y0 - y0) * (y1 - py);
+                            } else {
+                                double z0 = cen[c0 / (R * R)], z1 = xs[o * 3 + 2];
+                                dist = (x1 + px - x0 - x0) * (x1 - px) + (y1 + py - y0 - y0) * (y1 - py) +
+                                       (z1 + pz - z0 - z0) * (z1 - pz);
+                            }
+                            take = dist > 0.0;
+                        }
+                    }
+                    unsigned tb = __ballot_sync(0xffffffffu, take);
+                    __syncwarp();
+                    if (take) {
+                        claimed[ncl + __popc(tb & lt)] = (int16_t)c0;
+                        owner[c0] = (uint8_t)i;
+                    }
+                    ncl += __popc(tb);
+                    __syncwarp();
+                }
+                claimed_total += ncl;
+                update(i, ncl, nxt);
+            }
+            cur = nxt;
+            rounds++;
+            if (rounds > 4 * RC) overflow = true;   // never reached: each claim strictly improves ownership
+            if (claimed_total == 0 || overflow) break;
+        }
+        if (overflow) {
+            if (lane == 0) dvc_fail(a.status, UWG_ERR_CELL_FULL, el);
+            continue;
+        }
+
+        // centroids and weights (:198-254), summed in cell order per particle
+        for (int g0 = 0; g0 < n; g0 += 32) {
+            int i = g0 + lane;
+            double sx = 0.0, sy = 0.0, sz = 0.0;
+            int cnt = 0;
+            for (int c = 0; c < RC; c++) {
+                if (owner[c] == i) {
+                    sx += cen[c % R];
+                    sy += cen[(c / R) % R];
+                    if (DIM == 3) sz += cen[c / (R * R)];
+                    cnt++;
+                }
+            }
+            if (i < n) {
+                int64_t s = o0 + i;
+                a.ip_w[s] = cnt * da;
+                if (cnt != 0) { sx /= cnt; sy /= cnt; sz /= cnt; }
+                a.ip_xi[s * DIM + 0] = sx;
+                a.ip_xi[s * DIM + 1] = sy;
+                if (DIM == 3) a.ip_xi[s * DIM + DIM - 1] = sz;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+extern "C" int uwg_dvc_weights(uwg_ctx* c, int res, const int32_t* cell_offsets, double* ip_xi,
+                               double* ip_w) {
+    if (!c || !cell_offsets || !ip_xi || !ip_w || res < 1 || res > 16)
+        return uwg_set_error(c, UWG_ERR_ARG, "uwg_dvc_weights: bad argument (res must be 1..16)");
+    int dim = c->dim;
+    int RC = dim == 3 ? res * res * res : res * res;
+    size_t per_warp = (size_t)RC * 2 + (size_t)DVC_NMAX * 3 * 8 + (size_t)DVC_NMAX * 4 * 4;
+    per_warp = (per_warp + 15) & ~(size_t)15;
+    size_t shm = 128 + per_warp * DVC_WARPS;
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    void (*kern)(dvc_args) = dim == 3 ? k_dvc<3> : k_dvc<2>;
+    UWG_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+    int per_sm = 0;
+    UWG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * DVC_WARPS, shm));
+    if (per_sm < 1) per_sm = 1;
+    int64_t blocks = std::min<int64_t>((int64_t)nsm * per_sm, (c->n_el + DVC_WARPS - 1) / DVC_WARPS);
+    if (blocks < 1) blocks = 1;
+    int64_t warps = blocks * DVC_WARPS;
+    dvc_args a;
+    a.n_el = c->n_el;
+    a.R = res;
+    a.off = cell_offsets;
+    a.ip_xi = ip_xi;
+    a.ip_w = ip_w;
+    a.pcap = (int64_t)RC * 8;
+    void* scratch = nullptr;
+    size_t sbytes = (size_t)warps * (RC + 2 * a.pcap) * 2 + 64;
+    UWG_CUDA(c, cudaMallocAsync(&scratch, sbytes, c->stream));
+    a.scratch = (int16_t*)scratch;
+    a.status = (int32_t*)c->red;
+    UWG_CUDA(c, cudaMemsetAsync(a.status, 0, 8, c->stream));
+    kern<<<(unsigned)blocks, 32 * DVC_WARPS, shm, c->stream>>>(a);
+    cudaError_t e = cudaGetLastError();
+    int32_t st[2] = {0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(st, a.status, 8, cudaMemcpyDeviceToHost, c->stream);
+    cudaFreeAsync(scratch, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return uwg_set_error(c, UWG_ERR_CUDA, cudaGetErrorString(e));
+    if (st[0] == UWG_ERR_EMPTY_CELL)
+        return uwg_set_error(c, UWG_ERR_EMPTY_CELL, "element " + std::to_string(st[1]) +
+                             " holds no particle: add more particles per cell");
+    if (st[0] == UWG_ERR_CELL_FULL)
+        return uwg_set_error(c, UWG_ERR_CELL_FULL, "element " + std::to_string(st[1]) +
+                             " exceeds the DVC kernel limits (128 particles per element)");
+    return UWG_OK;
+}

@@ -1,0 +1,1004 @@
+// Stokes operators on regular Q1/dQ0 meshes.
+//
+// Viscous operator.  On an affine (axis-aligned) element the PIC integrand of
+// K_e = sum_q eta_q w_q detJ B^T D B (L/Underworld/Rheology/src/
+// ConstitutiveMatrixCartesian.cpp:238-429) is, for every particle, a polynomial
+// of degree <= 2 per axis in the local coordinate.  Lagrange interpolation on the
+// 3-point tensor rule s in {-1, 0, 1} reproduces such polynomials exactly, so
+//     W_j = sum_q eta_q w_q detJ_q l_j(xi_q)          (3^dim weights per element)
+// gives K_e = sum_j W_j B(s_j)^T D B(s_j) identically (up to rounding): an exact,
+// compact coefficient set that the matrix-free apply reads instead of K_e.
+// The same identity coarsens W to the parent element of a twice-coarser mesh,
+// which makes rediscretised coarse operators equal to Galerkin P^T K P.
+//
+// Gradient operator.  G_e[A,i] = -int_e dN_A/dx_i (dQ0 pressure, evaluated
+// exactly; L/StgFEM/Assembly/src/GradientStiffnessMatrixTerm.c:129-219 uses
+// Gauss quadrature, which is exact for this integrand).
+//
+// Schur preconditioner.  S_e = G_e^T diag(K_e)^-1 G_e - M_e
+// (L/StgFEM/SLE/ProvidedSystems/StokesFlow/src/UzawaPreconditionerTerm.c:124-207):
+// 1x1 per element for dQ0, so the assembled preconditioner is diagonal.
+//
+//   L/ = src/underworld/libUnderworld/
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "uwg_ops.cuh"
+
+static inline unsigned nblk(int64_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
+
+uwg_lgeom uwg_level_geom(const uwg_ctx* c, int l) {
+    uwg_lgeom g;
+    const uwg_level& L = c->lev[l];
+    g.dim = c->dim;
+    for (int d = 0; d < 3; d++) {
+        g.res[d] = L.res[d];
+        g.nx[d] = d < c->dim ? L.res[d] + 1 : 1;
+        g.ax[d] = L.ax[d];
+    }
+    g.n_el = L.n_el;
+    g.n_nodes = L.n_nodes;
+    return g;
+}
+
+__device__ __forceinline__ void q1_elem(const uwg_lgeom& g, int64_t e, int64_t* nodes, double* h) {
+    int ex = (int)(e % g.res[0]);
+    int ey = (int)((e / g.res[0]) % g.res[1]);
+    int ez = g.dim == 3 ? (int)(e / ((int64_t)g.res[0] * g.res[1])) : 0;
+    h[0] = g.ax[0][ex + 1] - g.ax[0][ex];
+    h[1] = g.ax[1][ey + 1] - g.ax[1][ey];
+    h[2] = g.dim == 3 ? g.ax[2][ez + 1] - g.ax[2][ez] : 1.0;
+    int64_t nx = g.nx[0], ny = g.nx[1];
+    int nn = g.dim == 3 ? 8 : 4;
+    for (int n = 0; n < nn; n++) {
+        int i = n & 1, j = (n >> 1) & 1, k = (n >> 2) & 1;
+        nodes[n] = (ex + i) + nx * ((ey + j) + ny * (int64_t)(ez + k));
+    }
+}
+
+// 1D quadratic Lagrange basis on {-1, 0, 1}
+__device__ __forceinline__ void lag3(double s, double* l) {
+    l[0] = 0.5 * s * (s - 1.0);
+    l[1] = 1.0 - s * s;
+    l[2] = 0.5 * s * (s + 1.0);
+}
+
+// Q1 basis value N_n(xi) (product form; assembly parity is to a tolerance)
+template <int DIM>
+__device__ __forceinline__ void q1_basis(const double* xi, double* N) {
+    for (int n = 0; n < (DIM == 3 ? 8 : 4); n++) {
+        double v = 1.0;
+        for (int d = 0; d < DIM; d++) {
+            double sg = ((n >> d) & 1) ? 1.0 : -1.0;
+            v *= 0.5 * (1.0 + sg * xi[d]);
+        }
+        N[n] = v;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Assembly from the PIC integration points: one thread per element.
+//   W[j*n_el + e] = sum_q eta w detJ l_j(xi_q)
+//   f[node*dim + i] += sum_q w detJ body_i N_A(xi_q)        (atomic scatter)
+//   Mp[e] = sum_q w detJ (-1/lambda_q)                         (optional)
+// ---------------------------------------------------------------------------
+template <int DIM>
+__global__ void k_assemble_q1(uwg_lgeom g, const int32_t* off, const int32_t* list, const double* ip_xi,
+                              const double* ip_w, const double* eta_p, const double* body_p,
+                              const double* lambda_p, double* W, double* f, double* Mp) {
+    constexpr int NQ = DIM == 3 ? 27 : 9;
+    constexpr int NEN = DIM == 3 ? 8 : 4;
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= g.n_el) return;
+    int64_t nodes[8];
+    double h[3];
+    q1_elem(g, e, nodes, h);
+    double detJ = DIM == 3 ? (h[0] * 0.5) * (h[1] * 0.5) * (h[2] * 0.5) : (h[0] * 0.5) * (h[1] * 0.5);
+    double Wl[NQ];
+    double fe[NEN * DIM];
+    double mp = 0.0;
+    for (int j = 0; j < NQ; j++) Wl[j] = 0.0;
+    for (int j = 0; j < NEN * DIM; j++) fe[j] = 0.0;
+    int32_t s0 = off[e], s1 = off[e + 1];
+    for (int32_t s = s0; s < s1; s++) {
+        int32_t p = list[s];
+        double xi[3];
+        for (int d = 0; d < DIM; d++) xi[d] = ip_xi[(int64_t)s * DIM + d];
+        double wd = ip_w[s] * detJ;
+        double c = eta_p[p] * wd;
+        double lx[3], ly[3], lz[3] = {1.0, 0.0, 0.0};
+        lag3(xi[0], lx);
+        lag3(xi[1], ly);
+        if (DIM == 3) lag3(xi[DIM - 1], lz);
+#pragma unroll
+        for (int kz = 0; kz < (DIM == 3 ? 3 : 1); kz++)
+#pragma unroll
+            for (int ky = 0; ky < 3; ky++)
+#pragma unroll
+                for (int kx = 0; kx < 3; kx++) Wl[kx + 3 * ky + 9 * kz] += c * lx[kx] * ly[ky] * lz[kz];
+        if (body_p) {
+            double N[NEN];
+            q1_basis<DIM>(xi, N);
+#pragma unroll
+            for (int a = 0; a < NEN; a++)
+#pragma unroll
+                for (int i = 0; i < DIM; i++) fe[a * DIM + i] += wd * body_p[(int64_t)p * DIM + i] * N[a];
+        }
+        if (lambda_p) mp += wd * -lambda_p[p];
+    }
+    for (int j = 0; j < NQ; j++) W[(int64_t)j * g.n_el + e] = Wl[j];
+    if (body_p)
+        for (int a = 0; a < NEN; a++)
+            for (int i = 0; i < DIM; i++) atomicAdd(&f[nodes[a] * DIM + i], fe[a * DIM + i]);
+    if (Mp) Mp[e] = mp;
+}
+
+// ---------------------------------------------------------------------------
+// Local derivative dN_n/dxi_d at the 3-point rule position (pa,pb,pc), Q1.
+// ---------------------------------------------------------------------------
+template <int DIM>
+__device__ __forceinline__ double q1_lderiv(int n, int d, const int* pt) {
+    // (1 + sg s)/2 at s = -1, 0, 1 : sg=-1 -> 1, .5, 0 ; sg=+1 -> 0, .5, 1
+    double v = 1.0;
+    for (int e = 0; e < DIM; e++) {
+        int sgp = (n >> e) & 1;
+        if (e == d) v *= sgp ? 0.5 : -0.5;
+        else v *= (pt[e] == 1) ? 0.5 : ((pt[e] == 2) == (sgp == 1) ? 1.0 : 0.0);
+    }
+    return v;
+}
+
+// Element diagonal of K_e from W (and, on the finest level, the Schur block).
+template <int DIM>
+__global__ void k_diag_q1(uwg_lgeom g, const double* W, const uint8_t* bc, double* diag, double* shat,
+                          const double* Mp) {
+    constexpr int NQ = DIM == 3 ? 27 : 9;
+    constexpr int NEN = DIM == 3 ? 8 : 4;
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= g.n_el) return;
+    int64_t nodes[8];
+    double h[3];
+    q1_elem(g, e, nodes, h);
+    double hi[3] = {2.0 / h[0], 2.0 / h[1], 2.0 / h[2]};
+    double kd[NEN * DIM];
+    for (int v = 0; v < NEN * DIM; v++) kd[v] = 0.0;
+    for (int j = 0; j < NQ; j++) {
+        int pt[3] = {j % 3, (j / 3) % 3, DIM == 3 ? j / 9 : 1};
+        double w = W[(int64_t)j * g.n_el + e];
+        for (int n = 0; n < NEN; n++) {
+            double gx[3];
+            for (int d = 0; d < DIM; d++) gx[d] = hi[d] * q1_lderiv<DIM>(n, d, pt);
+            double s2 = 0.0;
+            for (int d = 0; d < DIM; d++) s2 += gx[d] * gx[d];
+            for (int c = 0; c < DIM; c++) kd[n * DIM + c] += w * (s2 + gx[c] * gx[c]);
+        }
+    }
+    for (int n = 0; n < NEN; n++)
+        for (int c = 0; c < DIM; c++) {
+            int64_t dof = nodes[n] * DIM + c;
+            if (!bc[dof]) atomicAdd(&diag[dof], kd[n * DIM + c]);
+        }
+    if (shat) {
+        // G_e[A,i] = -sg_i(A) * prod_{d != i} h_d / 2^(dim-1)
+        double s = 0.0;
+        for (int n = 0; n < NEN; n++)
+            for (int i = 0; i < DIM; i++) {
+                double ge = 1.0;
+                for (int d = 0; d < DIM; d++)
+                    if (d != i) ge *= 0.5 * h[d];
+                ge *= ((n >> i) & 1) ? -1.0 : 1.0;
+                s += ge * (ge / kd[n * DIM + i]);
+            }
+        if (Mp) s -= Mp[e];
+        shat[e] = s;
+    }
+}
+
+__global__ void k_diag_bc(int64_t n, const uint8_t* bc, double* diag, float* diag32, double* inv) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double d = bc[i] ? 1.0 : diag[i];
+    diag[i] = d;
+    diag32[i] = (float)d;
+}
+
+// ---------------------------------------------------------------------------
+// Matrix-free K apply, sum-factorised on the 3-point rule.
+// y = P K P x + (I - P) x with P zeroing Dirichlet dofs.
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ void up3(T a, T b, T* o) { o[0] = a; o[1] = (T)0.5 * (a + b); o[2] = b; }
+
+template <typename T>
+__global__ void k_bc_copy(int64_t n, const uint8_t* bc, const T* x, T* y) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) y[i] = bc[i] ? x[i] : (T)0;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_applyK_q1_3d(uwg_lgeom g, const T* __restrict__ W,
+                                                      const uint8_t* __restrict__ bc, bool mask_in,
+                                                      const T* __restrict__ x, T* y) {
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= g.n_el) return;
+    int64_t nodes[8];
+    double hd[3];
+    q1_elem(g, e, nodes, hd);
+    const T hx = (T)(2.0 / hd[0]), hy = (T)(2.0 / hd[1]), hz = (T)(2.0 / hd[2]);
+    T u[8][3];
+    bool fix[8][3];
+#pragma unroll
+    for (int n = 0; n < 8; n++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            int64_t dof = nodes[n] * 3 + c;
+            fix[n][c] = bc[dof] != 0;
+            u[n][c] = (fix[n][c] && mask_in) ? (T)0 : x[dof];
+        }
+    // physical gradients on the 3x3 face grids
+    T Gx[3][3][3], Gy[3][3][3], Gz[3][3][3];   // [c][p][q]
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        T a0[3], a1[3];
+        // d/dx : depends on (y,z) point
+        {
+            T d00 = (T)0.5 * hx * (u[1][c] - u[0][c]), d10 = (T)0.5 * hx * (u[3][c] - u[2][c]);
+            T d01 = (T)0.5 * hx * (u[5][c] - u[4][c]), d11 = (T)0.5 * hx * (u[7][c] - u[6][c]);
+            up3(d00, d10, a0);
+            up3(d01, d11, a1);
+#pragma unroll
+            for (int p = 0; p < 3; p++) up3(a0[p], a1[p], Gx[c][p]);   // Gx[c][py][pz]
+        }
+        {
+            T d00 = (T)0.5 * hy * (u[2][c] - u[0][c]), d10 = (T)0.5 * hy * (u[3][c] - u[1][c]);
+            T d01 = (T)0.5 * hy * (u[6][c] - u[4][c]), d11 = (T)0.5 * hy * (u[7][c] - u[5][c]);
+            up3(d00, d10, a0);
+            up3(d01, d11, a1);
+#pragma unroll
+            for (int p = 0; p < 3; p++) up3(a0[p], a1[p], Gy[c][p]);   // Gy[c][px][pz]
+        }
+        {
+            T d00 = (T)0.5 * hz * (u[4][c] - u[0][c]), d10 = (T)0.5 * hz * (u[5][c] - u[1][c]);
+            T d01 = (T)0.5 * hz * (u[6][c] - u[2][c]), d11 = (T)0.5 * hz * (u[7][c] - u[3][c]);
+            up3(d00, d10, a0);
+            up3(d01, d11, a1);
+#pragma unroll
+            for (int p = 0; p < 3; p++) up3(a0[p], a1[p], Gz[c][p]);   // Gz[c][px][py]
+        }
+    }
+    // stresses summed along the derivative axis
+    T Rx[3][3][3], Ry[3][3][3], Rz[3][3][3];
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+#pragma unroll
+        for (int p = 0; p < 3; p++)
+#pragma unroll
+            for (int q = 0; q < 3; q++) { Rx[c][p][q] = 0; Ry[c][p][q] = 0; Rz[c][p][q] = 0; }
+#pragma unroll
+    for (int pz = 0; pz < 3; pz++)
+#pragma unroll
+        for (int py = 0; py < 3; py++)
+#pragma unroll
+            for (int px = 0; px < 3; px++) {
+                T w = W[(int64_t)(px + 3 * py + 9 * pz) * g.n_el + e];
+                T uxx = Gx[0][py][pz], uxy = Gy[0][px][pz], uxz = Gz[0][px][py];
+                T uyx = Gx[1][py][pz], uyy = Gy[1][px][pz], uyz = Gz[1][px][py];
+                T uzx = Gx[2][py][pz], uzy = Gy[2][px][pz], uzz = Gz[2][px][py];
+                T sxx = w * (uxx + uxx), syy = w * (uyy + uyy), szz = w * (uzz + uzz);
+                T sxy = w * (uxy + uyx), sxz = w * (uxz + uzx), syz = w * (uyz + uzy);
+                Rx[0][py][pz] += sxx; Ry[0][px][pz] += sxy; Rz[0][px][py] += sxz;
+                Rx[1][py][pz] += sxy; Ry[1][px][pz] += syy; Rz[1][px][py] += syz;
+                Rx[2][py][pz] += sxz; Ry[2][px][pz] += syz; Rz[2][px][py] += szz;
+            }
+    // transpose of the face interpolation and the derivative
+    T out[8][3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        // down-sample 3x3 -> 2x2: v[j][k] = sum L(j,p) L(k,q) R[p][q]
+        T v[2][2];
+#define DOWN(R_)                                                                          \
+    {                                                                                     \
+        T t0[3], t1[3];                                                                   \
+        for (int q = 0; q < 3; q++) {                                                     \
+            t0[q] = R_[c][0][q] + (T)0.5 * R_[c][1][q];                                   \
+            t1[q] = R_[c][2][q] + (T)0.5 * R_[c][1][q];                                   \
+        }                                                                                 \
+        v[0][0] = t0[0] + (T)0.5 * t0[1]; v[0][1] = t0[2] + (T)0.5 * t0[1];               \
+        v[1][0] = t1[0] + (T)0.5 * t1[1]; v[1][1] = t1[2] + (T)0.5 * t1[1];               \
+    }
+        DOWN(Rx);   // v[jy][kz]
+        {
+            T s = (T)0.5 * hx;
+            out[0][c] = -s * v[0][0]; out[1][c] = s * v[0][0];
+            out[2][c] = -s * v[1][0]; out[3][c] = s * v[1][0];
+            out[4][c] = -s * v[0][1]; out[5][c] = s * v[0][1];
+            out[6][c] = -s * v[1][1]; out[7][c] = s * v[1][1];
+        }
+        DOWN(Ry);   // v[ix][kz]
+        {
+            T s = (T)0.5 * hy;
+            out[0][c] -= s * v[0][0]; out[2][c] += s * v[0][0];
+            out[1][c] -= s * v[1][0]; out[3][c] += s * v[1][0];
+            out[4][c] -= s * v[0][1]; out[6][c] += s * v[0][1];
+            out[5][c] -= s * v[1][1]; out[7][c] += s * v[1][1];
+        }
+        DOWN(Rz);   // v[ix][jy]
+        {
+            T s = (T)0.5 * hz;
+            out[0][c] -= s * v[0][0]; out[4][c] += s * v[0][0];
+            out[1][c] -= s * v[1][0]; out[5][c] += s * v[1][0];
+            out[2][c] -= s * v[0][1]; out[6][c] += s * v[0][1];
+            out[3][c] -= s * v[1][1]; out[7][c] += s * v[1][1];
+        }
+#undef DOWN
+    }
+#pragma unroll
+    for (int n = 0; n < 8; n++)
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+            if (!fix[n][c]) atomicAdd(&y[nodes[n] * 3 + c], out[n][c]);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_applyK_q1_2d(uwg_lgeom g, const T* __restrict__ W,
+                                                      const uint8_t* __restrict__ bc, bool mask_in,
+                                                      const T* __restrict__ x, T* y) {
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= g.n_el) return;
+    int64_t nodes[8];
+    double hd[3];
+    q1_elem(g, e, nodes, hd);
+    const T hx = (T)(2.0 / hd[0]), hy = (T)(2.0 / hd[1]);
+    T u[4][2];
+    bool fix[4][2];
+#pragma unroll
+    for (int n = 0; n < 4; n++)
+#pragma unroll
+        for (int c = 0; c < 2; c++) {
+            int64_t dof = nodes[n] * 2 + c;
+            fix[n][c] = bc[dof] != 0;
+            u[n][c] = (fix[n][c] && mask_in) ? (T)0 : x[dof];
+        }
+    T Gx[2][3], Gy[2][3];
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+        up3((T)0.5 * hx * (u[1][c] - u[0][c]), (T)0.5 * hx * (u[3][c] - u[2][c]), Gx[c]);   // over py
+        up3((T)0.5 * hy * (u[2][c] - u[0][c]), (T)0.5 * hy * (u[3][c] - u[1][c]), Gy[c]);   // over px
+    }
+    T Rx[2][3] = {{0, 0, 0}, {0, 0, 0}}, Ry[2][3] = {{0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+    for (int py = 0; py < 3; py++)
+#pragma unroll
+        for (int px = 0; px < 3; px++) {
+            T w = W[(int64_t)(px + 3 * py) * g.n_el + e];
+            T uxx = Gx[0][py], uxy = Gy[0][px], uyx = Gx[1][py], uyy = Gy[1][px];
+            T sxx = w * (uxx + uxx), syy = w * (uyy + uyy), sxy = w * (uxy + uyx);
+            Rx[0][py] += sxx; Ry[0][px] += sxy;
+            Rx[1][py] += sxy; Ry[1][px] += syy;
+        }
+    T out[4][2];
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+        T v0 = Rx[c][0] + (T)0.5 * Rx[c][1], v1 = Rx[c][2] + (T)0.5 * Rx[c][1];   // over jy
+        T s = (T)0.5 * hx;
+        out[0][c] = -s * v0; out[1][c] = s * v0; out[2][c] = -s * v1; out[3][c] = s * v1;
+        v0 = Ry[c][0] + (T)0.5 * Ry[c][1]; v1 = Ry[c][2] + (T)0.5 * Ry[c][1];       // over ix
+        s = (T)0.5 * hy;
+        out[0][c] -= s * v0; out[2][c] += s * v0; out[1][c] -= s * v1; out[3][c] += s * v1;
+    }
+#pragma unroll
+    for (int n = 0; n < 4; n++)
+#pragma unroll
+        for (int c = 0; c < 2; c++)
+            if (!fix[n][c]) atomicAdd(&y[nodes[n] * 2 + c], out[n][c]);
+}
+
+template <typename T>
+int uwg_ops_applyK(uwg_ctx* c, int l, const T* x, T* y) {
+    const uwg_level& L = c->lev[l];
+    uwg_lgeom g = uwg_level_geom(c, l);
+    const T* W;
+    if constexpr (sizeof(T) == 8) W = (const T*)L.W64; else W = (const T*)L.W32;
+    k_bc_copy<T><<<nblk(L.n_dof), 256, 0, c->stream>>>(L.n_dof, L.bc, x, y);
+    if (c->dim == 3) k_applyK_q1_3d<T><<<nblk(L.n_el, 128), 128, 0, c->stream>>>(g, W, L.bc, true, x, y);
+    else k_applyK_q1_2d<T><<<nblk(L.n_el, 128), 128, 0, c->stream>>>(g, W, L.bc, true, x, y);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
+// y = P K x (Dirichlet dofs of x kept, rows of Dirichlet dofs zero): the
+// lifting term K_fb g of the right-hand side.
+int uwg_ops_applyK_lift(uwg_ctx* c, const double* x, double* y) {
+    const uwg_level& L = c->lev[0];
+    uwg_lgeom g = uwg_level_geom(c, 0);
+    vk_zero<double>(c->stream, L.n_dof, y);
+    if (c->dim == 3) k_applyK_q1_3d<double><<<nblk(L.n_el, 128), 128, 0, c->stream>>>(g, L.W64, L.bc, false, x, y);
+    else k_applyK_q1_2d<double><<<nblk(L.n_el, 128), 128, 0, c->stream>>>(g, L.W64, L.bc, false, x, y);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+template int uwg_ops_applyK<double>(uwg_ctx*, int, const double*, double*);
+template int uwg_ops_applyK<float>(uwg_ctx*, int, const float*, float*);
+
+// ---------------------------------------------------------------------------
+// Gradient and divergence (dQ0), element-wise closed form of -int dN_A/dx_i.
+// ---------------------------------------------------------------------------
+template <int DIM>
+__global__ void k_applyG(uwg_lgeom g, const uint8_t* bc, const double* p, double* y) {
+    constexpr int NEN = DIM == 3 ? 8 : 4;
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= g.n_el) return;
+    int64_t nodes[8];
+    double h[3];
+    q1_elem(g, e, nodes, h);
+    double pe = p[e];
+    for (int n = 0; n < NEN; n++)
+        for (int i = 0; i < DIM; i++) {
+            int64_t dof = nodes[n] * DIM + i;
+            if (bc[dof]) continue;
+            double ge = 1.0;
+            for (int d = 0; d < DIM; d++)
+                if (d != i) ge *= 0.5 * h[d];
+            ge *= ((n >> i) & 1) ? -1.0 : 1.0;
+            atomicAdd(&y[dof], ge * pe);
+        }
+}
+
+template <int DIM>
+__global__ void k_applyGt(uwg_lgeom g, const uint8_t* bc, int only_bc, const double* u, double* q) {
+    constexpr int NEN = DIM == 3 ? 8 : 4;
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= g.n_el) return;
+    int64_t nodes[8];
+    double h[3];
+    q1_elem(g, e, nodes, h);
+    double s = 0.0;
+    for (int n = 0; n < NEN; n++)
+        for (int i = 0; i < DIM; i++) {
+            int64_t dof = nodes[n] * DIM + i;
+            if ((bc[dof] != 0) != (only_bc != 0)) continue;
+            double ge = 1.0;
+            for (int d = 0; d < DIM; d++)
+                if (d != i) ge *= 0.5 * h[d];
+            ge *= ((n >> i) & 1) ? -1.0 : 1.0;
+            s += ge * u[dof];
+        }
+    q[e] = s;
+}
+
+int uwg_ops_applyG(uwg_ctx* c, const double* p, double* y) {
+    uwg_lgeom g = uwg_level_geom(c, 0);
+    vk_zero<double>(c->stream, c->n_vdof, y);
+    if (c->dim == 3) k_applyG<3><<<nblk(c->n_el), 256, 0, c->stream>>>(g, c->bc, p, y);
+    else k_applyG<2><<<nblk(c->n_el), 256, 0, c->stream>>>(g, c->bc, p, y);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
+int uwg_ops_applyGt(uwg_ctx* c, const double* u, double* q) { return uwg_ops_applyGt_mode(c, u, q, 0); }
+
+int uwg_ops_applyGt_mode(uwg_ctx* c, const double* u, double* q, int only_bc) {
+    uwg_lgeom g = uwg_level_geom(c, 0);
+    if (c->dim == 3) k_applyGt<3><<<nblk(c->n_el), 256, 0, c->stream>>>(g, c->bc, only_bc, u, q);
+    else k_applyGt<2><<<nblk(c->n_el), 256, 0, c->stream>>>(g, c->bc, only_bc, u, q);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
+__global__ void k_schur_pc(int64_t n, const double* shat, const double* r, double* z) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) z[i] = r[i] / shat[i];
+}
+
+int uwg_ops_schur_pc(uwg_ctx* c, const double* r, double* z) {
+    k_schur_pc<<<nblk(c->n_pdof), 256, 0, c->stream>>>(c->n_pdof, c->Shat, r, z);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
+__global__ void k_pmul(int64_t n, const double* a, const double* x, double* y) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) y[i] = a[i] * x[i];
+}
+
+int uwg_ops_apply_C(uwg_ctx* c, const double* p, double* q) {
+    if (!c->Mp) { vk_zero<double>(c->stream, c->n_pdof, q); return UWG_OK; }
+    k_pmul<<<nblk(c->n_pdof), 256, 0, c->stream>>>(c->n_pdof, c->Mp, p, q);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Multigrid transfer (Q1 nested meshes).
+// ---------------------------------------------------------------------------
+template <typename T, int DIM>
+__global__ void k_prolong_add(uwg_lgeom gf, uwg_lgeom gc, const uint8_t* bcf, const T* xc, T* xf) {
+    int64_t nd = gf.n_nodes;
+    int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (n >= nd) return;
+    int fi[3] = {(int)(n % gf.nx[0]), (int)((n / gf.nx[0]) % gf.nx[1]), DIM == 3 ? (int)(n / ((int64_t)gf.nx[0] * gf.nx[1])) : 0};
+    int lo[3], hi[3];
+    T wl[3], wh[3];
+    for (int d = 0; d < 3; d++) {
+        if (d >= DIM) { lo[d] = hi[d] = 0; wl[d] = 1; wh[d] = 0; continue; }
+        if (fi[d] & 1) { lo[d] = fi[d] >> 1; hi[d] = lo[d] + 1; wl[d] = 0.5; wh[d] = 0.5; }
+        else { lo[d] = hi[d] = fi[d] >> 1; wl[d] = 1; wh[d] = 0; }
+    }
+    T acc[3] = {0, 0, 0};
+    for (int kz = 0; kz < (DIM == 3 ? 2 : 1); kz++)
+        for (int ky = 0; ky < 2; ky++)
+            for (int kx = 0; kx < 2; kx++) {
+                T w = (kx ? wh[0] : wl[0]) * (ky ? wh[1] : wl[1]) * (DIM == 3 ? (kz ? wh[2] : wl[2]) : (T)1);
+                if (w == (T)0) continue;
+                int64_t cn = (kx ? hi[0] : lo[0]) + (int64_t)gc.nx[0] * ((ky ? hi[1] : lo[1]) + (int64_t)gc.nx[1] * (kz ? hi[2] : lo[2]));
+                for (int c = 0; c < DIM; c++) acc[c] += w * xc[cn * DIM + c];
+            }
+    for (int c = 0; c < DIM; c++)
+        if (!bcf[n * DIM + c]) xf[n * DIM + c] += acc[c];
+}
+
+template <typename T, int DIM>
+__global__ void k_restrict(uwg_lgeom gf, uwg_lgeom gc, const uint8_t* bcf, const uint8_t* bcc, const T* rf, T* rc) {
+    int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (n >= gc.n_nodes) return;
+    int ci[3] = {(int)(n % gc.nx[0]), (int)((n / gc.nx[0]) % gc.nx[1]), DIM == 3 ? (int)(n / ((int64_t)gc.nx[0] * gc.nx[1])) : 0};
+    T acc[3] = {0, 0, 0};
+    for (int dz = (DIM == 3 ? -1 : 0); dz <= (DIM == 3 ? 1 : 0); dz++)
+        for (int dy = -1; dy <= 1; dy++)
+            for (int dx = -1; dx <= 1; dx++) {
+                int f[3] = {2 * ci[0] + dx, 2 * ci[1] + dy, 2 * ci[2] + dz};
+                bool ok = true;
+                for (int d = 0; d < DIM; d++) ok = ok && f[d] >= 0 && f[d] < gf.nx[d];
+                if (!ok) continue;
+                T w = (dx ? (T)0.5 : (T)1) * (dy ? (T)0.5 : (T)1) * (dz ? (T)0.5 : (T)1);
+                int64_t fn = f[0] + (int64_t)gf.nx[0] * (f[1] + (int64_t)gf.nx[1] * f[2]);
+                for (int c = 0; c < DIM; c++)
+                    if (!bcf[fn * DIM + c]) acc[c] += w * rf[fn * DIM + c];
+            }
+    for (int c = 0; c < DIM; c++) rc[n * DIM + c] = bcc[n * DIM + c] ? (T)0 : acc[c];
+}
+
+template <typename T>
+int uwg_ops_prolong_add(uwg_ctx* c, int lc, const T* xc, T* xf) {
+    uwg_lgeom gf = uwg_level_geom(c, lc - 1), gc = uwg_level_geom(c, lc);
+    if (c->dim == 3) k_prolong_add<T, 3><<<nblk(gf.n_nodes), 256, 0, c->stream>>>(gf, gc, c->lev[lc - 1].bc, xc, xf);
+    else k_prolong_add<T, 2><<<nblk(gf.n_nodes), 256, 0, c->stream>>>(gf, gc, c->lev[lc - 1].bc, xc, xf);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+template <typename T>
+int uwg_ops_restrict(uwg_ctx* c, int lc, const T* rf, T* rc) {
+    uwg_lgeom gf = uwg_level_geom(c, lc - 1), gc = uwg_level_geom(c, lc);
+    if (c->dim == 3) k_restrict<T, 3><<<nblk(gc.n_nodes), 256, 0, c->stream>>>(gf, gc, c->lev[lc - 1].bc, c->lev[lc].bc, rf, rc);
+    else k_restrict<T, 2><<<nblk(gc.n_nodes), 256, 0, c->stream>>>(gf, gc, c->lev[lc - 1].bc, c->lev[lc].bc, rf, rc);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+template int uwg_ops_prolong_add<double>(uwg_ctx*, int, const double*, double*);
+template int uwg_ops_prolong_add<float>(uwg_ctx*, int, const float*, float*);
+template int uwg_ops_restrict<double>(uwg_ctx*, int, const double*, double*);
+template int uwg_ops_restrict<float>(uwg_ctx*, int, const float*, float*);
+
+// Coarsening of W: parent weights from the children's, separable 3x3 maps.
+// Child points s in {-1,0,1} sit at parent coordinate (s + 2*delta - 1)/2.
+__constant__ double c_T[2][3][3];   // [delta][child point][parent point]
+
+template <int DIM>
+__global__ void k_coarsen_W(uwg_lgeom gf, uwg_lgeom gc, const double* Wf, double* Wc) {
+    constexpr int NQ = DIM == 3 ? 27 : 9;
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= gc.n_el) return;
+    int ex = (int)(e % gc.res[0]), ey = (int)((e / gc.res[0]) % gc.res[1]);
+    int ez = DIM == 3 ? (int)(e / ((int64_t)gc.res[0] * gc.res[1])) : 0;
+    double acc[NQ];
+    for (int j = 0; j < NQ; j++) acc[j] = 0.0;
+    for (int cz = 0; cz < (DIM == 3 ? 2 : 1); cz++)
+        for (int cy = 0; cy < 2; cy++)
+            for (int cx = 0; cx < 2; cx++) {
+                int64_t fe = (2 * ex + cx) + (int64_t)gf.res[0] * ((2 * ey + cy) + (int64_t)gf.res[1] * (2 * ez + cz));
+                double w[NQ], t1[NQ], t2[NQ];
+                for (int j = 0; j < NQ; j++) w[j] = Wf[(int64_t)j * gf.n_el + fe];
+                // x
+                for (int k = 0; k < NQ / 3; k++)
+                    for (int a = 0; a < 3; a++) {
+                        double s = 0.0;
+                        for (int b = 0; b < 3; b++) s += c_T[cx][b][a] * w[b + 3 * k];
+                        t1[a + 3 * k] = s;
+                    }
+                // y
+                for (int kz = 0; kz < (DIM == 3 ? 3 : 1); kz++)
+                    for (int a = 0; a < 3; a++)
+                        for (int ix = 0; ix < 3; ix++) {
+                            double s = 0.0;
+                            for (int b = 0; b < 3; b++) s += c_T[cy][b][a] * t1[ix + 3 * b + 9 * kz];
+                            t2[ix + 3 * a + 9 * kz] = s;
+                        }
+                if (DIM == 3) {
+                    for (int a = 0; a < 3; a++)
+                        for (int ixy = 0; ixy < 9; ixy++) {
+                            double s = 0.0;
+                            for (int b = 0; b < 3; b++) s += c_T[cz][b][a] * t2[ixy + 9 * b];
+                            acc[ixy + 9 * a] += s;
+                        }
+                } else {
+                    for (int j = 0; j < NQ; j++) acc[j] += t2[j];
+                }
+            }
+    for (int j = 0; j < NQ; j++) Wc[(int64_t)j * gc.n_el + e] = acc[j];
+}
+
+int uwg_ops_coarsen(uwg_ctx* c, int l) {
+    static bool init = false;
+    if (!init) {
+        double T[2][3][3];
+        for (int dl = 0; dl < 2; dl++)
+            for (int b = 0; b < 3; b++) {
+                double s = ((b - 1) + (2 * dl - 1)) * 0.5;
+                T[dl][b][0] = 0.5 * s * (s - 1.0);
+                T[dl][b][1] = 1.0 - s * s;
+                T[dl][b][2] = 0.5 * s * (s + 1.0);
+            }
+        UWG_CUDA(c, cudaMemcpyToSymbol(c_T, T, sizeof(T)));
+        init = true;
+    }
+    uwg_lgeom gf = uwg_level_geom(c, l), gc = uwg_level_geom(c, l + 1);
+    if (c->dim == 3) k_coarsen_W<3><<<nblk(gc.n_el, 128), 128, 0, c->stream>>>(gf, gc, c->lev[l].W64, c->lev[l + 1].W64);
+    else k_coarsen_W<2><<<nblk(gc.n_el, 128), 128, 0, c->stream>>>(gf, gc, c->lev[l].W64, c->lev[l + 1].W64);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
+__global__ void k_bc_coarsen(uwg_lgeom gf, uwg_lgeom gc, int dim, const uint8_t* bcf, uint8_t* bcc) {
+    int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (n >= gc.n_nodes) return;
+    int ci[3] = {(int)(n % gc.nx[0]), (int)((n / gc.nx[0]) % gc.nx[1]), dim == 3 ? (int)(n / ((int64_t)gc.nx[0] * gc.nx[1])) : 0};
+    int64_t fn = 2 * ci[0] + (int64_t)gf.nx[0] * (2 * ci[1] + (int64_t)gf.nx[1] * 2 * ci[2]);
+    for (int c = 0; c < dim; c++) bcc[n * dim + c] = bcf[fn * dim + c];
+}
+
+int uwg_ops_bc_coarsen(uwg_ctx* c, int l) {
+    uwg_lgeom gf = uwg_level_geom(c, l), gc = uwg_level_geom(c, l + 1);
+    k_bc_coarsen<<<nblk(gc.n_nodes), 256, 0, c->stream>>>(gf, gc, c->dim, c->lev[l].bc, c->lev[l + 1].bc);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
+__global__ void k_to_f32(int64_t n, const double* a, float* b) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (float)a[i];
+}
+
+int uwg_ops_level_setup(uwg_ctx* c, int l) {
+    uwg_level& L = c->lev[l];
+    uwg_lgeom g = uwg_level_geom(c, l);
+    vk_zero<double>(c->stream, L.n_dof, L.diag64);
+    if (c->dim == 3) k_diag_q1<3><<<nblk(L.n_el), 256, 0, c->stream>>>(g, L.W64, L.bc, L.diag64, l == 0 ? c->Shat : nullptr, c->Mp);
+    else k_diag_q1<2><<<nblk(L.n_el), 256, 0, c->stream>>>(g, L.W64, L.bc, L.diag64, l == 0 ? c->Shat : nullptr, c->Mp);
+    UWG_CUDA(c, cudaGetLastError());
+    k_diag_bc<<<nblk(L.n_dof), 256, 0, c->stream>>>(L.n_dof, L.bc, L.diag64, L.diag32, nullptr);
+    int nq = c->dim == 3 ? 27 : 9;
+    k_to_f32<<<nblk(L.n_el * nq), 256, 0, c->stream>>>(L.n_el * nq, L.W64, L.W32);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Element matrices from W (diagnostics and the dense coarse operator).
+// ---------------------------------------------------------------------------
+template <int DIM>
+__device__ void q1_Ke_from_W(const double* Wl, const double* h, double* Ke) {
+    constexpr int NQ = DIM == 3 ? 27 : 9;
+    constexpr int NEN = DIM == 3 ? 8 : 4;
+    constexpr int ND = NEN * DIM;
+    double hi[3] = {2.0 / h[0], 2.0 / h[1], DIM == 3 ? 2.0 / h[2] : 1.0};
+    for (int i = 0; i < ND * ND; i++) Ke[i] = 0.0;
+    for (int j = 0; j < NQ; j++) {
+        int pt[3] = {j % 3, (j / 3) % 3, DIM == 3 ? j / 9 : 1};
+        double gx[NEN][3];
+        for (int n = 0; n < NEN; n++)
+            for (int d = 0; d < DIM; d++) gx[n][d] = hi[d] * q1_lderiv<DIM>(n, d, pt);
+        for (int a = 0; a < NEN; a++)
+            for (int b = 0; b < NEN; b++) {
+                double s2 = 0.0;
+                for (int d = 0; d < DIM; d++) s2 += gx[a][d] * gx[b][d];
+                for (int ci = 0; ci < DIM; ci++)
+                    for (int cj = 0; cj < DIM; cj++) {
+                        double v = gx[a][cj] * gx[b][ci] + (ci == cj ? s2 : 0.0);
+                        Ke[(a * DIM + ci) * ND + b * DIM + cj] += Wl[j] * v;
+                    }
+            }
+    }
+}
+
+template <int DIM>
+__global__ void k_element_matrices(uwg_lgeom g, int64_t e, const double* W, const double* shat, double* Ke,
+                                   double* Ge, double* Se) {
+    constexpr int NQ = DIM == 3 ? 27 : 9;
+    constexpr int NEN = DIM == 3 ? 8 : 4;
+    int64_t nodes[8];
+    double h[3], Wl[NQ];
+    q1_elem(g, e, nodes, h);
+    for (int j = 0; j < NQ; j++) Wl[j] = W[(int64_t)j * g.n_el + e];
+    q1_Ke_from_W<DIM>(Wl, h, Ke);
+    for (int n = 0; n < NEN; n++)
+        for (int i = 0; i < DIM; i++) {
+            double ge = 1.0;
+            for (int d = 0; d < DIM; d++)
+                if (d != i) ge *= 0.5 * h[d];
+            Ge[n * DIM + i] = ge * (((n >> i) & 1) ? -1.0 : 1.0);
+        }
+    Se[0] = shat[e];
+}
+
+int uwg_ops_element_matrices(uwg_ctx* c, int64_t el, double* Ke, double* fe, double* Ge, double* Se) {
+    int nd = c->dim * c->nen;
+    double* buf = nullptr;
+    UWG_CUDA(c, cudaMallocAsync((void**)&buf, sizeof(double) * (nd * nd + nd + 1), c->stream));
+    uwg_lgeom g = uwg_level_geom(c, 0);
+    if (c->dim == 3) k_element_matrices<3><<<1, 1, 0, c->stream>>>(g, el, c->lev[0].W64, c->Shat, buf, buf + nd * nd, buf + nd * nd + nd);
+    else k_element_matrices<2><<<1, 1, 0, c->stream>>>(g, el, c->lev[0].W64, c->Shat, buf, buf + nd * nd, buf + nd * nd + nd);
+    std::vector<double> h(nd * nd + nd + 1);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), buf, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->stream);
+    cudaFreeAsync(buf, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return uwg_set_error(c, UWG_ERR_CUDA, cudaGetErrorString(e));
+    if (Ke) std::copy(h.begin(), h.begin() + nd * nd, Ke);
+    if (Ge) std::copy(h.begin() + nd * nd, h.begin() + nd * nd + nd, Ge);
+    if (Se) Se[0] = h[nd * nd + nd];
+    if (fe) {
+        for (int i = 0; i < nd; i++) fe[i] = 0.0;   // element force is scattered at assembly
+    }
+    return UWG_OK;
+}
+
+// Dense coarse operator: assemble from W, then Gauss-Jordan inverse in one block.
+template <int DIM>
+__global__ void k_dense_assemble(uwg_lgeom g, const double* W, const uint8_t* bc, int64_t n, double* A) {
+    constexpr int NQ = DIM == 3 ? 27 : 9;
+    constexpr int NEN = DIM == 3 ? 8 : 4;
+    constexpr int ND = NEN * DIM;
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= g.n_el) return;
+    int64_t nodes[8];
+    double h[3], Wl[NQ], Ke[ND * ND];
+    q1_elem(g, e, nodes, h);
+    for (int j = 0; j < NQ; j++) Wl[j] = W[(int64_t)j * g.n_el + e];
+    q1_Ke_from_W<DIM>(Wl, h, Ke);
+    for (int a = 0; a < ND; a++)
+        for (int b = 0; b < ND; b++) {
+            int64_t r = nodes[a / DIM] * DIM + a % DIM, cc = nodes[b / DIM] * DIM + b % DIM;
+            if (bc[r] || bc[cc]) continue;
+            atomicAdd(&A[r * n + cc], Ke[a * ND + b]);
+        }
+}
+
+__global__ void k_dense_bcdiag(int64_t n, const uint8_t* bc, double* A) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n && bc[i]) A[i * n + i] = 1.0;
+}
+
+// In-place Gauss-Jordan inverse of an SPD matrix (no pivoting needed), one block.
+__global__ void k_dense_invert(int64_t n, double* A, double* B) {
+    // B <- I; eliminate column by column on [A | B]
+    for (int64_t i = threadIdx.x; i < n * n; i += blockDim.x) B[i] = (i / n == i % n) ? 1.0 : 0.0;
+    __syncthreads();
+    for (int64_t k = 0; k < n; k++) {
+        double piv = A[k * n + k];
+        __syncthreads();
+        for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
+            A[k * n + j] /= piv;
+            B[k * n + j] /= piv;
+        }
+        __syncthreads();
+        for (int64_t idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+            int64_t i = idx / n, j = idx % n;
+            if (i == k) continue;
+            double f = A[i * n + k];
+            if (j != k) A[i * n + j] -= f * A[k * n + j];
+            B[i * n + j] -= f * B[k * n + j];
+        }
+        __syncthreads();
+        for (int64_t i = threadIdx.x; i < n; i += blockDim.x)
+            if (i != k) A[i * n + k] = 0.0;
+        __syncthreads();
+    }
+}
+
+int uwg_ops_dense_coarse(uwg_ctx* c, int l) {
+    uwg_level& L = c->lev[l];
+    int64_t n = L.n_dof;
+    if (n > 4096) return uwg_set_error(c, UWG_ERR_ARG, "coarsest multigrid level too large for a dense solve");
+    uwg_lgeom g = uwg_level_geom(c, l);
+    double* A = nullptr;
+    UWG_CUDA(c, cudaMallocAsync((void**)&A, sizeof(double) * n * n, c->stream));
+    UWG_CUDA(c, cudaMemsetAsync(A, 0, sizeof(double) * n * n, c->stream));
+    if (c->dim == 3) k_dense_assemble<3><<<nblk(L.n_el, 64), 64, 0, c->stream>>>(g, L.W64, L.bc, n, A);
+    else k_dense_assemble<2><<<nblk(L.n_el, 64), 64, 0, c->stream>>>(g, L.W64, L.bc, n, A);
+    k_dense_bcdiag<<<nblk(n), 256, 0, c->stream>>>(n, L.bc, A);
+    k_dense_invert<<<1, 1024, 0, c->stream>>>(n, A, L.cinv64);
+    k_to_f32<<<nblk(n * n), 256, 0, c->stream>>>(n * n, L.cinv64, L.cinv32);
+    cudaError_t e = cudaGetLastError();
+    cudaFreeAsync(A, c->stream);
+    if (e != cudaSuccess) return uwg_set_error(c, UWG_ERR_CUDA, cudaGetErrorString(e));
+    return UWG_OK;
+}
+
+template <typename T>
+__global__ void k_dense_mv(int64_t n, const T* Ainv, const T* b, T* x) {
+    int64_t i = blockIdx.x * (int64_t)(blockDim.x / 32) + (threadIdx.x >> 5);
+    int lane = threadIdx.x & 31;
+    if (i >= n) return;
+    T s = 0;
+    for (int64_t j = lane; j < n; j += 32) s += Ainv[i * n + j] * b[j];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) x[i] = s;
+}
+
+template <typename T>
+int uwg_ops_dense_solve(uwg_ctx* c, int l, const T* b, T* x) {
+    uwg_level& L = c->lev[l];
+    const T* Ainv;
+    if constexpr (sizeof(T) == 8) Ainv = (const T*)L.cinv64; else Ainv = (const T*)L.cinv32;
+    k_dense_mv<T><<<nblk(L.n_dof * 32, 256), 256, 0, c->stream>>>(L.n_dof, Ainv, b, x);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+template int uwg_ops_dense_solve<double>(uwg_ctx*, int, const double*, double*);
+template int uwg_ops_dense_solve<float>(uwg_ctx*, int, const float*, float*);
+
+int uwg_ops_assemble(uwg_ctx* c, const int32_t* off, const int32_t* list, const double* ip_xi,
+                     const double* ip_w, const double* eta_p, const double* body_p, const double* lambda_p) {
+    uwg_lgeom g = uwg_level_geom(c, 0);
+    vk_zero<double>(c->stream, c->n_vdof, c->f);
+    if (c->dim == 3)
+        k_assemble_q1<3><<<nblk(c->n_el, 128), 128, 0, c->stream>>>(g, off, list, ip_xi, ip_w, eta_p, body_p, lambda_p,
+                                                                     c->lev[0].W64, c->f, c->Mp);
+    else
+        k_assemble_q1<2><<<nblk(c->n_el, 128), 128, 0, c->stream>>>(g, off, list, ip_xi, ip_w, eta_p, body_p, lambda_p,
+                                                                     c->lev[0].W64, c->f, c->Mp);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Vector kernels
+// ---------------------------------------------------------------------------
+template <typename T> __global__ void vk_copy_k(int64_t n, const T* x, T* y) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) y[i] = x[i];
+}
+template <typename A, typename B> __global__ void vk_convert_k(int64_t n, const A* x, B* y) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) y[i] = (B)x[i];
+}
+template <typename T> __global__ void vk_axpy_k(int64_t n, T a, const T* x, T* y) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) y[i] += a * x[i];
+}
+template <typename T> __global__ void vk_axpby_k(int64_t n, T a, const T* x, T b, T* y) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) y[i] = a * x[i] + b * y[i];
+}
+template <typename T> __global__ void vk_scale_k(int64_t n, T a, T* y) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) y[i] *= a;
+}
+template <typename T> __global__ void vk_mask_k(int64_t n, const uint8_t* bc, T* y) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n && bc[i]) y[i] = 0;
+}
+template <typename T> __global__ void vk_pdiv_k(int64_t n, const T* x, const T* d, T* y) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) y[i] = x[i] / d[i];
+}
+
+template <typename T> void vk_copy(cudaStream_t s, int64_t n, const T* x, T* y) { if (n) vk_copy_k<T><<<nblk(n), 256, 0, s>>>(n, x, y); }
+template <typename A, typename B> void vk_convert(cudaStream_t s, int64_t n, const A* x, B* y) { if (n) vk_convert_k<A, B><<<nblk(n), 256, 0, s>>>(n, x, y); }
+template <typename T> void vk_axpy(cudaStream_t s, int64_t n, T a, const T* x, T* y) { if (n) vk_axpy_k<T><<<nblk(n), 256, 0, s>>>(n, a, x, y); }
+template <typename T> void vk_axpby(cudaStream_t s, int64_t n, T a, const T* x, T b, T* y) { if (n) vk_axpby_k<T><<<nblk(n), 256, 0, s>>>(n, a, x, b, y); }
+template <typename T> void vk_scale(cudaStream_t s, int64_t n, T a, T* y) { if (n) vk_scale_k<T><<<nblk(n), 256, 0, s>>>(n, a, y); }
+template <typename T> void vk_zero(cudaStream_t s, int64_t n, T* y) { if (n) cudaMemsetAsync(y, 0, sizeof(T) * n, s); }
+template <typename T> void vk_mask(cudaStream_t s, int64_t n, const uint8_t* bc, T* y) { if (n) vk_mask_k<T><<<nblk(n), 256, 0, s>>>(n, bc, y); }
+template <typename T> void vk_pointwise_div(cudaStream_t s, int64_t n, const T* x, const T* d, T* y) { if (n) vk_pdiv_k<T><<<nblk(n), 256, 0, s>>>(n, x, d, y); }
+
+template void vk_copy<double>(cudaStream_t, int64_t, const double*, double*);
+template void vk_copy<float>(cudaStream_t, int64_t, const float*, float*);
+template void vk_convert<double, float>(cudaStream_t, int64_t, const double*, float*);
+template void vk_convert<float, double>(cudaStream_t, int64_t, const float*, double*);
+template void vk_axpy<double>(cudaStream_t, int64_t, double, const double*, double*);
+template void vk_axpy<float>(cudaStream_t, int64_t, float, const float*, float*);
+template void vk_axpby<double>(cudaStream_t, int64_t, double, const double*, double, double*);
+template void vk_axpby<float>(cudaStream_t, int64_t, float, const float*, float, float*);
+template void vk_scale<double>(cudaStream_t, int64_t, double, double*);
+template void vk_scale<float>(cudaStream_t, int64_t, float, float*);
+template void vk_zero<double>(cudaStream_t, int64_t, double*);
+template void vk_zero<float>(cudaStream_t, int64_t, float*);
+template void vk_mask<double>(cudaStream_t, int64_t, const uint8_t*, double*);
+template void vk_mask<float>(cudaStream_t, int64_t, const uint8_t*, float*);
+template void vk_pointwise_div<double>(cudaStream_t, int64_t, const double*, const double*, double*);
+template void vk_pointwise_div<float>(cudaStream_t, int64_t, const float*, const float*, float*);
+
+// Dot products: block partial sums in double, then atomics into dst.
+struct dot_ptrs { const void* a[4]; const void* b[4]; };
+
+template <typename T>
+__global__ void vk_dots_k(int64_t n, int k, dot_ptrs P, double* dst) {
+    __shared__ double sm[4][32];
+    double acc[4] = {0, 0, 0, 0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        for (int j = 0; j < k; j++) acc[j] += (double)((const T*)P.a[j])[i] * (double)((const T*)P.b[j])[i];
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int j = 0; j < k; j++) {
+        double v = acc[j];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) sm[j][w] = v;
+    }
+    __syncthreads();
+    if (w == 0) {
+        for (int j = 0; j < k; j++) {
+            double v = lane < (int)(blockDim.x >> 5) ? sm[j][lane] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) atomicAdd(&dst[j], v);
+        }
+    }
+}
+
+template <typename T>
+void vk_dots(cudaStream_t s, int64_t n, int k, const T* const* a, const T* const* b, double* dst) {
+    dot_ptrs P;
+    for (int j = 0; j < 4; j++) { P.a[j] = j < k ? a[j] : nullptr; P.b[j] = j < k ? b[j] : nullptr; }
+    cudaMemsetAsync(dst, 0, sizeof(double) * k, s);
+    unsigned nb = std::min<unsigned>(nblk(n, 256), 152u * 8u);
+    if (nb == 0) nb = 1;
+    vk_dots_k<T><<<nb, 256, 0, s>>>(n, k, P, dst);
+}
+template void vk_dots<double>(cudaStream_t, int64_t, int, const double* const*, const double* const*, double*);
+template void vk_dots<float>(cudaStream_t, int64_t, int, const float* const*, const float* const*, double*);
+
+#define MDOT_MAX 64
+struct mdot_ptrs { const double* v[MDOT_MAX]; };
+
+__global__ void vk_mdot_k(int64_t n, int k, mdot_ptrs P, const double* w, double* dst) {
+    // one block-column of vectors per blockIdx.y
+    __shared__ double sm[32];
+    int j = blockIdx.y;
+    double acc = 0.0;
+    const double* v = P.v[j];
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        acc += v[i] * w[i];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
+    if (lane == 0) sm[wi] = acc;
+    __syncthreads();
+    if (wi == 0) {
+        acc = lane < (int)(blockDim.x >> 5) ? sm[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) atomicAdd(&dst[j], acc);
+    }
+}
+
+void vk_mdot(cudaStream_t s, int64_t n, int k, const double* const* V, const double* w, double* dst) {
+    mdot_ptrs P;
+    for (int j = 0; j < MDOT_MAX; j++) P.v[j] = j < k ? V[j] : nullptr;
+    cudaMemsetAsync(dst, 0, sizeof(double) * k, s);
+    unsigned nb = std::min<unsigned>(nblk(n, 256), 256u);
+    if (nb == 0) nb = 1;
+    vk_mdot_k<<<dim3(nb, k), 256, 0, s>>>(n, k, P, w, dst);
+}
+
+__global__ void vk_maxpy_k(int64_t n, int k, mdot_ptrs P, const double* coef, double* y) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double s = 0.0;
+    for (int j = 0; j < k; j++) s += coef[j] * P.v[j][i];
+    y[i] += s;
+}
+
+// y += sum_j coef[j] V_j  (coef on the device)
+void vk_maxpy(cudaStream_t s, int64_t n, int k, const double* coef_dev, const double* const* V, double* y) {
+    mdot_ptrs P;
+    for (int j = 0; j < MDOT_MAX; j++) P.v[j] = j < k ? V[j] : nullptr;
+    if (n && k) vk_maxpy_k<<<nblk(n), 256, 0, s>>>(n, k, P, coef_dev, y);
+}

@@ -1,0 +1,53 @@
+// Operator kernels of the Stokes system on regular Q1/dQ0 meshes (declarations).
+#pragma once
+#include "uwg_internal.cuh"
+
+// Geometry of one level passed by value to kernels.
+struct uwg_lgeom {
+    int dim;
+    int res[3];
+    int nx[3];
+    const double* ax[3];
+    int64_t n_el, n_nodes;
+};
+
+uwg_lgeom uwg_level_geom(const uwg_ctx* c, int l);
+
+// Assembly from the PIC swarm (finest level): W, f, Mp.
+int uwg_ops_assemble(uwg_ctx* c, const int32_t* off, const int32_t* list, const double* ip_xi,
+                     const double* ip_w, const double* eta_p, const double* body_p, const double* lambda_p);
+// Per-level derived data: diag (and Shat on level 0), W32 copy, coarsening.
+int uwg_ops_level_setup(uwg_ctx* c, int l);
+int uwg_ops_coarsen(uwg_ctx* c, int l);          // W of level l+1 from level l
+int uwg_ops_bc_coarsen(uwg_ctx* c, int l);       // BC mask of level l+1 from level l
+int uwg_ops_dense_coarse(uwg_ctx* c, int l);     // dense inverse of level l
+
+template <typename T> int uwg_ops_applyK(uwg_ctx* c, int l, const T* x, T* y);
+template <typename T> int uwg_ops_prolong_add(uwg_ctx* c, int lc, const T* xc, T* xf);   // xf += P xc
+template <typename T> int uwg_ops_restrict(uwg_ctx* c, int lc, const T* rf, T* rc);       // rc = R rf
+template <typename T> int uwg_ops_dense_solve(uwg_ctx* c, int l, const T* b, T* x);
+int uwg_ops_applyG(uwg_ctx* c, const double* p, double* y);      // y = G p (BC rows zero)
+int uwg_ops_applyGt(uwg_ctx* c, const double* u, double* q);     // q = G^T u (BC dofs ignored)
+int uwg_ops_applyGt_mode(uwg_ctx* c, const double* u, double* q, int only_bc);
+int uwg_ops_applyK_lift(uwg_ctx* c, const double* x, double* y); // y = P K x, x unmasked
+int uwg_solver_setup(uwg_ctx* c);
+void uwg_solver_free(uwg_ctx* c);
+int uwg_solver_residuals(uwg_ctx* c, const double* u, const double* p, double* out4);
+int uwg_ops_schur_pc(uwg_ctx* c, const double* r, double* z);    // z = Shat^-1 r
+int uwg_ops_apply_C(uwg_ctx* c, const double* p, double* q);     // q = Mp p (compressibility)
+int uwg_ops_element_matrices(uwg_ctx* c, int64_t el, double* Ke, double* fe, double* Ge, double* Se);
+
+// Vector kernels ---------------------------------------------------------------
+template <typename T> void vk_copy(cudaStream_t s, int64_t n, const T* x, T* y);
+template <typename A, typename B> void vk_convert(cudaStream_t s, int64_t n, const A* x, B* y);
+template <typename T> void vk_axpy(cudaStream_t s, int64_t n, T a, const T* x, T* y);          // y += a x
+template <typename T> void vk_axpby(cudaStream_t s, int64_t n, T a, const T* x, T b, T* y);    // y = a x + b y
+template <typename T> void vk_scale(cudaStream_t s, int64_t n, T a, T* y);
+template <typename T> void vk_zero(cudaStream_t s, int64_t n, T* y);
+template <typename T> void vk_mask(cudaStream_t s, int64_t n, const uint8_t* bc, T* y);       // y[bc] = 0
+template <typename T> void vk_pointwise_div(cudaStream_t s, int64_t n, const T* x, const T* d, T* y);
+// Sums of products into dst[k] (double), k < 4: dots of (a_k, b_k) pairs.
+template <typename T> void vk_dots(cudaStream_t s, int64_t n, int k, const T* const* a, const T* const* b,
+                                   double* dst);
+void vk_mdot(cudaStream_t s, int64_t n, int k, const double* const* V, const double* w, double* dst);
+void vk_maxpy(cudaStream_t s, int64_t n, int k, const double* coef_dev, const double* const* V, double* y);

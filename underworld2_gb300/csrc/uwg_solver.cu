@@ -1,0 +1,556 @@
+// BSSCR Schur-complement Stokes solve on the GPU.
+//
+// Structure follows BSSCR_DRIVER_auglag with penalty 0
+// (L/Solvers/KSPSolvers/src/BSSCR/auglag-driver-DGTGD.c:64-578):
+//   1. velocity pre-solve      f~ = K^-1 f                         (:285-303)
+//   2. h^ = h - G^T f~                                               (:309-310)
+//   3. pressure solve          (C - G^T K^-1 G) p = h^  by FGMRES,   (:332-441)
+//      preconditioned with the assembled Uzawa term S^ (PC "uw", preconditioner.c:164-174)
+//   4. velocity back-solve     K u = f - G p                         (:494-532)
+// The Krylov and multigrid kernels behind PETSc's KSP/PCMG are replaced by
+// GPU-native ones: preconditioned CG on K (K is SPD once Dirichlet dofs are
+// eliminated) with a geometric V-cycle (Chebyshev-Jacobi smoothing, Galerkin-
+// exact coarse operators from coarsened quadrature weights, dense coarsest
+// solve), and flexible GMRES on the Schur complement.  In mixed mode the
+// velocity solves run in FP32 inside FP64 iterative refinement.
+//
+//   L/ = src/underworld/libUnderworld/
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "uwg_ops.cuh"
+
+namespace {
+
+double now() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+template <typename T> struct LevelVecs { T *r, *d, *t, *b, *x; };
+
+struct Work {
+    bool ready = false;
+    LevelVecs<double> v64[UWG_MAXLEV];
+    LevelVecs<float> v32[UWG_MAXLEV];
+    // finest-level Krylov vectors
+    double *cg_r, *cg_z, *cg_p, *cg_q;       // FP64 PCG
+    float *cg32_r, *cg32_z, *cg32_p, *cg32_q, *cg32_x, *cg32_b;
+    double *ref_r, *ref_d;                    // refinement
+    double *u_tmp, *u_tmp2;                   // velocity temps for the Schur apply
+    double *ftil, *bvec;
+    std::vector<double*> V, Z;                // FGMRES bases (pressure)
+    double *p_tmp, *p_tmp2, *hhat;
+    double* coef;                             // device coefficients
+    int restart = 0;
+};
+
+Work* work_of(uwg_ctx* c) {
+    if (c->ws.empty()) c->ws.push_back(new Work());
+    return (Work*)c->ws[0];
+}
+
+template <typename T> T* dalloc(uwg_ctx* c, int64_t n) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, sizeof(T) * (n > 0 ? n : 1)) != cudaSuccess) return nullptr;
+    c->ws.push_back(p);
+    return (T*)p;
+}
+
+int work_init(uwg_ctx* c, int restart) {
+    Work* w = work_of(c);
+    if (w->ready && w->restart >= restart) return UWG_OK;
+    int64_t nv = c->n_vdof, np = c->n_pdof;
+    if (!w->ready) {
+        for (int l = 0; l < c->nlev; l++) {
+            int64_t n = c->lev[l].n_dof;
+            w->v64[l] = {dalloc<double>(c, n), dalloc<double>(c, n), dalloc<double>(c, n), dalloc<double>(c, n), dalloc<double>(c, n)};
+            w->v32[l] = {dalloc<float>(c, n), dalloc<float>(c, n), dalloc<float>(c, n), dalloc<float>(c, n), dalloc<float>(c, n)};
+        }
+        w->cg_r = dalloc<double>(c, nv); w->cg_z = dalloc<double>(c, nv);
+        w->cg_p = dalloc<double>(c, nv); w->cg_q = dalloc<double>(c, nv);
+        w->cg32_r = dalloc<float>(c, nv); w->cg32_z = dalloc<float>(c, nv);
+        w->cg32_p = dalloc<float>(c, nv); w->cg32_q = dalloc<float>(c, nv); w->cg32_x = dalloc<float>(c, nv);
+        w->cg32_b = dalloc<float>(c, nv);
+        w->ref_r = dalloc<double>(c, nv); w->ref_d = dalloc<double>(c, nv);
+        w->u_tmp = dalloc<double>(c, nv); w->u_tmp2 = dalloc<double>(c, nv);
+        w->ftil = dalloc<double>(c, nv); w->bvec = dalloc<double>(c, nv);
+        w->p_tmp = dalloc<double>(c, np); w->p_tmp2 = dalloc<double>(c, np); w->hhat = dalloc<double>(c, np);
+        w->coef = dalloc<double>(c, 256);
+    }
+    while ((int)w->V.size() < restart + 1) w->V.push_back(dalloc<double>(c, np));
+    while ((int)w->Z.size() < restart) w->Z.push_back(dalloc<double>(c, np));
+    w->restart = restart;
+    w->ready = true;
+    for (double* p : w->V) if (!p) return uwg_set_error(c, UWG_ERR_CUDA, "out of device memory (solver workspace)");
+    if (!w->coef) return uwg_set_error(c, UWG_ERR_CUDA, "out of device memory (solver workspace)");
+    return UWG_OK;
+}
+
+// Host reductions through the context's pinned mirror.
+template <typename T>
+int dots(uwg_ctx* c, int64_t n, int k, const T* const* a, const T* const* b, double* out) {
+    vk_dots<T>(c->stream, n, k, a, b, (double*)c->red);
+    UWG_CUDA(c, cudaMemcpyAsync(c->red_host, c->red, sizeof(double) * k, cudaMemcpyDeviceToHost, c->stream));
+    UWG_CUDA(c, cudaStreamSynchronize(c->stream));
+    for (int j = 0; j < k; j++) out[j] = c->red_host[j];
+    return UWG_OK;
+}
+
+template <typename T> double* diag_of(uwg_level& L);
+template <> double* diag_of<double>(uwg_level& L) { return L.diag64; }
+
+template <typename T> LevelVecs<T>& vecs(Work* w, int l);
+template <> LevelVecs<double>& vecs<double>(Work* w, int l) { return w->v64[l]; }
+template <> LevelVecs<float>& vecs<float>(Work* w, int l) { return w->v32[l]; }
+
+template <typename T> const T* diagT(uwg_level& L);
+template <> const double* diagT<double>(uwg_level& L) { return L.diag64; }
+template <> const float* diagT<float>(uwg_level& L) { return L.diag32; }
+
+// Chebyshev-Jacobi smoothing of K x = b on level l, `deg` applications.
+template <typename T>
+int chebyshev(uwg_ctx* c, int l, const T* b, T* x, int deg, bool x_zero) {
+    uwg_level& L = c->lev[l];
+    Work* w = work_of(c);
+    LevelVecs<T>& v = vecs<T>(w, l);
+    int64_t n = L.n_dof;
+    cudaStream_t s = c->stream;
+    double lmax = L.lmax64;
+    double alpha = 0.1 * lmax, beta = 1.1 * lmax;
+    double theta = 0.5 * (beta + alpha), delta = 0.5 * (beta - alpha);
+    double sigma = theta / delta, rho = 1.0 / sigma;
+    int rc;
+    // r = b - K x
+    if (x_zero) vk_copy<T>(s, n, b, v.r);
+    else {
+        if ((rc = uwg_ops_applyK<T>(c, l, x, v.t))) return rc;
+        vk_copy<T>(s, n, b, v.r);
+        vk_axpy<T>(s, n, (T)-1, v.t, v.r);
+    }
+    // d = D^-1 r / theta
+    vk_pointwise_div<T>(s, n, v.r, diagT<T>(L), v.d);
+    vk_scale<T>(s, n, (T)(1.0 / theta), v.d);
+    vk_axpy<T>(s, n, (T)1, v.d, x);
+    for (int i = 1; i < deg; i++) {
+        if ((rc = uwg_ops_applyK<T>(c, l, x, v.t))) return rc;
+        vk_copy<T>(s, n, b, v.r);
+        vk_axpy<T>(s, n, (T)-1, v.t, v.r);
+        double rho1 = 1.0 / (2.0 * sigma - rho);
+        // d = rho1 rho d + (2 rho1 / delta) D^-1 r
+        vk_pointwise_div<T>(s, n, v.r, diagT<T>(L), v.t);
+        vk_axpby<T>(s, n, (T)(2.0 * rho1 / delta), v.t, (T)(rho1 * rho), v.d);
+        vk_axpy<T>(s, n, (T)1, v.d, x);
+        rho = rho1;
+    }
+    return UWG_OK;
+}
+
+// V-cycle: x = M^-1 b on level l (x overwritten).
+template <typename T>
+int vcycle(uwg_ctx* c, int l, const T* b, T* x, int deg) {
+    cudaStream_t s = c->stream;
+    uwg_level& L = c->lev[l];
+    int rc;
+    if (l == c->nlev - 1) return uwg_ops_dense_solve<T>(c, l, b, x);
+    Work* w = work_of(c);
+    LevelVecs<T>& v = vecs<T>(w, l);
+    LevelVecs<T>& vc = vecs<T>(w, l + 1);
+    vk_zero<T>(s, L.n_dof, x);
+    if ((rc = chebyshev<T>(c, l, b, x, deg, true))) return rc;
+    if ((rc = uwg_ops_applyK<T>(c, l, x, v.t))) return rc;
+    vk_axpby<T>(s, L.n_dof, (T)1, b, (T)-1, v.t);   // t = b - K x
+    if ((rc = uwg_ops_restrict<T>(c, l + 1, v.t, vc.b))) return rc;
+    if ((rc = vcycle<T>(c, l + 1, vc.b, vc.x, deg))) return rc;
+    if ((rc = uwg_ops_prolong_add<T>(c, l + 1, vc.x, x))) return rc;
+    return chebyshev<T>(c, l, b, x, deg, false);
+}
+
+// Preconditioned CG on the finest level: x (in/out), stops at ||r|| <= tol*||b||
+// (tol relative to bnorm passed in).  Returns iterations or negative error.
+template <typename T>
+int pcg(uwg_ctx* c, const T* b, T* x, double bnorm, double tol, int maxit, int deg, T* r, T* z, T* p, T* q,
+        bool x_zero, int* its) {
+    cudaStream_t s = c->stream;
+    int64_t n = c->n_vdof;
+    int rc;
+    *its = 0;
+    if (bnorm == 0.0) { vk_zero<T>(s, n, x); return UWG_OK; }
+    if (x_zero) { vk_zero<T>(s, n, x); vk_copy<T>(s, n, b, r); }
+    else {
+        if ((rc = uwg_ops_applyK<T>(c, 0, x, q))) return rc;
+        vk_copy<T>(s, n, b, r);
+        vk_axpy<T>(s, n, (T)-1, q, r);
+    }
+    if ((rc = vcycle<T>(c, 0, r, z, deg))) return rc;
+    vk_copy<T>(s, n, z, p);
+    double d2[2];
+    const T* a2[2] = {r, r};
+    const T* b2[2] = {z, r};
+    if ((rc = dots<T>(c, n, 2, a2, b2, d2))) return rc;
+    double rz = d2[0];
+    if (std::sqrt(d2[1]) <= tol * bnorm) return UWG_OK;
+    for (int it = 1; it <= maxit; it++) {
+        if ((rc = uwg_ops_applyK<T>(c, 0, p, q))) return rc;
+        double pq;
+        const T* a1[1] = {p};
+        const T* b1[1] = {q};
+        if ((rc = dots<T>(c, n, 1, a1, b1, &pq))) return rc;
+        if (!std::isfinite(pq) || pq <= 0.0) {
+            *its = it;
+            return uwg_set_error(c, std::isfinite(pq) ? UWG_ERR_NOT_CONVERGED : UWG_ERR_NAN,
+                                 "velocity CG breakdown (p.Kp = " + std::to_string(pq) + ")");
+        }
+        double alpha = rz / pq;
+        vk_axpy<T>(s, n, (T)alpha, p, x);
+        vk_axpy<T>(s, n, (T)-alpha, q, r);
+        if ((rc = vcycle<T>(c, 0, r, z, deg))) return rc;
+        if ((rc = dots<T>(c, n, 2, a2, b2, d2))) return rc;
+        *its = it;
+        if (!std::isfinite(d2[1])) return uwg_set_error(c, UWG_ERR_NAN, "non-finite residual in velocity CG");
+        if (std::sqrt(d2[1]) <= tol * bnorm) return UWG_OK;
+        double beta = d2[0] / rz;
+        rz = d2[0];
+        vk_axpby<T>(s, n, (T)1, z, (T)beta, p);
+    }
+    return uwg_set_error(c, UWG_ERR_NOT_CONVERGED, "velocity CG reached its iteration cap");
+}
+
+struct SolveCfg {
+    bool mixed;
+    double inner_rtol;
+    int max_inner;
+    int deg;
+};
+
+// x = A^-1 b for the velocity operator A = PKP + (I-P), FP64 result.
+// x holds the initial guess unless x_zero.  Returns iterations through *its.
+int velocity_solve(uwg_ctx* c, const SolveCfg& cfg, const double* b, double* x, bool x_zero, int* its,
+                   int* refine_steps) {
+    Work* w = work_of(c);
+    cudaStream_t s = c->stream;
+    int64_t n = c->n_vdof;
+    double bn;
+    const double* ab[1] = {b};
+    int rc = dots<double>(c, n, 1, ab, ab, &bn);
+    if (rc) return rc;
+    bn = std::sqrt(bn);
+    *its = 0;
+    if (!cfg.mixed)
+        return pcg<double>(c, b, x, bn, cfg.inner_rtol, cfg.max_inner, cfg.deg, w->cg_r, w->cg_z, w->cg_p,
+                           w->cg_q, x_zero, its);
+    // FP64 iterative refinement around FP32 PCG
+    if (x_zero) vk_zero<double>(s, n, x);
+    if (bn == 0.0) return UWG_OK;
+    for (int step = 0; step < 30; step++) {
+        if ((rc = uwg_ops_applyK<double>(c, 0, x, w->ref_d))) return rc;
+        vk_copy<double>(s, n, b, w->ref_r);
+        vk_axpy<double>(s, n, -1.0, w->ref_d, w->ref_r);
+        double rn;
+        const double* ar[1] = {w->ref_r};
+        if ((rc = dots<double>(c, n, 1, ar, ar, &rn))) return rc;
+        rn = std::sqrt(rn);
+        if (!std::isfinite(rn)) return uwg_set_error(c, UWG_ERR_NAN, "non-finite residual in refinement");
+        if (rn <= cfg.inner_rtol * bn) return UWG_OK;
+        if (refine_steps) (*refine_steps)++;
+        vk_convert<double, float>(s, n, w->ref_r, w->cg32_b);
+        // the FP32 correction only needs a few digits; ask for 1e-5 of this residual
+        double inner = std::max(1e-5, 0.5 * cfg.inner_rtol * bn / rn);
+        int it32 = 0;
+        rc = pcg<float>(c, w->cg32_b, w->cg32_x, rn, inner, cfg.max_inner, cfg.deg, w->cg32_r, w->cg32_z,
+                        w->cg32_p, w->cg32_q, true, &it32);
+        *its += it32;
+        if (rc && rc != UWG_ERR_NOT_CONVERGED) return rc;
+        vk_convert<float, double>(s, n, w->cg32_x, w->ref_d);
+        vk_axpy<double>(s, n, 1.0, w->ref_d, x);
+    }
+    return uwg_set_error(c, UWG_ERR_NOT_CONVERGED, "velocity refinement did not converge");
+}
+
+}  // namespace
+
+void uwg_solver_free(uwg_ctx* c) {
+    for (size_t i = 1; i < c->ws.size(); i++) cudaFree(c->ws[i]);
+    if (!c->ws.empty()) delete (Work*)c->ws[0];
+    c->ws.clear();
+}
+
+// Lanczos-free eigenvalue bound: power iteration on D^-1 K.
+int uwg_solver_estimate(uwg_ctx* c, int l) {
+    uwg_level& L = c->lev[l];
+    int rc = work_init(c, 30);
+    if (rc) return rc;
+    Work* w = work_of(c);
+    LevelVecs<double>& v = w->v64[l];
+    cudaStream_t s = c->stream;
+    int64_t n = L.n_dof;
+    // deterministic start vector: 1 + small variation, BC dofs zero
+    std::vector<double> h(n);
+    for (int64_t i = 0; i < n; i++) h[i] = 1.0 + 0.37 * std::sin(0.731 * (double)i);
+    UWG_CUDA(c, cudaMemcpyAsync(v.x, h.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    vk_mask<double>(s, n, L.bc, v.x);
+    double lam = 0.0;
+    for (int it = 0; it < 12; it++) {
+        if ((rc = uwg_ops_applyK<double>(c, l, v.x, v.t))) return rc;
+        vk_mask<double>(s, n, L.bc, v.t);
+        vk_pointwise_div<double>(s, n, v.t, L.diag64, v.d);
+        double d2[2];
+        const double* a[2] = {v.d, v.x};
+        const double* b[2] = {v.d, v.x};
+        if ((rc = dots<double>(c, n, 2, a, b, d2))) return rc;
+        if (d2[1] <= 0.0) break;
+        lam = std::sqrt(d2[0] / d2[1]);
+        vk_copy<double>(s, n, v.d, v.x);
+        vk_scale<double>(s, n, 1.0 / std::sqrt(d2[0]), v.x);
+    }
+    L.lmax64 = L.lmax32 = lam > 0.0 ? lam : 1.0;
+    return UWG_OK;
+}
+
+int uwg_solver_setup(uwg_ctx* c) {
+    int rc = work_init(c, 30);
+    if (rc) return rc;
+    for (int l = 0; l < c->nlev; l++) {
+        if (l > 0 && (rc = uwg_ops_coarsen(c, l - 1))) return rc;
+        if ((rc = uwg_ops_level_setup(c, l))) return rc;
+        if (l < c->nlev - 1 && (rc = uwg_solver_estimate(c, l))) return rc;
+    }
+    return uwg_ops_dense_coarse(c, c->nlev - 1);
+}
+
+extern "C" void uwg_solve_opts_default(uwg_solve_opts* o) {
+    if (!o) return;
+    o->mixed = 0;
+    o->rtol = 1e-8;
+    o->inner_rtol = 1e-10;
+    o->outer_rtol = 1e-9;
+    o->max_inner = 500;
+    o->max_outer = 500;
+    o->mg_levels = 0;
+    o->smooth_steps = 3;
+    o->restart = 30;
+    o->zero_guess = 1;
+}
+
+namespace {
+
+// q = (C - G^T A^-1 G) p  (one inner velocity solve)
+int schur_apply(uwg_ctx* c, const SolveCfg& cfg, const double* p, double* q, int* its, int* refine) {
+    Work* w = work_of(c);
+    int rc;
+    if ((rc = uwg_ops_applyG(c, p, w->u_tmp))) return rc;
+    int it = 0;
+    rc = velocity_solve(c, cfg, w->u_tmp, w->u_tmp2, true, &it, refine);
+    *its += it;
+    if (rc) return rc;
+    if ((rc = uwg_ops_applyGt(c, w->u_tmp2, q))) return rc;
+    if ((rc = uwg_ops_apply_C(c, p, w->p_tmp2))) return rc;
+    vk_axpby<double>(c->stream, c->n_pdof, 1.0, w->p_tmp2, -1.0, q);
+    return UWG_OK;
+}
+
+// Right-preconditioned flexible GMRES on the Schur complement, M^-1 = -S^^-1.
+int fgmres(uwg_ctx* c, const SolveCfg& cfg, const double* rhs, double* p, double rtol, int maxit, int m,
+           int* its, int* inner_its, int* refine) {
+    Work* w = work_of(c);
+    cudaStream_t s = c->stream;
+    int64_t n = c->n_pdof;
+    int rc;
+    double bn;
+    const double* ab[1] = {rhs};
+    if ((rc = dots<double>(c, n, 1, ab, ab, &bn))) return rc;
+    bn = std::sqrt(bn);
+    *its = 0;
+    vk_zero<double>(s, n, p);
+    if (bn == 0.0) return UWG_OK;
+    std::vector<double> H((m + 1) * m), cs(m), sn(m), g(m + 1), y(m);
+    int total = 0;
+    // r0 = rhs (p = 0)
+    vk_copy<double>(s, n, rhs, w->V[0]);
+    double beta = bn;
+    while (true) {
+        vk_scale<double>(s, n, 1.0 / beta, w->V[0]);
+        std::fill(g.begin(), g.end(), 0.0);
+        g[0] = beta;
+        int j = 0;
+        bool done = false;
+        for (; j < m && total < maxit; j++) {
+            // Z_j = -S^^-1 V_j
+            if ((rc = uwg_ops_schur_pc(c, w->V[j], w->Z[j]))) return rc;
+            vk_scale<double>(s, n, -1.0, w->Z[j]);
+            if ((rc = schur_apply(c, cfg, w->Z[j], w->V[j + 1], inner_its, refine))) return rc;
+            total++;
+            // classical Gram-Schmidt, two passes
+            std::vector<double> hcol(j + 1, 0.0);
+            for (int pass = 0; pass < 2; pass++) {
+                vk_mdot(s, n, j + 1, (const double* const*)w->V.data(), w->V[j + 1], w->coef);
+                std::vector<double> hh(j + 1);
+                UWG_CUDA(c, cudaMemcpyAsync(hh.data(), w->coef, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, s));
+                UWG_CUDA(c, cudaStreamSynchronize(s));
+                for (int i = 0; i <= j; i++) { hcol[i] += hh[i]; hh[i] = -hh[i]; }
+                UWG_CUDA(c, cudaMemcpyAsync(w->coef + 128, hh.data(), sizeof(double) * (j + 1), cudaMemcpyHostToDevice, s));
+                vk_maxpy(s, n, j + 1, w->coef + 128, (const double* const*)w->V.data(), w->V[j + 1]);
+            }
+            double hn;
+            const double* av[1] = {w->V[j + 1]};
+            if ((rc = dots<double>(c, n, 1, av, av, &hn))) return rc;
+            hn = std::sqrt(hn);
+            if (!std::isfinite(hn)) return uwg_set_error(c, UWG_ERR_NAN, "non-finite value in the pressure solve");
+            for (int i = 0; i <= j; i++) H[i * m + j] = hcol[i];
+            H[(j + 1) * m + j] = hn;
+            // apply previous rotations
+            for (int i = 0; i < j; i++) {
+                double t = cs[i] * H[i * m + j] + sn[i] * H[(i + 1) * m + j];
+                H[(i + 1) * m + j] = -sn[i] * H[i * m + j] + cs[i] * H[(i + 1) * m + j];
+                H[i * m + j] = t;
+            }
+            double a = H[j * m + j], b = H[(j + 1) * m + j];
+            double r = std::hypot(a, b);
+            cs[j] = r == 0.0 ? 1.0 : a / r;
+            sn[j] = r == 0.0 ? 0.0 : b / r;
+            H[j * m + j] = r;
+            H[(j + 1) * m + j] = 0.0;
+            g[j + 1] = -sn[j] * g[j];
+            g[j] = cs[j] * g[j];
+            if (hn > 0.0) vk_scale<double>(s, n, 1.0 / hn, w->V[j + 1]);
+            if (std::fabs(g[j + 1]) <= rtol * bn || hn == 0.0) { j++; done = true; break; }
+        }
+        // y = H^-1 g, p += Z y
+        for (int i = j - 1; i >= 0; i--) {
+            double t = g[i];
+            for (int k = i + 1; k < j; k++) t -= H[i * m + k] * y[k];
+            y[i] = t / H[i * m + i];
+        }
+        UWG_CUDA(c, cudaMemcpyAsync(w->coef, y.data(), sizeof(double) * j, cudaMemcpyHostToDevice, s));
+        vk_maxpy(s, n, j, w->coef, (const double* const*)w->Z.data(), p);
+        *its = total;
+        if (done) return UWG_OK;
+        if (total >= maxit) return uwg_set_error(c, UWG_ERR_NOT_CONVERGED, "pressure solve reached its iteration cap");
+        // restart: r = rhs - S p
+        if ((rc = schur_apply(c, cfg, p, w->p_tmp, inner_its, refine))) return rc;
+        vk_copy<double>(s, n, rhs, w->V[0]);
+        vk_axpy<double>(s, n, -1.0, w->p_tmp, w->V[0]);
+        const double* a0[1] = {w->V[0]};
+        if ((rc = dots<double>(c, n, 1, a0, a0, &beta))) return rc;
+        beta = std::sqrt(beta);
+        if (beta <= rtol * bn) return UWG_OK;
+    }
+}
+
+}  // namespace
+
+// ||f - Ku - Gp|| and ||h - G^T u - C p|| over free dofs, plus ||f||, ||h||.
+int uwg_solver_residuals(uwg_ctx* c, const double* u, const double* p, double* out4) {
+    int rc = work_init(c, 30);
+    if (rc) return rc;
+    Work* w = work_of(c);
+    cudaStream_t s = c->stream;
+    int64_t nv = c->n_vdof, np = c->n_pdof;
+    // momentum: r = f - K u - G p on free dofs (operator includes identity BC rows; mask them)
+    if ((rc = uwg_ops_applyK<double>(c, 0, u, w->u_tmp))) return rc;
+    if ((rc = uwg_ops_applyG(c, p, w->u_tmp2))) return rc;
+    vk_copy<double>(s, nv, c->f, w->ref_r);
+    vk_axpy<double>(s, nv, -1.0, w->u_tmp, w->ref_r);
+    vk_axpy<double>(s, nv, -1.0, w->u_tmp2, w->ref_r);
+    vk_mask<double>(s, nv, c->bc, w->ref_r);
+    vk_copy<double>(s, nv, c->f, w->ref_d);
+    vk_mask<double>(s, nv, c->bc, w->ref_d);
+    // continuity: q = h - G^T u - C p
+    if ((rc = uwg_ops_applyGt(c, u, w->p_tmp))) return rc;
+    if ((rc = uwg_ops_apply_C(c, p, w->p_tmp2))) return rc;
+    vk_axpby<double>(s, np, 1.0, c->h, -1.0, w->p_tmp);
+    vk_axpy<double>(s, np, -1.0, w->p_tmp2, w->p_tmp);
+    double d[4];
+    const double* a2[2] = {w->ref_r, w->ref_d};
+    if ((rc = dots<double>(c, nv, 2, a2, a2, d))) return rc;
+    const double* a3[2] = {w->p_tmp, c->h};
+    if ((rc = dots<double>(c, np, 2, a3, a3, d + 2))) return rc;
+    out4[0] = std::sqrt(d[0]);
+    out4[1] = std::sqrt(d[2]);
+    out4[2] = std::sqrt(d[1]);
+    out4[3] = std::sqrt(d[3]);
+    return UWG_OK;
+}
+
+extern "C" int uwg_stokes_solve(uwg_ctx* c, const uwg_solve_opts* o, double* u, double* p, uwg_solve_stats* st) {
+    if (!c || !u || !p) return uwg_set_error(c, UWG_ERR_ARG, "uwg_stokes_solve: bad argument");
+    if (!c->assembled) return uwg_set_error(c, UWG_ERR_STATE, "uwg_stokes_solve before uwg_assemble");
+    uwg_solve_opts def;
+    uwg_solve_opts_default(&def);
+    if (!o) o = &def;
+    uwg_solve_stats S;
+    memset(&S, 0, sizeof(S));
+    double t0 = now();
+    if (o->restart < 2 || o->restart > 60) return uwg_set_error(c, UWG_ERR_ARG, "restart must be in [2, 60]");
+    int rc = work_init(c, o->restart);
+    if (rc) return rc;
+    Work* w = work_of(c);
+    cudaStream_t s = c->stream;
+    int64_t nv = c->n_vdof, np = c->n_pdof;
+    SolveCfg cfg{o->mixed != 0, o->inner_rtol, o->max_inner, std::max(1, o->smooth_steps)};
+    // b = f with Dirichlet values in BC rows
+    vk_copy<double>(s, nv, c->f, w->bvec);
+    {
+        // bvec[bc] = bcval[bc]
+        vk_mask<double>(s, nv, c->bc, w->bvec);
+        // add values: bvec += bcval (bcval is zero on free dofs)
+        vk_axpy<double>(s, nv, 1.0, c->bcval, w->bvec);
+    }
+    double t1 = now();
+    S.setup_time = t1 - t0;
+    // 1. pre-solve
+    int it = 0;
+    rc = velocity_solve(c, cfg, w->bvec, w->ftil, true, &it, &S.refinement_steps);
+    S.velocity_presolve_its = it;
+    S.fhat_reason = rc ? -1 : 1;
+    if (rc) return rc;
+    // zero BC entries of f~ (the reduced system excludes them)
+    vk_mask<double>(s, nv, c->bc, w->ftil);
+    double t2 = now();
+    S.presolve_time = t2 - t1;
+    // 2. h^ = h - G^T f~
+    if ((rc = uwg_ops_applyGt(c, w->ftil, w->hhat))) return rc;
+    vk_axpby<double>(s, np, 1.0, c->h, -1.0, w->hhat);
+    // 3. pressure solve: S p = h^, S = C - G^T A^-1 G
+    int outer = 0, inner_its = 0;
+    rc = fgmres(c, cfg, w->hhat, p, o->outer_rtol, o->max_outer, std::max(2, o->restart), &outer, &inner_its,
+                &S.refinement_steps);
+    S.pressure_its = outer;
+    S.velocity_pressuresolve_its = inner_its;
+    S.outer_reason = rc ? -1 : 1;
+    if (rc) return rc;
+    double t3 = now();
+    S.pressure_time = t3 - t2;
+    // 4. back-solve: A u = b - G p
+    if ((rc = uwg_ops_applyG(c, p, w->u_tmp))) return rc;
+    vk_copy<double>(s, nv, w->bvec, w->cg_q);
+    vk_axpy<double>(s, nv, -1.0, w->u_tmp, w->cg_q);
+    vk_copy<double>(s, nv, w->cg_q, w->u_tmp2);
+    rc = velocity_solve(c, cfg, w->u_tmp2, u, o->zero_guess != 0, &it, &S.refinement_steps);
+    S.velocity_backsolve_its = it;
+    S.backsolve_reason = rc ? -1 : 1;
+    if (rc) return rc;
+    double t4 = now();
+    S.backsolve_time = t4 - t3;
+    S.velocity_total_its = S.velocity_presolve_its + S.velocity_pressuresolve_its + S.velocity_backsolve_its;
+    double r4[4];
+    if ((rc = uwg_solver_residuals(c, u, p, r4))) return rc;
+    double num = std::sqrt(r4[0] * r4[0] + r4[1] * r4[1]);
+    double den = std::sqrt(r4[2] * r4[2] + r4[3] * r4[3]);
+    S.residual = den > 0.0 ? num / den : num;
+    S.total_time = now() - t0;
+    if (st) *st = S;
+    return UWG_OK;
+}
+
+extern "C" int uwg_stokes_residuals(uwg_ctx* c, const double* u, const double* p, double* res_h) {
+    if (!c || !u || !p || !res_h) return uwg_set_error(c, UWG_ERR_ARG, "uwg_stokes_residuals: bad argument");
+    if (!c->assembled) return uwg_set_error(c, UWG_ERR_STATE, "residuals before uwg_assemble");
+    double r4[4];
+    int rc = uwg_solver_residuals(c, u, p, r4);
+    if (rc) return rc;
+    res_h[0] = r4[0];
+    res_h[1] = r4[1];
+    return UWG_OK;
+}
