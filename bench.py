@@ -1,0 +1,415 @@
+"""Benchmark of the PIC Stokes path: Stokes solve time to a 1e-8 relative
+residual and particles advected per second.
+
+Workload (default ``grf3d``): 3D unit cube, 128^3 Q1/dQ0 elements, free-slip
+walls, 20 particles per element (41,943,040 particles) from the seeded
+per-cell random layout.  T is a seeded Gaussian random field (correlation
+length 0.1, spectral synthesis on a 256^3 grid, Gaussian covariance),
+trilinearly sampled at the particles and scaled to [0, 1]; viscosity
+exp(-11.5 T) (contrast ~1e5), body force (0, 0, Ra T) with Ra = 1e6.
+``sinker2d`` is the 2D 64^2 sinker (circle r=0.1 at (0.5,0.6), viscosity 100,
+density 1, gravity (0,-1)) that the reference runs on a CPU.
+
+One step = the hot path over the swarm: coincident mapping + DVC weights,
+PIC assembly, BSSCR solve to 1e-8 (FP32 inner solves in FP64 refinement; the
+plain FP64 solve is timed beside it), RK2 advection at the maximum stable dt,
+owner update.  ``value`` = seconds per Stokes solve (mapping + weights +
+assembly + solve) with inputs resident on the device; ``e2e`` = the same
+measured through host buffers (particle coordinates, viscosity and body
+force copied in, velocity and pressure copied out, every step).
+
+``--impl reference`` times the CPU oracle (the reference's algorithms
+restated in C, OpenMP on all host cores) on a bounded sample of the same
+workload, extrapolated to the full size and labelled as such.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIGS = {
+    "grf3d": dict(dim=3, res=(128, 128, 128), ppc=20, kind="grf"),
+    "grf3d_small": dict(dim=3, res=(32, 32, 32), ppc=20, kind="grf"),
+    "sinker2d": dict(dim=2, res=(64, 64), ppc=20, kind="sinker"),
+}
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {"hbm_gbs": 6800.0, "_fallback": True}
+
+
+# ---------------------------------------------------------------------------
+# synthetic inputs
+# ---------------------------------------------------------------------------
+def grf_T(x, seed=1234, n=256, corr=0.1):
+    """Seeded Gaussian random field (Gaussian covariance, length corr) on an
+    n^3 periodic grid over the unit cube, trilinearly sampled at x, min-max
+    scaled to [0, 1].  Input generation only (torch)."""
+    import torch
+    g = torch.Generator(device=x.device).manual_seed(seed)
+    noise = torch.randn((n, n, n), generator=g, device=x.device, dtype=torch.float32)
+    k = torch.fft.fftfreq(n, d=1.0 / n, device=x.device).float() * 2 * torch.pi
+    k2 = k[:, None, None] ** 2 + k[None, :, None] ** 2 + k[None, None, :] ** 2
+    amp = torch.exp(-k2 * corr * corr / 4.0)          # sqrt of the Gaussian spectrum
+    f = torch.fft.ifftn(torch.fft.fftn(noise) * amp).real
+    f = (f - f.min()) / (f.max() - f.min())
+    # trilinear sample (grid point i at i/(n-1))
+    u = x.float() * (n - 1)
+    i0 = u.floor().clamp(0, n - 2).long()
+    t = (u - i0.float()).clamp(0, 1)
+    out = torch.zeros(x.shape[0], device=x.device, dtype=torch.float32)
+    for c in range(8):
+        a, b, cc = c & 1, (c >> 1) & 1, (c >> 2) & 1
+        w = ((t[:, 0] if a else 1 - t[:, 0]) * (t[:, 1] if b else 1 - t[:, 1]) * (t[:, 2] if cc else 1 - t[:, 2]))
+        out += w * f[i0[:, 2] + cc, i0[:, 1] + b, i0[:, 0] + a]
+    T = out.double()
+    return (T - T.min()) / (T.max() - T.min())
+
+
+def material(cfg, x):
+    import torch
+    dim = cfg["dim"]
+    if cfg["kind"] == "grf":
+        T = grf_T(x)
+        eta = torch.exp(-11.5 * T)
+        body = torch.zeros_like(x)
+        body[:, 2] = 1e6 * T
+        return eta.contiguous(), body.contiguous()
+    inside = ((x - torch.tensor([0.5, 0.6], device=x.device, dtype=x.dtype)) ** 2).sum(1) < 0.01
+    eta = torch.where(inside, 100.0, 1.0).double()
+    body = torch.zeros_like(x)
+    body[:, 1] = torch.where(inside, -1.0, 0.0)
+    return eta.contiguous(), body.contiguous()
+
+
+def freeslip_mask(ctx):
+    import numpy as np
+    import torch
+    dim = ctx.dim
+    n = [r + 1 for r in ctx.res]
+    idx = np.arange(int(np.prod(n)))
+    ijk = [idx % n[0], (idx // n[0]) % n[1]] + ([idx // (n[0] * n[1])] if dim == 3 else [])
+    m = np.zeros((len(idx), dim), np.uint8)
+    for d in range(dim):
+        m[:, d] = (ijk[d] == 0) | (ijk[d] == n[d] - 1)
+    return torch.from_numpy(m.ravel())
+
+
+# ---------------------------------------------------------------------------
+# clocks sampler
+# ---------------------------------------------------------------------------
+class Clocks:
+    def __init__(self):
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def start(self):
+        def run():
+            q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+            while not self._stop.is_set():
+                try:
+                    out = subprocess.run(["nvidia-smi", "--query-gpu=" + q, "--format=csv,noheader,nounits", "-i", "0"],
+                                         capture_output=True, text=True, timeout=5).stdout.strip()
+                    self.samples.append([s.strip() for s in out.split(",")])
+                except Exception:
+                    pass
+                self._stop.wait(0.2)
+        self._t = threading.Thread(target=run, daemon=True)
+        self._t.start()
+
+    def stop(self):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+        mhz = sorted(float(s[0]) for s in self.samples if s and s[0].replace(".", "").isdigit())
+        mx = next((float(s[1]) for s in self.samples if len(s) > 1 and s[1].replace(".", "").isdigit()), None)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 2 + i and s[2 + i].lower() == "active"})
+        return {"sm_mhz": mhz[len(mhz) // 2] if mhz else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_gpu(args):
+    import numpy as np
+    import torch
+    from underworld2_gb300._core import Context, rng_seed
+
+    cfg = CONFIGS[args.config]
+    dim = cfg["dim"]
+    ctx = Context(dim, cfg["res"], (0.0,) * dim, (1.0,) * dim)
+    ctx.set_bcs(freeslip_mask(ctx))
+    x0, owner0, off0, lst0, _ = ctx.layout_random(cfg["ppc"], rng_seed(13))
+    eta0, body0 = material(cfg, x0)
+    npart = x0.shape[0]
+    u = ctx.zeros(ctx.n_vdof)
+    p = ctx.zeros(ctx.n_pdof)
+    opts = dict(rtol=1e-8, inner_rtol=args.inner_rtol, outer_rtol=args.outer_rtol, smooth_steps=3, restart=30)
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+
+    def solve_step(x, off, lst, eta, body, mixed, times):
+        e = [ev() for _ in range(4)]
+        e[0].record()
+        ip_xi = ctx.pic_map(x, off, lst)
+        ip_w = ctx.dvc_weights(off, ip_xi)
+        e[1].record()
+        ctx.assemble(off, lst, ip_xi, ip_w, eta, body)
+        e[2].record()
+        u.zero_()
+        p.zero_()
+        st = ctx.solve(u, p, mixed=mixed, **opts)
+        e[3].record()
+        torch.cuda.synchronize()
+        times["map_dvc"].append(e[0].elapsed_time(e[1]) / 1e3)
+        times["assemble"].append(e[1].elapsed_time(e[2]) / 1e3)
+        times["solve"].append(e[2].elapsed_time(e[3]) / 1e3)
+        return st
+
+    def advect_step(x, owner, off, lst, times):
+        e = [ev() for _ in range(3)]
+        e[0].record()
+        dt = ctx.max_dt(u)
+        ctx.rk2(x, u, dt)
+        e[1].record()
+        ctx.update_owners(x, owner, off, lst)
+        e[2].record()
+        torch.cuda.synchronize()
+        times["rk2"].append(e[0].elapsed_time(e[1]) / 1e3)
+        times["migrate"].append(e[1].elapsed_time(e[2]) / 1e3)
+
+    mixed = 0 if args.mode == "fp64" else 1
+    # state copies so every step starts from the same swarm
+    x, owner, off, lst = x0.clone(), owner0.clone(), off0.clone(), lst0.clone()
+    warm = {k: [] for k in ("map_dvc", "assemble", "solve", "rk2", "migrate")}
+    for _ in range(args.warmup):
+        x.copy_(x0); owner.copy_(owner0); off.copy_(off0); lst.copy_(lst0)
+        solve_step(x, off, lst, eta0, body0, mixed, warm)
+        advect_step(x, owner, off, lst, warm)
+
+    clocks = Clocks()
+    clocks.start()
+    times = {k: [] for k in ("map_dvc", "assemble", "solve", "rk2", "migrate")}
+    stats = []
+    torch.cuda.synchronize()
+    for _ in range(args.steps):
+        x.copy_(x0); owner.copy_(owner0); off.copy_(off0); lst.copy_(lst0)
+        torch.cuda.synchronize()
+        stats.append(solve_step(x, off, lst, eta0, body0, mixed, times))
+        advect_step(x, owner, off, lst, times)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+
+    # plain FP64 solve on the same assembled system (one timed run)
+    fp64 = None
+    if not args.skip_fp64 and mixed:
+        x.copy_(x0); owner.copy_(owner0); off.copy_(off0); lst.copy_(lst0)
+        t64 = {k: [] for k in ("map_dvc", "assemble", "solve")}
+        st64 = solve_step(x, off, lst, eta0, body0, 0, t64)
+        fp64 = {"solve_s": t64["solve"][0], "pressure_its": st64["pressure_its"],
+                "velocity_total_its": st64["velocity_total_its"], "residual": st64["residual"]}
+
+    # end to end through host buffers
+    x_h = x0.cpu().pin_memory()
+    eta_h = eta0.cpu().pin_memory()
+    body_h = body0.cpu().pin_memory()
+    u_h = torch.empty(ctx.n_vdof, dtype=torch.float64).pin_memory()
+    p_h = torch.empty(ctx.n_pdof, dtype=torch.float64).pin_memory()
+    e2e_t = []
+    for it in range(max(1, min(args.steps, 3))):
+        owner.copy_(owner0); off.copy_(off0); lst.copy_(lst0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        x.copy_(x_h, non_blocking=True)
+        eta = eta_h.to(ctx.device, non_blocking=True)
+        body = body_h.to(ctx.device, non_blocking=True)
+        tt = {k: [] for k in ("map_dvc", "assemble", "solve")}
+        solve_step(x, off, lst, eta, body, mixed, tt)
+        u_h.copy_(u, non_blocking=True)
+        p_h.copy_(p, non_blocking=True)
+        torch.cuda.synchronize()
+        e2e_t.append(time.perf_counter() - t0)
+    h2d = x_h.numel() * 8 + eta_h.numel() * 8 + body_h.numel() * 8
+    d2h = u_h.numel() * 8 + p_h.numel() * 8
+
+    # roofline of the dominant kernel class: the matrix-free K apply (FP32)
+    kinfo = time_kernel_apply(ctx)
+    pk = peaks()
+    achieved = kinfo["bytes"] / kinfo["seconds"] / 1e9
+    per_step = [times["map_dvc"][i] + times["assemble"][i] + times["solve"][i] for i in range(args.steps)]
+    solve_s = float(np.mean(per_step))
+    adv_s = float(np.mean([times["rk2"][i] + times["migrate"][i] for i in range(args.steps)]))
+    line = {
+        "metric": "Stokes solve time @1e-8 resid (learned+FP32 vs FP64 GPU); particles/s advected",
+        "value": solve_s,
+        "unit": "s/solve",
+        "n_gpus": 1,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * (solve_s + adv_s),
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64" if not mixed else "f32+f64",
+        "data": "synthetic",
+        "config": {"workload": workload_name(args.config), "mesh": "x".join(map(str, cfg["res"])) + " Q1/dQ0",
+                   "particles": npart, "particles_per_cell": cfg["ppc"], "solve_mode": args.mode,
+                   "inputs_vs_L2": "particle arrays (%.1f GB) exceed the 129 MB L2" % (npart * 8 * (2 * dim + 1) / 1e9)},
+        "particles_per_s": npart / adv_s,
+        "phases_s": {k: float(np.mean(v)) for k, v in times.items()},
+        "solver": {"pressure_its": stats[-1]["pressure_its"], "velocity_total_its": stats[-1]["velocity_total_its"],
+                   "refinement_steps": stats[-1]["refinement_steps"], "residual": stats[-1]["residual"]},
+        "fp64_solve": fp64,
+        "e2e": {"value": float(np.mean(e2e_t)), "unit": "s/solve", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "roofline": {"bound": "hbm", "kernel": kinfo["name"], "achieved": achieved, "peak": pk.get("hbm_gbs"),
+                     "unit": "GB/s", "frac": achieved / pk.get("hbm_gbs", 6800.0),
+                     "peak_source": "fallback" if pk.get("_fallback") else "measured",
+                     "traffic": None, "bytes_per_launch": kinfo["bytes"], "launch_s": kinfo["seconds"]},
+        "clocks": clk,
+    }
+    if args.count_launches:
+        line["gpu_launches"] = count_launches(ctx, x0, owner0, off0, lst0, eta0, body0, mixed, opts, u, p) * args.steps
+    if args.cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args, quick=True)
+    return line
+
+
+def workload_name(key):
+    return {"grf3d": "3D 128^3 Q1/dQ0 GRF viscosity exp(-11.5T), Ra=1e6, 20 ppc, free-slip (config 3)",
+            "grf3d_small": "3D 32^3 Q1/dQ0 GRF viscosity, 20 ppc, free-slip",
+            "sinker2d": "2D 64^2 Q1/dQ0 sinker, 20 ppc, free-slip (config 1)"}[key]
+
+
+def time_kernel_apply(ctx, reps=20):
+    """CUDA-event time of the FP32 matrix-free K apply on the finest level.
+    Algorithmic bytes per apply: 4*(2*N_v) + 4*27*N_el (x read, y written,
+    equivalent-quadrature weights read)."""
+    import torch
+    x = torch.randn(ctx.n_vdof, dtype=torch.float32, device=ctx.device)
+    y = torch.empty_like(x)
+    for _ in range(3):
+        ctx._call("uwg_apply_K32", 0, __import__("ctypes").c_void_p(x.data_ptr()), __import__("ctypes").c_void_p(y.data_ptr()))
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(reps):
+        ctx._call("uwg_apply_K32", 0, __import__("ctypes").c_void_p(x.data_ptr()), __import__("ctypes").c_void_p(y.data_ptr()))
+    e.record()
+    torch.cuda.synchronize()
+    sec = s.elapsed_time(e) / 1e3 / reps
+    nq = 27 if ctx.dim == 3 else 9
+    byts = 4 * 2 * ctx.n_vdof + 4 * nq * ctx.n_el
+    return {"name": "k_applyK_q1_%dd<float> (+ BC copy)" % ctx.dim, "seconds": sec, "bytes": byts}
+
+
+def count_launches(ctx, x0, owner0, off0, lst0, eta0, body0, mixed, opts, u, p):
+    """Kernels launched by libuwg in one step, counted with the CUDA activity profiler."""
+    import torch
+    from torch.profiler import ProfilerActivity, profile
+    x, owner, off, lst = x0.clone(), owner0.clone(), off0.clone(), lst0.clone()
+    with profile(activities=[ProfilerActivity.CUDA]) as prof:
+        ip_xi = ctx.pic_map(x, off, lst)
+        ip_w = ctx.dvc_weights(off, ip_xi)
+        ctx.assemble(off, lst, ip_xi, ip_w, eta0, body0)
+        u.zero_(); p.zero_()
+        ctx.solve(u, p, mixed=mixed, **opts)
+        dt = ctx.max_dt(u)
+        ctx.rk2(x, u, dt)
+        ctx.update_owners(x, owner, off, lst)
+        torch.cuda.synchronize()
+    n = 0
+    for evt in prof.events():
+        name = evt.name or ""
+        if evt.device_type.name == "CUDA" and (name.startswith("k_") or name.startswith("vk_") or "uwg" in name
+                                                or name.startswith("void k_") or name.startswith("void vk_")):
+            n += 1
+    return n
+
+
+# ---------------------------------------------------------------------------
+# CPU arm: the oracle (reference algorithms restated in C) on host cores
+# ---------------------------------------------------------------------------
+def cpu_baseline(args, quick=False):
+    from oracle import cpu_reference
+    return cpu_reference.measure(CONFIGS[args.config], workload_name(args.config), quick=quick)
+
+
+def run_reference(args):
+    res = cpu_baseline(args)
+    line = {
+        "impl": "reference",
+        "metric": "Stokes solve time @1e-8 resid (learned+FP32 vs FP64 GPU); particles/s advected",
+        "value": res["value"],
+        "unit": "s/solve",
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": workload_name(args.config)},
+        "particles_per_s": res.get("particles_per_s"),
+        "cpu_baseline": res,
+        "e2e": {"value": res["value"], "unit": "s/solve", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    return line
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="grf3d", choices=sorted(CONFIGS))
+    ap.add_argument("--mode", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--inner-rtol", type=float, default=1e-10)
+    ap.add_argument("--outer-rtol", type=float, default=1e-9)
+    ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-count-launches", dest="count_launches", action="store_false")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        print(json.dumps(run_reference(args)))
+        return
+    if world > 1:
+        # replicas only: every rank runs the same single-GPU workload on its own device
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+        dist.barrier()
+        line = run_gpu(args)
+        t = torch.tensor([line["value"]], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        line["value"] = float(t.item())
+        line["n_gpus"] = world
+        if rank == 0:
+            print(json.dumps(line))
+        dist.destroy_process_group()
+        return
+    print(json.dumps(run_gpu(args)))
+
+
+if __name__ == "__main__":
+    main()

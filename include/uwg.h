@@ -143,6 +143,8 @@ typedef struct {
     int smooth_steps;      /* Chebyshev degree per smoothing */
     int restart;           /* FGMRES restart length */
     int zero_guess;        /* 1: start from u=p=0, else from the given u, p */
+    int schur_pc;          /* 0: assembled Uzawa term S^ (the reference's "uw"), 1: scaled BFBt */
+    double schur_pc_rtol;  /* relative tolerance of the pressure-Laplacian solves inside BFBt */
 } uwg_solve_opts;
 
 typedef struct {

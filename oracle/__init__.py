@@ -23,13 +23,13 @@ _lib = None
 
 def build(force=False):
     """Compile the oracle (seconds).  Rebuilds when the source is newer."""
-    src = os.path.join(_HERE, "uwo.c")
+    srcs = [os.path.join(_HERE, f) for f in ("uwo.c", "uwo_solve.c")]
     os.makedirs(_BUILD, exist_ok=True)
-    if not force and os.path.exists(_SO) and os.path.getmtime(_SO) >= os.path.getmtime(src):
+    if not force and os.path.exists(_SO) and all(os.path.getmtime(_SO) >= os.path.getmtime(s) for s in srcs):
         return _SO
     tmp = _SO + ".tmp%d" % os.getpid()
     cmd = ["gcc", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-std=c11",
-           "-o", tmp, src, "-lm"]
+           "-o", tmp] + srcs + ["-lm"]
     subprocess.check_call(cmd)
     os.replace(tmp, _SO)
     return _SO
@@ -70,6 +70,14 @@ def lib():
             "uwo_pressure_shape": (None, [ctypes.c_int, ctypes.c_int, _P, _P]),
             "uwo_interpolate": (ctypes.c_int, [M, _P, _P, _P, _P, _P, _P]),
             "uwo_rk2": (None, [M, _P, _P, _P, _P, ctypes.c_double, _I64, _I64, _P, _P]),
+            "uwo_sys_create": (_P, [ctypes.c_int, _P, _P, _P, _P]),
+            "uwo_sys_destroy": (None, [_P]),
+            "uwo_sys_set_bc": (None, [_P, _P, _P]),
+            "uwo_sys_assemble_points": (None, [_P, _P, _P, _P, _P, _P, _P]),
+            "uwo_sys_finish": (None, [_P]),
+            "uwo_sys_applyK": (None, [_P, ctypes.c_int, _P, _P]),
+            "uwo_sys_solve": (ctypes.c_int, [_P, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_int, _P, _P, _P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -250,3 +258,50 @@ def dvc_element(dim, res, xi):
     w = np.zeros(n)
     rounds = lib().uwo_dvc_element(dim, res, n, _p(xi), _p(cx), _p(w))
     return cx, w, rounds
+
+
+class StokesCPU:
+    """CPU assembly + BSSCR solve on a regular Q1/dQ0 mesh (uwo_solve.c)."""
+
+    def __init__(self, mesh):
+        self.mesh = mesh
+        L = mesh.L
+        res = np.array(list(mesh.res) + [1] * (3 - mesh.dim), np.int32)
+        self._res = res
+        self.h = L.uwo_sys_create(mesh.dim, _p(res), *mesh._ax())
+        self.nv = mesh.n_nodes * mesh.dim
+        self.np = mesh.n_el
+
+    def __del__(self):
+        try:
+            self.mesh.L.uwo_sys_destroy(self.h)
+        except Exception:
+            pass
+
+    def set_bc(self, mask, values=None):
+        mask = np.ascontiguousarray(mask, np.uint8)
+        values = None if values is None else np.ascontiguousarray(values, np.float64)
+        self.mesh.L.uwo_sys_set_bc(self.h, _p(mask), _p(values))
+
+    def assemble(self, off, lst, ip_xi, ip_w, eta, body):
+        a = [np.ascontiguousarray(off, np.int32), np.ascontiguousarray(lst, np.int32),
+             np.ascontiguousarray(ip_xi, np.float64), np.ascontiguousarray(ip_w, np.float64),
+             np.ascontiguousarray(eta, np.float64), np.ascontiguousarray(body, np.float64)]
+        self.mesh.L.uwo_sys_assemble_points(self.h, *[_p(x) for x in a])
+        self.mesh.L.uwo_sys_finish(self.h)
+
+    def applyK(self, x, level=0):
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros_like(x)
+        self.mesh.L.uwo_sys_applyK(self.h, level, _p(x), _p(y))
+        return y
+
+    def solve(self, inner_rtol=1e-10, outer_rtol=1e-9, max_inner=500, max_outer=500, deg=3):
+        u = np.zeros(self.nv)
+        p = np.zeros(self.np)
+        st = np.zeros(8)
+        rc = self.mesh.L.uwo_sys_solve(self.h, inner_rtol, outer_rtol, max_inner, max_outer, deg,
+                                       _p(u), _p(p), _p(st))
+        return u, p, {"rc": rc, "pressure_its": int(st[0]), "velocity_presolve_its": int(st[1]),
+                      "velocity_pressuresolve_its": int(st[2]), "velocity_backsolve_its": int(st[3]),
+                      "residual": float(st[4])}

@@ -204,3 +204,33 @@ def test_golden_known_answers(gpu):
     c = Context(2, (16, 16), (0.0, 0.0), (1.0, 1.0))
     own = c.locate(torch.tensor([g["owner_16x16"]["point"]], dtype=torch.float64, device="cuda"))
     assert int(own.cpu()[0]) == g["owner_16x16"]["cell"]
+
+
+def test_dvc_exact_ties_follow_particle_order(gpu):
+    """Exact distance ties go to the first claimer: GPU matches the oracle for
+    both particle orders (8x8 grid with binary-exact cell centres)."""
+    c = _ctx(2, (1, 1))
+    off = torch.tensor([0, 2], dtype=torch.int32, device="cuda")
+    for p in (np.array([[-0.375, 0.0625], [0.625, 0.0625]]), np.array([[0.625, 0.0625], [-0.375, 0.0625]])):
+        xi = torch.tensor(p, dtype=torch.float64, device="cuda")
+        w = c.dvc_weights(off, xi, res=8)
+        cx, wo, _ = oracle.dvc_element(2, 8, p)
+        np.testing.assert_array_equal(w.cpu().numpy(), wo)
+        np.testing.assert_array_equal(xi.cpu().numpy(), cx)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_dvc_random_many_particles(gpu, dim):
+    """Crowded elements (up to 100 particles) and a 16^d grid, bit-exact."""
+    rng = np.random.default_rng(11)
+    counts = [1, 2, 7, 33, 64, 100]
+    pts = [rng.uniform(-1, 1, (n, dim)) for n in counts]
+    c = _ctx(dim, (len(counts),) + (1,) * (dim - 1))
+    off = torch.tensor(np.concatenate([[0], np.cumsum(counts)]), dtype=torch.int32, device="cuda")
+    xi = torch.tensor(np.concatenate(pts), dtype=torch.float64, device="cuda")
+    w = c.dvc_weights(off, xi, res=16 if dim == 2 else 12)
+    for k, p in enumerate(pts):
+        cx, wo, _ = oracle.dvc_element(dim, 16 if dim == 2 else 12, p)
+        s = slice(int(off[k]), int(off[k + 1]))
+        np.testing.assert_array_equal(w.cpu().numpy()[s], wo)
+        np.testing.assert_array_equal(xi.cpu().numpy()[s], cx)

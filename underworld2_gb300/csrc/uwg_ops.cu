@@ -467,6 +467,114 @@ __global__ void k_applyGt(uwg_lgeom g, const uint8_t* bc, int only_bc, const dou
     q[e] = s;
 }
 
+// Pressure Laplacian of the scaled BFBt Schur preconditioner on level l:
+// L p = G^T diag(K)^-1 G p (Dirichlet dofs excluded).
+template <int DIM>
+__global__ void k_applyGt_scaled(uwg_lgeom g, const uint8_t* bc, const double* diag, const double* u, double* q) {
+    constexpr int NEN = DIM == 3 ? 8 : 4;
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= g.n_el) return;
+    int64_t nodes[8];
+    double h[3];
+    q1_elem(g, e, nodes, h);
+    double s = 0.0;
+    for (int n = 0; n < NEN; n++)
+        for (int i = 0; i < DIM; i++) {
+            int64_t dof = nodes[n] * DIM + i;
+            if (bc[dof]) continue;
+            double ge = 1.0;
+            for (int d = 0; d < DIM; d++)
+                if (d != i) ge *= 0.5 * h[d];
+            ge *= ((n >> i) & 1) ? -1.0 : 1.0;
+            s += ge * (u[dof] / diag[dof]);
+        }
+    q[e] = s;
+}
+
+template <int DIM>
+__global__ void k_Ldiag(uwg_lgeom g, const uint8_t* bc, const double* diag, double* out) {
+    constexpr int NEN = DIM == 3 ? 8 : 4;
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= g.n_el) return;
+    int64_t nodes[8];
+    double h[3];
+    q1_elem(g, e, nodes, h);
+    double s = 0.0;
+    for (int n = 0; n < NEN; n++)
+        for (int i = 0; i < DIM; i++) {
+            int64_t dof = nodes[n] * DIM + i;
+            if (bc[dof]) continue;
+            double ge = 1.0;
+            for (int d = 0; d < DIM; d++)
+                if (d != i) ge *= 0.5 * h[d];
+            s += ge * ge / diag[dof];
+        }
+    out[e] = s > 0.0 ? s : 1.0;
+}
+
+template <int DIM>
+__global__ void k_cell_restrict(uwg_lgeom gf, uwg_lgeom gc, const double* rf, double* rc) {
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= gc.n_el) return;
+    int ex = (int)(e % gc.res[0]), ey = (int)((e / gc.res[0]) % gc.res[1]);
+    int ez = DIM == 3 ? (int)(e / ((int64_t)gc.res[0] * gc.res[1])) : 0;
+    double s = 0.0;
+    for (int cz = 0; cz < (DIM == 3 ? 2 : 1); cz++)
+        for (int cy = 0; cy < 2; cy++)
+            for (int cx = 0; cx < 2; cx++)
+                s += rf[(2 * ex + cx) + (int64_t)gf.res[0] * ((2 * ey + cy) + (int64_t)gf.res[1] * (2 * ez + cz))];
+    rc[e] = s;
+}
+
+template <int DIM>
+__global__ void k_cell_prolong_add(uwg_lgeom gf, uwg_lgeom gc, const double* xc, double* xf) {
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= gf.n_el) return;
+    int ex = (int)(e % gf.res[0]), ey = (int)((e / gf.res[0]) % gf.res[1]);
+    int ez = DIM == 3 ? (int)(e / ((int64_t)gf.res[0] * gf.res[1])) : 0;
+    xf[e] += xc[(ex >> 1) + (int64_t)gc.res[0] * ((ey >> 1) + (int64_t)gc.res[1] * (ez >> 1))];
+}
+
+int uwg_ops_applyL(uwg_ctx* c, int l, const double* p, double* q, double* vtmp) {
+    const uwg_level& L = c->lev[l];
+    uwg_lgeom g = uwg_level_geom(c, l);
+    vk_zero<double>(c->stream, L.n_dof, vtmp);
+    if (c->dim == 3) {
+        k_applyG<3><<<nblk(L.n_el), 256, 0, c->stream>>>(g, L.bc, p, vtmp);
+        k_applyGt_scaled<3><<<nblk(L.n_el), 256, 0, c->stream>>>(g, L.bc, L.diag64, vtmp, q);
+    } else {
+        k_applyG<2><<<nblk(L.n_el), 256, 0, c->stream>>>(g, L.bc, p, vtmp);
+        k_applyGt_scaled<2><<<nblk(L.n_el), 256, 0, c->stream>>>(g, L.bc, L.diag64, vtmp, q);
+    }
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
+int uwg_ops_Ldiag(uwg_ctx* c, int l, double* out) {
+    const uwg_level& L = c->lev[l];
+    uwg_lgeom g = uwg_level_geom(c, l);
+    if (c->dim == 3) k_Ldiag<3><<<nblk(L.n_el), 256, 0, c->stream>>>(g, L.bc, L.diag64, out);
+    else k_Ldiag<2><<<nblk(L.n_el), 256, 0, c->stream>>>(g, L.bc, L.diag64, out);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
+int uwg_ops_cell_restrict(uwg_ctx* c, int lc, const double* rf, double* rc) {
+    uwg_lgeom gf = uwg_level_geom(c, lc - 1), gc = uwg_level_geom(c, lc);
+    if (c->dim == 3) k_cell_restrict<3><<<nblk(gc.n_el), 256, 0, c->stream>>>(gf, gc, rf, rc);
+    else k_cell_restrict<2><<<nblk(gc.n_el), 256, 0, c->stream>>>(gf, gc, rf, rc);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
+int uwg_ops_cell_prolong_add(uwg_ctx* c, int lc, const double* xc, double* xf) {
+    uwg_lgeom gf = uwg_level_geom(c, lc - 1), gc = uwg_level_geom(c, lc);
+    if (c->dim == 3) k_cell_prolong_add<3><<<nblk(gf.n_el), 256, 0, c->stream>>>(gf, gc, xc, xf);
+    else k_cell_prolong_add<2><<<nblk(gf.n_el), 256, 0, c->stream>>>(gf, gc, xc, xf);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
 int uwg_ops_applyG(uwg_ctx* c, const double* p, double* y) {
     uwg_lgeom g = uwg_level_geom(c, 0);
     vk_zero<double>(c->stream, c->n_vdof, y);

@@ -34,6 +34,10 @@ int uwg_solver_setup(uwg_ctx* c);
 void uwg_solver_free(uwg_ctx* c);
 int uwg_solver_residuals(uwg_ctx* c, const double* u, const double* p, double* out4);
 int uwg_ops_schur_pc(uwg_ctx* c, const double* r, double* z);    // z = Shat^-1 r
+int uwg_ops_applyL(uwg_ctx* c, int l, const double* p, double* q, double* vtmp);  // q = G^T D^-1 G p
+int uwg_ops_Ldiag(uwg_ctx* c, int l, double* out);
+int uwg_ops_cell_restrict(uwg_ctx* c, int lc, const double* rf, double* rc);
+int uwg_ops_cell_prolong_add(uwg_ctx* c, int lc, const double* xc, double* xf);
 int uwg_ops_apply_C(uwg_ctx* c, const double* p, double* q);     // q = Mp p (compressibility)
 int uwg_ops_element_matrices(uwg_ctx* c, int64_t el, double* Ke, double* fe, double* Ge, double* Se);
 

@@ -44,6 +44,13 @@ struct Work {
     double *p_tmp, *p_tmp2, *hhat;
     double* coef;                             // device coefficients
     int restart = 0;
+    // pressure multigrid (scaled BFBt)
+    LevelVecs<double> pv[UWG_MAXLEV];
+    double* pvel[UWG_MAXLEV];                 // velocity-sized temp per level
+    double* Ldiag[UWG_MAXLEV];
+    double Lmax[UWG_MAXLEV];
+    double *pcg_r, *pcg_z, *pcg_p, *pcg_q, *bf_y, *bf_m, *bf_v1, *bf_v2;
+    int lsolve_its = 0;
 };
 
 Work* work_of(uwg_ctx* c) {
@@ -78,6 +85,17 @@ int work_init(uwg_ctx* c, int restart) {
         w->ftil = dalloc<double>(c, nv); w->bvec = dalloc<double>(c, nv);
         w->p_tmp = dalloc<double>(c, np); w->p_tmp2 = dalloc<double>(c, np); w->hhat = dalloc<double>(c, np);
         w->coef = dalloc<double>(c, 256);
+        for (int l = 0; l < c->nlev; l++) {
+            int64_t ne = c->lev[l].n_el;
+            w->pv[l] = {dalloc<double>(c, ne), dalloc<double>(c, ne), dalloc<double>(c, ne), dalloc<double>(c, ne), dalloc<double>(c, ne)};
+            w->pvel[l] = dalloc<double>(c, c->lev[l].n_dof);
+            w->Ldiag[l] = dalloc<double>(c, ne);
+            w->Lmax[l] = 1.0;
+        }
+        w->pcg_r = dalloc<double>(c, np); w->pcg_z = dalloc<double>(c, np);
+        w->pcg_p = dalloc<double>(c, np); w->pcg_q = dalloc<double>(c, np);
+        w->bf_y = dalloc<double>(c, np); w->bf_m = dalloc<double>(c, np);
+        w->bf_v1 = dalloc<double>(c, nv); w->bf_v2 = dalloc<double>(c, nv);
     }
     while ((int)w->V.size() < restart + 1) w->V.push_back(dalloc<double>(c, np));
     while ((int)w->Z.size() < restart) w->Z.push_back(dalloc<double>(c, np));
@@ -222,7 +240,11 @@ struct SolveCfg {
     double inner_rtol;
     int max_inner;
     int deg;
+    int schur_pc;
+    double schur_pc_rtol;
 };
+
+int bfbt(uwg_ctx* c, const double* r, double* z, double rtol);
 
 // x = A^-1 b for the velocity operator A = PKP + (I-P), FP64 result.
 // x holds the initial guess unless x_zero.  Returns iterations through *its.
@@ -268,6 +290,147 @@ int velocity_solve(uwg_ctx* c, const SolveCfg& cfg, const double* b, double* x, 
     return uwg_set_error(c, UWG_ERR_NOT_CONVERGED, "velocity refinement did not converge");
 }
 
+
+// ---------------------------------------------------------------------------
+// Scaled BFBt Schur preconditioner (May & Moresi, PEPI 2008):
+//   S^-1 ~ L^-1 (G^T D^-1 K D^-1 G) L^-1,  L = G^T D^-1 G,  D = diag(K).
+// L is a cell-centred pressure Laplacian; its solves use CG preconditioned by a
+// cell multigrid V-cycle whose level operators are G_l^T D_l^-1 G_l with the
+// velocity hierarchy's diagonals (Chebyshev-Jacobi smoothing).
+// ---------------------------------------------------------------------------
+int cheb_L(uwg_ctx* c, int l, const double* b, double* x, int deg, bool x_zero) {
+    Work* w = work_of(c);
+    LevelVecs<double>& v = w->pv[l];
+    int64_t n = c->lev[l].n_el;
+    cudaStream_t s = c->stream;
+    double lmax = w->Lmax[l];
+    double alpha = 0.1 * lmax, beta = 1.1 * lmax;
+    double theta = 0.5 * (beta + alpha), delta = 0.5 * (beta - alpha);
+    double sigma = theta / delta, rho = 1.0 / sigma;
+    int rc;
+    if (x_zero) vk_copy<double>(s, n, b, v.r);
+    else {
+        if ((rc = uwg_ops_applyL(c, l, x, v.t, w->pvel[l]))) return rc;
+        vk_copy<double>(s, n, b, v.r);
+        vk_axpy<double>(s, n, -1.0, v.t, v.r);
+    }
+    vk_pointwise_div<double>(s, n, v.r, w->Ldiag[l], v.d);
+    vk_scale<double>(s, n, 1.0 / theta, v.d);
+    vk_axpy<double>(s, n, 1.0, v.d, x);
+    for (int i = 1; i < deg; i++) {
+        if ((rc = uwg_ops_applyL(c, l, x, v.t, w->pvel[l]))) return rc;
+        vk_copy<double>(s, n, b, v.r);
+        vk_axpy<double>(s, n, -1.0, v.t, v.r);
+        double rho1 = 1.0 / (2.0 * sigma - rho);
+        vk_pointwise_div<double>(s, n, v.r, w->Ldiag[l], v.t);
+        vk_axpby<double>(s, n, 2.0 * rho1 / delta, v.t, rho1 * rho, v.d);
+        vk_axpy<double>(s, n, 1.0, v.d, x);
+        rho = rho1;
+    }
+    return UWG_OK;
+}
+
+int pvcycle(uwg_ctx* c, int l, const double* b, double* x) {
+    Work* w = work_of(c);
+    cudaStream_t s = c->stream;
+    int64_t n = c->lev[l].n_el;
+    int rc;
+    vk_zero<double>(s, n, x);
+    if (l == c->nlev - 1) return cheb_L(c, l, b, x, 8, true);
+    LevelVecs<double>& v = w->pv[l];
+    LevelVecs<double>& vc = w->pv[l + 1];
+    if ((rc = cheb_L(c, l, b, x, 3, true))) return rc;
+    if ((rc = uwg_ops_applyL(c, l, x, v.t, w->pvel[l]))) return rc;
+    vk_axpby<double>(s, n, 1.0, b, -1.0, v.t);
+    if ((rc = uwg_ops_cell_restrict(c, l + 1, v.t, vc.b))) return rc;
+    if ((rc = pvcycle(c, l + 1, vc.b, vc.x))) return rc;
+    if ((rc = uwg_ops_cell_prolong_add(c, l + 1, vc.x, x))) return rc;
+    return cheb_L(c, l, b, x, 3, false);
+}
+
+// x = L^-1 b by multigrid-preconditioned CG from zero, to rtol
+int lsolve(uwg_ctx* c, const double* b, double* x, double rtol, int maxit) {
+    Work* w = work_of(c);
+    cudaStream_t s = c->stream;
+    int64_t n = c->n_pdof;
+    int rc;
+    double *r = w->pcg_r, *z = w->pcg_z, *p = w->pcg_p, *q = w->pcg_q;
+    vk_zero<double>(s, n, x);
+    vk_copy<double>(s, n, b, r);
+    if ((rc = pvcycle(c, 0, r, z))) return rc;
+    vk_copy<double>(s, n, z, p);
+    double d2[2];
+    const double* a2[2] = {r, r};
+    const double* b2[2] = {z, r};
+    if ((rc = dots<double>(c, n, 2, a2, b2, d2))) return rc;
+    double bn = std::sqrt(d2[1]), rz = d2[0];
+    if (bn == 0.0) return UWG_OK;
+    for (int it = 1; it <= maxit; it++) {
+        if ((rc = uwg_ops_applyL(c, 0, p, q, w->pvel[0]))) return rc;
+        double pq;
+        const double* a1[1] = {p};
+        const double* b1[1] = {q};
+        if ((rc = dots<double>(c, n, 1, a1, b1, &pq))) return rc;
+        w->lsolve_its++;
+        if (!(pq > 0.0)) return UWG_OK;
+        double alpha = rz / pq;
+        vk_axpy<double>(s, n, alpha, p, x);
+        vk_axpy<double>(s, n, -alpha, q, r);
+        if ((rc = pvcycle(c, 0, r, z))) return rc;
+        if ((rc = dots<double>(c, n, 2, a2, b2, d2))) return rc;
+        if (std::sqrt(d2[1]) <= rtol * bn) return UWG_OK;
+        double beta = d2[0] / rz;
+        rz = d2[0];
+        vk_axpby<double>(s, n, 1.0, z, beta, p);
+    }
+    return UWG_OK;   // a preconditioner: an inexact solve is acceptable
+}
+
+// z = -BFBt(r): the sign makes it approximate the inverse of C - G^T K^-1 G
+int bfbt(uwg_ctx* c, const double* r, double* z, double rtol) {
+    Work* w = work_of(c);
+    cudaStream_t s = c->stream;
+    int rc;
+    if ((rc = lsolve(c, r, w->bf_y, rtol, 200))) return rc;
+    if ((rc = uwg_ops_applyG(c, w->bf_y, w->bf_v1))) return rc;
+    vk_pointwise_div<double>(s, c->n_vdof, w->bf_v1, c->lev[0].diag64, w->bf_v1);
+    vk_mask<double>(s, c->n_vdof, c->bc, w->bf_v1);
+    if ((rc = uwg_ops_applyK<double>(c, 0, w->bf_v1, w->bf_v2))) return rc;
+    vk_mask<double>(s, c->n_vdof, c->bc, w->bf_v2);
+    vk_pointwise_div<double>(s, c->n_vdof, w->bf_v2, c->lev[0].diag64, w->bf_v2);
+    if ((rc = uwg_ops_applyGt(c, w->bf_v2, w->bf_m))) return rc;
+    if ((rc = lsolve(c, w->bf_m, z, rtol, 200))) return rc;
+    vk_scale<double>(s, c->n_pdof, -1.0, z);
+    return UWG_OK;
+}
+
+int bfbt_setup(uwg_ctx* c) {
+    Work* w = work_of(c);
+    cudaStream_t s = c->stream;
+    int rc;
+    for (int l = 0; l < c->nlev; l++) {
+        if ((rc = uwg_ops_Ldiag(c, l, w->Ldiag[l]))) return rc;
+        int64_t n = c->lev[l].n_el;
+        LevelVecs<double>& v = w->pv[l];
+        std::vector<double> hv(n);
+        for (int64_t i = 0; i < n; i++) hv[i] = 1.0 + 0.41 * std::sin(1.37 * (double)i) + ((i & 1) ? 0.3 : -0.3);
+        UWG_CUDA(c, cudaMemcpyAsync(v.x, hv.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+        double lam = 1.0;
+        for (int it = 0; it < 12; it++) {
+            if ((rc = uwg_ops_applyL(c, l, v.x, v.t, w->pvel[l]))) return rc;
+            vk_pointwise_div<double>(s, n, v.t, w->Ldiag[l], v.d);
+            double d2[2];
+            const double* a[2] = {v.d, v.x};
+            if ((rc = dots<double>(c, n, 2, a, a, d2))) return rc;
+            if (d2[0] <= 0.0 || d2[1] <= 0.0) break;
+            lam = std::sqrt(d2[0] / d2[1]);
+            vk_copy<double>(s, n, v.d, v.x);
+            vk_scale<double>(s, n, 1.0 / std::sqrt(d2[0]), v.x);
+        }
+        w->Lmax[l] = lam;
+    }
+    return UWG_OK;
+}
 }  // namespace
 
 void uwg_solver_free(uwg_ctx* c) {
@@ -309,14 +472,15 @@ int uwg_solver_estimate(uwg_ctx* c, int l) {
 }
 
 int uwg_solver_setup(uwg_ctx* c) {
-    int rc = work_init(c, 30);
+    int rc = work_init(c, 50);
     if (rc) return rc;
     for (int l = 0; l < c->nlev; l++) {
         if (l > 0 && (rc = uwg_ops_coarsen(c, l - 1))) return rc;
         if ((rc = uwg_ops_level_setup(c, l))) return rc;
         if (l < c->nlev - 1 && (rc = uwg_solver_estimate(c, l))) return rc;
     }
-    return uwg_ops_dense_coarse(c, c->nlev - 1);
+    if ((rc = uwg_ops_dense_coarse(c, c->nlev - 1))) return rc;
+    return bfbt_setup(c);
 }
 
 extern "C" void uwg_solve_opts_default(uwg_solve_opts* o) {
@@ -329,8 +493,10 @@ extern "C" void uwg_solve_opts_default(uwg_solve_opts* o) {
     o->max_outer = 500;
     o->mg_levels = 0;
     o->smooth_steps = 3;
-    o->restart = 30;
+    o->restart = 50;
     o->zero_guess = 1;
+    o->schur_pc = 1;
+    o->schur_pc_rtol = 1e-2;
 }
 
 namespace {
@@ -376,9 +542,13 @@ int fgmres(uwg_ctx* c, const SolveCfg& cfg, const double* rhs, double* p, double
         int j = 0;
         bool done = false;
         for (; j < m && total < maxit; j++) {
-            // Z_j = -S^^-1 V_j
-            if ((rc = uwg_ops_schur_pc(c, w->V[j], w->Z[j]))) return rc;
-            vk_scale<double>(s, n, -1.0, w->Z[j]);
+            // Z_j = M^-1 V_j: -S^^-1 (the reference's Uzawa term) or scaled BFBt
+            if (cfg.schur_pc == 1) {
+                if ((rc = bfbt(c, w->V[j], w->Z[j], cfg.schur_pc_rtol))) return rc;
+            } else {
+                if ((rc = uwg_ops_schur_pc(c, w->V[j], w->Z[j]))) return rc;
+                vk_scale<double>(s, n, -1.0, w->Z[j]);
+            }
             if ((rc = schur_apply(c, cfg, w->Z[j], w->V[j + 1], inner_its, refine))) return rc;
             total++;
             // classical Gram-Schmidt, two passes
@@ -488,7 +658,8 @@ extern "C" int uwg_stokes_solve(uwg_ctx* c, const uwg_solve_opts* o, double* u, 
     Work* w = work_of(c);
     cudaStream_t s = c->stream;
     int64_t nv = c->n_vdof, np = c->n_pdof;
-    SolveCfg cfg{o->mixed != 0, o->inner_rtol, o->max_inner, std::max(1, o->smooth_steps)};
+    SolveCfg cfg{o->mixed != 0, o->inner_rtol, o->max_inner, std::max(1, o->smooth_steps), o->schur_pc,
+                 o->schur_pc_rtol > 0.0 ? o->schur_pc_rtol : 1e-2};
     // b = f with Dirichlet values in BC rows
     vk_copy<double>(s, nv, c->f, w->bvec);
     {

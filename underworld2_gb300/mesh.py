@@ -1,0 +1,206 @@
+"""Regular Cartesian FE meshes and mesh variables (``uw.mesh`` subset).
+
+Mirrors ``FeMesh_Cartesian`` / ``MeshVariable`` of the reference
+(P/mesh/_mesh.py:1105-1160, P/mesh/_meshvariable.py) for Q1/dQ0 meshes:
+node numbering x-fastest, element numbering x-fastest, node coordinates
+``min + (i/n)*(max-min)`` (L/StgDomain/Mesh/src/CartesianGenerator.c:2003-2036).
+``MeshVariable.data`` is a host numpy array; the library copies it to the
+device when a solve or an advection reads it and writes results back in place.
+"""
+import re
+
+import numpy as np
+import torch
+
+from . import _core
+from . import function as _fn
+
+
+class IndexSet:
+    """A set of node indices (``uw.container.IndexSet`` subset)."""
+
+    def __init__(self, size, indices=()):
+        self.size = int(size)
+        self._set = np.unique(np.asarray(list(indices) if not isinstance(indices, np.ndarray) else indices,
+                                         dtype=np.int64))
+
+    @property
+    def data(self):
+        return self._set.copy()
+
+    def __add__(self, other):
+        return IndexSet(max(self.size, other.size), np.union1d(self._set, other._set))
+
+    def __len__(self):
+        return len(self._set)
+
+    def __iter__(self):
+        return iter(self._set.tolist())
+
+    def __contains__(self, i):
+        return int(i) in set(self._set.tolist())
+
+    def __repr__(self):
+        return "IndexSet(%s)" % self._set.tolist()
+
+
+class FeMesh_Cartesian:
+    """Regular Cartesian mesh, ``elementType`` 'Q1/dQ0' (primary Q1, dQ0 sub-mesh)."""
+
+    def __init__(self, elementType="Q1/dQ0", elementRes=(4, 4), minCoord=(0.0, 0.0), maxCoord=(1.0, 1.0),
+                 periodic=None, partitioned=True, **kwargs):
+        if isinstance(elementType, str):
+            elementType = re.split(",|-|/", elementType)
+        types = [t.upper() for t in elementType]
+        if types[0] not in ("Q1",) or (len(types) > 1 and types[1] not in ("DQ0",)):
+            raise ValueError("supported element type: 'Q1/dQ0' (got %s)" % "/".join(elementType))
+        if periodic and any(periodic):
+            raise ValueError("periodic meshes are not supported")
+        if len(elementRes) not in (2, 3) or len(minCoord) != len(elementRes) or len(maxCoord) != len(elementRes):
+            raise ValueError("elementRes, minCoord and maxCoord must have the same length (2 or 3)")
+        self.dim = len(elementRes)
+        self.elementRes = tuple(int(r) for r in elementRes)
+        self.minCoord = tuple(float(v) for v in minCoord)
+        self.maxCoord = tuple(float(v) for v in maxCoord)
+        self.elementType = "Q1"
+        self._ctx = None
+        n = [r + 1 for r in self.elementRes]
+        self.nodesGlobal = int(np.prod(n))
+        self.elementsGlobal = int(np.prod(self.elementRes))
+        self._axes = [self.minCoord[d] + (np.arange(n[d]) / (n[d] - 1)) * (self.maxCoord[d] - self.minCoord[d])
+                      for d in range(self.dim)]
+        for d in range(self.dim):
+            self._axes[d][0], self._axes[d][-1] = self.minCoord[d], self.maxCoord[d]
+        self.subMesh = _SubMesh(self)
+        self.specialSets = _SpecialSets(self)
+
+    @property
+    def ctx(self):
+        if self._ctx is None:
+            self._ctx = _core.Context(self.dim, self.elementRes, self.minCoord, self.maxCoord)
+        return self._ctx
+
+    @property
+    def data(self):
+        """Node coordinates [nodes, dim], node index x-fastest."""
+        g = np.meshgrid(*self._axes, indexing="ij")
+        return np.stack([a.transpose().ravel() for a in g], axis=1)
+
+    @property
+    def nodesLocal(self):
+        return self.nodesGlobal
+
+    @property
+    def elementsLocal(self):
+        return self.elementsGlobal
+
+    def add_variable(self, nodeDofCount, dataType="double", **kwargs):
+        return MeshVariable(self, nodeDofCount, dataType)
+
+    def _node_grid(self):
+        n = [r + 1 for r in self.elementRes]
+        idx = np.arange(self.nodesGlobal)
+        out = [idx % n[0], (idx // n[0]) % n[1]]
+        if self.dim == 3:
+            out.append(idx // (n[0] * n[1]))
+        return out, n
+
+
+class _SubMesh:
+    """The dQ0 pressure mesh: one node per element at its centroid."""
+
+    def __init__(self, mesh):
+        self.parent = mesh
+        self.dim = mesh.dim
+        self.elementType = "DQ0"
+        self.nodesGlobal = mesh.elementsGlobal
+        self.elementsGlobal = mesh.elementsGlobal
+        self.elementRes = mesh.elementRes
+
+    @property
+    def data(self):
+        ax = [0.5 * (a[1:] + a[:-1]) for a in self.parent._axes]
+        g = np.meshgrid(*ax, indexing="ij")
+        return np.stack([a.transpose().ravel() for a in g], axis=1)
+
+    def add_variable(self, nodeDofCount, dataType="double", **kwargs):
+        return MeshVariable(self, nodeDofCount, dataType)
+
+
+class _SpecialSets(dict):
+    """MinI/MaxI/MinJ/MaxJ(/MinK/MaxK) vertex sets and aliases (P/mesh/_mesh.py:1140-1158)."""
+
+    def __init__(self, mesh):
+        super().__init__()
+        (ii, nn), dim = mesh._node_grid(), mesh.dim
+        N = mesh.nodesGlobal
+        names = [("MinI_VertexSet", "Left_VertexSet", 0, 0), ("MaxI_VertexSet", "Right_VertexSet", 0, 1),
+                 ("MinJ_VertexSet", "Bottom_VertexSet", 1, 0), ("MaxJ_VertexSet", "Top_VertexSet", 1, 1)]
+        if dim == 3:
+            names += [("MinK_VertexSet", "Front_VertexSet", 2, 0), ("MaxK_VertexSet", "Back_VertexSet", 2, 1)]
+        allw = IndexSet(N)
+        for a, b, d, side in names:
+            sel = np.where(ii[d] == (0 if side == 0 else nn[d] - 1))[0]
+            s = IndexSet(N, sel)
+            self[a] = s
+            self[b] = s
+            allw = allw + s
+        self["AllWalls_VertexSet"] = allw
+        self["Empty"] = IndexSet(N)
+
+
+class MeshVariable:
+    """Nodal field with ``nodeDofCount`` components (host ``data`` + device mirror)."""
+
+    def __init__(self, mesh, nodeDofCount, dataType="double", **kwargs):
+        if dataType != "double":
+            raise ValueError("only 'double' mesh variables are supported")
+        self.mesh = mesh
+        self.nodeDofCount = int(nodeDofCount)
+        self._data = np.zeros((mesh.nodesGlobal, self.nodeDofCount))
+        self._dev = None
+
+    @property
+    def data(self):
+        return self._data
+
+    @data.setter
+    def data(self, v):
+        self._data[...] = v
+
+    def _primary(self):
+        return self.mesh if isinstance(self.mesh, FeMesh_Cartesian) else self.mesh.parent
+
+    def _to_device(self):
+        ctx = self._primary().ctx
+        t = torch.from_numpy(np.ascontiguousarray(self._data).ravel()).to(ctx.device)
+        if self._dev is None or self._dev.shape != t.shape:
+            self._dev = t.clone()
+        else:
+            self._dev.copy_(t)
+        return self._dev
+
+    def _from_device(self):
+        self._data[...] = self._dev.cpu().numpy().reshape(self._data.shape)
+
+    def _as_function(self):
+        return _fn._MeshVar(self)
+
+    def _interpolate(self, coords):
+        """Field values at global points (device tensor [n, dim] -> [n, k])."""
+        ctx = self._primary().ctx
+        if isinstance(self.mesh, FeMesh_Cartesian):
+            if self.nodeDofCount != self.mesh.dim:
+                raise ValueError("interpolation of Q1 fields needs dim components")
+            dev = self._to_device()
+            return ctx.interpolate(coords.contiguous(), dev)
+        own = ctx.locate(coords.contiguous()).long()
+        vals = torch.from_numpy(self._data).to(ctx.device)
+        return vals[own.clamp(max=vals.shape[0] - 1)]
+
+    def __add__(self, o): return self._as_function() + o
+    def __radd__(self, o): return o + self._as_function()
+    def __mul__(self, o): return self._as_function() * o
+    def __rmul__(self, o): return self._as_function() * o
+    def __sub__(self, o): return self._as_function() - o
+    def __getitem__(self, i): return self._as_function()[i]

@@ -1,0 +1,373 @@
+"""``uw.systems`` drop-ins for the PIC Stokes path: Stokes, Solver/StokesSolver,
+SwarmAdvector (P/systems/_stokes.py, _solver.py, _bsscr.py, _timeintegration.py).
+"""
+import time
+import warnings
+
+import numpy as np
+import torch
+
+from . import conditions as _cond
+from . import function as _fn
+from . import mesh as _mesh
+from . import swarm as _swarm
+
+
+class Stokes:
+    """The incompressible (or compressible) Stokes system K u + G p = f,
+    G^T u + C p = h on a Q1/dQ0 mesh (P/systems/_stokes.py:106-330)."""
+
+    def __init__(self, velocityField, pressureField, fn_viscosity, fn_bodyforce=None, fn_one_on_lambda=None,
+                 fn_source=None, voronoi_swarm=None, conditions=[], gauss_swarm=None, _removeBCs=True,
+                 _fn_viscosity2=None, _fn_director=None, fn_stresshistory=None, **kwargs):
+        if not isinstance(velocityField, _mesh.MeshVariable):
+            raise TypeError("Provided 'velocityField' must be of 'MeshVariable' class.")
+        if velocityField.nodeDofCount != velocityField.mesh.dim:
+            raise ValueError("Provided 'velocityField' must be a vector field of same dimensionality as its mesh.")
+        if not isinstance(pressureField, _mesh.MeshVariable):
+            raise TypeError("Provided 'pressureField' must be of 'MeshVariable' class.")
+        if pressureField.nodeDofCount != 1:
+            raise ValueError("Provided 'pressureField' must be a scalar field (ie pressureField.nodeDofCount==1).")
+        for name, v in (("_fn_viscosity2", _fn_viscosity2), ("_fn_director", _fn_director),
+                        ("fn_stresshistory", fn_stresshistory), ("fn_source", fn_source)):
+            if v is not None:
+                raise NotImplementedError("%s is not part of the GPU PIC Stokes path" % name)
+        if voronoi_swarm is not None and not isinstance(voronoi_swarm, _swarm.Swarm):
+            raise TypeError("Provided 'voronoi_swarm' must be of 'Swarm' class.")
+        self._velocityField = velocityField
+        self._pressureField = pressureField
+        self.mesh = velocityField.mesh
+        self.fn_viscosity = fn_viscosity
+        if fn_bodyforce is None:
+            fn_bodyforce = (0.0,) * self.mesh.dim
+        self.fn_bodyforce = fn_bodyforce
+        self._fn_one_on_lambda = _fn.Function.convert(fn_one_on_lambda) if fn_one_on_lambda is not None else None
+        self._swarm = voronoi_swarm
+        if not isinstance(conditions, (list, tuple)):
+            conditions = [conditions]
+        for c in conditions:
+            if not isinstance(c, _cond.SystemCondition):
+                raise TypeError("Provided 'conditions' must be 'SystemCondition' objects.")
+            if c.variable is not velocityField:
+                raise ValueError("Only Dirichlet conditions on the velocity field are supported.")
+        self._conditions = list(conditions)
+        if self._swarm is not None:
+            self._swarm._voronoi_swarm.repopulate()
+        self._u = None
+        self._p = None
+
+    # settable functions (P/systems/_stokes.py:334-355)
+    @property
+    def fn_viscosity(self):
+        return self._fn_viscosity
+
+    @fn_viscosity.setter
+    def fn_viscosity(self, value):
+        f = _fn.Function.convert(value)
+        if not isinstance(f, _fn.Function):
+            raise TypeError("Provided 'fn_viscosity' must be of or convertible to 'Function' class.")
+        self._fn_viscosity = f
+
+    @property
+    def fn_bodyforce(self):
+        return self._fn_bodyforce
+
+    @fn_bodyforce.setter
+    def fn_bodyforce(self, value):
+        self._fn_bodyforce = _fn.Function.convert(value)
+
+    # ------------------------------------------------------------------------
+    def _bc(self):
+        m = np.zeros(self._velocityField.data.shape, np.uint8)
+        for c in self._conditions:
+            m |= c.mask()
+        return m
+
+    def _integration_points(self):
+        """(offsets, list, ip_xi, ip_w, EvalContext) of the integration swarm."""
+        ctx = self.mesh.ctx
+        if self._swarm is not None:
+            vs = self._swarm._voronoi_swarm
+            vs.repopulate()
+            s = self._swarm
+            n = int(s._off[-1])
+            e = _fn.EvalContext(s._lst[:n].long(), vs.global_coords, ctx.device)
+            return s._off, s._lst, vs.ip_xi, vs.ip_w, e
+        # Gauss integration (3 points per axis), one "particle" per point
+        x1, w1 = np.polynomial.legendre.leggauss(3)
+        dim = self.mesh.dim
+        if dim == 2:
+            xi = np.array([[x1[i], x1[j]] for j in range(3) for i in range(3)])
+            w = np.array([w1[i] * w1[j] for j in range(3) for i in range(3)])
+        else:
+            xi = np.array([[x1[i], x1[j], x1[k]] for k in range(3) for j in range(3) for i in range(3)])
+            w = np.array([w1[i] * w1[j] * w1[k] for k in range(3) for j in range(3) for i in range(3)])
+        nq = len(w)
+        ne = ctx.n_el
+        ip_xi = torch.from_numpy(np.tile(xi, (ne, 1))).to(ctx.device)
+        ip_w = torch.from_numpy(np.tile(w, ne)).to(ctx.device)
+        off = (torch.arange(ne + 1, device=ctx.device) * nq).to(torch.int32)
+        lst = torch.arange(ne * nq, device=ctx.device, dtype=torch.int32)
+
+        def coords():
+            el = torch.arange(ne * nq, device=ctx.device) // nq
+            res = ctx.res
+            idx = [el % res[0], (el // res[0]) % res[1]] + ([el // (res[0] * res[1])] if dim == 3 else [])
+            out = torch.empty((ne * nq, dim), dtype=torch.float64, device=ctx.device)
+            for d in range(dim):
+                ax = torch.from_numpy(ctx.axes[d]).to(ctx.device)
+                lo, hi = ax[idx[d]], ax[idx[d] + 1]
+                out[:, d] = lo + (ip_xi[:, d] + 1.0) * 0.5 * (hi - lo)
+            return out
+
+        if self._fn_viscosity.depends_on({"swarm"}) or self._fn_bodyforce.depends_on({"swarm"}):
+            raise ValueError("swarm-variable functions need a voronoi_swarm")
+        return off, lst, ip_xi, ip_w, _fn.EvalContext(lst.long(), coords, ctx.device)
+
+    def _per_particle(self, f, ectx, npart, ncomp):
+        v = f.evaluate_at(ectx).to(torch.float64)
+        if v.shape[1] != ncomp:
+            raise ValueError("function returns %d components, %d expected" % (v.shape[1], ncomp))
+        out = torch.zeros((npart, ncomp), dtype=torch.float64, device=ectx.device)
+        out[ectx.pid] = v
+        return out.contiguous()
+
+    def _assemble(self):
+        ctx = self.mesh.ctx
+        off, lst, ip_xi, ip_w, ectx = self._integration_points()
+        npart = lst.shape[0]
+        eta = self._per_particle(self._fn_viscosity, ectx, npart, 1).view(-1)
+        body = self._per_particle(self._fn_bodyforce, ectx, npart, self.mesh.dim)
+        lam = None
+        if self._fn_one_on_lambda is not None:
+            lam = self._per_particle(self._fn_one_on_lambda, ectx, npart, 1).view(-1)
+        mask = self._bc()
+        vals = self._velocityField.data * (mask != 0)
+        ctx.set_bcs(torch.from_numpy(mask.ravel()), torch.from_numpy(np.ascontiguousarray(vals).ravel()))
+        ctx.assemble(off, lst, ip_xi, ip_w, eta, body, lam)
+
+    @property
+    def eqResiduals(self):
+        """(||f - K u - G p||, ||h - G^T u||) at the current fields (P/systems/_stokes.py:396-416)."""
+        ctx = self.mesh.ctx
+        self._assemble()
+        u = self._velocityField._to_device()
+        p = self._pressureField._to_device()
+        r = ctx.residuals(u, p)
+        return float(r[0]), float(r[1])
+
+    def velocity_rms(self):
+        """sqrt(int v.v / int 1) over the mesh, Gauss quadrature (P/systems/_stokes.py:435-448)."""
+        mesh = self.mesh
+        v = self._velocityField.data
+        dim = mesh.dim
+        x1, w1 = np.polynomial.legendre.leggauss(2)
+        n = [r + 1 for r in mesh.elementRes]
+        grid = v.reshape(*(n[::-1]), dim)
+        h = [np.diff(a) for a in mesh._axes]
+        num = 0.0
+        vol = 0.0
+        if dim == 2:
+            for j in range(2):
+                for i in range(2):
+                    sx, sy = (1 + x1[i]) / 2, (1 + x1[j]) / 2
+                    val = ((1 - sx) * (1 - sy) * grid[:-1, :-1] + sx * (1 - sy) * grid[:-1, 1:] +
+                           (1 - sx) * sy * grid[1:, :-1] + sx * sy * grid[1:, 1:])
+                    area = np.outer(h[1], h[0])
+                    num += np.sum(w1[i] * w1[j] * 0.25 * area * np.sum(val ** 2, axis=-1))
+                    vol += np.sum(w1[i] * w1[j] * 0.25 * area)
+        else:
+            for k in range(2):
+                for j in range(2):
+                    for i in range(2):
+                        s = [(1 + x1[i]) / 2, (1 + x1[j]) / 2, (1 + x1[k]) / 2]
+                        val = 0.0
+                        for c in range(8):
+                            a, b, cz = c & 1, (c >> 1) & 1, (c >> 2) & 1
+                            wgt = (s[0] if a else 1 - s[0]) * (s[1] if b else 1 - s[1]) * (s[2] if cz else 1 - s[2])
+                            val = val + wgt * grid[cz: cz + n[2] - 1, b: b + n[1] - 1, a: a + n[0] - 1]
+                        volm = h[2][:, None, None] * h[1][None, :, None] * h[0][None, None, :]
+                        num += np.sum(w1[i] * w1[j] * w1[k] * 0.125 * volm * np.sum(val ** 2, axis=-1))
+                        vol += np.sum(w1[i] * w1[j] * w1[k] * 0.125 * volm)
+        return float(np.sqrt(num / vol))
+
+
+class _Options:
+    def __init__(self, **kw):
+        self.__dict__.update(kw)
+
+
+class _OptionsGroup:
+    """solver.options.A11 / scr / main / mg (P/systems/_bsscr.py:36-194, subset)."""
+
+    def __init__(self):
+        self.A11 = _Options(ksp_rtol=1e-6, ksp_type="fgmres", _mixed=False)
+        self.scr = _Options(ksp_rtol=1e-5, ksp_type="fgmres", restart=30)
+        self.main = _Options(penalty=0.0, Q22_pc_type="uw", ksp_k2_type="NULL", max_inner=500, max_outer=500)
+        self.mg = _Options(active=True, levels=0, smooth_steps=3)
+
+
+class StokesSolverStats:
+    def __init__(self, d):
+        self.__dict__.update(d)
+
+    def __repr__(self):
+        return "StokesSolverStats(%s)" % ", ".join("%s=%r" % kv for kv in sorted(self.__dict__.items()))
+
+
+class StokesSolver:
+    """Block Stokes Schur-complement solver (P/systems/_bsscr.py:229-764).
+
+    Tolerances default to the reference's (inner 1e-6, outer 1e-5); the GPU
+    run-time driver additionally reports the true FP64 residual of the full
+    system in ``get_stats().residual``."""
+
+    def __init__(self, stokesSLE, **kwargs):
+        if not isinstance(stokesSLE, Stokes):
+            raise TypeError("Provided system must be of 'Stokes' class")
+        self._stokesSLE = stokesSLE
+        self.options = _OptionsGroup()
+        self._stats = None
+
+    def set_inner_method(self, solve_type="mg"):
+        """'mg' (FP64 multigrid CG) or 'mixed' (FP32 multigrid CG inside FP64 refinement)."""
+        if solve_type not in ("mg", "mixed", "mg_fp32"):
+            raise ValueError("inner method must be 'mg' or 'mixed' on the GPU path (got %r)" % solve_type)
+        self.options.A11._mixed = solve_type != "mg"
+
+    def set_inner_rtol(self, rtol):
+        self.options.A11.ksp_rtol = float(rtol)
+
+    def set_outer_rtol(self, rtol):
+        self.options.scr.ksp_rtol = float(rtol)
+
+    def set_mg_levels(self, levels):
+        self.options.mg.levels = int(levels)
+
+    def set_penalty(self, penalty):
+        if penalty:
+            raise NotImplementedError("the augmented-Lagrangian penalty path is not part of the GPU solver")
+
+    def _check_linearity(self, nonLinearIterate):
+        s = self._stokesSLE
+        nl = False
+        for f in (s.fn_viscosity, s.fn_bodyforce):
+            if _depends_on_fields(f, (s._velocityField, s._pressureField)):
+                nl = True
+        if nl and nonLinearIterate is None:
+            raise RuntimeError("Nonlinearity detected.\nYour viscosity or body force depends on the solution; "
+                               "set the solve() 'nonLinearIterate' parameter to True or False.")
+        return nl
+
+    def solve(self, nonLinearIterate=None, nonLinearTolerance=1.0e-2, nonLinearKillNonConvergent=False,
+              nonLinearMinIterations=1, nonLinearMaxIterations=500, callback_post_solve=None,
+              print_stats=False, reinitialise=True, **kwargs):
+        if kwargs:
+            raise ValueError("unknown solver options: %s" % ", ".join(sorted(kwargs)))
+        if not isinstance(nonLinearTolerance, float) or nonLinearTolerance < 0.0:
+            raise ValueError("'nonLinearTolerance' option must be of type 'float' and greater than 0.0")
+        if callback_post_solve is not None and not callable(callback_post_solve):
+            raise RuntimeError("The 'callback_post_solve' parameter is not 'None' and isn't callable")
+        nonlinear = self._check_linearity(nonLinearIterate) and bool(nonLinearIterate)
+        its = nonLinearMaxIterations if nonlinear else 1
+        prev = None
+        for it in range(its):
+            self._linear_solve(print_stats)
+            if callback_post_solve is not None:
+                callback_post_solve()
+            if not nonlinear:
+                break
+            v = self._stokesSLE._velocityField.data.copy()
+            if prev is not None and it + 1 >= nonLinearMinIterations:
+                change = np.linalg.norm(v - prev) / max(np.linalg.norm(v), 1e-300)
+                if change < nonLinearTolerance:
+                    break
+            prev = v
+
+    def _linear_solve(self, print_stats):
+        s = self._stokesSLE
+        ctx = s.mesh.ctx
+        t0 = time.perf_counter()
+        s._assemble()
+        t1 = time.perf_counter()
+        u = s._velocityField._to_device()
+        p = s._pressureField._to_device()
+        o = self.options
+        st = ctx.solve(u, p, mixed=int(o.A11._mixed), rtol=min(o.A11.ksp_rtol, o.scr.ksp_rtol),
+                       inner_rtol=o.A11.ksp_rtol, outer_rtol=o.scr.ksp_rtol, max_inner=o.main.max_inner,
+                       max_outer=o.main.max_outer, smooth_steps=o.mg.smooth_steps, restart=o.scr.restart)
+        s._velocityField._from_device()
+        s._pressureField._from_device()
+        st["assembly_time"] = t1 - t0
+        self._stats = StokesSolverStats(st)
+        if min(st["fhat_reason"], st["outer_reason"], st["backsolve_reason"]) < 0:
+            warnings.warn("A solver error has been encountered during the solve. The resultant convergence "
+                          "reasons are (f_hat, outer, backsolve) (%d,%d,%d)." % (
+                              st["fhat_reason"], st["outer_reason"], st["backsolve_reason"]))
+        if print_stats:
+            self.print_stats()
+
+    def get_stats(self):
+        return self._stats
+
+    def print_stats(self):
+        st = self._stats
+        if st is None:
+            return
+        print("Pressure iterations: %3d" % st.pressure_its)
+        print("Velocity iterations: %3d (presolve)" % st.velocity_presolve_its)
+        print("Velocity iterations: %3d (pressure solve)" % st.velocity_pressuresolve_its)
+        print("Velocity iterations: %3d (backsolve)" % st.velocity_backsolve_its)
+        print("Velocity iterations: %3d (total solve)" % st.velocity_total_its)
+        print("SCR RHS  solve time: %.4e" % st.presolve_time)
+        print("Pressure solve time: %.4e" % st.pressure_time)
+        print("Velocity solve time: %.4e (backsolve)" % st.backsolve_time)
+        print("Total solve time   : %.4e" % st.total_time)
+        print("Relative residual  : %.3e" % st.residual)
+
+
+def _depends_on_fields(f, fields):
+    if isinstance(f, _fn._MeshVar):
+        return f.var in fields
+    return any(_depends_on_fields(c, fields) for c in f._children())
+
+
+def Solver(eqs, type="BSSCR", *args, **kwargs):
+    """Solver factory (P/systems/_solver.py:26-35)."""
+    if isinstance(eqs, Stokes):
+        return StokesSolver(eqs, *args, **kwargs)
+    raise ValueError("the GPU path provides the Stokes solver only")
+
+
+class SwarmAdvector:
+    """Midpoint-RK2 particle advection with owner update (P/systems/_timeintegration.py:77-157)."""
+
+    def __init__(self, velocityField, swarm, order=2, **kwargs):
+        if not isinstance(velocityField, _mesh.MeshVariable):
+            raise ValueError("Provided 'velocityField' must be of 'MeshVariable' class.")
+        if swarm is not None and not isinstance(swarm, _swarm.Swarm):
+            raise ValueError("Provided 'swarm' must be of 'Swarm' class.")
+        if order != 2:
+            raise ValueError("only order=2 (midpoint RK2) is provided")
+        self._velocityField = velocityField
+        self._swarm = swarm
+
+    def get_max_dt(self):
+        """0.5 * minimum node separation / max |v| (SwarmAdvector_MaxDt)."""
+        ctx = self._swarm.mesh.ctx
+        return ctx.max_dt(self._velocityField._to_device())
+
+    def integrate(self, dt, update_owners=True):
+        s = self._swarm
+        ctx = s.mesh.ctx
+        vel = self._velocityField._to_device()
+        fb, failed = ctx.rk2(s._x, vel, dt)
+        if failed:
+            raise RuntimeError("Unable to determine valid velocity for %d particle(s): coordinate appears to be "
+                               "outside the global domain." % failed)
+        if not bool(torch.isfinite(s._x).all()):
+            raise RuntimeError("particle coordinates are not finite after advection")
+        s._host_x = None
+        s._toggle_state()
+        if update_owners:
+            s.update_particle_owners()
