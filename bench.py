@@ -158,7 +158,8 @@ def run_gpu(args):
     npart = x0.shape[0]
     u = ctx.zeros(ctx.n_vdof)
     p = ctx.zeros(ctx.n_pdof)
-    opts = dict(rtol=1e-8, inner_rtol=args.inner_rtol, outer_rtol=args.outer_rtol, smooth_steps=3, restart=30)
+    opts = dict(rtol=1e-8, inner_rtol=args.inner_rtol, outer_rtol=args.outer_rtol, smooth_steps=3, restart=50,
+                schur_pc=args.schur_pc, schur_pc_rtol=args.bfbt_rtol)
     ev = lambda: torch.cuda.Event(enable_timing=True)
 
     def solve_step(x, off, lst, eta, body, mixed, times):
@@ -220,7 +221,8 @@ def run_gpu(args):
         t64 = {k: [] for k in ("map_dvc", "assemble", "solve")}
         st64 = solve_step(x, off, lst, eta0, body0, 0, t64)
         fp64 = {"solve_s": t64["solve"][0], "pressure_its": st64["pressure_its"],
-                "velocity_total_its": st64["velocity_total_its"], "residual": st64["residual"]}
+                "velocity_total_its": st64["velocity_total_its"], "schur_pc_its": st64["schur_pc_its"],
+                "residual": st64["residual"]}
 
     # end to end through host buffers
     x_h = x0.cpu().pin_memory()
@@ -271,7 +273,10 @@ def run_gpu(args):
         "particles_per_s": npart / adv_s,
         "phases_s": {k: float(np.mean(v)) for k, v in times.items()},
         "solver": {"pressure_its": stats[-1]["pressure_its"], "velocity_total_its": stats[-1]["velocity_total_its"],
-                   "refinement_steps": stats[-1]["refinement_steps"], "residual": stats[-1]["residual"]},
+                   "schur_pc_its": stats[-1]["schur_pc_its"], "refinement_steps": stats[-1]["refinement_steps"],
+                   "residual": stats[-1]["residual"], "schur_pc": "scaled BFBt" if args.schur_pc else "Uzawa S^",
+                   "presolve_s": stats[-1]["presolve_time"], "pressure_s": stats[-1]["pressure_time"],
+                   "backsolve_s": stats[-1]["backsolve_time"]},
         "fp64_solve": fp64,
         "e2e": {"value": float(np.mean(e2e_t)), "unit": "s/solve", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
@@ -381,6 +386,8 @@ def main():
     ap.add_argument("--mode", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--inner-rtol", type=float, default=1e-10)
     ap.add_argument("--outer-rtol", type=float, default=1e-9)
+    ap.add_argument("--schur-pc", type=int, default=1, help="0: Uzawa S^ (reference), 1: scaled BFBt")
+    ap.add_argument("--bfbt-rtol", type=float, default=1e-2)
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-count-launches", dest="count_launches", action="store_false")

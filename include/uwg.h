@@ -158,6 +158,7 @@ typedef struct {
     double residual;       /* final relative residual of the full system, FP64 */
     double vmin, vmax, pmin, pmax;
     int fhat_reason, outer_reason, backsolve_reason; /* >0 converged, <0 not */
+    int schur_pc_its;      /* CG iterations of the pressure-Laplacian solves inside BFBt */
 } uwg_solve_stats;
 
 void uwg_solve_opts_default(uwg_solve_opts* o);

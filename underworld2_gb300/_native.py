@@ -46,7 +46,7 @@ class SolveStats(ctypes.Structure):
                 ("total_time", ctypes.c_double), ("residual", ctypes.c_double),
                 ("vmin", ctypes.c_double), ("vmax", ctypes.c_double), ("pmin", ctypes.c_double),
                 ("pmax", ctypes.c_double), ("fhat_reason", ctypes.c_int), ("outer_reason", ctypes.c_int),
-                ("backsolve_reason", ctypes.c_int)]
+                ("backsolve_reason", ctypes.c_int), ("schur_pc_its", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -993,6 +993,17 @@ template <typename T> __global__ void vk_scale_k(int64_t n, T a, T* y) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i < n) y[i] *= a;
 }
+// One Chebyshev step: r = b - t (t may be null: r = b); d = a*(r/diag) + c*d; x (+)= d
+template <typename T> __global__ void vk_cheb_k(int64_t n, const T* b, const T* t, const T* diag, T a, T c,
+                                             T* d, T* x, int first, int x_zero) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    T r = t ? b[i] - t[i] : b[i];
+    T dn = a * (r / diag[i]);
+    if (!first) dn += c * d[i];
+    d[i] = dn;
+    x[i] = x_zero ? dn : x[i] + dn;
+}
 template <typename T> __global__ void vk_mask_k(int64_t n, const uint8_t* bc, T* y) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i < n && bc[i]) y[i] = 0;
@@ -1009,6 +1020,14 @@ template <typename T> void vk_axpby(cudaStream_t s, int64_t n, T a, const T* x, 
 template <typename T> void vk_scale(cudaStream_t s, int64_t n, T a, T* y) { if (n) vk_scale_k<T><<<nblk(n), 256, 0, s>>>(n, a, y); }
 template <typename T> void vk_zero(cudaStream_t s, int64_t n, T* y) { if (n) cudaMemsetAsync(y, 0, sizeof(T) * n, s); }
 template <typename T> void vk_mask(cudaStream_t s, int64_t n, const uint8_t* bc, T* y) { if (n) vk_mask_k<T><<<nblk(n), 256, 0, s>>>(n, bc, y); }
+template <typename T> void vk_cheb(cudaStream_t s, int64_t n, const T* b, const T* t, const T* diag, T a, T c, T* d,
+                                   T* x, int first, int x_zero) {
+    if (n) vk_cheb_k<T><<<nblk(n), 256, 0, s>>>(n, b, t, diag, a, c, d, x, first, x_zero);
+}
+template void vk_cheb<double>(cudaStream_t, int64_t, const double*, const double*, const double*, double, double,
+                              double*, double*, int, int);
+template void vk_cheb<float>(cudaStream_t, int64_t, const float*, const float*, const float*, float, float, float*,
+                             float*, int, int);
 template <typename T> void vk_pointwise_div(cudaStream_t s, int64_t n, const T* x, const T* d, T* y) { if (n) vk_pdiv_k<T><<<nblk(n), 256, 0, s>>>(n, x, d, y); }
 
 template void vk_copy<double>(cudaStream_t, int64_t, const double*, double*);

@@ -49,6 +49,8 @@ template <typename T> void vk_axpby(cudaStream_t s, int64_t n, T a, const T* x, 
 template <typename T> void vk_scale(cudaStream_t s, int64_t n, T a, T* y);
 template <typename T> void vk_zero(cudaStream_t s, int64_t n, T* y);
 template <typename T> void vk_mask(cudaStream_t s, int64_t n, const uint8_t* bc, T* y);       // y[bc] = 0
+template <typename T> void vk_cheb(cudaStream_t s, int64_t n, const T* b, const T* t, const T* diag, T a, T c, T* d,
+                                   T* x, int first, int x_zero);
 template <typename T> void vk_pointwise_div(cudaStream_t s, int64_t n, const T* x, const T* d, T* y);
 // Sums of products into dst[k] (double), k < 4: dots of (a_k, b_k) pairs.
 template <typename T> void vk_dots(cudaStream_t s, int64_t n, int k, const T* const* a, const T* const* b,

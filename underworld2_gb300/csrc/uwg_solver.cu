@@ -20,6 +20,8 @@
 #include <cstring>
 #include <vector>
 
+#include <functional>
+
 #include "uwg_ops.cuh"
 
 namespace {
@@ -51,6 +53,10 @@ struct Work {
     double Lmax[UWG_MAXLEV];
     double *pcg_r, *pcg_z, *pcg_p, *pcg_q, *bf_y, *bf_m, *bf_v1, *bf_v2;
     int lsolve_its = 0;
+    // CUDA graphs of the V-cycles (captured at setup, replayed by the Krylov loops)
+    cudaStream_t gstream = nullptr;
+    cudaGraphExec_t g_v64 = nullptr, g_v32 = nullptr, g_pv = nullptr;
+    int g_deg = 0;
 };
 
 Work* work_of(uwg_ctx* c) {
@@ -127,7 +133,8 @@ template <typename T> const T* diagT(uwg_level& L);
 template <> const double* diagT<double>(uwg_level& L) { return L.diag64; }
 template <> const float* diagT<float>(uwg_level& L) { return L.diag32; }
 
-// Chebyshev-Jacobi smoothing of K x = b on level l, `deg` applications.
+// Chebyshev-Jacobi smoothing of K x = b on level l, `deg` applications
+// (one operator apply and one fused update kernel per step).
 template <typename T>
 int chebyshev(uwg_ctx* c, int l, const T* b, T* x, int deg, bool x_zero) {
     uwg_level& L = c->lev[l];
@@ -140,26 +147,12 @@ int chebyshev(uwg_ctx* c, int l, const T* b, T* x, int deg, bool x_zero) {
     double theta = 0.5 * (beta + alpha), delta = 0.5 * (beta - alpha);
     double sigma = theta / delta, rho = 1.0 / sigma;
     int rc;
-    // r = b - K x
-    if (x_zero) vk_copy<T>(s, n, b, v.r);
-    else {
-        if ((rc = uwg_ops_applyK<T>(c, l, x, v.t))) return rc;
-        vk_copy<T>(s, n, b, v.r);
-        vk_axpy<T>(s, n, (T)-1, v.t, v.r);
-    }
-    // d = D^-1 r / theta
-    vk_pointwise_div<T>(s, n, v.r, diagT<T>(L), v.d);
-    vk_scale<T>(s, n, (T)(1.0 / theta), v.d);
-    vk_axpy<T>(s, n, (T)1, v.d, x);
+    if (!x_zero && (rc = uwg_ops_applyK<T>(c, l, x, v.t))) return rc;
+    vk_cheb<T>(s, n, b, x_zero ? nullptr : v.t, diagT<T>(L), (T)(1.0 / theta), (T)0, v.d, x, 1, x_zero ? 1 : 0);
     for (int i = 1; i < deg; i++) {
         if ((rc = uwg_ops_applyK<T>(c, l, x, v.t))) return rc;
-        vk_copy<T>(s, n, b, v.r);
-        vk_axpy<T>(s, n, (T)-1, v.t, v.r);
         double rho1 = 1.0 / (2.0 * sigma - rho);
-        // d = rho1 rho d + (2 rho1 / delta) D^-1 r
-        vk_pointwise_div<T>(s, n, v.r, diagT<T>(L), v.t);
-        vk_axpby<T>(s, n, (T)(2.0 * rho1 / delta), v.t, (T)(rho1 * rho), v.d);
-        vk_axpy<T>(s, n, (T)1, v.d, x);
+        vk_cheb<T>(s, n, b, v.t, diagT<T>(L), (T)(2.0 * rho1 / delta), (T)(rho1 * rho), v.d, x, 0, 0);
         rho = rho1;
     }
     return UWG_OK;
@@ -175,7 +168,6 @@ int vcycle(uwg_ctx* c, int l, const T* b, T* x, int deg) {
     Work* w = work_of(c);
     LevelVecs<T>& v = vecs<T>(w, l);
     LevelVecs<T>& vc = vecs<T>(w, l + 1);
-    vk_zero<T>(s, L.n_dof, x);
     if ((rc = chebyshev<T>(c, l, b, x, deg, true))) return rc;
     if ((rc = uwg_ops_applyK<T>(c, l, x, v.t))) return rc;
     vk_axpby<T>(s, L.n_dof, (T)1, b, (T)-1, v.t);   // t = b - K x
@@ -183,6 +175,25 @@ int vcycle(uwg_ctx* c, int l, const T* b, T* x, int deg) {
     if ((rc = vcycle<T>(c, l + 1, vc.b, vc.x, deg))) return rc;
     if ((rc = uwg_ops_prolong_add<T>(c, l + 1, vc.x, x))) return rc;
     return chebyshev<T>(c, l, b, x, deg, false);
+}
+
+template <typename T> cudaGraphExec_t graph_of(Work* w);
+template <> cudaGraphExec_t graph_of<double>(Work* w) { return w->g_v64; }
+template <> cudaGraphExec_t graph_of<float>(Work* w) { return w->g_v32; }
+template <typename T> bool graph_buffers(Work* w, const T* b, const T* x);
+template <> bool graph_buffers<double>(Work* w, const double* b, const double* x) { return b == w->cg_r && x == w->cg_z; }
+template <> bool graph_buffers<float>(Work* w, const float* b, const float* x) { return b == w->cg32_r && x == w->cg32_z; }
+
+// Finest-level V-cycle: the captured graph when the buffers match, else launched directly.
+template <typename T>
+int run_vcycle(uwg_ctx* c, const T* b, T* x, int deg) {
+    Work* w = work_of(c);
+    cudaGraphExec_t g = graph_of<T>(w);
+    if (g && deg == w->g_deg && graph_buffers<T>(w, b, x)) {
+        UWG_CUDA(c, cudaGraphLaunch(g, c->stream));
+        return UWG_OK;
+    }
+    return vcycle<T>(c, 0, b, x, deg);
 }
 
 // Preconditioned CG on the finest level: x (in/out), stops at ||r|| <= tol*||b||
@@ -201,7 +212,7 @@ int pcg(uwg_ctx* c, const T* b, T* x, double bnorm, double tol, int maxit, int d
         vk_copy<T>(s, n, b, r);
         vk_axpy<T>(s, n, (T)-1, q, r);
     }
-    if ((rc = vcycle<T>(c, 0, r, z, deg))) return rc;
+    if ((rc = run_vcycle<T>(c, r, z, deg))) return rc;
     vk_copy<T>(s, n, z, p);
     double d2[2];
     const T* a2[2] = {r, r};
@@ -223,7 +234,7 @@ int pcg(uwg_ctx* c, const T* b, T* x, double bnorm, double tol, int maxit, int d
         double alpha = rz / pq;
         vk_axpy<T>(s, n, (T)alpha, p, x);
         vk_axpy<T>(s, n, (T)-alpha, q, r);
-        if ((rc = vcycle<T>(c, 0, r, z, deg))) return rc;
+        if ((rc = run_vcycle<T>(c, r, z, deg))) return rc;
         if ((rc = dots<T>(c, n, 2, a2, b2, d2))) return rc;
         *its = it;
         if (!std::isfinite(d2[1])) return uwg_set_error(c, UWG_ERR_NAN, "non-finite residual in velocity CG");
@@ -308,23 +319,12 @@ int cheb_L(uwg_ctx* c, int l, const double* b, double* x, int deg, bool x_zero) 
     double theta = 0.5 * (beta + alpha), delta = 0.5 * (beta - alpha);
     double sigma = theta / delta, rho = 1.0 / sigma;
     int rc;
-    if (x_zero) vk_copy<double>(s, n, b, v.r);
-    else {
-        if ((rc = uwg_ops_applyL(c, l, x, v.t, w->pvel[l]))) return rc;
-        vk_copy<double>(s, n, b, v.r);
-        vk_axpy<double>(s, n, -1.0, v.t, v.r);
-    }
-    vk_pointwise_div<double>(s, n, v.r, w->Ldiag[l], v.d);
-    vk_scale<double>(s, n, 1.0 / theta, v.d);
-    vk_axpy<double>(s, n, 1.0, v.d, x);
+    if (!x_zero && (rc = uwg_ops_applyL(c, l, x, v.t, w->pvel[l]))) return rc;
+    vk_cheb<double>(s, n, b, x_zero ? nullptr : v.t, w->Ldiag[l], 1.0 / theta, 0.0, v.d, x, 1, x_zero ? 1 : 0);
     for (int i = 1; i < deg; i++) {
         if ((rc = uwg_ops_applyL(c, l, x, v.t, w->pvel[l]))) return rc;
-        vk_copy<double>(s, n, b, v.r);
-        vk_axpy<double>(s, n, -1.0, v.t, v.r);
         double rho1 = 1.0 / (2.0 * sigma - rho);
-        vk_pointwise_div<double>(s, n, v.r, w->Ldiag[l], v.t);
-        vk_axpby<double>(s, n, 2.0 * rho1 / delta, v.t, rho1 * rho, v.d);
-        vk_axpy<double>(s, n, 1.0, v.d, x);
+        vk_cheb<double>(s, n, b, v.t, w->Ldiag[l], 2.0 * rho1 / delta, rho1 * rho, v.d, x, 0, 0);
         rho = rho1;
     }
     return UWG_OK;
@@ -335,7 +335,7 @@ int pvcycle(uwg_ctx* c, int l, const double* b, double* x) {
     cudaStream_t s = c->stream;
     int64_t n = c->lev[l].n_el;
     int rc;
-    vk_zero<double>(s, n, x);
+    (void)s; (void)n;
     if (l == c->nlev - 1) return cheb_L(c, l, b, x, 8, true);
     LevelVecs<double>& v = w->pv[l];
     LevelVecs<double>& vc = w->pv[l + 1];
@@ -348,6 +348,47 @@ int pvcycle(uwg_ctx* c, int l, const double* b, double* x) {
     return cheb_L(c, l, b, x, 3, false);
 }
 
+int run_pvcycle(uwg_ctx* c, const double* b, double* x) {
+    Work* w = work_of(c);
+    if (w->g_pv && b == w->pcg_r && x == w->pcg_z) {
+        UWG_CUDA(c, cudaGraphLaunch(w->g_pv, c->stream));
+        return UWG_OK;
+    }
+    return pvcycle(c, 0, b, x);
+}
+
+// Capture `body` (kernels only, no host synchronisation) into an executable graph.
+int capture(uwg_ctx* c, cudaGraphExec_t* out, const std::function<int()>& body) {
+    Work* w = work_of(c);
+    if (*out) { cudaGraphExecDestroy(*out); *out = nullptr; }
+    if (!w->gstream) UWG_CUDA(c, cudaStreamCreateWithFlags(&w->gstream, cudaStreamNonBlocking));
+    cudaStream_t saved = c->stream;
+    UWG_CUDA(c, cudaStreamSynchronize(saved));
+    c->stream = w->gstream;
+    cudaError_t e = cudaStreamBeginCapture(w->gstream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) { c->stream = saved; return uwg_set_error(c, UWG_ERR_CUDA, cudaGetErrorString(e)); }
+    int rc = body();
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(w->gstream, &g);
+    c->stream = saved;
+    if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+    if (e != cudaSuccess) return uwg_set_error(c, UWG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return uwg_set_error(c, UWG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    return UWG_OK;
+}
+
+int capture_cycles(uwg_ctx* c, int deg) {
+    Work* w = work_of(c);
+    int rc;
+    if ((rc = capture(c, &w->g_v64, [&]() { return vcycle<double>(c, 0, w->cg_r, w->cg_z, deg); }))) return rc;
+    if ((rc = capture(c, &w->g_v32, [&]() { return vcycle<float>(c, 0, w->cg32_r, w->cg32_z, deg); }))) return rc;
+    if ((rc = capture(c, &w->g_pv, [&]() { return pvcycle(c, 0, w->pcg_r, w->pcg_z); }))) return rc;
+    w->g_deg = deg;
+    return UWG_OK;
+}
+
 // x = L^-1 b by multigrid-preconditioned CG from zero, to rtol
 int lsolve(uwg_ctx* c, const double* b, double* x, double rtol, int maxit) {
     Work* w = work_of(c);
@@ -357,7 +398,7 @@ int lsolve(uwg_ctx* c, const double* b, double* x, double rtol, int maxit) {
     double *r = w->pcg_r, *z = w->pcg_z, *p = w->pcg_p, *q = w->pcg_q;
     vk_zero<double>(s, n, x);
     vk_copy<double>(s, n, b, r);
-    if ((rc = pvcycle(c, 0, r, z))) return rc;
+    if ((rc = run_pvcycle(c, r, z))) return rc;
     vk_copy<double>(s, n, z, p);
     double d2[2];
     const double* a2[2] = {r, r};
@@ -376,7 +417,7 @@ int lsolve(uwg_ctx* c, const double* b, double* x, double rtol, int maxit) {
         double alpha = rz / pq;
         vk_axpy<double>(s, n, alpha, p, x);
         vk_axpy<double>(s, n, -alpha, q, r);
-        if ((rc = pvcycle(c, 0, r, z))) return rc;
+        if ((rc = run_pvcycle(c, r, z))) return rc;
         if ((rc = dots<double>(c, n, 2, a2, b2, d2))) return rc;
         if (std::sqrt(d2[1]) <= rtol * bn) return UWG_OK;
         double beta = d2[0] / rz;
@@ -434,6 +475,13 @@ int bfbt_setup(uwg_ctx* c) {
 }  // namespace
 
 void uwg_solver_free(uwg_ctx* c) {
+    if (!c->ws.empty()) {
+        Work* w = (Work*)c->ws[0];
+        if (w->g_v64) cudaGraphExecDestroy(w->g_v64);
+        if (w->g_v32) cudaGraphExecDestroy(w->g_v32);
+        if (w->g_pv) cudaGraphExecDestroy(w->g_pv);
+        if (w->gstream) cudaStreamDestroy(w->gstream);
+    }
     for (size_t i = 1; i < c->ws.size(); i++) cudaFree(c->ws[i]);
     if (!c->ws.empty()) delete (Work*)c->ws[0];
     c->ws.clear();
@@ -480,7 +528,8 @@ int uwg_solver_setup(uwg_ctx* c) {
         if (l < c->nlev - 1 && (rc = uwg_solver_estimate(c, l))) return rc;
     }
     if ((rc = uwg_ops_dense_coarse(c, c->nlev - 1))) return rc;
-    return bfbt_setup(c);
+    if ((rc = bfbt_setup(c))) return rc;
+    return capture_cycles(c, 3);
 }
 
 extern "C" void uwg_solve_opts_default(uwg_solve_opts* o) {
@@ -517,8 +566,8 @@ int schur_apply(uwg_ctx* c, const SolveCfg& cfg, const double* p, double* q, int
 }
 
 // Right-preconditioned flexible GMRES on the Schur complement, M^-1 = -S^^-1.
-int fgmres(uwg_ctx* c, const SolveCfg& cfg, const double* rhs, double* p, double rtol, int maxit, int m,
-           int* its, int* inner_its, int* refine) {
+int fgmres(uwg_ctx* c, const SolveCfg& cfg, const double* rhs, double* p, double rtol, double atol, int maxit,
+           int m, int* its, int* inner_its, int* refine) {
     Work* w = work_of(c);
     cudaStream_t s = c->stream;
     int64_t n = c->n_pdof;
@@ -530,6 +579,8 @@ int fgmres(uwg_ctx* c, const SolveCfg& cfg, const double* rhs, double* p, double
     *its = 0;
     vk_zero<double>(s, n, p);
     if (bn == 0.0) return UWG_OK;
+    double tol = rtol * bn;
+    if (atol > 0.0 && atol < tol) tol = atol;
     std::vector<double> H((m + 1) * m), cs(m), sn(m), g(m + 1), y(m);
     int total = 0;
     // r0 = rhs (p = 0)
@@ -584,7 +635,7 @@ int fgmres(uwg_ctx* c, const SolveCfg& cfg, const double* rhs, double* p, double
             g[j + 1] = -sn[j] * g[j];
             g[j] = cs[j] * g[j];
             if (hn > 0.0) vk_scale<double>(s, n, 1.0 / hn, w->V[j + 1]);
-            if (std::fabs(g[j + 1]) <= rtol * bn || hn == 0.0) { j++; done = true; break; }
+            if (std::fabs(g[j + 1]) <= tol || hn == 0.0) { j++; done = true; break; }
         }
         // y = H^-1 g, p += Z y
         for (int i = j - 1; i >= 0; i--) {
@@ -604,7 +655,7 @@ int fgmres(uwg_ctx* c, const SolveCfg& cfg, const double* rhs, double* p, double
         const double* a0[1] = {w->V[0]};
         if ((rc = dots<double>(c, n, 1, a0, a0, &beta))) return rc;
         beta = std::sqrt(beta);
-        if (beta <= rtol * bn) return UWG_OK;
+        if (beta <= tol) return UWG_OK;
     }
 }
 
@@ -684,10 +735,24 @@ extern "C" int uwg_stokes_solve(uwg_ctx* c, const uwg_solve_opts* o, double* u, 
     if ((rc = uwg_ops_applyGt(c, w->ftil, w->hhat))) return rc;
     vk_axpby<double>(s, np, 1.0, c->h, -1.0, w->hhat);
     // 3. pressure solve: S p = h^, S = C - G^T A^-1 G
+    w->lsolve_its = 0;
     int outer = 0, inner_its = 0;
-    rc = fgmres(c, cfg, w->hhat, p, o->outer_rtol, o->max_outer, std::max(2, o->restart), &outer, &inner_its,
+    // the full-system target ||[f - Ku - Gp; h - G^T u]|| <= rtol ||[f; h]|| is met once the
+    // Schur residual is below it (the back-solve adds inner_rtol-level error)
+    double fh2[2];
+    {
+        vk_copy<double>(s, nv, c->f, w->u_tmp);
+        vk_mask<double>(s, nv, c->bc, w->u_tmp);
+        const double* a1[1] = {w->u_tmp};
+        if ((rc = dots<double>(c, nv, 1, a1, a1, &fh2[0]))) return rc;
+        const double* a2[1] = {c->h};
+        if ((rc = dots<double>(c, np, 1, a2, a2, &fh2[1]))) return rc;
+    }
+    double atol = o->rtol > 0.0 ? 0.5 * o->rtol * std::sqrt(fh2[0] + fh2[1]) : 0.0;
+    rc = fgmres(c, cfg, w->hhat, p, o->outer_rtol, atol, o->max_outer, std::max(2, o->restart), &outer, &inner_its,
                 &S.refinement_steps);
     S.pressure_its = outer;
+    S.schur_pc_its = w->lsolve_its;
     S.velocity_pressuresolve_its = inner_its;
     S.outer_reason = rc ? -1 : 1;
     if (rc) return rc;
