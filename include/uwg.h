@@ -102,6 +102,22 @@ int uwg_pic_map(uwg_ctx* ctx, int64_t np, const double* x, const int32_t* cell_o
 int uwg_dvc_weights(uwg_ctx* ctx, int res, const int32_t* cell_offsets, double* ip_xi,
                     double* ip_w);
 
+/* DVC weights without any device allocation and without a context.
+ * No counterpart in the reference: it exists for callers that cannot allocate
+ * device memory when they need the weights -- code running while a stream is
+ * captured into a CUDA graph (cudaMalloc is not capturable) and host frameworks
+ * that own all device memory -- and that therefore cannot create a context.
+ * Same inputs and outputs as uwg_dvc_weights (dim 2 or 3, res 1..16, at most
+ * 128 particles per element), on `cuda_stream`; synchronises the stream.
+ * The boundary-list scratch is a fixed 32 MiB device array inside libuwg that
+ * every GPU loading the library holds until exit; the first call on a device
+ * looks its address up (cudaGetSymbolAddress) and should come before any
+ * stream capture.  All calls share that array: calls that overlap on the GPU
+ * (different streams or threads) race and must be serialised by the caller.
+ * Returns 0, UWG_ERR_ARG, UWG_ERR_CUDA, UWG_ERR_EMPTY_CELL or UWG_ERR_CELL_FULL. */
+int uwg_dvc_weights_noalloc(int dim, int res, int64_t n_el, const int32_t* cell_offsets, double* ip_xi,
+                            double* ip_w, void* cuda_stream);
+
 /* Dirichlet conditions: bc_mask[n_vdof] (1 = fixed), values[n_vdof].
  * Replaces FeVariable_SetBC + SystemLinearEquations_BC_Setup
  * (P/systems/_stokes.py:194-204, L/StgFEM/SLE/SystemSetup/src/SystemLinearEquations.c:521). */
@@ -159,6 +175,8 @@ typedef struct {
     double vmin, vmax, pmin, pmax;
     int fhat_reason, outer_reason, backsolve_reason; /* >0 converged, <0 not */
     int schur_pc_its;      /* CG iterations of the pressure-Laplacian solves inside BFBt */
+    double schur_pc_time;  /* seconds in the Schur preconditioner */
+    double schur_op_time;  /* seconds in Schur-operator applications (inner velocity solves) */
 } uwg_solve_stats;
 
 void uwg_solve_opts_default(uwg_solve_opts* o);

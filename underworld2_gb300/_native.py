@@ -46,7 +46,8 @@ class SolveStats(ctypes.Structure):
                 ("total_time", ctypes.c_double), ("residual", ctypes.c_double),
                 ("vmin", ctypes.c_double), ("vmax", ctypes.c_double), ("pmin", ctypes.c_double),
                 ("pmax", ctypes.c_double), ("fhat_reason", ctypes.c_int), ("outer_reason", ctypes.c_int),
-                ("backsolve_reason", ctypes.c_int), ("schur_pc_its", ctypes.c_int)]
+                ("backsolve_reason", ctypes.c_int), ("schur_pc_its", ctypes.c_int),
+                ("schur_pc_time", ctypes.c_double), ("schur_op_time", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -71,6 +72,7 @@ SIGNATURES = {
     "uwg_update_owners": (_I, [_CTX, _I64, _P, _P, _P, _P, ctypes.POINTER(_I64)]),
     "uwg_pic_map": (_I, [_CTX, _I64, _P, _P, _P, _P]),
     "uwg_dvc_weights": (_I, [_CTX, _I, _P, _P, _P]),
+    "uwg_dvc_weights_noalloc": (_I, [_I, _I, _I64, _P, _P, _P, _P]),
     "uwg_set_bcs": (_I, [_CTX, _P, _P]),
     "uwg_assemble": (_I, [_CTX, _I64, _P, _P, _P, _P, _P, _P, _P]),
     "uwg_element_matrices": (_I, [_CTX, _I64, _P, _P, _P, _P]),

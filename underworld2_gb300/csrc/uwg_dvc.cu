@@ -269,3 +269,80 @@ extern "C" int uwg_dvc_weights(uwg_ctx* c, int res, const int32_t* cell_offsets,
                              " exceeds the DVC kernel limits (128 particles per element)");
     return UWG_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the DVC weights.
+//
+// Some callers cannot allocate device memory at the point where they need
+// the weights: code that runs while a CUDA stream is being captured into a
+// graph (cudaMalloc is not a capturable operation), and host frameworks that
+// hand out all device memory up front and forbid allocations afterwards.
+// They cannot create a uwg context either, because creating one allocates.
+// This entry point needs neither: the per-warp boundary lists live in the
+// fixed device array below, which every GPU that loads libuwg holds until the
+// process exits.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+#define UWG_NOALLOC_SCRATCH_BYTES (32u << 20)   // 32 MiB of boundary-list scratch
+#define UWG_NOALLOC_MAX_DEVICES 64
+
+static __device__ __align__(256) unsigned char uwg_noalloc_scratch[UWG_NOALLOC_SCRATCH_BYTES + 256];
+
+static std::mutex uwg_noalloc_mutex;
+static void* uwg_noalloc_ptr[UWG_NOALLOC_MAX_DEVICES];
+
+extern "C" int uwg_dvc_weights_noalloc(int dim, int res, int64_t n_el, const int32_t* cell_offsets,
+                                       double* ip_xi, double* ip_w, void* cuda_stream) {
+    if ((dim != 2 && dim != 3) || res < 1 || res > 16 || n_el < 0 || (n_el && (!cell_offsets || !ip_xi || !ip_w)))
+        return UWG_ERR_ARG;
+    if (n_el == 0) return UWG_OK;
+    cudaStream_t stream = (cudaStream_t)cuda_stream;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= UWG_NOALLOC_MAX_DEVICES) return UWG_ERR_CUDA;
+    unsigned char* base = nullptr;
+    {
+        // once per device, with that device current: the device address of the array
+        std::lock_guard<std::mutex> lock(uwg_noalloc_mutex);
+        if (!uwg_noalloc_ptr[dev]) {
+            void* p = nullptr;
+            if (cudaGetSymbolAddress(&p, uwg_noalloc_scratch) != cudaSuccess || !p) return UWG_ERR_CUDA;
+            uwg_noalloc_ptr[dev] = p;
+        }
+        base = (unsigned char*)uwg_noalloc_ptr[dev];
+    }
+    int RC = dim == 3 ? res * res * res : res * res;
+    size_t per_warp = (size_t)RC * 2 + (size_t)DVC_NMAX * 3 * 8 + (size_t)DVC_NMAX * 4 * 4;
+    per_warp = (per_warp + 15) & ~(size_t)15;
+    size_t shm = 128 + per_warp * DVC_WARPS;
+    dvc_args a;
+    a.n_el = n_el;
+    a.R = res;
+    a.off = cell_offsets;
+    a.ip_xi = ip_xi;
+    a.ip_w = ip_w;
+    a.pcap = (int64_t)RC * 8;
+    size_t warp_bytes = (size_t)(RC + 2 * a.pcap) * 2;
+    int64_t max_warps = (int64_t)(UWG_NOALLOC_SCRATCH_BYTES / warp_bytes);
+    int64_t max_blocks = max_warps / DVC_WARPS;
+    if (max_blocks < 1) return UWG_ERR_ARG;   // grid too fine for the fixed scratch
+    void (*kern)(dvc_args) = dim == 3 ? k_dvc<3> : k_dvc<2>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm) != cudaSuccess)
+        return UWG_ERR_CUDA;
+    int nsm = 0, per_sm = 0;
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return UWG_ERR_CUDA;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * DVC_WARPS, shm) != cudaSuccess)
+        return UWG_ERR_CUDA;
+    int64_t blocks = std::min<int64_t>((int64_t)nsm * std::max(per_sm, 1), (n_el + DVC_WARPS - 1) / DVC_WARPS);
+    blocks = std::max<int64_t>(1, std::min(blocks, max_blocks));
+    // status word first (must start at zero every call), then the boundary lists
+    a.status = (int32_t*)base;
+    a.scratch = (int16_t*)(base + 256);
+    if (cudaMemsetAsync(a.status, 0, 8, stream) != cudaSuccess) return UWG_ERR_CUDA;
+    kern<<<(unsigned)blocks, 32 * DVC_WARPS, shm, stream>>>(a);
+    if (cudaGetLastError() != cudaSuccess) return UWG_ERR_CUDA;
+    int32_t st[2] = {0, 0};
+    if (cudaMemcpyAsync(st, a.status, 8, cudaMemcpyDeviceToHost, stream) != cudaSuccess) return UWG_ERR_CUDA;
+    if (cudaStreamSynchronize(stream) != cudaSuccess) return UWG_ERR_CUDA;
+    return st[0];   // 0, UWG_ERR_EMPTY_CELL or UWG_ERR_CELL_FULL
+}
