@@ -159,7 +159,7 @@ def run_gpu(args):
     u = ctx.zeros(ctx.n_vdof)
     p = ctx.zeros(ctx.n_pdof)
     opts = dict(rtol=1e-8, inner_rtol=args.inner_rtol, outer_rtol=args.outer_rtol, smooth_steps=3, restart=50,
-                schur_pc=args.schur_pc, schur_pc_rtol=args.bfbt_rtol)
+                schur_pc=args.schur_pc, schur_pc_rtol=args.bfbt_rtol, max_outer=args.max_outer)
     ev = lambda: torch.cuda.Event(enable_timing=True)
 
     def solve_step(x, off, lst, eta, body, mixed, times):
@@ -231,7 +231,7 @@ def run_gpu(args):
     u_h = torch.empty(ctx.n_vdof, dtype=torch.float64).pin_memory()
     p_h = torch.empty(ctx.n_pdof, dtype=torch.float64).pin_memory()
     e2e_t = []
-    for it in range(max(1, min(args.steps, 3))):
+    for it in range(1):
         owner.copy_(owner0); off.copy_(off0); lst.copy_(lst0)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -276,7 +276,8 @@ def run_gpu(args):
                    "schur_pc_its": stats[-1]["schur_pc_its"], "refinement_steps": stats[-1]["refinement_steps"],
                    "residual": stats[-1]["residual"], "schur_pc": "scaled BFBt" if args.schur_pc else "Uzawa S^",
                    "presolve_s": stats[-1]["presolve_time"], "pressure_s": stats[-1]["pressure_time"],
-                   "backsolve_s": stats[-1]["backsolve_time"]},
+                   "backsolve_s": stats[-1]["backsolve_time"], "schur_pc_s": stats[-1]["schur_pc_time"],
+                   "schur_op_s": stats[-1]["schur_op_time"]},
         "fp64_solve": fp64,
         "e2e": {"value": float(np.mean(e2e_t)), "unit": "s/solve", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
@@ -319,6 +320,37 @@ def time_kernel_apply(ctx, reps=20):
     nq = 27 if ctx.dim == 3 else 9
     byts = 4 * 2 * ctx.n_vdof + 4 * nq * ctx.n_el
     return {"name": "k_applyK_q1_%dd<float> (+ BC copy)" % ctx.dim, "seconds": sec, "bytes": byts}
+
+
+def run_kernel(args):
+    """Set the workload up, then launch one operator kernel `--reps` times
+    (the target of the ncu captures recorded under profiles/)."""
+    import ctypes
+    import torch
+    from underworld2_gb300._core import Context, rng_seed
+    cfg = CONFIGS[args.config]
+    dim = cfg["dim"]
+    ctx = Context(dim, cfg["res"], (0.0,) * dim, (1.0,) * dim)
+    ctx.set_bcs(freeslip_mask(ctx))
+    ppc = args.kernel_ppc or cfg["ppc"]
+    x, owner, off, lst, _ = ctx.layout_random(ppc, rng_seed(13))
+    eta, body = material(cfg, x)
+    ip_xi = ctx.pic_map(x, off, lst)
+    ip_w = ctx.dvc_weights(off, ip_xi)
+    ctx.assemble(off, lst, ip_xi, ip_w, eta, body)
+    torch.cuda.synchronize()
+    dt = torch.float32 if args.kernel == "applyK32" else torch.float64
+    xv = torch.randn(ctx.n_vdof, dtype=dt, device=ctx.device)
+    yv = torch.empty_like(xv)
+    name = "uwg_apply_K32" if args.kernel == "applyK32" else "uwg_apply_K64"
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(args.reps):
+        ctx._call(name, 0, ctypes.c_void_p(xv.data_ptr()), ctypes.c_void_p(yv.data_ptr()))
+    e.record()
+    torch.cuda.synchronize()
+    print(json.dumps({"kernel": args.kernel, "config": args.config, "reps": args.reps,
+                      "ms_per_launch": s.elapsed_time(e) / args.reps}))
 
 
 def count_launches(ctx, x0, owner0, off0, lst0, eta0, body0, mixed, opts, u, p):
@@ -379,7 +411,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="grf3d", choices=sorted(CONFIGS))
@@ -388,10 +420,17 @@ def main():
     ap.add_argument("--outer-rtol", type=float, default=1e-9)
     ap.add_argument("--schur-pc", type=int, default=1, help="0: Uzawa S^ (reference), 1: scaled BFBt")
     ap.add_argument("--bfbt-rtol", type=float, default=1e-2)
+    ap.add_argument("--kernel", choices=["applyK32", "applyK64"], help="only launch one operator kernel (profiling)")
+    ap.add_argument("--kernel-ppc", type=int, default=0)
+    ap.add_argument("--reps", type=int, default=5)
+    ap.add_argument("--max-outer", type=int, default=500)
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-count-launches", dest="count_launches", action="store_false")
     args = ap.parse_args()
+    if args.kernel:
+        run_kernel(args)
+        return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":

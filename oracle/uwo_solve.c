@@ -616,6 +616,12 @@ int uwo_sys_solve(uwo_sys* s, double inner_rtol, double outer_rtol, int max_inne
     for (int64_t e = 0; e < np; e++) s->hhat[e] = s->h[e] - s->hhat[e];
     /* FGMRES(m), right preconditioner -S^-1 */
     double bn = sqrt(dot(np, s->hhat, s->hhat));
+    /* stop once the Schur residual is below half the full-system target (1e-8) */
+    double fnorm = 0.0;
+    for (int64_t i = 0; i < nv; i++) if (!s->L[0].bc[i]) fnorm += s->f[i] * s->f[i];
+    for (int64_t e = 0; e < np; e++) fnorm += s->h[e] * s->h[e];
+    double tol = outer_rtol * bn, atol = 0.5e-8 * sqrt(fnorm);
+    if (atol > 0.0 && atol < tol) tol = atol;
     memset(p, 0, sizeof(double) * np);
     int total = 0, inner_its = 0;
     double* H = (double*)calloc((size_t)(m + 1) * m, sizeof(double));
@@ -654,7 +660,7 @@ int uwo_sys_solve(uwo_sys* s, double inner_rtol, double outer_rtol, int max_inne
                 g[j + 1] = -sn[j] * g[j];
                 g[j] = cs[j] * g[j];
                 if (hn > 0.0) for (int64_t e = 0; e < np; e++) s->V[j + 1][e] /= hn;
-                if (fabs(g[j + 1]) <= outer_rtol * bn || hn == 0.0) { j++; done = 1; break; }
+                if (fabs(g[j + 1]) <= tol || hn == 0.0) { j++; done = 1; break; }
             }
             for (int i = j - 1; i >= 0; i--) {
                 double t = g[i];
@@ -667,7 +673,7 @@ int uwo_sys_solve(uwo_sys* s, double inner_rtol, double outer_rtol, int max_inne
                 inner_its += schur(s, p, s->pt1, inner_rtol, max_inner, deg);
                 for (int64_t e = 0; e < np; e++) s->V[0][e] = s->hhat[e] - s->pt1[e];
                 beta = sqrt(dot(np, s->V[0], s->V[0]));
-                if (beta <= outer_rtol * bn) done = 1;
+                if (beta <= tol) done = 1;
             }
         }
         if (!done) rc = -1;

@@ -216,26 +216,11 @@ __global__ void k_bc_copy(int64_t n, const uint8_t* bc, const T* x, T* y) {
     if (i < n) y[i] = bc[i] ? x[i] : (T)0;
 }
 
+// y_e = K_e u_e for one 3D Q1 element from its equivalent-quadrature weights
+// (sum-factorised on the 3-point rule).  hx,hy,hz = 2/h per axis.
 template <typename T>
-__global__ void __launch_bounds__(128) k_applyK_q1_3d(uwg_lgeom g, const T* __restrict__ W,
-                                                      const uint8_t* __restrict__ bc, bool mask_in,
-                                                      const T* __restrict__ x, T* y) {
-    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (e >= g.n_el) return;
-    int64_t nodes[8];
-    double hd[3];
-    q1_elem(g, e, nodes, hd);
-    const T hx = (T)(2.0 / hd[0]), hy = (T)(2.0 / hd[1]), hz = (T)(2.0 / hd[2]);
-    T u[8][3];
-    bool fix[8][3];
-#pragma unroll
-    for (int n = 0; n < 8; n++)
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-            int64_t dof = nodes[n] * 3 + c;
-            fix[n][c] = bc[dof] != 0;
-            u[n][c] = (fix[n][c] && mask_in) ? (T)0 : x[dof];
-        }
+__device__ __forceinline__ void q1_3d_element(const T* __restrict__ W, int64_t n_el, int64_t e, T hx, T hy, T hz,
+                                              const T (&u)[8][3], T (&out)[8][3]) {
     // physical gradients on the 3x3 face grids
     T Gx[3][3][3], Gy[3][3][3], Gz[3][3][3];   // [c][p][q]
 #pragma unroll
@@ -281,7 +266,7 @@ __global__ void __launch_bounds__(128) k_applyK_q1_3d(uwg_lgeom g, const T* __re
         for (int py = 0; py < 3; py++)
 #pragma unroll
             for (int px = 0; px < 3; px++) {
-                T w = W[(int64_t)(px + 3 * py + 9 * pz) * g.n_el + e];
+                T w = W[(int64_t)(px + 3 * py + 9 * pz) * n_el + e];
                 T uxx = Gx[0][py][pz], uxy = Gy[0][px][pz], uxz = Gz[0][px][py];
                 T uyx = Gx[1][py][pz], uyy = Gy[1][px][pz], uyz = Gz[1][px][py];
                 T uzx = Gx[2][py][pz], uzy = Gy[2][px][pz], uzz = Gz[2][px][py];
@@ -292,7 +277,6 @@ __global__ void __launch_bounds__(128) k_applyK_q1_3d(uwg_lgeom g, const T* __re
                 Rx[2][py][pz] += sxz; Ry[2][px][pz] += syz; Rz[2][px][py] += szz;
             }
     // transpose of the face interpolation and the derivative
-    T out[8][3];
 #pragma unroll
     for (int c = 0; c < 3; c++) {
         // down-sample 3x3 -> 2x2: v[j][k] = sum L(j,p) L(k,q) R[p][q]
@@ -333,11 +317,106 @@ __global__ void __launch_bounds__(128) k_applyK_q1_3d(uwg_lgeom g, const T* __re
         }
 #undef DOWN
     }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_applyK_q1_3d(uwg_lgeom g, const T* __restrict__ W,
+                                                      const uint8_t* __restrict__ bc, bool mask_in,
+                                                      const T* __restrict__ x, T* y) {
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= g.n_el) return;
+    int64_t nodes[8];
+    double hd[3];
+    q1_elem(g, e, nodes, hd);
+    const T hx = (T)(2.0 / hd[0]), hy = (T)(2.0 / hd[1]), hz = (T)(2.0 / hd[2]);
+    T u[8][3];
+    bool fix[8][3];
+#pragma unroll
+    for (int n = 0; n < 8; n++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            int64_t dof = nodes[n] * 3 + c;
+            fix[n][c] = bc[dof] != 0;
+            u[n][c] = (fix[n][c] && mask_in) ? (T)0 : x[dof];
+        }
+    T out[8][3];
+    q1_3d_element<T>(W, g.n_el, e, hx, hy, hz, u, out);
 #pragma unroll
     for (int n = 0; n < 8; n++)
 #pragma unroll
         for (int c = 0; c < 3; c++)
             if (!fix[n][c]) atomicAdd(&y[nodes[n] * 3 + c], out[n][c]);
+}
+
+
+// Shared-memory tiled K apply (3D): a CTA owns an 8x8x4 tile of elements, stages
+// the tile's 9x9x5 nodal values in shared memory (row-contiguous loads), adds
+// the element results into a shared tile with shared-memory atomics, and then
+// writes nodes inside the tile with plain stores and nodes on the tile faces
+// (shared with neighbouring tiles) with global atomics: 8x fewer global
+// atomics than the element-per-thread kernel.
+#define KT_X 8
+#define KT_Y 8
+#define KT_Z 4
+template <typename T>
+__global__ void __launch_bounds__(KT_X * KT_Y * KT_Z) k_applyK_q1_3d_tiled(uwg_lgeom g, const T* __restrict__ W,
+                                                                         const uint8_t* __restrict__ bc,
+                                                                         const T* __restrict__ x, T* y) {
+    constexpr int NX = KT_X + 1, NY = KT_Y + 1, NZ = KT_Z + 1, NN = NX * NY * NZ;
+    __shared__ T xs[NN * 3];
+    __shared__ T ys[NN * 3];
+    int ntx = (g.res[0] + KT_X - 1) / KT_X, nty = (g.res[1] + KT_Y - 1) / KT_Y;
+    int tile = blockIdx.x;
+    int tx0 = (tile % ntx) * KT_X, ty0 = ((tile / ntx) % nty) * KT_Y, tz0 = (tile / (ntx * nty)) * KT_Z;
+    int64_t gnx = g.nx[0], gny = g.nx[1];
+    // stage nodal values (masked) and clear the accumulator
+    for (int k = threadIdx.x; k < NN * 3; k += blockDim.x) {
+        int nl = k / 3, c = k % 3;
+        int li = nl % NX, lj = (nl / NX) % NY, lk = nl / (NX * NY);
+        int gi = tx0 + li, gj = ty0 + lj, gk = tz0 + lk;
+        T v = (T)0;
+        if (gi < g.nx[0] && gj < g.nx[1] && gk < g.nx[2]) {
+            int64_t dof = (gi + gnx * (gj + gny * (int64_t)gk)) * 3 + c;
+            v = bc[dof] ? (T)0 : x[dof];
+        }
+        xs[k] = v;
+        ys[k] = (T)0;
+    }
+    __syncthreads();
+    int li = threadIdx.x % KT_X, lj = (threadIdx.x / KT_X) % KT_Y, lk = threadIdx.x / (KT_X * KT_Y);
+    int ex = tx0 + li, ey = ty0 + lj, ez = tz0 + lk;
+    if (ex < g.res[0] && ey < g.res[1] && ez < g.res[2]) {
+        int64_t e = ex + (int64_t)g.res[0] * (ey + (int64_t)g.res[1] * ez);
+        const T hx = (T)(2.0 / (g.ax[0][ex + 1] - g.ax[0][ex]));
+        const T hy = (T)(2.0 / (g.ax[1][ey + 1] - g.ax[1][ey]));
+        const T hz = (T)(2.0 / (g.ax[2][ez + 1] - g.ax[2][ez]));
+        T u[8][3], out[8][3];
+#pragma unroll
+        for (int n = 0; n < 8; n++) {
+            int sl = (li + (n & 1)) + NX * ((lj + ((n >> 1) & 1)) + NY * (lk + ((n >> 2) & 1)));
+#pragma unroll
+            for (int c = 0; c < 3; c++) u[n][c] = xs[sl * 3 + c];
+        }
+        q1_3d_element<T>(W, g.n_el, e, hx, hy, hz, u, out);
+#pragma unroll
+        for (int n = 0; n < 8; n++) {
+            int sl = (li + (n & 1)) + NX * ((lj + ((n >> 1) & 1)) + NY * (lk + ((n >> 2) & 1)));
+#pragma unroll
+            for (int c = 0; c < 3; c++) atomicAdd(&ys[sl * 3 + c], out[n][c]);
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < NN * 3; k += blockDim.x) {
+        int nl = k / 3, c = k % 3;
+        int ni = nl % NX, nj = (nl / NX) % NY, nk = nl / (NX * NY);
+        int gi = tx0 + ni, gj = ty0 + nj, gk = tz0 + nk;
+        if (gi >= g.nx[0] || gj >= g.nx[1] || gk >= g.nx[2]) continue;
+        int64_t dof = (gi + gnx * (gj + gny * (int64_t)gk)) * 3 + c;
+        if (bc[dof]) continue;
+        bool interior = ni > 0 && ni < KT_X && nj > 0 && nj < KT_Y && nk > 0 && nk < KT_Z;
+        if (interior) y[dof] = ys[k];
+        else atomicAdd(&y[dof], ys[k]);
+    }
 }
 
 template <typename T>
@@ -401,8 +480,13 @@ int uwg_ops_applyK(uwg_ctx* c, int l, const T* x, T* y) {
     const T* W;
     if constexpr (sizeof(T) == 8) W = (const T*)L.W64; else W = (const T*)L.W32;
     k_bc_copy<T><<<nblk(L.n_dof), 256, 0, c->stream>>>(L.n_dof, L.bc, x, y);
-    if (c->dim == 3) k_applyK_q1_3d<T><<<nblk(L.n_el, 128), 128, 0, c->stream>>>(g, W, L.bc, true, x, y);
-    else k_applyK_q1_2d<T><<<nblk(L.n_el, 128), 128, 0, c->stream>>>(g, W, L.bc, true, x, y);
+    if (c->dim == 3) {
+        unsigned tiles = (unsigned)(((L.res[0] + KT_X - 1) / KT_X) * ((L.res[1] + KT_Y - 1) / KT_Y) *
+                                    ((L.res[2] + KT_Z - 1) / KT_Z));
+        k_applyK_q1_3d_tiled<T><<<tiles, KT_X * KT_Y * KT_Z, 0, c->stream>>>(g, W, L.bc, x, y);
+    } else {
+        k_applyK_q1_2d<T><<<nblk(L.n_el, 128), 128, 0, c->stream>>>(g, W, L.bc, true, x, y);
+    }
     UWG_CUDA(c, cudaGetLastError());
     return UWG_OK;
 }
@@ -465,6 +549,197 @@ __global__ void k_applyGt(uwg_lgeom g, const uint8_t* bc, int only_bc, const dou
             s += ge * u[dof];
         }
     q[e] = s;
+}
+
+// Node-centred (gather) gradient: v[n][c] = (G p)[n][c] / D[n][c] over the
+// 2^dim cells around node n, Dirichlet dofs zero.  D may be null (no scaling).
+// No atomics: every dof is written by one thread.
+template <int DIM>
+__global__ void k_gradG_nodes(uwg_lgeom g, const uint8_t* bc, const double* p, const double* D, double* v) {
+    int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (n >= g.n_nodes) return;
+    int ni = (int)(n % g.nx[0]), nj = (int)((n / g.nx[0]) % g.nx[1]);
+    int nk = DIM == 3 ? (int)(n / ((int64_t)g.nx[0] * g.nx[1])) : 0;
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (int cz = 0; cz < (DIM == 3 ? 2 : 1); cz++)
+        for (int cy = 0; cy < 2; cy++)
+            for (int cx = 0; cx < 2; cx++) {
+                int ex = ni - 1 + cx, ey = nj - 1 + cy, ez = DIM == 3 ? nk - 1 + cz : 0;
+                if (ex < 0 || ex >= g.res[0] || ey < 0 || ey >= g.res[1] || (DIM == 3 && (ez < 0 || ez >= g.res[2])))
+                    continue;
+                double h[3] = {g.ax[0][ex + 1] - g.ax[0][ex], g.ax[1][ey + 1] - g.ax[1][ey],
+                               DIM == 3 ? g.ax[2][ez + 1] - g.ax[2][ez] : 1.0};
+                double pe = p[ex + (int64_t)g.res[0] * (ey + (int64_t)g.res[1] * ez)];
+                int loc[3] = {1 - cx, 1 - cy, 1 - cz};   // node's local index in this cell
+                for (int c = 0; c < DIM; c++) {
+                    double ge = 1.0;
+                    for (int d = 0; d < DIM; d++)
+                        if (d != c) ge *= 0.5 * h[d];
+                    acc[c] += (loc[c] ? -ge : ge) * pe;
+                }
+            }
+    for (int c = 0; c < DIM; c++) {
+        int64_t dof = n * DIM + c;
+        v[dof] = bc[dof] ? 0.0 : (D ? acc[c] / D[dof] : acc[c]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// FP32 pressure-space operators of the weighted BFBt preconditioner (level l):
+//   v = Dinv * (G p)  (node gather),  q = G^T v  (cell gather),
+//   L p = G^T Dinv G p,  Dinv = 1/sqrt(diag K) on free dofs.
+// ---------------------------------------------------------------------------
+template <int DIM>
+__global__ void k_gradG32(uwg_lgeom g, const uint8_t* bc, const float* p, const float* Dinv, float* v) {
+    int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (n >= g.n_nodes) return;
+    int ni = (int)(n % g.nx[0]), nj = (int)((n / g.nx[0]) % g.nx[1]);
+    int nk = DIM == 3 ? (int)(n / ((int64_t)g.nx[0] * g.nx[1])) : 0;
+    float acc[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int cz = 0; cz < (DIM == 3 ? 2 : 1); cz++)
+#pragma unroll
+        for (int cy = 0; cy < 2; cy++)
+#pragma unroll
+            for (int cx = 0; cx < 2; cx++) {
+                int ex = ni - 1 + cx, ey = nj - 1 + cy, ez = DIM == 3 ? nk - 1 + cz : 0;
+                if (ex < 0 || ex >= g.res[0] || ey < 0 || ey >= g.res[1] || (DIM == 3 && (ez < 0 || ez >= g.res[2])))
+                    continue;
+                float hx = (float)(g.ax[0][ex + 1] - g.ax[0][ex]), hy = (float)(g.ax[1][ey + 1] - g.ax[1][ey]);
+                float hz = DIM == 3 ? (float)(g.ax[2][ez + 1] - g.ax[2][ez]) : 2.0f;
+                float pe = p[ex + (int64_t)g.res[0] * (ey + (int64_t)g.res[1] * ez)];
+                float a0 = 0.5f * hy * (DIM == 3 ? 0.5f * hz : 1.0f);
+                float a1 = 0.5f * hx * (DIM == 3 ? 0.5f * hz : 1.0f);
+                float a2 = 0.25f * hx * hy;
+                acc[0] += (cx ? a0 : -a0) * pe;   // node local index 1 - cx along x
+                acc[1] += (cy ? a1 : -a1) * pe;
+                if (DIM == 3) acc[2] += (cz ? a2 : -a2) * pe;
+            }
+#pragma unroll
+    for (int c = 0; c < DIM; c++) {
+        int64_t dof = n * DIM + c;
+        v[dof] = bc[dof] ? 0.f : (Dinv ? acc[c] * Dinv[dof] : acc[c]);
+    }
+}
+
+template <int DIM>
+__global__ void k_Gt32(uwg_lgeom g, const uint8_t* bc, const float* v, float* q) {
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= g.n_el) return;
+    int ex = (int)(e % g.res[0]), ey = (int)((e / g.res[0]) % g.res[1]);
+    int ez = DIM == 3 ? (int)(e / ((int64_t)g.res[0] * g.res[1])) : 0;
+    float hx = (float)(g.ax[0][ex + 1] - g.ax[0][ex]), hy = (float)(g.ax[1][ey + 1] - g.ax[1][ey]);
+    float hz = DIM == 3 ? (float)(g.ax[2][ez + 1] - g.ax[2][ez]) : 2.0f;
+    float a[3] = {0.5f * hy * (DIM == 3 ? 0.5f * hz : 1.0f), 0.5f * hx * (DIM == 3 ? 0.5f * hz : 1.0f), 0.25f * hx * hy};
+    int64_t nx = g.nx[0], ny = g.nx[1];
+    float s = 0.f;
+#pragma unroll
+    for (int n = 0; n < (DIM == 3 ? 8 : 4); n++) {
+        int64_t node = (ex + (n & 1)) + nx * ((ey + ((n >> 1) & 1)) + ny * (int64_t)(ez + ((n >> 2) & 1)));
+#pragma unroll
+        for (int i = 0; i < DIM; i++) {
+            int64_t dof = node * DIM + i;
+            float ge = ((n >> i) & 1) ? -a[i] : a[i];
+            s += bc[dof] ? 0.f : ge * v[dof];
+        }
+    }
+    q[e] = s;
+}
+
+template <int DIM>
+__global__ void k_Ldiag32(uwg_lgeom g, const uint8_t* bc, const float* Dinv, float* out) {
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= g.n_el) return;
+    int ex = (int)(e % g.res[0]), ey = (int)((e / g.res[0]) % g.res[1]);
+    int ez = DIM == 3 ? (int)(e / ((int64_t)g.res[0] * g.res[1])) : 0;
+    float hx = (float)(g.ax[0][ex + 1] - g.ax[0][ex]), hy = (float)(g.ax[1][ey + 1] - g.ax[1][ey]);
+    float hz = DIM == 3 ? (float)(g.ax[2][ez + 1] - g.ax[2][ez]) : 2.0f;
+    float a[3] = {0.5f * hy * (DIM == 3 ? 0.5f * hz : 1.0f), 0.5f * hx * (DIM == 3 ? 0.5f * hz : 1.0f), 0.25f * hx * hy};
+    int64_t nx = g.nx[0], ny = g.nx[1];
+    float s = 0.f;
+    for (int n = 0; n < (DIM == 3 ? 8 : 4); n++) {
+        int64_t node = (ex + (n & 1)) + nx * ((ey + ((n >> 1) & 1)) + ny * (int64_t)(ez + ((n >> 2) & 1)));
+        for (int i = 0; i < DIM; i++) {
+            int64_t dof = node * DIM + i;
+            if (!bc[dof]) s += a[i] * a[i] * Dinv[dof];
+        }
+    }
+    out[e] = s > 0.f ? s : 1.f;
+}
+
+__global__ void k_winv(int64_t n, const double* diag, const uint8_t* bc, float* out) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = bc[i] ? 0.f : (float)(1.0 / sqrt(diag[i]));
+}
+
+template <int DIM>
+__global__ void k_cell_restrict32(uwg_lgeom gf, uwg_lgeom gc, const float* rf, float* rc) {
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= gc.n_el) return;
+    int ex = (int)(e % gc.res[0]), ey = (int)((e / gc.res[0]) % gc.res[1]);
+    int ez = DIM == 3 ? (int)(e / ((int64_t)gc.res[0] * gc.res[1])) : 0;
+    float s = 0.f;
+    for (int cz = 0; cz < (DIM == 3 ? 2 : 1); cz++)
+        for (int cy = 0; cy < 2; cy++)
+            for (int cx = 0; cx < 2; cx++)
+                s += rf[(2 * ex + cx) + (int64_t)gf.res[0] * ((2 * ey + cy) + (int64_t)gf.res[1] * (2 * ez + cz))];
+    rc[e] = s;
+}
+
+template <int DIM>
+__global__ void k_cell_prolong_add32(uwg_lgeom gf, uwg_lgeom gc, const float* xc, float* xf) {
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= gf.n_el) return;
+    int ex = (int)(e % gf.res[0]), ey = (int)((e / gf.res[0]) % gf.res[1]);
+    int ez = DIM == 3 ? (int)(e / ((int64_t)gf.res[0] * gf.res[1])) : 0;
+    xf[e] += xc[(ex >> 1) + (int64_t)gc.res[0] * ((ey >> 1) + (int64_t)gc.res[1] * (ez >> 1))];
+}
+
+#define DIMCALL(KERN, GRID, ...)                                                        \
+    do {                                                                                 \
+        if (c->dim == 3) KERN<3><<<GRID, 256, 0, c->stream>>>(__VA_ARGS__);             \
+        else KERN<2><<<GRID, 256, 0, c->stream>>>(__VA_ARGS__);                         \
+    } while (0)
+
+int uwg_ops_G32(uwg_ctx* c, int l, const float* Dinv, const float* p, float* v) {
+    uwg_lgeom g = uwg_level_geom(c, l);
+    DIMCALL(k_gradG32, nblk(g.n_nodes), g, c->lev[l].bc, p, Dinv, v);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+int uwg_ops_Gt32(uwg_ctx* c, int l, const float* v, float* q) {
+    uwg_lgeom g = uwg_level_geom(c, l);
+    DIMCALL(k_Gt32, nblk(g.n_el), g, c->lev[l].bc, v, q);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+int uwg_ops_applyL32(uwg_ctx* c, int l, const float* Dinv, const float* p, float* q, float* vtmp) {
+    int rc = uwg_ops_G32(c, l, Dinv, p, vtmp);
+    return rc ? rc : uwg_ops_Gt32(c, l, vtmp, q);
+}
+int uwg_ops_Ldiag32(uwg_ctx* c, int l, const float* Dinv, float* out) {
+    uwg_lgeom g = uwg_level_geom(c, l);
+    DIMCALL(k_Ldiag32, nblk(g.n_el), g, c->lev[l].bc, Dinv, out);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+int uwg_ops_winv(uwg_ctx* c, int l, float* out) {
+    const uwg_level& L = c->lev[l];
+    k_winv<<<nblk(L.n_dof), 256, 0, c->stream>>>(L.n_dof, L.diag64, L.bc, out);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+int uwg_ops_cell_restrict32(uwg_ctx* c, int lc, const float* rf, float* rc_) {
+    uwg_lgeom gf = uwg_level_geom(c, lc - 1), gc = uwg_level_geom(c, lc);
+    DIMCALL(k_cell_restrict32, nblk(gc.n_el), gf, gc, rf, rc_);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+int uwg_ops_cell_prolong_add32(uwg_ctx* c, int lc, const float* xc, float* xf) {
+    uwg_lgeom gf = uwg_level_geom(c, lc - 1), gc = uwg_level_geom(c, lc);
+    DIMCALL(k_cell_prolong_add32, nblk(gf.n_el), gf, gc, xc, xf);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
 }
 
 // Pressure Laplacian of the scaled BFBt Schur preconditioner on level l:
@@ -538,13 +813,12 @@ __global__ void k_cell_prolong_add(uwg_lgeom gf, uwg_lgeom gc, const double* xc,
 int uwg_ops_applyL(uwg_ctx* c, int l, const double* p, double* q, double* vtmp) {
     const uwg_level& L = c->lev[l];
     uwg_lgeom g = uwg_level_geom(c, l);
-    vk_zero<double>(c->stream, L.n_dof, vtmp);
     if (c->dim == 3) {
-        k_applyG<3><<<nblk(L.n_el), 256, 0, c->stream>>>(g, L.bc, p, vtmp);
-        k_applyGt_scaled<3><<<nblk(L.n_el), 256, 0, c->stream>>>(g, L.bc, L.diag64, vtmp, q);
+        k_gradG_nodes<3><<<nblk(L.n_nodes), 256, 0, c->stream>>>(g, L.bc, p, L.diag64, vtmp);
+        k_applyGt<3><<<nblk(L.n_el), 256, 0, c->stream>>>(g, L.bc, 0, vtmp, q);
     } else {
-        k_applyG<2><<<nblk(L.n_el), 256, 0, c->stream>>>(g, L.bc, p, vtmp);
-        k_applyGt_scaled<2><<<nblk(L.n_el), 256, 0, c->stream>>>(g, L.bc, L.diag64, vtmp, q);
+        k_gradG_nodes<2><<<nblk(L.n_nodes), 256, 0, c->stream>>>(g, L.bc, p, L.diag64, vtmp);
+        k_applyGt<2><<<nblk(L.n_el), 256, 0, c->stream>>>(g, L.bc, 0, vtmp, q);
     }
     UWG_CUDA(c, cudaGetLastError());
     return UWG_OK;
@@ -577,9 +851,8 @@ int uwg_ops_cell_prolong_add(uwg_ctx* c, int lc, const double* xc, double* xf) {
 
 int uwg_ops_applyG(uwg_ctx* c, const double* p, double* y) {
     uwg_lgeom g = uwg_level_geom(c, 0);
-    vk_zero<double>(c->stream, c->n_vdof, y);
-    if (c->dim == 3) k_applyG<3><<<nblk(c->n_el), 256, 0, c->stream>>>(g, c->bc, p, y);
-    else k_applyG<2><<<nblk(c->n_el), 256, 0, c->stream>>>(g, c->bc, p, y);
+    if (c->dim == 3) k_gradG_nodes<3><<<nblk(c->n_nodes), 256, 0, c->stream>>>(g, c->bc, p, nullptr, y);
+    else k_gradG_nodes<2><<<nblk(c->n_nodes), 256, 0, c->stream>>>(g, c->bc, p, nullptr, y);
     UWG_CUDA(c, cudaGetLastError());
     return UWG_OK;
 }
@@ -1020,6 +1293,14 @@ template <typename T> void vk_axpby(cudaStream_t s, int64_t n, T a, const T* x, 
 template <typename T> void vk_scale(cudaStream_t s, int64_t n, T a, T* y) { if (n) vk_scale_k<T><<<nblk(n), 256, 0, s>>>(n, a, y); }
 template <typename T> void vk_zero(cudaStream_t s, int64_t n, T* y) { if (n) cudaMemsetAsync(y, 0, sizeof(T) * n, s); }
 template <typename T> void vk_mask(cudaStream_t s, int64_t n, const uint8_t* bc, T* y) { if (n) vk_mask_k<T><<<nblk(n), 256, 0, s>>>(n, bc, y); }
+__global__ void vk_mulmask_k(int64_t n, const float* w, float* y) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) y[i] *= w[i];
+}
+// y *= w (w is zero on Dirichlet dofs)
+void vk_pointwise_mul_mask(cudaStream_t s, int64_t n, const float* w, float* y) {
+    if (n) vk_mulmask_k<<<nblk(n), 256, 0, s>>>(n, w, y);
+}
 template <typename T> void vk_cheb(cudaStream_t s, int64_t n, const T* b, const T* t, const T* diag, T a, T c, T* d,
                                    T* x, int first, int x_zero) {
     if (n) vk_cheb_k<T><<<nblk(n), 256, 0, s>>>(n, b, t, diag, a, c, d, x, first, x_zero);

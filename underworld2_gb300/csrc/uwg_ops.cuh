@@ -37,6 +37,13 @@ int uwg_ops_schur_pc(uwg_ctx* c, const double* r, double* z);    // z = Shat^-1 
 int uwg_ops_applyL(uwg_ctx* c, int l, const double* p, double* q, double* vtmp);  // q = G^T D^-1 G p
 int uwg_ops_Ldiag(uwg_ctx* c, int l, double* out);
 int uwg_ops_cell_restrict(uwg_ctx* c, int lc, const double* rf, double* rc);
+int uwg_ops_G32(uwg_ctx* c, int l, const float* Dinv, const float* p, float* v);
+int uwg_ops_Gt32(uwg_ctx* c, int l, const float* v, float* q);
+int uwg_ops_applyL32(uwg_ctx* c, int l, const float* Dinv, const float* p, float* q, float* vtmp);
+int uwg_ops_Ldiag32(uwg_ctx* c, int l, const float* Dinv, float* out);
+int uwg_ops_winv(uwg_ctx* c, int l, float* out);
+int uwg_ops_cell_restrict32(uwg_ctx* c, int lc, const float* rf, float* rc);
+int uwg_ops_cell_prolong_add32(uwg_ctx* c, int lc, const float* xc, float* xf);
 int uwg_ops_cell_prolong_add(uwg_ctx* c, int lc, const double* xc, double* xf);
 int uwg_ops_apply_C(uwg_ctx* c, const double* p, double* q);     // q = Mp p (compressibility)
 int uwg_ops_element_matrices(uwg_ctx* c, int64_t el, double* Ke, double* fe, double* Ge, double* Se);
@@ -56,4 +63,5 @@ template <typename T> void vk_pointwise_div(cudaStream_t s, int64_t n, const T* 
 template <typename T> void vk_dots(cudaStream_t s, int64_t n, int k, const T* const* a, const T* const* b,
                                    double* dst);
 void vk_mdot(cudaStream_t s, int64_t n, int k, const double* const* V, const double* w, double* dst);
+void vk_pointwise_mul_mask(cudaStream_t s, int64_t n, const float* w, float* y);
 void vk_maxpy(cudaStream_t s, int64_t n, int k, const double* coef_dev, const double* const* V, double* y);

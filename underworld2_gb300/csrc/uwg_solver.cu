@@ -46,13 +46,15 @@ struct Work {
     double *p_tmp, *p_tmp2, *hhat;
     double* coef;                             // device coefficients
     int restart = 0;
-    // pressure multigrid (scaled BFBt)
-    LevelVecs<double> pv[UWG_MAXLEV];
-    double* pvel[UWG_MAXLEV];                 // velocity-sized temp per level
-    double* Ldiag[UWG_MAXLEV];
+    // pressure multigrid of the weighted BFBt preconditioner (FP32)
+    LevelVecs<float> pv[UWG_MAXLEV];
+    float* pvel[UWG_MAXLEV];                  // velocity-sized temp per level
+    float* Ldiag[UWG_MAXLEV];
+    float* Dinv[UWG_MAXLEV];                  // 1/sqrt(diag K) per level
     double Lmax[UWG_MAXLEV];
-    double *pcg_r, *pcg_z, *pcg_p, *pcg_q, *bf_y, *bf_m, *bf_v1, *bf_v2;
+    float *pcg_r, *pcg_z, *pcg_p, *pcg_q, *bf_r, *bf_y, *bf_m, *bf_z, *bf_v1, *bf_v2;
     int lsolve_its = 0;
+    double t_pc = 0.0, t_schur = 0.0;          // seconds in the Schur preconditioner / operator
     // CUDA graphs of the V-cycles (captured at setup, replayed by the Krylov loops)
     cudaStream_t gstream = nullptr;
     cudaGraphExec_t g_v64 = nullptr, g_v32 = nullptr, g_pv = nullptr;
@@ -93,15 +95,17 @@ int work_init(uwg_ctx* c, int restart) {
         w->coef = dalloc<double>(c, 256);
         for (int l = 0; l < c->nlev; l++) {
             int64_t ne = c->lev[l].n_el;
-            w->pv[l] = {dalloc<double>(c, ne), dalloc<double>(c, ne), dalloc<double>(c, ne), dalloc<double>(c, ne), dalloc<double>(c, ne)};
-            w->pvel[l] = dalloc<double>(c, c->lev[l].n_dof);
-            w->Ldiag[l] = dalloc<double>(c, ne);
+            w->pv[l] = {dalloc<float>(c, ne), dalloc<float>(c, ne), dalloc<float>(c, ne), dalloc<float>(c, ne), dalloc<float>(c, ne)};
+            w->pvel[l] = dalloc<float>(c, c->lev[l].n_dof);
+            w->Ldiag[l] = dalloc<float>(c, ne);
+            w->Dinv[l] = dalloc<float>(c, c->lev[l].n_dof);
             w->Lmax[l] = 1.0;
         }
-        w->pcg_r = dalloc<double>(c, np); w->pcg_z = dalloc<double>(c, np);
-        w->pcg_p = dalloc<double>(c, np); w->pcg_q = dalloc<double>(c, np);
-        w->bf_y = dalloc<double>(c, np); w->bf_m = dalloc<double>(c, np);
-        w->bf_v1 = dalloc<double>(c, nv); w->bf_v2 = dalloc<double>(c, nv);
+        w->pcg_r = dalloc<float>(c, np); w->pcg_z = dalloc<float>(c, np);
+        w->pcg_p = dalloc<float>(c, np); w->pcg_q = dalloc<float>(c, np);
+        w->bf_r = dalloc<float>(c, np); w->bf_y = dalloc<float>(c, np);
+        w->bf_m = dalloc<float>(c, np); w->bf_z = dalloc<float>(c, np);
+        w->bf_v1 = dalloc<float>(c, nv); w->bf_v2 = dalloc<float>(c, nv);
     }
     while ((int)w->V.size() < restart + 1) w->V.push_back(dalloc<double>(c, np));
     while ((int)w->Z.size() < restart) w->Z.push_back(dalloc<double>(c, np));
@@ -143,7 +147,7 @@ int chebyshev(uwg_ctx* c, int l, const T* b, T* x, int deg, bool x_zero) {
     int64_t n = L.n_dof;
     cudaStream_t s = c->stream;
     double lmax = L.lmax64;
-    double alpha = 0.1 * lmax, beta = 1.1 * lmax;
+    double alpha = 0.1 * lmax, beta = 1.2 * lmax;
     double theta = 0.5 * (beta + alpha), delta = 0.5 * (beta - alpha);
     double sigma = theta / delta, rho = 1.0 / sigma;
     int rc;
@@ -303,52 +307,53 @@ int velocity_solve(uwg_ctx* c, const SolveCfg& cfg, const double* b, double* x, 
 
 
 // ---------------------------------------------------------------------------
-// Scaled BFBt Schur preconditioner (May & Moresi, PEPI 2008):
-//   S^-1 ~ L^-1 (G^T D^-1 K D^-1 G) L^-1,  L = G^T D^-1 G,  D = diag(K).
-// L is a cell-centred pressure Laplacian; its solves use CG preconditioned by a
-// cell multigrid V-cycle whose level operators are G_l^T D_l^-1 G_l with the
-// velocity hierarchy's diagonals (Chebyshev-Jacobi smoothing).
+// Weighted BFBt Schur preconditioner (scaled BFBt, May & Moresi, PEPI 2008,
+// with the sqrt-diagonal weight of w-BFBt, Rudi et al., SISC 2017):
+//   S^-1 ~ L^-1 (G^T W K W G) L^-1,  L = G^T W G,  W = diag(K)^-1/2.
+// The square-root weight narrows the coefficient range of L (1e5 viscosity
+// contrast -> ~300), which both improves the preconditioner and makes L easy
+// for a cell-centred multigrid.  All of it runs in FP32: it is a
+// preconditioner inside flexible GMRES, whose residuals stay FP64.
 // ---------------------------------------------------------------------------
-int cheb_L(uwg_ctx* c, int l, const double* b, double* x, int deg, bool x_zero) {
+int cheb_L(uwg_ctx* c, int l, const float* b, float* x, int deg, bool x_zero) {
     Work* w = work_of(c);
-    LevelVecs<double>& v = w->pv[l];
+    LevelVecs<float>& v = w->pv[l];
     int64_t n = c->lev[l].n_el;
     cudaStream_t s = c->stream;
     double lmax = w->Lmax[l];
-    double alpha = 0.1 * lmax, beta = 1.1 * lmax;
+    double alpha = 0.1 * lmax, beta = 1.2 * lmax;
     double theta = 0.5 * (beta + alpha), delta = 0.5 * (beta - alpha);
     double sigma = theta / delta, rho = 1.0 / sigma;
     int rc;
-    if (!x_zero && (rc = uwg_ops_applyL(c, l, x, v.t, w->pvel[l]))) return rc;
-    vk_cheb<double>(s, n, b, x_zero ? nullptr : v.t, w->Ldiag[l], 1.0 / theta, 0.0, v.d, x, 1, x_zero ? 1 : 0);
+    if (!x_zero && (rc = uwg_ops_applyL32(c, l, w->Dinv[l], x, v.t, w->pvel[l]))) return rc;
+    vk_cheb<float>(s, n, b, x_zero ? nullptr : v.t, w->Ldiag[l], (float)(1.0 / theta), 0.f, v.d, x, 1, x_zero ? 1 : 0);
     for (int i = 1; i < deg; i++) {
-        if ((rc = uwg_ops_applyL(c, l, x, v.t, w->pvel[l]))) return rc;
+        if ((rc = uwg_ops_applyL32(c, l, w->Dinv[l], x, v.t, w->pvel[l]))) return rc;
         double rho1 = 1.0 / (2.0 * sigma - rho);
-        vk_cheb<double>(s, n, b, v.t, w->Ldiag[l], 2.0 * rho1 / delta, rho1 * rho, v.d, x, 0, 0);
+        vk_cheb<float>(s, n, b, v.t, w->Ldiag[l], (float)(2.0 * rho1 / delta), (float)(rho1 * rho), v.d, x, 0, 0);
         rho = rho1;
     }
     return UWG_OK;
 }
 
-int pvcycle(uwg_ctx* c, int l, const double* b, double* x) {
+int pvcycle(uwg_ctx* c, int l, const float* b, float* x) {
     Work* w = work_of(c);
     cudaStream_t s = c->stream;
     int64_t n = c->lev[l].n_el;
     int rc;
-    (void)s; (void)n;
     if (l == c->nlev - 1) return cheb_L(c, l, b, x, 8, true);
-    LevelVecs<double>& v = w->pv[l];
-    LevelVecs<double>& vc = w->pv[l + 1];
+    LevelVecs<float>& v = w->pv[l];
+    LevelVecs<float>& vc = w->pv[l + 1];
     if ((rc = cheb_L(c, l, b, x, 3, true))) return rc;
-    if ((rc = uwg_ops_applyL(c, l, x, v.t, w->pvel[l]))) return rc;
-    vk_axpby<double>(s, n, 1.0, b, -1.0, v.t);
-    if ((rc = uwg_ops_cell_restrict(c, l + 1, v.t, vc.b))) return rc;
+    if ((rc = uwg_ops_applyL32(c, l, w->Dinv[l], x, v.t, w->pvel[l]))) return rc;
+    vk_axpby<float>(s, n, 1.f, b, -1.f, v.t);
+    if ((rc = uwg_ops_cell_restrict32(c, l + 1, v.t, vc.b))) return rc;
     if ((rc = pvcycle(c, l + 1, vc.b, vc.x))) return rc;
-    if ((rc = uwg_ops_cell_prolong_add(c, l + 1, vc.x, x))) return rc;
+    if ((rc = uwg_ops_cell_prolong_add32(c, l + 1, vc.x, x))) return rc;
     return cheb_L(c, l, b, x, 3, false);
 }
 
-int run_pvcycle(uwg_ctx* c, const double* b, double* x) {
+int run_pvcycle(uwg_ctx* c, const float* b, float* x) {
     Work* w = work_of(c);
     if (w->g_pv && b == w->pcg_r && x == w->pcg_z) {
         UWG_CUDA(c, cudaGraphLaunch(w->g_pv, c->stream));
@@ -389,40 +394,41 @@ int capture_cycles(uwg_ctx* c, int deg) {
     return UWG_OK;
 }
 
-// x = L^-1 b by multigrid-preconditioned CG from zero, to rtol
-int lsolve(uwg_ctx* c, const double* b, double* x, double rtol, int maxit) {
+// x = L^-1 b by multigrid-preconditioned CG from zero, to rtol (FP32 vectors,
+// FP64 reductions)
+int lsolve(uwg_ctx* c, const float* b, float* x, double rtol, int maxit) {
     Work* w = work_of(c);
     cudaStream_t s = c->stream;
     int64_t n = c->n_pdof;
     int rc;
-    double *r = w->pcg_r, *z = w->pcg_z, *p = w->pcg_p, *q = w->pcg_q;
-    vk_zero<double>(s, n, x);
-    vk_copy<double>(s, n, b, r);
+    float *r = w->pcg_r, *z = w->pcg_z, *p = w->pcg_p, *q = w->pcg_q;
+    vk_zero<float>(s, n, x);
+    vk_copy<float>(s, n, b, r);
     if ((rc = run_pvcycle(c, r, z))) return rc;
-    vk_copy<double>(s, n, z, p);
+    vk_copy<float>(s, n, z, p);
     double d2[2];
-    const double* a2[2] = {r, r};
-    const double* b2[2] = {z, r};
-    if ((rc = dots<double>(c, n, 2, a2, b2, d2))) return rc;
+    const float* a2[2] = {r, r};
+    const float* b2[2] = {z, r};
+    if ((rc = dots<float>(c, n, 2, a2, b2, d2))) return rc;
     double bn = std::sqrt(d2[1]), rz = d2[0];
     if (bn == 0.0) return UWG_OK;
     for (int it = 1; it <= maxit; it++) {
-        if ((rc = uwg_ops_applyL(c, 0, p, q, w->pvel[0]))) return rc;
+        if ((rc = uwg_ops_applyL32(c, 0, w->Dinv[0], p, q, w->pvel[0]))) return rc;
         double pq;
-        const double* a1[1] = {p};
-        const double* b1[1] = {q};
-        if ((rc = dots<double>(c, n, 1, a1, b1, &pq))) return rc;
+        const float* a1[1] = {p};
+        const float* b1[1] = {q};
+        if ((rc = dots<float>(c, n, 1, a1, b1, &pq))) return rc;
         w->lsolve_its++;
         if (!(pq > 0.0)) return UWG_OK;
         double alpha = rz / pq;
-        vk_axpy<double>(s, n, alpha, p, x);
-        vk_axpy<double>(s, n, -alpha, q, r);
+        vk_axpy<float>(s, n, (float)alpha, p, x);
+        vk_axpy<float>(s, n, (float)-alpha, q, r);
         if ((rc = run_pvcycle(c, r, z))) return rc;
-        if ((rc = dots<double>(c, n, 2, a2, b2, d2))) return rc;
+        if ((rc = dots<float>(c, n, 2, a2, b2, d2))) return rc;
         if (std::sqrt(d2[1]) <= rtol * bn) return UWG_OK;
         double beta = d2[0] / rz;
         rz = d2[0];
-        vk_axpby<double>(s, n, 1.0, z, beta, p);
+        vk_axpby<float>(s, n, 1.f, z, (float)beta, p);
     }
     return UWG_OK;   // a preconditioner: an inexact solve is acceptable
 }
@@ -431,17 +437,17 @@ int lsolve(uwg_ctx* c, const double* b, double* x, double rtol, int maxit) {
 int bfbt(uwg_ctx* c, const double* r, double* z, double rtol) {
     Work* w = work_of(c);
     cudaStream_t s = c->stream;
+    int64_t np = c->n_pdof, nv = c->n_vdof;
     int rc;
-    if ((rc = lsolve(c, r, w->bf_y, rtol, 200))) return rc;
-    if ((rc = uwg_ops_applyG(c, w->bf_y, w->bf_v1))) return rc;
-    vk_pointwise_div<double>(s, c->n_vdof, w->bf_v1, c->lev[0].diag64, w->bf_v1);
-    vk_mask<double>(s, c->n_vdof, c->bc, w->bf_v1);
-    if ((rc = uwg_ops_applyK<double>(c, 0, w->bf_v1, w->bf_v2))) return rc;
-    vk_mask<double>(s, c->n_vdof, c->bc, w->bf_v2);
-    vk_pointwise_div<double>(s, c->n_vdof, w->bf_v2, c->lev[0].diag64, w->bf_v2);
-    if ((rc = uwg_ops_applyGt(c, w->bf_v2, w->bf_m))) return rc;
-    if ((rc = lsolve(c, w->bf_m, z, rtol, 200))) return rc;
-    vk_scale<double>(s, c->n_pdof, -1.0, z);
+    vk_convert<double, float>(s, np, r, w->bf_r);
+    if ((rc = lsolve(c, w->bf_r, w->bf_y, rtol, 200))) return rc;
+    if ((rc = uwg_ops_G32(c, 0, w->Dinv[0], w->bf_y, w->bf_v1))) return rc;        // W G y
+    if ((rc = uwg_ops_applyK<float>(c, 0, w->bf_v1, w->bf_v2))) return rc;         // K W G y
+    vk_pointwise_mul_mask(s, nv, w->Dinv[0], w->bf_v2);                             // W K W G y
+    if ((rc = uwg_ops_Gt32(c, 0, w->bf_v2, w->bf_m))) return rc;
+    if ((rc = lsolve(c, w->bf_m, w->bf_z, rtol, 200))) return rc;
+    vk_convert<float, double>(s, np, w->bf_z, z);
+    vk_scale<double>(s, np, -1.0, z);
     return UWG_OK;
 }
 
@@ -450,24 +456,26 @@ int bfbt_setup(uwg_ctx* c) {
     cudaStream_t s = c->stream;
     int rc;
     for (int l = 0; l < c->nlev; l++) {
-        if ((rc = uwg_ops_Ldiag(c, l, w->Ldiag[l]))) return rc;
+        if ((rc = uwg_ops_winv(c, l, w->Dinv[l]))) return rc;
+        if ((rc = uwg_ops_Ldiag32(c, l, w->Dinv[l], w->Ldiag[l]))) return rc;
         int64_t n = c->lev[l].n_el;
-        LevelVecs<double>& v = w->pv[l];
-        std::vector<double> hv(n);
-        for (int64_t i = 0; i < n; i++) hv[i] = 1.0 + 0.41 * std::sin(1.37 * (double)i) + ((i & 1) ? 0.3 : -0.3);
-        UWG_CUDA(c, cudaMemcpyAsync(v.x, hv.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+        LevelVecs<float>& v = w->pv[l];
+        std::vector<float> hv(n);
+        for (int64_t i = 0; i < n; i++) hv[i] = (float)(1.0 + 0.41 * std::sin(1.37 * (double)i) + ((i & 1) ? 0.3 : -0.3));
+        UWG_CUDA(c, cudaMemcpyAsync(v.x, hv.data(), sizeof(float) * n, cudaMemcpyHostToDevice, s));
         double lam = 1.0;
-        for (int it = 0; it < 12; it++) {
-            if ((rc = uwg_ops_applyL(c, l, v.x, v.t, w->pvel[l]))) return rc;
-            vk_pointwise_div<double>(s, n, v.t, w->Ldiag[l], v.d);
+        for (int it = 0; it < 30; it++) {
+            if ((rc = uwg_ops_applyL32(c, l, w->Dinv[l], v.x, v.t, w->pvel[l]))) return rc;
+            vk_pointwise_div<float>(s, n, v.t, w->Ldiag[l], v.d);
             double d2[2];
-            const double* a[2] = {v.d, v.x};
-            if ((rc = dots<double>(c, n, 2, a, a, d2))) return rc;
+            const float* a[2] = {v.d, v.x};
+            if ((rc = dots<float>(c, n, 2, a, a, d2))) return rc;
             if (d2[0] <= 0.0 || d2[1] <= 0.0) break;
             lam = std::sqrt(d2[0] / d2[1]);
-            vk_copy<double>(s, n, v.d, v.x);
-            vk_scale<double>(s, n, 1.0 / std::sqrt(d2[0]), v.x);
+            vk_copy<float>(s, n, v.d, v.x);
+            vk_scale<float>(s, n, (float)(1.0 / std::sqrt(d2[0])), v.x);
         }
+        UWG_CUDA(c, cudaStreamSynchronize(s));   // the host vector must outlive its copy
         w->Lmax[l] = lam;
     }
     return UWG_OK;
@@ -502,7 +510,7 @@ int uwg_solver_estimate(uwg_ctx* c, int l) {
     UWG_CUDA(c, cudaMemcpyAsync(v.x, h.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
     vk_mask<double>(s, n, L.bc, v.x);
     double lam = 0.0;
-    for (int it = 0; it < 12; it++) {
+    for (int it = 0; it < 30; it++) {
         if ((rc = uwg_ops_applyK<double>(c, l, v.x, v.t))) return rc;
         vk_mask<double>(s, n, L.bc, v.t);
         vk_pointwise_div<double>(s, n, v.t, L.diag64, v.d);
@@ -594,13 +602,18 @@ int fgmres(uwg_ctx* c, const SolveCfg& cfg, const double* rhs, double* p, double
         bool done = false;
         for (; j < m && total < maxit; j++) {
             // Z_j = M^-1 V_j: -S^^-1 (the reference's Uzawa term) or scaled BFBt
+            double tp0 = now();
             if (cfg.schur_pc == 1) {
                 if ((rc = bfbt(c, w->V[j], w->Z[j], cfg.schur_pc_rtol))) return rc;
+                cudaStreamSynchronize(s);
+                w->t_pc += now() - tp0;
             } else {
                 if ((rc = uwg_ops_schur_pc(c, w->V[j], w->Z[j]))) return rc;
                 vk_scale<double>(s, n, -1.0, w->Z[j]);
             }
+            double ts0 = now();
             if ((rc = schur_apply(c, cfg, w->Z[j], w->V[j + 1], inner_its, refine))) return rc;
+            w->t_schur += now() - ts0;
             total++;
             // classical Gram-Schmidt, two passes
             std::vector<double> hcol(j + 1, 0.0);
@@ -736,6 +749,7 @@ extern "C" int uwg_stokes_solve(uwg_ctx* c, const uwg_solve_opts* o, double* u, 
     vk_axpby<double>(s, np, 1.0, c->h, -1.0, w->hhat);
     // 3. pressure solve: S p = h^, S = C - G^T A^-1 G
     w->lsolve_its = 0;
+    w->t_pc = w->t_schur = 0.0;
     int outer = 0, inner_its = 0;
     // the full-system target ||[f - Ku - Gp; h - G^T u]|| <= rtol ||[f; h]|| is met once the
     // Schur residual is below it (the back-solve adds inner_rtol-level error)
@@ -753,9 +767,16 @@ extern "C" int uwg_stokes_solve(uwg_ctx* c, const uwg_solve_opts* o, double* u, 
                 &S.refinement_steps);
     S.pressure_its = outer;
     S.schur_pc_its = w->lsolve_its;
+    S.schur_pc_time = w->t_pc;
+    S.schur_op_time = w->t_schur;
     S.velocity_pressuresolve_its = inner_its;
     S.outer_reason = rc ? -1 : 1;
-    if (rc) return rc;
+    if (rc) {
+        S.velocity_total_its = S.velocity_presolve_its + S.velocity_pressuresolve_its;
+        S.total_time = now() - t0;
+        if (st) *st = S;   // partial statistics of the failed solve
+        return rc;
+    }
     double t3 = now();
     S.pressure_time = t3 - t2;
     // 4. back-solve: A u = b - G p
