@@ -158,7 +158,7 @@ def run_gpu(args):
     npart = x0.shape[0]
     u = ctx.zeros(ctx.n_vdof)
     p = ctx.zeros(ctx.n_pdof)
-    opts = dict(rtol=1e-8, inner_rtol=args.inner_rtol, outer_rtol=args.outer_rtol, smooth_steps=3, restart=50,
+    opts = dict(rtol=1e-8, inner_rtol=args.inner_rtol, outer_rtol=args.outer_rtol, smooth_steps=3, restart=120,
                 schur_pc=args.schur_pc, schur_pc_rtol=args.bfbt_rtol, max_outer=args.max_outer)
     ev = lambda: torch.cuda.Event(enable_timing=True)
 

@@ -1217,6 +1217,22 @@ __global__ void k_dense_mv(int64_t n, const T* Ainv, const T* b, T* x) {
     if (lane == 0) x[i] = s;
 }
 
+int uwg_ops_dense_invert(uwg_ctx* c, int64_t n, double* A, double* B) {
+    k_dense_invert<<<1, 1024, 0, c->stream>>>(n, A, B);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+int uwg_ops_to_f32(uwg_ctx* c, int64_t n, const double* a, float* b) {
+    k_to_f32<<<nblk(n), 256, 0, c->stream>>>(n, a, b);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+int uwg_ops_dense_mv32(uwg_ctx* c, int64_t n, const float* Ainv, const float* b, float* x) {
+    k_dense_mv<float><<<nblk(n * 32, 256), 256, 0, c->stream>>>(n, Ainv, b, x);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
 template <typename T>
 int uwg_ops_dense_solve(uwg_ctx* c, int l, const T* b, T* x) {
     uwg_level& L = c->lev[l];

@@ -48,6 +48,22 @@ int uwg_ops_cell_prolong_add(uwg_ctx* c, int lc, const double* xc, double* xf);
 int uwg_ops_apply_C(uwg_ctx* c, const double* p, double* q);     // q = Mp p (compressibility)
 int uwg_ops_element_matrices(uwg_ctx* c, int64_t el, double* Ke, double* fe, double* Ge, double* Se);
 
+int uwg_ops_dense_invert(uwg_ctx* c, int64_t n, double* A, double* B);   // B = A^-1 (A destroyed)
+int uwg_ops_to_f32(uwg_ctx* c, int64_t n, const double* a, float* b);
+int uwg_ops_dense_mv32(uwg_ctx* c, int64_t n, const float* Ainv, const float* b, float* x);
+
+// Pressure-Laplacian multigrid of the weighted BFBt preconditioner (uwg_pmg.cu).
+// Level 0 has one unknown per cell, coarser levels two (smooth, checkerboard).
+int uwg_pmg_ncomp(int l);
+int64_t uwg_pmg_stencil_size(const uwg_ctx* c, int l);
+// level 0: stencil of G^T W G from W0; level l > 0: Galerkin product of st_fine
+int uwg_pmg_stencil(uwg_ctx* c, int l, const float* W0, const float* st_fine, float* st);
+int uwg_pmg_apply(uwg_ctx* c, int l, const float* st, const float* x, float* y);
+int uwg_pmg_diag(uwg_ctx* c, int l, const float* st, float* d);
+int uwg_pmg_restrict(uwg_ctx* c, int lc, const float* rf, float* rc);
+int uwg_pmg_prolong_add(uwg_ctx* c, int lc, const float* xc, float* xf);
+int uwg_pmg_dense_inverse(uwg_ctx* c, int l, const float* st, float* inv32);
+
 // Vector kernels ---------------------------------------------------------------
 template <typename T> void vk_copy(cudaStream_t s, int64_t n, const T* x, T* y);
 template <typename A, typename B> void vk_convert(cudaStream_t s, int64_t n, const A* x, B* y);

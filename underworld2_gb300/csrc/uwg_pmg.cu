@@ -1,0 +1,370 @@
+// Multigrid for the pressure Laplacian L = G^T W G of the weighted BFBt Schur
+// preconditioner on Q1/dQ0 meshes.
+//
+// Q1/dQ0 is not inf-sup stable: pressure fields of the form
+// (-1)^(i+j+k) f(x) lie close to the kernel of G (exactly in it away from the
+// walls when f depends on one coordinate only), so L has a whole branch of
+// small eigenvalues on checkerboard-modulated smooth fields.  A multigrid with
+// piecewise-constant coarse spaces cannot represent that branch and its CG
+// iteration count grows with the mesh.  This hierarchy carries two unknowns
+// per coarse cell from the first coarsening on: a smooth part and a
+// checkerboard part, with prolongation
+//     p_fine(i) = s(I) + (-1)^(i_x+i_y+i_z) c(I),      I = parent of i,
+// and Galerkin coarse operators A_{l+1} = P^T A_l P.  Every level is stored as
+// an explicit 3^dim-point cell stencil (2x2 blocks on coarse levels) in
+// structure-of-arrays form, so an apply reads each coefficient once, coalesced.
+//
+// Layouts (n = cells of the level):
+//   level 0  : st[o * n + e]                        = L[e, e + off(o)]
+//   level >=1: st[((o * 2 + a) * 2 + b) * n + e]    = A[(a, e), (b, e + off(o))]
+//   vectors  : level 0 x[e];  level >= 1 x[a * n + e]  (a = 0 smooth, 1 checkerboard)
+//   off(o)   : o = (dx+1) + 3 (dy+1) + 9 (dz+1),  d* in {-1, 0, 1}
+#include "uwg_ops.cuh"
+
+namespace {
+
+inline unsigned nblk(int64_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
+
+template <int DIM>
+__device__ __forceinline__ void cell_xyz(const uwg_lgeom& g, int64_t e, int& ex, int& ey, int& ez) {
+    ex = (int)(e % g.res[0]);
+    ey = (int)((e / g.res[0]) % g.res[1]);
+    ez = DIM == 3 ? (int)(e / ((int64_t)g.res[0] * g.res[1])) : 0;
+}
+
+// |integral of dN/dx_d| over cell (ex, ey, ez) for each Q1 node (the sign
+// is + for the node on the low side of axis d, - on the high side)
+template <int DIM>
+__device__ __forceinline__ void g_coef(const uwg_lgeom& g, int ex, int ey, int ez, float* a) {
+    float hx = (float)(g.ax[0][ex + 1] - g.ax[0][ex]), hy = (float)(g.ax[1][ey + 1] - g.ax[1][ey]);
+    float hz = DIM == 3 ? (float)(g.ax[2][ez + 1] - g.ax[2][ez]) : 2.0f;
+    a[0] = 0.5f * hy * (DIM == 3 ? 0.5f * hz : 1.0f);
+    a[1] = 0.5f * hx * (DIM == 3 ? 0.5f * hz : 1.0f);
+    a[2] = 0.25f * hx * hy;
+}
+
+template <int DIM>
+__device__ __forceinline__ bool in_grid(const uwg_lgeom& g, int x, int y, int z) {
+    return x >= 0 && x < g.res[0] && y >= 0 && y < g.res[1] && (DIM == 2 || (z >= 0 && z < g.res[2]));
+}
+
+// Level-0 stencil of L = G^T W G; W is zero on Dirichlet dofs.
+template <int DIM>
+__global__ void k_pst0(uwg_lgeom g, const float* __restrict__ W, float* __restrict__ st) {
+    constexpr int NO = DIM == 3 ? 27 : 9;
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= g.n_el) return;
+    int ex, ey, ez;
+    cell_xyz<DIM>(g, e, ex, ey, ez);
+    float a[3];
+    g_coef<DIM>(g, ex, ey, ez, a);
+    float acc[NO];
+#pragma unroll
+    for (int o = 0; o < NO; o++) acc[o] = 0.f;
+#pragma unroll
+    for (int ln = 0; ln < (1 << DIM); ln++) {
+        const int lx = ln & 1, ly = (ln >> 1) & 1, lz = DIM == 3 ? (ln >> 2) & 1 : 0;
+        int64_t node = (ex + lx) + (int64_t)g.nx[0] * ((ey + ly) + (int64_t)g.nx[1] * (ez + lz));
+        float w[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+        for (int d = 0; d < DIM; d++) w[d] = W[node * DIM + d];
+        const float ge0 = lx ? -a[0] : a[0], ge1 = ly ? -a[1] : a[1], ge2 = lz ? -a[2] : a[2];
+#pragma unroll
+        for (int cn = 0; cn < (1 << DIM); cn++) {
+            const int cx = cn & 1, cy = (cn >> 1) & 1, cz = DIM == 3 ? (cn >> 2) & 1 : 0;
+            const int fx = ex + lx - 1 + cx, fy = ey + ly - 1 + cy, fz = DIM == 3 ? ez + lz - 1 + cz : 0;
+            if (!in_grid<DIM>(g, fx, fy, fz)) continue;
+            float b[3];
+            g_coef<DIM>(g, fx, fy, fz, b);
+            // the node is local corner (1-cx, 1-cy, 1-cz) of the neighbour
+            float s = w[0] * ge0 * (cx ? b[0] : -b[0]) + w[1] * ge1 * (cy ? b[1] : -b[1]);
+            if (DIM == 3) s += w[2] * ge2 * (cz ? b[2] : -b[2]);
+            acc[(lx + cx) + 3 * (ly + cy) + (DIM == 3 ? 9 * (lz + cz) : 0)] += s;
+        }
+    }
+#pragma unroll
+    for (int o = 0; o < NO; o++) st[o * g.n_el + e] = acc[o];
+}
+
+// Coarse offset index of fine offset (o) seen from child (c) of a coarse cell:
+// floor((c + o) / 2) per axis.
+__host__ __device__ constexpr int coarse_off(int c, int o) { return ((c + o + 2) >> 1) - 1; }
+
+// Galerkin level 0 (one unknown per cell) -> level 1 (smooth + checkerboard).
+template <int DIM>
+__global__ void k_pgal01(uwg_lgeom gf, uwg_lgeom gc, const float* __restrict__ st0, float* __restrict__ st1) {
+    constexpr int NO = DIM == 3 ? 27 : 9;
+    int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (I >= gc.n_el) return;
+    int X, Y, Z;
+    cell_xyz<DIM>(gc, I, X, Y, Z);
+    float acc[NO][4];
+#pragma unroll
+    for (int o = 0; o < NO; o++)
+#pragma unroll
+        for (int k = 0; k < 4; k++) acc[o][k] = 0.f;
+    const int64_t nf = gf.n_el;
+#pragma unroll
+    for (int cn = 0; cn < (1 << DIM); cn++) {
+        const int cx = cn & 1, cy = (cn >> 1) & 1, cz = DIM == 3 ? (cn >> 2) & 1 : 0;
+        const int64_t i = (2 * X + cx) + (int64_t)gf.res[0] * ((2 * Y + cy) + (int64_t)gf.res[1] * (2 * Z + cz));
+        const float si = ((cx + cy + cz) & 1) ? -1.f : 1.f;
+#pragma unroll
+        for (int o = 0; o < NO; o++) {
+            const int ox = o % 3 - 1, oy = (o / 3) % 3 - 1, oz = DIM == 3 ? o / 9 - 1 : 0;
+            const float v = st0[o * nf + i];
+            const float sj = ((cx + ox + cy + oy + cz + oz) & 1) ? -1.f : 1.f;
+            const int O = (coarse_off(cx, ox) + 1) + 3 * (coarse_off(cy, oy) + 1) +
+                          (DIM == 3 ? 9 * (coarse_off(cz, oz) + 1) : 0);
+            acc[O][0] += v;
+            acc[O][1] += sj * v;
+            acc[O][2] += si * v;
+            acc[O][3] += si * sj * v;
+        }
+    }
+#pragma unroll
+    for (int o = 0; o < NO; o++)
+#pragma unroll
+        for (int k = 0; k < 4; k++) st1[(o * 4 + k) * gc.n_el + I] = acc[o][k];
+}
+
+// Galerkin level l -> l + 1, both with two unknowns per cell (aggregation per component).
+template <int DIM>
+__global__ void k_pgal22(uwg_lgeom gf, uwg_lgeom gc, const float* __restrict__ stf, float* __restrict__ stc) {
+    constexpr int NO = DIM == 3 ? 27 : 9;
+    int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (I >= gc.n_el) return;
+    int X, Y, Z;
+    cell_xyz<DIM>(gc, I, X, Y, Z);
+    float acc[NO][4];
+#pragma unroll
+    for (int o = 0; o < NO; o++)
+#pragma unroll
+        for (int k = 0; k < 4; k++) acc[o][k] = 0.f;
+    const int64_t nf = gf.n_el;
+#pragma unroll
+    for (int cn = 0; cn < (1 << DIM); cn++) {
+        const int cx = cn & 1, cy = (cn >> 1) & 1, cz = DIM == 3 ? (cn >> 2) & 1 : 0;
+        const int64_t i = (2 * X + cx) + (int64_t)gf.res[0] * ((2 * Y + cy) + (int64_t)gf.res[1] * (2 * Z + cz));
+#pragma unroll
+        for (int o = 0; o < NO; o++) {
+            const int ox = o % 3 - 1, oy = (o / 3) % 3 - 1, oz = DIM == 3 ? o / 9 - 1 : 0;
+            const int O = (coarse_off(cx, ox) + 1) + 3 * (coarse_off(cy, oy) + 1) +
+                          (DIM == 3 ? 9 * (coarse_off(cz, oz) + 1) : 0);
+#pragma unroll
+            for (int k = 0; k < 4; k++) acc[O][k] += stf[(o * 4 + k) * nf + i];
+        }
+    }
+#pragma unroll
+    for (int o = 0; o < NO; o++)
+#pragma unroll
+        for (int k = 0; k < 4; k++) stc[(o * 4 + k) * gc.n_el + I] = acc[o][k];
+}
+
+// y = A x on a level with nc unknowns per cell (1 or 2)
+template <int DIM, int NC>
+__global__ void k_papply(uwg_lgeom g, const float* __restrict__ st, const float* __restrict__ x,
+                         float* __restrict__ y) {
+    constexpr int NO = DIM == 3 ? 27 : 9;
+    const int64_t n = g.n_el;
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    int ex, ey, ez;
+    cell_xyz<DIM>(g, e, ex, ey, ez);
+    const int64_t sx = 1, sy = g.res[0], sz = (int64_t)g.res[0] * g.res[1];
+    float acc[NC];
+#pragma unroll
+    for (int a = 0; a < NC; a++) acc[a] = 0.f;
+#pragma unroll
+    for (int o = 0; o < NO; o++) {
+        const int ox = o % 3 - 1, oy = (o / 3) % 3 - 1, oz = DIM == 3 ? o / 9 - 1 : 0;
+        if (!in_grid<DIM>(g, ex + ox, ey + oy, ez + oz)) continue;
+        const int64_t j = e + ox * sx + oy * sy + oz * sz;
+        if constexpr (NC == 1) {
+            acc[0] += st[o * n + e] * x[j];
+        } else {
+            const float x0 = x[j], x1 = x[n + j];
+            acc[0] += st[(o * 4 + 0) * n + e] * x0 + st[(o * 4 + 1) * n + e] * x1;
+            acc[NC - 1] += st[(o * 4 + 2) * n + e] * x0 + st[(o * 4 + 3) * n + e] * x1;
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < NC; a++) y[a * n + e] = acc[a];
+}
+
+template <int NC>
+__global__ void k_pdiag(int64_t n, int center, const float* __restrict__ st, float* __restrict__ d) {
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= n) return;
+#pragma unroll
+    for (int a = 0; a < NC; a++) {
+        float v = st[(NC == 1 ? center : center * 4 + a * 3) * n + e];
+        d[a * n + e] = v > 0.f ? v : 1.f;
+    }
+}
+
+// rc = P^T rf between level lc-1 (ncf unknowns per cell) and lc (two per cell)
+template <int DIM, int NCF>
+__global__ void k_prestrict(uwg_lgeom gf, uwg_lgeom gc, const float* __restrict__ rf, float* __restrict__ rc) {
+    int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (I >= gc.n_el) return;
+    int X, Y, Z;
+    cell_xyz<DIM>(gc, I, X, Y, Z);
+    float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+    for (int cn = 0; cn < (1 << DIM); cn++) {
+        const int cx = cn & 1, cy = (cn >> 1) & 1, cz = DIM == 3 ? (cn >> 2) & 1 : 0;
+        const int64_t i = (2 * X + cx) + (int64_t)gf.res[0] * ((2 * Y + cy) + (int64_t)gf.res[1] * (2 * Z + cz));
+        if constexpr (NCF == 1) {
+            const float v = rf[i];
+            s0 += v;
+            s1 += ((cx + cy + cz) & 1) ? -v : v;
+        } else {
+            s0 += rf[i];
+            s1 += rf[gf.n_el + i];
+        }
+    }
+    rc[I] = s0;
+    rc[gc.n_el + I] = s1;
+}
+
+// xf += P xc
+template <int DIM, int NCF>
+__global__ void k_pprolong_add(uwg_lgeom gf, uwg_lgeom gc, const float* __restrict__ xc, float* __restrict__ xf) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= gf.n_el) return;
+    int x, y, z;
+    cell_xyz<DIM>(gf, i, x, y, z);
+    const int64_t I = (x >> 1) + (int64_t)gc.res[0] * ((y >> 1) + (int64_t)gc.res[1] * (z >> 1));
+    if constexpr (NCF == 1) {
+        const float c = xc[gc.n_el + I];
+        xf[i] += xc[I] + (((x + y + z) & 1) ? -c : c);
+    } else {
+        xf[i] += xc[I];
+        xf[gf.n_el + i] += xc[gc.n_el + I];
+    }
+}
+
+// Dense (ncomp n) x (ncomp n) matrix of a level, FP64, plus tau/n on the
+// smooth-smooth block: the constant pressure is the kernel of L, and adding
+// tau v v^T (v the normalised constant) makes the matrix invertible without
+// changing its action on the complement of v.
+template <int DIM, int NC>
+__global__ void k_pdense(uwg_lgeom g, const float* __restrict__ st, double* __restrict__ A) {
+    constexpr int NO = DIM == 3 ? 27 : 9;
+    const int64_t n = g.n_el, m = NC * n;
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    int ex, ey, ez;
+    cell_xyz<DIM>(g, e, ex, ey, ez);
+    for (int o = 0; o < NO; o++) {
+        const int ox = o % 3 - 1, oy = (o / 3) % 3 - 1, oz = DIM == 3 ? o / 9 - 1 : 0;
+        if (!in_grid<DIM>(g, ex + ox, ey + oy, ez + oz)) continue;
+        const int64_t j = e + ox + (int64_t)oy * g.res[0] + (int64_t)oz * g.res[0] * g.res[1];
+        for (int a = 0; a < NC; a++)
+            for (int b = 0; b < NC; b++)
+                A[(a * n + e) * m + b * n + j] = st[(NC == 1 ? o : o * 4 + a * 2 + b) * n + e];
+    }
+}
+
+__global__ void k_pdense_fix(int64_t m, int64_t n, double* A) {
+    __shared__ double red[1024];
+    double mx = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) mx = fmax(mx, A[i * m + i]);
+    red[threadIdx.x] = mx;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+        __syncthreads();
+    }
+    const double tau = (red[0] > 0.0 ? red[0] : 1.0) / (double)n;
+    for (int64_t k = threadIdx.x; k < n * n; k += blockDim.x) A[(k / n) * m + (k % n)] += tau;
+}
+
+}  // namespace
+
+#define PMG_DIM(KERN, GRID, ...)                                               \
+    do {                                                                        \
+        if (c->dim == 3) KERN<3><<<GRID, 256, 0, c->stream>>>(__VA_ARGS__);    \
+        else KERN<2><<<GRID, 256, 0, c->stream>>>(__VA_ARGS__);                \
+    } while (0)
+#define PMG_DIM_NC(KERN, NC, GRID, ...)                                                        \
+    do {                                                                                        \
+        if (c->dim == 3) {                                                                      \
+            if (NC == 1) KERN<3, 1><<<GRID, 256, 0, c->stream>>>(__VA_ARGS__);                 \
+            else KERN<3, 2><<<GRID, 256, 0, c->stream>>>(__VA_ARGS__);                         \
+        } else {                                                                                \
+            if (NC == 1) KERN<2, 1><<<GRID, 256, 0, c->stream>>>(__VA_ARGS__);                 \
+            else KERN<2, 2><<<GRID, 256, 0, c->stream>>>(__VA_ARGS__);                         \
+        }                                                                                       \
+    } while (0)
+
+int uwg_pmg_ncomp(int l) { return l == 0 ? 1 : 2; }
+
+int64_t uwg_pmg_stencil_size(const uwg_ctx* c, int l) {
+    int no = c->dim == 3 ? 27 : 9;
+    return (int64_t)no * (l == 0 ? 1 : 4) * c->lev[l].n_el;
+}
+
+int uwg_pmg_stencil(uwg_ctx* c, int l, const float* W0, const float* st_fine, float* st) {
+    if (l == 0) {
+        uwg_lgeom g = uwg_level_geom(c, 0);
+        PMG_DIM(k_pst0, nblk(g.n_el), g, W0, st);
+    } else {
+        uwg_lgeom gf = uwg_level_geom(c, l - 1), gc = uwg_level_geom(c, l);
+        if (l == 1) PMG_DIM(k_pgal01, nblk(gc.n_el, 128), gf, gc, st_fine, st);
+        else PMG_DIM(k_pgal22, nblk(gc.n_el, 128), gf, gc, st_fine, st);
+    }
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
+int uwg_pmg_apply(uwg_ctx* c, int l, const float* st, const float* x, float* y) {
+    uwg_lgeom g = uwg_level_geom(c, l);
+    PMG_DIM_NC(k_papply, uwg_pmg_ncomp(l), nblk(g.n_el), g, st, x, y);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
+int uwg_pmg_diag(uwg_ctx* c, int l, const float* st, float* d) {
+    int64_t n = c->lev[l].n_el;
+    int center = c->dim == 3 ? 13 : 4;
+    if (l == 0) k_pdiag<1><<<nblk(n), 256, 0, c->stream>>>(n, center, st, d);
+    else k_pdiag<2><<<nblk(n), 256, 0, c->stream>>>(n, center, st, d);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
+int uwg_pmg_restrict(uwg_ctx* c, int lc, const float* rf, float* rc) {
+    uwg_lgeom gf = uwg_level_geom(c, lc - 1), gc = uwg_level_geom(c, lc);
+    PMG_DIM_NC(k_prestrict, uwg_pmg_ncomp(lc - 1), nblk(gc.n_el), gf, gc, rf, rc);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
+int uwg_pmg_prolong_add(uwg_ctx* c, int lc, const float* xc, float* xf) {
+    uwg_lgeom gf = uwg_level_geom(c, lc - 1), gc = uwg_level_geom(c, lc);
+    PMG_DIM_NC(k_pprolong_add, uwg_pmg_ncomp(lc - 1), nblk(gf.n_el), gf, gc, xc, xf);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
+int uwg_pmg_dense_inverse(uwg_ctx* c, int l, const float* st, float* inv32) {
+    uwg_lgeom g = uwg_level_geom(c, l);
+    int nc = uwg_pmg_ncomp(l);
+    int64_t n = g.n_el, m = nc * n;
+    if (m > 4096) return uwg_set_error(c, UWG_ERR_ARG, "coarsest pressure level too large for a dense solve");
+    double *A = nullptr, *B = nullptr;
+    UWG_CUDA(c, cudaMallocAsync((void**)&A, sizeof(double) * m * m, c->stream));
+    UWG_CUDA(c, cudaMallocAsync((void**)&B, sizeof(double) * m * m, c->stream));
+    UWG_CUDA(c, cudaMemsetAsync(A, 0, sizeof(double) * m * m, c->stream));
+    PMG_DIM_NC(k_pdense, nc, nblk(n, 64), g, st, A);
+    k_pdense_fix<<<1, 1024, 0, c->stream>>>(m, n, A);
+    int rc = uwg_ops_dense_invert(c, m, A, B);
+    if (!rc) rc = uwg_ops_to_f32(c, m * m, B, inv32);
+    cudaFreeAsync(A, c->stream);
+    cudaFreeAsync(B, c->stream);
+    if (rc) return rc;
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}

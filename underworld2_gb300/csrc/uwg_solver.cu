@@ -46,11 +46,13 @@ struct Work {
     double *p_tmp, *p_tmp2, *hhat;
     double* coef;                             // device coefficients
     int restart = 0;
-    // pressure multigrid of the weighted BFBt preconditioner (FP32)
+    // pressure multigrid of the weighted BFBt preconditioner (FP32): one
+    // unknown per cell on level 0, two (smooth, checkerboard) on coarser levels
     LevelVecs<float> pv[UWG_MAXLEV];
-    float* pvel[UWG_MAXLEV];                  // velocity-sized temp per level
-    float* Ldiag[UWG_MAXLEV];
-    float* Dinv[UWG_MAXLEV];                  // 1/sqrt(diag K) per level
+    float* pst[UWG_MAXLEV];                   // explicit cell stencils (uwg_pmg.cu layout)
+    float* pdg[UWG_MAXLEV];                   // their diagonals
+    float* pcinv = nullptr;                   // dense inverse of the coarsest level
+    float* W0 = nullptr;                      // 1/sqrt(diag K) on level 0, 0 on Dirichlet dofs
     double Lmax[UWG_MAXLEV];
     float *pcg_r, *pcg_z, *pcg_p, *pcg_q, *bf_r, *bf_y, *bf_m, *bf_z, *bf_v1, *bf_v2;
     int lsolve_its = 0;
@@ -92,15 +94,17 @@ int work_init(uwg_ctx* c, int restart) {
         w->u_tmp = dalloc<double>(c, nv); w->u_tmp2 = dalloc<double>(c, nv);
         w->ftil = dalloc<double>(c, nv); w->bvec = dalloc<double>(c, nv);
         w->p_tmp = dalloc<double>(c, np); w->p_tmp2 = dalloc<double>(c, np); w->hhat = dalloc<double>(c, np);
-        w->coef = dalloc<double>(c, 256);
+        w->coef = dalloc<double>(c, 512);
         for (int l = 0; l < c->nlev; l++) {
-            int64_t ne = c->lev[l].n_el;
+            int64_t ne = uwg_pmg_ncomp(l) * c->lev[l].n_el;
             w->pv[l] = {dalloc<float>(c, ne), dalloc<float>(c, ne), dalloc<float>(c, ne), dalloc<float>(c, ne), dalloc<float>(c, ne)};
-            w->pvel[l] = dalloc<float>(c, c->lev[l].n_dof);
-            w->Ldiag[l] = dalloc<float>(c, ne);
-            w->Dinv[l] = dalloc<float>(c, c->lev[l].n_dof);
+            w->pst[l] = dalloc<float>(c, uwg_pmg_stencil_size(c, l));
+            w->pdg[l] = dalloc<float>(c, ne);
             w->Lmax[l] = 1.0;
+            if (l == c->nlev - 1) w->pcinv = dalloc<float>(c, ne * ne);
+            if (!w->pst[l] || !w->pdg[l] || !w->pv[l].x) return uwg_set_error(c, UWG_ERR_CUDA, "out of device memory (pressure multigrid)");
         }
+        w->W0 = dalloc<float>(c, nv);
         w->pcg_r = dalloc<float>(c, np); w->pcg_z = dalloc<float>(c, np);
         w->pcg_p = dalloc<float>(c, np); w->pcg_q = dalloc<float>(c, np);
         w->bf_r = dalloc<float>(c, np); w->bf_y = dalloc<float>(c, np);
@@ -318,19 +322,19 @@ int velocity_solve(uwg_ctx* c, const SolveCfg& cfg, const double* b, double* x, 
 int cheb_L(uwg_ctx* c, int l, const float* b, float* x, int deg, bool x_zero) {
     Work* w = work_of(c);
     LevelVecs<float>& v = w->pv[l];
-    int64_t n = c->lev[l].n_el;
+    int64_t n = uwg_pmg_ncomp(l) * c->lev[l].n_el;
     cudaStream_t s = c->stream;
     double lmax = w->Lmax[l];
     double alpha = 0.1 * lmax, beta = 1.2 * lmax;
     double theta = 0.5 * (beta + alpha), delta = 0.5 * (beta - alpha);
     double sigma = theta / delta, rho = 1.0 / sigma;
     int rc;
-    if (!x_zero && (rc = uwg_ops_applyL32(c, l, w->Dinv[l], x, v.t, w->pvel[l]))) return rc;
-    vk_cheb<float>(s, n, b, x_zero ? nullptr : v.t, w->Ldiag[l], (float)(1.0 / theta), 0.f, v.d, x, 1, x_zero ? 1 : 0);
+    if (!x_zero && (rc = uwg_pmg_apply(c, l, w->pst[l], x, v.t))) return rc;
+    vk_cheb<float>(s, n, b, x_zero ? nullptr : v.t, w->pdg[l], (float)(1.0 / theta), 0.f, v.d, x, 1, x_zero ? 1 : 0);
     for (int i = 1; i < deg; i++) {
-        if ((rc = uwg_ops_applyL32(c, l, w->Dinv[l], x, v.t, w->pvel[l]))) return rc;
+        if ((rc = uwg_pmg_apply(c, l, w->pst[l], x, v.t))) return rc;
         double rho1 = 1.0 / (2.0 * sigma - rho);
-        vk_cheb<float>(s, n, b, v.t, w->Ldiag[l], (float)(2.0 * rho1 / delta), (float)(rho1 * rho), v.d, x, 0, 0);
+        vk_cheb<float>(s, n, b, v.t, w->pdg[l], (float)(2.0 * rho1 / delta), (float)(rho1 * rho), v.d, x, 0, 0);
         rho = rho1;
     }
     return UWG_OK;
@@ -339,17 +343,17 @@ int cheb_L(uwg_ctx* c, int l, const float* b, float* x, int deg, bool x_zero) {
 int pvcycle(uwg_ctx* c, int l, const float* b, float* x) {
     Work* w = work_of(c);
     cudaStream_t s = c->stream;
-    int64_t n = c->lev[l].n_el;
+    int64_t n = uwg_pmg_ncomp(l) * c->lev[l].n_el;
     int rc;
-    if (l == c->nlev - 1) return cheb_L(c, l, b, x, 8, true);
+    if (l == c->nlev - 1) return uwg_ops_dense_mv32(c, n, w->pcinv, b, x);
     LevelVecs<float>& v = w->pv[l];
     LevelVecs<float>& vc = w->pv[l + 1];
     if ((rc = cheb_L(c, l, b, x, 3, true))) return rc;
-    if ((rc = uwg_ops_applyL32(c, l, w->Dinv[l], x, v.t, w->pvel[l]))) return rc;
+    if ((rc = uwg_pmg_apply(c, l, w->pst[l], x, v.t))) return rc;
     vk_axpby<float>(s, n, 1.f, b, -1.f, v.t);
-    if ((rc = uwg_ops_cell_restrict32(c, l + 1, v.t, vc.b))) return rc;
+    if ((rc = uwg_pmg_restrict(c, l + 1, v.t, vc.b))) return rc;
     if ((rc = pvcycle(c, l + 1, vc.b, vc.x))) return rc;
-    if ((rc = uwg_ops_cell_prolong_add32(c, l + 1, vc.x, x))) return rc;
+    if ((rc = uwg_pmg_prolong_add(c, l + 1, vc.x, x))) return rc;
     return cheb_L(c, l, b, x, 3, false);
 }
 
@@ -413,7 +417,7 @@ int lsolve(uwg_ctx* c, const float* b, float* x, double rtol, int maxit) {
     double bn = std::sqrt(d2[1]), rz = d2[0];
     if (bn == 0.0) return UWG_OK;
     for (int it = 1; it <= maxit; it++) {
-        if ((rc = uwg_ops_applyL32(c, 0, w->Dinv[0], p, q, w->pvel[0]))) return rc;
+        if ((rc = uwg_pmg_apply(c, 0, w->pst[0], p, q))) return rc;
         double pq;
         const float* a1[1] = {p};
         const float* b1[1] = {q};
@@ -441,9 +445,9 @@ int bfbt(uwg_ctx* c, const double* r, double* z, double rtol) {
     int rc;
     vk_convert<double, float>(s, np, r, w->bf_r);
     if ((rc = lsolve(c, w->bf_r, w->bf_y, rtol, 200))) return rc;
-    if ((rc = uwg_ops_G32(c, 0, w->Dinv[0], w->bf_y, w->bf_v1))) return rc;        // W G y
+    if ((rc = uwg_ops_G32(c, 0, w->W0, w->bf_y, w->bf_v1))) return rc;             // W G y
     if ((rc = uwg_ops_applyK<float>(c, 0, w->bf_v1, w->bf_v2))) return rc;         // K W G y
-    vk_pointwise_mul_mask(s, nv, w->Dinv[0], w->bf_v2);                             // W K W G y
+    vk_pointwise_mul_mask(s, nv, w->W0, w->bf_v2);                                  // W K W G y
     if ((rc = uwg_ops_Gt32(c, 0, w->bf_v2, w->bf_m))) return rc;
     if ((rc = lsolve(c, w->bf_m, w->bf_z, rtol, 200))) return rc;
     vk_convert<float, double>(s, np, w->bf_z, z);
@@ -455,18 +459,21 @@ int bfbt_setup(uwg_ctx* c) {
     Work* w = work_of(c);
     cudaStream_t s = c->stream;
     int rc;
+    if ((rc = uwg_ops_winv(c, 0, w->W0))) return rc;
     for (int l = 0; l < c->nlev; l++) {
-        if ((rc = uwg_ops_winv(c, l, w->Dinv[l]))) return rc;
-        if ((rc = uwg_ops_Ldiag32(c, l, w->Dinv[l], w->Ldiag[l]))) return rc;
-        int64_t n = c->lev[l].n_el;
+        if ((rc = uwg_pmg_stencil(c, l, w->W0, l ? w->pst[l - 1] : nullptr, w->pst[l]))) return rc;
+        if ((rc = uwg_pmg_diag(c, l, w->pst[l], w->pdg[l]))) return rc;
+        if (l == c->nlev - 1) break;
+        // largest eigenvalue of D^-1 A by power iteration (Chebyshev interval)
+        int64_t n = uwg_pmg_ncomp(l) * c->lev[l].n_el;
         LevelVecs<float>& v = w->pv[l];
         std::vector<float> hv(n);
         for (int64_t i = 0; i < n; i++) hv[i] = (float)(1.0 + 0.41 * std::sin(1.37 * (double)i) + ((i & 1) ? 0.3 : -0.3));
         UWG_CUDA(c, cudaMemcpyAsync(v.x, hv.data(), sizeof(float) * n, cudaMemcpyHostToDevice, s));
         double lam = 1.0;
         for (int it = 0; it < 30; it++) {
-            if ((rc = uwg_ops_applyL32(c, l, w->Dinv[l], v.x, v.t, w->pvel[l]))) return rc;
-            vk_pointwise_div<float>(s, n, v.t, w->Ldiag[l], v.d);
+            if ((rc = uwg_pmg_apply(c, l, w->pst[l], v.x, v.t))) return rc;
+            vk_pointwise_div<float>(s, n, v.t, w->pdg[l], v.d);
             double d2[2];
             const float* a[2] = {v.d, v.x};
             if ((rc = dots<float>(c, n, 2, a, a, d2))) return rc;
@@ -478,7 +485,7 @@ int bfbt_setup(uwg_ctx* c) {
         UWG_CUDA(c, cudaStreamSynchronize(s));   // the host vector must outlive its copy
         w->Lmax[l] = lam;
     }
-    return UWG_OK;
+    return uwg_pmg_dense_inverse(c, c->nlev - 1, w->pst[c->nlev - 1], w->pcinv);
 }
 }  // namespace
 
@@ -550,7 +557,7 @@ extern "C" void uwg_solve_opts_default(uwg_solve_opts* o) {
     o->max_outer = 500;
     o->mg_levels = 0;
     o->smooth_steps = 3;
-    o->restart = 50;
+    o->restart = 120;
     o->zero_guess = 1;
     o->schur_pc = 1;
     o->schur_pc_rtol = 1e-2;
@@ -618,13 +625,19 @@ int fgmres(uwg_ctx* c, const SolveCfg& cfg, const double* rhs, double* p, double
             // classical Gram-Schmidt, two passes
             std::vector<double> hcol(j + 1, 0.0);
             for (int pass = 0; pass < 2; pass++) {
-                vk_mdot(s, n, j + 1, (const double* const*)w->V.data(), w->V[j + 1], w->coef);
+                for (int i0 = 0; i0 <= j; i0 += 64) {
+                    int k = std::min(64, j + 1 - i0);
+                    vk_mdot(s, n, k, (const double* const*)w->V.data() + i0, w->V[j + 1], w->coef + i0);
+                }
                 std::vector<double> hh(j + 1);
                 UWG_CUDA(c, cudaMemcpyAsync(hh.data(), w->coef, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, s));
                 UWG_CUDA(c, cudaStreamSynchronize(s));
                 for (int i = 0; i <= j; i++) { hcol[i] += hh[i]; hh[i] = -hh[i]; }
-                UWG_CUDA(c, cudaMemcpyAsync(w->coef + 128, hh.data(), sizeof(double) * (j + 1), cudaMemcpyHostToDevice, s));
-                vk_maxpy(s, n, j + 1, w->coef + 128, (const double* const*)w->V.data(), w->V[j + 1]);
+                UWG_CUDA(c, cudaMemcpyAsync(w->coef + 256, hh.data(), sizeof(double) * (j + 1), cudaMemcpyHostToDevice, s));
+                for (int i0 = 0; i0 <= j; i0 += 64) {
+                    int k = std::min(64, j + 1 - i0);
+                    vk_maxpy(s, n, k, w->coef + 256 + i0, (const double* const*)w->V.data() + i0, w->V[j + 1]);
+                }
             }
             double hn;
             const double* av[1] = {w->V[j + 1]};
@@ -657,7 +670,8 @@ int fgmres(uwg_ctx* c, const SolveCfg& cfg, const double* rhs, double* p, double
             y[i] = t / H[i * m + i];
         }
         UWG_CUDA(c, cudaMemcpyAsync(w->coef, y.data(), sizeof(double) * j, cudaMemcpyHostToDevice, s));
-        vk_maxpy(s, n, j, w->coef, (const double* const*)w->Z.data(), p);
+        for (int i0 = 0; i0 < j; i0 += 64)
+            vk_maxpy(s, n, std::min(64, j - i0), w->coef + i0, (const double* const*)w->Z.data() + i0, p);
         *its = total;
         if (done) return UWG_OK;
         if (total >= maxit) return uwg_set_error(c, UWG_ERR_NOT_CONVERGED, "pressure solve reached its iteration cap");
@@ -716,7 +730,7 @@ extern "C" int uwg_stokes_solve(uwg_ctx* c, const uwg_solve_opts* o, double* u, 
     uwg_solve_stats S;
     memset(&S, 0, sizeof(S));
     double t0 = now();
-    if (o->restart < 2 || o->restart > 60) return uwg_set_error(c, UWG_ERR_ARG, "restart must be in [2, 60]");
+    if (o->restart < 2 || o->restart > 240) return uwg_set_error(c, UWG_ERR_ARG, "restart must be in [2, 240]");
     int rc = work_init(c, o->restart);
     if (rc) return rc;
     Work* w = work_of(c);
