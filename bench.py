@@ -353,6 +353,33 @@ def run_kernel(args):
                       "ms_per_launch": s.elapsed_time(e) / args.reps}))
 
 
+def run_profile_solve(args):
+    """One map + DVC + assembly + solve of the workload, untimed (the target of
+    the launch-list captures recorded under profiles/); `--kernel-ppc` lowers
+    the particle count to keep the device footprint small."""
+    import torch
+    from underworld2_gb300._core import Context, rng_seed
+    cfg = CONFIGS[args.config]
+    dim = cfg["dim"]
+    ctx = Context(dim, cfg["res"], (0.0,) * dim, (1.0,) * dim)
+    ctx.set_bcs(freeslip_mask(ctx))
+    ppc = args.kernel_ppc or cfg["ppc"]
+    x, owner, off, lst, _ = ctx.layout_random(ppc, rng_seed(13))
+    eta, body = material(cfg, x)
+    ip_xi = ctx.pic_map(x, off, lst)
+    ip_w = ctx.dvc_weights(off, ip_xi)
+    ctx.assemble(off, lst, ip_xi, ip_w, eta, body)
+    u, p = ctx.zeros(ctx.n_vdof), ctx.zeros(ctx.n_pdof)
+    st = ctx.solve(u, p, mixed=1 if args.mode == "mixed" else 0, rtol=1e-8, inner_rtol=args.inner_rtol,
+                   outer_rtol=args.outer_rtol, smooth_steps=3, restart=120, schur_pc=args.schur_pc,
+                   schur_pc_rtol=args.bfbt_rtol, max_outer=args.max_outer)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_solve": args.config, "particles_per_cell": ppc,
+                      "pressure_its": st["pressure_its"], "schur_pc_its": st["schur_pc_its"],
+                      "velocity_total_its": st["velocity_total_its"], "residual": st["residual"],
+                      "total_time": st["total_time"]}))
+
+
 def count_launches(ctx, x0, owner0, off0, lst0, eta0, body0, mixed, opts, u, p):
     """Kernels launched by libuwg in one step, counted with the CUDA activity profiler."""
     import torch
@@ -422,6 +449,7 @@ def main():
     ap.add_argument("--bfbt-rtol", type=float, default=1e-2)
     ap.add_argument("--kernel", choices=["applyK32", "applyK64"], help="only launch one operator kernel (profiling)")
     ap.add_argument("--kernel-ppc", type=int, default=0)
+    ap.add_argument("--profile-solve", action="store_true", help="one untimed solve (profiling target)")
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--max-outer", type=int, default=500)
     ap.add_argument("--skip-fp64", action="store_true")
@@ -430,6 +458,9 @@ def main():
     args = ap.parse_args()
     if args.kernel:
         run_kernel(args)
+        return
+    if args.profile_solve:
+        run_profile_solve(args)
         return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

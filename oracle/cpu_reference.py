@@ -9,8 +9,9 @@ sample of the benchmark workload, and extrapolates to the full size:
 * PIC assembly and owner update: the full workload;
 * Stokes solve: (CPU time of one multigrid-preconditioned CG iteration on the
   full mesh) x (inner iterations of the same BSSCR algorithm run to the same
-  tolerance on a coarser mesh of the same workload; multigrid iteration
-  counts are nearly mesh independent) plus the full-mesh solver setup;
+  tolerance on an 8^d mesh of the same workload).  The outer iteration count
+  of the reference's Schur preconditioner grows with the resolution, so this
+  figure is a lower bound of the full-size CPU solve and is labelled so;
 * RK2 advection: a sample of particles, scaled by the particle count.
 
 Every extrapolated figure is labelled in the returned dict.
@@ -88,7 +89,7 @@ def measure(cfg, workload, quick=False):
     tbl, cnt, owner = m.initial_tables(ppc, ppc)
 
     # 1. mapping + DVC on a sample of elements
-    frac = 1.0 if n_el <= 8192 else (1.0 / 256 if quick else 1.0 / 64)
+    frac = 1.0 if n_el <= 8192 else 1.0 / 256
     n_s = max(1, int(n_el * frac))
     ip_xi = np.zeros((npart, dim))
     ip_w = np.zeros(npart)
@@ -112,14 +113,14 @@ def measure(cfg, workload, quick=False):
     t_asm = time.perf_counter() - t0
 
     # 3. solve: per-iteration cost on the full mesh x converged iteration count
-    if n_el <= 70000 and not quick:
+    if n_el <= 70000:
         t0 = time.perf_counter()
         u, pr, st = s.solve(inner_rtol=1e-10, outer_rtol=1e-9)
         t_solve = time.perf_counter() - t0
         solve_note = "full converged solve"
         its = st
     else:
-        coarse = tuple(max(8, r // 4) for r in res) if not quick else tuple(max(8, r // 8) for r in res)
+        coarse = tuple(min(8, r) for r in res)
         its = _solve_counts(cfg, coarse)
         n_it = its["velocity_presolve_its"] + its["velocity_pressuresolve_its"] + its["velocity_backsolve_its"]
         t0 = time.perf_counter()
@@ -128,8 +129,10 @@ def measure(cfg, workload, quick=False):
         it_done = st["velocity_presolve_its"] + st["velocity_pressuresolve_its"] + st["velocity_backsolve_its"]
         t_it = dt / max(it_done, 1)
         t_solve = n_it * t_it
-        solve_note = ("extrapolated: %.3f s per MG-CG iteration on the full mesh x %d iterations of the "
-                      "converged %s solve" % (t_it, n_it, "x".join(map(str, coarse))))
+        conv = "converged" if its.get("rc", 0) == 0 else "iteration-capped"
+        solve_note = ("solve extrapolated as a LOWER BOUND: %.3f s per MG-CG iteration on the full mesh x %d "
+                      "iterations of the %s %s solve (outer iterations of this preconditioner grow with "
+                      "resolution)" % (t_it, n_it, conv, "x".join(map(str, coarse))))
 
     # 4. RK2 on a sample of particles + owner update on all
     vel = np.zeros(m.n_nodes * dim)

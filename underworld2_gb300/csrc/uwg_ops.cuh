@@ -59,6 +59,7 @@ int64_t uwg_pmg_stencil_size(const uwg_ctx* c, int l);
 // level 0: stencil of G^T W G from W0; level l > 0: Galerkin product of st_fine
 int uwg_pmg_stencil(uwg_ctx* c, int l, const float* W0, const float* st_fine, float* st);
 int uwg_pmg_apply(uwg_ctx* c, int l, const float* st, const float* x, float* y);
+int uwg_pmg_apply0_mf(uwg_ctx* c, const float* W0, const float* x, float* y);   // level 0, 3D, no stencil
 int uwg_pmg_diag(uwg_ctx* c, int l, const float* st, float* d);
 int uwg_pmg_restrict(uwg_ctx* c, int lc, const float* rf, float* rc);
 int uwg_pmg_prolong_add(uwg_ctx* c, int lc, const float* xc, float* xf);

@@ -281,6 +281,80 @@ __global__ void k_pdense_fix(int64_t m, int64_t n, double* A) {
     for (int64_t k = threadIdx.x; k < n * n; k += blockDim.x) A[(k / n) * m + (k % n)] += tau;
 }
 
+
+// Level-0 apply without the stencil (3D): y = G^T (W (G x)).  A CTA owns a
+// 16x8x8 tile of cells; it stages the tile's cell values with a one-cell halo
+// in shared memory, forms W G x at the tile's 17x9x9 nodes in shared memory,
+// and then sums G^T over each cell's eight nodes.  DRAM traffic is x, W (three
+// floats per node) and y: about a sixth of the 27-coefficient stencil's.
+#define PT_X 16
+#define PT_Y 8
+#define PT_Z 8
+__global__ void __launch_bounds__(256) k_papply0_mf(uwg_lgeom g, const float* __restrict__ W,
+                                                    const float* __restrict__ x, float* __restrict__ y) {
+    constexpr int HX = PT_X + 2, HY = PT_Y + 2, HZ = PT_Z + 2, NH = HX * HY * HZ;
+    constexpr int NX = PT_X + 1, NY = PT_Y + 1, NZ = PT_Z + 1, NN = NX * NY * NZ;
+    __shared__ float ps[NH];
+    __shared__ float vs[3][NN];
+    __shared__ float hs[3][HX];   // cell sizes along each axis (halo included, 0 outside)
+    const int ntx = (g.res[0] + PT_X - 1) / PT_X, nty = (g.res[1] + PT_Y - 1) / PT_Y;
+    const int tile = blockIdx.x;
+    const int tx0 = (tile % ntx) * PT_X, ty0 = ((tile / ntx) % nty) * PT_Y, tz0 = (tile / (ntx * nty)) * PT_Z;
+    const int64_t sy = g.res[0], sz = (int64_t)g.res[0] * g.res[1];
+    for (int k = threadIdx.x; k < NH; k += blockDim.x) {
+        const int i = k % HX, j = (k / HX) % HY, l = k / (HX * HY);
+        const int cx = tx0 - 1 + i, cy = ty0 - 1 + j, cz = tz0 - 1 + l;
+        ps[k] = in_grid<3>(g, cx, cy, cz) ? x[cx + sy * cy + sz * cz] : 0.f;
+    }
+    if (threadIdx.x < 3 * HX) {
+        const int d = threadIdx.x / HX, i = threadIdx.x % HX;
+        const int c0 = (d == 0 ? tx0 : d == 1 ? ty0 : tz0) - 1 + i;
+        const int r = d == 0 ? g.res[0] : d == 1 ? g.res[1] : g.res[2];
+        const double* a = d == 0 ? g.ax[0] : d == 1 ? g.ax[1] : g.ax[2];
+        hs[d][i] = (c0 >= 0 && c0 < r) ? (float)(a[c0 + 1] - a[c0]) : 0.f;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < NN; k += blockDim.x) {
+        const int ni = k % NX, nj = (k / NX) % NY, nk = k / (NX * NY);
+        const int gi = tx0 + ni, gj = ty0 + nj, gk = tz0 + nk;
+        float v0 = 0.f, v1 = 0.f, v2 = 0.f;
+        if (gi < g.nx[0] && gj < g.nx[1] && gk < g.nx[2]) {
+#pragma unroll
+            for (int c = 0; c < 8; c++) {
+                const int cx = c & 1, cy = (c >> 1) & 1, cz = c >> 2;
+                const float pe = ps[(ni + cx) + HX * ((nj + cy) + HY * (nk + cz))];
+                const float hx = hs[0][ni + cx], hy = hs[1][nj + cy], hz = hs[2][nk + cz];
+                const float a0 = 0.25f * hy * hz, a1 = 0.25f * hx * hz, a2 = 0.25f * hx * hy;
+                v0 += (cx ? a0 : -a0) * pe;
+                v1 += (cy ? a1 : -a1) * pe;
+                v2 += (cz ? a2 : -a2) * pe;
+            }
+            const int64_t node = gi + (int64_t)g.nx[0] * (gj + (int64_t)g.nx[1] * gk);
+            v0 *= W[node * 3 + 0];
+            v1 *= W[node * 3 + 1];
+            v2 *= W[node * 3 + 2];
+        }
+        vs[0][k] = v0;
+        vs[1][k] = v1;
+        vs[2][k] = v2;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < PT_X * PT_Y * PT_Z; k += blockDim.x) {
+        const int i = k % PT_X, j = (k / PT_X) % PT_Y, l = k / (PT_X * PT_Y);
+        const int ex = tx0 + i, ey = ty0 + j, ez = tz0 + l;
+        if (!in_grid<3>(g, ex, ey, ez)) continue;
+        const float hx = hs[0][i + 1], hy = hs[1][j + 1], hz = hs[2][l + 1];
+        const float a0 = 0.25f * hy * hz, a1 = 0.25f * hx * hz, a2 = 0.25f * hx * hy;
+        float s = 0.f;
+#pragma unroll
+        for (int n = 0; n < 8; n++) {
+            const int lx = n & 1, ly = (n >> 1) & 1, lz = n >> 2;
+            const int q = (i + lx) + NX * ((j + ly) + NY * (l + lz));
+            s += (lx ? -a0 : a0) * vs[0][q] + (ly ? -a1 : a1) * vs[1][q] + (lz ? -a2 : a2) * vs[2][q];
+        }
+        y[ex + sy * ey + sz * ez] = s;
+    }
+}
 }  // namespace
 
 #define PMG_DIM(KERN, GRID, ...)                                               \
@@ -322,6 +396,16 @@ int uwg_pmg_stencil(uwg_ctx* c, int l, const float* W0, const float* st_fine, fl
 int uwg_pmg_apply(uwg_ctx* c, int l, const float* st, const float* x, float* y) {
     uwg_lgeom g = uwg_level_geom(c, l);
     PMG_DIM_NC(k_papply, uwg_pmg_ncomp(l), nblk(g.n_el), g, st, x, y);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
+int uwg_pmg_apply0_mf(uwg_ctx* c, const float* W0, const float* x, float* y) {
+    if (c->dim != 3) return uwg_set_error(c, UWG_ERR_ARG, "matrix-free pressure apply is 3D only");
+    const uwg_level& L = c->lev[0];
+    unsigned tiles = (unsigned)(((L.res[0] + PT_X - 1) / PT_X) * ((L.res[1] + PT_Y - 1) / PT_Y) *
+                                ((L.res[2] + PT_Z - 1) / PT_Z));
+    k_papply0_mf<<<tiles, 256, 0, c->stream>>>(uwg_level_geom(c, 0), W0, x, y);
     UWG_CUDA(c, cudaGetLastError());
     return UWG_OK;
 }

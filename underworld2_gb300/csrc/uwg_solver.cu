@@ -319,6 +319,13 @@ int velocity_solve(uwg_ctx* c, const SolveCfg& cfg, const double* b, double* x, 
 // for a cell-centred multigrid.  All of it runs in FP32: it is a
 // preconditioner inside flexible GMRES, whose residuals stay FP64.
 // ---------------------------------------------------------------------------
+// y = A_l x on pressure-multigrid level l (level 0 in 3D without its stencil)
+int papply(uwg_ctx* c, int l, const float* x, float* y) {
+    Work* w = work_of(c);
+    if (l == 0 && c->dim == 3) return uwg_pmg_apply0_mf(c, w->W0, x, y);
+    return uwg_pmg_apply(c, l, w->pst[l], x, y);
+}
+
 int cheb_L(uwg_ctx* c, int l, const float* b, float* x, int deg, bool x_zero) {
     Work* w = work_of(c);
     LevelVecs<float>& v = w->pv[l];
@@ -329,10 +336,10 @@ int cheb_L(uwg_ctx* c, int l, const float* b, float* x, int deg, bool x_zero) {
     double theta = 0.5 * (beta + alpha), delta = 0.5 * (beta - alpha);
     double sigma = theta / delta, rho = 1.0 / sigma;
     int rc;
-    if (!x_zero && (rc = uwg_pmg_apply(c, l, w->pst[l], x, v.t))) return rc;
+    if (!x_zero && (rc = papply(c, l, x, v.t))) return rc;
     vk_cheb<float>(s, n, b, x_zero ? nullptr : v.t, w->pdg[l], (float)(1.0 / theta), 0.f, v.d, x, 1, x_zero ? 1 : 0);
     for (int i = 1; i < deg; i++) {
-        if ((rc = uwg_pmg_apply(c, l, w->pst[l], x, v.t))) return rc;
+        if ((rc = papply(c, l, x, v.t))) return rc;
         double rho1 = 1.0 / (2.0 * sigma - rho);
         vk_cheb<float>(s, n, b, v.t, w->pdg[l], (float)(2.0 * rho1 / delta), (float)(rho1 * rho), v.d, x, 0, 0);
         rho = rho1;
@@ -349,7 +356,7 @@ int pvcycle(uwg_ctx* c, int l, const float* b, float* x) {
     LevelVecs<float>& v = w->pv[l];
     LevelVecs<float>& vc = w->pv[l + 1];
     if ((rc = cheb_L(c, l, b, x, 3, true))) return rc;
-    if ((rc = uwg_pmg_apply(c, l, w->pst[l], x, v.t))) return rc;
+    if ((rc = papply(c, l, x, v.t))) return rc;
     vk_axpby<float>(s, n, 1.f, b, -1.f, v.t);
     if ((rc = uwg_pmg_restrict(c, l + 1, v.t, vc.b))) return rc;
     if ((rc = pvcycle(c, l + 1, vc.b, vc.x))) return rc;
@@ -417,7 +424,7 @@ int lsolve(uwg_ctx* c, const float* b, float* x, double rtol, int maxit) {
     double bn = std::sqrt(d2[1]), rz = d2[0];
     if (bn == 0.0) return UWG_OK;
     for (int it = 1; it <= maxit; it++) {
-        if ((rc = uwg_pmg_apply(c, 0, w->pst[0], p, q))) return rc;
+        if ((rc = papply(c, 0, p, q))) return rc;
         double pq;
         const float* a1[1] = {p};
         const float* b1[1] = {q};
@@ -472,7 +479,7 @@ int bfbt_setup(uwg_ctx* c) {
         UWG_CUDA(c, cudaMemcpyAsync(v.x, hv.data(), sizeof(float) * n, cudaMemcpyHostToDevice, s));
         double lam = 1.0;
         for (int it = 0; it < 30; it++) {
-            if ((rc = uwg_pmg_apply(c, l, w->pst[l], v.x, v.t))) return rc;
+            if ((rc = papply(c, l, v.x, v.t))) return rc;
             vk_pointwise_div<float>(s, n, v.t, w->pdg[l], v.d);
             double d2[2];
             const float* a[2] = {v.d, v.x};
