@@ -161,6 +161,8 @@ typedef struct {
     int zero_guess;        /* 1: start from u=p=0, else from the given u, p */
     int schur_pc;          /* 0: assembled Uzawa term S^ (the reference's "uw"), 1: scaled BFBt */
     double schur_pc_rtol;  /* relative tolerance of the pressure-Laplacian solves inside BFBt */
+    int relax_inner;       /* 1: loosen the velocity-solve tolerance inside the Schur iteration as its
+                              residual falls (inexact Krylov), then confirm with one strict residual */
 } uwg_solve_opts;
 
 typedef struct {

@@ -34,7 +34,8 @@ class SolveOpts(ctypes.Structure):
     _fields_ = [("mixed", ctypes.c_int), ("rtol", ctypes.c_double), ("inner_rtol", ctypes.c_double),
                 ("outer_rtol", ctypes.c_double), ("max_inner", ctypes.c_int), ("max_outer", ctypes.c_int),
                 ("mg_levels", ctypes.c_int), ("smooth_steps", ctypes.c_int), ("restart", ctypes.c_int),
-                ("zero_guess", ctypes.c_int), ("schur_pc", ctypes.c_int), ("schur_pc_rtol", ctypes.c_double)]
+                ("zero_guess", ctypes.c_int), ("schur_pc", ctypes.c_int), ("schur_pc_rtol", ctypes.c_double),
+                ("relax_inner", ctypes.c_int)]
 
 
 class SolveStats(ctypes.Structure):
