@@ -219,7 +219,7 @@ __global__ void k_bc_copy(int64_t n, const uint8_t* bc, const T* x, T* y) {
 // y_e = K_e u_e for one 3D Q1 element from its equivalent-quadrature weights
 // (sum-factorised on the 3-point rule).  hx,hy,hz = 2/h per axis.
 template <typename T>
-__device__ __forceinline__ void q1_3d_element(const T* __restrict__ W, int64_t n_el, int64_t e, T hx, T hy, T hz,
+__device__ __forceinline__ void q1_3d_element(const T* __restrict__ Wp, int64_t stride, T hx, T hy, T hz,
                                               const T (&u)[8][3], T (&out)[8][3]) {
     // physical gradients on the 3x3 face grids
     T Gx[3][3][3], Gy[3][3][3], Gz[3][3][3];   // [c][p][q]
@@ -266,7 +266,7 @@ __device__ __forceinline__ void q1_3d_element(const T* __restrict__ W, int64_t n
         for (int py = 0; py < 3; py++)
 #pragma unroll
             for (int px = 0; px < 3; px++) {
-                T w = W[(int64_t)(px + 3 * py + 9 * pz) * n_el + e];
+                T w = Wp[(int64_t)(px + 3 * py + 9 * pz) * stride];
                 T uxx = Gx[0][py][pz], uxy = Gy[0][px][pz], uxz = Gz[0][px][py];
                 T uyx = Gx[1][py][pz], uyy = Gy[1][px][pz], uyz = Gz[1][px][py];
                 T uzx = Gx[2][py][pz], uzy = Gy[2][px][pz], uzz = Gz[2][px][py];
@@ -340,7 +340,7 @@ __global__ void __launch_bounds__(128) k_applyK_q1_3d(uwg_lgeom g, const T* __re
             u[n][c] = (fix[n][c] && mask_in) ? (T)0 : x[dof];
         }
     T out[8][3];
-    q1_3d_element<T>(W, g.n_el, e, hx, hy, hz, u, out);
+    q1_3d_element<T>(W + e, g.n_el, hx, hy, hz, u, out);
 #pragma unroll
     for (int n = 0; n < 8; n++)
 #pragma unroll
@@ -354,26 +354,50 @@ __global__ void __launch_bounds__(128) k_applyK_q1_3d(uwg_lgeom g, const T* __re
 // the element results into a shared tile with shared-memory atomics, and then
 // writes nodes inside the tile with plain stores and nodes on the tile faces
 // (shared with neighbouring tiles) with global atomics: 8x fewer global
-// atomics than the element-per-thread kernel.
+// atomics than the element-per-thread kernel.  In FP32 the tile's 27 weight
+// planes are copied to shared memory with cp.async at the start, so their
+// DRAM latency overlaps the nodal staging instead of stalling the element
+// arithmetic.
 #define KT_X 8
 #define KT_Y 8
 #define KT_Z 4
-template <typename T>
-__global__ void __launch_bounds__(KT_X * KT_Y * KT_Z) k_applyK_q1_3d_tiled(uwg_lgeom g, const T* __restrict__ W,
-                                                                         const uint8_t* __restrict__ bc,
-                                                                         const T* __restrict__ x, T* y) {
+#define KT_N (KT_X * KT_Y * KT_Z)
+
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+    unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;\n" ::: "memory");
+}
+
+template <typename T, bool STAGE_W>
+__global__ void __launch_bounds__(KT_N, STAGE_W ? 3 : 1) k_applyK_q1_3d_tiled(uwg_lgeom g, const T* __restrict__ W,
+                                                            const uint8_t* __restrict__ bc,
+                                                            const T* __restrict__ x, T* y) {
     constexpr int NX = KT_X + 1, NY = KT_Y + 1, NZ = KT_Z + 1, NN = NX * NY * NZ;
     __shared__ T xs[NN * 3];
     __shared__ T ys[NN * 3];
+    __shared__ T ws[STAGE_W ? 27 * KT_N : 1];
     int ntx = (g.res[0] + KT_X - 1) / KT_X, nty = (g.res[1] + KT_Y - 1) / KT_Y;
     int tile = blockIdx.x;
     int tx0 = (tile % ntx) * KT_X, ty0 = ((tile / ntx) % nty) * KT_Y, tz0 = (tile / (ntx * nty)) * KT_Z;
     int64_t gnx = g.nx[0], gny = g.nx[1];
+    int li = threadIdx.x % KT_X, lj = (threadIdx.x / KT_X) % KT_Y, lk = threadIdx.x / (KT_X * KT_Y);
+    int ex = tx0 + li, ey = ty0 + lj, ez = tz0 + lk;
+    const bool own = ex < g.res[0] && ey < g.res[1] && ez < g.res[2];
+    const int64_t e = own ? ex + (int64_t)g.res[0] * (ey + (int64_t)g.res[1] * ez) : 0;
+    if constexpr (STAGE_W) {
+        if (own) {
+#pragma unroll
+            for (int j = 0; j < 27; j++) cp_async4(&ws[j * KT_N + threadIdx.x], W + (int64_t)j * g.n_el + e);
+        }
+    }
     // stage nodal values (masked) and clear the accumulator
     for (int k = threadIdx.x; k < NN * 3; k += blockDim.x) {
         int nl = k / 3, c = k % 3;
-        int li = nl % NX, lj = (nl / NX) % NY, lk = nl / (NX * NY);
-        int gi = tx0 + li, gj = ty0 + lj, gk = tz0 + lk;
+        int ni = nl % NX, nj = (nl / NX) % NY, nk = nl / (NX * NY);
+        int gi = tx0 + ni, gj = ty0 + nj, gk = tz0 + nk;
         T v = (T)0;
         if (gi < g.nx[0] && gj < g.nx[1] && gk < g.nx[2]) {
             int64_t dof = (gi + gnx * (gj + gny * (int64_t)gk)) * 3 + c;
@@ -382,11 +406,9 @@ __global__ void __launch_bounds__(KT_X * KT_Y * KT_Z) k_applyK_q1_3d_tiled(uwg_l
         xs[k] = v;
         ys[k] = (T)0;
     }
+    if constexpr (STAGE_W) cp_async_wait_all();
     __syncthreads();
-    int li = threadIdx.x % KT_X, lj = (threadIdx.x / KT_X) % KT_Y, lk = threadIdx.x / (KT_X * KT_Y);
-    int ex = tx0 + li, ey = ty0 + lj, ez = tz0 + lk;
-    if (ex < g.res[0] && ey < g.res[1] && ez < g.res[2]) {
-        int64_t e = ex + (int64_t)g.res[0] * (ey + (int64_t)g.res[1] * ez);
+    if (own) {
         const T hx = (T)(2.0 / (g.ax[0][ex + 1] - g.ax[0][ex]));
         const T hy = (T)(2.0 / (g.ax[1][ey + 1] - g.ax[1][ey]));
         const T hz = (T)(2.0 / (g.ax[2][ez + 1] - g.ax[2][ez]));
@@ -397,7 +419,8 @@ __global__ void __launch_bounds__(KT_X * KT_Y * KT_Z) k_applyK_q1_3d_tiled(uwg_l
 #pragma unroll
             for (int c = 0; c < 3; c++) u[n][c] = xs[sl * 3 + c];
         }
-        q1_3d_element<T>(W, g.n_el, e, hx, hy, hz, u, out);
+        if constexpr (STAGE_W) q1_3d_element<T>(ws + threadIdx.x, KT_N, hx, hy, hz, u, out);
+        else q1_3d_element<T>(W + e, g.n_el, hx, hy, hz, u, out);
 #pragma unroll
         for (int n = 0; n < 8; n++) {
             int sl = (li + (n & 1)) + NX * ((lj + ((n >> 1) & 1)) + NY * (lk + ((n >> 2) & 1)));
@@ -483,7 +506,7 @@ int uwg_ops_applyK(uwg_ctx* c, int l, const T* x, T* y) {
     if (c->dim == 3) {
         unsigned tiles = (unsigned)(((L.res[0] + KT_X - 1) / KT_X) * ((L.res[1] + KT_Y - 1) / KT_Y) *
                                     ((L.res[2] + KT_Z - 1) / KT_Z));
-        k_applyK_q1_3d_tiled<T><<<tiles, KT_X * KT_Y * KT_Z, 0, c->stream>>>(g, W, L.bc, x, y);
+        k_applyK_q1_3d_tiled<T, sizeof(T) == 4><<<tiles, KT_N, 0, c->stream>>>(g, W, L.bc, x, y);
     } else {
         k_applyK_q1_2d<T><<<nblk(L.n_el, 128), 128, 0, c->stream>>>(g, W, L.bc, true, x, y);
     }
