@@ -163,6 +163,7 @@ typedef struct {
     double schur_pc_rtol;  /* relative tolerance of the pressure-Laplacian solves inside BFBt */
     int relax_inner;       /* 1: loosen the velocity-solve tolerance inside the Schur iteration as its
                               residual falls (inexact Krylov), then confirm with one strict residual */
+    int schur_pc_smooth;   /* Chebyshev degree of the pressure-multigrid smoother inside BFBt */
 } uwg_solve_opts;
 
 typedef struct {

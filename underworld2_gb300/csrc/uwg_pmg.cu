@@ -286,7 +286,13 @@ __global__ void k_pdense_fix(int64_t m, int64_t n, double* A) {
 // 16x8x8 tile of cells; it stages the tile's cell values with a one-cell halo
 // in shared memory, forms W G x at the tile's 17x9x9 nodes in shared memory,
 // and then sums G^T over each cell's eight nodes.  DRAM traffic is x, W (three
-// floats per node) and y: about a sixth of the 27-coefficient stencil's.
+// floats per node) and y: about a sixth of the 27-coefficient stencil's.  The
+// tile's W is copied into shared memory with cp.async first, so its latency
+// overlaps the staging of x.
+__device__ __forceinline__ void pmg_cp_async4(void* smem, const void* gmem) {
+    unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem));
+}
 #define PT_X 16
 #define PT_Y 8
 #define PT_Z 8
@@ -301,6 +307,16 @@ __global__ void __launch_bounds__(256) k_papply0_mf(uwg_lgeom g, const float* __
     const int tile = blockIdx.x;
     const int tx0 = (tile % ntx) * PT_X, ty0 = ((tile / ntx) % nty) * PT_Y, tz0 = (tile / (ntx * nty)) * PT_Z;
     const int64_t sy = g.res[0], sz = (int64_t)g.res[0] * g.res[1];
+    for (int k = threadIdx.x; k < NN; k += blockDim.x) {
+        const int ni = k % NX, nj = (k / NX) % NY, nk = k / (NX * NY);
+        const int gi = tx0 + ni, gj = ty0 + nj, gk = tz0 + nk;
+        if (gi < g.nx[0] && gj < g.nx[1] && gk < g.nx[2]) {
+            const float* src = W + (gi + (int64_t)g.nx[0] * (gj + (int64_t)g.nx[1] * gk)) * 3;
+            pmg_cp_async4(&vs[0][k], src);
+            pmg_cp_async4(&vs[1][k], src + 1);
+            pmg_cp_async4(&vs[2][k], src + 2);
+        }
+    }
     for (int k = threadIdx.x; k < NH; k += blockDim.x) {
         const int i = k % HX, j = (k / HX) % HY, l = k / (HX * HY);
         const int cx = tx0 - 1 + i, cy = ty0 - 1 + j, cz = tz0 - 1 + l;
@@ -313,6 +329,7 @@ __global__ void __launch_bounds__(256) k_papply0_mf(uwg_lgeom g, const float* __
         const double* a = d == 0 ? g.ax[0] : d == 1 ? g.ax[1] : g.ax[2];
         hs[d][i] = (c0 >= 0 && c0 < r) ? (float)(a[c0 + 1] - a[c0]) : 0.f;
     }
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;\n" ::: "memory");
     __syncthreads();
     for (int k = threadIdx.x; k < NN; k += blockDim.x) {
         const int ni = k % NX, nj = (k / NX) % NY, nk = k / (NX * NY);
@@ -329,10 +346,9 @@ __global__ void __launch_bounds__(256) k_papply0_mf(uwg_lgeom g, const float* __
                 v1 += (cy ? a1 : -a1) * pe;
                 v2 += (cz ? a2 : -a2) * pe;
             }
-            const int64_t node = gi + (int64_t)g.nx[0] * (gj + (int64_t)g.nx[1] * gk);
-            v0 *= W[node * 3 + 0];
-            v1 *= W[node * 3 + 1];
-            v2 *= W[node * 3 + 2];
+            v0 *= vs[0][k];
+            v1 *= vs[1][k];
+            v2 *= vs[2][k];
         }
         vs[0][k] = v0;
         vs[1][k] = v1;

@@ -61,6 +61,7 @@ struct Work {
     cudaStream_t gstream = nullptr;
     cudaGraphExec_t g_v64 = nullptr, g_v32 = nullptr, g_pv = nullptr;
     int g_deg = 0;
+    int pdeg = 3, g_pdeg = 0;                  // pressure smoother degree (in use / captured)
 };
 
 Work* work_of(uwg_ctx* c) {
@@ -356,18 +357,18 @@ int pvcycle(uwg_ctx* c, int l, const float* b, float* x) {
     if (l == c->nlev - 1) return uwg_ops_dense_mv32(c, n, w->pcinv, b, x);
     LevelVecs<float>& v = w->pv[l];
     LevelVecs<float>& vc = w->pv[l + 1];
-    if ((rc = cheb_L(c, l, b, x, 3, true))) return rc;
+    if ((rc = cheb_L(c, l, b, x, w->pdeg, true))) return rc;
     if ((rc = papply(c, l, x, v.t))) return rc;
     vk_axpby<float>(s, n, 1.f, b, -1.f, v.t);
     if ((rc = uwg_pmg_restrict(c, l + 1, v.t, vc.b))) return rc;
     if ((rc = pvcycle(c, l + 1, vc.b, vc.x))) return rc;
     if ((rc = uwg_pmg_prolong_add(c, l + 1, vc.x, x))) return rc;
-    return cheb_L(c, l, b, x, 3, false);
+    return cheb_L(c, l, b, x, w->pdeg, false);
 }
 
 int run_pvcycle(uwg_ctx* c, const float* b, float* x) {
     Work* w = work_of(c);
-    if (w->g_pv && b == w->pcg_r && x == w->pcg_z) {
+    if (w->g_pv && w->g_pdeg == w->pdeg && b == w->pcg_r && x == w->pcg_z) {
         UWG_CUDA(c, cudaGraphLaunch(w->g_pv, c->stream));
         return UWG_OK;
     }
@@ -403,6 +404,7 @@ int capture_cycles(uwg_ctx* c, int deg) {
     if ((rc = capture(c, &w->g_v32, [&]() { return vcycle<float>(c, 0, w->cg32_r, w->cg32_z, deg); }))) return rc;
     if ((rc = capture(c, &w->g_pv, [&]() { return pvcycle(c, 0, w->pcg_r, w->pcg_z); }))) return rc;
     w->g_deg = deg;
+    w->g_pdeg = w->pdeg;
     return UWG_OK;
 }
 
@@ -567,6 +569,7 @@ extern "C" void uwg_solve_opts_default(uwg_solve_opts* o) {
     o->smooth_steps = 3;
     o->restart = 120;
     o->relax_inner = 1;
+    o->schur_pc_smooth = 3;
     o->zero_guess = 1;
     o->schur_pc = 1;
     o->schur_pc_rtol = 1e-2;
@@ -752,6 +755,13 @@ extern "C" int uwg_stokes_solve(uwg_ctx* c, const uwg_solve_opts* o, double* u, 
     if (rc) return rc;
     Work* w = work_of(c);
     cudaStream_t s = c->stream;
+    if (o->schur_pc_smooth < 1 || o->schur_pc_smooth > 16)
+        return uwg_set_error(c, UWG_ERR_ARG, "schur_pc_smooth must be in [1, 16]");
+    w->pdeg = o->schur_pc_smooth;
+    if (w->pdeg != w->g_pdeg &&
+        (rc = capture(c, &w->g_pv, [&]() { return pvcycle(c, 0, w->pcg_r, w->pcg_z); })) == UWG_OK)
+        w->g_pdeg = w->pdeg;
+    if (rc) return rc;
     int64_t nv = c->n_vdof, np = c->n_pdof;
     SolveCfg cfg{o->mixed != 0, o->inner_rtol, o->max_inner, std::max(1, o->smooth_steps), o->schur_pc,
                  o->schur_pc_rtol > 0.0 ? o->schur_pc_rtol : 1e-2, o->relax_inner != 0};
