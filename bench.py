@@ -158,7 +158,7 @@ def run_gpu(args):
     npart = x0.shape[0]
     u = ctx.zeros(ctx.n_vdof)
     p = ctx.zeros(ctx.n_pdof)
-    opts = dict(rtol=1e-8, inner_rtol=args.inner_rtol, outer_rtol=args.outer_rtol, smooth_steps=3, restart=120,
+    opts = dict(rtol=1e-8, inner_rtol=args.inner_rtol, outer_rtol=args.outer_rtol, smooth_steps=2, restart=120,
                 schur_pc=args.schur_pc, schur_pc_rtol=args.bfbt_rtol, max_outer=args.max_outer)
     ev = lambda: torch.cuda.Event(enable_timing=True)
 
@@ -371,7 +371,7 @@ def run_profile_solve(args):
     ctx.assemble(off, lst, ip_xi, ip_w, eta, body)
     u, p = ctx.zeros(ctx.n_vdof), ctx.zeros(ctx.n_pdof)
     st = ctx.solve(u, p, mixed=1 if args.mode == "mixed" else 0, rtol=1e-8, inner_rtol=args.inner_rtol,
-                   outer_rtol=args.outer_rtol, smooth_steps=3, restart=120, schur_pc=args.schur_pc,
+                   outer_rtol=args.outer_rtol, smooth_steps=2, restart=120, schur_pc=args.schur_pc,
                    schur_pc_rtol=args.bfbt_rtol, max_outer=args.max_outer)
     torch.cuda.synchronize()
     print(json.dumps({"profile_solve": args.config, "particles_per_cell": ppc,

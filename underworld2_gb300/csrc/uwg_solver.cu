@@ -61,7 +61,7 @@ struct Work {
     cudaStream_t gstream = nullptr;
     cudaGraphExec_t g_v64 = nullptr, g_v32 = nullptr, g_pv = nullptr;
     int g_deg = 0;
-    int pdeg = 3, g_pdeg = 0;                  // pressure smoother degree (in use / captured)
+    int pdeg = 2, g_pdeg = 0;                  // pressure smoother degree (in use / captured)
 };
 
 Work* work_of(uwg_ctx* c) {
@@ -569,7 +569,7 @@ extern "C" void uwg_solve_opts_default(uwg_solve_opts* o) {
     o->smooth_steps = 3;
     o->restart = 120;
     o->relax_inner = 1;
-    o->schur_pc_smooth = 3;
+    o->schur_pc_smooth = 2;
     o->zero_guess = 1;
     o->schur_pc = 1;
     o->schur_pc_rtol = 1e-2;
