@@ -554,7 +554,7 @@ int uwg_solver_setup(uwg_ctx* c) {
     }
     if ((rc = uwg_ops_dense_coarse(c, c->nlev - 1))) return rc;
     if ((rc = bfbt_setup(c))) return rc;
-    return capture_cycles(c, 3);
+    return capture_cycles(c, work_of(c)->g_deg > 0 ? work_of(c)->g_deg : 3);
 }
 
 extern "C" void uwg_solve_opts_default(uwg_solve_opts* o) {
@@ -762,6 +762,9 @@ extern "C" int uwg_stokes_solve(uwg_ctx* c, const uwg_solve_opts* o, double* u, 
         (rc = capture(c, &w->g_pv, [&]() { return pvcycle(c, 0, w->pcg_r, w->pcg_z); })) == UWG_OK)
         w->g_pdeg = w->pdeg;
     if (rc) return rc;
+    // velocity V-cycle graphs for this smoother degree
+    if (std::max(1, o->smooth_steps) != w->g_deg && (rc = capture_cycles(c, std::max(1, o->smooth_steps))))
+        return rc;
     int64_t nv = c->n_vdof, np = c->n_pdof;
     SolveCfg cfg{o->mixed != 0, o->inner_rtol, o->max_inner, std::max(1, o->smooth_steps), o->schur_pc,
                  o->schur_pc_rtol > 0.0 ? o->schur_pc_rtol : 1e-2, o->relax_inner != 0};
