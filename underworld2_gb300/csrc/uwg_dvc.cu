@@ -31,10 +31,26 @@ struct dvc_args {
     int16_t* scratch;    // per warp: claimed[RC] + pool0[PCAP] + pool1[PCAP]
     int64_t pcap;
     int32_t* status;     // [0] = first error code, [1] = element
+    int nmax;            // particle slots per warp in shared memory (<= DVC_NMAX)
 };
+
+// Shared memory of one warp for a grid of RC cells and nmax particle slots.
+__host__ __device__ inline size_t dvc_warp_bytes(int RC, int nmax) {
+    size_t b = (size_t)RC * 2 + (size_t)nmax * 3 * 8 + (size_t)nmax * 4 * 4 + (size_t)nmax * 3 * 4;
+    return (b + 15) & ~(size_t)15;
+}
 
 __device__ __forceinline__ void dvc_fail(int32_t* status, int code, int64_t el) {
     if (atomicCAS(&status[0], 0, code) == 0) status[1] = (int32_t)el;
+}
+
+// Largest particle count of any element (sizes the kernel's shared memory).
+__global__ void k_max_count(int64_t n_el, const int32_t* off, int32_t* out) {
+    int m = 0;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n_el; e += (int64_t)gridDim.x * blockDim.x)
+        m = max(m, off[e + 1] - off[e]);
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, m);
 }
 
 template <int DIM>
@@ -46,17 +62,18 @@ __global__ void __launch_bounds__(32 * DVC_WARPS) k_dvc(dvc_args a) {
     int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     // per-block cell centre table (accumulated exactly as _DVCWeights_ConstructGrid)
     double* cen = (double*)smem;                       // [16]
-    size_t per_warp = (size_t)RC * 2 + (size_t)DVC_NMAX * 3 * 8 + (size_t)DVC_NMAX * 4 * 4;
-    per_warp = (per_warp + 15) & ~(size_t)15;
-    unsigned char* wbase = smem + 128 + per_warp * wib;
-    double* xs = (double*)wbase;                       // [NMAX][3]
-    int32_t* hdr = (int32_t*)(xs + DVC_NMAX * 3);      // [2][NMAX][2] (offset, length) per pool
-    uint8_t* owner = (uint8_t*)(hdr + DVC_NMAX * 4);   // [RC]
+    float* cenf = (float*)(cen + 16);                  // [16] FP32 copies
+    const int NM = a.nmax;
+    unsigned char* wbase = smem + 192 + dvc_warp_bytes(RC, NM) * wib;
+    double* xs = (double*)wbase;                       // [NM][3]
+    int32_t* hdr = (int32_t*)(xs + NM * 3);            // [2][NM][2] (offset, length) per pool
+    float* xf = (float*)(hdr + NM * 4);                // [NM][3] FP32 copies (distance pre-test)
+    uint8_t* owner = (uint8_t*)(xf + NM * 3);          // [RC]
     uint8_t* done = owner + RC;                        // [RC]
     if (threadIdx.x == 0) {
         double dx = (1.0 - -1.0) / R;
         double X = -1.0 - dx / 2.0;
-        for (int i = 0; i < R; i++) { X = X + dx; cen[i] = X; }
+        for (int i = 0; i < R; i++) { X = X + dx; cen[i] = X; cenf[i] = (float)X; }
     }
     __syncthreads();
     const double dx = (1.0 - -1.0) / R;
@@ -72,11 +89,14 @@ __global__ void __launch_bounds__(32 * DVC_WARPS) k_dvc(dvc_args a) {
         int32_t o0 = a.off[el];
         int n = a.off[el + 1] - o0;
         if (n == 0) { if (lane == 0) dvc_fail(a.status, UWG_ERR_EMPTY_CELL, el); continue; }
-        if (n > DVC_NMAX) { if (lane == 0) dvc_fail(a.status, UWG_ERR_CELL_FULL, el); continue; }
+        if (n > NM) { if (lane == 0) dvc_fail(a.status, UWG_ERR_CELL_FULL, el); continue; }
         for (int k = lane; k < n; k += 32) {
             xs[k * 3 + 0] = a.ip_xi[(int64_t)(o0 + k) * DIM + 0];
             xs[k * 3 + 1] = a.ip_xi[(int64_t)(o0 + k) * DIM + 1];
             xs[k * 3 + 2] = DIM == 3 ? a.ip_xi[(int64_t)(o0 + k) * DIM + DIM - 1] : 0.0;
+            xf[k * 3 + 0] = (float)xs[k * 3 + 0];
+            xf[k * 3 + 1] = (float)xs[k * 3 + 1];
+            xf[k * 3 + 2] = (float)xs[k * 3 + 2];
         }
         for (int c = lane; c < RC; c += 32) { owner[c] = 0xFF; done[c] = 0; }
         __syncwarp();
@@ -120,22 +140,27 @@ __global__ void __launch_bounds__(32 * DVC_WARPS) k_dvc(dvc_args a) {
             if (start + cnt > a.pcap) overflow = true;
             for (int k = lane; k < cnt && start + k < a.pcap; k += 32) done[pool[dst][start + k]] = 0;
             if (lane == 0) {
-                hdr[(dst * DVC_NMAX + i) * 2 + 0] = (int32_t)start;
-                hdr[(dst * DVC_NMAX + i) * 2 + 1] = cnt;
+                hdr[(dst * NM + i) * 2 + 0] = (int32_t)start;
+                hdr[(dst * NM + i) * 2 + 1] = cnt;
             }
             bump = start + cnt;
             __syncwarp();
         };
 
-        // seeding (:687-705 / :735-756)
-        for (int i = 0; i < n; i++) {
+        // seeding (:687-705 / :735-756): the seed cells of all particles are
+        // computed in parallel (same expressions), then claimed in order
+        for (int i = lane; i < n; i += 32) {
             int k = (int)((xs[i * 3 + 0] - -1.0) / dx);
             int j = (int)((xs[i * 3 + 1] - -1.0) / dx);
             int l = DIM == 3 ? (int)((xs[i * 3 + 2] - -1.0) / dx) : 0;
             if (k == R) k--;
             if (j == R) j--;
             if (DIM == 3 && l == R) l--;
-            int c = k + j * R + l * R * R;
+            hdr[(NM + i) * 2] = k + j * R + l * R * R;   // pool-1 headers are unused until round 1
+        }
+        __syncwarp();
+        for (int i = 0; i < n; i++) {
+            int c = hdr[(NM + i) * 2];
             if (lane == 0) { owner[c] = (uint8_t)i; claimed[0] = (int16_t)c; }
             __syncwarp();
             update(i, 1, 0);
@@ -148,9 +173,10 @@ __global__ void __launch_bounds__(32 * DVC_WARPS) k_dvc(dvc_args a) {
             bump = 0;
             int claimed_total = 0;
             for (int i = 0; i < n; i++) {
-                int bo = hdr[(cur * DVC_NMAX + i) * 2 + 0], bl = hdr[(cur * DVC_NMAX + i) * 2 + 1];
+                int bo = hdr[(cur * NM + i) * 2 + 0], bl = hdr[(cur * NM + i) * 2 + 1];
                 int ncl = 0;
                 const double px = xs[i * 3 + 0], py = xs[i * 3 + 1], pz = xs[i * 3 + 2];
+                const float fpx = xf[i * 3 + 0], fpy = xf[i * 3 + 1], fpz = xf[i * 3 + 2];
                 for (int base = 0; base < bl; base += 32) {
                     int t = base + lane;
                     bool take = false;
@@ -160,6 +186,22 @@ __global__ void __launch_bounds__(32 * DVC_WARPS) k_dvc(dvc_args a) {
                         int o = owner[c0];
                         if (o == 0xFF) take = true;
                         else if (o != i) {
+                            // FP32 pre-test: coordinates lie in [-1, 1], so the FP32
+                            // value is within 2e-5 of the exact one; only values near
+                            // zero need the FP64 expression, whose sign is the result.
+                            float fd;
+                            {
+                                const float fx0 = cenf[c0 % R], fy0 = cenf[(c0 / R) % R];
+                                const float fx1 = xf[o * 3 + 0], fy1 = xf[o * 3 + 1];
+                                fd = (fx1 + fpx - fx0 - fx0) * (fx1 - fpx) + (fy1 + fpy - fy0 - fy0) * (fy1 - fpy);
+                                if (DIM == 3) {
+                                    const float fz0 = cenf[c0 / (R * R)], fz1 = xf[o * 3 + 2];
+                                    fd += (fz1 + fpz - fz0 - fz0) * (fz1 - fpz);
+                                }
+                            }
+                            if (fd > 1e-4f) take = true;
+                            else if (fd < -1e-4f) take = false;
+                            else {
                             double x0 = cen[c0 % R], y0 = cen[(c0 / R) % R];
                             double x1 = xs[o * 3 + 0], y1 = xs[o * 3 + 1];
                             double dist;
@@ -171,6 +213,7 @@ __global__ void __launch_bounds__(32 * DVC_WARPS) k_dvc(dvc_args a) {
                                        (z1 + pz - z0 - z0) * (z1 - pz);
                             }
                             take = dist > 0.0;
+                            }
                         }
                     }
                     unsigned tb = __ballot_sync(0xffffffffu, take);
@@ -195,23 +238,51 @@ __global__ void __launch_bounds__(32 * DVC_WARPS) k_dvc(dvc_args a) {
             continue;
         }
 
-        // centroids and weights (:198-254), summed in cell order per particle
+        // centroids and weights (:198-254), summed in cell order per particle:
+        // a stable counting sort of the cells by owner (into `claimed`, free
+        // now) gives every particle its cells in cell order, so each lane sums
+        // its own particle's centres in exactly the reference's order.
+        int32_t* cnt = hdr;            // [NM]
+        int32_t* pos = hdr + NM;       // [NM]
+        for (int i = lane; i < n; i += 32) cnt[i] = 0;
+        __syncwarp();
+        for (int c = lane; c < RC; c += 32) {
+            int o = owner[c];
+            if (o < n) atomicAdd(&cnt[o], 1);
+        }
+        __syncwarp();
+        if (lane == 0) {
+            int run = 0;
+            for (int i = 0; i < n; i++) { pos[i] = run; run += cnt[i]; }
+        }
+        __syncwarp();
+        for (int cb = 0; cb < RC; cb += 32) {
+            int c = cb + lane;
+            int o = c < RC ? owner[c] : 0xFF;
+            bool valid = o < n;
+            unsigned peers = __match_any_sync(0xffffffffu, valid ? o : 0x100 + lane);
+            int p0 = valid ? pos[o] : 0;
+            __syncwarp();
+            if (valid) {
+                claimed[p0 + __popc(peers & lt)] = (int16_t)c;
+                if (__ffs(peers) - 1 == lane) pos[o] = p0 + __popc(peers);
+            }
+            __syncwarp();
+        }
         for (int g0 = 0; g0 < n; g0 += 32) {
             int i = g0 + lane;
-            double sx = 0.0, sy = 0.0, sz = 0.0;
-            int cnt = 0;
-            for (int c = 0; c < RC; c++) {
-                if (owner[c] == i) {
+            if (i < n) {
+                const int m = cnt[i], end = pos[i];
+                double sx = 0.0, sy = 0.0, sz = 0.0;
+                for (int k = end - m; k < end; k++) {
+                    const int c = claimed[k];
                     sx += cen[c % R];
                     sy += cen[(c / R) % R];
                     if (DIM == 3) sz += cen[c / (R * R)];
-                    cnt++;
                 }
-            }
-            if (i < n) {
                 int64_t s = o0 + i;
-                a.ip_w[s] = cnt * da;
-                if (cnt != 0) { sx /= cnt; sy /= cnt; sz /= cnt; }
+                a.ip_w[s] = m * da;
+                if (m != 0) { sx /= m; sy /= m; sz /= m; }
                 a.ip_xi[s * DIM + 0] = sx;
                 a.ip_xi[s * DIM + 1] = sy;
                 if (DIM == 3) a.ip_xi[s * DIM + DIM - 1] = sz;
@@ -227,9 +298,15 @@ extern "C" int uwg_dvc_weights(uwg_ctx* c, int res, const int32_t* cell_offsets,
         return uwg_set_error(c, UWG_ERR_ARG, "uwg_dvc_weights: bad argument (res must be 1..16)");
     int dim = c->dim;
     int RC = dim == 3 ? res * res * res : res * res;
-    size_t per_warp = (size_t)RC * 2 + (size_t)DVC_NMAX * 3 * 8 + (size_t)DVC_NMAX * 4 * 4;
-    per_warp = (per_warp + 15) & ~(size_t)15;
-    size_t shm = 128 + per_warp * DVC_WARPS;
+    // size the per-warp particle slots by the fullest element (more warps per SM)
+    int32_t* mx = (int32_t*)c->red;
+    UWG_CUDA(c, cudaMemsetAsync(mx, 0, 4, c->stream));
+    k_max_count<<<(unsigned)std::min<int64_t>((c->n_el + 255) / 256, 4096), 256, 0, c->stream>>>(c->n_el, cell_offsets, mx);
+    int32_t nfull = 0;
+    UWG_CUDA(c, cudaMemcpyAsync(&nfull, mx, 4, cudaMemcpyDeviceToHost, c->stream));
+    UWG_CUDA(c, cudaStreamSynchronize(c->stream));
+    const int nmax = std::min(DVC_NMAX, std::max(8, (nfull + 7) & ~7));
+    size_t shm = 192 + dvc_warp_bytes(RC, nmax) * DVC_WARPS;
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -248,6 +325,7 @@ extern "C" int uwg_dvc_weights(uwg_ctx* c, int res, const int32_t* cell_offsets,
     a.ip_xi = ip_xi;
     a.ip_w = ip_w;
     a.pcap = (int64_t)RC * 8;
+    a.nmax = nmax;
     void* scratch = nullptr;
     size_t sbytes = (size_t)warps * (RC + 2 * a.pcap) * 2 + 64;
     UWG_CUDA(c, cudaMallocAsync(&scratch, sbytes, c->stream));
@@ -312,10 +390,9 @@ extern "C" int uwg_dvc_weights_noalloc(int dim, int res, int64_t n_el, const int
         base = (unsigned char*)uwg_noalloc_ptr[dev];
     }
     int RC = dim == 3 ? res * res * res : res * res;
-    size_t per_warp = (size_t)RC * 2 + (size_t)DVC_NMAX * 3 * 8 + (size_t)DVC_NMAX * 4 * 4;
-    per_warp = (per_warp + 15) & ~(size_t)15;
-    size_t shm = 128 + per_warp * DVC_WARPS;
+    size_t shm = 192 + dvc_warp_bytes(RC, DVC_NMAX) * DVC_WARPS;
     dvc_args a;
+    a.nmax = DVC_NMAX;
     a.n_el = n_el;
     a.R = res;
     a.off = cell_offsets;
