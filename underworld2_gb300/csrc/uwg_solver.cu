@@ -60,6 +60,10 @@ struct Work {
     // CUDA graphs of the V-cycles (captured at setup, replayed by the Krylov loops)
     cudaStream_t gstream = nullptr;
     cudaGraphExec_t g_v64 = nullptr, g_v32 = nullptr, g_pv = nullptr;
+    cudaGraphExec_t g_lcg = nullptr;          // two CG iterations of the L-solve
+    float* pcg_x = nullptr;                   // L-solve iterate (fixed buffer of the graph)
+    double* lcg_s = nullptr;                  // L-solve scalars on the device
+    double* lcg_h = nullptr;                  // pinned host mirror of lcg_s
     int g_deg = 0;
     int pdeg = 2, g_pdeg = 0;                  // pressure smoother degree (in use / captured)
 };
@@ -107,6 +111,9 @@ int work_init(uwg_ctx* c, int restart) {
         }
         w->W0 = dalloc<float>(c, nv);
         w->pcg_r = dalloc<float>(c, np); w->pcg_z = dalloc<float>(c, np);
+        w->pcg_x = dalloc<float>(c, np);
+        w->lcg_s = dalloc<double>(c, 16);
+        if (!w->lcg_h && cudaMallocHost((void**)&w->lcg_h, sizeof(double) * 16) != cudaSuccess) w->lcg_h = nullptr;
         w->pcg_p = dalloc<float>(c, np); w->pcg_q = dalloc<float>(c, np);
         w->bf_r = dalloc<float>(c, np); w->bf_y = dalloc<float>(c, np);
         w->bf_m = dalloc<float>(c, np); w->bf_z = dalloc<float>(c, np);
@@ -397,53 +404,103 @@ int capture(uwg_ctx* c, cudaGraphExec_t* out, const std::function<int()>& body) 
     return UWG_OK;
 }
 
+int capture_lcg(uwg_ctx* c);
+
 int capture_cycles(uwg_ctx* c, int deg) {
     Work* w = work_of(c);
     int rc;
     if ((rc = capture(c, &w->g_v64, [&]() { return vcycle<double>(c, 0, w->cg_r, w->cg_z, deg); }))) return rc;
     if ((rc = capture(c, &w->g_v32, [&]() { return vcycle<float>(c, 0, w->cg32_r, w->cg32_z, deg); }))) return rc;
     if ((rc = capture(c, &w->g_pv, [&]() { return pvcycle(c, 0, w->pcg_r, w->pcg_z); }))) return rc;
+    if ((rc = capture_lcg(c))) return rc;
     w->g_deg = deg;
     w->g_pdeg = w->pdeg;
     return UWG_OK;
 }
 
+// L-solve CG with its scalars on the device, so that iterations need no host
+// round trip: S[4..5] / S[6..7] hold (r.z, r.r) of alternate iterations,
+// S[2] holds p.q, S[9] flags a breakdown (p.q <= 0).
+__global__ void k_lcg_step1(int64_t n, double* S, int rz_old, const float* p, const float* q, float* x, float* r) {
+    double pq = S[2];
+    bool ok = pq > 0.0 && S[9] == 0.0;
+    if (!ok) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) S[9] = 1.0;
+        return;
+    }
+    float al = (float)(S[rz_old] / pq);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        x[i] += al * p[i];
+        r[i] -= al * q[i];
+    }
+}
+__global__ void k_lcg_step2(int64_t n, const double* S, int rz_old, int rz_new, const float* z, float* p) {
+    if (S[9] != 0.0) return;
+    float be = (float)(S[rz_new] / S[rz_old]);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = z[i] + be * p[i];
+}
+
+// one CG iteration: old (r.z) in S[rz_old], new (r.z, r.r) into S[rz_new], S[rz_new + 1]
+int lcg_iteration(uwg_ctx* c, int rz_old, int rz_new) {
+    Work* w = work_of(c);
+    cudaStream_t s = c->stream;
+    int64_t n = c->n_pdof;
+    unsigned nb = (unsigned)std::min<int64_t>((n + 255) / 256, 152 * 8);
+    int rc;
+    float *r = w->pcg_r, *z = w->pcg_z, *p = w->pcg_p, *q = w->pcg_q;
+    if ((rc = papply(c, 0, p, q))) return rc;
+    const float* a1[1] = {p};
+    const float* b1[1] = {q};
+    vk_dots<float>(s, n, 1, a1, b1, w->lcg_s + 2);
+    k_lcg_step1<<<nb, 256, 0, s>>>(n, w->lcg_s, rz_old, p, q, w->pcg_x, r);
+    if ((rc = pvcycle(c, 0, r, z))) return rc;
+    const float* a2[2] = {r, r};
+    const float* b2[2] = {z, r};
+    vk_dots<float>(s, n, 2, a2, b2, w->lcg_s + rz_new);
+    k_lcg_step2<<<nb, 256, 0, s>>>(n, w->lcg_s, rz_old, rz_new, z, p);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
+int capture_lcg(uwg_ctx* c) {
+    Work* w = work_of(c);
+    return capture(c, &w->g_lcg, [&]() {
+        int rc = lcg_iteration(c, 4, 6);
+        return rc ? rc : lcg_iteration(c, 6, 4);
+    });
+}
+
 // x = L^-1 b by multigrid-preconditioned CG from zero, to rtol (FP32 vectors,
-// FP64 reductions)
+// FP64 reductions); convergence is checked every second iteration.
 int lsolve(uwg_ctx* c, const float* b, float* x, double rtol, int maxit) {
     Work* w = work_of(c);
     cudaStream_t s = c->stream;
     int64_t n = c->n_pdof;
     int rc;
-    float *r = w->pcg_r, *z = w->pcg_z, *p = w->pcg_p, *q = w->pcg_q;
-    vk_zero<float>(s, n, x);
+    if (!w->g_lcg || !w->lcg_h || w->g_pdeg != w->pdeg) return uwg_set_error(c, UWG_ERR_CUDA, "L-solve graph missing");
+    float *r = w->pcg_r, *z = w->pcg_z, *p = w->pcg_p;
+    vk_zero<float>(s, n, w->pcg_x);
     vk_copy<float>(s, n, b, r);
     if ((rc = run_pvcycle(c, r, z))) return rc;
     vk_copy<float>(s, n, z, p);
-    double d2[2];
+    UWG_CUDA(c, cudaMemsetAsync(w->lcg_s, 0, sizeof(double) * 16, s));
     const float* a2[2] = {r, r};
     const float* b2[2] = {z, r};
-    if ((rc = dots<float>(c, n, 2, a2, b2, d2))) return rc;
-    double bn = std::sqrt(d2[1]), rz = d2[0];
-    if (bn == 0.0) return UWG_OK;
-    for (int it = 1; it <= maxit; it++) {
-        if ((rc = papply(c, 0, p, q))) return rc;
-        double pq;
-        const float* a1[1] = {p};
-        const float* b1[1] = {q};
-        if ((rc = dots<float>(c, n, 1, a1, b1, &pq))) return rc;
-        w->lsolve_its++;
-        if (!(pq > 0.0)) return UWG_OK;
-        double alpha = rz / pq;
-        vk_axpy<float>(s, n, (float)alpha, p, x);
-        vk_axpy<float>(s, n, (float)-alpha, q, r);
-        if ((rc = run_pvcycle(c, r, z))) return rc;
-        if ((rc = dots<float>(c, n, 2, a2, b2, d2))) return rc;
-        if (std::sqrt(d2[1]) <= rtol * bn) return UWG_OK;
-        double beta = d2[0] / rz;
-        rz = d2[0];
-        vk_axpby<float>(s, n, 1.f, z, (float)beta, p);
+    vk_dots<float>(s, n, 2, a2, b2, w->lcg_s + 4);
+    UWG_CUDA(c, cudaMemcpyAsync(w->lcg_h, w->lcg_s, sizeof(double) * 16, cudaMemcpyDeviceToHost, s));
+    UWG_CUDA(c, cudaStreamSynchronize(s));
+    double bn = std::sqrt(w->lcg_h[5]);
+    if (bn > 0.0) {
+        for (int it = 0; it < maxit; it += 2) {
+            UWG_CUDA(c, cudaGraphLaunch(w->g_lcg, s));
+            w->lsolve_its += 2;
+            UWG_CUDA(c, cudaMemcpyAsync(w->lcg_h, w->lcg_s, sizeof(double) * 16, cudaMemcpyDeviceToHost, s));
+            UWG_CUDA(c, cudaStreamSynchronize(s));
+            if (w->lcg_h[9] != 0.0 || !(std::sqrt(w->lcg_h[5]) > rtol * bn)) break;
+        }
     }
+    vk_copy<float>(s, n, w->pcg_x, x);
     return UWG_OK;   // a preconditioner: an inexact solve is acceptable
 }
 
@@ -505,6 +562,8 @@ void uwg_solver_free(uwg_ctx* c) {
         if (w->g_v64) cudaGraphExecDestroy(w->g_v64);
         if (w->g_v32) cudaGraphExecDestroy(w->g_v32);
         if (w->g_pv) cudaGraphExecDestroy(w->g_pv);
+        if (w->g_lcg) cudaGraphExecDestroy(w->g_lcg);
+        if (w->lcg_h) cudaFreeHost(w->lcg_h);
         if (w->gstream) cudaStreamDestroy(w->gstream);
     }
     for (size_t i = 1; i < c->ws.size(); i++) cudaFree(c->ws[i]);
@@ -759,7 +818,8 @@ extern "C" int uwg_stokes_solve(uwg_ctx* c, const uwg_solve_opts* o, double* u, 
         return uwg_set_error(c, UWG_ERR_ARG, "schur_pc_smooth must be in [1, 16]");
     w->pdeg = o->schur_pc_smooth;
     if (w->pdeg != w->g_pdeg &&
-        (rc = capture(c, &w->g_pv, [&]() { return pvcycle(c, 0, w->pcg_r, w->pcg_z); })) == UWG_OK)
+        (rc = capture(c, &w->g_pv, [&]() { return pvcycle(c, 0, w->pcg_r, w->pcg_z); })) == UWG_OK &&
+        (rc = capture_lcg(c)) == UWG_OK)
         w->g_pdeg = w->pdeg;
     if (rc) return rc;
     // velocity V-cycle graphs for this smoother degree
