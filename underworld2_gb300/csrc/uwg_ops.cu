@@ -1373,9 +1373,12 @@ struct dot_ptrs { const void* a[4]; const void* b[4]; };
 template <typename T>
 __global__ void vk_dots_k(int64_t n, int k, dot_ptrs P, double* dst) {
     __shared__ double sm[4][32];
-    double acc[4] = {0, 0, 0, 0};
+    // per-thread partial sums in the vectors' own precision (a few dozen terms;
+    // FP64 arithmetic is scarce on this GPU), FP64 from the warp reduction on
+    T part[4] = {0, 0, 0, 0};
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        for (int j = 0; j < k; j++) acc[j] += (double)((const T*)P.a[j])[i] * (double)((const T*)P.b[j])[i];
+        for (int j = 0; j < k; j++) part[j] += ((const T*)P.a[j])[i] * ((const T*)P.b[j])[i];
+    double acc[4] = {(double)part[0], (double)part[1], (double)part[2], (double)part[3]};
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int j = 0; j < k; j++) {
         double v = acc[j];

@@ -161,7 +161,10 @@ __global__ void k_pgal22(uwg_lgeom gf, uwg_lgeom gc, const float* __restrict__ s
         for (int k = 0; k < 4; k++) stc[(o * 4 + k) * gc.n_el + I] = acc[o][k];
 }
 
-// y = A x on a level with nc unknowns per cell (1 or 2)
+// y = A x on a level with nc unknowns per cell (1 or 2).  Branch-free: a
+// neighbour outside the grid has a zero coefficient, so its index is only
+// clamped into the array, and all loads of a thread can be in flight at once
+// (the coarse levels are latency-bound otherwise).
 template <int DIM, int NC>
 __global__ void k_papply(uwg_lgeom g, const float* __restrict__ st, const float* __restrict__ x,
                          float* __restrict__ y) {
@@ -169,23 +172,21 @@ __global__ void k_papply(uwg_lgeom g, const float* __restrict__ st, const float*
     const int64_t n = g.n_el;
     int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (e >= n) return;
-    int ex, ey, ez;
-    cell_xyz<DIM>(g, e, ex, ey, ez);
-    const int64_t sx = 1, sy = g.res[0], sz = (int64_t)g.res[0] * g.res[1];
+    const int64_t sy = g.res[0], sz = (int64_t)g.res[0] * g.res[1];
     float acc[NC];
 #pragma unroll
     for (int a = 0; a < NC; a++) acc[a] = 0.f;
 #pragma unroll
     for (int o = 0; o < NO; o++) {
         const int ox = o % 3 - 1, oy = (o / 3) % 3 - 1, oz = DIM == 3 ? o / 9 - 1 : 0;
-        if (!in_grid<DIM>(g, ex + ox, ey + oy, ez + oz)) continue;
-        const int64_t j = e + ox * sx + oy * sy + oz * sz;
+        int64_t j = e + ox + oy * sy + oz * sz;
+        j = j < 0 ? 0 : (j >= n ? n - 1 : j);
         if constexpr (NC == 1) {
-            acc[0] += st[o * n + e] * x[j];
+            acc[0] += __ldg(&st[o * n + e]) * __ldg(&x[j]);
         } else {
-            const float x0 = x[j], x1 = x[n + j];
-            acc[0] += st[(o * 4 + 0) * n + e] * x0 + st[(o * 4 + 1) * n + e] * x1;
-            acc[NC - 1] += st[(o * 4 + 2) * n + e] * x0 + st[(o * 4 + 3) * n + e] * x1;
+            const float x0 = __ldg(&x[j]), x1 = __ldg(&x[n + j]);
+            acc[0] += __ldg(&st[(o * 4 + 0) * n + e]) * x0 + __ldg(&st[(o * 4 + 1) * n + e]) * x1;
+            acc[NC - 1] += __ldg(&st[(o * 4 + 2) * n + e]) * x0 + __ldg(&st[(o * 4 + 3) * n + e]) * x1;
         }
     }
 #pragma unroll

@@ -422,21 +422,30 @@ int capture_cycles(uwg_ctx* c, int deg) {
 // round trip: S[4..5] / S[6..7] hold (r.z, r.r) of alternate iterations,
 // S[2] holds p.q, S[9] flags a breakdown (p.q <= 0).
 __global__ void k_lcg_step1(int64_t n, double* S, int rz_old, const float* p, const float* q, float* x, float* r) {
-    double pq = S[2];
-    bool ok = pq > 0.0 && S[9] == 0.0;
-    if (!ok) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) S[9] = 1.0;
-        return;
+    __shared__ float al;
+    __shared__ int ok;
+    if (threadIdx.x == 0) {
+        double pq = S[2];
+        ok = pq > 0.0 && S[9] == 0.0;
+        al = ok ? (float)(S[rz_old] / pq) : 0.f;
+        if (!ok && blockIdx.x == 0) S[9] = 1.0;
     }
-    float al = (float)(S[rz_old] / pq);
+    __syncthreads();
+    if (!ok) return;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         x[i] += al * p[i];
         r[i] -= al * q[i];
     }
 }
 __global__ void k_lcg_step2(int64_t n, const double* S, int rz_old, int rz_new, const float* z, float* p) {
-    if (S[9] != 0.0) return;
-    float be = (float)(S[rz_new] / S[rz_old]);
+    __shared__ float be;
+    __shared__ int ok;
+    if (threadIdx.x == 0) {
+        ok = S[9] == 0.0;
+        be = ok ? (float)(S[rz_new] / S[rz_old]) : 0.f;
+    }
+    __syncthreads();
+    if (!ok) return;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         p[i] = z[i] + be * p[i];
 }
