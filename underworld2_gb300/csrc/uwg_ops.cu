@@ -367,18 +367,23 @@ __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
     unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem));
 }
+__device__ __forceinline__ void cp_async4z(void* smem, const void* gmem, bool valid) {
+    unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sa), "l"(gmem), "r"(valid ? 4 : 0));
+}
 __device__ __forceinline__ void cp_async_wait_all() {
     asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;\n" ::: "memory");
 }
 
 template <typename T, bool STAGE_W>
-__global__ void __launch_bounds__(KT_N, STAGE_W ? 3 : 1) k_applyK_q1_3d_tiled(uwg_lgeom g, const T* __restrict__ W,
+__global__ void __launch_bounds__(KT_N, STAGE_W ? 2 : 1) k_applyK_q1_3d_tiled(uwg_lgeom g, const T* __restrict__ W,
                                                             const uint8_t* __restrict__ bc,
                                                             const T* __restrict__ x, T* y) {
     constexpr int NX = KT_X + 1, NY = KT_Y + 1, NZ = KT_Z + 1, NN = NX * NY * NZ;
     __shared__ T xs[NN * 3];
     __shared__ T ys[NN * 3];
     __shared__ T ws[STAGE_W ? 27 * KT_N : 1];
+    __shared__ uint8_t bs[NN * 3];
     int ntx = (g.res[0] + KT_X - 1) / KT_X, nty = (g.res[1] + KT_Y - 1) / KT_Y;
     int tile = blockIdx.x;
     int tx0 = (tile % ntx) * KT_X, ty0 = ((tile / ntx) % nty) * KT_Y, tz0 = (tile / (ntx * nty)) * KT_Z;
@@ -393,17 +398,17 @@ __global__ void __launch_bounds__(KT_N, STAGE_W ? 3 : 1) k_applyK_q1_3d_tiled(uw
             for (int j = 0; j < 27; j++) cp_async4(&ws[j * KT_N + threadIdx.x], W + (int64_t)j * g.n_el + e);
         }
     }
-    // stage nodal values (masked) and clear the accumulator
+    // stage nodal values and Dirichlet flags, clear the accumulator (in FP32 the
+    // values arrive by cp.async, so no thread waits on a chain of loads)
     for (int k = threadIdx.x; k < NN * 3; k += blockDim.x) {
         int nl = k / 3, c = k % 3;
         int ni = nl % NX, nj = (nl / NX) % NY, nk = nl / (NX * NY);
         int gi = tx0 + ni, gj = ty0 + nj, gk = tz0 + nk;
-        T v = (T)0;
-        if (gi < g.nx[0] && gj < g.nx[1] && gk < g.nx[2]) {
-            int64_t dof = (gi + gnx * (gj + gny * (int64_t)gk)) * 3 + c;
-            v = bc[dof] ? (T)0 : x[dof];
-        }
-        xs[k] = v;
+        const bool in = gi < g.nx[0] && gj < g.nx[1] && gk < g.nx[2];
+        const int64_t dof = in ? (gi + gnx * (gj + gny * (int64_t)gk)) * 3 + c : 0;
+        if constexpr (STAGE_W) cp_async4z(&xs[k], x + dof, in);
+        else xs[k] = in ? x[dof] : (T)0;
+        bs[k] = in ? bc[dof] : (uint8_t)1;
         ys[k] = (T)0;
     }
     if constexpr (STAGE_W) cp_async_wait_all();
@@ -417,7 +422,7 @@ __global__ void __launch_bounds__(KT_N, STAGE_W ? 3 : 1) k_applyK_q1_3d_tiled(uw
         for (int n = 0; n < 8; n++) {
             int sl = (li + (n & 1)) + NX * ((lj + ((n >> 1) & 1)) + NY * (lk + ((n >> 2) & 1)));
 #pragma unroll
-            for (int c = 0; c < 3; c++) u[n][c] = xs[sl * 3 + c];
+            for (int c = 0; c < 3; c++) u[n][c] = bs[sl * 3 + c] ? (T)0 : xs[sl * 3 + c];
         }
         if constexpr (STAGE_W) q1_3d_element<T>(ws + threadIdx.x, KT_N, hx, hy, hz, u, out);
         else q1_3d_element<T>(W + e, g.n_el, hx, hy, hz, u, out);
@@ -435,7 +440,7 @@ __global__ void __launch_bounds__(KT_N, STAGE_W ? 3 : 1) k_applyK_q1_3d_tiled(uw
         int gi = tx0 + ni, gj = ty0 + nj, gk = tz0 + nk;
         if (gi >= g.nx[0] || gj >= g.nx[1] || gk >= g.nx[2]) continue;
         int64_t dof = (gi + gnx * (gj + gny * (int64_t)gk)) * 3 + c;
-        if (bc[dof]) continue;
+        if (bs[k]) continue;
         bool interior = ni > 0 && ni < KT_X && nj > 0 && nj < KT_Y && nk > 0 && nk < KT_Z;
         if (interior) y[dof] = ys[k];
         else atomicAdd(&y[dof], ys[k]);

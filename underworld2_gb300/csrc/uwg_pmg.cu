@@ -166,9 +166,10 @@ __global__ void k_pgal22(uwg_lgeom gf, uwg_lgeom gc, const float* __restrict__ s
 // clamped into the array, and all loads of a thread can be in flight at once
 // (the coarse levels are latency-bound otherwise).
 template <int DIM, int NC>
-__global__ void k_papply(uwg_lgeom g, const float* __restrict__ st, const float* __restrict__ x,
-                         float* __restrict__ y) {
+__global__ void __launch_bounds__(256) k_papply(uwg_lgeom g, const float* __restrict__ st,
+                                                const float* __restrict__ x, float* __restrict__ y) {
     constexpr int NO = DIM == 3 ? 27 : 9;
+    constexpr int GRP = 9;   // offsets whose loads are issued together
     const int64_t n = g.n_el;
     int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (e >= n) return;
@@ -177,17 +178,25 @@ __global__ void k_papply(uwg_lgeom g, const float* __restrict__ st, const float*
 #pragma unroll
     for (int a = 0; a < NC; a++) acc[a] = 0.f;
 #pragma unroll
-    for (int o = 0; o < NO; o++) {
-        const int ox = o % 3 - 1, oy = (o / 3) % 3 - 1, oz = DIM == 3 ? o / 9 - 1 : 0;
-        int64_t j = e + ox + oy * sy + oz * sz;
-        j = j < 0 ? 0 : (j >= n ? n - 1 : j);
-        if constexpr (NC == 1) {
-            acc[0] += __ldg(&st[o * n + e]) * __ldg(&x[j]);
-        } else {
-            const float x0 = __ldg(&x[j]), x1 = __ldg(&x[n + j]);
-            acc[0] += __ldg(&st[(o * 4 + 0) * n + e]) * x0 + __ldg(&st[(o * 4 + 1) * n + e]) * x1;
-            acc[NC - 1] += __ldg(&st[(o * 4 + 2) * n + e]) * x0 + __ldg(&st[(o * 4 + 3) * n + e]) * x1;
+    for (int o0 = 0; o0 < NO; o0 += GRP) {
+        float sv[GRP][NC * NC], xv[GRP][NC];
+#pragma unroll
+        for (int k = 0; k < GRP; k++) {
+            const int o = o0 + k;
+            const int ox = o % 3 - 1, oy = (o / 3) % 3 - 1, oz = DIM == 3 ? o / 9 - 1 : 0;
+            int64_t j = e + ox + oy * sy + oz * sz;
+            j = j < 0 ? 0 : (j >= n ? n - 1 : j);
+#pragma unroll
+            for (int q = 0; q < NC * NC; q++) sv[k][q] = __ldg(&st[(o * NC * NC + q) * n + e]);
+#pragma unroll
+            for (int b = 0; b < NC; b++) xv[k][b] = __ldg(&x[b * n + j]);
         }
+#pragma unroll
+        for (int k = 0; k < GRP; k++)
+#pragma unroll
+            for (int a = 0; a < NC; a++)
+#pragma unroll
+                for (int b = 0; b < NC; b++) acc[a] += sv[k][a * NC + b] * xv[k][b];
     }
 #pragma unroll
     for (int a = 0; a < NC; a++) y[a * n + e] = acc[a];
@@ -294,6 +303,11 @@ __device__ __forceinline__ void pmg_cp_async4(void* smem, const void* gmem) {
     unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem));
 }
+// as pmg_cp_async4, writing zero instead when `valid` is false (src-size 0)
+__device__ __forceinline__ void pmg_cp_async4z(void* smem, const void* gmem, bool valid) {
+    unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sa), "l"(gmem), "r"(valid ? 4 : 0));
+}
 #define PT_X 16
 #define PT_Y 8
 #define PT_Z 8
@@ -321,7 +335,8 @@ __global__ void __launch_bounds__(256) k_papply0_mf(uwg_lgeom g, const float* __
     for (int k = threadIdx.x; k < NH; k += blockDim.x) {
         const int i = k % HX, j = (k / HX) % HY, l = k / (HX * HY);
         const int cx = tx0 - 1 + i, cy = ty0 - 1 + j, cz = tz0 - 1 + l;
-        ps[k] = in_grid<3>(g, cx, cy, cz) ? x[cx + sy * cy + sz * cz] : 0.f;
+        const bool in = in_grid<3>(g, cx, cy, cz);
+        pmg_cp_async4z(&ps[k], x + (in ? cx + sy * cy + sz * cz : 0), in);
     }
     if (threadIdx.x < 3 * HX) {
         const int d = threadIdx.x / HX, i = threadIdx.x % HX;
