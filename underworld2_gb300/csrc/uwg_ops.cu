@@ -376,7 +376,7 @@ __device__ __forceinline__ void cp_async_wait_all() {
 }
 
 template <typename T, bool STAGE_W>
-__global__ void __launch_bounds__(KT_N, STAGE_W ? 2 : 1) k_applyK_q1_3d_tiled(uwg_lgeom g, const T* __restrict__ W,
+__global__ void __launch_bounds__(KT_N, STAGE_W ? 3 : 1) k_applyK_q1_3d_tiled(uwg_lgeom g, const T* __restrict__ W,
                                                             const uint8_t* __restrict__ bc,
                                                             const T* __restrict__ x, T* y) {
     constexpr int NX = KT_X + 1, NY = KT_Y + 1, NZ = KT_Z + 1, NN = NX * NY * NZ;
