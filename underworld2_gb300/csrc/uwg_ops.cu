@@ -328,7 +328,9 @@ __global__ void __launch_bounds__(128) k_applyK_q1_3d(uwg_lgeom g, const T* __re
     int64_t nodes[8];
     double hd[3];
     q1_elem(g, e, nodes, hd);
-    const T hx = (T)(2.0 / hd[0]), hy = (T)(2.0 / hd[1]), hz = (T)(2.0 / hd[2]);
+    // 2/h in the operator's precision (an FP64 division costs dozens of FP64
+    // instructions, and FP64 throughput is scarce on this GPU)
+    const T hx = (T)2 / (T)hd[0], hy = (T)2 / (T)hd[1], hz = (T)2 / (T)hd[2];
     T u[8][3];
     bool fix[8][3];
 #pragma unroll
@@ -414,9 +416,9 @@ __global__ void __launch_bounds__(KT_N, STAGE_W ? 3 : 1) k_applyK_q1_3d_tiled(uw
     if constexpr (STAGE_W) cp_async_wait_all();
     __syncthreads();
     if (own) {
-        const T hx = (T)(2.0 / (g.ax[0][ex + 1] - g.ax[0][ex]));
-        const T hy = (T)(2.0 / (g.ax[1][ey + 1] - g.ax[1][ey]));
-        const T hz = (T)(2.0 / (g.ax[2][ez + 1] - g.ax[2][ez]));
+        const T hx = (T)2 / (T)(g.ax[0][ex + 1] - g.ax[0][ex]);   // 2/h in the operator's precision
+        const T hy = (T)2 / (T)(g.ax[1][ey + 1] - g.ax[1][ey]);
+        const T hz = (T)2 / (T)(g.ax[2][ez + 1] - g.ax[2][ez]);
         T u[8][3], out[8][3];
 #pragma unroll
         for (int n = 0; n < 8; n++) {
@@ -456,7 +458,7 @@ __global__ void __launch_bounds__(128) k_applyK_q1_2d(uwg_lgeom g, const T* __re
     int64_t nodes[8];
     double hd[3];
     q1_elem(g, e, nodes, hd);
-    const T hx = (T)(2.0 / hd[0]), hy = (T)(2.0 / hd[1]);
+    const T hx = (T)2 / (T)hd[0], hy = (T)2 / (T)hd[1];   // 2/h in the operator's precision
     T u[4][2];
     bool fix[4][2];
 #pragma unroll
