@@ -24,14 +24,14 @@ def assemble(mesh, pts, eta_p, body_p, bc_mask, bc_val):
     """Full-dof K, G, f, h plus reduced-system index maps.
 
     pts: list per element of (particle ids, xi, w).  bc_mask/bc_val: [n_nodes*dim]."""
-    dim, nen = mesh.dim, mesh.nen
+    dim, nen, npn = mesh.dim, mesh.nen, mesh.npn
     nv = mesh.n_nodes * dim
     ne = mesh.n_el
     Kr, Kc, Kv = [], [], []
     Gr, Gc, Gv = [], [], []
     f = np.zeros(nv)
     gxi, gw = mesh.gauss_points()
-    Shat = np.zeros(ne)
+    Shat = np.zeros(ne) if npn == 1 else np.zeros((ne, npn, npn))
     for e in range(ne):
         nodes = mesh.element_nodes(e)
         dofs = (nodes[:, None] * dim + np.arange(dim)[None, :]).ravel()
@@ -40,12 +40,15 @@ def assemble(mesh, pts, eta_p, body_p, bc_mask, bc_val):
         fe = mesh.element_f(e, xi, w, body_p[ps])
         Ge = mesh.element_G(e, gxi, gw)
         Se = mesh.element_S(Ke, Ge)
-        Shat[e] = Se[0, 0]
+        if npn == 1:
+            Shat[e] = Se[0, 0]
+        else:
+            Shat[e] = Se
         Kr.append(np.repeat(dofs, len(dofs))); Kc.append(np.tile(dofs, len(dofs))); Kv.append(Ke.ravel())
-        Gr.append(dofs); Gc.append(np.full(len(dofs), e)); Gv.append(Ge[:, 0])
+        Gr.append(np.repeat(dofs, npn)); Gc.append(np.tile(e * npn + np.arange(npn), len(dofs))); Gv.append(Ge.ravel())
         f[dofs] += fe
     K = sp.csr_matrix((np.concatenate(Kv), (np.concatenate(Kr), np.concatenate(Kc))), shape=(nv, nv))
-    G = sp.csr_matrix((np.concatenate(Gv), (np.concatenate(Gr), np.concatenate(Gc))), shape=(nv, ne))
+    G = sp.csr_matrix((np.concatenate(Gv), (np.concatenate(Gr), np.concatenate(Gc))), shape=(nv, ne * npn))
     free = np.where(bc_mask == 0)[0]
     bcd = np.where(bc_mask != 0)[0]
     g = bc_val[bcd]

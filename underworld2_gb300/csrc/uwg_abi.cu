@@ -57,7 +57,9 @@ extern "C" int uwg_ctx_create(const uwg_mesh_desc* d, uwg_ctx** out) {
     if (!d || !out) return UWG_ERR_ARG;
     *out = nullptr;
     if (d->dim != 2 && d->dim != 3) return UWG_ERR_ARG;
-    if (d->order != 1 || d->porder != 0) return UWG_ERR_ARG;   // Q1/dQ0 operators
+    // Q1/dQ0 in 2D and 3D, Q2/dPc1 in 2D
+    bool q1 = d->order == 1 && d->porder == 0, q2 = d->dim == 2 && d->order == 2 && d->porder == 1;
+    if (!q1 && !q2) return UWG_ERR_ARG;
     for (int i = 0; i < d->dim; i++)
         if (d->res[i] < 1 || !(d->maxc[i] > d->minc[i])) return UWG_ERR_ARG;
     int dev_count = 0;
@@ -79,10 +81,10 @@ extern "C" int uwg_ctx_create(const uwg_mesh_desc* d, uwg_ctx** out) {
     for (int i = 0; i < c->dim; i++) nn *= (int64_t)c->res[i] * c->order + 1;
     c->n_nodes = nn;
     c->n_vdof = nn * c->dim;
-    c->nen = c->dim == 3 ? 8 : 4;
-    c->npn = 1;
+    c->nen = c->order == 2 ? 9 : (c->dim == 3 ? 8 : 4);
+    c->npn = c->porder == 1 ? 3 : 1;
     c->n_pdof = c->n_el * c->npn;
-    c->nq = c->dim == 3 ? 27 : 9;
+    c->nq = c->order == 2 ? 25 : (c->dim == 3 ? 27 : 9);
     c->dvc_res = 15;
     c->assembled = false;
     c->red_host = nullptr;
@@ -103,7 +105,9 @@ extern "C" int uwg_ctx_create(const uwg_mesh_desc* d, uwg_ctx** out) {
         if (ok) cudaMemcpy(c->ax[i], hax[i].data(), sizeof(double) * hax[i].size(), cudaMemcpyHostToDevice);
     }
     c->min_sep = minsep;
-    // multigrid levels: halve while every axis is even (reference rule, L/.../_bsscr.py:73-91)
+    // multigrid levels: halve while every axis is even (reference rule, L/.../_bsscr.py:73-91);
+    // a Q2 context adds the Q1 mesh on the same elements as level 1
+    const int q2lev = c->order == 2 ? 1 : 0;
     int nlev = 1;
     {
         int r[3] = {c->res[0], c->res[1], c->res[2]};
@@ -115,14 +119,18 @@ extern "C" int uwg_ctx_create(const uwg_mesh_desc* d, uwg_ctx** out) {
             nlev++;
         }
     }
+    nlev = std::min(nlev + q2lev, UWG_MAXLEV);
     c->nlev = nlev;
     for (int l = 0; l < nlev && ok; l++) {
         uwg_level& L = c->lev[l];
+        L.order = (q2lev && l == 0) ? 2 : 1;
+        L.nq = L.order == 2 ? 25 : (c->dim == 3 ? 27 : 9);
+        const int shift = q2lev ? std::max(l - 1, 0) : l;
         int64_t ne = 1, nnod = 1;
         for (int i = 0; i < 3; i++) {
-            L.res[i] = i < c->dim ? (c->res[i] >> l) : 1;
+            L.res[i] = i < c->dim ? (c->res[i] >> shift) : 1;
             ne *= L.res[i];
-            if (i < c->dim) nnod *= L.res[i] + 1;
+            if (i < c->dim) nnod *= (int64_t)L.res[i] * L.order + 1;
         }
         L.n_el = ne;
         L.n_nodes = nnod;
@@ -135,8 +143,8 @@ extern "C" int uwg_ctx_create(const uwg_mesh_desc* d, uwg_ctx** out) {
             L.ax[i] = (double*)dmalloc(sizeof(double) * v.size(), &ok);
             if (ok) cudaMemcpy(L.ax[i], v.data(), sizeof(double) * v.size(), cudaMemcpyHostToDevice);
         }
-        L.W64 = (double*)dmalloc(sizeof(double) * c->nq * ne, &ok);
-        L.W32 = (float*)dmalloc(sizeof(float) * c->nq * ne, &ok);
+        L.W64 = (double*)dmalloc(sizeof(double) * L.nq * ne, &ok);
+        L.W32 = (float*)dmalloc(sizeof(float) * L.nq * ne, &ok);
         L.bc = (uint8_t*)dmalloc(L.n_dof, &ok);
         L.diag64 = (double*)dmalloc(sizeof(double) * L.n_dof, &ok);
         L.diag32 = (float*)dmalloc(sizeof(float) * L.n_dof, &ok);
@@ -157,7 +165,7 @@ extern "C" int uwg_ctx_create(const uwg_mesh_desc* d, uwg_ctx** out) {
     c->f = (double*)dmalloc(sizeof(double) * c->n_vdof, &ok);
     c->bcval = (double*)dmalloc(sizeof(double) * c->n_vdof, &ok);
     c->h = (double*)dmalloc(sizeof(double) * c->n_pdof, &ok);
-    c->Shat = (double*)dmalloc(sizeof(double) * c->n_pdof, &ok);
+    c->Shat = (double*)dmalloc(sizeof(double) * c->n_el * c->npn * c->npn, &ok);
     c->Mp = (double*)dmalloc(sizeof(double) * c->n_pdof, &ok);
     c->red = dmalloc(4096 * sizeof(double), &ok);
     if (ok && cudaMallocHost((void**)&c->red_host, 4096 * sizeof(double)) != cudaSuccess) ok = false;
@@ -167,6 +175,7 @@ extern "C" int uwg_ctx_create(const uwg_mesh_desc* d, uwg_ctx** out) {
         cudaMemset(c->Mp, 0, sizeof(double) * c->n_pdof);
         cudaMemset(c->f, 0, sizeof(double) * c->n_vdof);
     }
+    if (ok && c->order == 2 && uwg_q2_init(c) != UWG_OK) ok = false;
     if (!ok || cudaDeviceSynchronize() != cudaSuccess) {
         uwg_ctx_destroy(c);
         return UWG_ERR_CUDA;

@@ -15,6 +15,8 @@
 
 // One multigrid level of the velocity operator.  Level 0 is the finest.
 struct uwg_level {
+    int order;            // velocity element order of the level (2 only on level 0 of Q2 contexts)
+    int nq;               // equivalent-quadrature weights per element
     int res[3];
     int64_t n_el, n_nodes, n_dof;
     double* ax[3];        // node coordinates per axis (device)

@@ -32,9 +32,10 @@ uwg_lgeom uwg_level_geom(const uwg_ctx* c, int l) {
     uwg_lgeom g;
     const uwg_level& L = c->lev[l];
     g.dim = c->dim;
+    g.order = L.order > 0 ? L.order : 1;
     for (int d = 0; d < 3; d++) {
         g.res[d] = L.res[d];
-        g.nx[d] = d < c->dim ? L.res[d] + 1 : 1;
+        g.nx[d] = d < c->dim ? L.res[d] * g.order + 1 : 1;
         g.ax[d] = L.ax[d];
     }
     g.n_el = L.n_el;
@@ -510,6 +511,7 @@ int uwg_ops_applyK(uwg_ctx* c, int l, const T* x, T* y) {
     const T* W;
     if constexpr (sizeof(T) == 8) W = (const T*)L.W64; else W = (const T*)L.W32;
     k_bc_copy<T><<<nblk(L.n_dof), 256, 0, c->stream>>>(L.n_dof, L.bc, x, y);
+    if (L.order == 2) return uwg_q2_applyK<T>(c, x, y, true);
     if (c->dim == 3) {
         unsigned tiles = (unsigned)(((L.res[0] + KT_X - 1) / KT_X) * ((L.res[1] + KT_Y - 1) / KT_Y) *
                                     ((L.res[2] + KT_Z - 1) / KT_Z));
@@ -527,6 +529,7 @@ int uwg_ops_applyK_lift(uwg_ctx* c, const double* x, double* y) {
     const uwg_level& L = c->lev[0];
     uwg_lgeom g = uwg_level_geom(c, 0);
     vk_zero<double>(c->stream, L.n_dof, y);
+    if (L.order == 2) return uwg_q2_applyK<double>(c, x, y, false);
     if (c->dim == 3) k_applyK_q1_3d<double><<<nblk(L.n_el, 128), 128, 0, c->stream>>>(g, L.W64, L.bc, false, x, y);
     else k_applyK_q1_2d<double><<<nblk(L.n_el, 128), 128, 0, c->stream>>>(g, L.W64, L.bc, false, x, y);
     UWG_CUDA(c, cudaGetLastError());
@@ -880,6 +883,7 @@ int uwg_ops_cell_prolong_add(uwg_ctx* c, int lc, const double* xc, double* xf) {
 }
 
 int uwg_ops_applyG(uwg_ctx* c, const double* p, double* y) {
+    if (c->porder == 1) return uwg_q2_applyG(c, p, y);
     uwg_lgeom g = uwg_level_geom(c, 0);
     if (c->dim == 3) k_gradG_nodes<3><<<nblk(c->n_nodes), 256, 0, c->stream>>>(g, c->bc, p, nullptr, y);
     else k_gradG_nodes<2><<<nblk(c->n_nodes), 256, 0, c->stream>>>(g, c->bc, p, nullptr, y);
@@ -890,6 +894,7 @@ int uwg_ops_applyG(uwg_ctx* c, const double* p, double* y) {
 int uwg_ops_applyGt(uwg_ctx* c, const double* u, double* q) { return uwg_ops_applyGt_mode(c, u, q, 0); }
 
 int uwg_ops_applyGt_mode(uwg_ctx* c, const double* u, double* q, int only_bc) {
+    if (c->porder == 1) return uwg_q2_applyGt(c, u, q, only_bc);
     uwg_lgeom g = uwg_level_geom(c, 0);
     if (c->dim == 3) k_applyGt<3><<<nblk(c->n_el), 256, 0, c->stream>>>(g, c->bc, only_bc, u, q);
     else k_applyGt<2><<<nblk(c->n_el), 256, 0, c->stream>>>(g, c->bc, only_bc, u, q);
@@ -903,6 +908,7 @@ __global__ void k_schur_pc(int64_t n, const double* shat, const double* r, doubl
 }
 
 int uwg_ops_schur_pc(uwg_ctx* c, const double* r, double* z) {
+    if (c->porder == 1) return uwg_q2_schur_pc(c, r, z);
     k_schur_pc<<<nblk(c->n_pdof), 256, 0, c->stream>>>(c->n_pdof, c->Shat, r, z);
     UWG_CUDA(c, cudaGetLastError());
     return UWG_OK;
@@ -1084,6 +1090,14 @@ int uwg_ops_level_setup(uwg_ctx* c, int l) {
     uwg_level& L = c->lev[l];
     uwg_lgeom g = uwg_level_geom(c, l);
     vk_zero<double>(c->stream, L.n_dof, L.diag64);
+    if (L.order == 2) {
+        int rc = uwg_q2_diag(c, l == 0 ? c->Shat : nullptr);
+        if (rc) return rc;
+        k_diag_bc<<<nblk(L.n_dof), 256, 0, c->stream>>>(L.n_dof, L.bc, L.diag64, L.diag32, nullptr);
+        k_to_f32<<<nblk(L.n_el * L.nq), 256, 0, c->stream>>>(L.n_el * L.nq, L.W64, L.W32);
+        UWG_CUDA(c, cudaGetLastError());
+        return UWG_OK;
+    }
     if (c->dim == 3) k_diag_q1<3><<<nblk(L.n_el), 256, 0, c->stream>>>(g, L.W64, L.bc, L.diag64, l == 0 ? c->Shat : nullptr, c->Mp);
     else k_diag_q1<2><<<nblk(L.n_el), 256, 0, c->stream>>>(g, L.W64, L.bc, L.diag64, l == 0 ? c->Shat : nullptr, c->Mp);
     UWG_CUDA(c, cudaGetLastError());
@@ -1144,6 +1158,10 @@ __global__ void k_element_matrices(uwg_lgeom g, int64_t e, const double* W, cons
 
 int uwg_ops_element_matrices(uwg_ctx* c, int64_t el, double* Ke, double* fe, double* Ge, double* Se) {
     int nd = c->dim * c->nen;
+    if (c->order == 2) {
+        if (fe) for (int i = 0; i < nd; i++) fe[i] = 0.0;   // element force is scattered at assembly
+        return uwg_q2_element_matrices(c, el, Ke, Ge, Se);
+    }
     double* buf = nullptr;
     UWG_CUDA(c, cudaMallocAsync((void**)&buf, sizeof(double) * (nd * nd + nd + 1), c->stream));
     uwg_lgeom g = uwg_level_geom(c, 0);
@@ -1277,6 +1295,10 @@ template int uwg_ops_dense_solve<float>(uwg_ctx*, int, const float*, float*);
 
 int uwg_ops_assemble(uwg_ctx* c, const int32_t* off, const int32_t* list, const double* ip_xi,
                      const double* ip_w, const double* eta_p, const double* body_p, const double* lambda_p) {
+    if (c->order == 2) {
+        if (lambda_p) return uwg_set_error(c, UWG_ERR_ARG, "compressibility is not available for Q2/dPc1");
+        return uwg_q2_assemble(c, off, list, ip_xi, ip_w, eta_p, body_p);
+    }
     uwg_lgeom g = uwg_level_geom(c, 0);
     vk_zero<double>(c->stream, c->n_vdof, c->f);
     if (c->dim == 3)

@@ -100,7 +100,7 @@ int work_init(uwg_ctx* c, int restart) {
         w->ftil = dalloc<double>(c, nv); w->bvec = dalloc<double>(c, nv);
         w->p_tmp = dalloc<double>(c, np); w->p_tmp2 = dalloc<double>(c, np); w->hhat = dalloc<double>(c, np);
         w->coef = dalloc<double>(c, 512);
-        for (int l = 0; l < c->nlev; l++) {
+        for (int l = 0; l < c->nlev && c->porder == 0; l++) {   // the BFBt pressure multigrid is dQ0 only
             int64_t ne = uwg_pmg_ncomp(l) * c->lev[l].n_el;
             w->pv[l] = {dalloc<float>(c, ne), dalloc<float>(c, ne), dalloc<float>(c, ne), dalloc<float>(c, ne), dalloc<float>(c, ne)};
             w->pst[l] = dalloc<float>(c, uwg_pmg_stencil_size(c, l));
@@ -411,8 +411,10 @@ int capture_cycles(uwg_ctx* c, int deg) {
     int rc;
     if ((rc = capture(c, &w->g_v64, [&]() { return vcycle<double>(c, 0, w->cg_r, w->cg_z, deg); }))) return rc;
     if ((rc = capture(c, &w->g_v32, [&]() { return vcycle<float>(c, 0, w->cg32_r, w->cg32_z, deg); }))) return rc;
-    if ((rc = capture(c, &w->g_pv, [&]() { return pvcycle(c, 0, w->pcg_r, w->pcg_z); }))) return rc;
-    if ((rc = capture_lcg(c))) return rc;
+    if (c->porder == 0) {
+        if ((rc = capture(c, &w->g_pv, [&]() { return pvcycle(c, 0, w->pcg_r, w->pcg_z); }))) return rc;
+        if ((rc = capture_lcg(c))) return rc;
+    }
     w->g_deg = deg;
     w->g_pdeg = w->pdeg;
     return UWG_OK;
@@ -616,12 +618,13 @@ int uwg_solver_setup(uwg_ctx* c) {
     int rc = work_init(c, 50);
     if (rc) return rc;
     for (int l = 0; l < c->nlev; l++) {
-        if (l > 0 && (rc = uwg_ops_coarsen(c, l - 1))) return rc;
+        // (level 1 of a Q2 context is assembled from the particles, not coarsened)
+        if (l > 0 && c->lev[l - 1].order == 1 && (rc = uwg_ops_coarsen(c, l - 1))) return rc;
         if ((rc = uwg_ops_level_setup(c, l))) return rc;
         if (l < c->nlev - 1 && (rc = uwg_solver_estimate(c, l))) return rc;
     }
     if ((rc = uwg_ops_dense_coarse(c, c->nlev - 1))) return rc;
-    if ((rc = bfbt_setup(c))) return rc;
+    if (c->porder == 0 && (rc = bfbt_setup(c))) return rc;
     return capture_cycles(c, work_of(c)->g_deg > 0 ? work_of(c)->g_deg : 3);
 }
 
@@ -825,8 +828,10 @@ extern "C" int uwg_stokes_solve(uwg_ctx* c, const uwg_solve_opts* o, double* u, 
     cudaStream_t s = c->stream;
     if (o->schur_pc_smooth < 1 || o->schur_pc_smooth > 16)
         return uwg_set_error(c, UWG_ERR_ARG, "schur_pc_smooth must be in [1, 16]");
+    if (o->schur_pc == 1 && c->porder != 0)
+        return uwg_set_error(c, UWG_ERR_ARG, "scaled BFBt is implemented for Q1/dQ0; use schur_pc = 0 with Q2/dPc1");
     w->pdeg = o->schur_pc_smooth;
-    if (w->pdeg != w->g_pdeg &&
+    if (c->porder == 0 && w->pdeg != w->g_pdeg &&
         (rc = capture(c, &w->g_pv, [&]() { return pvcycle(c, 0, w->pcg_r, w->pcg_z); })) == UWG_OK &&
         (rc = capture_lcg(c)) == UWG_OK)
         w->g_pdeg = w->pdeg;
