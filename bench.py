@@ -8,7 +8,12 @@ length 0.1, spectral synthesis on a 256^3 grid, Gaussian covariance),
 trilinearly sampled at the particles and scaled to [0, 1]; viscosity
 exp(-11.5 T) (contrast ~1e5), body force (0, 0, Ra T) with Ra = 1e6.
 ``sinker2d`` is the 2D 64^2 sinker (circle r=0.1 at (0.5,0.6), viscosity 100,
-density 1, gravity (0,-1)) that the reference runs on a CPU.
+density 1, gravity (0,-1)) that the reference runs on a CPU.  ``rt2d_q2`` is
+the 2D 256^2 Q2/dPc1 Rayleigh-Taylor case: a dense layer (density 1,
+viscosity 1) over a light one (density 0, viscosity 0.01) with the interface
+at y = 0.2 + 0.02 cos(pi x), per-particle viscosity times a seeded
+log-uniform factor in [1e-1, 1e1], 40 particles per element; its Schur
+preconditioner is the reference's Uzawa term.
 
 One step = the hot path over the swarm: coincident mapping + DVC weights,
 PIC assembly, BSSCR solve to 1e-8 (FP32 inner solves in FP64 refinement; the
@@ -37,6 +42,8 @@ CONFIGS = {
     "grf3d": dict(dim=3, res=(128, 128, 128), ppc=20, kind="grf"),
     "grf3d_small": dict(dim=3, res=(32, 32, 32), ppc=20, kind="grf"),
     "sinker2d": dict(dim=2, res=(64, 64), ppc=20, kind="sinker"),
+    # 2D Q2/dPc1 Rayleigh-Taylor layering, 40 particles per element
+    "rt2d_q2": dict(dim=2, res=(256, 256), ppc=40, kind="rt", order=2, porder=1),
 }
 
 
@@ -84,6 +91,14 @@ def material(cfg, x):
         body = torch.zeros_like(x)
         body[:, 2] = 1e6 * T
         return eta.contiguous(), body.contiguous()
+    if cfg["kind"] == "rt":
+        g = torch.Generator(device=x.device).manual_seed(4321)
+        dense = x[:, 1] > 0.2 + 0.02 * torch.cos(torch.pi * x[:, 0])
+        fac = 10.0 ** (2.0 * torch.rand(x.shape[0], generator=g, device=x.device, dtype=torch.float64) - 1.0)
+        eta = torch.where(dense, 1.0, 0.01).double() * fac
+        body = torch.zeros_like(x)
+        body[:, 1] = torch.where(dense, -1.0, 0.0)
+        return eta.contiguous(), body.contiguous()
     inside = ((x - torch.tensor([0.5, 0.6], device=x.device, dtype=x.dtype)) ** 2).sum(1) < 0.01
     eta = torch.where(inside, 100.0, 1.0).double()
     body = torch.zeros_like(x)
@@ -95,7 +110,7 @@ def freeslip_mask(ctx):
     import numpy as np
     import torch
     dim = ctx.dim
-    n = [r + 1 for r in ctx.res]
+    n = [r * ctx.order + 1 for r in ctx.res]
     idx = np.arange(int(np.prod(n)))
     ijk = [idx % n[0], (idx // n[0]) % n[1]] + ([idx // (n[0] * n[1])] if dim == 3 else [])
     m = np.zeros((len(idx), dim), np.uint8)
@@ -151,7 +166,7 @@ def run_gpu(args):
 
     cfg = CONFIGS[args.config]
     dim = cfg["dim"]
-    ctx = Context(dim, cfg["res"], (0.0,) * dim, (1.0,) * dim)
+    ctx = Context(dim, cfg["res"], (0.0,) * dim, (1.0,) * dim, order=cfg.get("order", 1), porder=cfg.get("porder", 0))
     ctx.set_bcs(freeslip_mask(ctx))
     x0, owner0, off0, lst0, _ = ctx.layout_random(cfg["ppc"], rng_seed(13))
     eta0, body0 = material(cfg, x0)
@@ -159,7 +174,7 @@ def run_gpu(args):
     u = ctx.zeros(ctx.n_vdof)
     p = ctx.zeros(ctx.n_pdof)
     opts = dict(rtol=1e-8, inner_rtol=args.inner_rtol, outer_rtol=args.outer_rtol, smooth_steps=2, restart=120,
-                schur_pc=args.schur_pc, schur_pc_rtol=args.bfbt_rtol, max_outer=args.max_outer)
+                schur_pc=args.schur_pc if cfg.get("porder", 0) == 0 else 0, schur_pc_rtol=args.bfbt_rtol, max_outer=args.max_outer)
     ev = lambda: torch.cuda.Event(enable_timing=True)
 
     def solve_step(x, off, lst, eta, body, mixed, times):
@@ -267,14 +282,14 @@ def run_gpu(args):
         "vs_baseline": None,
         "dtype": "f64" if not mixed else "f32+f64",
         "data": "synthetic",
-        "config": {"workload": workload_name(args.config), "mesh": "x".join(map(str, cfg["res"])) + " Q1/dQ0",
+        "config": {"workload": workload_name(args.config), "mesh": "x".join(map(str, cfg["res"])) + (" Q2/dPc1" if cfg.get("order", 1) == 2 else " Q1/dQ0"),
                    "particles": npart, "particles_per_cell": cfg["ppc"], "solve_mode": args.mode,
                    "inputs_vs_L2": "particle arrays (%.1f GB) exceed the 129 MB L2" % (npart * 8 * (2 * dim + 1) / 1e9)},
         "particles_per_s": npart / adv_s,
         "phases_s": {k: float(np.mean(v)) for k, v in times.items()},
         "solver": {"pressure_its": stats[-1]["pressure_its"], "velocity_total_its": stats[-1]["velocity_total_its"],
                    "schur_pc_its": stats[-1]["schur_pc_its"], "refinement_steps": stats[-1]["refinement_steps"],
-                   "residual": stats[-1]["residual"], "schur_pc": "scaled BFBt" if args.schur_pc else "Uzawa S^",
+                   "residual": stats[-1]["residual"], "schur_pc": "scaled BFBt" if (args.schur_pc and cfg.get("porder", 0) == 0) else "Uzawa S^",
                    "presolve_s": stats[-1]["presolve_time"], "pressure_s": stats[-1]["pressure_time"],
                    "backsolve_s": stats[-1]["backsolve_time"], "schur_pc_s": stats[-1]["schur_pc_time"],
                    "schur_op_s": stats[-1]["schur_op_time"]},
@@ -297,13 +312,15 @@ def run_gpu(args):
 def workload_name(key):
     return {"grf3d": "3D 128^3 Q1/dQ0 GRF viscosity exp(-11.5T), Ra=1e6, 20 ppc, free-slip (config 3)",
             "grf3d_small": "3D 32^3 Q1/dQ0 GRF viscosity, 20 ppc, free-slip",
-            "sinker2d": "2D 64^2 Q1/dQ0 sinker, 20 ppc, free-slip (config 1)"}[key]
+            "sinker2d": "2D 64^2 Q1/dQ0 sinker, 20 ppc, free-slip (config 1)",
+            "rt2d_q2": "2D 256^2 Q2/dPc1 Rayleigh-Taylor, 40 ppc, viscosity x 10^U(-1,1), free-slip (config 2)"}[key]
 
 
 def time_kernel_apply(ctx, reps=20):
     """CUDA-event time of the FP32 matrix-free K apply on the finest level.
-    Algorithmic bytes per apply: 4*(2*N_v) + 4*27*N_el (x read, y written,
-    equivalent-quadrature weights read)."""
+    Algorithmic bytes per apply: 4*(2*N_v) + 4*M*N_el (x read, y written,
+    M equivalent-quadrature weights read: 27 for 3D Q1, 9 for 2D Q1, 25 for
+    2D Q2)."""
     import torch
     x = torch.randn(ctx.n_vdof, dtype=torch.float32, device=ctx.device)
     y = torch.empty_like(x)
@@ -317,9 +334,10 @@ def time_kernel_apply(ctx, reps=20):
     e.record()
     torch.cuda.synchronize()
     sec = s.elapsed_time(e) / 1e3 / reps
-    nq = 27 if ctx.dim == 3 else 9
+    nq = 25 if ctx.order == 2 else (27 if ctx.dim == 3 else 9)
     byts = 4 * 2 * ctx.n_vdof + 4 * nq * ctx.n_el
-    return {"name": "k_applyK_q1_%dd<float> (+ BC copy)" % ctx.dim, "seconds": sec, "bytes": byts}
+    name = "k_applyK_q2<float>" if ctx.order == 2 else ("k_applyK_q1_3d_tiled<float>" if ctx.dim == 3 else "k_applyK_q1_2d<float>")
+    return {"name": name + " (+ BC copy)", "seconds": sec, "bytes": byts}
 
 
 def run_kernel(args):
@@ -330,7 +348,7 @@ def run_kernel(args):
     from underworld2_gb300._core import Context, rng_seed
     cfg = CONFIGS[args.config]
     dim = cfg["dim"]
-    ctx = Context(dim, cfg["res"], (0.0,) * dim, (1.0,) * dim)
+    ctx = Context(dim, cfg["res"], (0.0,) * dim, (1.0,) * dim, order=cfg.get("order", 1), porder=cfg.get("porder", 0))
     ctx.set_bcs(freeslip_mask(ctx))
     ppc = args.kernel_ppc or cfg["ppc"]
     x, owner, off, lst, _ = ctx.layout_random(ppc, rng_seed(13))
@@ -361,7 +379,7 @@ def run_profile_solve(args):
     from underworld2_gb300._core import Context, rng_seed
     cfg = CONFIGS[args.config]
     dim = cfg["dim"]
-    ctx = Context(dim, cfg["res"], (0.0,) * dim, (1.0,) * dim)
+    ctx = Context(dim, cfg["res"], (0.0,) * dim, (1.0,) * dim, order=cfg.get("order", 1), porder=cfg.get("porder", 0))
     ctx.set_bcs(freeslip_mask(ctx))
     ppc = args.kernel_ppc or cfg["ppc"]
     x, owner, off, lst, _ = ctx.layout_random(ppc, rng_seed(13))
@@ -371,7 +389,7 @@ def run_profile_solve(args):
     ctx.assemble(off, lst, ip_xi, ip_w, eta, body)
     u, p = ctx.zeros(ctx.n_vdof), ctx.zeros(ctx.n_pdof)
     st = ctx.solve(u, p, mixed=1 if args.mode == "mixed" else 0, rtol=1e-8, inner_rtol=args.inner_rtol,
-                   outer_rtol=args.outer_rtol, smooth_steps=2, restart=120, schur_pc=args.schur_pc,
+                   outer_rtol=args.outer_rtol, smooth_steps=2, restart=120, schur_pc=args.schur_pc if cfg.get("porder", 0) == 0 else 0,
                    schur_pc_rtol=args.bfbt_rtol, max_outer=args.max_outer)
     torch.cuda.synchronize()
     print(json.dumps({"profile_solve": args.config, "particles_per_cell": ppc,
@@ -409,11 +427,16 @@ def count_launches(ctx, x0, owner0, off0, lst0, eta0, body0, mixed, opts, u, p):
 # ---------------------------------------------------------------------------
 def cpu_baseline(args, quick=False):
     from oracle import cpu_reference
-    return cpu_reference.measure(CONFIGS[args.config], workload_name(args.config), quick=quick)
+    try:
+        return cpu_reference.measure(CONFIGS[args.config], workload_name(args.config), quick=quick)
+    except NotImplementedError as e:
+        return {"unavailable": str(e)}
 
 
 def run_reference(args):
     res = cpu_baseline(args)
+    if "unavailable" in res:
+        return {"impl": "reference", "unavailable": res["unavailable"]}
     line = {
         "impl": "reference",
         "metric": "Stokes solve time @1e-8 resid (learned+FP32 vs FP64 GPU); particles/s advected",

@@ -79,6 +79,8 @@ def _solve_counts(cfg, res):
 
 
 def measure(cfg, workload, quick=False):
+    if cfg.get("order", 1) != 1:
+        raise NotImplementedError("the CPU solver port covers Q1/dQ0 only")
     dim, ppc = cfg["dim"], cfg["ppc"]
     res = cfg["res"]
     L = oracle.lib()
