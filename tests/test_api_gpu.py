@@ -93,3 +93,44 @@ def test_errors_match_reference(gpu):
         s.solve(nonLinearTolerance=-1.0)
     with pytest.raises(ValueError):
         s.set_inner_method("lu")
+
+
+def test_q2_dpc1_rayleigh_taylor_through_the_api(gpu):
+    """The same script shape on a Q2/dPc1 mesh (the reference's Rayleigh-Taylor
+    examples use this element pair): solve, residuals, vrms, RK2 against the oracle."""
+    import underworld2_gb300 as uw
+    res = (16, 16)
+    mesh = uw.mesh.FeMesh_Cartesian(elementType="Q2/dPc1", elementRes=res, minCoord=(0.0, 0.0), maxCoord=(1.0, 1.0))
+    assert mesh.data.shape == ((2 * res[0] + 1) * (2 * res[1] + 1), 2)
+    velocityField = mesh.add_variable(nodeDofCount=2)
+    pressureField = mesh.subMesh.add_variable(nodeDofCount=1)
+    assert pressureField.data.shape == (3 * res[0] * res[1], 1)
+    swarm = uw.swarm.Swarm(mesh=mesh)
+    material = swarm.add_variable(dataType="int", count=1)
+    swarm.populate_using_layout(layout=uw.swarm.layouts.PerCellRandomLayout(swarm=swarm, particlesPerCell=20, seed=13))
+    xy = swarm.particleCoordinates.data
+    material.data[:, 0] = (xy[:, 1] > 0.2 + 0.02 * np.cos(np.pi * xy[:, 0])).astype(np.int32)
+    fn_visc = uw.function.branching.map(fn_key=material, mapping={0: 0.01, 1: 1.0})
+    fn_dens = uw.function.branching.map(fn_key=material, mapping={0: 0.0, 1: 1.0})
+    iWalls = mesh.specialSets["MinI_VertexSet"] + mesh.specialSets["MaxI_VertexSet"]
+    jWalls = mesh.specialSets["MinJ_VertexSet"] + mesh.specialSets["MaxJ_VertexSet"]
+    bc = uw.conditions.DirichletCondition(variable=velocityField, indexSetsPerDof=(iWalls, jWalls))
+    stokes = uw.systems.Stokes(velocityField=velocityField, pressureField=pressureField, voronoi_swarm=swarm,
+                               conditions=[bc], fn_viscosity=fn_visc, fn_bodyforce=fn_dens * (0.0, -1.0))
+    solver = uw.systems.Solver(stokes)
+    solver.set_inner_method("mixed")
+    solver.set_inner_rtol(1e-10)
+    solver.set_outer_rtol(1e-9)
+    solver.solve()
+    st = solver.get_stats()
+    assert st.residual <= 1e-8
+    r_mom, r_cont = stokes.eqResiduals
+    assert r_mom < 1e-7 and r_cont < 1e-7
+    assert stokes.velocity_rms() > 0.0
+    adv = uw.systems.SwarmAdvector(velocityField=velocityField, swarm=swarm, order=2)
+    dt = adv.get_max_dt()
+    m = oracle.Mesh(2, 2, res, (0.0, 0.0), (1.0, 1.0), porder=1)
+    x0 = swarm.particleCoordinates.data.copy()
+    adv.integrate(dt)
+    xo, counts = m.rk2(velocityField.data.ravel(), dt, x0)
+    np.testing.assert_array_equal(swarm.particleCoordinates.data, xo)

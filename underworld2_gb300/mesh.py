@@ -45,15 +45,20 @@ class IndexSet:
 
 
 class FeMesh_Cartesian:
-    """Regular Cartesian mesh, ``elementType`` 'Q1/dQ0' (primary Q1, dQ0 sub-mesh)."""
+    """Regular Cartesian mesh: ``elementType`` 'Q1/dQ0' (2D and 3D) or 'Q2/dPc1'
+    (2D): primary velocity mesh and the pressure sub-mesh."""
 
     def __init__(self, elementType="Q1/dQ0", elementRes=(4, 4), minCoord=(0.0, 0.0), maxCoord=(1.0, 1.0),
                  periodic=None, partitioned=True, **kwargs):
         if isinstance(elementType, str):
             elementType = re.split(",|-|/", elementType)
         types = [t.upper() for t in elementType]
-        if types[0] not in ("Q1",) or (len(types) > 1 and types[1] not in ("DQ0",)):
-            raise ValueError("supported element type: 'Q1/dQ0' (got %s)" % "/".join(elementType))
+        if types[0] == "Q1" and (len(types) == 1 or types[1] == "DQ0"):
+            order, porder = 1, 0
+        elif types[0] == "Q2" and len(types) > 1 and types[1] == "DPC1" and len(elementRes) == 2:
+            order, porder = 2, 1
+        else:
+            raise ValueError("supported element types: 'Q1/dQ0', and 'Q2/dPc1' in 2D (got %s)" % "/".join(elementType))
         if periodic and any(periodic):
             raise ValueError("periodic meshes are not supported")
         if len(elementRes) not in (2, 3) or len(minCoord) != len(elementRes) or len(maxCoord) != len(elementRes):
@@ -62,9 +67,10 @@ class FeMesh_Cartesian:
         self.elementRes = tuple(int(r) for r in elementRes)
         self.minCoord = tuple(float(v) for v in minCoord)
         self.maxCoord = tuple(float(v) for v in maxCoord)
-        self.elementType = "Q1"
+        self.elementType = "Q%d" % order
+        self._order, self._porder = order, porder
         self._ctx = None
-        n = [r + 1 for r in self.elementRes]
+        n = [r * order + 1 for r in self.elementRes]
         self.nodesGlobal = int(np.prod(n))
         self.elementsGlobal = int(np.prod(self.elementRes))
         self._axes = [self.minCoord[d] + (np.arange(n[d]) / (n[d] - 1)) * (self.maxCoord[d] - self.minCoord[d])
@@ -77,7 +83,8 @@ class FeMesh_Cartesian:
     @property
     def ctx(self):
         if self._ctx is None:
-            self._ctx = _core.Context(self.dim, self.elementRes, self.minCoord, self.maxCoord)
+            self._ctx = _core.Context(self.dim, self.elementRes, self.minCoord, self.maxCoord,
+                                      order=self._order, porder=self._porder)
         return self._ctx
 
     @property
@@ -98,7 +105,7 @@ class FeMesh_Cartesian:
         return MeshVariable(self, nodeDofCount, dataType)
 
     def _node_grid(self):
-        n = [r + 1 for r in self.elementRes]
+        n = [r * self._order + 1 for r in self.elementRes]
         idx = np.arange(self.nodesGlobal)
         out = [idx % n[0], (idx // n[0]) % n[1]]
         if self.dim == 3:
@@ -107,21 +114,26 @@ class FeMesh_Cartesian:
 
 
 class _SubMesh:
-    """The dQ0 pressure mesh: one node per element at its centroid."""
+    """The pressure mesh: dQ0 (one node per element at its centroid) or dPc1
+    (three per element, the coefficients of the linear basis of
+    BilinearInnerElType.c:169-179)."""
 
     def __init__(self, mesh):
         self.parent = mesh
         self.dim = mesh.dim
-        self.elementType = "DQ0"
-        self.nodesGlobal = mesh.elementsGlobal
+        self.elementType = "DQ0" if mesh._porder == 0 else "DPC1"
+        self._npn = 1 if mesh._porder == 0 else 3
+        self.nodesGlobal = mesh.elementsGlobal * self._npn
         self.elementsGlobal = mesh.elementsGlobal
         self.elementRes = mesh.elementRes
 
     @property
     def data(self):
-        ax = [0.5 * (a[1:] + a[:-1]) for a in self.parent._axes]
+        o = self.parent._order
+        ax = [0.5 * (a[o::o] + a[:-o:o]) for a in self.parent._axes]
         g = np.meshgrid(*ax, indexing="ij")
-        return np.stack([a.transpose().ravel() for a in g], axis=1)
+        c = np.stack([a.transpose().ravel() for a in g], axis=1)
+        return np.repeat(c, self._npn, axis=0)
 
     def add_variable(self, nodeDofCount, dataType="double", **kwargs):
         return MeshVariable(self, nodeDofCount, dataType)
@@ -191,12 +203,25 @@ class MeshVariable:
         ctx = self._primary().ctx
         if isinstance(self.mesh, FeMesh_Cartesian):
             if self.nodeDofCount != self.mesh.dim:
-                raise ValueError("interpolation of Q1 fields needs dim components")
+                raise ValueError("interpolation of velocity-mesh fields needs dim components")
             dev = self._to_device()
             return ctx.interpolate(coords.contiguous(), dev)
         own = ctx.locate(coords.contiguous()).long()
         vals = torch.from_numpy(self._data).to(ctx.device)
-        return vals[own.clamp(max=vals.shape[0] - 1)]
+        npn = self.mesh._npn
+        if npn == 1:
+            return vals[own.clamp(max=vals.shape[0] - 1)]
+        # dPc1: sum_k p_k M_k(xi) at the points' local coordinates
+        pm = self._primary()
+        el = own.clamp(max=pm.elementsGlobal - 1)
+        ij = (el % pm.elementRes[0], el // pm.elementRes[0])
+        xi = []
+        for d in range(2):
+            corners = torch.from_numpy(np.ascontiguousarray(pm._axes[d][:: pm._order])).to(ctx.device)
+            lo, hi = corners[ij[d]], corners[ij[d] + 1]
+            xi.append(2.0 * (coords[:, d] - lo) / (hi - lo) - 1.0)
+        M = torch.stack([-xi[0] - 0.5 * xi[1] + 0.25, xi[0] - 0.5 * xi[1] + 0.25, xi[1] + 0.5], 1)
+        return (vals.view(-1, 3)[el] * M).sum(1, keepdim=True)
 
     def __add__(self, o): return self._as_function() + o
     def __radd__(self, o): return o + self._as_function()

@@ -15,7 +15,7 @@ from . import swarm as _swarm
 
 class Stokes:
     """The incompressible (or compressible) Stokes system K u + G p = f,
-    G^T u + C p = h on a Q1/dQ0 mesh (P/systems/_stokes.py:106-330)."""
+    G^T u + C p = h on a Q1/dQ0 or 2D Q2/dPc1 mesh (P/systems/_stokes.py:106-330)."""
 
     def __init__(self, velocityField, pressureField, fn_viscosity, fn_bodyforce=None, fn_one_on_lambda=None,
                  fn_source=None, voronoi_swarm=None, conditions=[], gauss_swarm=None, _removeBCs=True,
@@ -156,11 +156,16 @@ class Stokes:
         r = ctx.residuals(u, p)
         return float(r[0]), float(r[1])
 
+    def _velocity_rms_q2(self, v):
+        return _q2_rms(self.mesh, v)
+
     def velocity_rms(self):
         """sqrt(int v.v / int 1) over the mesh, Gauss quadrature (P/systems/_stokes.py:435-448)."""
         mesh = self.mesh
         v = self._velocityField.data
         dim = mesh.dim
+        if mesh._order == 2:
+            return self._velocity_rms_q2(v)
         x1, w1 = np.polynomial.legendre.leggauss(2)
         n = [r + 1 for r in mesh.elementRes]
         grid = v.reshape(*(n[::-1]), dim)
@@ -190,6 +195,28 @@ class Stokes:
                         num += np.sum(w1[i] * w1[j] * w1[k] * 0.125 * volm * np.sum(val ** 2, axis=-1))
                         vol += np.sum(w1[i] * w1[j] * w1[k] * 0.125 * volm)
         return float(np.sqrt(num / vol))
+
+
+def _q2_rms(mesh, v):
+    """velocity_rms on a 2D Q2 mesh: 3x3 Gauss points per element."""
+    x1, w1 = np.polynomial.legendre.leggauss(3)
+    rx, ry = mesh.elementRes
+    grid = v.reshape(2 * ry + 1, 2 * rx + 1, 2)
+    hx = np.diff(mesh._axes[0][::2])
+    hy = np.diff(mesh._axes[1][::2])
+    area = np.outer(hy, hx)
+    N = lambda s: (0.5 * s * (s - 1.0), 1.0 - s * s, 0.5 * s * (s + 1.0))
+    num = vol = 0.0
+    for j in range(3):
+        for i in range(3):
+            Nx, Ny = N(x1[i]), N(x1[j])
+            val = 0.0
+            for b in range(3):
+                for a in range(3):
+                    val = val + Nx[a] * Ny[b] * grid[b: b + 2 * ry: 2, a: a + 2 * rx: 2]
+            num += np.sum(w1[i] * w1[j] * 0.25 * area * np.sum(val ** 2, axis=-1))
+            vol += np.sum(w1[i] * w1[j] * 0.25 * area)
+    return float(np.sqrt(num / vol))
 
 
 class _Options:
@@ -295,7 +322,8 @@ class StokesSolver:
         o = self.options
         st = ctx.solve(u, p, mixed=int(o.A11._mixed), rtol=min(o.A11.ksp_rtol, o.scr.ksp_rtol),
                        inner_rtol=o.A11.ksp_rtol, outer_rtol=o.scr.ksp_rtol, max_inner=o.main.max_inner,
-                       max_outer=o.main.max_outer, smooth_steps=o.mg.smooth_steps, restart=o.scr.restart)
+                       max_outer=o.main.max_outer, smooth_steps=o.mg.smooth_steps, restart=o.scr.restart,
+                       schur_pc=1 if s.mesh._porder == 0 else 0)
         s._velocityField._from_device()
         s._pressureField._from_device()
         st["assembly_time"] = t1 - t0
