@@ -311,19 +311,28 @@ __device__ __forceinline__ void pmg_cp_async4z(void* smem, const void* gmem, boo
 #define PT_X 16
 #define PT_Y 8
 #define PT_Z 8
+// cell size along axis d of halo cell i of a tile starting at t0 (0 outside the grid)
+__device__ __forceinline__ float pmg_hcell(const uwg_lgeom& g, int d, int t0, int i) {
+    const int c0 = t0 - 1 + i;
+    const int r = d == 0 ? g.res[0] : d == 1 ? g.res[1] : g.res[2];
+    const double* a = d == 0 ? g.ax[0] : d == 1 ? g.ax[1] : g.ax[2];
+    return (c0 >= 0 && c0 < r) ? (float)(a[c0 + 1] - a[c0]) : 0.f;
+}
+
 __global__ void __launch_bounds__(256) k_papply0_mf(uwg_lgeom g, const float* __restrict__ W,
                                                     const float* __restrict__ x, float* __restrict__ y) {
-    constexpr int HX = PT_X + 2, HY = PT_Y + 2, HZ = PT_Z + 2, NH = HX * HY * HZ;
-    constexpr int NX = PT_X + 1, NY = PT_Y + 1, NZ = PT_Z + 1, NN = NX * NY * NZ;
+    constexpr int HX = PT_X + 2, HY = PT_Y + 2, HZ = PT_Z + 2, NH = HX * HY * HZ, HXY = HX * HY;
+    constexpr int NX = PT_X + 1, NY = PT_Y + 1, NZ = PT_Z + 1, NN = NX * NY * NZ, NXY = NX * NY;
     __shared__ float ps[NH];
     __shared__ float vs[3][NN];
-    __shared__ float hs[3][HX];   // cell sizes along each axis (halo included, 0 outside)
+    // face areas of the halo cells, / 4: A0 = hy hz, A1 = hx hz, A2 = hx hy
+    __shared__ float A0[HY][HZ], A1[HX][HZ], A2[HX][HY];
     const int ntx = (g.res[0] + PT_X - 1) / PT_X, nty = (g.res[1] + PT_Y - 1) / PT_Y;
     const int tile = blockIdx.x;
     const int tx0 = (tile % ntx) * PT_X, ty0 = ((tile / ntx) % nty) * PT_Y, tz0 = (tile / (ntx * nty)) * PT_Z;
     const int64_t sy = g.res[0], sz = (int64_t)g.res[0] * g.res[1];
     for (int k = threadIdx.x; k < NN; k += blockDim.x) {
-        const int ni = k % NX, nj = (k / NX) % NY, nk = k / (NX * NY);
+        const int ni = k % NX, nj = (k / NX) % NY, nk = k / NXY;
         const int gi = tx0 + ni, gj = ty0 + nj, gk = tz0 + nk;
         if (gi < g.nx[0] && gj < g.nx[1] && gk < g.nx[2]) {
             const float* src = W + (gi + (int64_t)g.nx[0] * (gj + (int64_t)g.nx[1] * gk)) * 3;
@@ -333,35 +342,40 @@ __global__ void __launch_bounds__(256) k_papply0_mf(uwg_lgeom g, const float* __
         }
     }
     for (int k = threadIdx.x; k < NH; k += blockDim.x) {
-        const int i = k % HX, j = (k / HX) % HY, l = k / (HX * HY);
+        const int i = k % HX, j = (k / HX) % HY, l = k / HXY;
         const int cx = tx0 - 1 + i, cy = ty0 - 1 + j, cz = tz0 - 1 + l;
         const bool in = in_grid<3>(g, cx, cy, cz);
         pmg_cp_async4z(&ps[k], x + (in ? cx + sy * cy + sz * cz : 0), in);
     }
-    if (threadIdx.x < 3 * HX) {
-        const int d = threadIdx.x / HX, i = threadIdx.x % HX;
-        const int c0 = (d == 0 ? tx0 : d == 1 ? ty0 : tz0) - 1 + i;
-        const int r = d == 0 ? g.res[0] : d == 1 ? g.res[1] : g.res[2];
-        const double* a = d == 0 ? g.ax[0] : d == 1 ? g.ax[1] : g.ax[2];
-        hs[d][i] = (c0 >= 0 && c0 < r) ? (float)(a[c0 + 1] - a[c0]) : 0.f;
+    for (int t = threadIdx.x; t < HY * HZ + HX * HZ + HX * HY; t += blockDim.x) {
+        if (t < HY * HZ) {
+            const int j = t / HZ, l = t % HZ;
+            A0[j][l] = 0.25f * pmg_hcell(g, 1, ty0, j) * pmg_hcell(g, 2, tz0, l);
+        } else if (t < HY * HZ + HX * HZ) {
+            const int u = t - HY * HZ, i = u / HZ, l = u % HZ;
+            A1[i][l] = 0.25f * pmg_hcell(g, 0, tx0, i) * pmg_hcell(g, 2, tz0, l);
+        } else {
+            const int u = t - HY * HZ - HX * HZ, i = u / HY, j = u % HY;
+            A2[i][j] = 0.25f * pmg_hcell(g, 0, tx0, i) * pmg_hcell(g, 1, ty0, j);
+        }
     }
     asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;\n" ::: "memory");
     __syncthreads();
+    // W G x at the tile's nodes: differences of the eight surrounding cells
     for (int k = threadIdx.x; k < NN; k += blockDim.x) {
-        const int ni = k % NX, nj = (k / NX) % NY, nk = k / (NX * NY);
+        const int ni = k % NX, nj = (k / NX) % NY, nk = k / NXY;
         const int gi = tx0 + ni, gj = ty0 + nj, gk = tz0 + nk;
         float v0 = 0.f, v1 = 0.f, v2 = 0.f;
         if (gi < g.nx[0] && gj < g.nx[1] && gk < g.nx[2]) {
-#pragma unroll
-            for (int c = 0; c < 8; c++) {
-                const int cx = c & 1, cy = (c >> 1) & 1, cz = c >> 2;
-                const float pe = ps[(ni + cx) + HX * ((nj + cy) + HY * (nk + cz))];
-                const float hx = hs[0][ni + cx], hy = hs[1][nj + cy], hz = hs[2][nk + cz];
-                const float a0 = 0.25f * hy * hz, a1 = 0.25f * hx * hz, a2 = 0.25f * hx * hy;
-                v0 += (cx ? a0 : -a0) * pe;
-                v1 += (cy ? a1 : -a1) * pe;
-                v2 += (cz ? a2 : -a2) * pe;
-            }
+            const float* P = &ps[ni + HX * nj + HXY * nk];
+            const float p000 = P[0], p100 = P[1], p010 = P[HX], p110 = P[HX + 1];
+            const float p001 = P[HXY], p101 = P[HXY + 1], p011 = P[HXY + HX], p111 = P[HXY + HX + 1];
+            v0 = A0[nj][nk] * (p100 - p000) + A0[nj + 1][nk] * (p110 - p010) + A0[nj][nk + 1] * (p101 - p001) +
+                 A0[nj + 1][nk + 1] * (p111 - p011);
+            v1 = A1[ni][nk] * (p010 - p000) + A1[ni + 1][nk] * (p110 - p100) + A1[ni][nk + 1] * (p011 - p001) +
+                 A1[ni + 1][nk + 1] * (p111 - p101);
+            v2 = A2[ni][nj] * (p001 - p000) + A2[ni + 1][nj] * (p101 - p100) + A2[ni][nj + 1] * (p011 - p010) +
+                 A2[ni + 1][nj + 1] * (p111 - p110);
             v0 *= vs[0][k];
             v1 *= vs[1][k];
             v2 *= vs[2][k];
@@ -371,20 +385,19 @@ __global__ void __launch_bounds__(256) k_papply0_mf(uwg_lgeom g, const float* __
         vs[2][k] = v2;
     }
     __syncthreads();
+    // G^T: each cell sums its eight nodes, grouped by face
     for (int k = threadIdx.x; k < PT_X * PT_Y * PT_Z; k += blockDim.x) {
         const int i = k % PT_X, j = (k / PT_X) % PT_Y, l = k / (PT_X * PT_Y);
         const int ex = tx0 + i, ey = ty0 + j, ez = tz0 + l;
         if (!in_grid<3>(g, ex, ey, ez)) continue;
-        const float hx = hs[0][i + 1], hy = hs[1][j + 1], hz = hs[2][l + 1];
-        const float a0 = 0.25f * hy * hz, a1 = 0.25f * hx * hz, a2 = 0.25f * hx * hy;
-        float s = 0.f;
-#pragma unroll
-        for (int n = 0; n < 8; n++) {
-            const int lx = n & 1, ly = (n >> 1) & 1, lz = n >> 2;
-            const int q = (i + lx) + NX * ((j + ly) + NY * (l + lz));
-            s += (lx ? -a0 : a0) * vs[0][q] + (ly ? -a1 : a1) * vs[1][q] + (lz ? -a2 : a2) * vs[2][q];
-        }
-        y[ex + sy * ey + sz * ez] = s;
+        const int q = i + NX * j + NXY * l;
+        const float* V0 = &vs[0][q];
+        const float* V1 = &vs[1][q];
+        const float* V2 = &vs[2][q];
+        const float d0 = (V0[0] - V0[1]) + (V0[NX] - V0[NX + 1]) + (V0[NXY] - V0[NXY + 1]) + (V0[NXY + NX] - V0[NXY + NX + 1]);
+        const float d1 = (V1[0] - V1[NX]) + (V1[1] - V1[NX + 1]) + (V1[NXY] - V1[NXY + NX]) + (V1[NXY + 1] - V1[NXY + NX + 1]);
+        const float d2 = (V2[0] - V2[NXY]) + (V2[1] - V2[NXY + 1]) + (V2[NX] - V2[NXY + NX]) + (V2[NX + 1] - V2[NXY + NX + 1]);
+        y[ex + sy * ey + sz * ez] = A0[j + 1][l + 1] * d0 + A1[i + 1][l + 1] * d1 + A2[i + 1][j + 1] * d2;
     }
 }
 }  // namespace
