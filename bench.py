@@ -299,7 +299,8 @@ def run_gpu(args):
         "roofline": {"bound": "hbm", "kernel": kinfo["name"], "achieved": achieved, "peak": pk.get("hbm_gbs"),
                      "unit": "GB/s", "frac": achieved / pk.get("hbm_gbs", 6800.0),
                      "peak_source": "fallback" if pk.get("_fallback") else "measured",
-                     "traffic": None, "bytes_per_launch": kinfo["bytes"], "launch_s": kinfo["seconds"]},
+                     "traffic": dram_traffic(kinfo["name"], args.config), "bytes_per_launch": kinfo["bytes"],
+                     "launch_s": kinfo["seconds"]},
         "clocks": clk,
     }
     if args.count_launches:
@@ -314,6 +315,17 @@ def workload_name(key):
             "grf3d_small": "3D 32^3 Q1/dQ0 GRF viscosity, 20 ppc, free-slip",
             "sinker2d": "2D 64^2 Q1/dQ0 sinker, 20 ppc, free-slip (config 1)",
             "rt2d_q2": "2D 256^2 Q2/dPc1 Rayleigh-Taylor, 40 ppc, viscosity x 10^U(-1,1), free-slip (config 2)"}[key]
+
+
+def dram_traffic(kernel_name, config):
+    """DRAM bytes (read + write) per launch of the kernel on this workload, from
+    the ncu capture recorded in profiles/dram_traffic.json (None if absent)."""
+    try:
+        d = json.load(open(os.path.join(ROOT, "profiles", "dram_traffic.json")))
+        e = d[kernel_name.split(" ")[0] + " " + config]
+        return e["dram_bytes_read_per_launch"] + e["dram_bytes_write_per_launch"]
+    except Exception:
+        return None
 
 
 def time_kernel_apply(ctx, reps=20):
