@@ -400,6 +400,234 @@ __global__ void __launch_bounds__(256) k_papply0_mf(uwg_lgeom g, const float* __
         y[ex + sy * ey + sz * ez] = A0[j + 1][l + 1] * d0 + A1[i + 1][l + 1] * d1 + A2[i + 1][j + 1] * d2;
     }
 }
+
+// ---------------------------------------------------------------------------
+// Smooth checkerboard coarse space on the first coarsening.  With piecewise-
+// constant interpolation of the checkerboard component the CG iteration count
+// of L still grows with the mesh (the checkerboard branch of L behaves like a
+// fourth-order operator); interpolating that component cell-centred
+// trilinearly instead,
+//     p_fine(i) += (-1)^(i_x+i_y+i_z) sum_J w(i, J) c(J)
+// (weights 3/4, 1/4 per axis, clipped onto the cell itself at the walls),
+// halves it on 32^3 and more on finer meshes.  Level 1 then carries a
+// 5^dim-point checkerboard-checkerboard block, stored after the 3^dim x 2 x 2
+// blocks; deeper levels aggregate piecewise-constantly again, which brings
+// the stencil back to 3^dim points.
+// ---------------------------------------------------------------------------
+// 1D trilinear support of fine cell f: (p, 3/4) and (q, 1/4), q clipped to p at the walls
+__device__ __forceinline__ void tri1d(int f, int rc, int& p, int& q) {
+    p = f >> 1;
+    q = (f & 1) ? p + 1 : p - 1;
+    if (q < 0 || q >= rc) q = p;
+}
+// weight of coarse cell I in fine cell f's 1D support
+__device__ __forceinline__ float tri1w(int f, int rc, int I) {
+    int p, q;
+    tri1d(f, rc, p, q);
+    return (p == I ? 0.75f : 0.f) + (q == I ? 0.25f : 0.f);
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(128) k_pgal01_tri(uwg_lgeom gf, uwg_lgeom gc, const float* __restrict__ st0,
+                                                    float* __restrict__ st1, float* __restrict__ cc5) {
+    constexpr int NO = DIM == 3 ? 27 : 9, N5 = DIM == 3 ? 125 : 25, NF = DIM == 3 ? 64 : 16;
+    __shared__ float ss[NO], sc[NO], cs[NO], cc[N5];
+    const int64_t I = blockIdx.x;
+    const int64_t nf = gf.n_el, nc = gc.n_el;
+    int X, Y, Z;
+    cell_xyz<DIM>(gc, I, X, Y, Z);
+    const int rc[3] = {gc.res[0], gc.res[1], DIM == 3 ? gc.res[2] : 1};
+    for (int k = threadIdx.x; k < N5; k += blockDim.x) {
+        cc[k] = 0.f;
+        if (k < NO) { ss[k] = 0.f; sc[k] = 0.f; cs[k] = 0.f; }
+    }
+    __syncthreads();
+    // rows of the smooth component: the children of I (weight 1)
+    for (int t = threadIdx.x; t < (1 << DIM) * NO; t += blockDim.x) {
+        const int ch = t / NO, o = t % NO;
+        const int ix = 2 * X + (ch & 1), iy = 2 * Y + ((ch >> 1) & 1), iz = DIM == 3 ? 2 * Z + (ch >> 2) : 0;
+        const int64_t i = ix + (int64_t)gf.res[0] * (iy + (int64_t)gf.res[1] * iz);
+        const float v = st0[o * nf + i];
+        if (v == 0.f) continue;
+        const int jx = ix + o % 3 - 1, jy = iy + (o / 3) % 3 - 1, jz = DIM == 3 ? iz + o / 9 - 1 : 0;
+        if (!in_grid<DIM>(gf, jx, jy, jz)) continue;
+        atomicAdd(&ss[((jx >> 1) - X + 1) + 3 * ((jy >> 1) - Y + 1) + (DIM == 3 ? 9 * ((jz >> 1) - Z + 1) : 0)], v);
+        const float vj = ((jx + jy + jz) & 1) ? -v : v;
+        int px, qx, py, qy, pz = 0, qz = 0;
+        tri1d(jx, rc[0], px, qx);
+        tri1d(jy, rc[1], py, qy);
+        if (DIM == 3) tri1d(jz, rc[2], pz, qz);
+        for (int cz = 0; cz < (DIM == 3 ? 2 : 1); cz++)
+            for (int cy = 0; cy < 2; cy++)
+                for (int cx = 0; cx < 2; cx++) {
+                    const int Jx = cx ? qx : px, Jy = cy ? qy : py, Jz = cz ? qz : pz;
+                    const float w = (cx ? 0.25f : 0.75f) * (cy ? 0.25f : 0.75f) * (DIM == 3 ? (cz ? 0.25f : 0.75f) : 1.f);
+                    atomicAdd(&sc[(Jx - X + 1) + 3 * (Jy - Y + 1) + (DIM == 3 ? 9 * (Jz - Z + 1) : 0)], w * vj);
+                }
+    }
+    // rows of the checkerboard component: the fine cells of I's trilinear support
+    for (int t = threadIdx.x; t < NF * NO; t += blockDim.x) {
+        const int f = t / NO, o = t % NO;
+        const int ix = 2 * X - 1 + (f & 3), iy = 2 * Y - 1 + ((f >> 2) & 3), iz = DIM == 3 ? 2 * Z - 1 + (f >> 4) : 0;
+        if (!in_grid<DIM>(gf, ix, iy, iz)) continue;
+        const float wi = tri1w(ix, rc[0], X) * tri1w(iy, rc[1], Y) * (DIM == 3 ? tri1w(iz, rc[2], Z) : 1.f);
+        if (wi == 0.f) continue;
+        const int64_t i = ix + (int64_t)gf.res[0] * (iy + (int64_t)gf.res[1] * iz);
+        const float v0 = st0[o * nf + i];
+        if (v0 == 0.f) continue;
+        const float v = (((ix + iy + iz) & 1) ? -wi : wi) * v0;
+        const int jx = ix + o % 3 - 1, jy = iy + (o / 3) % 3 - 1, jz = DIM == 3 ? iz + o / 9 - 1 : 0;
+        if (!in_grid<DIM>(gf, jx, jy, jz)) continue;
+        atomicAdd(&cs[((jx >> 1) - X + 1) + 3 * ((jy >> 1) - Y + 1) + (DIM == 3 ? 9 * ((jz >> 1) - Z + 1) : 0)], v);
+        const float vj = ((jx + jy + jz) & 1) ? -v : v;
+        int px, qx, py, qy, pz = 0, qz = 0;
+        tri1d(jx, rc[0], px, qx);
+        tri1d(jy, rc[1], py, qy);
+        if (DIM == 3) tri1d(jz, rc[2], pz, qz);
+        for (int cz = 0; cz < (DIM == 3 ? 2 : 1); cz++)
+            for (int cy = 0; cy < 2; cy++)
+                for (int cx = 0; cx < 2; cx++) {
+                    const int Jx = cx ? qx : px, Jy = cy ? qy : py, Jz = cz ? qz : pz;
+                    const float w = (cx ? 0.25f : 0.75f) * (cy ? 0.25f : 0.75f) * (DIM == 3 ? (cz ? 0.25f : 0.75f) : 1.f);
+                    atomicAdd(&cc[(Jx - X + 2) + 5 * (Jy - Y + 2) + (DIM == 3 ? 25 * (Jz - Z + 2) : 0)], w * vj);
+                }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < N5; k += blockDim.x) {
+        cc5[k * nc + I] = cc[k];
+        if (k < NO) {
+            st1[(k * 4 + 0) * nc + I] = ss[k];
+            st1[(k * 4 + 1) * nc + I] = sc[k];
+            st1[(k * 4 + 2) * nc + I] = cs[k];
+            st1[(k * 4 + 3) * nc + I] = 0.f;
+        }
+    }
+}
+
+// Galerkin level 1 (smooth checkerboard block) -> level 2 (piecewise constant)
+template <int DIM>
+__global__ void k_pgal12(uwg_lgeom gf, uwg_lgeom gc, const float* __restrict__ stf, const float* __restrict__ cc5,
+                         float* __restrict__ stc) {
+    constexpr int NO = DIM == 3 ? 27 : 9, N5 = DIM == 3 ? 125 : 25;
+    int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (I >= gc.n_el) return;
+    int X, Y, Z;
+    cell_xyz<DIM>(gc, I, X, Y, Z);
+    float acc[NO][4];
+#pragma unroll
+    for (int o = 0; o < NO; o++)
+#pragma unroll
+        for (int k = 0; k < 4; k++) acc[o][k] = 0.f;
+    const int64_t nf = gf.n_el;
+    for (int cn = 0; cn < (1 << DIM); cn++) {
+        const int cx = cn & 1, cy = (cn >> 1) & 1, cz = DIM == 3 ? (cn >> 2) & 1 : 0;
+        const int64_t i = (2 * X + cx) + (int64_t)gf.res[0] * ((2 * Y + cy) + (int64_t)gf.res[1] * (2 * Z + cz));
+#pragma unroll
+        for (int o = 0; o < NO; o++) {
+            const int ox = o % 3 - 1, oy = (o / 3) % 3 - 1, oz = DIM == 3 ? o / 9 - 1 : 0;
+            const int O = (coarse_off(cx, ox) + 1) + 3 * (coarse_off(cy, oy) + 1) +
+                          (DIM == 3 ? 9 * (coarse_off(cz, oz) + 1) : 0);
+#pragma unroll
+            for (int k = 0; k < 3; k++) acc[O][k] += stf[(o * 4 + k) * nf + i];
+        }
+#pragma unroll
+        for (int o = 0; o < N5; o++) {
+            const int ox = o % 5 - 2, oy = (o / 5) % 5 - 2, oz = DIM == 3 ? o / 25 - 2 : 0;
+            const int O = (((cx + ox + 4) >> 1) - 1) + 3 * (((cy + oy + 4) >> 1) - 1) +
+                          (DIM == 3 ? 9 * (((cz + oz + 4) >> 1) - 1) : 0);
+            acc[O][3] += cc5[o * nf + i];
+        }
+    }
+#pragma unroll
+    for (int o = 0; o < NO; o++)
+#pragma unroll
+        for (int k = 0; k < 4; k++) stc[(o * 4 + k) * gc.n_el + I] = acc[o][k];
+}
+
+// y = A_1 x on level 1 with the smooth checkerboard block (branch-free, clamped)
+template <int DIM>
+__global__ void __launch_bounds__(256) k_papply1_tri(uwg_lgeom g, const float* __restrict__ st,
+                                                     const float* __restrict__ cc5, const float* __restrict__ x,
+                                                     float* __restrict__ y) {
+    constexpr int NO = DIM == 3 ? 27 : 9, N5 = DIM == 3 ? 125 : 25;
+    const int64_t n = g.n_el;
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const int64_t sy = g.res[0], sz = (int64_t)g.res[0] * g.res[1];
+    float a0 = 0.f, a1 = 0.f;
+#pragma unroll 9
+    for (int o = 0; o < NO; o++) {
+        const int ox = o % 3 - 1, oy = (o / 3) % 3 - 1, oz = DIM == 3 ? o / 9 - 1 : 0;
+        int64_t j = e + ox + oy * sy + oz * sz;
+        j = j < 0 ? 0 : (j >= n ? n - 1 : j);
+        const float xs = __ldg(&x[j]), xc = __ldg(&x[n + j]);
+        a0 += __ldg(&st[(o * 4 + 0) * n + e]) * xs + __ldg(&st[(o * 4 + 1) * n + e]) * xc;
+        a1 += __ldg(&st[(o * 4 + 2) * n + e]) * xs;
+    }
+#pragma unroll 25
+    for (int o = 0; o < N5; o++) {
+        const int ox = o % 5 - 2, oy = (o / 5) % 5 - 2, oz = DIM == 3 ? o / 25 - 2 : 0;
+        int64_t j = e + ox + oy * sy + oz * sz;
+        j = j < 0 ? 0 : (j >= n ? n - 1 : j);
+        a1 += __ldg(&cc5[o * n + e]) * __ldg(&x[n + j]);
+    }
+    y[e] = a0;
+    y[n + e] = a1;
+}
+
+// rc = P^T rf, level 0 -> 1, smooth checkerboard component
+template <int DIM>
+__global__ void k_prestrict_tri(uwg_lgeom gf, uwg_lgeom gc, const float* __restrict__ rf, float* __restrict__ rc_) {
+    int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (I >= gc.n_el) return;
+    int X, Y, Z;
+    cell_xyz<DIM>(gc, I, X, Y, Z);
+    float s0 = 0.f, s1 = 0.f;
+    for (int f = 0; f < (DIM == 3 ? 64 : 16); f++) {
+        const int ix = 2 * X - 1 + (f & 3), iy = 2 * Y - 1 + ((f >> 2) & 3), iz = DIM == 3 ? 2 * Z - 1 + (f >> 4) : 0;
+        if (!in_grid<DIM>(gf, ix, iy, iz)) continue;
+        const float v = rf[ix + (int64_t)gf.res[0] * (iy + (int64_t)gf.res[1] * iz)];
+        if ((ix >> 1) == X && (iy >> 1) == Y && (DIM == 2 || (iz >> 1) == Z)) s0 += v;
+        const float w = tri1w(ix, gc.res[0], X) * tri1w(iy, gc.res[1], Y) * (DIM == 3 ? tri1w(iz, gc.res[2], Z) : 1.f);
+        s1 += (((ix + iy + iz) & 1) ? -w : w) * v;
+    }
+    rc_[I] = s0;
+    rc_[gc.n_el + I] = s1;
+}
+
+// xf += P xc, level 1 -> 0, smooth checkerboard component
+template <int DIM>
+__global__ void k_pprolong_tri(uwg_lgeom gf, uwg_lgeom gc, const float* __restrict__ xc, float* __restrict__ xf) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= gf.n_el) return;
+    int x, y, z;
+    cell_xyz<DIM>(gf, i, x, y, z);
+    const int64_t nc = gc.n_el, sy = gc.res[0], sz = (int64_t)gc.res[0] * gc.res[1];
+    int px, qx, py, qy, pz = 0, qz = 0;
+    tri1d(x, gc.res[0], px, qx);
+    tri1d(y, gc.res[1], py, qy);
+    if (DIM == 3) tri1d(z, gc.res[2], pz, qz);
+    float c = 0.f;
+#pragma unroll
+    for (int cz = 0; cz < (DIM == 3 ? 2 : 1); cz++)
+#pragma unroll
+        for (int cy = 0; cy < 2; cy++)
+#pragma unroll
+            for (int cx = 0; cx < 2; cx++) {
+                const float w = (cx ? 0.25f : 0.75f) * (cy ? 0.25f : 0.75f) * (DIM == 3 ? (cz ? 0.25f : 0.75f) : 1.f);
+                c += w * xc[nc + (cx ? qx : px) + sy * (cy ? qy : py) + sz * (cz ? qz : pz)];
+            }
+    xf[i] += xc[(x >> 1) + sy * (y >> 1) + sz * (DIM == 3 ? (z >> 1) : 0)] + (((x + y + z) & 1) ? -c : c);
+}
+
+__global__ void k_pdiag1_tri(int64_t n, int center, int center5, const float* __restrict__ st,
+                             const float* __restrict__ cc5, float* __restrict__ d) {
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const float a = st[(center * 4) * n + e], b = cc5[center5 * n + e];
+    d[e] = a > 0.f ? a : 1.f;
+    d[n + e] = b > 0.f ? b : 1.f;
+}
 }  // namespace
 
 #define PMG_DIM(KERN, GRID, ...)                                               \
@@ -420,9 +648,17 @@ __global__ void __launch_bounds__(256) k_papply0_mf(uwg_lgeom g, const float* __
 
 int uwg_pmg_ncomp(int l) { return l == 0 ? 1 : 2; }
 
+// level 1 uses the smooth checkerboard interpolation when it is not the coarsest level
+static bool smooth1(const uwg_ctx* c) { return c->nlev >= 3; }
+
 int64_t uwg_pmg_stencil_size(const uwg_ctx* c, int l) {
-    int no = c->dim == 3 ? 27 : 9;
-    return (int64_t)no * (l == 0 ? 1 : 4) * c->lev[l].n_el;
+    int no = c->dim == 3 ? 27 : 9, n5 = c->dim == 3 ? 125 : 25;
+    int64_t s = (int64_t)no * (l == 0 ? 1 : 4) * c->lev[l].n_el;
+    if (l == 1 && smooth1(c)) s += (int64_t)n5 * c->lev[l].n_el;   // 5^dim checkerboard block after the 3^dim blocks
+    return s;
+}
+static float* cc5_of(const uwg_ctx* c, const float* st1) {
+    return (float*)st1 + (int64_t)(c->dim == 3 ? 27 : 9) * 4 * c->lev[1].n_el;
 }
 
 int uwg_pmg_stencil(uwg_ctx* c, int l, const float* W0, const float* st_fine, float* st) {
@@ -431,8 +667,16 @@ int uwg_pmg_stencil(uwg_ctx* c, int l, const float* W0, const float* st_fine, fl
         PMG_DIM(k_pst0, nblk(g.n_el), g, W0, st);
     } else {
         uwg_lgeom gf = uwg_level_geom(c, l - 1), gc = uwg_level_geom(c, l);
-        if (l == 1) PMG_DIM(k_pgal01, nblk(gc.n_el, 128), gf, gc, st_fine, st);
-        else PMG_DIM(k_pgal22, nblk(gc.n_el, 128), gf, gc, st_fine, st);
+        if (l == 1 && smooth1(c)) {
+            if (c->dim == 3) k_pgal01_tri<3><<<(unsigned)gc.n_el, 128, 0, c->stream>>>(gf, gc, st_fine, st, cc5_of(c, st));
+            else k_pgal01_tri<2><<<(unsigned)gc.n_el, 128, 0, c->stream>>>(gf, gc, st_fine, st, cc5_of(c, st));
+        } else if (l == 1) {
+            PMG_DIM(k_pgal01, nblk(gc.n_el, 128), gf, gc, st_fine, st);
+        } else if (l == 2 && smooth1(c)) {
+            PMG_DIM(k_pgal12, nblk(gc.n_el, 128), gf, gc, st_fine, cc5_of(c, st_fine), st);
+        } else {
+            PMG_DIM(k_pgal22, nblk(gc.n_el, 128), gf, gc, st_fine, st);
+        }
     }
     UWG_CUDA(c, cudaGetLastError());
     return UWG_OK;
@@ -440,6 +684,11 @@ int uwg_pmg_stencil(uwg_ctx* c, int l, const float* W0, const float* st_fine, fl
 
 int uwg_pmg_apply(uwg_ctx* c, int l, const float* st, const float* x, float* y) {
     uwg_lgeom g = uwg_level_geom(c, l);
+    if (l == 1 && smooth1(c)) {
+        PMG_DIM(k_papply1_tri, nblk(g.n_el), g, st, cc5_of(c, st), x, y);
+        UWG_CUDA(c, cudaGetLastError());
+        return UWG_OK;
+    }
     PMG_DIM_NC(k_papply, uwg_pmg_ncomp(l), nblk(g.n_el), g, st, x, y);
     UWG_CUDA(c, cudaGetLastError());
     return UWG_OK;
@@ -459,6 +708,7 @@ int uwg_pmg_diag(uwg_ctx* c, int l, const float* st, float* d) {
     int64_t n = c->lev[l].n_el;
     int center = c->dim == 3 ? 13 : 4;
     if (l == 0) k_pdiag<1><<<nblk(n), 256, 0, c->stream>>>(n, center, st, d);
+    else if (l == 1 && smooth1(c)) k_pdiag1_tri<<<nblk(n), 256, 0, c->stream>>>(n, center, c->dim == 3 ? 62 : 12, st, cc5_of(c, st), d);
     else k_pdiag<2><<<nblk(n), 256, 0, c->stream>>>(n, center, st, d);
     UWG_CUDA(c, cudaGetLastError());
     return UWG_OK;
@@ -466,14 +716,16 @@ int uwg_pmg_diag(uwg_ctx* c, int l, const float* st, float* d) {
 
 int uwg_pmg_restrict(uwg_ctx* c, int lc, const float* rf, float* rc) {
     uwg_lgeom gf = uwg_level_geom(c, lc - 1), gc = uwg_level_geom(c, lc);
-    PMG_DIM_NC(k_prestrict, uwg_pmg_ncomp(lc - 1), nblk(gc.n_el), gf, gc, rf, rc);
+    if (lc == 1 && smooth1(c)) PMG_DIM(k_prestrict_tri, nblk(gc.n_el), gf, gc, rf, rc);
+    else PMG_DIM_NC(k_prestrict, uwg_pmg_ncomp(lc - 1), nblk(gc.n_el), gf, gc, rf, rc);
     UWG_CUDA(c, cudaGetLastError());
     return UWG_OK;
 }
 
 int uwg_pmg_prolong_add(uwg_ctx* c, int lc, const float* xc, float* xf) {
     uwg_lgeom gf = uwg_level_geom(c, lc - 1), gc = uwg_level_geom(c, lc);
-    PMG_DIM_NC(k_pprolong_add, uwg_pmg_ncomp(lc - 1), nblk(gf.n_el), gf, gc, xc, xf);
+    if (lc == 1 && smooth1(c)) PMG_DIM(k_pprolong_tri, nblk(gf.n_el), gf, gc, xc, xf);
+    else PMG_DIM_NC(k_pprolong_add, uwg_pmg_ncomp(lc - 1), nblk(gf.n_el), gf, gc, xc, xf);
     UWG_CUDA(c, cudaGetLastError());
     return UWG_OK;
 }
