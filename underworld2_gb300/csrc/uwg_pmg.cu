@@ -544,54 +544,32 @@ __global__ void k_pgal12(uwg_lgeom gf, uwg_lgeom gc, const float* __restrict__ s
         for (int k = 0; k < 4; k++) stc[(o * 4 + k) * gc.n_el + I] = acc[o][k];
 }
 
-// y = A_1 x on level 1 with the smooth checkerboard block (branch-free, clamped;
-// loads issued in groups so that many are in flight per thread)
+// y = A_1 x on level 1 with the smooth checkerboard block (branch-free, clamped)
 template <int DIM>
 __global__ void __launch_bounds__(256) k_papply1_tri(uwg_lgeom g, const float* __restrict__ st,
                                                      const float* __restrict__ cc5, const float* __restrict__ x,
                                                      float* __restrict__ y) {
     constexpr int NO = DIM == 3 ? 27 : 9, N5 = DIM == 3 ? 125 : 25;
-    constexpr int G3 = 9, G5 = DIM == 3 ? 25 : 5;
     const int64_t n = g.n_el;
     int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (e >= n) return;
     const int64_t sy = g.res[0], sz = (int64_t)g.res[0] * g.res[1];
     float a0 = 0.f, a1 = 0.f;
-#pragma unroll
-    for (int o0 = 0; o0 < NO; o0 += G3) {
-        float s0[G3], s1[G3], s2[G3], xs[G3], xc[G3];
-#pragma unroll
-        for (int k = 0; k < G3; k++) {
-            const int o = o0 + k;
-            const int ox = o % 3 - 1, oy = (o / 3) % 3 - 1, oz = DIM == 3 ? o / 9 - 1 : 0;
-            int64_t j = e + ox + oy * sy + oz * sz;
-            j = j < 0 ? 0 : (j >= n ? n - 1 : j);
-            xs[k] = __ldg(&x[j]);
-            xc[k] = __ldg(&x[n + j]);
-            s0[k] = __ldg(&st[(o * 4 + 0) * n + e]);
-            s1[k] = __ldg(&st[(o * 4 + 1) * n + e]);
-            s2[k] = __ldg(&st[(o * 4 + 2) * n + e]);
-        }
-#pragma unroll
-        for (int k = 0; k < G3; k++) {
-            a0 += s0[k] * xs[k] + s1[k] * xc[k];
-            a1 += s2[k] * xs[k];
-        }
+#pragma unroll 9
+    for (int o = 0; o < NO; o++) {
+        const int ox = o % 3 - 1, oy = (o / 3) % 3 - 1, oz = DIM == 3 ? o / 9 - 1 : 0;
+        int64_t j = e + ox + oy * sy + oz * sz;
+        j = j < 0 ? 0 : (j >= n ? n - 1 : j);
+        const float xs = __ldg(&x[j]), xc = __ldg(&x[n + j]);
+        a0 += __ldg(&st[(o * 4 + 0) * n + e]) * xs + __ldg(&st[(o * 4 + 1) * n + e]) * xc;
+        a1 += __ldg(&st[(o * 4 + 2) * n + e]) * xs;
     }
-#pragma unroll
-    for (int o0 = 0; o0 < N5; o0 += G5) {
-        float cv[G5], xv[G5];
-#pragma unroll
-        for (int k = 0; k < G5; k++) {
-            const int o = o0 + k;
-            const int ox = o % 5 - 2, oy = (o / 5) % 5 - 2, oz = DIM == 3 ? o / 25 - 2 : 0;
-            int64_t j = e + ox + oy * sy + oz * sz;
-            j = j < 0 ? 0 : (j >= n ? n - 1 : j);
-            cv[k] = __ldg(&cc5[o * n + e]);
-            xv[k] = __ldg(&x[n + j]);
-        }
-#pragma unroll
-        for (int k = 0; k < G5; k++) a1 += cv[k] * xv[k];
+#pragma unroll 25
+    for (int o = 0; o < N5; o++) {
+        const int ox = o % 5 - 2, oy = (o / 5) % 5 - 2, oz = DIM == 3 ? o / 25 - 2 : 0;
+        int64_t j = e + ox + oy * sy + oz * sz;
+        j = j < 0 ? 0 : (j >= n ? n - 1 : j);
+        a1 += __ldg(&cc5[o * n + e]) * __ldg(&x[n + j]);
     }
     y[e] = a0;
     y[n + e] = a1;
