@@ -575,21 +575,50 @@ __global__ void __launch_bounds__(256) k_papply1_tri(uwg_lgeom g, const float* _
     y[n + e] = a1;
 }
 
-// rc = P^T rf, level 0 -> 1, smooth checkerboard component
+// rc = P^T rf, level 0 -> 1, smooth checkerboard component.  The 1D weights of
+// the four fine cells 2X-1 .. 2X+2 are formed once per axis.
 template <int DIM>
 __global__ void k_prestrict_tri(uwg_lgeom gf, uwg_lgeom gc, const float* __restrict__ rf, float* __restrict__ rc_) {
     int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (I >= gc.n_el) return;
-    int X, Y, Z;
-    cell_xyz<DIM>(gc, I, X, Y, Z);
+    int X[3];
+    cell_xyz<DIM>(gc, I, X[0], X[1], X[2]);
+    float w[3][4];
+    int lo[3], hi[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const int rf_d = d == 0 ? gf.res[0] : d == 1 ? gf.res[1] : gf.res[2];
+        const int rc_d = d == 0 ? gc.res[0] : d == 1 ? gc.res[1] : gc.res[2];
+        lo[d] = 0;
+        hi[d] = (d < DIM) ? 4 : 1;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int f = 2 * X[d] - 1 + k;
+            w[d][k] = (d < DIM && f >= 0 && f < rf_d) ? tri1w(f, rc_d, X[d]) : 0.f;
+        }
+        if (d >= DIM) w[d][0] = 1.f;
+    }
+    const int64_t sy = gf.res[0], sz = (int64_t)gf.res[0] * gf.res[1];
     float s0 = 0.f, s1 = 0.f;
-    for (int f = 0; f < (DIM == 3 ? 64 : 16); f++) {
-        const int ix = 2 * X - 1 + (f & 3), iy = 2 * Y - 1 + ((f >> 2) & 3), iz = DIM == 3 ? 2 * Z - 1 + (f >> 4) : 0;
-        if (!in_grid<DIM>(gf, ix, iy, iz)) continue;
-        const float v = rf[ix + (int64_t)gf.res[0] * (iy + (int64_t)gf.res[1] * iz)];
-        if ((ix >> 1) == X && (iy >> 1) == Y && (DIM == 2 || (iz >> 1) == Z)) s0 += v;
-        const float w = tri1w(ix, gc.res[0], X) * tri1w(iy, gc.res[1], Y) * (DIM == 3 ? tri1w(iz, gc.res[2], Z) : 1.f);
-        s1 += (((ix + iy + iz) & 1) ? -w : w) * v;
+    for (int c = lo[2]; c < hi[2]; c++) {
+        const int iz = DIM == 3 ? 2 * X[2] - 1 + c : 0;
+        if (DIM == 3 && (iz < 0 || iz >= gf.res[2])) continue;
+        for (int b = 0; b < 4; b++) {
+            const int iy = 2 * X[1] - 1 + b;
+            if (iy < 0 || iy >= gf.res[1]) continue;
+            const float wyz = w[1][b] * w[2][c];
+            const float* row = rf + iy * sy + iz * sz;
+            const bool child_yz = (b == 1 || b == 2) && (DIM == 2 || c == 1 || c == 2);
+#pragma unroll
+            for (int a = 0; a < 4; a++) {
+                const int ix = 2 * X[0] - 1 + a;
+                if (ix < 0 || ix >= gf.res[0]) continue;
+                const float v = row[ix];
+                if (child_yz && (a == 1 || a == 2)) s0 += v;
+                const float wv = w[0][a] * wyz * v;
+                s1 += ((ix + iy + iz) & 1) ? -wv : wv;
+            }
+        }
     }
     rc_[I] = s0;
     rc_[gc.n_el + I] = s1;
