@@ -665,7 +665,7 @@ int schur_apply(uwg_ctx* c, const SolveCfg& cfg, const double* p, double* q, int
 
 // Right-preconditioned flexible GMRES on the Schur complement, M^-1 = -S^^-1.
 int fgmres(uwg_ctx* c, const SolveCfg& cfg, const double* rhs, double* p, double rtol, double atol, int maxit,
-           int m, int* its, int* inner_its, int* refine) {
+           int m, int* its, int* inner_its, int* refine, bool use_p0) {
     Work* w = work_of(c);
     cudaStream_t s = c->stream;
     int64_t n = c->n_pdof;
@@ -675,15 +675,23 @@ int fgmres(uwg_ctx* c, const SolveCfg& cfg, const double* rhs, double* p, double
     if ((rc = dots<double>(c, n, 1, ab, ab, &bn))) return rc;
     bn = std::sqrt(bn);
     *its = 0;
-    vk_zero<double>(s, n, p);
-    if (bn == 0.0) return UWG_OK;
+    if (!use_p0) vk_zero<double>(s, n, p);
+    if (bn == 0.0 && !use_p0) return UWG_OK;
     double tol = rtol * bn;
     if (atol > 0.0 && atol < tol) tol = atol;
     std::vector<double> H((m + 1) * m), cs(m), sn(m), g(m + 1), y(m);
     int total = 0;
-    // r0 = rhs (p = 0)
+    // r0 = rhs - S p0 (p0 = 0 unless an initial guess is given)
     vk_copy<double>(s, n, rhs, w->V[0]);
     double beta = bn;
+    if (use_p0) {
+        if ((rc = schur_apply(c, cfg, p, w->p_tmp, inner_its, refine))) return rc;
+        vk_axpy<double>(s, n, -1.0, w->p_tmp, w->V[0]);
+        const double* a0[1] = {w->V[0]};
+        if ((rc = dots<double>(c, n, 1, a0, a0, &beta))) return rc;
+        beta = std::sqrt(beta);
+        if (beta <= tol) return UWG_OK;
+    }
     while (true) {
         vk_scale<double>(s, n, 1.0 / beta, w->V[0]);
         std::fill(g.begin(), g.end(), 0.0);
@@ -882,7 +890,7 @@ extern "C" int uwg_stokes_solve(uwg_ctx* c, const uwg_solve_opts* o, double* u, 
     }
     double atol = o->rtol > 0.0 ? 0.5 * o->rtol * std::sqrt(fh2[0] + fh2[1]) : 0.0;
     rc = fgmres(c, cfg, w->hhat, p, o->outer_rtol, atol, o->max_outer, std::max(2, o->restart), &outer, &inner_its,
-                &S.refinement_steps);
+                &S.refinement_steps, o->zero_guess == 0);
     S.pressure_its = outer;
     S.schur_pc_its = w->lsolve_its;
     S.schur_pc_time = w->t_pc;
