@@ -228,6 +228,23 @@ int uwg_interpolate(uwg_ctx* ctx, int64_t n, const double* pts, const double* ve
  * (L/PICellerator/MaterialPoints/src/SwarmAdvector.c:370-387). */
 int uwg_max_dt(uwg_ctx* ctx, const double* vel, double* dt_h);
 
+/* ---- SUPG advection-diffusion of a nodal scalar (Q1 meshes) ----------------
+ * One time step of the explicit predictor-multicorrector with SUPG residual and
+ * lumped mass.  Replaces _AdvectionDiffusionSLE_Execute for the SUPG method
+ * (P/systems/_advectiondiffusion.py:995-1007 -> L/Underworld/Utils/AdvectionDiffusion/
+ * src/Multicorrector.c:166-300, Residual.cpp:213-341, LumpedMassMatrixForceTerm.c:139-172).
+ *   vel       [n_nodes*dim] nodal velocity, or NULL for pure diffusion
+ *   kappa_q   [n_el*3^dim] diffusivity at the 3-point Gauss points of each element
+ *   source_q  same layout, or NULL
+ *   bc        [n_nodes] 1 = Dirichlet node, with phi = bcval and phi-dot = bcdot (NULL: 0)
+ *   phi, phidot [n_nodes] advanced in place; iterations (2) and gamma (0.5) as the reference */
+int uwg_advdiff_step(uwg_ctx* ctx, double dt, const double* vel, const double* kappa_q, const double* source_q,
+                     const uint8_t* bc, const double* bcval, const double* bcdot, double* phi, double* phidot,
+                     int iterations, double gamma);
+/* Time-step bound of AdvectionDiffusionSLE_CalculateDt (Timestep.c:31-117): courant *
+ * min(advective, diffusive); the reference's SUPG system uses courant = 0.5. */
+int uwg_advdiff_max_dt(uwg_ctx* ctx, const double* vel, const double* kappa_q, double courant, double* dt_h);
+
 #ifdef __cplusplus
 }
 #endif

@@ -176,6 +176,33 @@ class Context:
         self._call("uwg_max_dt", _ptr(vel), ctypes.byref(dt))
         return dt.value
 
+    # -- SUPG advection-diffusion --------------------------------------------
+    def gauss_coords(self):
+        """Global coordinates of the 3^dim Gauss points of every element,
+        [n_el * 3^dim, dim] on the device (x-fastest points, element order)."""
+        x = np.sqrt(0.6)
+        g1 = np.array([-x, 0.0, x])
+        pts = np.stack(np.meshgrid(*([g1] * self.dim), indexing="ij"), axis=-1).reshape(-1, self.dim)
+        pts = pts[:, ::-1] if self.dim > 1 else pts                    # x fastest
+        ex = np.indices(self.res[::-1]).reshape(self.dim, -1)[::-1].T   # element index grid, x fastest
+        out = np.zeros((self.n_el, len(pts), self.dim))
+        for d in range(self.dim):
+            a = self.axes[d]
+            lo, hi = a[ex[:, d]], a[ex[:, d] + 1]
+            out[:, :, d] = lo[:, None] + 0.5 * (pts[None, :, d] + 1.0) * (hi - lo)[:, None]
+        return torch.from_numpy(out.reshape(-1, self.dim)).to(self.device)
+
+    def advdiff_step(self, dt, vel, kappa_q, phi, phidot, bc, bcval, bcdot=None, source_q=None, iterations=2,
+                     gamma=0.5):
+        bc = bc.to(self.device, torch.uint8).contiguous()
+        self._call("uwg_advdiff_step", float(dt), _ptr(vel), _ptr(kappa_q), _ptr(source_q), _ptr(bc), _ptr(bcval),
+                   _ptr(bcdot), _ptr(phi), _ptr(phidot), int(iterations), float(gamma))
+
+    def advdiff_max_dt(self, vel, kappa_q, courant=0.5):
+        dt = ctypes.c_double(0.0)
+        self._call("uwg_advdiff_max_dt", _ptr(vel), _ptr(kappa_q), float(courant), ctypes.byref(dt))
+        return dt.value
+
 
 def rng_seed(seed):
     """Park-Miller state after Swarm_Random_Seed (L/StgDomain/Swarm/src/Random.c:37-40)."""

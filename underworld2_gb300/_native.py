@@ -87,6 +87,8 @@ SIGNATURES = {
     "uwg_rk2_advect": (_I, [_CTX, _I64, _D, _P, _P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
     "uwg_interpolate": (_I, [_CTX, _I64, _P, _P, _P]),
     "uwg_max_dt": (_I, [_CTX, _P, ctypes.POINTER(_D)]),
+    "uwg_advdiff_step": (_I, [_CTX, _D, _P, _P, _P, _P, _P, _P, _P, _P, _I, _D]),
+    "uwg_advdiff_max_dt": (_I, [_CTX, _P, _P, _D, ctypes.POINTER(_D)]),
 }
 
 

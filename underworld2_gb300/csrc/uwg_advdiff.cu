@@ -1,0 +1,248 @@
+// SUPG advection-diffusion of a nodal scalar on the Q1 velocity mesh: the
+// explicit predictor-multicorrector of the reference's AdvDiffMulticorrector
+// (L/Underworld/Utils/AdvectionDiffusion/src/Multicorrector.c:166-300) with the
+// residual of AdvDiffResidualForceTerm (Residual.cpp:213-341), the upwind
+// diffusivity of Brooks & Hughes 1982 (Residual.cpp:416-506, "Exact" xi,
+// :557-568), the lumped mass of LumpedMassMatrixForceTerm.c:139-172 and the
+// time-step bound of Timestep.c:31-117.  Integration is the default Gauss
+// swarm: 3 points per axis.
+//
+// One thread per element assembles its residual and scatters it with FP64
+// atomics; the vector updates are element-free.  Dirichlet nodes are left out
+// of every update (the reference removes them from its equation numbering).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "uwg_geom.cuh"
+#include "uwg_ops.cuh"
+
+namespace {
+
+inline unsigned nblk(int64_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
+
+#define SUPG_MIN_DIFFUSIVITY 1.0e-20
+#define SUPG_ISQRT15 0.25819888974716112567
+
+// Gauss-Legendre 3-point rule on [-1, 1]
+__constant__ double c_gx[3] = {-0.7745966692414834, 0.0, 0.7745966692414834};
+__constant__ double c_gw[3] = {0.5555555555555556, 0.8888888888888888, 0.5555555555555556};
+
+// xi(alpha) = coth(alpha) - 1/alpha with the reference's asymptotic branches
+__device__ __forceinline__ double upwind_xi_exact(double pe) {
+    if (fabs(pe) < 1.0e-8) return 0.33333333333333 * pe;
+    if (pe < -20.0) return -1.0 - 1.0 / pe;
+    if (pe > 20.0) return +1.0 - 1.0 / pe;
+    return cosh(pe) / sinh(pe) - 1.0 / pe;
+}
+
+template <int DIM>
+__device__ __forceinline__ void elem_nodes(const uwg_lgeom& g, int64_t e, int* ex, int64_t* nodes, double* h) {
+    ex[0] = (int)(e % g.res[0]);
+    ex[1] = (int)((e / g.res[0]) % g.res[1]);
+    ex[2] = DIM == 3 ? (int)(e / ((int64_t)g.res[0] * g.res[1])) : 0;
+    for (int d = 0; d < DIM; d++) h[d] = g.ax[d][ex[d] + 1] - g.ax[d][ex[d]];
+    for (int n = 0; n < (1 << DIM); n++) {
+        const int i = n & 1, j = (n >> 1) & 1, k = (n >> 2) & 1;
+        nodes[n] = (ex[0] + i) + (int64_t)g.nx[0] * ((ex[1] + j) + (int64_t)g.nx[1] * (DIM == 3 ? ex[2] + k : 0));
+    }
+}
+
+template <int DIM>
+__global__ void k_supg_residual(uwg_lgeom g, const double* __restrict__ vel, const double* __restrict__ phi,
+                                const double* __restrict__ phidot, const double* __restrict__ kappa_q,
+                                const double* __restrict__ source_q, const uint8_t* __restrict__ bc, int pure_diffusion,
+                                double* R, double* Mlump) {
+    constexpr int NEN = 1 << DIM, NQ = DIM == 3 ? 27 : 9;
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= g.n_el) return;
+    int ex[3];
+    int64_t nodes[NEN];
+    double h[3] = {1.0, 1.0, 1.0};
+    elem_nodes<DIM>(g, e, ex, nodes, h);
+    double v[NEN][3], ph[NEN], pd[NEN];
+    for (int n = 0; n < NEN; n++) {
+        for (int d = 0; d < DIM; d++) v[n][d] = vel ? vel[nodes[n] * DIM + d] : 0.0;
+        ph[n] = phi[nodes[n]];
+        pd[n] = phidot[nodes[n]];
+    }
+    // upwind diffusivity from the element-average diffusivity and the centre velocity
+    double kavg = 0.0;
+    for (int q = 0; q < NQ; q++) kavg += kappa_q[e * NQ + q];
+    kavg /= (double)NQ;
+    if (kavg < SUPG_MIN_DIFFUSIVITY) kavg = SUPG_MIN_DIFFUSIVITY;
+    double xi0[3] = {0.0, 0.0, 0.0}, N0[NEN];
+    Shape<DIM, 1>::N(xi0, N0);
+    double vc[3] = {0.0, 0.0, 0.0};
+    for (int d = 0; d < DIM; d++) {
+        double s = 0.0;
+        for (int n = 0; n < NEN; n++) s += N0[n] * v[n][d];
+        vc[d] = s;
+    }
+    double upwind = 0.0;
+    for (int d = 0; d < DIM; d++) {
+        const double L = fabs(h[d]);
+        const double pe = vc[d] * L / (2.0 * kavg);
+        upwind += upwind_xi_exact(pe) * vc[d] * L;
+    }
+    upwind *= SUPG_ISQRT15;
+    const double detJ = DIM == 3 ? (0.5 * h[0]) * (0.5 * h[1]) * (0.5 * h[2]) : (0.5 * h[0]) * (0.5 * h[1]);
+    double Re[NEN], Me[NEN];
+    for (int n = 0; n < NEN; n++) { Re[n] = 0.0; Me[n] = 0.0; }
+    for (int q = 0; q < NQ; q++) {
+        const int qi = q % 3, qj = (q / 3) % 3, qk = q / 9;
+        const double xi[3] = {c_gx[qi], c_gx[qj], DIM == 3 ? c_gx[qk] : 0.0};
+        const double w = c_gw[qi] * c_gw[qj] * (DIM == 3 ? c_gw[qk] : 1.0);
+        double N[NEN], dN[3][NEN], GNx[3][NEN];
+        Shape<DIM, 1>::N(xi, N);
+        Shape<DIM, 1>::dN(xi, dN);
+        for (int d = 0; d < DIM; d++)
+            for (int n = 0; n < NEN; n++) GNx[d][n] = dN[d][n] * (2.0 / h[d]);
+        double vq[3] = {0.0, 0.0, 0.0};
+        for (int d = 0; d < DIM; d++)
+            for (int n = 0; n < NEN; n++) vq[d] += N[n] * v[n][d];
+        double udotu = 0.0;
+        for (int d = 0; d < DIM; d++) udotu += vq[d] * vq[d];
+        const double supgfactor = upwind / udotu;
+        // (local nodes are x-fastest, the numbering of Shape<DIM, 1>)
+        double pdq = 0.0, grad[3] = {0.0, 0.0, 0.0};
+        for (int n = 0; n < NEN; n++) {
+            pdq += N[n] * pd[n];
+            for (int d = 0; d < DIM; d++) grad[d] += GNx[d][n] * ph[n];
+        }
+        double total = pdq;
+        for (int d = 0; d < DIM; d++) total += vq[d] * grad[d];
+        const double kq = kappa_q[e * NQ + q];
+        if (source_q) total -= source_q[e * NQ + q];
+        const double factor = w * detJ;
+        double sumN = 0.0;
+        for (int n = 0; n < NEN; n++) sumN += N[n];
+        for (int n = 0; n < NEN; n++) {
+            double supgN = N[n];
+            if (!(fabs(upwind) < SUPG_MIN_DIFFUSIVITY)) {
+                double pert = 0.0;
+                for (int d = 0; d < DIM; d++) pert += vq[d] * GNx[d][n];
+                supgN = N[n] + supgfactor * pert;
+            }
+            double diff = 0.0;
+            for (int d = 0; d < DIM; d++) diff += GNx[d][n] * grad[d];
+            diff *= kq;
+            Re[n] -= pure_diffusion ? factor * diff : factor * (supgN * total + diff);
+            Me[n] += N[n] * sumN * factor;
+        }
+    }
+    for (int n = 0; n < NEN; n++) {
+        if (bc[nodes[n]]) continue;
+        atomicAdd(&R[nodes[n]], Re[n]);
+        if (Mlump) atomicAdd(&Mlump[nodes[n]], Me[n]);
+    }
+}
+
+__global__ void k_supg_predict(int64_t n, const uint8_t* bc, const double* bcval, const double* bcdot, double f,
+                               double* phi, double* phidot) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (bc[i]) {
+        phi[i] = bcval[i];
+        phidot[i] = bcdot ? bcdot[i] : 0.0;
+        return;
+    }
+    phi[i] += f * phidot[i];
+    phidot[i] = 0.0;
+}
+
+__global__ void k_supg_correct(int64_t n, const uint8_t* bc, const double* R, const double* M, double f, double* phi,
+                               double* phidot) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n || bc[i]) return;
+    const double d = R[i] / M[i];
+    phi[i] += f * d;
+    phidot[i] += d;
+}
+
+// time-step bounds: per node min_d |minsep_d / v_d| (advective) and, per Gauss
+// point, the diffusivity maximum; both reduced through the bit patterns of
+// non-negative doubles
+__global__ void k_supg_dt(int64_t n_nodes, int dim, const double* vel, double s0, double s1, double s2,
+                          int64_t nk, const double* kappa_q, unsigned long long* out) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n_nodes && vel) {
+        double t = HUGE_VAL;
+        const double sep[3] = {s0, s1, s2};
+        for (int d = 0; d < dim; d++) {
+            const double vd = vel[i * dim + d];
+            if (vd == 0.0) continue;
+            t = fmin(t, fabs(sep[d] / vd));
+        }
+        if (t < HUGE_VAL) atomicMin(&out[0], (unsigned long long)__double_as_longlong(t));
+    }
+    if (i < nk) atomicMax(&out[1], (unsigned long long)__double_as_longlong(fmax(kappa_q[i], 0.0)));
+}
+
+}  // namespace
+
+// Courant-limited time step of the reference's AdvectionDiffusionSLE_CalculateDt
+// (Timestep.c:31-117): courant * min(min_nodes,d |minsep_d / v_d|, minsep^2 / max kappa).
+extern "C" int uwg_advdiff_max_dt(uwg_ctx* c, const double* vel, const double* kappa_q, double courant,
+                                  double* dt_out) {
+    if (!c || !kappa_q || !dt_out) return uwg_set_error(c, UWG_ERR_ARG, "uwg_advdiff_max_dt: bad argument");
+    double sep[3] = {HUGE_VAL, HUGE_VAL, HUGE_VAL};
+    for (int d = 0; d < c->dim; d++) {
+        std::vector<double> ax(c->res[d] + 1);
+        UWG_CUDA(c, cudaMemcpy(ax.data(), c->ax[d], sizeof(double) * ax.size(), cudaMemcpyDeviceToHost));
+        for (size_t k = 0; k + 1 < ax.size(); k++) sep[d] = std::min(sep[d], std::fabs(ax[k + 1] - ax[k]));
+    }
+    double minsep = std::min(sep[0], std::min(sep[1], sep[2]));
+    unsigned long long* out = (unsigned long long*)c->red;
+    unsigned long long init[2] = {(unsigned long long)0x7FF0000000000000ull, 0ull};   // +inf, 0
+    UWG_CUDA(c, cudaMemcpyAsync(out, init, sizeof(init), cudaMemcpyHostToDevice, c->stream));
+    const int64_t nk = c->n_el * (c->dim == 3 ? 27 : 9);
+    const int64_t nt = std::max<int64_t>(c->n_nodes, nk);
+    k_supg_dt<<<nblk(nt), 256, 0, c->stream>>>(c->n_nodes, c->dim, vel, sep[0], sep[1], sep[2], nk, kappa_q, out);
+    unsigned long long h[2];
+    UWG_CUDA(c, cudaGetLastError());
+    UWG_CUDA(c, cudaMemcpyAsync(h, out, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    UWG_CUDA(c, cudaStreamSynchronize(c->stream));
+    double adv, kmax;
+    std::memcpy(&adv, &h[0], 8);
+    std::memcpy(&kmax, &h[1], 8);
+    const double diff = kmax > 0.0 ? minsep * minsep / kmax : HUGE_VAL;
+    *dt_out = courant * std::min(vel ? adv : HUGE_VAL, diff);
+    return UWG_OK;
+}
+
+// One time step of SUPG advection-diffusion (see the file header).
+//   vel      [n_nodes*dim] nodal velocity (NULL: pure diffusion)
+//   kappa_q  [n_el*3^dim] diffusivity at the Gauss points; source_q likewise or NULL
+//   bc       [n_nodes] 1 = Dirichlet node; bcval, bcdot its phi and phi-dot values
+extern "C" int uwg_advdiff_step(uwg_ctx* c, double dt, const double* vel, const double* kappa_q,
+                                const double* source_q, const uint8_t* bc, const double* bcval, const double* bcdot,
+                                double* phi, double* phidot, int iterations, double gamma) {
+    if (!c || !kappa_q || !bc || !bcval || !phi || !phidot || iterations < 0 || !(dt >= 0.0))
+        return uwg_set_error(c, UWG_ERR_ARG, "uwg_advdiff_step: bad argument");
+    if (c->order != 1) return uwg_set_error(c, UWG_ERR_ARG, "advection-diffusion is provided on Q1 meshes");
+    const int64_t n = c->n_nodes;
+    uwg_lgeom g = uwg_level_geom(c, 0);
+    double *R = nullptr, *M = nullptr;
+    UWG_CUDA(c, cudaMallocAsync((void**)&R, sizeof(double) * n, c->stream));
+    UWG_CUDA(c, cudaMallocAsync((void**)&M, sizeof(double) * n, c->stream));
+    k_supg_predict<<<nblk(n), 256, 0, c->stream>>>(n, bc, bcval, bcdot, dt * (1.0 - gamma), phi, phidot);
+    cudaError_t err = cudaGetLastError();
+    for (int it = 0; it < iterations && err == cudaSuccess; it++) {
+        cudaMemsetAsync(R, 0, sizeof(double) * n, c->stream);
+        if (it == 0) cudaMemsetAsync(M, 0, sizeof(double) * n, c->stream);
+        if (c->dim == 3)
+            k_supg_residual<3><<<nblk(c->n_el, 128), 128, 0, c->stream>>>(g, vel, phi, phidot, kappa_q, source_q, bc,
+                                                                          vel ? 0 : 1, R, it == 0 ? M : nullptr);
+        else
+            k_supg_residual<2><<<nblk(c->n_el, 128), 128, 0, c->stream>>>(g, vel, phi, phidot, kappa_q, source_q, bc,
+                                                                          vel ? 0 : 1, R, it == 0 ? M : nullptr);
+        k_supg_correct<<<nblk(n), 256, 0, c->stream>>>(n, bc, R, M, dt * gamma, phi, phidot);
+        err = cudaGetLastError();
+    }
+    cudaFreeAsync(R, c->stream);
+    cudaFreeAsync(M, c->stream);
+    if (err != cudaSuccess) return uwg_set_error(c, UWG_ERR_CUDA, cudaGetErrorString(err));
+    return UWG_OK;
+}

@@ -367,6 +367,89 @@ def Solver(eqs, type="BSSCR", *args, **kwargs):
     raise ValueError("the GPU path provides the Stokes solver only")
 
 
+def _uses_swarm(f):
+    if isinstance(f, _fn._SwarmVar):
+        return True
+    return any(_uses_swarm(c) for c in f._children())
+
+
+class AdvectionDiffusion:
+    """SUPG advection-diffusion of a scalar mesh variable (P/systems/_advectiondiffusion.py:16-150,
+    method "SUPG": :838-1020) on Q1 meshes, integrated with the reference's default
+    Gauss swarm (3 points per axis).  ``integrate(dt)`` advances ``phiField`` and
+    ``phiDotField`` by the explicit predictor-multicorrector; ``get_max_dt()`` is the
+    reference's Courant bound (courant factor 0.5)."""
+
+    def __init__(self, phiField, velocityField, fn_diffusivity, fn_sourceTerm=None, method="SUPG",
+                 phiDotField=None, conditions=[], gauss_swarm=None, **kwargs):
+        if method.upper() != "SUPG":
+            raise NotImplementedError("the GPU path provides the SUPG method")
+        if not isinstance(phiField, _mesh.MeshVariable) or phiField.nodeDofCount != 1:
+            raise TypeError("Provided 'phiField' must be a scalar 'MeshVariable'.")
+        if not isinstance(phiField.mesh, _mesh.FeMesh_Cartesian) or phiField.mesh._order != 1:
+            raise ValueError("'phiField' must live on a Q1 mesh")
+        if velocityField is not None and not isinstance(velocityField, _mesh.MeshVariable):
+            raise TypeError("Provided 'velocityField' must be of 'MeshVariable' class.")
+        if phiDotField is None:
+            phiDotField = phiField.mesh.add_variable(nodeDofCount=1)
+        if not isinstance(phiDotField, _mesh.MeshVariable) or phiDotField.data.shape != phiField.data.shape:
+            raise TypeError("Provided 'phiDotField' is not the same shape as the provided 'phiField'")
+        if not isinstance(conditions, (list, tuple)):
+            conditions = [conditions]
+        for c in conditions:
+            if not isinstance(c, _cond.DirichletCondition) or c.variable is not phiField:
+                raise ValueError("only Dirichlet conditions on 'phiField' are supported")
+        self._phi, self._phidot, self._vel = phiField, phiDotField, velocityField
+        self.mesh = phiField.mesh
+        self._conditions = list(conditions)
+        self.fn_diffusivity = _fn.Function.convert(fn_diffusivity)
+        self.fn_sourceTerm = _fn.Function.convert(fn_sourceTerm) if fn_sourceTerm is not None else None
+        for f in (self.fn_diffusivity, self.fn_sourceTerm):
+            if f is not None and _uses_swarm(f):
+                raise ValueError("Gauss-point integration cannot evaluate swarm variables")
+
+    @property
+    def phiField(self):
+        return self._phi
+
+    @property
+    def velocityField(self):
+        return self._vel
+
+    def _at_gauss(self, f):
+        ctx = self.mesh.ctx
+        coords = ctx.gauss_coords()
+        ectx = _fn.EvalContext(torch.full((coords.shape[0],), -1, dtype=torch.int64, device=ctx.device),
+                               lambda: coords, ctx.device)
+        return f.evaluate_at(ectx)[:, 0].contiguous()
+
+    def _bc(self):
+        m = np.zeros(self._phi.data.shape[0], np.uint8)
+        for c in self._conditions:
+            m |= c.mask()[:, 0]
+        return m
+
+    def integrate(self, dt, **kwargs):
+        ctx = self.mesh.ctx
+        kappa = self._at_gauss(self.fn_diffusivity)
+        src = self._at_gauss(self.fn_sourceTerm) if self.fn_sourceTerm is not None else None
+        mask = self._bc()
+        phi = self._phi._to_device().contiguous()
+        phidot = self._phidot._to_device().contiguous()
+        bcval = phi.clone()
+        bcdot = phidot.clone()
+        vel = self._vel._to_device() if self._vel is not None else None
+        ctx.advdiff_step(dt, vel, kappa, phi, phidot, torch.from_numpy(mask), bcval, bcdot, source_q=src)
+        self._phi._from_device()
+        self._phidot._from_device()
+
+    def get_max_dt(self):
+        ctx = self.mesh.ctx
+        kappa = self._at_gauss(self.fn_diffusivity)
+        vel = self._vel._to_device() if self._vel is not None else None
+        return ctx.advdiff_max_dt(vel, kappa, 0.5)
+
+
 class SwarmAdvector:
     """Midpoint-RK2 particle advection with owner update (P/systems/_timeintegration.py:77-157)."""
 
