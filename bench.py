@@ -383,6 +383,52 @@ def run_kernel(args):
                       "ms_per_launch": s.elapsed_time(e) / args.reps}))
 
 
+def run_advdiff(args):
+    """SUPG advection-diffusion of T on the workload's Q1 mesh: a cellular
+    velocity field, diffusivity 1 at the Gauss points, T fixed on the top and
+    bottom walls, `--reps` steps at the Courant time step after 3 untimed.
+    Algorithmic bytes per step: the predictor reads phi, phidot, bc (+ writes
+    phi, phidot); each of the two corrector passes reads phi, phidot, the
+    velocity and the 3^d Gauss-point diffusivities and writes R (+ M once),
+    then reads R, M, bc, phi, phidot and writes phi, phidot."""
+    import torch
+    from underworld2_gb300._core import Context
+    cfg = CONFIGS[args.config]
+    dim = cfg["dim"]
+    ctx = Context(dim, cfg["res"], (0.0,) * dim, (1.0,) * dim)
+    xyz = torch.stack(torch.meshgrid(*[torch.tensor(a, device=ctx.device) for a in reversed(ctx.axes)],
+                                     indexing="ij")[::-1], dim=-1).reshape(-1, dim)
+    s, c = torch.sin(torch.pi * xyz), torch.cos(torch.pi * xyz)
+    vel = torch.zeros_like(xyz)
+    vel[:, 0] = s[:, 0] * c[:, dim - 1]
+    vel[:, dim - 1] = -c[:, 0] * s[:, dim - 1]
+    vel = (1e3 * vel).contiguous().reshape(-1)
+    nq = 3 ** dim
+    kappa = torch.ones(ctx.n_el * nq, dtype=torch.float64, device=ctx.device)
+    top, bot = xyz[:, dim - 1] == 1.0, xyz[:, dim - 1] == 0.0
+    bc = (top | bot).to(torch.uint8)
+    phi = (1.0 - xyz[:, dim - 1]).contiguous()
+    phidot = torch.zeros_like(phi)
+    bcval = phi.clone()
+    dt = ctx.advdiff_max_dt(vel, kappa)
+    for _ in range(3):
+        ctx.advdiff_step(dt, vel, kappa, phi, phidot, bc, bcval)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(args.reps):
+        ctx.advdiff_step(dt, vel, kappa, phi, phidot, bc, bcval)
+    ev1.record()
+    torch.cuda.synchronize()
+    sec = ev0.elapsed_time(ev1) / 1e3 / args.reps
+    n, ne = ctx.n_nodes, ctx.n_el
+    byts = (8 * 4 * n + n) + 2 * (8 * (2 + dim) * n + 8 * nq * ne + 8 * n) + 8 * n + 2 * (8 * 6 * n + n)
+    print(json.dumps({"kernel": "advdiff", "config": args.config, "res": list(ctx.res), "reps": args.reps, "dt": dt,
+                      "ms_per_step": sec * 1e3, "algorithmic_bytes_per_step": byts,
+                      "GBps": byts / sec / 1e9, "T_finite": bool(torch.isfinite(phi).all()),
+                      "T_range": [float(phi.min()), float(phi.max())]}))
+
+
 def run_profile_solve(args):
     """One map + DVC + assembly + solve of the workload, untimed (the target of
     the launch-list captures recorded under profiles/); `--kernel-ppc` lowers
@@ -482,7 +528,8 @@ def main():
     ap.add_argument("--outer-rtol", type=float, default=1e-9)
     ap.add_argument("--schur-pc", type=int, default=1, help="0: Uzawa S^ (reference), 1: scaled BFBt")
     ap.add_argument("--bfbt-rtol", type=float, default=3e-2)
-    ap.add_argument("--kernel", choices=["applyK32", "applyK64"], help="only launch one operator kernel (profiling)")
+    ap.add_argument("--kernel", choices=["applyK32", "applyK64", "advdiff"],
+                    help="only launch one operator kernel, or time SUPG advection-diffusion steps (profiling)")
     ap.add_argument("--kernel-ppc", type=int, default=0)
     ap.add_argument("--profile-solve", action="store_true", help="one untimed solve (profiling target)")
     ap.add_argument("--reps", type=int, default=5)
@@ -491,6 +538,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-count-launches", dest="count_launches", action="store_false")
     args = ap.parse_args()
+    if args.kernel == "advdiff":
+        run_advdiff(args)
+        return
     if args.kernel:
         run_kernel(args)
         return

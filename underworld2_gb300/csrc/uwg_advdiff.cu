@@ -7,8 +7,9 @@
 // time-step bound of Timestep.c:31-117.  Integration is the default Gauss
 // swarm: 3 points per axis.
 //
-// One thread per element assembles its residual and scatters it with FP64
-// atomics; the vector updates are element-free.  Dirichlet nodes are left out
+// One thread per element assembles its residual (sum-factorised over the
+// tensor Gauss points) and scatters it with FP64 atomics; the vector updates
+// are element-free.  Dirichlet nodes are left out
 // of every update (the reference removes them from its equation numbering).
 #include <algorithm>
 #include <cmath>
@@ -49,93 +50,185 @@ __device__ __forceinline__ void elem_nodes(const uwg_lgeom& g, int64_t e, int* e
     }
 }
 
+// Residual of one element, sum-factorised over the 3^DIM tensor Gauss points.
+// On an axis-aligned box the Q1 shape functions are products of the 1D
+// N0 = (1 - g)/2, N1 = (1 + g)/2, and their global derivatives are
+// +-1/h_d times the other axes' 1D factors.  So the nodal fields are
+// interpolated to the points axis by axis (z plane, y line, x point), and the
+// per-point terms
+//   s_q = -w_q detJ total_q,
+//   w_q = -w_q detJ ((upwind total_q / |v_q|^2) v_q + kappa_q grad phi_q)
+// are projected back by the transposed contraction:
+//   R_n = sum_q s_q N_n(q) + w_q . grad N_n(q)
+// which is the reference's sum_q -factor (supgN_n total + kappa GNx_n . grad)
+// regrouped.  The lumped mass sum_q N_n(q) sum_m N_m(q) w_q detJ equals detJ
+// exactly (partition of unity; sum_g w_g N(g) = 1 on each axis).  The FP64
+// pipe bounds this kernel, so the regrouping is what sets its speed.
 template <int DIM>
-__global__ void k_supg_residual(uwg_lgeom g, const double* __restrict__ vel, const double* __restrict__ phi,
-                                const double* __restrict__ phidot, const double* __restrict__ kappa_q,
-                                const double* __restrict__ source_q, const uint8_t* __restrict__ bc, int pure_diffusion,
-                                double* R, double* Mlump) {
-    constexpr int NEN = 1 << DIM, NQ = DIM == 3 ? 27 : 9;
+__global__ void __launch_bounds__(128) k_supg_residual(uwg_lgeom g, const double* __restrict__ vel,
+                                                       const double* __restrict__ phi,
+                                                       const double* __restrict__ phidot,
+                                                       const double* __restrict__ kappa_q,
+                                                       const double* __restrict__ source_q,
+                                                       const uint8_t* __restrict__ bc, int pure_diffusion, double* R,
+                                                       double* Mlump) {
+    constexpr int NEN = 1 << DIM, NQ = DIM == 3 ? 27 : 9, NZ = DIM == 3 ? 3 : 1;
     int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (e >= g.n_el) return;
     int ex[3];
     int64_t nodes[NEN];
     double h[3] = {1.0, 1.0, 1.0};
     elem_nodes<DIM>(g, e, ex, nodes, h);
-    double v[NEN][3], ph[NEN], pd[NEN];
+    double v[NEN][DIM], ph[NEN], pd[NEN];
+#pragma unroll
     for (int n = 0; n < NEN; n++) {
+#pragma unroll
         for (int d = 0; d < DIM; d++) v[n][d] = vel ? vel[nodes[n] * DIM + d] : 0.0;
         ph[n] = phi[nodes[n]];
         pd[n] = phidot[nodes[n]];
     }
+    const double* kq = kappa_q + e * NQ;
+    const double* sq = source_q ? source_q + e * NQ : nullptr;
     // upwind diffusivity from the element-average diffusivity and the centre velocity
     double kavg = 0.0;
-    for (int q = 0; q < NQ; q++) kavg += kappa_q[e * NQ + q];
+#pragma unroll
+    for (int q = 0; q < NQ; q++) kavg += kq[q];
     kavg /= (double)NQ;
     if (kavg < SUPG_MIN_DIFFUSIVITY) kavg = SUPG_MIN_DIFFUSIVITY;
-    double xi0[3] = {0.0, 0.0, 0.0}, N0[NEN];
-    Shape<DIM, 1>::N(xi0, N0);
-    double vc[3] = {0.0, 0.0, 0.0};
-    for (int d = 0; d < DIM; d++) {
-        double s = 0.0;
-        for (int n = 0; n < NEN; n++) s += N0[n] * v[n][d];
-        vc[d] = s;
-    }
     double upwind = 0.0;
+#pragma unroll
     for (int d = 0; d < DIM; d++) {
+        double vc = 0.0;
+#pragma unroll
+        for (int n = 0; n < NEN; n++) vc += v[n][d];
+        vc *= 1.0 / NEN;
         const double L = fabs(h[d]);
-        const double pe = vc[d] * L / (2.0 * kavg);
-        upwind += upwind_xi_exact(pe) * vc[d] * L;
+        upwind += upwind_xi_exact(vc * L / (2.0 * kavg)) * vc * L;
     }
     upwind *= SUPG_ISQRT15;
+    const bool perturb = !pure_diffusion && !(fabs(upwind) < SUPG_MIN_DIFFUSIVITY);
     const double detJ = DIM == 3 ? (0.5 * h[0]) * (0.5 * h[1]) * (0.5 * h[2]) : (0.5 * h[0]) * (0.5 * h[1]);
-    double Re[NEN], Me[NEN];
-    for (int n = 0; n < NEN; n++) { Re[n] = 0.0; Me[n] = 0.0; }
-    for (int q = 0; q < NQ; q++) {
-        const int qi = q % 3, qj = (q / 3) % 3, qk = q / 9;
-        const double xi[3] = {c_gx[qi], c_gx[qj], DIM == 3 ? c_gx[qk] : 0.0};
-        const double w = c_gw[qi] * c_gw[qj] * (DIM == 3 ? c_gw[qk] : 1.0);
-        double N[NEN], dN[3][NEN], GNx[3][NEN];
-        Shape<DIM, 1>::N(xi, N);
-        Shape<DIM, 1>::dN(xi, dN);
-        for (int d = 0; d < DIM; d++)
-            for (int n = 0; n < NEN; n++) GNx[d][n] = dN[d][n] * (2.0 / h[d]);
-        double vq[3] = {0.0, 0.0, 0.0};
-        for (int d = 0; d < DIM; d++)
-            for (int n = 0; n < NEN; n++) vq[d] += N[n] * v[n][d];
-        double udotu = 0.0;
-        for (int d = 0; d < DIM; d++) udotu += vq[d] * vq[d];
-        const double supgfactor = upwind / udotu;
-        // (local nodes are x-fastest, the numbering of Shape<DIM, 1>)
-        double pdq = 0.0, grad[3] = {0.0, 0.0, 0.0};
-        for (int n = 0; n < NEN; n++) {
-            pdq += N[n] * pd[n];
-            for (int d = 0; d < DIM; d++) grad[d] += GNx[d][n] * ph[n];
-        }
-        double total = pdq;
-        for (int d = 0; d < DIM; d++) total += vq[d] * grad[d];
-        const double kq = kappa_q[e * NQ + q];
-        if (source_q) total -= source_q[e * NQ + q];
-        const double factor = w * detJ;
-        double sumN = 0.0;
-        for (int n = 0; n < NEN; n++) sumN += N[n];
-        for (int n = 0; n < NEN; n++) {
-            double supgN = N[n];
-            if (!(fabs(upwind) < SUPG_MIN_DIFFUSIVITY)) {
-                double pert = 0.0;
-                for (int d = 0; d < DIM; d++) pert += vq[d] * GNx[d][n];
-                supgN = N[n] + supgfactor * pert;
+    double ih[3];
+#pragma unroll
+    for (int d = 0; d < DIM; d++) ih[d] = 0.5 * (2.0 / h[d]);
+    double t1[3], w1[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        t1[a] = 0.5 * (1.0 + c_gx[a]);
+        w1[a] = c_gw[a];
+    }
+    // projected residual per node: D (from s and w_x, w_y), E (from w_z) per (i, j) in the plane
+    double Re[NEN];
+#pragma unroll
+    for (int n = 0; n < NEN; n++) Re[n] = 0.0;
+#pragma unroll
+    for (int qk = 0; qk < NZ; qk++) {
+        // plane values at (i, j): nodal fields interpolated in z, and d/dz phi
+        double pv[4][DIM], pph[4], ppd[4], pdz[4];
+        const double tz = t1[qk];
+#pragma unroll
+        for (int p = 0; p < 4; p++) {
+            if (DIM == 3) {
+#pragma unroll
+                for (int d = 0; d < DIM; d++) pv[p][d] = v[p][d] + (v[p + 4][d] - v[p][d]) * tz;
+                pph[p] = ph[p] + (ph[p + 4] - ph[p]) * tz;
+                ppd[p] = pd[p] + (pd[p + 4] - pd[p]) * tz;
+                pdz[p] = (ph[p + 4] - ph[p]) * ih[DIM - 1];
+            } else {
+#pragma unroll
+                for (int d = 0; d < DIM; d++) pv[p][d] = v[p][d];
+                pph[p] = ph[p];
+                ppd[p] = pd[p];
+                pdz[p] = 0.0;
             }
-            double diff = 0.0;
-            for (int d = 0; d < DIM; d++) diff += GNx[d][n] * grad[d];
-            diff *= kq;
-            Re[n] -= pure_diffusion ? factor * diff : factor * (supgN * total + diff);
-            Me[n] += N[n] * sumN * factor;
+        }
+        double D[4] = {0.0, 0.0, 0.0, 0.0}, E[4] = {0.0, 0.0, 0.0, 0.0};
+        const double wk = (DIM == 3 ? w1[qk] : 1.0) * detJ;
+#pragma unroll
+        for (int qj = 0; qj < 3; qj++) {
+            const double ty = t1[qj];
+            // line values at i = 0, 1
+            double lv[2][DIM], lpd[2], ldz[2], ldy[2], lph[2];
+#pragma unroll
+            for (int i = 0; i < 2; i++) {
+#pragma unroll
+                for (int d = 0; d < DIM; d++) lv[i][d] = pv[i][d] + (pv[i + 2][d] - pv[i][d]) * ty;
+                lph[i] = pph[i] + (pph[i + 2] - pph[i]) * ty;
+                lpd[i] = ppd[i] + (ppd[i + 2] - ppd[i]) * ty;
+                ldz[i] = pdz[i] + (pdz[i + 2] - pdz[i]) * ty;
+                ldy[i] = (pph[i + 2] - pph[i]) * ih[1];
+            }
+            const double dx = (lph[1] - lph[0]) * ih[0];
+            double dv[DIM];
+#pragma unroll
+            for (int d = 0; d < DIM; d++) dv[d] = lv[1][d] - lv[0][d];
+            const double dpd = lpd[1] - lpd[0], ddz = ldz[1] - ldz[0], ddy = ldy[1] - ldy[0];
+            const double wjk = w1[qj] * wk;
+            double s0 = 0.0, s1 = 0.0, sx = 0.0, y0 = 0.0, y1 = 0.0, z0 = 0.0, z1 = 0.0;
+#pragma unroll
+            for (int qi = 0; qi < 3; qi++) {
+                const double tx = t1[qi], ux = 1.0 - tx;
+                const int q = qi + 3 * qj + 9 * qk;
+                double vq[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+                for (int d = 0; d < DIM; d++) vq[d] = lv[0][d] + dv[d] * tx;
+                const double gy = ldy[0] + ddy * tx;
+                const double gz = DIM == 3 ? ldz[0] + ddz * tx : 0.0;
+                const double factor = w1[qi] * wjk;
+                const double fk = factor * kq[q];
+                double wx = fk * dx, wy = fk * gy, wz = fk * gz;
+                double sv = 0.0;
+                if (!pure_diffusion) {
+                    double total = lpd[0] + dpd * tx;
+                    total += vq[0] * dx + vq[1] * gy + (DIM == 3 ? vq[2] * gz : 0.0);
+                    if (sq) total -= sq[q];
+                    const double ftot = factor * total;
+                    sv = ftot;
+                    if (perturb) {
+                        const double udotu = vq[0] * vq[0] + vq[1] * vq[1] + (DIM == 3 ? vq[2] * vq[2] : 0.0);
+                        const double cs = ftot * (upwind / udotu);
+                        wx += cs * vq[0];
+                        wy += cs * vq[1];
+                        if (DIM == 3) wz += cs * vq[2];
+                    }
+                }
+                s0 += sv * ux;
+                s1 += sv * tx;
+                sx += wx;
+                y0 += wy * ux;
+                y1 += wy * tx;
+                z0 += wz * ux;
+                z1 += wz * tx;
+            }
+            // x-projected: A_i (s and w_x), B_i (w_y), C_i (w_z); then project in y
+            const double A[2] = {s0 - sx * ih[0], s1 + sx * ih[0]};
+            const double B[2] = {y0, y1}, C[2] = {z0, z1};
+            const double uy = 1.0 - ty;
+#pragma unroll
+            for (int i = 0; i < 2; i++) {
+                D[i] += A[i] * uy - B[i] * ih[1];
+                D[i + 2] += A[i] * ty + B[i] * ih[1];
+                E[i] += C[i] * uy;
+                E[i + 2] += C[i] * ty;
+            }
+        }
+        if (DIM == 3) {
+            const double uz = 1.0 - tz;
+#pragma unroll
+            for (int p = 0; p < 4; p++) {
+                Re[p] += D[p] * uz - E[p] * ih[2];
+                Re[p + 4] += D[p] * tz + E[p] * ih[2];
+            }
+        } else {
+#pragma unroll
+            for (int p = 0; p < 4; p++) Re[p] += D[p];
         }
     }
+#pragma unroll
     for (int n = 0; n < NEN; n++) {
         if (bc[nodes[n]]) continue;
-        atomicAdd(&R[nodes[n]], Re[n]);
-        if (Mlump) atomicAdd(&Mlump[nodes[n]], Me[n]);
+        atomicAdd(&R[nodes[n]], -Re[n]);
+        if (Mlump) atomicAdd(&Mlump[nodes[n]], detJ);
     }
 }
 
