@@ -245,6 +245,23 @@ int uwg_advdiff_step(uwg_ctx* ctx, double dt, const double* vel, const double* k
  * min(advective, diffusive); the reference's SUPG system uses courant = 0.5. */
 int uwg_advdiff_max_dt(uwg_ctx* ctx, const double* vel, const double* kappa_q, double courant, double* dt_h);
 
+/* ---- SLCN advection-diffusion (semi-Lagrangian Crank-Nicolson, Q1 meshes) ---
+ * Departure values phi*: every node traced back over dt along vel (classical RK4
+ * clamped to the domain) and phi interpolated there by 4^dim Lagrange cubics on
+ * the reference's static stencils.  Replaces SemiLagrangianIntegrator_SolveNew
+ * (L/StgFEM/Utils/src/SemiLagrangianIntegrator.c:600-653; called from
+ * P/systems/_advectiondiffusion.py:740-746).  Bit-exact.  Needs >= 4 nodes per axis. */
+int uwg_slcn_phistar(uwg_ctx* ctx, double dt, const double* vel, const double* phi, double* phistar);
+/* Crank-Nicolson diffusion solve (M + dt/2 D) phi = (M - dt/2 D) phi* + dt int N S with
+ * Dirichlet nodes eliminated; replaces the assembly terms of
+ * P/systems/_advectiondiffusion.py:211-259 and its SolveLinearSystem solve (:755).
+ *   kappa_q, source_q [n_el*5^dim] at the 5-point Gauss points (source_q may be NULL)
+ *   bc [n_nodes] 1 = Dirichlet node (its value is phi's current value)
+ *   phi in: current field (initial guess), out: solution; CG to rtol (relative
+ *   residual), its_out / res_out report the iterations and final residual. */
+int uwg_slcn_solve(uwg_ctx* ctx, double dt, const double* kappa_q, const double* source_q, const uint8_t* bc,
+                   const double* phistar, double* phi, double rtol, int max_its, int* its_out, double* res_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -70,6 +70,7 @@ def lib():
             "uwo_pressure_shape": (None, [ctypes.c_int, ctypes.c_int, _P, _P]),
             "uwo_interpolate": (ctypes.c_int, [M, _P, _P, _P, _P, _P, _P]),
             "uwo_rk2": (None, [M, _P, _P, _P, _P, ctypes.c_double, _I64, _I64, _P, _P]),
+            "uwo_slcn_phistar": (ctypes.c_int, [M, _P, _P, _P, _P, _P, ctypes.c_double, ctypes.c_double, _P]),
             "uwo_sys_create": (_P, [ctypes.c_int, _P, _P, _P, _P]),
             "uwo_sys_destroy": (None, [_P]),
             "uwo_sys_set_bc": (None, [_P, _P, _P]),
@@ -242,6 +243,18 @@ class Mesh:
         self.L.uwo_rk2(ctypes.byref(self._c), *self._ax(), _p(np.ascontiguousarray(vel, np.float64)),
                        float(dt), 0, len(coords), _p(coords), _p(counts))
         return coords, counts
+
+    def min_sep(self):
+        """Mesh minimum separation: the closest adjacent node pair along an axis."""
+        return min(float(np.min(np.sqrt(np.diff(a) ** 2))) for a in self.axes[: self.dim])
+
+    def slcn_phistar(self, vel, phi, dt):
+        out = np.zeros(self.n_nodes)
+        rc = self.L.uwo_slcn_phistar(ctypes.byref(self._c), *self._ax(), _p(np.ascontiguousarray(vel, np.float64)),
+                                     _p(np.ascontiguousarray(phi, np.float64)), float(dt), self.min_sep(), _p(out))
+        if rc != 0:
+            raise ValueError("semi-Lagrangian stencils need at least 4 nodes per axis")
+        return out
 
     def interpolate(self, vel, x):
         v = np.zeros(3)

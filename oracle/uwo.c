@@ -817,3 +817,106 @@ void uwo_rk2(const uwo_mesh* m, const double* ax0, const double* ax1, const doub
     counts[0] += failed;
     counts[1] += fallback;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Semi-Lagrangian departure values (SLCN advection-diffusion)               */
+/* ------------------------------------------------------------------------ */
+/* PeriodicUpdate, non-periodic: clamp one coordinate to the domain
+ * (L/StgFEM/Utils/src/SemiLagrangianIntegrator.c:382-393). */
+static void slcn_clamp(const uwo_mesh* m, double* p, int d) {
+    if (p[d] < m->minc[d]) { p[d] = m->minc[d]; return; }
+    if (p[d] > m->maxc[d]) p[d] = m->maxc[d];
+}
+
+/* InterpLagrange (SemiLagrangianIntegrator.c:357-380), one dof. */
+static double slcn_lagrange(double x, const double* c, const double* v) {
+    double r = 0.0;
+    for (int n = 0; n < 4; n++) {
+        double f = 1.0;
+        for (int o = 0; o < 4; o++) {
+            if (o == n) continue;
+            f *= (x - c[o]) / (c[n] - c[o]);
+        }
+        r += v[n] * f;
+    }
+    return r;
+}
+
+/* SemiLagrangianIntegrator_BuildStaticStencils (:534-598), one axis, serial. */
+static int slcn_stencil_start(int i, int n) {
+    int s = i > 0 ? i - 1 : i;
+    s += 3;
+    return s >= n ? s - 4 : s - 3;
+}
+
+/* SemiLagrangianIntegrator_SolveNew (:600-653) on a Q1 mesh: each node is
+ * traced back over dt with IntegrateRungeKutta (:267-302, classical RK4, the
+ * reference's INV6 = 0.166666666667, every stage clamped to the domain); if the
+ * launch point is within 1e-6 * minsep of the node the node value is kept,
+ * else BicubicInterpolatorNew (:395-505) evaluates the 4^dim Lagrange
+ * interpolant on the static stencil of the element holding the launch point.
+ * Returns -1 if an axis has fewer than 4 nodes (the reference aborts). */
+int uwo_slcn_phistar(const uwo_mesh* m, const double* ax0, const double* ax1, const double* ax2,
+                     const double* vel, const double* phi, double dt, double minsep, double* out) {
+    const double* ax[3] = {ax0, ax1, ax2};
+    int dim = m->dim;
+    int64_t nx[3] = {1, 1, 1};
+    for (int d = 0; d < dim; d++) {
+        nx[d] = uwo_nodes_per_axis(m, d);
+        if (nx[d] < 4) return -1;
+    }
+    int64_t nn = nx[0] * nx[1] * nx[2];
+    const double INV6 = 0.166666666667;
+    for (int64_t i = 0; i < nn; i++) {
+        int64_t id[3] = {i % nx[0], (i / nx[0]) % nx[1], i / (nx[0] * nx[1])};
+        double x0[3] = {0, 0, 0}, xp[3] = {0, 0, 0}, pos[3] = {0, 0, 0};
+        double k[4][3] = {{0}};
+        for (int d = 0; d < dim; d++) x0[d] = ax[d][id[d]];
+        uwo_interpolate(m, ax0, ax1, ax2, vel, x0, k[0]);
+        for (int d = 0; d < dim; d++) { xp[d] = x0[d] - 0.5 * dt * k[0][d]; slcn_clamp(m, xp, d); }
+        uwo_interpolate(m, ax0, ax1, ax2, vel, xp, k[1]);
+        for (int d = 0; d < dim; d++) { xp[d] = x0[d] - 0.5 * dt * k[1][d]; slcn_clamp(m, xp, d); }
+        uwo_interpolate(m, ax0, ax1, ax2, vel, xp, k[2]);
+        for (int d = 0; d < dim; d++) { xp[d] = x0[d] - dt * k[2][d]; slcn_clamp(m, xp, d); }
+        uwo_interpolate(m, ax0, ax1, ax2, vel, xp, k[3]);
+        for (int d = 0; d < dim; d++) {
+            pos[d] = x0[d] - INV6 * dt * (k[0][d] + 2.0 * k[1][d] + 2.0 * k[2][d] + k[3][d]);
+            slcn_clamp(m, pos, d);
+        }
+        /* SemiLagrangianIntegrator_PointsAreClose(pos, x0, dim, 0, 1e-6 minsep) (:507-532) */
+        double disp[3] = {0, 0, 0}, dot = 0.0;
+        for (int d = 0; d < dim; d++) disp[d] = pos[d] - x0[d];
+        for (int d = dim - 1; d >= 0; d--) dot = dot + disp[d] * disp[d];
+        int64_t el;
+        if (sqrt(dot) < 1e-6 * minsep || !uwo_search_element(m, pos, &el)) {
+            out[i] = phi[i];
+            continue;
+        }
+        int64_t e[3] = {el % m->res[0], (el / m->res[0]) % m->res[1], el / ((int64_t)m->res[0] * m->res[1])};
+        int64_t s[3] = {0, 0, 0};
+        double c[3][4];
+        for (int d = 0; d < dim; d++) {
+            s[d] = slcn_stencil_start((int)e[d], (int)nx[d]);
+            for (int a = 0; a < 4; a++) c[d][a] = ax[d][s[d] + a];
+        }
+        double ptsX[4], ptsY[4], ptsZ[4];
+        if (dim == 2) {
+            for (int yi = 0; yi < 4; yi++) {
+                for (int xi = 0; xi < 4; xi++) ptsX[xi] = phi[(s[0] + xi) + (s[1] + yi) * nx[0]];
+                ptsY[yi] = slcn_lagrange(pos[0], c[0], ptsX);
+            }
+            out[i] = slcn_lagrange(pos[1], c[1], ptsY);
+        } else {
+            for (int zi = 0; zi < 4; zi++) {
+                for (int yi = 0; yi < 4; yi++) {
+                    for (int xi = 0; xi < 4; xi++)
+                        ptsX[xi] = phi[(s[0] + xi) + (s[1] + yi) * nx[0] + (s[2] + zi) * nx[0] * nx[1]];
+                    ptsY[yi] = slcn_lagrange(pos[0], c[0], ptsX);
+                }
+                ptsZ[zi] = slcn_lagrange(pos[1], c[1], ptsY);
+            }
+            out[i] = slcn_lagrange(pos[2], c[2], ptsZ);
+        }
+    }
+    return 0;
+}

@@ -57,6 +57,8 @@ class Context:
             buf = np.zeros(self.res[a] * order + 1)
             self.L.uwg_mesh_axis(self.h, a, ctypes.c_void_p(buf.ctypes.data))
             self.axes.append(buf)
+        # minimum node separation (as the library computes it: closest adjacent pair on an axis)
+        self.min_sep = min(float(np.min(np.sqrt(np.diff(a) ** 2))) for a in self.axes)
 
     def __del__(self):
         try:
@@ -177,11 +179,11 @@ class Context:
         return dt.value
 
     # -- SUPG advection-diffusion --------------------------------------------
-    def gauss_coords(self):
-        """Global coordinates of the 3^dim Gauss points of every element,
-        [n_el * 3^dim, dim] on the device (x-fastest points, element order)."""
-        x = np.sqrt(0.6)
-        g1 = np.array([-x, 0.0, x])
+    def gauss_coords(self, n=3):
+        """Global coordinates of the n^dim Gauss points (n = 3 or 5) of every
+        element, [n_el * n^dim, dim] on the device (x-fastest points, element
+        order, ascending abscissae)."""
+        g1 = gauss_abscissae(n)
         pts = np.stack(np.meshgrid(*([g1] * self.dim), indexing="ij"), axis=-1).reshape(-1, self.dim)
         pts = pts[:, ::-1] if self.dim > 1 else pts                    # x fastest
         ex = np.indices(self.res[::-1]).reshape(self.dim, -1)[::-1].T   # element index grid, x fastest
@@ -202,6 +204,32 @@ class Context:
         dt = ctypes.c_double(0.0)
         self._call("uwg_advdiff_max_dt", _ptr(vel), _ptr(kappa_q), float(courant), ctypes.byref(dt))
         return dt.value
+
+    # -- SLCN advection-diffusion --------------------------------------------
+    def slcn_phistar(self, dt, vel, phi):
+        out = torch.empty_like(phi)
+        self._call("uwg_slcn_phistar", float(dt), _ptr(vel), _ptr(phi), _ptr(out))
+        return out
+
+    def slcn_solve(self, dt, kappa_q, bc, phistar, phi, source_q=None, rtol=1e-10, max_its=5000):
+        bc = bc.to(self.device, torch.uint8).contiguous()
+        its, res = ctypes.c_int(0), ctypes.c_double(0.0)
+        self._call("uwg_slcn_solve", float(dt), _ptr(kappa_q), _ptr(source_q), _ptr(bc), _ptr(phistar), _ptr(phi),
+                   float(rtol), int(max_its), ctypes.byref(its), ctypes.byref(res))
+        return its.value, res.value
+
+
+def gauss_abscissae(n):
+    """Ascending Gauss-Legendre abscissae on [-1, 1] for n = 3 or 5, in the
+    closed forms the library uses."""
+    if n == 3:
+        x = np.sqrt(0.6)
+        return np.array([-x, 0.0, x])
+    if n == 5:
+        a = np.sqrt(5.0 - 2.0 * np.sqrt(10.0 / 7.0)) / 3.0
+        b = np.sqrt(5.0 + 2.0 * np.sqrt(10.0 / 7.0)) / 3.0
+        return np.array([-b, -a, 0.0, a, b])
+    raise ValueError("Gauss rules of 3 or 5 points per axis are provided")
 
 
 def rng_seed(seed):

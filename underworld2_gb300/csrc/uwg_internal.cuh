@@ -63,6 +63,8 @@ struct uwg_ctx {
     void* red;              // reduction scratch (double[4096])
     double* red_host;       // pinned host mirror
     std::vector<void*> ws;  // solver workspaces (freed with the context)
+    double* slcn_ws;        // SLCN element matrices and CG vectors (grown on demand)
+    size_t slcn_ws_bytes;
 };
 
 // Error helpers --------------------------------------------------------------

@@ -482,6 +482,136 @@ extern "C" int uwg_interpolate(uwg_ctx* c, int64_t n, const double* pts, const d
     return UWG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Semi-Lagrangian departure values for SLCN advection-diffusion
+// (SemiLagrangianIntegrator_SolveNew, L/StgFEM/Utils/src/SemiLagrangianIntegrator.c:600-653)
+// on a Q1 mesh, one thread per node: RK4 back along the velocity (IntegrateRungeKutta,
+// :267-302, every stage clamped to the domain by the non-periodic PeriodicUpdate,
+// :382-393), then the node value if the launch point lies within 1e-6 minsep of the
+// node (:507-532, rtol 0), else the 4^dim Lagrange interpolant (InterpLagrange,
+// :357-380) on the static stencil (:534-598) of the element that holds the launch
+// point (BicubicInterpolatorNew, :395-505).  Bit-exact with the reference's order.
+#define SLCN_INV6 0.166666666667   // the reference's INV6, not 1/6
+
+__device__ __forceinline__ void slcn_clamp(const uwg_geom& g, double* p, int d) {
+    if (p[d] < g.minc[d]) { p[d] = g.minc[d]; return; }
+    if (p[d] > g.maxc[d]) p[d] = g.maxc[d];
+}
+
+__device__ __forceinline__ int slcn_stencil_start(int i, int n) {
+    int s = i > 0 ? i - 1 : i;
+    s += 3;
+    return s >= n ? s - 4 : s - 3;
+}
+
+// Lagrange factors of the 4 stencil coordinates at x, in InterpLagrange's order
+__device__ __forceinline__ void slcn_factors(double x, const double* c, double* f) {
+#pragma unroll
+    for (int n = 0; n < 4; n++) {
+        double v = 1.0;
+#pragma unroll
+        for (int o = 0; o < 4; o++) {
+            if (o == n) continue;
+            v *= (x - c[o]) / (c[n] - c[o]);
+        }
+        f[n] = v;
+    }
+}
+
+__device__ __forceinline__ double slcn_dot4(const double* v, const double* f) {
+    double r = 0.0;
+#pragma unroll
+    for (int n = 0; n < 4; n++) r += v[n] * f[n];
+    return r;
+}
+
+template <int DIM>
+__global__ void k_slcn_departure(uwg_geom g, int64_t n_nodes, double dt, const double* __restrict__ vel,
+                                 const double* __restrict__ phi, double atol, double* __restrict__ phistar) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n_nodes) return;
+    const int64_t id[3] = {i % g.nx[0], (i / g.nx[0]) % g.nx[1], i / ((int64_t)g.nx[0] * g.nx[1])};
+    double x0[3] = {0.0, 0.0, 0.0}, xp[3] = {0.0, 0.0, 0.0}, pos[3] = {0.0, 0.0, 0.0};
+    double k[4][3];
+#pragma unroll
+    for (int s = 0; s < 4; s++) k[s][0] = k[s][1] = k[s][2] = 0.0;
+#pragma unroll
+    for (int d = 0; d < DIM; d++) x0[d] = g.ax[d][id[d]];
+    // the reference ignores the interpolation status: every stage point is inside the domain
+    eval_velocity<DIM, 1>(g, vel, x0, k[0]);
+#pragma unroll
+    for (int d = 0; d < DIM; d++) { xp[d] = x0[d] - 0.5 * dt * k[0][d]; slcn_clamp(g, xp, d); }
+    eval_velocity<DIM, 1>(g, vel, xp, k[1]);
+#pragma unroll
+    for (int d = 0; d < DIM; d++) { xp[d] = x0[d] - 0.5 * dt * k[1][d]; slcn_clamp(g, xp, d); }
+    eval_velocity<DIM, 1>(g, vel, xp, k[2]);
+#pragma unroll
+    for (int d = 0; d < DIM; d++) { xp[d] = x0[d] - dt * k[2][d]; slcn_clamp(g, xp, d); }
+    eval_velocity<DIM, 1>(g, vel, xp, k[3]);
+#pragma unroll
+    for (int d = 0; d < DIM; d++) {
+        pos[d] = x0[d] - SLCN_INV6 * dt * (k[0][d] + 2.0 * k[1][d] + 2.0 * k[2][d] + k[3][d]);
+        slcn_clamp(g, pos, d);
+    }
+    double dot = 0.0;
+#pragma unroll
+    for (int d = DIM - 1; d >= 0; d--) dot = dot + (pos[d] - x0[d]) * (pos[d] - x0[d]);
+    int e[3] = {0, 0, 0};
+    if (sqrt(dot) < atol || !search_element<DIM>(g, pos, e)) {
+        phistar[i] = phi[i];
+        return;
+    }
+    int s[3] = {0, 0, 0};
+    double f[3][4];
+#pragma unroll
+    for (int d = 0; d < DIM; d++) {
+        s[d] = slcn_stencil_start(e[d], g.nx[d]);
+        double c[4];
+#pragma unroll
+        for (int a = 0; a < 4; a++) c[a] = g.ax[d][s[d] + a];
+        slcn_factors(pos[d], c, f[d]);
+    }
+    double ptsX[4], ptsY[4], ptsZ[4];
+    if (DIM == 2) {
+#pragma unroll
+        for (int yi = 0; yi < 4; yi++) {
+            const double* row = phi + (s[0] + (int64_t)(s[1] + yi) * g.nx[0]);
+#pragma unroll
+            for (int xi = 0; xi < 4; xi++) ptsX[xi] = row[xi];
+            ptsY[yi] = slcn_dot4(ptsX, f[0]);
+        }
+        phistar[i] = slcn_dot4(ptsY, f[1]);
+    } else {
+#pragma unroll
+        for (int zi = 0; zi < 4; zi++) {
+#pragma unroll
+            for (int yi = 0; yi < 4; yi++) {
+                const double* row = phi + (s[0] + (int64_t)g.nx[0] * ((s[1] + yi) + (int64_t)g.nx[1] * (s[2] + zi)));
+#pragma unroll
+                for (int xi = 0; xi < 4; xi++) ptsX[xi] = row[xi];
+                ptsY[yi] = slcn_dot4(ptsX, f[0]);
+            }
+            ptsZ[zi] = slcn_dot4(ptsY, f[1]);
+        }
+        phistar[i] = slcn_dot4(ptsZ, f[2]);
+    }
+}
+
+extern "C" int uwg_slcn_phistar(uwg_ctx* c, double dt, const double* vel, const double* phi, double* phistar) {
+    if (!c || !vel || !phi || !phistar || !(dt == dt))
+        return uwg_set_error(c, UWG_ERR_ARG, "uwg_slcn_phistar: bad argument");
+    if (c->order != 1) return uwg_set_error(c, UWG_ERR_ARG, "semi-Lagrangian advection is provided on Q1 meshes");
+    for (int d = 0; d < c->dim; d++)
+        if (c->res[d] < 3)
+            return uwg_set_error(c, UWG_ERR_ARG, "semi-Lagrangian stencils need at least 4 nodes per axis");
+    uwg_geom g = make_geom(c);
+    const double atol = 1e-6 * c->min_sep;
+    if (c->dim == 2) k_slcn_departure<2><<<nblk(c->n_nodes, 128), 128, 0, c->stream>>>(g, c->n_nodes, dt, vel, phi, atol, phistar);
+    else k_slcn_departure<3><<<nblk(c->n_nodes, 128), 128, 0, c->stream>>>(g, c->n_nodes, dt, vel, phi, atol, phistar);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
 extern "C" int uwg_max_dt(uwg_ctx* c, const double* vel, double* dt_h) {
     if (!c || !vel || !dt_h) return uwg_set_error(c, UWG_ERR_ARG, "uwg_max_dt: bad argument");
     unsigned long long* m = (unsigned long long*)c->red;

@@ -1,5 +1,6 @@
 """``uw.systems`` drop-ins for the PIC Stokes path: Stokes, Solver/StokesSolver,
-SwarmAdvector (P/systems/_stokes.py, _solver.py, _bsscr.py, _timeintegration.py).
+SwarmAdvector, AdvectionDiffusion (P/systems/_stokes.py, _solver.py, _bsscr.py,
+_timeintegration.py, _advectiondiffusion.py).
 """
 import time
 import warnings
@@ -373,81 +374,179 @@ def _uses_swarm(f):
     return any(_uses_swarm(c) for c in f._children())
 
 
-class AdvectionDiffusion:
-    """SUPG advection-diffusion of a scalar mesh variable (P/systems/_advectiondiffusion.py:16-150,
-    method "SUPG": :838-1020) on Q1 meshes, integrated with the reference's default
-    Gauss swarm (3 points per axis).  ``integrate(dt)`` advances ``phiField`` and
-    ``phiDotField`` by the explicit predictor-multicorrector; ``get_max_dt()`` is the
-    reference's Courant bound (courant factor 0.5)."""
+def _gauss_eval(mesh, f, n):
+    """Values of the function at the n^dim Gauss points of every element (flat, element-major)."""
+    ctx = mesh.ctx
+    coords = ctx.gauss_coords(n)
+    ectx = _fn.EvalContext(torch.full((coords.shape[0],), -1, dtype=torch.int64, device=ctx.device),
+                           lambda: coords, ctx.device)
+    return f.evaluate_at(ectx)[:, 0].contiguous()
 
-    def __init__(self, phiField, velocityField, fn_diffusivity, fn_sourceTerm=None, method="SUPG",
-                 phiDotField=None, conditions=[], gauss_swarm=None, **kwargs):
-        if method.upper() != "SUPG":
-            raise NotImplementedError("the GPU path provides the SUPG method")
-        if not isinstance(phiField, _mesh.MeshVariable) or phiField.nodeDofCount != 1:
-            raise TypeError("Provided 'phiField' must be a scalar 'MeshVariable'.")
+
+def _dirichlet_mask(conditions, var):
+    m = np.zeros(var.data.shape[0], np.uint8)
+    for c in conditions:
+        if isinstance(c, _cond.DirichletCondition) and c.variable is var:
+            m |= c.mask()[:, 0]
+    return m
+
+
+def _check_conditions(conditions, phiField):
+    if not isinstance(conditions, (list, tuple)):
+        conditions = [conditions]
+    for c in conditions:
+        if not isinstance(c, _cond.SystemCondition):
+            raise TypeError("Provided 'conditions' must be a list 'SystemCondition' objects.")
+        if not isinstance(c, _cond.DirichletCondition):
+            raise RuntimeError("Input condition type not recognised.")
+    return list(conditions)
+
+
+class AdvectionDiffusion:
+    """Advection-diffusion of a scalar mesh variable (P/systems/_advectiondiffusion.py:16-150):
+    ``method="SUPG"`` (explicit predictor-multicorrector, Streamline Upwind
+    Petrov-Galerkin) or ``method="SLCN"`` (semi-Lagrangian departure values,
+    Crank-Nicolson diffusion), on Q1 meshes."""
+
+    def __init__(self, phiField=None, velocityField=None, fn_diffusivity=None, fn_sourceTerm=None, method="SUPG",
+                 conditions=[], phiDotField=None, allow_non_q1=False, gauss_swarm=None, **kwargs):
+        if not isinstance(method, str) or method.upper() not in ("SUPG", "SLCN"):
+            raise ValueError("'method' parameter must be 'SUPG' or 'SLCN'")
+        self.method = method.upper()
+        if self.method == "SLCN" and phiDotField:
+            warnings.warn("'phiDotField' doesn't influence the 'SLCN' method. It's only required for the 'SUPG' method")
+        if self.method == "SUPG" and not phiDotField:
+            raise ValueError("'phiDotField' is required for the 'SUPG' method")
+        if not isinstance(phiField, _mesh.MeshVariable):
+            raise TypeError("Provided 'phiField' must be of 'MeshVariable' class.")
+        if phiField.data.shape[1] != 1:
+            raise TypeError("Provided 'phiField' must be a scalar")
+        if velocityField.data.shape[1] != phiField.mesh.dim:
+            raise TypeError("Provided 'velocityField' must be the same dimensionality as the phiField's mesh")
         if not isinstance(phiField.mesh, _mesh.FeMesh_Cartesian) or phiField.mesh._order != 1:
-            raise ValueError("'phiField' must live on a Q1 mesh")
-        if velocityField is not None and not isinstance(velocityField, _mesh.MeshVariable):
-            raise TypeError("Provided 'velocityField' must be of 'MeshVariable' class.")
-        if phiDotField is None:
-            phiDotField = phiField.mesh.add_variable(nodeDofCount=1)
-        if not isinstance(phiDotField, _mesh.MeshVariable) or phiDotField.data.shape != phiField.data.shape:
+            raise ValueError("The 'phiField' must be discretised on a Q1 mesh: advection-diffusion is provided "
+                             "for Q1 elements only (allow_non_q1 is not supported on the GPU path)")
+        if gauss_swarm is not None:
+            raise ValueError("the GPU path integrates on its own Gauss points (3 per axis for SUPG, 5 for SLCN)")
+        if self.method == "SUPG":
+            self.system = _SUPG_AdvectionDiffusion(phiField, phiDotField, velocityField, fn_diffusivity,
+                                                   fn_sourceTerm, conditions)
+        else:
+            self.system = _SLCN_AdvectionDiffusion(phiField, velocityField, fn_diffusivity, fn_sourceTerm, conditions)
+
+    @property
+    def velocityField(self):
+        return self.system.velocityField
+
+    @property
+    def phiField(self):
+        return self.system.phiField
+
+    def integrate(self, dt=0.0, **kwargs):
+        """Advance phiField by dt."""
+        self.system.integrate(dt, **kwargs)
+
+    def get_max_dt(self):
+        """The method's time-step bound for the current velocity and diffusivity."""
+        return self.system.get_max_dt()
+
+
+class _SUPG_AdvectionDiffusion:
+    """SUPG (P/systems/_advectiondiffusion.py:838-1020): the explicit
+    predictor-multicorrector integrated on the 3-point Gauss swarm;
+    ``get_max_dt()`` is the Courant bound with courant factor 0.5."""
+
+    def __init__(self, phiField, phiDotField, velocityField, fn_diffusivity, fn_sourceTerm=None, conditions=[]):
+        if not isinstance(phiDotField, _mesh.MeshVariable):
+            raise TypeError("Provided 'phiDotField' must be 'None' or of 'MeshVariable' class.")
+        if phiDotField.data.shape != phiField.data.shape:
             raise TypeError("Provided 'phiDotField' is not the same shape as the provided 'phiField'")
-        if not isinstance(conditions, (list, tuple)):
-            conditions = [conditions]
-        for c in conditions:
-            if not isinstance(c, _cond.DirichletCondition) or c.variable is not phiField:
-                raise ValueError("only Dirichlet conditions on 'phiField' are supported")
-        self._phi, self._phidot, self._vel = phiField, phiDotField, velocityField
+        self.phiField, self._phidot, self.velocityField = phiField, phiDotField, velocityField
         self.mesh = phiField.mesh
-        self._conditions = list(conditions)
+        self._conditions = _check_conditions(conditions, phiField)
         self.fn_diffusivity = _fn.Function.convert(fn_diffusivity)
         self.fn_sourceTerm = _fn.Function.convert(fn_sourceTerm) if fn_sourceTerm is not None else None
         for f in (self.fn_diffusivity, self.fn_sourceTerm):
             if f is not None and _uses_swarm(f):
                 raise ValueError("Gauss-point integration cannot evaluate swarm variables")
 
-    @property
-    def phiField(self):
-        return self._phi
-
-    @property
-    def velocityField(self):
-        return self._vel
-
-    def _at_gauss(self, f):
-        ctx = self.mesh.ctx
-        coords = ctx.gauss_coords()
-        ectx = _fn.EvalContext(torch.full((coords.shape[0],), -1, dtype=torch.int64, device=ctx.device),
-                               lambda: coords, ctx.device)
-        return f.evaluate_at(ectx)[:, 0].contiguous()
-
-    def _bc(self):
-        m = np.zeros(self._phi.data.shape[0], np.uint8)
-        for c in self._conditions:
-            m |= c.mask()[:, 0]
-        return m
-
     def integrate(self, dt, **kwargs):
         ctx = self.mesh.ctx
-        kappa = self._at_gauss(self.fn_diffusivity)
-        src = self._at_gauss(self.fn_sourceTerm) if self.fn_sourceTerm is not None else None
-        mask = self._bc()
-        phi = self._phi._to_device().contiguous()
+        kappa = _gauss_eval(self.mesh, self.fn_diffusivity, 3)
+        src = _gauss_eval(self.mesh, self.fn_sourceTerm, 3) if self.fn_sourceTerm is not None else None
+        mask = _dirichlet_mask(self._conditions, self.phiField)
+        phi = self.phiField._to_device().contiguous()
         phidot = self._phidot._to_device().contiguous()
+        # Dirichlet values: phi's and phi-dot's current values (FeVariable_SetBC on both)
         bcval = phi.clone()
         bcdot = phidot.clone()
-        vel = self._vel._to_device() if self._vel is not None else None
+        vel = self.velocityField._to_device()
         ctx.advdiff_step(dt, vel, kappa, phi, phidot, torch.from_numpy(mask), bcval, bcdot, source_q=src)
-        self._phi._from_device()
+        self.phiField._from_device()
         self._phidot._from_device()
 
     def get_max_dt(self):
         ctx = self.mesh.ctx
-        kappa = self._at_gauss(self.fn_diffusivity)
-        vel = self._vel._to_device() if self._vel is not None else None
-        return ctx.advdiff_max_dt(vel, kappa, 0.5)
+        kappa = _gauss_eval(self.mesh, self.fn_diffusivity, 3)
+        return ctx.advdiff_max_dt(self.velocityField._to_device(), kappa, 0.5)
+
+
+class _SLCN_AdvectionDiffusion:
+    """Semi-Lagrangian Crank-Nicolson (P/systems/_advectiondiffusion.py:153-823):
+    departure values by RK4 back-tracing and Lagrange cubics on static stencils
+    (the reference's default interpolator), then the Crank-Nicolson diffusion
+    system on the 5-point Gauss swarm, Dirichlet nodes keeping their values."""
+
+    def __init__(self, phiField, velocityField, fn_diffusivity, fn_sourceTerm=None, conditions=[]):
+        self.phiField, self.velocityField = phiField, velocityField
+        self.mesh = phiField.mesh
+        self._conditions = _check_conditions(conditions, phiField)
+        self.fn_diffusivity = _fn.Function.convert(fn_diffusivity)
+        self.fn_sourceTerm = _fn.Function.convert(fn_sourceTerm) if fn_sourceTerm is not None else None
+        for f in (self.fn_diffusivity, self.fn_sourceTerm):
+            if f is not None and _uses_swarm(f):
+                raise ValueError("Gauss-point integration cannot evaluate swarm variables")
+        self._phiStar = self.mesh.add_variable(nodeDofCount=1)
+        self.last_solve = None
+
+    def integrate(self, dt=0.0, phiStar=None, interpolator="", solve=True, phiStarCopy=None, smooth=0.9,
+                  substeps=1, rtol=1e-10, **kwargs):
+        if interpolator:
+            raise NotImplementedError("the GPU path provides the default cubic-stencil interpolator only")
+        ctx = self.mesh.ctx
+        dts = dt / float(substeps)
+        for _ in range(substeps):
+            phi = self.phiField._to_device().contiguous()
+            if phiStar is None:
+                # the reference traces back over the whole dt in every substep
+                # (SemiLagrangianIntegrator_SolveNew is called with dt, :740-746)
+                ps = ctx.slcn_phistar(dt, self.velocityField._to_device(), phi)
+                self._phiStar.data[:, 0] = ps.cpu().numpy()
+            else:
+                self._phiStar.data[...] = phiStar.data
+                ps = self._phiStar._to_device().contiguous()
+            if phiStarCopy is not None:
+                phiStarCopy.data[...] = self._phiStar.data
+            if solve:
+                kappa = _gauss_eval(self.mesh, self.fn_diffusivity, 5)
+                src = _gauss_eval(self.mesh, self.fn_sourceTerm, 5) if self.fn_sourceTerm is not None else None
+                mask = torch.from_numpy(_dirichlet_mask(self._conditions, self.phiField))
+                its, res = ctx.slcn_solve(dts, kappa, mask, ps, phi, source_q=src, rtol=rtol)
+                self.last_solve = {"iterations": its, "residual": res}
+                self.phiField._from_device()
+
+    def get_max_dt(self):
+        ctx = self.mesh.ctx
+        vel = self.velocityField._to_device().reshape(-1, self.mesh.dim)
+        vmax = float(torch.sqrt(torch.max(torch.sum(vel * vel, dim=1))))
+        nodes = torch.from_numpy(self.mesh.data).to(ctx.device)
+        ectx = _fn.EvalContext(torch.full((nodes.shape[0],), -1, dtype=torch.int64, device=ctx.device),
+                               lambda: nodes, ctx.device)
+        kmax = float(self.fn_diffusivity.evaluate_at(ectx).max())
+        dx = ctx.min_sep
+        adv = dx / vmax if vmax > 0.0 else float("inf")
+        diff = dx * dx / kmax if kmax > 0.0 else float("inf")
+        return min(adv, diff)
 
 
 class SwarmAdvector:
