@@ -429,6 +429,51 @@ def run_advdiff(args):
                       "T_range": [float(phi.min()), float(phi.max())]}))
 
 
+def run_slcn(args):
+    """SLCN advection-diffusion of T on the workload's Q1 mesh (same cellular
+    velocity, diffusivity 1e-3 at the 5^d Gauss points, T fixed on the top and
+    bottom walls): `--reps` steps of departure values + Crank-Nicolson CG solve
+    (relative residual 1e-10) at dt = min(dx / v_max, dx^2 / kappa) after 3
+    untimed steps.  Reported with the CG iteration count of the last step."""
+    import torch
+    from underworld2_gb300._core import Context
+    cfg = CONFIGS[args.config]
+    dim = cfg["dim"]
+    ctx = Context(dim, cfg["res"], (0.0,) * dim, (1.0,) * dim)
+    xyz = torch.stack(torch.meshgrid(*[torch.tensor(a, device=ctx.device) for a in reversed(ctx.axes)],
+                                     indexing="ij")[::-1], dim=-1).reshape(-1, dim)
+    s, c = torch.sin(torch.pi * xyz), torch.cos(torch.pi * xyz)
+    vel = torch.zeros_like(xyz)
+    vel[:, 0] = s[:, 0] * c[:, dim - 1]
+    vel[:, dim - 1] = -c[:, 0] * s[:, dim - 1]
+    vmax = float(vel.norm(dim=1).max()) * 1e3
+    vel = (1e3 * vel).contiguous().reshape(-1)
+    kappa = torch.full((ctx.n_el * 5 ** dim,), 1e-3, dtype=torch.float64, device=ctx.device)
+    bc = ((xyz[:, dim - 1] == 1.0) | (xyz[:, dim - 1] == 0.0)).to(torch.uint8)
+    phi = (1.0 - xyz[:, dim - 1]).contiguous()
+    dt = min(ctx.min_sep / vmax, ctx.min_sep ** 2 / 1e-3)
+    st = {}
+
+    def step():
+        ps = ctx.slcn_phistar(dt, vel, phi)
+        st["its"], st["res"] = ctx.slcn_solve(dt, kappa, bc, ps, phi, rtol=1e-10)
+
+    for _ in range(3):
+        step()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(args.reps):
+        step()
+    ev1.record()
+    torch.cuda.synchronize()
+    sec = ev0.elapsed_time(ev1) / 1e3 / args.reps
+    print(json.dumps({"kernel": "slcn", "config": args.config, "res": list(ctx.res), "reps": args.reps, "dt": dt,
+                      "ms_per_step": sec * 1e3, "cg_iterations": st["its"], "cg_residual": st["res"],
+                      "T_finite": bool(torch.isfinite(phi).all()),
+                      "T_range": [float(phi.min()), float(phi.max())]}))
+
+
 def run_profile_solve(args):
     """One map + DVC + assembly + solve of the workload, untimed (the target of
     the launch-list captures recorded under profiles/); `--kernel-ppc` lowers
@@ -528,8 +573,8 @@ def main():
     ap.add_argument("--outer-rtol", type=float, default=1e-9)
     ap.add_argument("--schur-pc", type=int, default=1, help="0: Uzawa S^ (reference), 1: scaled BFBt")
     ap.add_argument("--bfbt-rtol", type=float, default=3e-2)
-    ap.add_argument("--kernel", choices=["applyK32", "applyK64", "advdiff"],
-                    help="only launch one operator kernel, or time SUPG advection-diffusion steps (profiling)")
+    ap.add_argument("--kernel", choices=["applyK32", "applyK64", "advdiff", "slcn"],
+                    help="only launch one operator kernel, or time SUPG / SLCN advection-diffusion steps (profiling)")
     ap.add_argument("--kernel-ppc", type=int, default=0)
     ap.add_argument("--profile-solve", action="store_true", help="one untimed solve (profiling target)")
     ap.add_argument("--reps", type=int, default=5)
@@ -540,6 +585,9 @@ def main():
     args = ap.parse_args()
     if args.kernel == "advdiff":
         run_advdiff(args)
+        return
+    if args.kernel == "slcn":
+        run_slcn(args)
         return
     if args.kernel:
         run_kernel(args)
