@@ -227,6 +227,13 @@ int uwg_interpolate(uwg_ctx* ctx, int64_t n, const double* pts, const double* ve
 /* dt = 0.5 * minimum node separation / max |v|.  Replaces SwarmAdvector_MaxDt
  * (L/PICellerator/MaterialPoints/src/SwarmAdvector.c:370-387). */
 int uwg_max_dt(uwg_ctx* ctx, const double* vel, double* dt_h);
+/* Values [n][ncomp] and optional global gradients [n][ncomp][dim] (grad may be NULL)
+ * of a nodal field with ncomp components at points [n][dim]; NaN outside the mesh.
+ * Replaces FeVariable_InterpolateValueAt / FeVariable_InterpolateDerivativesAt
+ * (L/StgFEM/Discretisation/src/FeVariable.c:549-599,1007-1044) behind the function
+ * graph's MeshVariable and fn_gradient inputs (P/mesh/_meshvariable.py:297-327). */
+int uwg_interpolate_field(uwg_ctx* ctx, int64_t n, const double* pts, const double* field, int ncomp, double* out,
+                          double* grad);
 
 /* ---- SUPG advection-diffusion of a nodal scalar (Q1 meshes) ----------------
  * One time step of the explicit predictor-multicorrector with SUPG residual and

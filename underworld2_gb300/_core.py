@@ -173,6 +173,13 @@ class Context:
         self._call("uwg_interpolate", pts.shape[0], _ptr(pts), _ptr(vel), _ptr(out))
         return out
 
+    def interpolate_field(self, pts, field, ncomp, grad=False):
+        """Values [n, ncomp] (and gradients [n, ncomp, dim]) of a nodal field at points."""
+        out = torch.empty((pts.shape[0], ncomp), dtype=torch.float64, device=self.device)
+        g = torch.empty((pts.shape[0], ncomp, self.dim), dtype=torch.float64, device=self.device) if grad else None
+        self._call("uwg_interpolate_field", pts.shape[0], _ptr(pts), _ptr(field), int(ncomp), _ptr(out), _ptr(g))
+        return out, g
+
     def max_dt(self, vel):
         dt = ctypes.c_double(0.0)
         self._call("uwg_max_dt", _ptr(vel), ctypes.byref(dt))

@@ -482,6 +482,85 @@ extern "C" int uwg_interpolate(uwg_ctx* c, int64_t n, const double* pts, const d
     return UWG_OK;
 }
 
+// Values (and optionally global gradients) of a nodal field with ncomp
+// components at arbitrary points: FeVariable_InterpolateValueAt /
+// FeVariable_InterpolateDerivativesAt (L/StgFEM/Discretisation/src/FeVariable.c:549-599,
+// 1007-1044) for the function graph's mesh-variable inputs.  Values use
+// eval_velocity's arithmetic order (bit-exact with it for ncomp = dim); gradients
+// are dN/dxi over the axis-aligned Jacobian, laid out [point][comp][axis].
+// Points outside the mesh get NaN.
+template <int DIM, int ORDER>
+__global__ void k_interp_field(uwg_geom g, int64_t n, const double* __restrict__ pts,
+                               const double* __restrict__ field, int ncomp, double* __restrict__ out,
+                               double* __restrict__ grad) {
+    constexpr int NEN = Shape<DIM, ORDER>::NEN;
+    constexpr int K = ORDER + 1;
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double pt[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int d = 0; d < DIM; d++) pt[d] = pts[i * DIM + d];
+    int eidx[3] = {0, 0, 0};
+    if (!search_element<DIM>(g, pt, eidx)) {
+        for (int c = 0; c < ncomp; c++) {
+            out[i * ncomp + c] = nan("");
+            if (grad)
+                for (int d = 0; d < DIM; d++) grad[(i * ncomp + c) * DIM + d] = nan("");
+        }
+        return;
+    }
+    double xi[3], N[NEN], dN[3][NEN];
+    global_to_local<DIM, ORDER>(g, eidx, pt, xi);
+    Shape<DIM, ORDER>::N(xi, N);
+    int64_t node[NEN];
+#pragma unroll
+    for (int a = 0; a < NEN; a++) {
+        int64_t ix = eidx[0] * ORDER + a % K;
+        int64_t iy = eidx[1] * ORDER + (a / K) % K;
+        int64_t iz = DIM == 3 ? eidx[2] * ORDER + a / (K * K) : 0;
+        node[a] = ix + g.nx[0] * (iy + (int64_t)g.nx[1] * iz);
+    }
+    double jac[3] = {1.0, 1.0, 1.0};
+    if (grad) {
+        Shape<DIM, ORDER>::dN(xi, dN);
+#pragma unroll
+        for (int d = 0; d < DIM; d++) {
+            double s = 0.0;
+#pragma unroll
+            for (int a = 0; a < NEN; a++) s += node_coord<DIM, ORDER>(g, eidx, a, d) * dN[d][a];
+            jac[d] = s;
+        }
+    }
+    for (int c = 0; c < ncomp; c++) {
+        double v = 0.0;
+#pragma unroll
+        for (int a = 0; a < NEN; a++) v += field[node[a] * ncomp + c] * N[a];
+        out[i * ncomp + c] = v;
+        if (grad) {
+#pragma unroll
+            for (int d = 0; d < DIM; d++) {
+                double s = 0.0;
+#pragma unroll
+                for (int a = 0; a < NEN; a++) s += field[node[a] * ncomp + c] * dN[d][a];
+                grad[(i * ncomp + c) * DIM + d] = s / jac[d];
+            }
+        }
+    }
+}
+
+extern "C" int uwg_interpolate_field(uwg_ctx* c, int64_t n, const double* pts, const double* field, int ncomp,
+                                     double* out, double* grad) {
+    if (!c || n < 0 || ncomp < 1 || (n && (!pts || !field || !out)))
+        return uwg_set_error(c, UWG_ERR_ARG, "uwg_interpolate_field: bad argument");
+    if (!n) return UWG_OK;
+    uwg_geom g = make_geom(c);
+#define L_(D, O) k_interp_field<D, O><<<nblk(n, 128), 128, 0, c->stream>>>(g, n, pts, field, ncomp, out, grad)
+    UWG_DISPATCH(c, L_);
+#undef L_
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Semi-Lagrangian departure values for SLCN advection-diffusion
 // (SemiLagrangianIntegrator_SolveNew, L/StgFEM/Utils/src/SemiLagrangianIntegrator.c:600-653)

@@ -8,12 +8,20 @@ particle, L/Underworld/Function/src/SwarmVariableFn.cpp:30-110; coordinate
 inputs are the integration point's global position).
 
 Supported: constants and tuples, ``input()``/``coord()``, swarm and mesh
-variables, arithmetic (+ - * / **, unary -), comparisons and logical
-and/or, ``math.exp/log/sqrt/sin/cos/abs/pow/dot``, ``branching.map`` and
-``branching.conditional``.
+variables and mesh-variable gradients, arithmetic (+ - * / **, unary -),
+comparisons and logical and/or, the ``math`` functions of
+P/function/math.py, ``misc.min/max``, ``tensor.symmetric/antisymmetric/
+second_invariant/deviatoric`` (L/StgDomain/Geometry/src/TensorMath.c
+conventions: full tensors row-major, symmetric tensors [00, 11, (22,) 01,
+(02, 12)]), ``shape.Polygon``, ``branching.map/conditional``,
+``view.min_max``, ``exception.SafeMaths`` and
+``rheology.stress_limiting_viscosity``.  ``Function.evaluate`` accepts
+coordinates, a mesh or a swarm, as the reference's.
 """
+import math as _pymath
 import numbers
 
+import numpy as np
 import torch
 
 
@@ -39,7 +47,12 @@ class EvalContext:
 
 
 class Function:
-    """Base class: ``_eval(ctx)`` returns a float64 tensor of shape (n, k)."""
+    """Base class: ``_eval(ctx)`` returns a float64 tensor of shape (n, k).
+    ``_kind`` is the value type where it matters: "tensor" (full, row-major),
+    "symtensor" or None; ``_bool`` marks boolean results (stored as 0/1)."""
+
+    _kind = None
+    _bool = False
 
     @staticmethod
     def convert(obj):
@@ -73,6 +86,16 @@ class Function:
     def _children(self):
         return []
 
+    def evaluate(self, inputData=None, inputType=None):
+        """Values at coordinates (float, tuple, list or [n, dim] array), at the
+        nodes of a mesh or at the particles of a swarm (P/function/_function.py:808-930).
+        Returns an [n, k] numpy array (bool for boolean functions)."""
+        ctx = _input_context(inputData)
+        if ctx.n == 0:
+            return np.zeros((0, 1), dtype=bool if self._bool else np.float64)
+        v = self.evaluate_at(ctx).cpu().numpy()
+        return v != 0 if self._bool else np.array(v, dtype=np.float64)
+
     # arithmetic
     def __add__(self, o): return _Bin(torch.add, self, Function.convert(o))
     def __radd__(self, o): return _Bin(torch.add, Function.convert(o), self)
@@ -84,12 +107,13 @@ class Function:
     def __rtruediv__(self, o): return _Bin(torch.div, Function.convert(o), self)
     def __pow__(self, o): return _Bin(torch.pow, self, Function.convert(o))
     def __neg__(self): return _Un(torch.neg, self)
-    def __lt__(self, o): return _Bin(lambda a, b: (a < b).double(), self, Function.convert(o))
-    def __le__(self, o): return _Bin(lambda a, b: (a <= b).double(), self, Function.convert(o))
-    def __gt__(self, o): return _Bin(lambda a, b: (a > b).double(), self, Function.convert(o))
-    def __ge__(self, o): return _Bin(lambda a, b: (a >= b).double(), self, Function.convert(o))
-    def __and__(self, o): return _Bin(lambda a, b: ((a != 0) & (b != 0)).double(), self, Function.convert(o))
-    def __or__(self, o): return _Bin(lambda a, b: ((a != 0) | (b != 0)).double(), self, Function.convert(o))
+    def __lt__(self, o): return _Bool(lambda a, b: a < b, self, Function.convert(o))
+    def __le__(self, o): return _Bool(lambda a, b: a <= b, self, Function.convert(o))
+    def __gt__(self, o): return _Bool(lambda a, b: a > b, self, Function.convert(o))
+    def __ge__(self, o): return _Bool(lambda a, b: a >= b, self, Function.convert(o))
+    def __and__(self, o): return _Bool(lambda a, b: (a != 0) & (b != 0), self, Function.convert(o))
+    def __or__(self, o): return _Bool(lambda a, b: (a != 0) | (b != 0), self, Function.convert(o))
+    def __xor__(self, o): return _Bool(lambda a, b: (a != 0) ^ (b != 0), self, Function.convert(o))
 
     def __getitem__(self, i):
         return _Index(self, i)
@@ -122,6 +146,8 @@ class _Vector(Function):
 class _Bin(Function):
     def __init__(self, op, a, b):
         self.op, self.a, self.b = op, a, b
+        # a scalar times (or plus) a tensor keeps the tensor's type
+        self._kind = a._kind or b._kind
 
     def _children(self):
         return [self.a, self.b]
@@ -130,9 +156,23 @@ class _Bin(Function):
         return self.op(self.a.evaluate_at(ctx), self.b.evaluate_at(ctx))
 
 
+class _Bool(Function):
+    _bool = True
+
+    def __init__(self, op, a, b):
+        self.op, self.a, self.b = op, a, b
+
+    def _children(self):
+        return [self.a, self.b]
+
+    def _eval(self, ctx):
+        return self.op(self.a.evaluate_at(ctx), self.b.evaluate_at(ctx)).double()
+
+
 class _Un(Function):
     def __init__(self, op, a):
         self.op, self.a = op, a
+        self._kind = a._kind
 
     def _children(self):
         return [self.a]
@@ -190,31 +230,51 @@ class _MeshVar(Function):
         return "coord" in kinds or "mesh" in kinds
 
 
+def _unary(op):
+    return staticmethod(lambda fn=None: _Un(op, Function.convert(fn) if fn is not None else input()))
+
+
+class _MeshGrad(Function):
+    def __init__(self, var):
+        self.var = var
+        self._kind = "tensor" if var.nodeDofCount > 1 else None
+
+    def _eval(self, ctx):
+        return self.var._interpolate_grad(ctx.coords)
+
+    def depends_on(self, kinds):
+        return "coord" in kinds or "mesh" in kinds
+
+
 class math:
-    @staticmethod
-    def exp(f): return _Un(torch.exp, Function.convert(f))
+    """Elementwise functions of P/function/math.py (the argument defaults to input())."""
+    cos = _unary(torch.cos)
+    sin = _unary(torch.sin)
+    tan = _unary(torch.tan)
+    acos = _unary(torch.acos)
+    asin = _unary(torch.asin)
+    atan = _unary(torch.atan)
+    cosh = _unary(torch.cosh)
+    sinh = _unary(torch.sinh)
+    tanh = _unary(torch.tanh)
+    acosh = _unary(torch.acosh)
+    asinh = _unary(torch.asinh)
+    atanh = _unary(torch.atanh)
+    exp = _unary(torch.exp)
+    log = _unary(torch.log)
+    log2 = _unary(torch.log2)
+    log10 = _unary(torch.log10)
+    sqrt = _unary(torch.sqrt)
+    erf = _unary(torch.erf)
+    erfc = _unary(torch.erfc)
+    abs = _unary(torch.abs)
 
     @staticmethod
-    def log(f): return _Un(torch.log, Function.convert(f))
+    def pow(fn1, fn2): return _Bin(torch.pow, Function.convert(fn1), Function.convert(fn2))
 
     @staticmethod
-    def sqrt(f): return _Un(torch.sqrt, Function.convert(f))
-
-    @staticmethod
-    def sin(f): return _Un(torch.sin, Function.convert(f))
-
-    @staticmethod
-    def cos(f): return _Un(torch.cos, Function.convert(f))
-
-    @staticmethod
-    def abs(f): return _Un(torch.abs, Function.convert(f))
-
-    @staticmethod
-    def pow(a, b): return _Bin(torch.pow, Function.convert(a), Function.convert(b))
-
-    @staticmethod
-    def dot(a, b):
-        return _Bin(lambda x, y: (x * y).sum(dim=1, keepdim=True), Function.convert(a), Function.convert(b))
+    def dot(fn1, fn2):
+        return _Bin(lambda x, y: (x * y).sum(dim=1, keepdim=True), Function.convert(fn1), Function.convert(fn2))
 
 
 class _Map(Function):
@@ -282,3 +342,214 @@ class branching:
 
 class misc:
     constant = constant
+
+    @staticmethod
+    def max(fn1, fn2):
+        """Elementwise maximum of two scalar functions (P/function/misc.py)."""
+        return _Bin(torch.maximum, Function.convert(fn1), Function.convert(fn2))
+
+    @staticmethod
+    def min(fn1, fn2):
+        """Elementwise minimum of two scalar functions (P/function/misc.py)."""
+        return _Bin(torch.minimum, Function.convert(fn1), Function.convert(fn2))
+
+
+def _dim_of(k, kind):
+    return {("tensor", 4): 2, ("tensor", 9): 3, ("symtensor", 3): 2, ("symtensor", 6): 3}.get((kind, k))
+
+
+class _TensorFn(Function):
+    def __init__(self, what, fn):
+        self.what, self.a = what, Function.convert(fn)
+        need = {"symmetric": "tensor", "antisymmetric": "tensor", "deviatoric": "symtensor"}.get(what)
+        if need and self.a._kind != need:
+            raise ValueError("TensorFunc expects %s input for '%s'" % ("Tensor" if need == "tensor" else
+                                                                      "SymmetricTensor", what))
+        if what == "second_invariant" and self.a._kind not in ("tensor", "symtensor"):
+            raise ValueError("second_invariant expects a Tensor or SymmetricTensor input")
+        self._kind = {"symmetric": "symtensor", "antisymmetric": "tensor", "deviatoric": "symtensor"}.get(what)
+
+    def _children(self):
+        return [self.a]
+
+    def _eval(self, ctx):
+        t = self.a.evaluate_at(ctx)
+        dim = _dim_of(t.shape[1], self.a._kind)
+        if dim is None:
+            raise ValueError("tensor function input has %d components" % t.shape[1])
+        if self.a._kind == "tensor":
+            F = t.reshape(-1, dim, dim)
+            if self.what == "symmetric":      # TensorArray_GetSymmetricPart (TensorMath.c:229-270)
+                S = 0.5 * (F + F.transpose(1, 2))
+                cols = [F[:, 0, 0], F[:, 1, 1]] + ([F[:, 2, 2]] if dim == 3 else []) + [S[:, 0, 1]] + \
+                    ([S[:, 0, 2], S[:, 1, 2]] if dim == 3 else [])
+                return torch.stack(cols, dim=1)
+            if self.what == "antisymmetric":  # TensorArray_GetAntisymmetricPart (:167-227)
+                return (0.5 * (F - F.transpose(1, 2))).reshape(-1, dim * dim)
+            return torch.sqrt(0.5 * (t * t).sum(dim=1, keepdim=True))   # TensorArray_2ndInvariant (:379-405)
+        # symmetric storage
+        diag = t[:, :dim]
+        off = t[:, dim:]
+        if self.what == "second_invariant":   # SymmetricTensor_2ndInvariant (:409-437)
+            return torch.sqrt(0.5 * (diag * diag).sum(dim=1, keepdim=True) + (off * off).sum(dim=1, keepdim=True))
+        mean = diag.sum(dim=1, keepdim=True) / dim      # deviatoric (Tensor.cpp get_deviatoric)
+        return torch.cat([diag - mean, off], dim=1)
+
+
+class tensor:
+    """Tensor functions of P/function/tensor.py."""
+
+    @staticmethod
+    def symmetric(fn): return _TensorFn("symmetric", fn)
+
+    @staticmethod
+    def antisymmetric(fn): return _TensorFn("antisymmetric", fn)
+
+    @staticmethod
+    def second_invariant(fn): return _TensorFn("second_invariant", fn)
+
+    @staticmethod
+    def deviatoric(fn): return _TensorFn("deviatoric", fn)
+
+
+class _Polygon(Function):
+    """Inside test of _PolygonShape_IsCoordInside (L/StgDomain/Shape/src/PolygonShape.c:268-316):
+    the signed angles subtended by the edges sum to +-2 pi inside, 0 outside."""
+    _bool = True
+
+    def __init__(self, vertices, fn=None):
+        if not isinstance(vertices, np.ndarray):
+            raise TypeError("Provided 'vertices' must be a numpy array.")
+        if len(vertices.shape) != 2:
+            raise TypeError("Provided 'vertices' array must be 2 dimensional.")
+        if vertices.shape[0] < 3:
+            raise TypeError("Provided 'vertices' array must contain at least 3 vertices.")
+        if vertices.shape[1] != 2:
+            raise TypeError("Provided 'vertices' array must contain 2d vectors.")
+        self.v = np.array(vertices, dtype=np.float64)
+        self.a = Function.convert(fn) if fn is not None else input()
+
+    def _children(self):
+        return [self.a]
+
+    def _eval(self, ctx):
+        p = self.a.evaluate_at(ctx)
+        if p.shape[1] not in (2, 3):
+            raise ValueError("Polygon shape expects input to be be 2 or 3 dimensional vector.")
+        x, y = p[:, 0], p[:, 1]
+        V = torch.from_numpy(self.v).to(p.device)
+        total = torch.zeros_like(x)
+        for i in range(len(self.v)):
+            sx, sy = x - V[i, 0], y - V[i, 1]
+            j = (i + 1) % len(self.v)
+            ex, ey = x - V[j, 0], y - V[j, 1]
+            val = (sx * ex + sy * ey) / (torch.sqrt(sx * sx + sy * sy) * torch.sqrt(ex * ex + ey * ey))
+            ang = torch.where(val >= 1.0, torch.zeros_like(val),
+                              torch.where(val <= -1.0, torch.full_like(val, _pymath.pi), torch.acos(val)))
+            cross = ex * sy - ey * sx
+            total = torch.where(cross > 0.0, total + ang, total - ang)
+        return (~(torch.abs(total) < _pymath.pi)).double()[:, None]
+
+
+class shape:
+    @staticmethod
+    def Polygon(vertices, fn=None, *args, **kwargs): return _Polygon(vertices, fn)
+
+
+class _SafeMaths(Function):
+    def __init__(self, fn):
+        self.a = Function.convert(fn)
+        self._kind = self.a._kind
+
+    def _children(self):
+        return [self.a]
+
+    def _eval(self, ctx):
+        v = self.a.evaluate_at(ctx)
+        if not bool(torch.isfinite(v).all()):
+            raise RuntimeError("Function evaluation produced a non-finite value (SafeMaths).")
+        return v
+
+
+class exception:
+    @staticmethod
+    def SafeMaths(fn, *args, **kwargs): return _SafeMaths(fn)
+
+
+class _StressLimit(Function):
+    def __init__(self, fn_stress, fn_stresslimit, fn_inputviscosity):
+        self.s, self.lim, self.eta = (Function.convert(f) for f in (fn_stress, fn_stresslimit, fn_inputviscosity))
+
+    def _children(self):
+        return [self.s, self.lim, self.eta]
+
+    def _eval(self, ctx):
+        sII = _TensorFn("second_invariant", self.s).evaluate_at(ctx)
+        lim = self.lim.evaluate_at(ctx)
+        eta = self.eta.evaluate_at(ctx)
+        return torch.where(sII > lim, eta * lim / sII, eta)
+
+
+class rheology:
+    @staticmethod
+    def stress_limiting_viscosity(fn_stress, fn_stresslimit, fn_inputviscosity, *args, **kwargs):
+        """eta * limit / stress_II where the stress invariant exceeds the limit
+        (P/function/rheology.py; StressLimitingViscosity.cpp)."""
+        return _StressLimit(fn_stress, fn_stresslimit, fn_inputviscosity)
+
+
+class _MinMax(Function):
+    def __init__(self, fn, fn_norm=None, fn_auxiliary=None):
+        self.a = Function.convert(fn)
+        self.norm = Function.convert(fn_norm) if fn_norm is not None else None
+        self.reset()
+
+    def _children(self):
+        return [self.a] + ([self.norm] if self.norm is not None else [])
+
+    def reset(self):
+        self._min, self._max = float("inf"), float("-inf")
+
+    def _eval(self, ctx):
+        v = self.a.evaluate_at(ctx)
+        q = self.norm.evaluate_at(ctx) if self.norm is not None else v
+        if q.shape[1] != 1:
+            q = torch.sqrt((q * q).sum(dim=1, keepdim=True))
+        if q.shape[0]:
+            self._min = min(self._min, float(q.min()))
+            self._max = max(self._max, float(q.max()))
+        return v
+
+    def min_local(self): return self._min
+    def max_local(self): return self._max
+    def min_global(self): return self._min
+    def max_global(self): return self._max
+
+
+class view:
+    @staticmethod
+    def min_max(fn, fn_norm=None, fn_auxiliary=None, *args, **kwargs):
+        """Pass-through that records the extrema of its input (of fn_norm where
+        given, of the magnitude for vectors) over every evaluation (P/function/view.py)."""
+        return _MinMax(fn, fn_norm, fn_auxiliary)
+
+
+def _input_context(inputData):
+    """EvalContext for Function.evaluate: coordinates, a mesh's nodes or a swarm's particles."""
+    dev = torch.device("cuda") if torch.cuda.is_available() else torch.device("cpu")
+    if hasattr(inputData, "particleCoordinates") and hasattr(inputData, "_x"):
+        x = inputData._x if inputData._x is not None else torch.zeros((0, inputData.dim), dtype=torch.float64)
+        dev = x.device
+        return EvalContext(torch.arange(x.shape[0], device=dev), lambda: x, dev)
+    if hasattr(inputData, "_axes") and hasattr(inputData, "elementRes"):
+        pts = np.asarray(inputData.data, dtype=np.float64)
+    elif inputData is None:
+        pts = np.zeros((1, 1))
+    elif isinstance(inputData, numbers.Number):
+        pts = np.array([[float(inputData)]])
+    else:
+        pts = np.asarray(inputData, dtype=np.float64)
+        if pts.ndim == 1:
+            pts = pts[None, :]
+    t = torch.from_numpy(np.ascontiguousarray(pts)).to(dev)
+    return EvalContext(torch.full((t.shape[0],), -1, dtype=torch.int64, device=dev), lambda: t, dev)

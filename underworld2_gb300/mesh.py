@@ -198,14 +198,29 @@ class MeshVariable:
     def _as_function(self):
         return _fn._MeshVar(self)
 
+    def _interpolate_grad(self, coords):
+        """Global gradients at points: [n, k*dim], row-major (d v_i / d x_j at i*dim + j)."""
+        if not isinstance(self.mesh, FeMesh_Cartesian):
+            raise ValueError("gradients are provided for velocity-mesh variables")
+        ctx = self.mesh.ctx
+        _, g = ctx.interpolate_field(coords.contiguous(), self._to_device(), self.nodeDofCount, grad=True)
+        return g.reshape(g.shape[0], -1)
+
+    @property
+    def fn_gradient(self):
+        """Function of the gradient field (P/mesh/_meshvariable.py:184-225): [dT/dx, dT/dy(, dT/dz)]
+        for a scalar, the row-major tensor [dv_x/dx, dv_x/dy, ..., dv_z/dz] for a vector."""
+        return _fn._MeshGrad(self)
+
+    def evaluate(self, inputData=None, inputType=None):
+        return self._as_function().evaluate(inputData, inputType)
+
     def _interpolate(self, coords):
         """Field values at global points (device tensor [n, dim] -> [n, k])."""
         ctx = self._primary().ctx
         if isinstance(self.mesh, FeMesh_Cartesian):
-            if self.nodeDofCount != self.mesh.dim:
-                raise ValueError("interpolation of velocity-mesh fields needs dim components")
             dev = self._to_device()
-            return ctx.interpolate(coords.contiguous(), dev)
+            return ctx.interpolate_field(coords.contiguous(), dev, self.nodeDofCount)[0]
         own = ctx.locate(coords.contiguous()).long()
         vals = torch.from_numpy(self._data).to(ctx.device)
         npn = self.mesh._npn
