@@ -235,6 +235,26 @@ int uwg_max_dt(uwg_ctx* ctx, const double* vel, double* dt_h);
 int uwg_interpolate_field(uwg_ctx* ctx, int64_t n, const double* pts, const double* field, int ncomp, double* out,
                           double* grad);
 
+/* ---- Particle deletion and creation ----------------------------------------
+ * Two-step: a plan replays the reference's sequential swarm edits on the host
+ * and reports the new particle count; uwg_pop_apply then writes the new
+ * particle arrays (caller-allocated for np_new particles, cell offsets for
+ * n_el+1) and src_h[np_new], the old index whose swarm-variable data each new
+ * particle carries.  Escaped removal replaces EscapedRoutine_RemoveFromSwarm
+ * (L/PICellerator/PopulationControl/src/EscapedRoutine.c:174-284, called from
+ * P/swarm/_swarm.py:644); PCDVC replaces the population control of
+ * _PCDVC_Calculate2D/3D (L/PICellerator/Utils/src/PCDVC.c:313-1084, the
+ * non-aggressive path) behind PopulationControl.repopulate
+ * (P/swarm/_population_control.py:82-93); ip_w (and, at apply, ip_xi) are the
+ * uwg_dvc_weights outputs of the current cell tables. */
+int uwg_pop_plan_escaped(uwg_ctx* ctx, int64_t np, const int32_t* owner, const int32_t* cell_offsets,
+                         const int32_t* cell_list, int64_t* np_new_h);
+int uwg_pop_plan_pcdvc(uwg_ctx* ctx, int64_t np, const int32_t* owner, const int32_t* cell_offsets,
+                       const int32_t* cell_list, const double* ip_w, double split_threshold, double delete_threshold,
+                       int max_splits, int max_deletions, int64_t* np_new_h, int64_t* n_split_h, int64_t* n_deleted_h);
+int uwg_pop_apply(uwg_ctx* ctx, const double* ip_xi, const double* x_old, double* x_new, int32_t* owner_new,
+                  int32_t* cell_offsets_new, int32_t* cell_list_new, int64_t* src_h);
+
 /* ---- SUPG advection-diffusion of a nodal scalar (Q1 meshes) ----------------
  * One time step of the explicit predictor-multicorrector with SUPG residual and
  * lumped mass.  Replaces _AdvectionDiffusionSLE_Execute for the SUPG method

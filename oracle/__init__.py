@@ -71,6 +71,7 @@ def lib():
             "uwo_interpolate": (ctypes.c_int, [M, _P, _P, _P, _P, _P, _P]),
             "uwo_rk2": (None, [M, _P, _P, _P, _P, ctypes.c_double, _I64, _I64, _P, _P]),
             "uwo_slcn_phistar": (ctypes.c_int, [M, _P, _P, _P, _P, _P, ctypes.c_double, ctypes.c_double, _P]),
+            "uwo_local_to_global": (None, [M, _P, _P, _P, _I64, _P, _P]),
             "uwo_sys_create": (_P, [ctypes.c_int, _P, _P, _P, _P]),
             "uwo_sys_destroy": (None, [_P]),
             "uwo_sys_set_bc": (None, [_P, _P, _P]),
@@ -243,6 +244,12 @@ class Mesh:
         self.L.uwo_rk2(ctypes.byref(self._c), *self._ax(), _p(np.ascontiguousarray(vel, np.float64)),
                        float(dt), 0, len(coords), _p(coords), _p(counts))
         return coords, counts
+
+    def local_to_global(self, el, xi):
+        x = np.zeros(3)
+        self.L.uwo_local_to_global(ctypes.byref(self._c), *self._ax(), int(el),
+                                   _p(np.ascontiguousarray(xi, np.float64)), _p(x))
+        return x[: self.dim]
 
     def min_sep(self):
         """Mesh minimum separation: the closest adjacent node pair along an axis."""

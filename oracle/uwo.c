@@ -920,3 +920,10 @@ int uwo_slcn_phistar(const uwo_mesh* m, const double* ax0, const double* ax1, co
     }
     return 0;
 }
+
+/* FeMesh_CoordLocalToGlobal (L/StgFEM/Discretisation/src/FeMesh.c:333-360). */
+void uwo_local_to_global(const uwo_mesh* m, const double* ax0, const double* ax1, const double* ax2,
+                         int64_t el, const double* xi, double* x) {
+    const double* ax[3] = {ax0, ax1, ax2};
+    local_to_global(m, ax, el, xi, x);
+}

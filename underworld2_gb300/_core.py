@@ -111,6 +111,31 @@ class Context:
         self._call("uwg_dvc_weights", int(res), _ptr(off), _ptr(ip_xi), _ptr(ip_w))
         return ip_w
 
+    # -- particle deletion and creation ---------------------------------------
+    def pop_plan_escaped(self, owner, off, lst):
+        n = ctypes.c_int64(0)
+        self._call("uwg_pop_plan_escaped", owner.shape[0], _ptr(owner), _ptr(off), _ptr(lst), ctypes.byref(n))
+        return n.value
+
+    def pop_plan_pcdvc(self, owner, off, lst, ip_w, split_threshold, delete_threshold, max_splits, max_deletions):
+        n, ns, nd = ctypes.c_int64(0), ctypes.c_int64(0), ctypes.c_int64(0)
+        self._call("uwg_pop_plan_pcdvc", owner.shape[0], _ptr(owner), _ptr(off), _ptr(lst), _ptr(ip_w),
+                   float(split_threshold), float(delete_threshold), int(max_splits), int(max_deletions),
+                   ctypes.byref(n), ctypes.byref(ns), ctypes.byref(nd))
+        return n.value, ns.value, nd.value
+
+    def pop_apply(self, ip_xi, x_old, np_new):
+        """Apply the pending plan: new (x, owner, cell_offsets, cell_list) and the
+        old index whose data each new particle carries (host int64)."""
+        x = self.zeros(np_new, self.dim)
+        owner = self.zeros(np_new, dtype=torch.int32)
+        off = self.zeros(self.n_el + 1, dtype=torch.int32)
+        lst = self.zeros(np_new, dtype=torch.int32)
+        src = np.zeros(np_new, np.int64)
+        self._call("uwg_pop_apply", _ptr(ip_xi), _ptr(x_old), _ptr(x), _ptr(owner), _ptr(off), _ptr(lst),
+                   ctypes.c_void_p(src.ctypes.data))
+        return x, owner, off, lst, src
+
     # -- assembly and solve ----------------------------------------------------
     def set_bcs(self, mask, values=None):
         mask = mask.to(self.device, torch.uint8).contiguous()

@@ -91,6 +91,10 @@ SIGNATURES = {
     "uwg_advdiff_max_dt": (_I, [_CTX, _P, _P, _D, ctypes.POINTER(_D)]),
     "uwg_slcn_phistar": (_I, [_CTX, _D, _P, _P, _P]),
     "uwg_interpolate_field": (_I, [_CTX, ctypes.c_int64, _P, _P, _I, _P, _P]),
+    "uwg_pop_plan_escaped": (_I, [_CTX, _I64, _P, _P, _P, ctypes.POINTER(_I64)]),
+    "uwg_pop_plan_pcdvc": (_I, [_CTX, _I64, _P, _P, _P, _P, _D, _D, _I, _I, ctypes.POINTER(_I64),
+                                ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
+    "uwg_pop_apply": (_I, [_CTX, _P, _P, _P, _P, _P, _P, _P]),
     "uwg_slcn_solve": (_I, [_CTX, _D, _P, _P, _P, _P, _P, _D, _I, ctypes.POINTER(_I), ctypes.POINTER(_D)]),
 }
 

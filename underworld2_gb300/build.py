@@ -19,7 +19,7 @@ LIB = os.path.join(BUILD, "libuwg.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
           "-Xcompiler", "-O2", "--expt-relaxed-constexpr"]
-EXACT = {"uwg_particles.cu", "uwg_dvc.cu"}
+EXACT = {"uwg_particles.cu", "uwg_dvc.cu", "uwg_population.cu"}
 
 
 def nvcc():

@@ -35,6 +35,7 @@ extern "C" void uwg_ctx_destroy(uwg_ctx* c) {
     cudaFree(c->f); cudaFree(c->h); cudaFree(c->Shat); cudaFree(c->Mp); cudaFree(c->bcval);
     cudaFree(c->red);
     if (c->slcn_ws) cudaFree(c->slcn_ws);
+    uwg_pop_free(c);
     if (c->red_host) cudaFreeHost(c->red_host);
     uwg_solver_free(c);
     delete c;

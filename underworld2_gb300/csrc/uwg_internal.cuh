@@ -64,11 +64,13 @@ struct uwg_ctx {
     double* red_host;       // pinned host mirror
     std::vector<void*> ws;  // solver workspaces (freed with the context)
     double* slcn_ws;        // SLCN element matrices and CG vectors (grown on demand)
+    void* pop;              // pending population plan (uwg_population.cu)
     size_t slcn_ws_bytes;
 };
 
 // Error helpers --------------------------------------------------------------
 int uwg_set_error(uwg_ctx* c, int code, const std::string& msg);
+void uwg_pop_free(uwg_ctx* c);
 #define UWG_CUDA(c, call)                                                                   \
     do {                                                                                     \
         cudaError_t _e = (call);                                                             \

@@ -1,10 +1,12 @@
 """Particle swarms on the GPU (``uw.swarm`` subset).
 
 The particle state -- coordinates, owning element and the per-element cell
-tables -- lives on the device.  Particle index order never changes (no
-particle deletion), so swarm variables are plain arrays indexed by particle.
+tables -- lives on the device; swarm variables are arrays indexed by particle.
+Particles are deleted and created with the reference's array semantics
+(escaped-particle removal, population control), which reorder the particle
+index; swarm-variable rows follow their particles.
 Reference: P/swarm/_swarm.py, P/swarm/_swarmabstract.py, P/swarm/layouts.py,
-P/swarm/_integration_swarm.py.
+P/swarm/_integration_swarm.py, P/swarm/_population_control.py.
 """
 import contextlib
 
@@ -153,8 +155,28 @@ class Swarm:
         n0 = self.particleLocalCount
         ret = np.full(len(coordinatesArray), -1, dtype=np.int32)
         ret[keep.cpu().numpy()] = np.arange(n0, n0 + int(keep.sum()), dtype=np.int32)
-        x = kept if self._x is None else torch.cat([self._x, kept])
-        self._set_particles(x, rebuild=True)
+        if self._x is None or n0 == 0:
+            self._set_particles(kept, rebuild=True)
+            return ret
+        # Swarm_AddParticleToCell: each new particle is appended to its element's
+        # table, in array order, after the particles already there
+        n_in = int(self._off[-1])
+        old_lst = self._lst[:n_in].long()
+        old_cells = self._owner.long()[old_lst]
+        new_cells = own[keep].long()
+        keys = torch.cat([old_cells, new_cells])
+        vals = torch.cat([old_lst, torch.arange(n0, n0 + kept.shape[0], device=ctx.device)])
+        order = torch.argsort(keys, stable=True)
+        counts = torch.bincount(keys, minlength=ctx.n_el)[: ctx.n_el]
+        off = torch.zeros(ctx.n_el + 1, dtype=torch.int32, device=ctx.device)
+        off[1:] = torch.cumsum(counts, 0).to(torch.int32)
+        x = torch.cat([self._x, kept])
+        owner = torch.cat([self._owner, own[keep].to(torch.int32)])
+        lst = vals[order].to(torch.int32)
+        pad = x.shape[0] - lst.shape[0]
+        if pad:
+            lst = torch.cat([lst, torch.zeros(pad, dtype=torch.int32, device=ctx.device)])
+        self._set_particles(x, owner, off, lst.contiguous())
         return ret
 
     def _set_particles(self, x, owner=None, off=None, lst=None, rebuild=False):
@@ -197,15 +219,30 @@ class Swarm:
                 self.update_particle_owners()
 
     def update_particle_owners(self):
-        """Swarm_UpdateAllParticleOwners with the reference's escape check (P/swarm/_swarm.py:613-654)."""
-        lost = self.mesh.ctx.update_owners(self._x, self._owner, self._off, self._lst)
+        """Swarm_UpdateAllParticleOwners, then EscapedRoutine_RemoveFromSwarm: particles
+        outside the mesh are deleted, and that is an error unless particleEscape is set
+        (P/swarm/_swarm.py:613-654)."""
+        ctx = self.mesh.ctx
+        lost = ctx.update_owners(self._x, self._owner, self._off, self._lst)
+        if lost:
+            np_new = ctx.pop_plan_escaped(self._owner, self._off, self._lst)
+            self._apply_population(np_new, None)
+        self._host_x = None
+        self._toggle_state()
         if lost and not self.particleEscape:
             raise RuntimeError("Particles appear to have left the domain, but swarm flag `particleEscape` is False. "
                                "Check your velocity field or your particle relocation routines, or set the "
                                "`particleEscape` swarm constructor parameter to True to allow escape.")
-        self._host_x = None
-        self._toggle_state()
         return lost
+
+    def _apply_population(self, np_new, ip_xi):
+        """Write the library's pending deletion/creation plan into the particle arrays."""
+        x, owner, off, lst, src = self.mesh.ctx.pop_apply(ip_xi, self._x, np_new)
+        for v in self._variables:
+            v._data = np.ascontiguousarray(v._data[src])
+            v._dirty = True
+        self._x, self._owner, self._off, self._lst = x, owner, off, lst
+        self._host_x = None
 
     # -- the PIC integration swarm ---------------------------------------------
     @property
@@ -251,6 +288,62 @@ class VoronoiIntegrationSwarm:
             lo, hi = ax[idx[d]], ax[idx[d] + 1]
             out[:, d] = lo + (self.ip_xi[:n, d] + 1.0) * 0.5 * (hi - lo)
         return out
+
+
+class PopulationControl:
+    """Per-element population control with discrete Voronoi volumes
+    (P/swarm/_population_control.py:14-93; PCDVC.c): particles whose Voronoi
+    volume fraction of their element exceeds ``splitThreshold`` are split (at
+    most ``maxSplits`` per element, the copy placed at the centroid of the
+    particle's Voronoi cell), those below ``deleteThreshold`` are deleted (at
+    most ``maxDeletions`` per element)."""
+
+    def __init__(self, swarm, deleteThreshold=0.006, splitThreshold=0.25, maxDeletions=0, maxSplits=3,
+                 aggressive=False, aggressiveThreshold=0.8, particlesPerCell=None, **kwargs):
+        if not isinstance(swarm, Swarm):
+            raise TypeError("Provided 'swarm' must be of 'Swarm' class.")
+        if not isinstance(deleteThreshold, (int, float)):
+            raise TypeError("'deleteThreshold' parameter must of type 'float'.")
+        if deleteThreshold < 0.0 or deleteThreshold > 1.0:
+            raise ValueError("'deleteThreshold' parameter must take values in [0.,1.].")
+        if not isinstance(splitThreshold, (int, float)):
+            raise TypeError("'splitThreshold' parameter must of type 'float'.")
+        if splitThreshold < 0.0 or splitThreshold > 1.0:
+            raise ValueError("'splitThreshold' parameter must take values in [0.,1.].")
+        if deleteThreshold > splitThreshold:
+            raise ValueError("'deleteThreshold' must be less than 'splitThreshold'.")
+        if not isinstance(maxDeletions, int):
+            raise TypeError("'maxDeletions' parameter must of type 'int'.")
+        if maxDeletions < 0:
+            raise ValueError("'maxDeletions' parameter must take non-negative values.")
+        if not isinstance(maxSplits, int):
+            raise TypeError("'maxSplits' parameter must of type 'int'.")
+        if maxSplits < 0:
+            raise ValueError("'maxSplits' parameter must take non-negative values.")
+        if not isinstance(aggressive, bool):
+            raise TypeError("'aggressive' parameter must of type 'bool'.")
+        if aggressive:
+            raise NotImplementedError("aggressive population control draws from the C library's rand() stream; "
+                                      "it is not provided on the GPU path")
+        self._swarm = swarm
+        self.deleteThreshold, self.splitThreshold = float(deleteThreshold), float(splitThreshold)
+        self.maxDeletions, self.maxSplits = maxDeletions, maxSplits
+        self.last = None
+
+    def repopulate(self):
+        """Split and delete particles; the swarm's state changes (its integration swarm is re-mapped)."""
+        s = self._swarm
+        if s.particleLocalCount == 0:
+            return
+        ctx = s.mesh.ctx
+        ip_xi = ctx.pic_map(s._x, s._off, s._lst)
+        ip_w = ctx.dvc_weights(s._off, ip_xi, 15)
+        np_new, ns, nd = ctx.pop_plan_pcdvc(s._owner, s._off, s._lst, ip_w, self.splitThreshold,
+                                            self.deleteThreshold, self.maxSplits, self.maxDeletions)
+        if ns or nd:
+            s._apply_population(np_new, ip_xi)
+        self.last = {"splits": ns, "deletions": nd}
+        s._toggle_state()
 
 
 class _ParticleLayoutAbstract:
