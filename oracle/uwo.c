@@ -173,28 +173,38 @@ static void q2_2d(const double* l, double* N, double (*G)[27]) {
     }
 }
 
-/* Triquadratic basis (L/StgFEM/Discretisation/src/Triquadratic.c:193-400):
- * products of the 1D quadratics {0.5 s (s-1), 1 - s^2, 0.5 s (s+1)}, with
- * derivatives from the product rule.  Only used for assembly (tolerance
- * parity); the bit-exact Newton path is exercised on Q1 meshes. */
-static void quad1d(double s, double* v, double* dv) {
-    v[0] = 0.5 * s * (s - 1.0); v[1] = 1.0 - s * s; v[2] = 0.5 * s * (s + 1.0);
-    dv[0] = s - 0.5; dv[1] = -2.0 * s; dv[2] = s + 0.5;
-}
+/* Triquadratic basis (L/StgFEM/Discretisation/src/Triquadratic.c:193-400).
+ * Node n = a + 3b + 9c; basis = m * A_a * B_b * C_c with A = {xi-1, 1-xi^2,
+ * xi+1} (B, C likewise) and m the reference's m0..m6: the product of the
+ * 1/2-scaled coordinates of the axes on which the node is a corner node.  A
+ * derivative swaps one factor for {xi-1/2, -2xi, xi+1/2} and keeps the m
+ * factor of the other two axes.  Products are formed in the reference's order. */
 static void q2_3d(const double* l, double* N, double (*G)[27]) {
-    double vx[3], vy[3], vz[3], dx[3], dy[3], dz[3];
-    quad1d(l[0], vx, dx); quad1d(l[1], vy, dy); quad1d(l[2], vz, dz);
-    int n = 0;
-    for (int c = 0; c < 3; c++)
-        for (int b = 0; b < 3; b++)
-            for (int a = 0; a < 3; a++, n++) {
-                N[n] = vx[a] * vy[b] * vz[c];
-                if (G) {
-                    G[0][n] = dx[a] * vy[b] * vz[c];
-                    G[1][n] = vx[a] * dy[b] * vz[c];
-                    G[2][n] = vx[a] * vy[b] * dz[c];
-                }
-            }
+    double xi = l[0], eta = l[1], zeta = l[2];
+    double A[3] = {xi - 1.0, 1.0 - xi * xi, xi + 1.0};
+    double B[3] = {eta - 1.0, 1.0 - eta * eta, eta + 1.0};
+    double C[3] = {zeta - 1.0, 1.0 - zeta * zeta, zeta + 1.0};
+    double dA[3] = {xi - 0.5, -2.0 * xi, xi + 0.5};
+    double dB[3] = {eta - 0.5, -2.0 * eta, eta + 0.5};
+    double dC[3] = {zeta - 0.5, -2.0 * zeta, zeta + 0.5};
+    double m0 = 0.5 * xi, m1 = 0.5 * eta, m2 = 0.5 * zeta;
+    double m3 = 0.25 * xi * eta, m4 = 0.25 * xi * zeta, m5 = 0.25 * eta * zeta;
+    double m6 = 0.125 * xi * eta * zeta;
+    /* m for the corner-axis set (x: 4, y: 2, z: 1) */
+    double mfull[8] = {1.0, m2, m1, m5, m0, m4, m3, m6};
+    for (int n = 0; n < 27; n++) {
+        int a = n % 3, b = (n / 3) % 3, c = n / 9;
+        int ex = a != 1, ey = b != 1, ez = c != 1;
+        int sel = ex * 4 + ey * 2 + ez;
+        N[n] = sel ? mfull[sel] * A[a] * B[b] * C[c] : A[a] * B[b] * C[c];
+        if (!G) continue;
+        double myz = ey && ez ? m5 : ey ? m1 : ez ? m2 : 0.0;
+        double mxz = ex && ez ? m4 : ex ? m0 : ez ? m2 : 0.0;
+        double mxy = ex && ey ? m3 : ex ? m0 : ey ? m1 : 0.0;
+        G[0][n] = (ey || ez) ? dA[a] * myz * B[b] * C[c] : dA[a] * B[b] * C[c];
+        G[1][n] = (ex || ez) ? dB[b] * mxz * A[a] * C[c] : dB[b] * A[a] * C[c];
+        G[2][n] = (ex || ey) ? dC[c] * mxy * A[a] * B[b] : dC[c] * A[a] * B[b];
+    }
 }
 
 void uwo_shape(int dim, int order, const double* xi, double* N, double* G /* [3][27] */) {

@@ -59,8 +59,8 @@ extern "C" int uwg_ctx_create(const uwg_mesh_desc* d, uwg_ctx** out) {
     if (!d || !out) return UWG_ERR_ARG;
     *out = nullptr;
     if (d->dim != 2 && d->dim != 3) return UWG_ERR_ARG;
-    // Q1/dQ0 in 2D and 3D, Q2/dPc1 in 2D
-    bool q1 = d->order == 1 && d->porder == 0, q2 = d->dim == 2 && d->order == 2 && d->porder == 1;
+    // Q1/dQ0 and Q2/dPc1, 2D and 3D
+    bool q1 = d->order == 1 && d->porder == 0, q2 = d->order == 2 && d->porder == 1;
     if (!q1 && !q2) return UWG_ERR_ARG;
     for (int i = 0; i < d->dim; i++)
         if (d->res[i] < 1 || !(d->maxc[i] > d->minc[i])) return UWG_ERR_ARG;
@@ -83,10 +83,10 @@ extern "C" int uwg_ctx_create(const uwg_mesh_desc* d, uwg_ctx** out) {
     for (int i = 0; i < c->dim; i++) nn *= (int64_t)c->res[i] * c->order + 1;
     c->n_nodes = nn;
     c->n_vdof = nn * c->dim;
-    c->nen = c->order == 2 ? 9 : (c->dim == 3 ? 8 : 4);
-    c->npn = c->porder == 1 ? 3 : 1;
+    c->nen = c->order == 2 ? (c->dim == 3 ? 27 : 9) : (c->dim == 3 ? 8 : 4);
+    c->npn = c->porder == 1 ? (c->dim == 3 ? 4 : 3) : 1;
     c->n_pdof = c->n_el * c->npn;
-    c->nq = c->order == 2 ? 25 : (c->dim == 3 ? 27 : 9);
+    c->nq = c->order == 2 ? (c->dim == 3 ? 125 : 25) : (c->dim == 3 ? 27 : 9);
     c->dvc_res = 15;
     c->assembled = false;
     c->red_host = nullptr;
@@ -126,7 +126,7 @@ extern "C" int uwg_ctx_create(const uwg_mesh_desc* d, uwg_ctx** out) {
     for (int l = 0; l < nlev && ok; l++) {
         uwg_level& L = c->lev[l];
         L.order = (q2lev && l == 0) ? 2 : 1;
-        L.nq = L.order == 2 ? 25 : (c->dim == 3 ? 27 : 9);
+        L.nq = L.order == 2 ? (c->dim == 3 ? 125 : 25) : (c->dim == 3 ? 27 : 9);
         const int shift = q2lev ? std::max(l - 1, 0) : l;
         int64_t ne = 1, nnod = 1;
         for (int i = 0; i < 3; i++) {

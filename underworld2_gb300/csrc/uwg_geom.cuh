@@ -116,6 +116,67 @@ template <> struct Shape<2, 2> {
     }
 };
 
+// Triquadratic: L/StgFEM/Discretisation/src/Triquadratic.c:193-400.  Node n =
+// a + 3b + 9c (x fastest); basis = m * A_a * B_b * C_c where A_0 = xi - 1,
+// A_1 = 1 - xi^2, A_2 = xi + 1 (B, C likewise) and m is the product of the
+// 1/2-scaled coordinates of the axes on which the node is a corner node
+// (m0..m6 of the reference); derivatives replace one factor by its derivative
+// (xi - 1/2, -2 xi, xi + 1/2) and keep the other axes' m factor.  Same products
+// in the same order as the reference.
+template <> struct Shape<3, 2> {
+    static constexpr int NEN = 27;
+    __device__ static void N(const double* l, double* n) {
+        const double xi = l[0], eta = l[1], zeta = l[2];
+        const double A[3] = {xi - 1.0, 1.0 - xi * xi, xi + 1.0};
+        const double B[3] = {eta - 1.0, 1.0 - eta * eta, eta + 1.0};
+        const double C[3] = {zeta - 1.0, 1.0 - zeta * zeta, zeta + 1.0};
+        const double m0 = 0.5 * xi, m1 = 0.5 * eta, m2 = 0.5 * zeta;
+        const double m3 = 0.25 * xi * eta, m4 = 0.25 * xi * zeta, m5 = 0.25 * eta * zeta;
+        const double m6 = 0.125 * xi * eta * zeta;
+#pragma unroll
+        for (int k = 0; k < 27; k++) {
+            const int a = k % 3, b = (k / 3) % 3, c = k / 9;
+            const bool ex = a != 1, ey = b != 1, ez = c != 1;
+            const int sel = (ex ? 4 : 0) | (ey ? 2 : 0) | (ez ? 1 : 0);
+            if (sel == 0) n[k] = A[a] * B[b] * C[c];
+            else {
+                const double m = sel == 7 ? m6 : sel == 3 ? m5 : sel == 5 ? m4 : sel == 6 ? m3
+                               : sel == 1 ? m2 : sel == 2 ? m1 : m0;
+                n[k] = m * A[a] * B[b] * C[c];
+            }
+        }
+    }
+    __device__ static void dN(const double* l, double (*g)[NEN]) {
+        const double xi = l[0], eta = l[1], zeta = l[2];
+        const double A[3] = {xi - 1.0, 1.0 - xi * xi, xi + 1.0};
+        const double B[3] = {eta - 1.0, 1.0 - eta * eta, eta + 1.0};
+        const double C[3] = {zeta - 1.0, 1.0 - zeta * zeta, zeta + 1.0};
+        const double dA[3] = {xi - 0.5, -2.0 * xi, xi + 0.5};
+        const double dB[3] = {eta - 0.5, -2.0 * eta, eta + 0.5};
+        const double dC[3] = {zeta - 0.5, -2.0 * zeta, zeta + 0.5};
+        const double m0 = 0.5 * xi, m1 = 0.5 * eta, m2 = 0.5 * zeta;
+        const double m3 = 0.25 * xi * eta, m4 = 0.25 * xi * zeta, m5 = 0.25 * eta * zeta;
+#pragma unroll
+        for (int k = 0; k < 27; k++) {
+            const int a = k % 3, b = (k / 3) % 3, c = k / 9;
+            const bool ex = a != 1, ey = b != 1, ez = c != 1;
+            // d/dxi: m over (y, z); d/deta: m over (x, z); d/dzeta: m over (x, y)
+            if (ey && ez) g[0][k] = dA[a] * m5 * B[b] * C[c];
+            else if (ey) g[0][k] = dA[a] * m1 * B[b] * C[c];
+            else if (ez) g[0][k] = dA[a] * m2 * B[b] * C[c];
+            else g[0][k] = dA[a] * B[b] * C[c];
+            if (ex && ez) g[1][k] = dB[b] * m4 * A[a] * C[c];
+            else if (ex) g[1][k] = dB[b] * m0 * A[a] * C[c];
+            else if (ez) g[1][k] = dB[b] * m2 * A[a] * C[c];
+            else g[1][k] = dB[b] * A[a] * C[c];
+            if (ex && ey) g[2][k] = dC[c] * m3 * A[a] * B[b];
+            else if (ex) g[2][k] = dC[c] * m0 * A[a] * B[b];
+            else if (ey) g[2][k] = dC[c] * m1 * A[a] * B[b];
+            else g[2][k] = dC[c] * A[a] * B[b];
+        }
+    }
+};
+
 // Element node coordinate (local node n, axis d) of element (ex,ey,ez), x fastest.
 template <int DIM, int ORDER>
 __device__ __forceinline__ double node_coord(const uwg_geom& g, const int* eidx, int n, int d) {

@@ -48,7 +48,7 @@ int uwg_ops_cell_prolong_add(uwg_ctx* c, int lc, const double* xc, double* xf);
 int uwg_ops_apply_C(uwg_ctx* c, const double* p, double* q);     // q = Mp p (compressibility)
 int uwg_ops_element_matrices(uwg_ctx* c, int64_t el, double* Ke, double* fe, double* Ge, double* Se);
 
-// 2D Q2/dPc1 (uwg_q2.cu): level 0 operators of Q2 contexts
+// Q2/dPc1 (uwg_q2.cu): level 0 operators of Q2 contexts
 int uwg_q2_init(uwg_ctx* c);
 int uwg_q2_assemble(uwg_ctx* c, const int32_t* off, const int32_t* list, const double* ip_xi, const double* ip_w,
                     const double* eta_p, const double* body_p);
@@ -58,6 +58,16 @@ int uwg_q2_applyG(uwg_ctx* c, const double* p, double* y);
 int uwg_q2_applyGt(uwg_ctx* c, const double* u, double* q, int only_bc);
 int uwg_q2_schur_pc(uwg_ctx* c, const double* r, double* z);
 int uwg_q2_element_matrices(uwg_ctx* c, int64_t el, double* Ke, double* Ge, double* Se);
+// 3D Q2/dPc1 (uwg_q2_3d.cu), dispatched from the uwg_q2_* entry points
+int uwg_q2_3d_init(uwg_ctx* c);
+int uwg_q2_3d_assemble(uwg_ctx* c, const int32_t* off, const int32_t* list, const double* ip_xi, const double* ip_w,
+                       const double* eta_p, const double* body_p);
+template <typename T> int uwg_q2_3d_applyK(uwg_ctx* c, const T* x, T* y, bool mask_in);
+int uwg_q2_3d_diag(uwg_ctx* c, double* sinv);
+int uwg_q2_3d_applyG(uwg_ctx* c, const double* p, double* y);
+int uwg_q2_3d_applyGt(uwg_ctx* c, const double* u, double* q, int only_bc);
+int uwg_q2_3d_schur_pc(uwg_ctx* c, const double* r, double* z);
+int uwg_q2_3d_element_matrices(uwg_ctx* c, int64_t el, double* Ke, double* Ge, double* Se);
 
 int uwg_ops_dense_invert(uwg_ctx* c, int64_t n, double* A, double* B);   // B = A^-1 (A destroyed)
 int uwg_ops_to_f32(uwg_ctx* c, int64_t n, const double* a, float* b);

@@ -324,6 +324,7 @@ static inline unsigned nblk(int64_t n, int t = 256) { return (unsigned)((n + t -
         if ((c)->dim == 2 && (c)->order == 1) { CALL(2, 1); }                   \
         else if ((c)->dim == 3 && (c)->order == 1) { CALL(3, 1); }              \
         else if ((c)->dim == 2 && (c)->order == 2) { CALL(2, 2); }              \
+        else if ((c)->dim == 3 && (c)->order == 2) { CALL(3, 2); }              \
         else return uwg_set_error(c, UWG_ERR_ARG, "element type not supported"); \
     } while (0)
 

@@ -317,7 +317,8 @@ extern "C" int uwg_pop_apply(uwg_ctx* c, const double* ip_xi, const double* x_ol
             uwg_geom g = pop_geom(c);
             if (c->dim == 2 && c->order == 1) k_pop_new_coords<2, 1><<<nblk(nn), 256, 0, c->stream>>>(g, nn, d_idx, d_cell, d_slot, ip_xi, x_new);
             else if (c->dim == 3 && c->order == 1) k_pop_new_coords<3, 1><<<nblk(nn), 256, 0, c->stream>>>(g, nn, d_idx, d_cell, d_slot, ip_xi, x_new);
-            else k_pop_new_coords<2, 2><<<nblk(nn), 256, 0, c->stream>>>(g, nn, d_idx, d_cell, d_slot, ip_xi, x_new);
+            else if (c->dim == 2) k_pop_new_coords<2, 2><<<nblk(nn), 256, 0, c->stream>>>(g, nn, d_idx, d_cell, d_slot, ip_xi, x_new);
+            else k_pop_new_coords<3, 2><<<nblk(nn), 256, 0, c->stream>>>(g, nn, d_idx, d_cell, d_slot, ip_xi, x_new);
             e = cudaGetLastError();
         }
     }

@@ -362,6 +362,7 @@ void q2_1d_host(double s, double* N, double* D) {
 // Host wrappers
 // ---------------------------------------------------------------------------
 int uwg_q2_init(uwg_ctx* c) {
+    if (c->dim == 3) return uwg_q2_3d_init(c);
     // reference gradient integrals with the 3-point Gauss rule (exact: degree <= 3 per axis)
     const double gp[3] = {-std::sqrt(0.6), 0.0, std::sqrt(0.6)}, gw[3] = {5.0 / 9.0, 8.0 / 9.0, 5.0 / 9.0};
     double GR[2][9][3] = {};
@@ -384,6 +385,7 @@ int uwg_q2_init(uwg_ctx* c) {
 
 int uwg_q2_assemble(uwg_ctx* c, const int32_t* off, const int32_t* list, const double* ip_xi, const double* ip_w,
                     const double* eta_p, const double* body_p) {
+    if (c->dim == 3) return uwg_q2_3d_assemble(c, off, list, ip_xi, ip_w, eta_p, body_p);
     uwg_lgeom g = uwg_level_geom(c, 0);
     vk_zero<double>(c->stream, c->n_vdof, c->f);
     k_assemble_q2<<<nblk(c->n_el, 128), 128, 0, c->stream>>>(g, off, list, ip_xi, ip_w, eta_p, body_p, c->lev[0].W64,
@@ -394,6 +396,7 @@ int uwg_q2_assemble(uwg_ctx* c, const int32_t* off, const int32_t* list, const d
 
 template <typename T>
 int uwg_q2_applyK(uwg_ctx* c, const T* x, T* y, bool mask_in) {
+    if (c->dim == 3) return uwg_q2_3d_applyK<T>(c, x, y, mask_in);
     const uwg_level& L = c->lev[0];
     const T* W;
     if constexpr (sizeof(T) == 8) W = (const T*)L.W64; else W = (const T*)L.W32;
@@ -405,6 +408,7 @@ template int uwg_q2_applyK<double>(uwg_ctx*, const double*, double*, bool);
 template int uwg_q2_applyK<float>(uwg_ctx*, const float*, float*, bool);
 
 int uwg_q2_diag(uwg_ctx* c, double* sinv) {
+    if (c->dim == 3) return uwg_q2_3d_diag(c, sinv);
     const uwg_level& L = c->lev[0];
     k_diag_q2<<<nblk(L.n_el), 256, 0, c->stream>>>(uwg_level_geom(c, 0), L.W64, L.bc, L.diag64, sinv);
     UWG_CUDA(c, cudaGetLastError());
@@ -412,6 +416,7 @@ int uwg_q2_diag(uwg_ctx* c, double* sinv) {
 }
 
 int uwg_q2_applyG(uwg_ctx* c, const double* p, double* y) {
+    if (c->dim == 3) return uwg_q2_3d_applyG(c, p, y);
     vk_zero<double>(c->stream, c->n_vdof, y);
     k_applyG_q2<<<nblk(c->n_el), 256, 0, c->stream>>>(uwg_level_geom(c, 0), c->bc, p, y);
     UWG_CUDA(c, cudaGetLastError());
@@ -419,18 +424,21 @@ int uwg_q2_applyG(uwg_ctx* c, const double* p, double* y) {
 }
 
 int uwg_q2_applyGt(uwg_ctx* c, const double* u, double* q, int only_bc) {
+    if (c->dim == 3) return uwg_q2_3d_applyGt(c, u, q, only_bc);
     k_applyGt_q2<<<nblk(c->n_el), 256, 0, c->stream>>>(uwg_level_geom(c, 0), c->bc, only_bc, u, q);
     UWG_CUDA(c, cudaGetLastError());
     return UWG_OK;
 }
 
 int uwg_q2_schur_pc(uwg_ctx* c, const double* r, double* z) {
+    if (c->dim == 3) return uwg_q2_3d_schur_pc(c, r, z);
     k_schur_pc_q2<<<nblk(c->n_el), 256, 0, c->stream>>>(c->n_el, c->Shat, r, z);
     UWG_CUDA(c, cudaGetLastError());
     return UWG_OK;
 }
 
 int uwg_q2_element_matrices(uwg_ctx* c, int64_t el, double* Ke, double* Ge, double* Se) {
+    if (c->dim == 3) return uwg_q2_3d_element_matrices(c, el, Ke, Ge, Se);
     double* buf = nullptr;
     const int nk = 18 * 18, ng = 18 * 3, ns = 9;
     UWG_CUDA(c, cudaMallocAsync((void**)&buf, sizeof(double) * (nk + ng + ns), c->stream));

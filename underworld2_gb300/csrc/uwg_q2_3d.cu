@@ -1,0 +1,531 @@
+// 3D Q2/dPc1 operators: triquadratic velocity (27 nodes), linear discontinuous
+// pressure (4 coefficients per element, TrilinearInnerElType.c:202-215).
+//
+// The 2D design carried to 3D:
+// * Viscous operator.  Every entry of the PIC integrand B^T D(eta) B of a Q2
+//   element is a polynomial of degree <= 4 per axis on an affine element, so
+//   5-point tensor Lagrange interpolation on {-1,-1/2,0,1/2,1}^3 reproduces it:
+//       W_j = sum_q eta_q w_q detJ L_j(xi_q)   (125 weights per element),
+//   and K_e u_e is evaluated on that 5x5x5 grid, sum-factorised axis by axis.
+//   Level 1 of the velocity multigrid is the Q1 mesh on the same elements; its
+//   operator is the Galerkin product P^T K P exactly, i.e. the Q1 PIC integral
+//   with the 3-point weights of the same particles.
+// * Gradient: G_e[(A,i)][k] = -int dN_A/dx_i M_k (GradientStiffnessMatrixTerm.c
+//   :189-218) = -(prod_{j != i} h_j/2) times a reference integral, tabulated once.
+// * Schur preconditioner: the reference's Uzawa term S^_e = G_e^T diag(K_e)^-1 G_e
+//   (UzawaPreconditionerTerm.c:124-207), a 4x4 block per element, stored inverted
+//   (the ILU(0) of a block-diagonal matrix is its exact inverse).
+//
+// The apply keeps one element per thread: the element's velocities are staged
+// in shared memory, and each output component is produced in its own pass over
+// the 125 points (gradients are recomputed per pass so that the accumulators of
+// one component, not three, stay in registers).
+#include <cmath>
+#include <vector>
+
+#include "uwg_ops.cuh"
+
+namespace {
+
+inline unsigned nblk(int64_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
+
+// 1D quadratic basis (nodes -1, 0, 1) and its derivative at {-1,-1/2,0,1/2,1}
+__constant__ double c3_B5[5][3] = {{1.0, 0.0, 0.0}, {0.375, 0.75, -0.125}, {0.0, 1.0, 0.0},
+                                   {-0.125, 0.75, 0.375}, {0.0, 0.0, 1.0}};
+__constant__ double c3_D5[5][3] = {{-1.5, 2.0, -0.5}, {-1.0, 1.0, 0.0}, {-0.5, 0.0, 0.5},
+                                   {0.0, -1.0, 1.0}, {0.5, -2.0, 1.5}};
+__constant__ float c3_B5f[5][3] = {{1.0f, 0.0f, 0.0f}, {0.375f, 0.75f, -0.125f}, {0.0f, 1.0f, 0.0f},
+                                   {-0.125f, 0.75f, 0.375f}, {0.0f, 0.0f, 1.0f}};
+__constant__ float c3_D5f[5][3] = {{-1.5f, 2.0f, -0.5f}, {-1.0f, 1.0f, 0.0f}, {-0.5f, 0.0f, 0.5f},
+                                   {0.0f, -1.0f, 1.0f}, {0.5f, -2.0f, 1.5f}};
+// reference gradient integrals: c3_GR[i][A][k] = int dN_A/dxi_i M_k over [-1,1]^3
+__constant__ double c3_GR[3][27][4];
+
+template <typename T> __device__ __forceinline__ T B5(int p, int a);
+template <typename T> __device__ __forceinline__ T D5(int p, int a);
+template <> __device__ __forceinline__ double B5<double>(int p, int a) { return c3_B5[p][a]; }
+template <> __device__ __forceinline__ double D5<double>(int p, int a) { return c3_D5[p][a]; }
+template <> __device__ __forceinline__ float B5<float>(int p, int a) { return c3_B5f[p][a]; }
+template <> __device__ __forceinline__ float D5<float>(int p, int a) { return c3_D5f[p][a]; }
+
+__device__ __forceinline__ void q2e3(const uwg_lgeom& g, int64_t e, int* ex, double* h) {
+    ex[0] = (int)(e % g.res[0]);
+    ex[1] = (int)((e / g.res[0]) % g.res[1]);
+    ex[2] = (int)(e / ((int64_t)g.res[0] * g.res[1]));
+    for (int d = 0; d < 3; d++) h[d] = g.ax[d][2 * ex[d] + 2] - g.ax[d][2 * ex[d]];
+}
+__device__ __forceinline__ int64_t q2node3(const uwg_lgeom& g, const int* ex, int A) {
+    const int a = A % 3, b = (A / 3) % 3, c = A / 9;
+    return (2 * ex[0] + a) + (int64_t)g.nx[0] * ((2 * ex[1] + b) + (int64_t)g.nx[1] * (2 * ex[2] + c));
+}
+
+__device__ __forceinline__ double lag5v(double s, int j) {
+    const double n[5] = {-1.0, -0.5, 0.0, 0.5, 1.0};
+    double v = 1.0;
+#pragma unroll
+    for (int k = 0; k < 5; k++)
+        if (k != j) v *= (s - n[k]) / (n[j] - n[k]);
+    return v;
+}
+__device__ __forceinline__ double lag3v(double s, int j) {
+    return j == 0 ? 0.5 * s * (s - 1.0) : (j == 1 ? 1.0 - s * s : 0.5 * s * (s + 1.0));
+}
+
+// PIC assembly, one warp per element: lane l owns W125 entries l, l+32, l+64,
+// l+96, the Q1 weight l (< 27) and body-force entries l, l+32, l+64 (< 81).
+// The 15 5-point and 9 3-point Lagrange values of each particle are computed by
+// one lane each and broadcast.
+__global__ void k_assemble_q2_3d(uwg_lgeom g, const int32_t* off, const int32_t* list, const double* ip_xi,
+                                 const double* ip_w, const double* eta_p, const double* body_p, double* W125,
+                                 double* W27, double* f) {
+    const int lane = threadIdx.x & 31;
+    const int64_t e = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (e >= g.n_el) return;   // warp-uniform
+    int ex[3];
+    double h[3];
+    q2e3(g, e, ex, h);
+    const double detJ = (h[0] * 0.5) * (h[1] * 0.5) * (h[2] * 0.5);
+    double w125[4] = {0.0, 0.0, 0.0, 0.0}, w27 = 0.0, fe[3] = {0.0, 0.0, 0.0};
+    for (int32_t s = off[e]; s < off[e + 1]; s++) {
+        const int32_t p = list[s];
+        double v = 0.0;
+        if (lane < 15) v = lag5v(ip_xi[(int64_t)s * 3 + lane / 5], lane % 5);
+        else if (lane < 24) v = lag3v(ip_xi[(int64_t)s * 3 + (lane - 15) / 3], (lane - 15) % 3);
+        const double wd = ip_w[s] * detJ, cf = eta_p[p] * wd;
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+            const int j = lane + 32 * m;
+            const int jj = j < 125 ? j : 0;
+            const double lx = __shfl_sync(0xffffffffu, v, jj % 5);
+            const double ly = __shfl_sync(0xffffffffu, v, 5 + (jj / 5) % 5);
+            const double lz = __shfl_sync(0xffffffffu, v, 10 + jj / 25);
+            if (j < 125) w125[m] += cf * lx * ly * lz;
+        }
+        {
+            const int jj = lane < 27 ? lane : 0;
+            const double lx = __shfl_sync(0xffffffffu, v, 15 + jj % 3);
+            const double ly = __shfl_sync(0xffffffffu, v, 18 + (jj / 3) % 3);
+            const double lz = __shfl_sync(0xffffffffu, v, 21 + jj / 9);
+            if (lane < 27) w27 += cf * lx * ly * lz;
+        }
+        if (body_p) {
+#pragma unroll
+            for (int m = 0; m < 3; m++) {
+                const int k = lane + 32 * m;
+                const int A = (k < 81 ? k : 0) / 3;
+                const double nx = __shfl_sync(0xffffffffu, v, 15 + A % 3);
+                const double ny = __shfl_sync(0xffffffffu, v, 18 + (A / 3) % 3);
+                const double nz = __shfl_sync(0xffffffffu, v, 21 + A / 9);
+                if (k < 81) fe[m] += wd * body_p[(int64_t)p * 3 + k % 3] * (nx * ny * nz);
+            }
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < 4; m++)
+        if (lane + 32 * m < 125) W125[(int64_t)(lane + 32 * m) * g.n_el + e] = w125[m];
+    if (lane < 27) W27[(int64_t)lane * g.n_el + e] = w27;
+    if (body_p)
+#pragma unroll
+        for (int m = 0; m < 3; m++) {
+            const int k = lane + 32 * m;
+            if (k < 81) atomicAdd(&f[q2node3(g, ex, k / 3) * 3 + k % 3], fe[m]);
+        }
+}
+
+// y += K x over free dofs, one element per thread (see the file header).
+template <typename T, int BS>
+__global__ void __launch_bounds__(BS) k_applyK_q2_3d(uwg_lgeom g, const T* __restrict__ W,
+                                                     const uint8_t* __restrict__ bc, bool mask_in,
+                                                     const T* __restrict__ x, T* y) {
+    __shared__ T us[81 * BS];
+    const int tid = threadIdx.x;
+    const int64_t e = blockIdx.x * (int64_t)BS + tid;
+    if (e >= g.n_el) return;
+    int ex[3];
+    double h[3];
+    q2e3(g, e, ex, h);
+    const T sxyz[3] = {(T)2 / (T)h[0], (T)2 / (T)h[1], (T)2 / (T)h[2]};
+    uint32_t fixbits[3] = {0u, 0u, 0u};   // bit A of word i: dof (A, i) is Dirichlet
+#pragma unroll 1
+    for (int A = 0; A < 27; A++) {
+        const int64_t n = q2node3(g, ex, A);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const bool fx = bc[n * 3 + c] != 0;
+            if (fx) fixbits[c] |= 1u << A;
+            us[(A * 3 + c) * BS + tid] = (fx && mask_in) ? (T)0 : x[n * 3 + c];
+        }
+    }
+    const T* Wp = W + e;
+    const int64_t st = g.n_el;
+#pragma unroll 1
+    for (int i = 0; i < 3; i++) {
+        T out[27];
+#pragma unroll
+        for (int A = 0; A < 27; A++) out[A] = (T)0;
+#pragma unroll 1
+        for (int r = 0; r < 5; r++) {
+            // z contractions: tz (value along z), sz (z derivative), per component and (a, b)
+            T tz[3][9], sz[3][9];
+#pragma unroll
+            for (int c = 0; c < 3; c++)
+#pragma unroll
+                for (int ab = 0; ab < 9; ab++) {
+                    T tv = 0, sv = 0;
+#pragma unroll
+                    for (int k = 0; k < 3; k++) {
+                        const T u = us[((ab + 9 * k) * 3 + c) * BS + tid];
+                        tv += B5<T>(r, k) * u;
+                        sv += D5<T>(r, k) * u;
+                    }
+                    tz[c][ab] = tv;
+                    sz[c][ab] = sv;
+                }
+            T P1[9], P3[9];
+#pragma unroll
+            for (int k = 0; k < 9; k++) P1[k] = P3[k] = (T)0;
+#pragma unroll 1
+            for (int q = 0; q < 5; q++) {
+                T T1[3][3], T2[3][3], T3[3][3];
+#pragma unroll
+                for (int c = 0; c < 3; c++)
+#pragma unroll
+                    for (int a = 0; a < 3; a++) {
+                        T v1 = 0, v2 = 0, v3 = 0;
+#pragma unroll
+                        for (int b = 0; b < 3; b++) {
+                            v1 += B5<T>(q, b) * tz[c][a + 3 * b];
+                            v2 += D5<T>(q, b) * tz[c][a + 3 * b];
+                            v3 += B5<T>(q, b) * sz[c][a + 3 * b];
+                        }
+                        T1[c][a] = v1;
+                        T2[c][a] = v2;
+                        T3[c][a] = v3;
+                    }
+                T L1[3] = {0, 0, 0}, L2[3] = {0, 0, 0}, L3[3] = {0, 0, 0};
+#pragma unroll
+                for (int p = 0; p < 5; p++) {
+                    T gr[3][3];   // gr[c][j] = d u_c / d x_j
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        T d0 = 0, d1 = 0, d2 = 0;
+#pragma unroll
+                        for (int a = 0; a < 3; a++) {
+                            d0 += D5<T>(p, a) * T1[c][a];
+                            d1 += B5<T>(p, a) * T2[c][a];
+                            d2 += B5<T>(p, a) * T3[c][a];
+                        }
+                        gr[c][0] = sxyz[0] * d0;
+                        gr[c][1] = sxyz[1] * d1;
+                        gr[c][2] = sxyz[2] * d2;
+                    }
+                    const T w = Wp[(int64_t)(p + 5 * q + 25 * r) * st];
+                    // sigma_ij for the output component i, j = 0..2 (selects keep gr in registers)
+                    const T gi0 = i == 0 ? gr[0][0] : (i == 1 ? gr[1][0] : gr[2][0]);
+                    const T gi1 = i == 0 ? gr[0][1] : (i == 1 ? gr[1][1] : gr[2][1]);
+                    const T gi2 = i == 0 ? gr[0][2] : (i == 1 ? gr[1][2] : gr[2][2]);
+                    const T g0i = i == 0 ? gr[0][0] : (i == 1 ? gr[0][1] : gr[0][2]);
+                    const T g1i = i == 0 ? gr[1][0] : (i == 1 ? gr[1][1] : gr[1][2]);
+                    const T g2i = i == 0 ? gr[2][0] : (i == 1 ? gr[2][1] : gr[2][2]);
+                    const T s0 = w * (gi0 + g0i), s1 = w * (gi1 + g1i), s2 = w * (gi2 + g2i);
+#pragma unroll
+                    for (int a = 0; a < 3; a++) {
+                        L1[a] += D5<T>(p, a) * s0;
+                        L2[a] += B5<T>(p, a) * s1;
+                        L3[a] += B5<T>(p, a) * s2;
+                    }
+                }
+#pragma unroll
+                for (int b = 0; b < 3; b++)
+#pragma unroll
+                    for (int a = 0; a < 3; a++) {
+                        P1[a + 3 * b] += B5<T>(q, b) * (sxyz[0] * L1[a]) + D5<T>(q, b) * (sxyz[1] * L2[a]);
+                        P3[a + 3 * b] += B5<T>(q, b) * (sxyz[2] * L3[a]);
+                    }
+            }
+#pragma unroll
+            for (int c = 0; c < 3; c++)
+#pragma unroll
+                for (int ab = 0; ab < 9; ab++) out[ab + 9 * c] += B5<T>(r, c) * P1[ab] + D5<T>(r, c) * P3[ab];
+        }
+#pragma unroll 1
+        const uint32_t fb = i == 0 ? fixbits[0] : (i == 1 ? fixbits[1] : fixbits[2]);
+#pragma unroll
+        for (int A = 0; A < 27; A++)
+            if (!((fb >> A) & 1u)) atomicAdd(&y[q2node3(g, ex, A) * 3 + i], out[A]);
+    }
+}
+
+// G_e[(A,i)][k] = -(prod_{j != i} h_j / 2) GR[i][A][k]
+__device__ __forceinline__ double q2_Ge3(const double* h, int A, int i, int k) {
+    const double f = i == 0 ? (h[1] * 0.5) * (h[2] * 0.5) : (i == 1 ? (h[0] * 0.5) * (h[2] * 0.5) : (h[0] * 0.5) * (h[1] * 0.5));
+    return -f * c3_GR[i][A][k];
+}
+
+// Diagonal of K (assembled over free dofs) and, per element, the inverse of S^_e.
+// diag K_(A,i) = sum_points w (|grad N_A|^2 + (d_i N_A)^2); each of the three
+// squared-derivative sums is a separable contraction of the 125 weights.
+__global__ void k_diag_q2_3d(uwg_lgeom g, const double* W, const uint8_t* bc, double* diag, double* sinv) {
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= g.n_el) return;
+    int ex[3];
+    double h[3];
+    q2e3(g, e, ex, h);
+    const double s2[3] = {4.0 / (h[0] * h[0]), 4.0 / (h[1] * h[1]), 4.0 / (h[2] * h[2])};
+    double kd[27][3];
+    for (int A = 0; A < 27; A++) kd[A][0] = kd[A][1] = kd[A][2] = 0.0;
+    // Dj[A] = sum_points w (d_j N_A / s_j)^2 for j = 0, 1, 2
+    double Dsum[3][27];
+    for (int j = 0; j < 3; j++)
+        for (int A = 0; A < 27; A++) Dsum[j][A] = 0.0;
+    for (int r = 0; r < 5; r++)
+        for (int q = 0; q < 5; q++)
+            for (int p = 0; p < 5; p++) {
+                const double w = W[(int64_t)(p + 5 * q + 25 * r) * g.n_el + e];
+                for (int A = 0; A < 27; A++) {
+                    const int a = A % 3, b = (A / 3) % 3, c = A / 9;
+                    const double bx = c3_B5[p][a], by = c3_B5[q][b], bz = c3_B5[r][c];
+                    const double dx = c3_D5[p][a] * by * bz, dy = bx * c3_D5[q][b] * bz, dz = bx * by * c3_D5[r][c];
+                    Dsum[0][A] += w * dx * dx;
+                    Dsum[1][A] += w * dy * dy;
+                    Dsum[2][A] += w * dz * dz;
+                }
+            }
+    for (int A = 0; A < 27; A++) {
+        const double gsq = s2[0] * Dsum[0][A] + s2[1] * Dsum[1][A] + s2[2] * Dsum[2][A];
+        for (int i = 0; i < 3; i++) kd[A][i] = gsq + s2[i] * Dsum[i][A];
+    }
+    for (int A = 0; A < 27; A++) {
+        const int64_t n = q2node3(g, ex, A);
+        for (int i = 0; i < 3; i++)
+            if (!bc[n * 3 + i]) atomicAdd(&diag[n * 3 + i], kd[A][i]);
+    }
+    if (!sinv) return;
+    double S[4][8];
+    for (int k = 0; k < 4; k++)
+        for (int l = 0; l < 4; l++) {
+            double s = 0.0;
+            for (int A = 0; A < 27; A++)
+                for (int i = 0; i < 3; i++) s += q2_Ge3(h, A, i, k) * (q2_Ge3(h, A, i, l) / kd[A][i]);
+            S[k][l] = s;
+            S[k][4 + l] = k == l ? 1.0 : 0.0;
+        }
+    // Gauss-Jordan with partial pivoting on the 4x4 block
+    for (int col = 0; col < 4; col++) {
+        int piv = col;
+        for (int r = col + 1; r < 4; r++)
+            if (fabs(S[r][col]) > fabs(S[piv][col])) piv = r;
+        if (piv != col)
+            for (int k = 0; k < 8; k++) { double t = S[col][k]; S[col][k] = S[piv][k]; S[piv][k] = t; }
+        const double d = 1.0 / S[col][col];
+        for (int k = 0; k < 8; k++) S[col][k] *= d;
+        for (int r = 0; r < 4; r++) {
+            if (r == col) continue;
+            const double f = S[r][col];
+            for (int k = 0; k < 8; k++) S[r][k] -= f * S[col][k];
+        }
+    }
+    double* o = sinv + e * 16;
+    for (int k = 0; k < 4; k++)
+        for (int l = 0; l < 4; l++) o[k * 4 + l] = S[k][4 + l];
+}
+
+__global__ void k_applyG_q2_3d(uwg_lgeom g, const uint8_t* bc, const double* p, double* y) {
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= g.n_el) return;
+    int ex[3];
+    double h[3];
+    q2e3(g, e, ex, h);
+    const double pe[4] = {p[e * 4], p[e * 4 + 1], p[e * 4 + 2], p[e * 4 + 3]};
+    for (int A = 0; A < 27; A++) {
+        const int64_t n = q2node3(g, ex, A);
+        for (int i = 0; i < 3; i++) {
+            if (bc[n * 3 + i]) continue;
+            double s = 0.0;
+            for (int k = 0; k < 4; k++) s += q2_Ge3(h, A, i, k) * pe[k];
+            atomicAdd(&y[n * 3 + i], s);
+        }
+    }
+}
+
+__global__ void k_applyGt_q2_3d(uwg_lgeom g, const uint8_t* bc, int only_bc, const double* u, double* q) {
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= g.n_el) return;
+    int ex[3];
+    double h[3];
+    q2e3(g, e, ex, h);
+    double s[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int A = 0; A < 27; A++) {
+        const int64_t n = q2node3(g, ex, A);
+        for (int i = 0; i < 3; i++) {
+            if ((bc[n * 3 + i] != 0) != (only_bc != 0)) continue;
+            const double v = u[n * 3 + i];
+            for (int k = 0; k < 4; k++) s[k] += q2_Ge3(h, A, i, k) * v;
+        }
+    }
+    for (int k = 0; k < 4; k++) q[e * 4 + k] = s[k];
+}
+
+__global__ void k_schur_pc_q2_3d(int64_t n_el, const double* sinv, const double* r, double* z) {
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= n_el) return;
+    const double* S = sinv + e * 16;
+    const double r0 = r[e * 4], r1 = r[e * 4 + 1], r2 = r[e * 4 + 2], r3 = r[e * 4 + 3];
+    for (int k = 0; k < 4; k++) z[e * 4 + k] = S[4 * k] * r0 + S[4 * k + 1] * r1 + S[4 * k + 2] * r2 + S[4 * k + 3] * r3;
+}
+
+// Element matrices of one element (diagnostics): K_e from the 125 weights by
+// the direct formula K_(A,i),(B,j) = sum_points w (delta_ij grad N_A . grad N_B
+// + d_j N_A d_i N_B), G_e and S^_e.  One block of 81 threads, thread = column.
+__global__ void k_element_matrices_q2_3d(uwg_lgeom g, int64_t e, const double* W, double* Ke, double* Ge_out,
+                                         double* Se) {
+    int ex[3];
+    double h[3];
+    q2e3(g, e, ex, h);
+    const double s[3] = {2.0 / h[0], 2.0 / h[1], 2.0 / h[2]};
+    const int col = threadIdx.x;
+    if (col < 81) {
+        const int B = col / 3, j = col % 3;
+        const int ba = B % 3, bb = (B / 3) % 3, bc_ = B / 9;
+        double acc[81];
+        for (int k = 0; k < 81; k++) acc[k] = 0.0;
+        for (int r = 0; r < 5; r++)
+            for (int q = 0; q < 5; q++)
+                for (int p = 0; p < 5; p++) {
+                    const double w = W[(int64_t)(p + 5 * q + 25 * r) * g.n_el + e];
+                    const double gB[3] = {s[0] * c3_D5[p][ba] * c3_B5[q][bb] * c3_B5[r][bc_],
+                                          s[1] * c3_B5[p][ba] * c3_D5[q][bb] * c3_B5[r][bc_],
+                                          s[2] * c3_B5[p][ba] * c3_B5[q][bb] * c3_D5[r][bc_]};
+                    for (int A = 0; A < 27; A++) {
+                        const int a = A % 3, b = (A / 3) % 3, c = A / 9;
+                        const double gA[3] = {s[0] * c3_D5[p][a] * c3_B5[q][b] * c3_B5[r][c],
+                                              s[1] * c3_B5[p][a] * c3_D5[q][b] * c3_B5[r][c],
+                                              s[2] * c3_B5[p][a] * c3_B5[q][b] * c3_D5[r][c]};
+                        const double dot = gA[0] * gB[0] + gA[1] * gB[1] + gA[2] * gB[2];
+                        for (int i = 0; i < 3; i++) acc[A * 3 + i] += w * ((i == j ? dot : 0.0) + gA[j] * gB[i]);
+                    }
+                }
+        for (int k = 0; k < 81; k++) Ke[k * 81 + col] = acc[k];
+        for (int k = 0; k < 4; k++) Ge_out[col * 4 + k] = q2_Ge3(h, B, j, k);
+    }
+    __syncthreads();
+    if (col < 16) {
+        const int k = col / 4, l = col % 4;
+        double sum = 0.0;
+        for (int rr = 0; rr < 81; rr++) sum += Ge_out[rr * 4 + k] * (Ge_out[rr * 4 + l] / Ke[rr * 81 + rr]);
+        Se[k * 4 + l] = sum;
+    }
+}
+
+void dpc1_3d_host(double xi, double eta, double zeta, double* M) {
+    const double fac = 1.0 / 9.0;
+    M[0] = fac * (-4.0 * xi - 20.0 * eta + 12.0 * zeta + 3.0);
+    M[1] = fac * (16.0 * xi - 64.0 * eta + 60.0 * zeta + 6.0);
+    M[2] = fac * (36.0 * eta - 36.0 * zeta);
+    M[3] = fac * (-12.0 * xi + 48.0 * eta - 36.0 * zeta);
+}
+void q2_1d_host3(double s, double* N, double* D) {
+    N[0] = 0.5 * s * (s - 1.0); N[1] = 1.0 - s * s; N[2] = 0.5 * s * (s + 1.0);
+    D[0] = s - 0.5; D[1] = -2.0 * s; D[2] = s + 0.5;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Host wrappers (called by the uwg_q2_* dispatchers for 3D contexts)
+// ---------------------------------------------------------------------------
+int uwg_q2_3d_init(uwg_ctx* c) {
+    // reference gradient integrals, 3-point Gauss (exact: degree <= 3 per axis)
+    const double gp[3] = {-std::sqrt(0.6), 0.0, std::sqrt(0.6)}, gw[3] = {5.0 / 9.0, 8.0 / 9.0, 5.0 / 9.0};
+    static double GR[3][27][4];
+    for (int i = 0; i < 3; i++)
+        for (int A = 0; A < 27; A++)
+            for (int k = 0; k < 4; k++) GR[i][A][k] = 0.0;
+    for (int kz = 0; kz < 3; kz++)
+        for (int jy = 0; jy < 3; jy++)
+            for (int ix = 0; ix < 3; ix++) {
+                double Nx[3], Dx[3], Ny[3], Dy[3], Nz[3], Dz[3], M[4];
+                q2_1d_host3(gp[ix], Nx, Dx);
+                q2_1d_host3(gp[jy], Ny, Dy);
+                q2_1d_host3(gp[kz], Nz, Dz);
+                dpc1_3d_host(gp[ix], gp[jy], gp[kz], M);
+                const double w = gw[ix] * gw[jy] * gw[kz];
+                for (int A = 0; A < 27; A++) {
+                    const int a = A % 3, b = (A / 3) % 3, cc = A / 9;
+                    for (int k = 0; k < 4; k++) {
+                        GR[0][A][k] += w * Dx[a] * Ny[b] * Nz[cc] * M[k];
+                        GR[1][A][k] += w * Nx[a] * Dy[b] * Nz[cc] * M[k];
+                        GR[2][A][k] += w * Nx[a] * Ny[b] * Dz[cc] * M[k];
+                    }
+                }
+            }
+    UWG_CUDA(c, cudaMemcpyToSymbol(c3_GR, GR, sizeof(GR)));
+    return UWG_OK;
+}
+
+int uwg_q2_3d_assemble(uwg_ctx* c, const int32_t* off, const int32_t* list, const double* ip_xi, const double* ip_w,
+                       const double* eta_p, const double* body_p) {
+    uwg_lgeom g = uwg_level_geom(c, 0);
+    vk_zero<double>(c->stream, c->n_vdof, c->f);
+    k_assemble_q2_3d<<<nblk(c->n_el * 32, 128), 128, 0, c->stream>>>(g, off, list, ip_xi, ip_w, eta_p, body_p,
+                                                                    c->lev[0].W64, c->lev[1].W64, c->f);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
+template <typename T>
+int uwg_q2_3d_applyK(uwg_ctx* c, const T* x, T* y, bool mask_in) {
+    const uwg_level& L = c->lev[0];
+    const T* W;
+    if constexpr (sizeof(T) == 8) W = (const T*)L.W64; else W = (const T*)L.W32;
+    constexpr int BS = sizeof(T) == 8 ? 64 : 128;
+    k_applyK_q2_3d<T, BS><<<nblk(L.n_el, BS), BS, 0, c->stream>>>(uwg_level_geom(c, 0), W, L.bc, mask_in, x, y);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+template int uwg_q2_3d_applyK<double>(uwg_ctx*, const double*, double*, bool);
+template int uwg_q2_3d_applyK<float>(uwg_ctx*, const float*, float*, bool);
+
+int uwg_q2_3d_diag(uwg_ctx* c, double* sinv) {
+    const uwg_level& L = c->lev[0];
+    k_diag_q2_3d<<<nblk(L.n_el, 64), 64, 0, c->stream>>>(uwg_level_geom(c, 0), L.W64, L.bc, L.diag64, sinv);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
+int uwg_q2_3d_applyG(uwg_ctx* c, const double* p, double* y) {
+    vk_zero<double>(c->stream, c->n_vdof, y);
+    k_applyG_q2_3d<<<nblk(c->n_el), 256, 0, c->stream>>>(uwg_level_geom(c, 0), c->bc, p, y);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
+int uwg_q2_3d_applyGt(uwg_ctx* c, const double* u, double* q, int only_bc) {
+    k_applyGt_q2_3d<<<nblk(c->n_el), 256, 0, c->stream>>>(uwg_level_geom(c, 0), c->bc, only_bc, u, q);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
+int uwg_q2_3d_schur_pc(uwg_ctx* c, const double* r, double* z) {
+    k_schur_pc_q2_3d<<<nblk(c->n_el), 256, 0, c->stream>>>(c->n_el, c->Shat, r, z);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
+int uwg_q2_3d_element_matrices(uwg_ctx* c, int64_t el, double* Ke, double* Ge, double* Se) {
+    double* buf = nullptr;
+    const int nk = 81 * 81, ng = 81 * 4, ns = 16;
+    UWG_CUDA(c, cudaMallocAsync((void**)&buf, sizeof(double) * (nk + ng + ns), c->stream));
+    k_element_matrices_q2_3d<<<1, 96, 0, c->stream>>>(uwg_level_geom(c, 0), el, c->lev[0].W64, buf, buf + nk,
+                                                      buf + nk + ng);
+    std::vector<double> h(nk + ng + ns);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), buf, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->stream);
+    cudaFreeAsync(buf, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return uwg_set_error(c, UWG_ERR_CUDA, cudaGetErrorString(e));
+    if (Ke) for (int i = 0; i < nk; i++) Ke[i] = h[i];
+    if (Ge) for (int i = 0; i < ng; i++) Ge[i] = h[nk + i];
+    if (Se) for (int i = 0; i < ns; i++) Se[i] = h[nk + ng + i];
+    return UWG_OK;
+}

@@ -45,8 +45,8 @@ class IndexSet:
 
 
 class FeMesh_Cartesian:
-    """Regular Cartesian mesh: ``elementType`` 'Q1/dQ0' (2D and 3D) or 'Q2/dPc1'
-    (2D): primary velocity mesh and the pressure sub-mesh."""
+    """Regular Cartesian mesh: ``elementType`` 'Q1/dQ0' or 'Q2/dPc1' (2D and 3D):
+    primary velocity mesh and the pressure sub-mesh."""
 
     def __init__(self, elementType="Q1/dQ0", elementRes=(4, 4), minCoord=(0.0, 0.0), maxCoord=(1.0, 1.0),
                  periodic=None, partitioned=True, **kwargs):
@@ -55,10 +55,10 @@ class FeMesh_Cartesian:
         types = [t.upper() for t in elementType]
         if types[0] == "Q1" and (len(types) == 1 or types[1] == "DQ0"):
             order, porder = 1, 0
-        elif types[0] == "Q2" and len(types) > 1 and types[1] == "DPC1" and len(elementRes) == 2:
+        elif types[0] == "Q2" and len(types) > 1 and types[1] == "DPC1":
             order, porder = 2, 1
         else:
-            raise ValueError("supported element types: 'Q1/dQ0', and 'Q2/dPc1' in 2D (got %s)" % "/".join(elementType))
+            raise ValueError("supported element types: 'Q1/dQ0' and 'Q2/dPc1' (got %s)" % "/".join(elementType))
         if periodic and any(periodic):
             raise ValueError("periodic meshes are not supported")
         if len(elementRes) not in (2, 3) or len(minCoord) != len(elementRes) or len(maxCoord) != len(elementRes):
@@ -115,14 +115,14 @@ class FeMesh_Cartesian:
 
 class _SubMesh:
     """The pressure mesh: dQ0 (one node per element at its centroid) or dPc1
-    (three per element, the coefficients of the linear basis of
-    BilinearInnerElType.c:169-179)."""
+    (three per element in 2D, four in 3D: the coefficients of the linear bases
+    of BilinearInnerElType.c:169-179 and TrilinearInnerElType.c:202-215)."""
 
     def __init__(self, mesh):
         self.parent = mesh
         self.dim = mesh.dim
         self.elementType = "DQ0" if mesh._porder == 0 else "DPC1"
-        self._npn = 1 if mesh._porder == 0 else 3
+        self._npn = 1 if mesh._porder == 0 else (3 if mesh.dim == 2 else 4)
         self.nodesGlobal = mesh.elementsGlobal * self._npn
         self.elementsGlobal = mesh.elementsGlobal
         self.elementRes = mesh.elementRes
@@ -229,14 +229,20 @@ class MeshVariable:
         # dPc1: sum_k p_k M_k(xi) at the points' local coordinates
         pm = self._primary()
         el = own.clamp(max=pm.elementsGlobal - 1)
-        ij = (el % pm.elementRes[0], el // pm.elementRes[0])
+        r = pm.elementRes
+        ij = [el % r[0], (el // r[0]) % r[1]] + ([el // (r[0] * r[1])] if pm.dim == 3 else [])
         xi = []
-        for d in range(2):
+        for d in range(pm.dim):
             corners = torch.from_numpy(np.ascontiguousarray(pm._axes[d][:: pm._order])).to(ctx.device)
             lo, hi = corners[ij[d]], corners[ij[d] + 1]
             xi.append(2.0 * (coords[:, d] - lo) / (hi - lo) - 1.0)
-        M = torch.stack([-xi[0] - 0.5 * xi[1] + 0.25, xi[0] - 0.5 * xi[1] + 0.25, xi[1] + 0.5], 1)
-        return (vals.view(-1, 3)[el] * M).sum(1, keepdim=True)
+        if pm.dim == 2:
+            M = torch.stack([-xi[0] - 0.5 * xi[1] + 0.25, xi[0] - 0.5 * xi[1] + 0.25, xi[1] + 0.5], 1)
+        else:
+            x, y, z = xi
+            M = torch.stack([-4.0 * x - 20.0 * y + 12.0 * z + 3.0, 16.0 * x - 64.0 * y + 60.0 * z + 6.0,
+                             36.0 * y - 36.0 * z, -12.0 * x + 48.0 * y - 36.0 * z], 1) / 9.0
+        return (vals.view(-1, npn)[el] * M).sum(1, keepdim=True)
 
     def __add__(self, o): return self._as_function() + o
     def __radd__(self, o): return o + self._as_function()

@@ -16,7 +16,7 @@ from . import swarm as _swarm
 
 class Stokes:
     """The incompressible (or compressible) Stokes system K u + G p = f,
-    G^T u + C p = h on a Q1/dQ0 or 2D Q2/dPc1 mesh (P/systems/_stokes.py:106-330)."""
+    G^T u + C p = h on a Q1/dQ0 or Q2/dPc1 mesh (P/systems/_stokes.py:106-330)."""
 
     def __init__(self, velocityField, pressureField, fn_viscosity, fn_bodyforce=None, fn_one_on_lambda=None,
                  fn_source=None, voronoi_swarm=None, conditions=[], gauss_swarm=None, _removeBCs=True,
@@ -199,24 +199,27 @@ class Stokes:
 
 
 def _q2_rms(mesh, v):
-    """velocity_rms on a 2D Q2 mesh: 3x3 Gauss points per element."""
+    """velocity_rms on a Q2 mesh: 3^dim Gauss points per element."""
     x1, w1 = np.polynomial.legendre.leggauss(3)
-    rx, ry = mesh.elementRes
-    grid = v.reshape(2 * ry + 1, 2 * rx + 1, 2)
-    hx = np.diff(mesh._axes[0][::2])
-    hy = np.diff(mesh._axes[1][::2])
-    area = np.outer(hy, hx)
+    dim = mesh.dim
+    r = mesh.elementRes
+    grid = v.reshape(*[2 * n + 1 for n in r[::-1]], dim)
+    h = [np.diff(a[::2]) for a in mesh._axes]
+    vol_el = h[1][:, None] * h[0][None, :] if dim == 2 else \
+        h[2][:, None, None] * h[1][None, :, None] * h[0][None, None, :]
     N = lambda s: (0.5 * s * (s - 1.0), 1.0 - s * s, 0.5 * s * (s + 1.0))
     num = vol = 0.0
-    for j in range(3):
-        for i in range(3):
-            Nx, Ny = N(x1[i]), N(x1[j])
-            val = 0.0
-            for b in range(3):
-                for a in range(3):
-                    val = val + Nx[a] * Ny[b] * grid[b: b + 2 * ry: 2, a: a + 2 * rx: 2]
-            num += np.sum(w1[i] * w1[j] * 0.25 * area * np.sum(val ** 2, axis=-1))
-            vol += np.sum(w1[i] * w1[j] * 0.25 * area)
+    scale = 0.5 ** dim
+    for q in np.ndindex(*([3] * dim)):
+        Ns = [N(x1[qi]) for qi in q]          # per axis, q[0] = x
+        wq = np.prod([w1[qi] for qi in q])
+        val = 0.0
+        for a in np.ndindex(*([3] * dim)):
+            wgt = np.prod([Ns[d][a[d]] for d in range(dim)])
+            sl = tuple(slice(a[d], a[d] + 2 * r[d], 2) for d in reversed(range(dim)))
+            val = val + wgt * grid[sl]
+        num += np.sum(wq * scale * vol_el * np.sum(val ** 2, axis=-1))
+        vol += np.sum(wq * scale * vol_el)
     return float(np.sqrt(num / vol))
 
 
