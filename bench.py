@@ -44,6 +44,10 @@ CONFIGS = {
     "sinker2d": dict(dim=2, res=(64, 64), ppc=20, kind="sinker"),
     # 2D Q2/dPc1 Rayleigh-Taylor layering, 40 particles per element
     "rt2d_q2": dict(dim=2, res=(256, 256), ppc=40, kind="rt", order=2, porder=1),
+    # 3D Q2/dPc1 thermal-convection Stokes step: T = 1 - z + seeded 1e-2 noise,
+    # viscosity exp(-9.2 T), buoyancy Ra T (Ra = 1e6), 30 particles per element
+    "conv3d_q2": dict(dim=3, res=(96, 96, 96), ppc=30, kind="conv", order=2, porder=1),
+    "conv3d_q2_small": dict(dim=3, res=(32, 32, 32), ppc=30, kind="conv", order=2, porder=1),
 }
 
 
@@ -88,6 +92,20 @@ def material(cfg, x):
     if cfg["kind"] == "grf":
         T = grf_T(x)
         eta = torch.exp(-11.5 * T)
+        body = torch.zeros_like(x)
+        body[:, 2] = 1e6 * T
+        return eta.contiguous(), body.contiguous()
+    if cfg["kind"] == "conv":
+        # seeded smooth perturbation: a few random Fourier modes vanishing at z = 0, 1
+        g = torch.Generator(device="cpu").manual_seed(4242)
+        a = (torch.rand(4, 3, generator=g, dtype=torch.float64) * 2.0 - 1.0).tolist()
+        noise = torch.zeros(x.shape[0], dtype=torch.float64, device=x.device)
+        for k in range(1, 5):
+            ax, ay, az = a[k - 1]
+            noise += ax * torch.cos(torch.pi * k * x[:, 0] + ay) * torch.cos(torch.pi * k * x[:, 1] + az) * \
+                torch.sin(torch.pi * x[:, 2])
+        T = (1.0 - x[:, 2] + 0.01 * noise / 4.0).clamp(0.0, 1.0)
+        eta = torch.exp(-9.2 * T)
         body = torch.zeros_like(x)
         body[:, 2] = 1e6 * T
         return eta.contiguous(), body.contiguous()
@@ -314,7 +332,9 @@ def workload_name(key):
     return {"grf3d": "3D 128^3 Q1/dQ0 GRF viscosity exp(-11.5T), Ra=1e6, 20 ppc, free-slip (config 3)",
             "grf3d_small": "3D 32^3 Q1/dQ0 GRF viscosity, 20 ppc, free-slip",
             "sinker2d": "2D 64^2 Q1/dQ0 sinker, 20 ppc, free-slip (config 1)",
-            "rt2d_q2": "2D 256^2 Q2/dPc1 Rayleigh-Taylor, 40 ppc, viscosity x 10^U(-1,1), free-slip (config 2)"}[key]
+            "rt2d_q2": "2D 256^2 Q2/dPc1 Rayleigh-Taylor, 40 ppc, viscosity x 10^U(-1,1), free-slip (config 2)",
+            "conv3d_q2": "3D 96^3 Q2/dPc1 convection Stokes step, T = 1 - z + 1e-2 noise, viscosity exp(-9.2T), Ra=1e6, 30 ppc, free-slip (config 5 solve)",
+            "conv3d_q2_small": "3D 32^3 Q2/dPc1 convection Stokes step, 30 ppc"}[key]
 
 
 def dram_traffic(kernel_name, config):
@@ -332,7 +352,7 @@ def time_kernel_apply(ctx, reps=20):
     """CUDA-event time of the FP32 matrix-free K apply on the finest level.
     Algorithmic bytes per apply: 4*(2*N_v) + 4*M*N_el (x read, y written,
     M equivalent-quadrature weights read: 27 for 3D Q1, 9 for 2D Q1, 25 for
-    2D Q2)."""
+    2D Q2, 125 for 3D Q2)."""
     import torch
     x = torch.randn(ctx.n_vdof, dtype=torch.float32, device=ctx.device)
     y = torch.empty_like(x)
@@ -346,9 +366,12 @@ def time_kernel_apply(ctx, reps=20):
     e.record()
     torch.cuda.synchronize()
     sec = s.elapsed_time(e) / 1e3 / reps
-    nq = 25 if ctx.order == 2 else (27 if ctx.dim == 3 else 9)
+    nq = (125 if ctx.dim == 3 else 25) if ctx.order == 2 else (27 if ctx.dim == 3 else 9)
     byts = 4 * 2 * ctx.n_vdof + 4 * nq * ctx.n_el
-    name = "k_applyK_q2<float>" if ctx.order == 2 else ("k_applyK_q1_3d_tiled<float>" if ctx.dim == 3 else "k_applyK_q1_2d<float>")
+    if ctx.order == 2:
+        name = "k_applyK_q2_3d<float>" if ctx.dim == 3 else "k_applyK_q2<float>"
+    else:
+        name = "k_applyK_q1_3d_tiled<float>" if ctx.dim == 3 else "k_applyK_q1_2d<float>"
     return {"name": name + " (+ BC copy)", "seconds": sec, "bytes": byts}
 
 
