@@ -255,6 +255,28 @@ int uwg_pop_plan_pcdvc(uwg_ctx* ctx, int64_t np, const int32_t* owner, const int
 int uwg_pop_apply(uwg_ctx* ctx, const double* ip_xi, const double* x_old, double* x_new, int32_t* owner_new,
                   int32_t* cell_offsets_new, int32_t* cell_list_new, int64_t* src_h);
 
+/* ---- Learned warm start: BF16 tensor-core kernels of a small CNN ------------
+ * No counterpart in the reference.  Device pointers; BF16 buffers as uint16_t;
+ * activations NHWC.  C[m][n] (+)= sum_k A(m,k) B(k,n) (+ bias[n]) (ReLU) with
+ * A(m,k) = a_trans ? A[k*lda+m] : A[m*lda+k], B(k,n) = b_trans ? B[n*ldb+k] :
+ * B[k*ldb+n], FP32 accumulation (mma.sync m16n8k16 bf16); Cf (FP32) and/or Cb
+ * (BF16) outputs. */
+int uwg_cnn_gemm(uwg_ctx* ctx, int M, int N, int K, const uint16_t* A, int64_t lda, int a_trans, const uint16_t* B,
+                 int64_t ldb, int b_trans, float* Cf, uint16_t* Cb, int64_t ldc, const float* bias, int relu,
+                 int accumulate);
+/* 3x3 im2col (BF16, zero padding) and its transpose col2im (FP32). */
+int uwg_cnn_im2col(uwg_ctx* ctx, int nb, int H, int W, int C, const uint16_t* x, uint16_t* col);
+int uwg_cnn_col2im(uwg_ctx* ctx, int nb, int H, int W, int C, const float* col, float* out);
+/* op 0 ReLU backward, 1 2x2 average pool, 2 its transpose, 3 nearest 2x upsampling,
+ * 4 its transpose, 5 BF16 add, 6 FP32 -> BF16. */
+int uwg_cnn_elementwise(uwg_ctx* ctx, int op, int nb, int H, int W, int C, const uint16_t* a16, const uint16_t* b16,
+                        uint16_t* c16, const float* fa, float* fb);
+int uwg_cnn_bias_grad(uwg_ctx* ctx, int64_t P, int C, const float* g, float* db);
+/* mean-squared error over the first nout of C channels; gradient into g, loss into *loss (device). */
+int uwg_cnn_mse(uwg_ctx* ctx, int64_t P, int C, int nout, const float* y, const float* t, float* g, float* loss);
+int uwg_cnn_adam(uwg_ctx* ctx, int64_t n, float* w, const float* g, float* m, float* v, uint16_t* wb, float lr,
+                 float b1, float b2, float eps, int step);
+
 /* ---- SUPG advection-diffusion of a nodal scalar (Q1 meshes) ----------------
  * One time step of the explicit predictor-multicorrector with SUPG residual and
  * lumped mass.  Replaces _AdvectionDiffusionSLE_Execute for the SUPG method

@@ -95,6 +95,14 @@ SIGNATURES = {
     "uwg_pop_plan_pcdvc": (_I, [_CTX, _I64, _P, _P, _P, _P, _D, _D, _I, _I, ctypes.POINTER(_I64),
                                 ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
     "uwg_pop_apply": (_I, [_CTX, _P, _P, _P, _P, _P, _P, _P]),
+    "uwg_cnn_gemm": (_I, [_CTX, _I, _I, _I, _P, _I64, _I, _P, _I64, _I, _P, _P, _I64, _P, _I, _I]),
+    "uwg_cnn_im2col": (_I, [_CTX, _I, _I, _I, _I, _P, _P]),
+    "uwg_cnn_col2im": (_I, [_CTX, _I, _I, _I, _I, _P, _P]),
+    "uwg_cnn_elementwise": (_I, [_CTX, _I, _I, _I, _I, _I, _P, _P, _P, _P, _P]),
+    "uwg_cnn_bias_grad": (_I, [_CTX, _I64, _I, _P, _P]),
+    "uwg_cnn_mse": (_I, [_CTX, _I64, _I, _I, _P, _P, _P, _P]),
+    "uwg_cnn_adam": (_I, [_CTX, _I64, _P, _P, _P, _P, _P, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                          ctypes.c_float, _I]),
     "uwg_slcn_solve": (_I, [_CTX, _D, _P, _P, _P, _P, _P, _D, _I, ctypes.POINTER(_I), ctypes.POINTER(_D)]),
 }
 
