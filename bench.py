@@ -497,6 +497,68 @@ def run_slcn(args):
                       "T_range": [float(phi.min()), float(phi.max())]}))
 
 
+def run_learned(args):
+    """Learned warm start on the 2D 128^2 Q1/dQ0 problem family of the training
+    set (log10 viscosity GRF with correlation length U[0.05, 0.2] and contrast
+    10^U[3,6], 0-8 inclusions of radius U[0.03, 0.1] with density +-1, 20
+    particles per element, free slip): generate `--train` solves with the plain
+    path, train the CNN, then on `--eval` held-out seeds compare outer (Schur
+    FGMRES) iterations and time to a 1e-8 residual of the plain FP64 solve, the
+    mixed-precision solve from zero and the mixed-precision solve from the
+    network's pressure as the first Schur search direction ("learned") and as
+    the initial guess ("guess"), prediction time included.  Problems without
+    buoyancy (no inclusions: zero solution) are left out of the means."""
+    import numpy as np
+    import torch
+    from underworld2_gb300 import learned
+    ps = learned.ProblemSet(res=128, ppc=20)
+    t0 = time.perf_counter()
+    X, Y = learned.generate(ps, list(range(1000, 1000 + args.train)))
+    torch.cuda.synchronize()
+    t_gen = time.perf_counter() - t0
+    net = learned.WarmStartNet(ps.ctx, seed=0)
+    t0 = time.perf_counter()
+    losses = learned.train(net, X, Y, epochs=args.epochs, batch=8)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    rows = []
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    for s in range(900000, 900000 + args.eval):
+        f, eta_ref = ps.assemble(s)
+        u64, p64, st64 = ps.solve(0)
+        um, pm, stm = ps.solve(1)
+        e0, e1 = ev(), ev()
+        e0.record()
+        p0 = learned.predict_pressure(net, f)
+        e1.record()
+        torch.cuda.synchronize()
+        t_pred = e0.elapsed_time(e1) / 1e3
+        ul, pl, stl, fb = learned.solve_with_warm_start(ps, net, f, mode="direction")
+        ug, pg, stg, fbg = learned.solve_with_warm_start(ps, net, f, mode="guess")
+        pt = p64 - p64.mean()
+        err = float((p0 - pt).norm() / max(float(pt.norm()), 1e-300))
+        rows.append({"fp64_its": st64["pressure_its"], "fp64_s": st64["total_time"],
+                     "mixed_its": stm["pressure_its"], "mixed_s": stm["total_time"],
+                     "learned_its": stl["pressure_its"], "learned_s": stl["total_time"] + t_pred,
+                     "guess_its": stg["pressure_its"], "guess_s": stg["total_time"] + t_pred,
+                     "predict_s": t_pred, "fallback": fb or fbg, "p_rel_err": err,
+                     "residual": max(stl["residual"], stg["residual"]), "trivial": float(pt.norm()) == 0.0})
+    rows_nt = [r for r in rows if not r["trivial"]]
+    agg = lambda k: float(np.mean([r[k] for r in rows_nt]))
+    med = lambda k: float(np.median([r[k] for r in rows_nt]))
+    print(json.dumps({
+        "learned": "CNN warm start (pressure initial guess of the Schur FGMRES)",
+        "params": net.n_params(), "train_solves": args.train, "eval_solves": args.eval, "epochs": args.epochs,
+        "generate_s": t_gen, "train_s": t_train, "loss_first_epoch": losses[0], "loss_last_epoch": losses[-1],
+        "mean": {k: agg(k) for k in ("fp64_its", "fp64_s", "mixed_its", "mixed_s", "learned_its", "learned_s",
+                                      "guess_its", "guess_s", "predict_s", "p_rel_err")},
+        "median_p_rel_err": med("p_rel_err"), "trivial_problems": int(sum(r["trivial"] for r in rows)),
+        "fallbacks": int(sum(r["fallback"] for r in rows)),
+        "max_residual": float(max(r["residual"] for r in rows)),
+        "speedup_learned_vs_fp64": agg("fp64_s") / agg("learned_s"),
+        "speedup_mixed_vs_fp64": agg("fp64_s") / agg("mixed_s")}))
+
+
 def run_profile_solve(args):
     """One map + DVC + assembly + solve of the workload, untimed (the target of
     the launch-list captures recorded under profiles/); `--kernel-ppc` lowers
@@ -600,6 +662,11 @@ def main():
                     help="only launch one operator kernel, or time SUPG / SLCN advection-diffusion steps (profiling)")
     ap.add_argument("--kernel-ppc", type=int, default=0)
     ap.add_argument("--profile-solve", action="store_true", help="one untimed solve (profiling target)")
+    ap.add_argument("--learned", action="store_true",
+                    help="train the warm-start CNN on generated 2D 128^2 solves and evaluate it on held-out seeds")
+    ap.add_argument("--train", type=int, default=800)
+    ap.add_argument("--eval", type=int, default=100)
+    ap.add_argument("--epochs", type=int, default=20)
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--max-outer", type=int, default=500)
     ap.add_argument("--skip-fp64", action="store_true")
@@ -617,6 +684,9 @@ def main():
         return
     if args.profile_solve:
         run_profile_solve(args)
+        return
+    if args.learned:
+        run_learned(args)
         return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -164,6 +164,9 @@ typedef struct {
     int relax_inner;       /* 1: loosen the velocity-solve tolerance inside the Schur iteration as its
                               residual falls (inexact Krylov), then confirm with one strict residual */
     int schur_pc_smooth;   /* Chebyshev degree of the pressure-multigrid smoother inside BFBt */
+    const double* p_dir;   /* device [n_pdof] or NULL: first search direction of the Schur FGMRES in
+                              place of the first preconditioner application (a learned correction;
+                              the least-squares step of the iteration chooses its weight) */
 } uwg_solve_opts;
 
 typedef struct {

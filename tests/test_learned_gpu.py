@@ -106,6 +106,11 @@ def test_warm_start_solve_and_fallback(gpu):
     pm = lambda p: p - p.mean()
     dp = (pm(p1) - pm(p0)).abs().max().item() / pm(p0).abs().max().item()
     assert du < 1e-6 and dp < 1e-6
+    u3, p3, st3, fb3 = learned.solve_with_warm_start(ps, net, f, mode="guess")
+    assert not fb3 and st3["residual"] <= 1e-8
+    # the exact pressure as the first search direction: one Schur iteration suffices
+    u4, p4, st4 = ps.solve(1, p_dir=p0 - p0.mean())
+    assert st4["residual"] <= 1e-8 and st4["pressure_its"] <= 2 < st0["pressure_its"]
     # a network returning garbage: the plain FP64 solve takes over
     net.out.b.fill_(float("nan"))
     u2, p2, st2, fb2 = learned.solve_with_warm_start(ps, net, f)

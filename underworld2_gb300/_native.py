@@ -35,7 +35,7 @@ class SolveOpts(ctypes.Structure):
                 ("outer_rtol", ctypes.c_double), ("max_inner", ctypes.c_int), ("max_outer", ctypes.c_int),
                 ("mg_levels", ctypes.c_int), ("smooth_steps", ctypes.c_int), ("restart", ctypes.c_int),
                 ("zero_guess", ctypes.c_int), ("schur_pc", ctypes.c_int), ("schur_pc_rtol", ctypes.c_double),
-                ("relax_inner", ctypes.c_int), ("schur_pc_smooth", ctypes.c_int)]
+                ("relax_inner", ctypes.c_int), ("schur_pc_smooth", ctypes.c_int), ("p_dir", ctypes.c_void_p)]
 
 
 class SolveStats(ctypes.Structure):

@@ -644,6 +644,7 @@ extern "C" void uwg_solve_opts_default(uwg_solve_opts* o) {
     o->zero_guess = 1;
     o->schur_pc = 1;
     o->schur_pc_rtol = 3e-2;
+    o->p_dir = nullptr;
 }
 
 namespace {
@@ -665,7 +666,7 @@ int schur_apply(uwg_ctx* c, const SolveCfg& cfg, const double* p, double* q, int
 
 // Right-preconditioned flexible GMRES on the Schur complement, M^-1 = -S^^-1.
 int fgmres(uwg_ctx* c, const SolveCfg& cfg, const double* rhs, double* p, double rtol, double atol, int maxit,
-           int m, int* its, int* inner_its, int* refine, bool use_p0) {
+           int m, int* its, int* inner_its, int* refine, bool use_p0, const double* z0) {
     Work* w = work_of(c);
     cudaStream_t s = c->stream;
     int64_t n = c->n_pdof;
@@ -701,7 +702,10 @@ int fgmres(uwg_ctx* c, const SolveCfg& cfg, const double* rhs, double* p, double
         for (; j < m && total < maxit; j++) {
             // Z_j = M^-1 V_j: -S^^-1 (the reference's Uzawa term) or scaled BFBt
             double tp0 = now();
-            if (cfg.schur_pc == 1) {
+            if (z0 && total == 0) {
+                // a given first direction (the learned correction) in place of M^-1 V_0
+                vk_copy<double>(s, n, z0, w->Z[j]);
+            } else if (cfg.schur_pc == 1) {
                 if ((rc = bfbt(c, w->V[j], w->Z[j], cfg.schur_pc_rtol))) return rc;
                 cudaStreamSynchronize(s);
                 w->t_pc += now() - tp0;
@@ -890,7 +894,7 @@ extern "C" int uwg_stokes_solve(uwg_ctx* c, const uwg_solve_opts* o, double* u, 
     }
     double atol = o->rtol > 0.0 ? 0.5 * o->rtol * std::sqrt(fh2[0] + fh2[1]) : 0.0;
     rc = fgmres(c, cfg, w->hhat, p, o->outer_rtol, atol, o->max_outer, std::max(2, o->restart), &outer, &inner_its,
-                &S.refinement_steps, o->zero_guess == 0);
+                &S.refinement_steps, o->zero_guess == 0, o->p_dir);
     S.pressure_its = outer;
     S.schur_pc_its = w->lsolve_its;
     S.schur_pc_time = w->t_pc;

@@ -135,6 +135,8 @@ class WarmStartNet:
         self.layers = [self.e1a, self.e1, self.e2a, self.e2, self.e3a, self.e3, self.bt, self.d3a, self.d3,
                        self.d2a, self.d2, self.d1a, self.d1, self.out]
         self.step = 0
+        # per-channel scale of the targets (set from the training set by ``train``)
+        self.scale = torch.ones(3, dtype=torch.float32, device=dev)
 
     def n_params(self):
         return sum(l.n_params() for l in self.layers)
@@ -355,12 +357,16 @@ class ProblemSet:
         f, le_mean = features(log_eta, rho, self.res, ctx.device)
         return f, 10.0 ** le_mean
 
-    def solve(self, mixed, p0=None, rtol=1e-8):
+    def solve(self, mixed, p0=None, p_dir=None, rtol=1e-8):
+        """Solve the assembled problem; p0: initial pressure, p_dir: first search
+        direction of the Schur FGMRES (both device tensors, or None)."""
         ctx = self.ctx
         u = ctx.zeros(ctx.n_vdof)
         p = ctx.zeros(ctx.n_pdof) if p0 is None else p0.reshape(-1).to(torch.float64).contiguous().clone()
+        d = None if p_dir is None else p_dir.reshape(-1).to(torch.float64).contiguous()
         st = ctx.solve(u, p, mixed=int(mixed), rtol=rtol, inner_rtol=1e-10, outer_rtol=1e-9, smooth_steps=2,
-                       restart=120, schur_pc=1, max_outer=500, zero_guess=0 if p0 is not None else 1)
+                       restart=120, schur_pc=1, max_outer=500, zero_guess=0 if p0 is not None else 1,
+                       p_dir=None if d is None else d.data_ptr())
         return u, p, st
 
 
@@ -378,7 +384,11 @@ def generate(ps, seeds, rtol=1e-8):
 
 
 def train(net, X, Y, epochs=20, batch=8, lr=1e-3, lr_final=1e-4, seed=0, log=None):
+    """Adam with an exponentially decaying learning rate on targets scaled per
+    channel by their standard deviation over the training set."""
     n = X.shape[0]
+    net.scale = Y.reshape(-1, 3).std(dim=0).clamp_min(1e-12).float()
+    Y = (Y / net.scale).contiguous()
     gen = torch.Generator().manual_seed(seed)
     steps = epochs * ((n + batch - 1) // batch)
     k = 0
@@ -400,18 +410,23 @@ def train(net, X, Y, epochs=20, batch=8, lr=1e-3, lr_final=1e-4, seed=0, log=Non
 def predict_pressure(net, f):
     """Cell pressure guess (mean-free) for one problem's feature grid."""
     y = net.predict(f[None].to(_BF).contiguous())
-    p = y[0, :, :, 2].reshape(-1).double()
+    p = y[0, :, :, 2].reshape(-1).double() * float(net.scale[2])
     return p - p.mean()
 
 
-def solve_with_warm_start(ps, net, f, rtol=1e-8):
-    """Mixed-precision solve from the network's pressure; the plain FP64 solve if
-    that does not reach rtol.  Returns (u, p, stats, fell_back)."""
+def solve_with_warm_start(ps, net, f, rtol=1e-8, mode="direction"):
+    """Mixed-precision solve using the network's pressure -- as the first search
+    direction of the Schur FGMRES (mode "direction": the iteration's least-squares
+    step weighs it) or as the initial guess (mode "guess") -- and the plain FP64
+    solve if that does not reach rtol.  Returns (u, p, stats, fell_back)."""
     p0 = predict_pressure(net, f)
     try:
         if not bool(torch.isfinite(p0).all()):
             raise FloatingPointError("non-finite network output")
-        u, p, st = ps.solve(1, p0=p0, rtol=rtol)
+        if mode == "guess":
+            u, p, st = ps.solve(1, p0=p0, rtol=rtol)
+        else:
+            u, p, st = ps.solve(1, p_dir=p0, rtol=rtol)
         if st["residual"] <= rtol:
             return u, p, st, False
     except (FloatingPointError, _native.UwgError):
