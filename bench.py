@@ -304,6 +304,8 @@ def run_gpu(args):
                    "particles": npart, "particles_per_cell": cfg["ppc"], "solve_mode": args.mode,
                    "inputs_vs_L2": "particle arrays (%.1f GB) exceed the 129 MB L2" % (npart * 8 * (2 * dim + 1) / 1e9)},
         "particles_per_s": npart / adv_s,
+        "throughput": {"K_apply_mdof_per_s": ctx.n_vdof / kinfo["seconds"] / 1e6,
+                       "stokes_solves_per_s": 1.0 / solve_s},
         "phases_s": {k: float(np.mean(v)) for k, v in times.items()},
         "solver": {"pressure_its": stats[-1]["pressure_its"], "velocity_total_its": stats[-1]["velocity_total_its"],
                    "schur_pc_its": stats[-1]["schur_pc_its"], "refinement_steps": stats[-1]["refinement_steps"],
