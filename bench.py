@@ -704,16 +704,30 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
         dist.barrier()
-        line = run_gpu(args)
-        t = torch.tensor([line["value"]], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        line["value"] = float(t.item())
-        line["n_gpus"] = world
+        line = combine_replicas(run_gpu(args), world, "cuda")
         if rank == 0:
             print(json.dumps(line))
         dist.destroy_process_group()
         return
     print(json.dumps(run_gpu(args)))
+
+
+def combine_replicas(line, world, device):
+    """Replicas only: every rank solved its own copy of the workload.  Times are
+    the maximum over ranks (the job ends with the slowest replica), throughputs
+    the whole job's (all ranks' particles over that time)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([line["value"], line["ms_per_step"], line["e2e"]["value"],
+                      line["particles_per_s"] ** -1 if line.get("particles_per_s") else 0.0],
+                     dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    line["value"], line["ms_per_step"], line["e2e"]["value"] = float(t[0]), float(t[1]), float(t[2])
+    if line.get("particles_per_s"):
+        line["particles_per_s"] = world / float(t[3])
+    line["n_gpus"] = world
+    line["config"]["parallelism"] = "replicas x%d" % world
+    return line
 
 
 if __name__ == "__main__":
