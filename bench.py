@@ -526,23 +526,29 @@ def run_learned(args):
     rows = []
     ev = lambda: torch.cuda.Event(enable_timing=True)
     for s in range(900000, 900000 + args.eval):
-        f, eta_ref = ps.assemble(s)
+        f, scales = ps.assemble(s)
         u64, p64, st64 = ps.solve(0)
         um, pm, stm = ps.solve(1)
         e0, e1 = ev(), ev()
         e0.record()
-        p0 = learned.predict_pressure(net, f)
+        p0 = learned.predict_pressure(net, f, scales)
         e1.record()
         torch.cuda.synchronize()
         t_pred = e0.elapsed_time(e1) / 1e3
-        ul, pl, stl, fb = learned.solve_with_warm_start(ps, net, f, mode="direction")
-        ug, pg, stg, fbg = learned.solve_with_warm_start(ps, net, f, mode="guess")
+        ul, pl, stl, fb = learned.solve_with_warm_start(ps, net, f, scales, mode="direction")
+        ug, pg, stg, fbg = learned.solve_with_warm_start(ps, net, f, scales, mode="guess")
+        # control: the hydrostatic pressure alone (the third input channel) as the direction
+        ph = (f[:, :, 2].reshape(-1).double() * scales[1]).contiguous()
+        uh, phs, sth = ps.solve(1, p_dir=ph)
         pt = p64 - p64.mean()
-        err = float((p0 - pt).norm() / max(float(pt.norm()), 1e-300))
+        nt = max(float(pt.norm()), 1e-300)
+        err = float((p0 - pt).norm() / nt)
+        err_h = float((ph - ph.mean() - pt).norm() / nt)
         rows.append({"fp64_its": st64["pressure_its"], "fp64_s": st64["total_time"],
                      "mixed_its": stm["pressure_its"], "mixed_s": stm["total_time"],
                      "learned_its": stl["pressure_its"], "learned_s": stl["total_time"] + t_pred,
                      "guess_its": stg["pressure_its"], "guess_s": stg["total_time"] + t_pred,
+                     "hydro_its": sth["pressure_its"], "hydro_p_rel_err": err_h,
                      "predict_s": t_pred, "fallback": fb or fbg, "p_rel_err": err,
                      "residual": max(stl["residual"], stg["residual"]), "trivial": float(pt.norm()) == 0.0})
     rows_nt = [r for r in rows if not r["trivial"]]
@@ -553,7 +559,8 @@ def run_learned(args):
         "params": net.n_params(), "train_solves": args.train, "eval_solves": args.eval, "epochs": args.epochs,
         "generate_s": t_gen, "train_s": t_train, "loss_first_epoch": losses[0], "loss_last_epoch": losses[-1],
         "mean": {k: agg(k) for k in ("fp64_its", "fp64_s", "mixed_its", "mixed_s", "learned_its", "learned_s",
-                                      "guess_its", "guess_s", "predict_s", "p_rel_err")},
+                                      "guess_its", "guess_s", "hydro_its", "hydro_p_rel_err", "predict_s",
+                                      "p_rel_err")},
         "median_p_rel_err": med("p_rel_err"), "trivial_problems": int(sum(r["trivial"] for r in rows)),
         "fallbacks": int(sum(r["fallback"] for r in rows)),
         "max_residual": float(max(r["residual"] for r in rows)),

@@ -86,32 +86,32 @@ def test_training_reduces_loss(gpu):
     from underworld2_gb300.learned import WarmStartNet
     net = WarmStartNet(_ctx(), seed=1, base=8)
     g = torch.Generator(device="cuda").manual_seed(0)
-    X = torch.randn((4, 16, 16, 2), device="cuda", generator=g)
-    Y = torch.stack([X[..., 0], X[..., 1], X[..., 0] - X[..., 1]], -1)
+    X = torch.randn((4, 16, 16, 3), device="cuda", generator=g)
+    Y = torch.stack([X[..., 0], X[..., 1], X[..., 2] - X[..., 1]], -1)
     l0 = net.train_step(X.to(torch.bfloat16), Y, 3e-3)
-    for _ in range(60):
+    for _ in range(150):
         l1 = net.train_step(X.to(torch.bfloat16), Y, 3e-3)
-    assert np.isfinite(l1) and l1 < 0.3 * l0
+    assert np.isfinite(l1) and l1 < 0.4 * l0
 
 
 def test_warm_start_solve_and_fallback(gpu):
     from underworld2_gb300 import learned
     ps = learned.ProblemSet(res=32, ppc=12)
     net = learned.WarmStartNet(ps.ctx, seed=2, base=8)
-    f, _ = ps.assemble(11)
+    f, scales = ps.assemble(11)
     u0, p0, st0 = ps.solve(0)
-    u1, p1, st1, fb = learned.solve_with_warm_start(ps, net, f)
+    u1, p1, st1, fb = learned.solve_with_warm_start(ps, net, f, scales)
     assert not fb and st1["residual"] <= 1e-8 and st0["residual"] <= 1e-8
     du = (u1 - u0).abs().max().item() / u0.abs().max().item()
     pm = lambda p: p - p.mean()
     dp = (pm(p1) - pm(p0)).abs().max().item() / pm(p0).abs().max().item()
     assert du < 1e-6 and dp < 1e-6
-    u3, p3, st3, fb3 = learned.solve_with_warm_start(ps, net, f, mode="guess")
+    u3, p3, st3, fb3 = learned.solve_with_warm_start(ps, net, f, scales, mode="guess")
     assert not fb3 and st3["residual"] <= 1e-8
     # the exact pressure as the first search direction: one Schur iteration suffices
     u4, p4, st4 = ps.solve(1, p_dir=p0 - p0.mean())
     assert st4["residual"] <= 1e-8 and st4["pressure_its"] <= 2 < st0["pressure_its"]
     # a network returning garbage: the plain FP64 solve takes over
     net.out.b.fill_(float("nan"))
-    u2, p2, st2, fb2 = learned.solve_with_warm_start(ps, net, f)
+    u2, p2, st2, fb2 = learned.solve_with_warm_start(ps, net, f, scales)
     assert fb2 and st2["residual"] <= 1e-8

@@ -36,6 +36,7 @@ extern "C" void uwg_ctx_destroy(uwg_ctx* c) {
     cudaFree(c->red);
     if (c->slcn_ws) cudaFree(c->slcn_ws);
     uwg_pop_free(c);
+    if (c->q2_ke) cudaFree(c->q2_ke);
     if (c->red_host) cudaFreeHost(c->red_host);
     uwg_solver_free(c);
     delete c;

@@ -65,6 +65,7 @@ struct uwg_ctx {
     std::vector<void*> ws;  // solver workspaces (freed with the context)
     double* slcn_ws;        // SLCN element matrices and CG vectors (grown on demand)
     void* pop;              // pending population plan (uwg_population.cu)
+    double* q2_ke;          // 3D Q2: packed FP64 element matrices [n_el][3321] for the FP64 apply
     size_t slcn_ws_bytes;
 };
 

@@ -256,6 +256,122 @@ __global__ void __launch_bounds__(BS) k_applyK_q2_3d(uwg_lgeom g, const T* __res
     }
 }
 
+// ---------------------------------------------------------------------------
+// FP64 apply from stored element matrices.  GB300 runs FP64 at 1/64 of the FP32
+// rate, so the FP64 operator (the refinement residuals of the mixed solve and
+// the plain FP64 solve) is applied from the 81x81 element matrices (symmetric,
+// 3321 packed entries, element-major): 6561 FMAs per element instead of the
+// ~25k of the matrix-free pass.  They are built once per assembly from the 125
+// weights, sum-factorised:
+//   K_(A,i),(B,j) = delta_ij sum_k M_kk(A,B) + M_ji(A,B),
+//   M_kl(A,B) = sum_points w d_k N_A d_l N_B,
+// each M_kl a separable contraction of the weights over x, then y, then z.
+// ---------------------------------------------------------------------------
+constexpr int KE_N = 81 * 82 / 2;   // 3321
+
+__device__ __forceinline__ int ke_idx(int r, int c) {   // r <= c, row-major upper triangle
+    return r * 81 - r * (r - 1) / 2 + (c - r);
+}
+
+// one warp per element; shared scratch per warp
+struct ElmatScratch {
+    double w[125];
+    double T1[5 * 5 * 9];     // [q][r][ax*3+bx]
+    double T2[5 * 81];        // [r][(ax*3+bx)*9 + ay*3+by]
+    double M[729];            // [(ax,bx)][(ay,by)][(az,bz)]
+    double L[729];
+};
+
+__global__ void __launch_bounds__(32) k_elmat_q2_3d(uwg_lgeom g, const double* __restrict__ W, double* Ke) {
+    extern __shared__ double smem_raw[];
+    ElmatScratch& S = *reinterpret_cast<ElmatScratch*>(smem_raw);
+    const int lane = threadIdx.x;
+    const int64_t e = blockIdx.x;
+    if (e >= g.n_el) return;
+    int ex[3];
+    double h[3];
+    q2e3(g, e, ex, h);
+    const double sc[3] = {2.0 / h[0], 2.0 / h[1], 2.0 / h[2]};
+    for (int j = lane; j < 125; j += 32) S.w[j] = W[(int64_t)j * g.n_el + e];
+    for (int j = lane; j < 729; j += 32) S.L[j] = 0.0;
+    double* out = Ke + e * (int64_t)KE_N;
+    for (int j = lane; j < KE_N; j += 32) out[j] = 0.0;
+    __syncwarp();
+    for (int k = 0; k < 3; k++)
+        for (int l = 0; l < 3; l++) {
+            // axis factors: X (test side, derivative on axis k), Y (trial side, derivative on axis l)
+            auto X = [&](int d, int t, int a) { return d == k ? sc[d] * c3_D5[t][a] : c3_B5[t][a]; };
+            auto Y = [&](int d, int t, int b) { return d == l ? sc[d] * c3_D5[t][b] : c3_B5[t][b]; };
+            for (int o = lane; o < 225; o += 32) {          // T1[q][r][ab_x]
+                const int ab = o % 9, qr = o / 9, q = qr % 5, r = qr / 5;
+                const int a = ab / 3, b = ab % 3;
+                double s = 0.0;
+                for (int p = 0; p < 5; p++) s += S.w[p + 5 * q + 25 * r] * (X(0, p, a) * Y(0, p, b));
+                S.T1[(q + 5 * r) * 9 + ab] = s;
+            }
+            __syncwarp();
+            for (int o = lane; o < 405; o += 32) {          // T2[r][abx][aby]
+                const int aby = o % 9, abx = (o / 9) % 9, r = o / 81;
+                const int a = aby / 3, b = aby % 3;
+                double s = 0.0;
+                for (int q = 0; q < 5; q++) s += S.T1[(q + 5 * r) * 9 + abx] * (X(1, q, a) * Y(1, q, b));
+                S.T2[r * 81 + abx * 9 + aby] = s;
+            }
+            __syncwarp();
+            for (int o = lane; o < 729; o += 32) {          // M[abx][aby][abz]
+                const int abz = o % 9, xy = o / 9;
+                const int a = abz / 3, b = abz % 3;
+                double s = 0.0;
+                for (int r = 0; r < 5; r++) s += S.T2[r * 81 + xy] * (X(2, r, a) * Y(2, r, b));
+                S.M[o] = s;
+            }
+            __syncwarp();
+            // M_kl(A, B) -> K[(A, l), (B, k)] (upper triangle); diagonal sums into L
+            for (int o = lane; o < 729; o += 32) {
+                const int abz = o % 9, aby = (o / 9) % 9, abx = o / 81;
+                const int A = (abx / 3) + 3 * (aby / 3) + 9 * (abz / 3);
+                const int B = (abx % 3) + 3 * (aby % 3) + 9 * (abz % 3);
+                const double v = S.M[o];
+                if (k == l) S.L[A * 27 + B] += v;
+                const int rr = 3 * A + l, cc = 3 * B + k;
+                if (rr <= cc) out[ke_idx(rr, cc)] += v;
+            }
+            __syncwarp();
+        }
+    for (int o = lane; o < 729; o += 32) {
+        const int A = o / 27, B = o % 27;
+        for (int i = 0; i < 3; i++) {
+            const int rr = 3 * A + i, cc = 3 * B + i;
+            if (rr <= cc) out[ke_idx(rr, cc)] += S.L[o];
+        }
+    }
+}
+
+// y += K x from the stored element matrices: one warp per element, lane owns rows
+__global__ void __launch_bounds__(128) k_applyK_q2_3d_em(uwg_lgeom g, const double* __restrict__ Ke,
+                                                         const uint8_t* __restrict__ bc, bool mask_in,
+                                                         const double* __restrict__ x, double* y) {
+    __shared__ double us[4][81];
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    const int64_t e = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (e >= g.n_el) return;   // warp-uniform
+    int ex[3];
+    double h[3];
+    q2e3(g, e, ex, h);
+    for (int k = lane; k < 81; k += 32) {
+        const int64_t dof = q2node3(g, ex, k / 3) * 3 + k % 3;
+        us[wl][k] = (mask_in && bc[dof]) ? 0.0 : x[dof];
+    }
+    __syncwarp();
+    const double* K = Ke + e * (int64_t)KE_N;
+    for (int rr = lane; rr < 81; rr += 32) {
+        double s = 0.0;
+        for (int cc = 0; cc < 81; cc++) s += K[rr <= cc ? ke_idx(rr, cc) : ke_idx(cc, rr)] * us[wl][cc];
+        const int64_t dof = q2node3(g, ex, rr / 3) * 3 + rr % 3;
+        if (!bc[dof]) atomicAdd(&y[dof], s);
+    }
+}
+
 // G_e[(A,i)][k] = -(prod_{j != i} h_j / 2) GR[i][A][k]
 __device__ __forceinline__ double q2_Ge3(const double* h, int A, int i, int k) {
     const double f = i == 0 ? (h[1] * 0.5) * (h[2] * 0.5) : (i == 1 ? (h[0] * 0.5) * (h[2] * 0.5) : (h[0] * 0.5) * (h[1] * 0.5));
@@ -470,12 +586,33 @@ int uwg_q2_3d_assemble(uwg_ctx* c, const int32_t* off, const int32_t* list, cons
     k_assemble_q2_3d<<<nblk(c->n_el * 32, 128), 128, 0, c->stream>>>(g, off, list, ip_xi, ip_w, eta_p, body_p,
                                                                     c->lev[0].W64, c->lev[1].W64, c->f);
     UWG_CUDA(c, cudaGetLastError());
+    // element matrices of the FP64 apply, rebuilt with every assembly (before the
+    // right-hand side's Dirichlet lifting uses the operator)
+    if (!c->q2_ke) {
+        cudaError_t e = cudaMalloc((void**)&c->q2_ke, sizeof(double) * (size_t)KE_N * c->n_el);
+        if (e != cudaSuccess) {
+            c->q2_ke = nullptr;   // no room: the matrix-free FP64 apply is used
+            cudaGetLastError();
+        }
+    }
+    if (c->q2_ke) {
+        k_elmat_q2_3d<<<(unsigned)c->n_el, 32, sizeof(ElmatScratch), c->stream>>>(g, c->lev[0].W64, c->q2_ke);
+        UWG_CUDA(c, cudaGetLastError());
+    }
     return UWG_OK;
 }
 
 template <typename T>
 int uwg_q2_3d_applyK(uwg_ctx* c, const T* x, T* y, bool mask_in) {
     const uwg_level& L = c->lev[0];
+    if constexpr (sizeof(T) == 8) {
+        if (c->q2_ke) {
+            k_applyK_q2_3d_em<<<nblk(L.n_el * 32, 128), 128, 0, c->stream>>>(uwg_level_geom(c, 0), c->q2_ke, L.bc,
+                                                                             mask_in, x, y);
+            UWG_CUDA(c, cudaGetLastError());
+            return UWG_OK;
+        }
+    }
     const T* W;
     if constexpr (sizeof(T) == 8) W = (const T*)L.W64; else W = (const T*)L.W32;
     constexpr int BS = sizeof(T) == 8 ? 64 : 128;
@@ -488,6 +625,7 @@ template int uwg_q2_3d_applyK<float>(uwg_ctx*, const float*, float*, bool);
 
 int uwg_q2_3d_diag(uwg_ctx* c, double* sinv) {
     const uwg_level& L = c->lev[0];
+
     k_diag_q2_3d<<<nblk(L.n_el, 64), 64, 0, c->stream>>>(uwg_level_geom(c, 0), L.W64, L.bc, L.diag64, sinv);
     UWG_CUDA(c, cudaGetLastError());
     return UWG_OK;

@@ -1,9 +1,10 @@
 """Learned warm start for the Stokes solve.
 
-A small convolutional network (about 1.15M parameters, 4 resolution levels,
+A small convolutional network (about 1.16M parameters, 4 resolution levels,
 32 base channels, encoder-decoder with additive skips) maps per-cell
-log10-viscosity and buoyancy of a 2D Q1/dQ0 problem to the cell velocity and
-pressure.  It is trained on solves of this library's own BSSCR path, and its
+log10-viscosity and buoyancy of a 2D Q1/dQ0 problem (with the buoyancy's
+column integral, the hydrostatic pressure, as a third input) to the cell
+velocity and pressure.  It is trained on solves of this library's own BSSCR path, and its
 pressure is the initial guess of the Schur FGMRES (``zero_guess = 0``); the
 velocity channels are trained alongside but the BSSCR iteration only takes a
 pressure guess.  Every convolution runs as BF16 tensor-core GEMMs with FP32
@@ -114,7 +115,8 @@ class Conv3x3:
 
 
 class WarmStartNet:
-    """Encoder-decoder CNN: 2 input channels (log10 viscosity / 3, buoyancy) on an
+    """Encoder-decoder CNN: 3 input channels (log10 viscosity / 3, buoyancy,
+    scaled hydrostatic pressure) on an
     H x W cell grid (H, W divisible by 8) -> 3 output channels (viscosity-scaled
     velocity x and y, pressure) per cell."""
 
@@ -124,7 +126,7 @@ class WarmStartNet:
         g = torch.Generator().manual_seed(seed)
         c1, c2, c3, c4 = base, 2 * base, 4 * base, 8 * base
         C = lambda a, b, r=True: Conv3x3(a, b, r, g, dev)
-        self.e1a, self.e1 = C(2, c1), C(c1, c1)
+        self.e1a, self.e1 = C(3, c1), C(c1, c1)
         self.e2a, self.e2 = C(c1, c2), C(c2, c2)
         self.e3a, self.e3 = C(c2, c3), C(c3, c3)
         self.bt = C(c3, c4)
@@ -171,7 +173,7 @@ class WarmStartNet:
         return out
 
     def forward(self, x):
-        """x: [nb, H, W, 2] BF16 -> [nb, H, W, 3] FP32; activations kept for backward."""
+        """x: [nb, H, W, 3] BF16 -> [nb, H, W, 3] FP32; activations kept for backward."""
         o = self.ops
         a = {"x": x}
         a["e1a"] = self.e1a.forward(o, x)
@@ -308,19 +310,32 @@ def cell_centres(res, device):
 
 
 def features(log_eta, rho, res, device):
+    """Per-cell inputs: log10 viscosity / 3, buoyancy, and the hydrostatic
+    pressure of the buoyancy column above the cell (mean-free, divided by its
+    RMS); plus the scales of the problem: the reference viscosity 10^mean(log10
+    eta) and the RMS of the hydrostatic pressure, by which targets are divided."""
     xc = cell_centres(res, device)
     le = log_eta(xc)
-    f = torch.stack([le / 3.0, rho(xc)], 1).reshape(res, res, 2)
-    return f, float(le.mean())
+    r = rho(xc).reshape(res, res)
+    # body force (0, -rho): dp/dy = -rho, p = 0 on top -> p(y) = sum of rho over the cells above
+    hyd = torch.flip(torch.cumsum(torch.flip(r, [0]), 0), [0]) / res - 0.5 * r / res
+    hyd = hyd - hyd.mean()
+    s = float(torch.sqrt((hyd * hyd).mean()))
+    s = s if s > 0.0 else 1.0
+    f = torch.stack([le.reshape(res, res) / 3.0, r, hyd / s], 2)
+    return f, (10.0 ** float(le.mean()), s)
 
 
-def targets(u, p, res, eta_ref):
-    """Cell velocity (mean of the 4 nodes) scaled by eta_ref and mean-free cell pressure."""
+def targets(u, p, res, scales):
+    """Cell velocity (mean of the 4 nodes) and mean-free cell pressure, both
+    divided by the hydrostatic scale, velocity also multiplied by the reference
+    viscosity."""
+    eta_ref, s = scales
     n = res + 1
     U = u.reshape(n, n, 2)
     uc = 0.25 * (U[:-1, :-1] + U[:-1, 1:] + U[1:, :-1] + U[1:, 1:])
     pc = (p - p.mean()).reshape(res, res, 1)
-    return torch.cat([uc * eta_ref, pc], 2)
+    return torch.cat([uc * (eta_ref / s), pc / s], 2)
 
 
 def freeslip_mask(res):
@@ -354,8 +369,8 @@ class ProblemSet:
         ip_xi = ctx.pic_map(x, off, lst)
         ip_w = ctx.dvc_weights(off, ip_xi)
         ctx.assemble(off, lst, ip_xi, ip_w, eta, body.contiguous())
-        f, le_mean = features(log_eta, rho, self.res, ctx.device)
-        return f, 10.0 ** le_mean
+        f, scales = features(log_eta, rho, self.res, ctx.device)
+        return f, scales
 
     def solve(self, mixed, p0=None, p_dir=None, rtol=1e-8):
         """Solve the assembled problem; p0: initial pressure, p_dir: first search
@@ -373,13 +388,13 @@ class ProblemSet:
 def generate(ps, seeds, rtol=1e-8):
     """Inputs [n, res, res, 2] and targets [n, res, res, 3] (FP32, device)."""
     res = ps.res
-    X = torch.empty((len(seeds), res, res, 2), dtype=torch.float32, device=ps.ctx.device)
+    X = torch.empty((len(seeds), res, res, 3), dtype=torch.float32, device=ps.ctx.device)
     Y = torch.empty((len(seeds), res, res, 3), dtype=torch.float32, device=ps.ctx.device)
     for i, s in enumerate(seeds):
-        f, eta_ref = ps.assemble(s)
+        f, scales = ps.assemble(s)
         u, p, st = ps.solve(1, rtol=rtol)
         X[i] = f.float()
-        Y[i] = targets(u, p, res, eta_ref).float()
+        Y[i] = targets(u, p, res, scales).float()
     return X, Y
 
 
@@ -407,19 +422,19 @@ def train(net, X, Y, epochs=20, batch=8, lr=1e-3, lr_final=1e-4, seed=0, log=Non
     return losses
 
 
-def predict_pressure(net, f):
+def predict_pressure(net, f, scales):
     """Cell pressure guess (mean-free) for one problem's feature grid."""
     y = net.predict(f[None].to(_BF).contiguous())
-    p = y[0, :, :, 2].reshape(-1).double() * float(net.scale[2])
+    p = y[0, :, :, 2].reshape(-1).double() * (float(net.scale[2]) * scales[1])
     return p - p.mean()
 
 
-def solve_with_warm_start(ps, net, f, rtol=1e-8, mode="direction"):
+def solve_with_warm_start(ps, net, f, scales, rtol=1e-8, mode="direction"):
     """Mixed-precision solve using the network's pressure -- as the first search
     direction of the Schur FGMRES (mode "direction": the iteration's least-squares
     step weighs it) or as the initial guess (mode "guess") -- and the plain FP64
     solve if that does not reach rtol.  Returns (u, p, stats, fell_back)."""
-    p0 = predict_pressure(net, f)
+    p0 = predict_pressure(net, f, scales)
     try:
         if not bool(torch.isfinite(p0).all()):
             raise FloatingPointError("non-finite network output")
