@@ -568,6 +568,87 @@ def run_learned(args):
         "speedup_mixed_vs_fp64": agg("fp64_s") / agg("mixed_s")}))
 
 
+def run_convection(args):
+    """Thermal-convection time loop of the 3D Q2/dPc1 configuration
+    (`--config conv3d_q2` or `conv3d_q2_small`), `--steps` steps after one
+    untimed: T lives on the Q1 mesh of the same elements (T = 1 at the bottom,
+    0 at the top, initial 1 - z + seeded 1e-2 noise, diffusivity 1); per step
+    T is sampled at the particles, viscosity exp(-9.2 T) and buoyancy Ra T
+    (Ra = 1e6) are assembled, the Stokes system is solved in mixed precision
+    from the previous pressure, T is advanced by one SUPG step with the
+    velocity at the Q1 nodes, and the particles by one RK2 step, all at the
+    smaller of the particle and SUPG Courant steps.  The plain FP64 solve of
+    the last step's system is timed beside it."""
+    import numpy as np
+    import torch
+    from underworld2_gb300._core import Context, rng_seed
+    cfg = CONFIGS[args.config]
+    assert cfg.get("order", 1) == 2 and cfg["dim"] == 3, "convection loop: a 3D Q2/dPc1 config"
+    res = cfg["res"]
+    ctx = Context(3, res, (0.0,) * 3, (1.0,) * 3, order=2, porder=1)
+    ctx.set_bcs(freeslip_mask(ctx))
+    tctx = Context(3, res, (0.0,) * 3, (1.0,) * 3)
+    x, owner, off, lst, _ = ctx.layout_random(cfg["ppc"], rng_seed(13))
+    nq = [r + 1 for r in res]
+    zz, yy, xx = torch.meshgrid(*[torch.tensor(a, device=ctx.device) for a in reversed(tctx.axes)], indexing="ij")
+    g = torch.Generator(device="cpu").manual_seed(7)
+    a = (torch.rand(4, 3, generator=g, dtype=torch.float64) * 2.0 - 1.0).tolist()
+    noise = sum(a[k - 1][0] * torch.cos(torch.pi * k * xx + a[k - 1][1]) * torch.cos(torch.pi * k * yy + a[k - 1][2])
+                for k in range(1, 5)) * torch.sin(torch.pi * zz) / 4.0
+    T = (1.0 - zz + 0.01 * noise).clamp(0.0, 1.0).reshape(-1).contiguous()
+    Tdot = torch.zeros_like(T)
+    tbc = ((zz == 0.0) | (zz == 1.0)).reshape(-1).to(torch.uint8)
+    Tbc = T.clone()
+    kappa = torch.ones(tctx.n_el * 27, dtype=torch.float64, device=ctx.device)
+    u = ctx.zeros(ctx.n_vdof)
+    p = ctx.zeros(ctx.n_pdof)
+    n2 = [2 * r + 1 for r in res]
+    opts = dict(rtol=1e-8, inner_rtol=1e-10, outer_rtol=1e-9, smooth_steps=2, restart=120, schur_pc=0, max_outer=500)
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    rec = []
+
+    def step(timed):
+        e = [ev() for _ in range(5)]
+        e[0].record()
+        Tp = tctx.interpolate_field(x, T, 1)[0][:, 0]
+        eta = torch.exp(-9.2 * Tp).contiguous()
+        body = torch.zeros_like(x)
+        body[:, 2] = 1e6 * Tp
+        ip_xi = ctx.pic_map(x, off, lst)
+        ip_w = ctx.dvc_weights(off, ip_xi)
+        ctx.assemble(off, lst, ip_xi, ip_w, eta, body.contiguous())
+        e[1].record()
+        st = ctx.solve(u, p, mixed=1, zero_guess=0, **opts)
+        e[2].record()
+        uq1 = u.reshape(n2[2], n2[1], n2[0], 3)[::2, ::2, ::2].contiguous().reshape(-1)
+        dt = min(ctx.max_dt(u), tctx.advdiff_max_dt(uq1, kappa))
+        tctx.advdiff_step(dt, uq1, kappa, T, Tdot, tbc, Tbc)
+        e[3].record()
+        ctx.rk2(x, u, dt)
+        ctx.update_owners(x, owner, off, lst)
+        e[4].record()
+        torch.cuda.synchronize()
+        if timed:
+            rec.append({"assemble_s": e[0].elapsed_time(e[1]) / 1e3, "solve_s": e[1].elapsed_time(e[2]) / 1e3,
+                        "advdiff_s": e[2].elapsed_time(e[3]) / 1e3, "advect_s": e[3].elapsed_time(e[4]) / 1e3,
+                        "step_s": e[0].elapsed_time(e[4]) / 1e3, "dt": dt, "outer_its": st["pressure_its"],
+                        "residual": st["residual"], "T_mean": float(T.mean()), "vrms_proxy": float(u.norm())})
+
+    step(False)
+    for _ in range(args.steps):
+        step(True)
+    # the plain FP64 path on the last step's system
+    u64, p64 = ctx.zeros(ctx.n_vdof), ctx.zeros(ctx.n_pdof)
+    st64 = ctx.solve(u64, p64, mixed=0, **opts)
+    agg = lambda k: float(np.mean([r[k] for r in rec]))
+    print(json.dumps({"convection": workload_name(args.config), "steps": args.steps,
+                      "per_step_s": agg("step_s"), "phases_s": {k: agg(k) for k in ("assemble_s", "solve_s",
+                                                                                     "advdiff_s", "advect_s")},
+                      "mean_outer_its": agg("outer_its"), "max_residual": max(r["residual"] for r in rec),
+                      "fp64_solve_s": st64["total_time"], "fp64_outer_its": st64["pressure_its"],
+                      "fp64_residual": st64["residual"], "steps_detail": rec[-3:]}))
+
+
 def run_profile_solve(args):
     """One map + DVC + assembly + solve of the workload, untimed (the target of
     the launch-list captures recorded under profiles/); `--kernel-ppc` lowers
@@ -671,6 +752,8 @@ def main():
                     help="only launch one operator kernel, or time SUPG / SLCN advection-diffusion steps (profiling)")
     ap.add_argument("--kernel-ppc", type=int, default=0)
     ap.add_argument("--profile-solve", action="store_true", help="one untimed solve (profiling target)")
+    ap.add_argument("--convection", action="store_true",
+                    help="time the 3D Q2/dPc1 thermal-convection loop (advection-diffusion + Stokes + RK2)")
     ap.add_argument("--learned", action="store_true",
                     help="train the warm-start CNN on generated 2D 128^2 solves and evaluate it on held-out seeds")
     ap.add_argument("--train", type=int, default=800)
@@ -696,6 +779,9 @@ def main():
         return
     if args.learned:
         run_learned(args)
+        return
+    if args.convection:
+        run_convection(args)
         return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
