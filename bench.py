@@ -615,24 +615,35 @@ def run_convection(args):
         body = torch.zeros_like(x)
         body[:, 2] = 1e6 * Tp
         ip_xi = ctx.pic_map(x, off, lst)
+        n_in = int(off[-1])
+        diag = {"nan_positions": int(torch.isnan(x).any(dim=1).sum()), "listed": n_in,
+                "max_abs_xi": float(ip_xi[:n_in].abs().max()) if n_in else 0.0,
+                "max_per_cell": int((off[1:] - off[:-1]).max())}
+        if diag["nan_positions"] or diag["max_abs_xi"] > 1.0 + 1e-9:
+            raise RuntimeError("convection loop: inconsistent particle state %s" % diag)
         ip_w = ctx.dvc_weights(off, ip_xi)
         ctx.assemble(off, lst, ip_xi, ip_w, eta, body.contiguous())
         e[1].record()
         st = ctx.solve(u, p, mixed=1, zero_guess=0, **opts)
+        if not bool(torch.isfinite(u).all()):
+            raise RuntimeError("convection loop: non-finite velocity %s" % st)
         e[2].record()
         uq1 = u.reshape(n2[2], n2[1], n2[0], 3)[::2, ::2, ::2].contiguous().reshape(-1)
         dt = min(ctx.max_dt(u), tctx.advdiff_max_dt(uq1, kappa))
         tctx.advdiff_step(dt, uq1, kappa, T, Tdot, tbc, Tbc)
         e[3].record()
         ctx.rk2(x, u, dt)
-        ctx.update_owners(x, owner, off, lst)
+        lost = ctx.update_owners(x, owner, off, lst)
         e[4].record()
+        diag["lost"] = lost
+        diag["dt"] = dt
         torch.cuda.synchronize()
         if timed:
             rec.append({"assemble_s": e[0].elapsed_time(e[1]) / 1e3, "solve_s": e[1].elapsed_time(e[2]) / 1e3,
                         "advdiff_s": e[2].elapsed_time(e[3]) / 1e3, "advect_s": e[3].elapsed_time(e[4]) / 1e3,
                         "step_s": e[0].elapsed_time(e[4]) / 1e3, "dt": dt, "outer_its": st["pressure_its"],
-                        "residual": st["residual"], "T_mean": float(T.mean()), "vrms_proxy": float(u.norm())})
+                        "residual": st["residual"], "T_mean": float(T.mean()), "vrms_proxy": float(u.norm()),
+                        "particles": diag})
 
     step(False)
     for _ in range(args.steps):

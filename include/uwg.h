@@ -114,7 +114,8 @@ int uwg_dvc_weights(uwg_ctx* ctx, int res, const int32_t* cell_offsets, double* 
  * looks its address up (cudaGetSymbolAddress) and should come before any
  * stream capture.  All calls share that array: calls that overlap on the GPU
  * (different streams or threads) race and must be serialised by the caller.
- * Returns 0, UWG_ERR_ARG, UWG_ERR_CUDA, UWG_ERR_EMPTY_CELL or UWG_ERR_CELL_FULL. */
+ * Returns 0, UWG_ERR_ARG, UWG_ERR_CUDA, UWG_ERR_EMPTY_CELL, UWG_ERR_CELL_FULL or UWG_ERR_STATE
+ * (a listed particle's local coordinates lie outside [-1, 1]). */
 int uwg_dvc_weights_noalloc(int dim, int res, int64_t n_el, const int32_t* cell_offsets, double* ip_xi,
                             double* ip_w, void* cuda_stream);
 

@@ -149,14 +149,28 @@ __global__ void __launch_bounds__(32 * DVC_WARPS) k_dvc(dvc_args a) {
 
         // seeding (:687-705 / :735-756): the seed cells of all particles are
         // computed in parallel (same expressions), then claimed in order
+        bool bad = false;
         for (int i = lane; i < n; i += 32) {
-            int k = (int)((xs[i * 3 + 0] - -1.0) / dx);
-            int j = (int)((xs[i * 3 + 1] - -1.0) / dx);
-            int l = DIM == 3 ? (int)((xs[i * 3 + 2] - -1.0) / dx) : 0;
+            // a local coordinate outside [-1, 1] (a particle listed in the wrong
+            // element, or a non-finite position) would seed outside the grid:
+            // reported, never indexed
+            const double vx = (xs[i * 3 + 0] - -1.0) / dx, vy = (xs[i * 3 + 1] - -1.0) / dx;
+            const double vz = DIM == 3 ? (xs[i * 3 + 2] - -1.0) / dx : 0.0;
+            if (!(vx >= 0.0 && vx < R + 1.0 && vy >= 0.0 && vy < R + 1.0 && vz >= 0.0 && vz < R + 1.0)) {
+                bad = true;
+                continue;
+            }
+            int k = (int)vx;
+            int j = (int)vy;
+            int l = DIM == 3 ? (int)vz : 0;
             if (k == R) k--;
             if (j == R) j--;
             if (DIM == 3 && l == R) l--;
             hdr[(NM + i) * 2] = k + j * R + l * R * R;   // pool-1 headers are unused until round 1
+        }
+        if (__any_sync(0xffffffffu, bad)) {
+            if (lane == 0) dvc_fail(a.status, UWG_ERR_STATE, el);
+            continue;
         }
         __syncwarp();
         for (int i = 0; i < n; i++) {
@@ -345,6 +359,9 @@ extern "C" int uwg_dvc_weights(uwg_ctx* c, int res, const int32_t* cell_offsets,
     if (st[0] == UWG_ERR_CELL_FULL)
         return uwg_set_error(c, UWG_ERR_CELL_FULL, "element " + std::to_string(st[1]) +
                              " exceeds the DVC kernel limits (128 particles per element)");
+    if (st[0] == UWG_ERR_STATE)
+        return uwg_set_error(c, UWG_ERR_STATE, "element " + std::to_string(st[1]) +
+                             " lists a particle whose local coordinates lie outside [-1, 1]");
     return UWG_OK;
 }
 
@@ -421,5 +438,5 @@ extern "C" int uwg_dvc_weights_noalloc(int dim, int res, int64_t n_el, const int
     int32_t st[2] = {0, 0};
     if (cudaMemcpyAsync(st, a.status, 8, cudaMemcpyDeviceToHost, stream) != cudaSuccess) return UWG_ERR_CUDA;
     if (cudaStreamSynchronize(stream) != cudaSuccess) return UWG_ERR_CUDA;
-    return st[0];   // 0, UWG_ERR_EMPTY_CELL or UWG_ERR_CELL_FULL
+    return st[0];   // 0, UWG_ERR_EMPTY_CELL, UWG_ERR_CELL_FULL or UWG_ERR_STATE
 }
