@@ -160,7 +160,8 @@ def test_solve_matches_direct(gpu, dim, res, ppc, mixed):
     np.testing.assert_array_equal(x_gpu.cpu().numpy(), x_or)
 
 
-@pytest.mark.parametrize("dim,res", [(2, (6, 6)), (3, (3, 3, 3))])
+# meshes above one block of cells (128) as well as below
+@pytest.mark.parametrize("dim,res", [(2, (6, 6)), (3, (3, 3, 3)), (2, (24, 20)), (3, (8, 7, 6))])
 def test_owner_update_tables(gpu, dim, res):
     """Random moves; owners and cell tables equal the sequential reference semantics."""
     from underworld2_gb300._core import rng_seed

@@ -416,7 +416,7 @@ extern "C" int uwg_update_owners(uwg_ctx* c, int64_t np, const double* x, int32_
     UWG_CUDA(c, cudaMallocAsync(&b_tmp.p, ((size_t)std::max(tot[0], 1) + (size_t)std::max(tot[1], 1)) * 4, s));
     int32_t* tmp = (int32_t*)b_tmp.p;
     int32_t* nlist = tmp + std::max(tot[0], 1);
-    k_owner_replay<<<nblk(n_el), 128, 0, s>>>(n_el, cell_offsets, cell_list, ev_off, (int64_t*)b_ev.p,
+    k_owner_replay<<<nblk(n_el, 128), 128, 0, s>>>(n_el, cell_offsets, cell_list, ev_off, (int64_t*)b_ev.p,
                                               tmp_off, tmp, new_off, nlist, err);
     UWG_CUDA(c, cudaGetLastError());
     int32_t herr = 0;
