@@ -372,137 +372,6 @@ __global__ void __launch_bounds__(128) k_applyK_q2_3d_em(uwg_lgeom g, const doub
     }
 }
 
-// ---------------------------------------------------------------------------
-// FP32 apply, one warp per element: the sum-factorised passes (z, y, x forward
-// to the 125 points, stresses, x, y, z back) each spread over the lanes, the
-// intermediate planes in shared memory, nothing recomputed.
-// ---------------------------------------------------------------------------
-struct WarpQ2 {
-    float u[81];
-    float tz[2][3][5][9];     // forward: [value/z-derivative][comp][r][ab]; backward: P1/P3 [i][r][ab]
-    float t[3][3][25][3];     // forward: [T1/T2/T3][comp][qr][a]; backward: [L1/L2/L3][i][qr][a]
-    float sig[125][6];        // stresses: xx, yy, zz, xy, xz, yz
-};
-
-__global__ void __launch_bounds__(128) k_applyK_q2_3d_warp(uwg_lgeom g, const float* __restrict__ W,
-                                                           const uint8_t* __restrict__ bc, bool mask_in,
-                                                           const float* __restrict__ x, float* y) {
-    extern __shared__ float smem_q2w[];
-    WarpQ2& S = reinterpret_cast<WarpQ2*>(smem_q2w)[threadIdx.x >> 5];
-    const int lane = threadIdx.x & 31;
-    const int64_t e = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    if (e >= g.n_el) return;   // warp-uniform
-    int ex[3];
-    double h[3];
-    q2e3(g, e, ex, h);
-    const float sx = 2.0f / (float)h[0], sy = 2.0f / (float)h[1], sz = 2.0f / (float)h[2];
-    for (int k = lane; k < 81; k += 32) {
-        const int64_t dof = q2node3(g, ex, k / 3) * 3 + k % 3;
-        S.u[k] = (mask_in && bc[dof]) ? 0.f : x[dof];
-    }
-    __syncwarp();
-    // z: tz[0][c][r][ab] = sum_k B5[r][k] u[ab + 9k][c], tz[1] with D5
-    for (int o = lane; o < 135; o += 32) {
-        const int ab = o % 9, r = (o / 9) % 5, c = o / 45;
-        float tv = 0.f, sv = 0.f;
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-            const float uv = S.u[(ab + 9 * k) * 3 + c];
-            tv += c3_B5f[r][k] * uv;
-            sv += c3_D5f[r][k] * uv;
-        }
-        S.tz[0][c][r][ab] = tv;
-        S.tz[1][c][r][ab] = sv;
-    }
-    __syncwarp();
-    // y: T1 = B_y tz, T2 = D_y tz, T3 = B_y sz at (q, r), per component and a
-    for (int o = lane; o < 225; o += 32) {
-        const int a = o % 3, qr = (o / 3) % 25, c = o / 75;
-        const int q = qr % 5, r = qr / 5;
-        float v1 = 0.f, v2 = 0.f, v3 = 0.f;
-#pragma unroll
-        for (int b = 0; b < 3; b++) {
-            const float tv = S.tz[0][c][r][a + 3 * b], sv = S.tz[1][c][r][a + 3 * b];
-            v1 += c3_B5f[q][b] * tv;
-            v2 += c3_D5f[q][b] * tv;
-            v3 += c3_B5f[q][b] * sv;
-        }
-        S.t[0][c][qr][a] = v1;
-        S.t[1][c][qr][a] = v2;
-        S.t[2][c][qr][a] = v3;
-    }
-    __syncwarp();
-    // x: gradients at the points, stresses
-    for (int pt = lane; pt < 125; pt += 32) {
-        const int p = pt % 5, qr = pt / 5;
-        float gr[3][3];
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-            float d0 = 0.f, d1 = 0.f, d2 = 0.f;
-#pragma unroll
-            for (int a = 0; a < 3; a++) {
-                d0 += c3_D5f[p][a] * S.t[0][c][qr][a];
-                d1 += c3_B5f[p][a] * S.t[1][c][qr][a];
-                d2 += c3_B5f[p][a] * S.t[2][c][qr][a];
-            }
-            gr[c][0] = sx * d0;
-            gr[c][1] = sy * d1;
-            gr[c][2] = sz * d2;
-        }
-        const float w = W[(int64_t)pt * g.n_el + e];
-        S.sig[pt][0] = w * (gr[0][0] + gr[0][0]);
-        S.sig[pt][1] = w * (gr[1][1] + gr[1][1]);
-        S.sig[pt][2] = w * (gr[2][2] + gr[2][2]);
-        S.sig[pt][3] = w * (gr[0][1] + gr[1][0]);
-        S.sig[pt][4] = w * (gr[0][2] + gr[2][0]);
-        S.sig[pt][5] = w * (gr[1][2] + gr[2][1]);
-    }
-    __syncwarp();
-    // x back: L1[i] = sum_p D5 sigma_i0, L2[i] = sum_p B5 sigma_i1, L3[i] = sum_p B5 sigma_i2
-    for (int o = lane; o < 225; o += 32) {
-        const int a = o % 3, qr = (o / 3) % 25, i = o / 75;
-        const int s0 = i == 0 ? 0 : (i == 1 ? 3 : 4);   // sigma_i0
-        const int s1 = i == 0 ? 3 : (i == 1 ? 1 : 5);   // sigma_i1
-        const int s2 = i == 0 ? 4 : (i == 1 ? 5 : 2);   // sigma_i2
-        float l1 = 0.f, l2 = 0.f, l3 = 0.f;
-#pragma unroll
-        for (int p = 0; p < 5; p++) {
-            const float* sg = S.sig[p + 5 * qr];
-            l1 += c3_D5f[p][a] * sg[s0];
-            l2 += c3_B5f[p][a] * sg[s1];
-            l3 += c3_B5f[p][a] * sg[s2];
-        }
-        S.t[0][i][qr][a] = sx * l1;
-        S.t[1][i][qr][a] = sy * l2;
-        S.t[2][i][qr][a] = sz * l3;
-    }
-    __syncwarp();
-    // y back: P1 = sum_q B5 L1 + D5 L2, P3 = sum_q B5 L3
-    for (int o = lane; o < 135; o += 32) {
-        const int ab = o % 9, r = (o / 9) % 5, i = o / 45;
-        const int a = ab % 3, b = ab / 3;
-        float p1 = 0.f, p3 = 0.f;
-#pragma unroll
-        for (int q = 0; q < 5; q++) {
-            const int qr = q + 5 * r;
-            p1 += c3_B5f[q][b] * S.t[0][i][qr][a] + c3_D5f[q][b] * S.t[1][i][qr][a];
-            p3 += c3_B5f[q][b] * S.t[2][i][qr][a];
-        }
-        S.tz[0][i][r][ab] = p1;
-        S.tz[1][i][r][ab] = p3;
-    }
-    __syncwarp();
-    // z back and scatter
-    for (int o = lane; o < 81; o += 32) {
-        const int i = o % 3, A = o / 3, ab = A % 9, cz = A / 9;
-        float v = 0.f;
-#pragma unroll
-        for (int r = 0; r < 5; r++) v += c3_B5f[r][cz] * S.tz[0][i][r][ab] + c3_D5f[r][cz] * S.tz[1][i][r][ab];
-        const int64_t dof = q2node3(g, ex, A) * 3 + i;
-        if (!bc[dof]) atomicAdd(&y[dof], v);
-    }
-}
-
 // G_e[(A,i)][k] = -(prod_{j != i} h_j / 2) GR[i][A][k]
 __device__ __forceinline__ double q2_Ge3(const double* h, int A, int i, int k) {
     const double f = i == 0 ? (h[1] * 0.5) * (h[2] * 0.5) : (i == 1 ? (h[0] * 0.5) * (h[2] * 0.5) : (h[0] * 0.5) * (h[1] * 0.5));
@@ -743,12 +612,6 @@ int uwg_q2_3d_applyK(uwg_ctx* c, const T* x, T* y, bool mask_in) {
             UWG_CUDA(c, cudaGetLastError());
             return UWG_OK;
         }
-    }
-    if constexpr (sizeof(T) == 4) {
-        k_applyK_q2_3d_warp<<<nblk(L.n_el * 32, 128), 128, 4 * sizeof(WarpQ2), c->stream>>>(
-            uwg_level_geom(c, 0), L.W32, L.bc, mask_in, x, y);
-        UWG_CUDA(c, cudaGetLastError());
-        return UWG_OK;
     }
     const T* W;
     if constexpr (sizeof(T) == 8) W = (const T*)L.W64; else W = (const T*)L.W32;
