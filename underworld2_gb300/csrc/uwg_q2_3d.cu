@@ -132,6 +132,121 @@ __global__ void k_assemble_q2_3d(uwg_lgeom g, const int32_t* off, const int32_t*
         }
 }
 
+// One output component I of y += K x for the thread's element.  sigma_Ij =
+// w (d_j u_I + d_I u_j) needs five gradient entries per point: d_j u_I (three)
+// and d_I u_c for the two other components, so the forward passes carry the
+// value/derivative planes of component I and only the I-direction planes of
+// the others.  The x-direction point loop is unrolled; z and y run as loops.
+template <typename T, int BS, int I>
+__device__ __forceinline__ void q2_3d_apply_component(const uwg_lgeom& g, const T* us, const T* __restrict__ Wp,
+                                                      int64_t st, const T* sc, const int* ex, uint32_t fb, T* y) {
+    constexpr int C1 = (I + 1) % 3, C2 = (I + 2) % 3;
+    const int tid = threadIdx.x;
+    T out[27];
+#pragma unroll
+    for (int A = 0; A < 27; A++) out[A] = (T)0;
+#pragma unroll 1
+    for (int r = 0; r < 5; r++) {
+        // z stage: value (tI) and z derivative (sI) of u_I; the I-direction plane of u_C1, u_C2
+        T tI[9], sI[9], o1[9], o2[9];
+#pragma unroll
+        for (int ab = 0; ab < 9; ab++) {
+            T t = 0, sd = 0, v1 = 0, v2 = 0;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                const T* un = us + ((ab + 9 * k) * 3) * BS + tid;
+                const T uI = un[I * BS], u1 = un[C1 * BS], u2 = un[C2 * BS];
+                const T bz = B5<T>(r, k), dz = D5<T>(r, k);
+                const T oz = I == 2 ? dz : bz;
+                t += bz * uI;
+                sd += dz * uI;
+                v1 += oz * u1;
+                v2 += oz * u2;
+            }
+            tI[ab] = t;
+            sI[ab] = sd;
+            o1[ab] = v1;
+            o2[ab] = v2;
+        }
+        T P1[9], P3[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) P1[k] = P3[k] = (T)0;
+#pragma unroll 1
+        for (int q = 0; q < 5; q++) {
+            // y stage
+            T A1[3], A2[3], A3[3], O1[3], O2[3];
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                T v1 = 0, v2 = 0, v3 = 0, w1 = 0, w2 = 0;
+#pragma unroll
+                for (int b = 0; b < 3; b++) {
+                    const T by = B5<T>(q, b), dy = D5<T>(q, b);
+                    const T oy = I == 1 ? dy : by;
+                    v1 += by * tI[a + 3 * b];
+                    v2 += dy * tI[a + 3 * b];
+                    v3 += by * sI[a + 3 * b];
+                    w1 += oy * o1[a + 3 * b];
+                    w2 += oy * o2[a + 3 * b];
+                }
+                A1[a] = v1;
+                A2[a] = v2;
+                A3[a] = v3;
+                O1[a] = w1;
+                O2[a] = w2;
+            }
+            T L1[3] = {0, 0, 0}, L2[3] = {0, 0, 0}, L3[3] = {0, 0, 0};
+#pragma unroll
+            for (int p = 0; p < 5; p++) {
+                // x stage: the five gradient entries at point (p, q, r)
+                T gI[3], h1 = 0, h2 = 0;
+                {
+                    T d0 = 0, d1 = 0, d2 = 0;
+#pragma unroll
+                    for (int a = 0; a < 3; a++) {
+                        const T bx = B5<T>(p, a), dx = D5<T>(p, a);
+                        const T ox = I == 0 ? dx : bx;
+                        d0 += dx * A1[a];
+                        d1 += bx * A2[a];
+                        d2 += bx * A3[a];
+                        h1 += ox * O1[a];
+                        h2 += ox * O2[a];
+                    }
+                    gI[0] = sc[0] * d0;
+                    gI[1] = sc[1] * d1;
+                    gI[2] = sc[2] * d2;
+                    h1 *= sc[I];
+                    h2 *= sc[I];
+                }
+                const T w = Wp[(int64_t)(p + 5 * q + 25 * r) * st];
+                T sg[3];
+                sg[I] = w * (gI[I] + gI[I]);
+                sg[C1] = w * (gI[C1] + h1);
+                sg[C2] = w * (gI[C2] + h2);
+#pragma unroll
+                for (int a = 0; a < 3; a++) {
+                    L1[a] += D5<T>(p, a) * sg[0];
+                    L2[a] += B5<T>(p, a) * sg[1];
+                    L3[a] += B5<T>(p, a) * sg[2];
+                }
+            }
+#pragma unroll
+            for (int b = 0; b < 3; b++)
+#pragma unroll
+                for (int a = 0; a < 3; a++) {
+                    P1[a + 3 * b] += B5<T>(q, b) * (sc[0] * L1[a]) + D5<T>(q, b) * (sc[1] * L2[a]);
+                    P3[a + 3 * b] += B5<T>(q, b) * (sc[2] * L3[a]);
+                }
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+#pragma unroll
+            for (int ab = 0; ab < 9; ab++) out[ab + 9 * c] += B5<T>(r, c) * P1[ab] + D5<T>(r, c) * P3[ab];
+    }
+#pragma unroll
+    for (int A = 0; A < 27; A++)
+        if (!((fb >> A) & 1u)) atomicAdd(&y[q2node3(g, ex, A) * 3 + I], out[A]);
+}
+
 // y += K x over free dofs, one element per thread (see the file header).
 template <typename T, int BS>
 __global__ void __launch_bounds__(BS) k_applyK_q2_3d(uwg_lgeom g, const T* __restrict__ W,
@@ -144,7 +259,7 @@ __global__ void __launch_bounds__(BS) k_applyK_q2_3d(uwg_lgeom g, const T* __res
     int ex[3];
     double h[3];
     q2e3(g, e, ex, h);
-    const T sxyz[3] = {(T)2 / (T)h[0], (T)2 / (T)h[1], (T)2 / (T)h[2]};
+    const T sc[3] = {(T)2 / (T)h[0], (T)2 / (T)h[1], (T)2 / (T)h[2]};
     uint32_t fixbits[3] = {0u, 0u, 0u};   // bit A of word i: dof (A, i) is Dirichlet
 #pragma unroll 1
     for (int A = 0; A < 27; A++) {
@@ -158,102 +273,9 @@ __global__ void __launch_bounds__(BS) k_applyK_q2_3d(uwg_lgeom g, const T* __res
     }
     const T* Wp = W + e;
     const int64_t st = g.n_el;
-#pragma unroll 1
-    for (int i = 0; i < 3; i++) {
-        T out[27];
-#pragma unroll
-        for (int A = 0; A < 27; A++) out[A] = (T)0;
-#pragma unroll 1
-        for (int r = 0; r < 5; r++) {
-            // z contractions: tz (value along z), sz (z derivative), per component and (a, b)
-            T tz[3][9], sz[3][9];
-#pragma unroll
-            for (int c = 0; c < 3; c++)
-#pragma unroll
-                for (int ab = 0; ab < 9; ab++) {
-                    T tv = 0, sv = 0;
-#pragma unroll
-                    for (int k = 0; k < 3; k++) {
-                        const T u = us[((ab + 9 * k) * 3 + c) * BS + tid];
-                        tv += B5<T>(r, k) * u;
-                        sv += D5<T>(r, k) * u;
-                    }
-                    tz[c][ab] = tv;
-                    sz[c][ab] = sv;
-                }
-            T P1[9], P3[9];
-#pragma unroll
-            for (int k = 0; k < 9; k++) P1[k] = P3[k] = (T)0;
-#pragma unroll 1
-            for (int q = 0; q < 5; q++) {
-                T T1[3][3], T2[3][3], T3[3][3];
-#pragma unroll
-                for (int c = 0; c < 3; c++)
-#pragma unroll
-                    for (int a = 0; a < 3; a++) {
-                        T v1 = 0, v2 = 0, v3 = 0;
-#pragma unroll
-                        for (int b = 0; b < 3; b++) {
-                            v1 += B5<T>(q, b) * tz[c][a + 3 * b];
-                            v2 += D5<T>(q, b) * tz[c][a + 3 * b];
-                            v3 += B5<T>(q, b) * sz[c][a + 3 * b];
-                        }
-                        T1[c][a] = v1;
-                        T2[c][a] = v2;
-                        T3[c][a] = v3;
-                    }
-                T L1[3] = {0, 0, 0}, L2[3] = {0, 0, 0}, L3[3] = {0, 0, 0};
-#pragma unroll
-                for (int p = 0; p < 5; p++) {
-                    T gr[3][3];   // gr[c][j] = d u_c / d x_j
-#pragma unroll
-                    for (int c = 0; c < 3; c++) {
-                        T d0 = 0, d1 = 0, d2 = 0;
-#pragma unroll
-                        for (int a = 0; a < 3; a++) {
-                            d0 += D5<T>(p, a) * T1[c][a];
-                            d1 += B5<T>(p, a) * T2[c][a];
-                            d2 += B5<T>(p, a) * T3[c][a];
-                        }
-                        gr[c][0] = sxyz[0] * d0;
-                        gr[c][1] = sxyz[1] * d1;
-                        gr[c][2] = sxyz[2] * d2;
-                    }
-                    const T w = Wp[(int64_t)(p + 5 * q + 25 * r) * st];
-                    // sigma_ij for the output component i, j = 0..2 (selects keep gr in registers)
-                    const T gi0 = i == 0 ? gr[0][0] : (i == 1 ? gr[1][0] : gr[2][0]);
-                    const T gi1 = i == 0 ? gr[0][1] : (i == 1 ? gr[1][1] : gr[2][1]);
-                    const T gi2 = i == 0 ? gr[0][2] : (i == 1 ? gr[1][2] : gr[2][2]);
-                    const T g0i = i == 0 ? gr[0][0] : (i == 1 ? gr[0][1] : gr[0][2]);
-                    const T g1i = i == 0 ? gr[1][0] : (i == 1 ? gr[1][1] : gr[1][2]);
-                    const T g2i = i == 0 ? gr[2][0] : (i == 1 ? gr[2][1] : gr[2][2]);
-                    const T s0 = w * (gi0 + g0i), s1 = w * (gi1 + g1i), s2 = w * (gi2 + g2i);
-#pragma unroll
-                    for (int a = 0; a < 3; a++) {
-                        L1[a] += D5<T>(p, a) * s0;
-                        L2[a] += B5<T>(p, a) * s1;
-                        L3[a] += B5<T>(p, a) * s2;
-                    }
-                }
-#pragma unroll
-                for (int b = 0; b < 3; b++)
-#pragma unroll
-                    for (int a = 0; a < 3; a++) {
-                        P1[a + 3 * b] += B5<T>(q, b) * (sxyz[0] * L1[a]) + D5<T>(q, b) * (sxyz[1] * L2[a]);
-                        P3[a + 3 * b] += B5<T>(q, b) * (sxyz[2] * L3[a]);
-                    }
-            }
-#pragma unroll
-            for (int c = 0; c < 3; c++)
-#pragma unroll
-                for (int ab = 0; ab < 9; ab++) out[ab + 9 * c] += B5<T>(r, c) * P1[ab] + D5<T>(r, c) * P3[ab];
-        }
-#pragma unroll 1
-        const uint32_t fb = i == 0 ? fixbits[0] : (i == 1 ? fixbits[1] : fixbits[2]);
-#pragma unroll
-        for (int A = 0; A < 27; A++)
-            if (!((fb >> A) & 1u)) atomicAdd(&y[q2node3(g, ex, A) * 3 + i], out[A]);
-    }
+    q2_3d_apply_component<T, BS, 0>(g, us, Wp, st, sc, ex, fixbits[0], y);
+    q2_3d_apply_component<T, BS, 1>(g, us, Wp, st, sc, ex, fixbits[1], y);
+    q2_3d_apply_component<T, BS, 2>(g, us, Wp, st, sc, ex, fixbits[2], y);
 }
 
 // ---------------------------------------------------------------------------
