@@ -17,9 +17,10 @@
 //   (the ILU(0) of a block-diagonal matrix is its exact inverse).
 //
 // The apply keeps one element per thread: the element's velocities are staged
-// in shared memory, and each output component is produced in its own pass over
-// the 125 points (gradients are recomputed per pass so that the accumulators of
-// one component, not three, stay in registers).
+// in shared memory, and each output component I is produced in its own pass over
+// the 125 points, so that the accumulators of one component, not three, stay in
+// registers; a pass evaluates only the five gradient entries its stresses
+// sigma_Ij = w (d_j u_I + d_I u_j) read.
 #include <cmath>
 #include <vector>
 

@@ -7,6 +7,7 @@ node numbering x-fastest, element numbering x-fastest, node coordinates
 ``MeshVariable.data`` is a host numpy array; the library copies it to the
 device when a solve or an advection reads it and writes results back in place.
 """
+import os
 import re
 
 import numpy as np
@@ -14,6 +15,8 @@ import torch
 
 from . import _core
 from . import function as _fn
+from . import h5 as _h5
+from . import utils as _utils
 
 
 class IndexSet:
@@ -103,6 +106,70 @@ class FeMesh_Cartesian:
 
     def add_variable(self, nodeDofCount, dataType="double", **kwargs):
         return MeshVariable(self, nodeDofCount, dataType)
+
+    @property
+    def data_elementNodes(self):
+        """Element-node map [elements, nodes per element]: global node indices,
+        element x-fastest, nodes of an element in lexicographic order."""
+        o, r, dim = self._order, self.elementRes, self.dim
+        n = [ri * o + 1 for ri in r]
+        k = o + 1
+        e = np.arange(self.elementsGlobal)
+        ei = [e % r[0], (e // r[0]) % r[1]] + ([e // (r[0] * r[1])] if dim == 3 else [])
+        loc = np.arange(k ** dim)
+        li = [loc % k, (loc // k) % k] + ([loc // (k * k)] if dim == 3 else [])
+        g = [ei[d][:, None] * o + li[d][None, :] for d in range(dim)]
+        node = g[0] + n[0] * g[1]
+        if dim == 3:
+            node = node + n[0] * n[1] * g[2]
+        return node.astype(np.int32)
+
+    # -- checkpointing (P/mesh/_mesh.py:495-675) -----------------------------
+    def save(self, filename, units=None, **kwargs):
+        """Write the mesh to an HDF5 file: ``vertices`` [nodes, dim], ``en_map``
+        [elements, nodes per element] and the attributes dimensions, mesh
+        resolution, max, min, regular and elementType (plus ``kwargs`` as
+        strings).  Returns a ``SavedFileData``."""
+        if not isinstance(filename, str):
+            raise TypeError("Expected 'filename' to be provided as a string")
+        if units is not None:
+            raise NotImplementedError("saving with units (dimensional scaling) is not supported")
+        attrs = {"dimensions": self.dim, "mesh resolution": self.elementRes, "max": self.maxCoord,
+                 "min": self.minCoord, "regular": True, "elementType": self.elementType}
+        attrs.update({str(k): str(v) for k, v in kwargs.items()})
+        _h5.write(filename, {"vertices": self.data, "en_map": self.data_elementNodes}, attrs)
+        return _utils.SavedFileData(self, filename)
+
+    def load(self, filename):
+        """Read mesh vertices saved by ``save``.  The mesh stays regular: the
+        vertices must form the regular grid of this resolution, whose extent
+        becomes the mesh's ``minCoord``/``maxCoord``."""
+        if not isinstance(filename, str):
+            raise TypeError("Expected 'filename' to be provided as a string")
+        with _h5.File(filename) as f:
+            v = f["vertices"]
+        if v.shape[1] != self.dim:
+            raise RuntimeError("Can't load hdf5 '%s', incompatible data shape" % filename)
+        if v.shape[0] != self.nodesGlobal:
+            raise RuntimeError("Provided data file appears to be for a different resolution mesh.")
+        (ii, nn) = self._node_grid()
+        axes = []
+        for d in range(self.dim):
+            ax = np.zeros(nn[d])
+            ax[ii[d]] = v[:, d]
+            if not np.array_equal(ax[ii[d]], v[:, d]) or np.any(np.diff(ax) <= 0):
+                raise NotImplementedError("the saved mesh is deformed; only regular meshes are supported")
+            axes.append(ax)
+        lo = tuple(float(a[0]) for a in axes)
+        hi = tuple(float(a[-1]) for a in axes)
+        mesh = FeMesh_Cartesian("Q%d/%s" % (self._order, "dQ0" if self._porder == 0 else "dPc1"),
+                                self.elementRes, lo, hi)
+        if any(not np.allclose(mesh._axes[d], axes[d], rtol=0, atol=1e-12 * (1 + abs(hi[d] - lo[d])))
+               for d in range(self.dim)):
+            raise NotImplementedError("the saved mesh is deformed; only regular meshes are supported")
+        self.minCoord, self.maxCoord = lo, hi
+        self._axes = mesh._axes
+        self._ctx = None
 
     def _node_grid(self):
         n = [r * self._order + 1 for r in self.elementRes]
@@ -243,6 +310,91 @@ class MeshVariable:
             M = torch.stack([-4.0 * x - 20.0 * y + 12.0 * z + 3.0, 16.0 * x - 64.0 * y + 60.0 * z + 6.0,
                              36.0 * y - 36.0 * z, -12.0 * x + 48.0 * y - 36.0 * z], 1) / 9.0
         return (vals.view(-1, npn)[el] * M).sum(1, keepdim=True)
+
+    # -- checkpointing (P/mesh/_meshvariable.py:227-620) ----------------------
+    def save(self, filename, meshHandle=None, units=None, **kwargs):
+        """Write ``data`` to an HDF5 file (dataset ``data`` [nodes, components];
+        attributes units, elementType, ``kwargs`` as strings, and ``mesh``, the
+        path of the linked mesh file when ``meshHandle`` is given).  Returns a
+        ``SavedFileData``."""
+        if not isinstance(filename, str):
+            raise TypeError("Expected 'filename' to be provided as a string")
+        if units is not None:
+            raise NotImplementedError("saving with units (dimensional scaling) is not supported")
+        attrs = {str(k): str(v) for k, v in kwargs.items()}
+        attrs["units"] = "None"
+        attrs["elementType"] = np.bytes_(self.mesh.elementType.encode())
+        if meshHandle is not None:
+            if not isinstance(meshHandle, (str, _utils.SavedFileData)):
+                raise TypeError("Expected 'meshHandle' to be of type 'uw.utils.SavedFileData'")
+            mfile = meshHandle if isinstance(meshHandle, str) else meshHandle.filename
+            if not os.path.exists(mfile):
+                raise ValueError("You are trying to link against the mesh file '%s' that does not appear to exist."
+                                 % mfile)
+            attrs["mesh"] = os.path.abspath(mfile)
+        _h5.write(filename, {"data": self._data}, attrs)
+        return _utils.SavedFileData(self, filename)
+
+    def load(self, filename, interpolate=False):
+        """Read ``data`` saved by ``save``.  With ``interpolate=True`` a field
+        saved on a different resolution of the same element type is evaluated
+        at this variable's nodes (the mesh file linked at save time gives the
+        source mesh)."""
+        if not isinstance(filename, str):
+            raise TypeError("Expected 'filename' to be provided as a string")
+        with _h5.File(filename) as f:
+            d = f["data"]
+            link = f.attrs.get("mesh")
+        if d.ndim != 2 or d.shape[1] != self.nodeDofCount:
+            raise RuntimeError("Can't load hdf5 '%s', incompatible data shape" % filename)
+        if d.shape[0] == self._data.shape[0]:
+            self._data[...] = d
+            return
+        if not interpolate:
+            raise RuntimeError("Provided data file appears to be for a different resolution MeshVariable.\n"
+                               "Set 'interpolate=True' to interpolate it onto this variable's nodes.")
+        if not isinstance(self.mesh, FeMesh_Cartesian):
+            raise NotImplementedError("interpolated loading is provided for velocity-mesh variables")
+        if link is None:
+            raise RuntimeError("'%s' has no linked mesh file to interpolate from" % filename)
+        link = link.decode() if isinstance(link, bytes) else str(link)
+        with _h5.File(link) as f:
+            a = f.attrs
+            res = tuple(int(r) for r in a["mesh resolution"])
+            lo = tuple(float(x) for x in a["min"])
+            hi = tuple(float(x) for x in a["max"])
+            et = a["elementType"]
+        et = et.decode() if isinstance(et, bytes) else str(et)
+        src = FeMesh_Cartesian("Q1/dQ0" if et.upper() == "Q1" else "Q2/dPc1", res, lo, hi)
+        if src.nodesGlobal != d.shape[0]:
+            raise RuntimeError("the linked mesh file does not match the saved field")
+        var = MeshVariable(src, self.nodeDofCount)
+        var.data[...] = d
+        pts = torch.from_numpy(np.ascontiguousarray(self.mesh.data)).to(src.ctx.device)
+        self._data[...] = var._interpolate(pts).cpu().numpy().reshape(self._data.shape)
+
+    def xdmf(self, filename, fieldSavedData, varname, meshSavedData, meshname, modeltime=0.):
+        """Write an XDMF file describing the saved field on the saved mesh."""
+        if not isinstance(varname, str):
+            raise ValueError("'varname' must be of type str")
+        if not isinstance(meshname, str):
+            raise ValueError("'meshname' must be of type str")
+        if not isinstance(filename, str):
+            raise ValueError("'filename' must be of type str")
+        if not isinstance(meshSavedData, _utils.SavedFileData):
+            raise ValueError("'meshSavedData' must be of type SavedFileData")
+        if not isinstance(fieldSavedData, _utils.SavedFileData):
+            raise ValueError("'fieldSavedData' must be of type SavedFileData")
+        if not isinstance(modeltime, (int, float)):
+            raise ValueError("'modeltime' must be of type int or float")
+        if self._primary() is not meshSavedData.pyobj:
+            raise RuntimeError("'meshSavedData file doesn't correspond to the object's mesh")
+        if not filename.lower().endswith(".xdmf"):
+            filename += ".xdmf"
+        text = (_utils._xdmf_header() + _utils._mesh_grid(meshSavedData, meshname, float(modeltime)) +
+                _utils._field(fieldSavedData, varname) + _utils._xdmf_footer())
+        with open(filename, "w") as fh:
+            fh.write(text)
 
     def __add__(self, o): return self._as_function() + o
     def __radd__(self, o): return o + self._as_function()

@@ -9,12 +9,15 @@ Reference: P/swarm/_swarm.py, P/swarm/_swarmabstract.py, P/swarm/layouts.py,
 P/swarm/_integration_swarm.py, P/swarm/_population_control.py.
 """
 import contextlib
+import os
 
 import numpy as np
 import torch
 
 from . import _core
 from . import function as _fn
+from . import h5 as _h5
+from . import utils as _utils
 
 # Park-Miller stream state shared by every random layout, as in
 # L/StgDomain/Swarm/src/Random.c (one static seed for the process).
@@ -55,6 +58,72 @@ class SwarmVariable:
 
     def _as_function(self):
         return _fn._SwarmVar(self)
+
+    # -- checkpointing (P/swarm/_swarmvariable.py:244-600) --------------------
+    def save(self, filename, collective=False, swarmHandle=None, units=None, **kwargs):
+        """Write ``data`` to an HDF5 file (dataset ``data`` [particles,
+        components]; attributes proc_offset, units, ``kwargs`` as strings, and
+        ``swarm``, the path of the linked swarm file when ``swarmHandle`` is
+        given).  Returns a ``SavedFileData``."""
+        if not isinstance(filename, str):
+            raise TypeError("'filename' parameter must be of type 'str'")
+        if units is not None:
+            raise NotImplementedError("saving with units (dimensional scaling) is not supported")
+        attrs = {"proc_offset": np.array([self.swarm.particleLocalCount], dtype=np.int64), "units": "None"}
+        if swarmHandle is not None:
+            if not isinstance(swarmHandle, (str, _utils.SavedFileData)):
+                raise TypeError("Expected 'swarmHandle' to be of type 'uw.utils.SavedFileData'")
+            sfile = swarmHandle if isinstance(swarmHandle, str) else swarmHandle.filename
+            if not os.path.exists(sfile):
+                raise ValueError("You are trying to link against the swarm file '%s' that does not appear to exist."
+                                 % sfile)
+            attrs["swarm"] = os.path.abspath(sfile)
+        attrs.update({str(k): str(v) for k, v in kwargs.items()})
+        _h5.write(filename, {"data": self._data}, attrs)
+        return _utils.SavedFileData(self, filename)
+
+    def load(self, filename, collective=False):
+        """Read ``data`` saved by ``save`` into the particles of a swarm that was
+        itself loaded from its checkpoint (``Swarm.load``), row by saved index."""
+        if not isinstance(filename, str):
+            raise TypeError("'filename' parameter must be of type 'str'")
+        sw = self.swarm
+        if getattr(sw, "_checkpointMapsToState", None) != sw.stateId:
+            raise RuntimeError("'Swarm' associate with this 'SwarmVariable' does not appear to be in the correct "
+                               "state.\nPlease ensure that you have loaded the swarm prior to loading any swarm "
+                               "variables.")
+        with _h5.File(filename) as f:
+            d = f["data"]
+        if d.shape[1] != self._data.shape[1]:
+            raise RuntimeError("Cannot load file data on current swarm. Data in file '%s' has %d components, the "
+                               "variable has %d" % (filename, d.shape[1], self._data.shape[1]))
+        if d.shape[0] != sw._checkpointCount:
+            raise RuntimeError("It appears that the swarm has %d particles, but provided h5 file has %d data points."
+                               % (sw._checkpointCount, d.shape[0]))
+        first = sw._checkpointFirst
+        self._data[first:first + len(sw._local2globalMap)] = d[sw._local2globalMap]
+        self._dirty = True
+
+    def xdmf(self, filename, varSavedData, varname, swarmSavedData, swarmname, modeltime=0.):
+        """Write an XDMF file describing the saved variable on the saved swarm."""
+        if not isinstance(varname, str):
+            raise ValueError("'varname' must be of type str")
+        if not isinstance(swarmname, str):
+            raise ValueError("'swarmname' must be of type str")
+        if not isinstance(filename, str):
+            raise ValueError("'filename' must be of type str")
+        if not isinstance(swarmSavedData, _utils.SavedFileData):
+            raise ValueError("'swarmSavedData' must be of type SavedFileData")
+        if not isinstance(varSavedData, _utils.SavedFileData):
+            raise ValueError("'varSavedData' must be of type SavedFileData")
+        if not isinstance(modeltime, (int, float)):
+            raise ValueError("'modeltime' must be of type int or float")
+        if not filename.lower().endswith(".xdmf"):
+            filename += ".xdmf"
+        text = (_utils._xdmf_header() + _utils._swarm_grid(swarmSavedData, swarmname, float(modeltime)) +
+                _utils._swarmvar(varSavedData, varname) + _utils._xdmf_footer())
+        with open(filename, "w") as fh:
+            fh.write(text)
 
     def __add__(self, o): return self._as_function() + o
     def __radd__(self, o): return o + self._as_function()
@@ -130,6 +199,41 @@ class Swarm:
         v = SwarmVariable(self, dataType, count)
         self._variables.append(v)
         return v
+
+    # -- checkpointing (P/swarm/_swarm.py:226-420) ----------------------------
+    def save(self, filename, collective=False, units=None, **kwargs):
+        """Write the particle coordinates to an HDF5 file (dataset ``data``
+        [particles, dim]; attributes proc_offset, units and ``kwargs`` as
+        strings).  Returns a ``SavedFileData``."""
+        if not isinstance(filename, str):
+            raise TypeError("Expected 'filename' to be provided as a string")
+        if units is not None:
+            raise NotImplementedError("saving with units (dimensional scaling) is not supported")
+        attrs = {"proc_offset": np.array([self.particleLocalCount], dtype=np.int64), "units": "None"}
+        attrs.update({str(k): str(v) for k, v in kwargs.items()})
+        _h5.write(filename, {"data": self.data}, attrs)
+        return _utils.SavedFileData(self, filename)
+
+    def load(self, filename, collective=False, try_optimise=True):
+        """Add the particles saved in ``filename`` (coordinates outside the mesh
+        are skipped), in file order, and record which saved row each one came
+        from so that swarm variables saved with the swarm can be loaded."""
+        if not isinstance(filename, str):
+            raise TypeError("Expected 'filename' to be provided as a string")
+        with _h5.File(filename) as f:
+            d = f["data"]
+        if d.ndim != 2 or d.shape[1] != self.dim:
+            raise RuntimeError("Cannot load file data on current swarm. Data in file '%s' has %d components, the "
+                               "particle coordinates have %d" % (filename, d.shape[1], self.dim))
+        chunk = 20_000_000
+        self._checkpointFirst = self.particleLocalCount
+        rows = []
+        for start in range(0, d.shape[0], chunk):
+            ret = self.add_particles_with_coordinates(np.ascontiguousarray(d[start:start + chunk]))
+            rows.append(start + np.nonzero(ret >= 0)[0])
+        self._local2globalMap = np.concatenate(rows) if rows else np.zeros(0, dtype=np.int64)
+        self._checkpointCount = d.shape[0]
+        self._checkpointMapsToState = self.stateId
 
     # -- population ------------------------------------------------------------
     def populate_using_layout(self, layout):
