@@ -248,15 +248,35 @@ __device__ __forceinline__ void q2_3d_apply_component(const uwg_lgeom& g, const 
         if (!((fb >> A) & 1u)) atomicAdd(&y[q2node3(g, ex, A) * 3 + I], out[A]);
 }
 
-// y += K x over free dofs, one element per thread (see the file header).
+// Asynchronous copy of one FP32 or FP64 value into shared memory.
+template <int BYTES>
+__device__ __forceinline__ void q2_cp_async(void* smem, const void* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(sa), "l"(gmem), "n"(BYTES));
+}
+
+// Dynamic shared memory of the apply: the element's 81 nodal values and its
+// 125 weights for each of the BS threads (thread-fastest, conflict-free).
+template <typename T, int BS>
+constexpr size_t q2_3d_apply_smem() { return (size_t)(81 + 125) * BS * sizeof(T); }
+
+// y += K x over free dofs, one element per thread (see the file header).  The
+// 125 weights of the thread's element are copied to shared memory with
+// cp.async while the nodal values are gathered, so the point loops read them
+// without waiting on DRAM; every thread reads only what it copied itself.
 template <typename T, int BS>
 __global__ void __launch_bounds__(BS) k_applyK_q2_3d(uwg_lgeom g, const T* __restrict__ W,
                                                      const uint8_t* __restrict__ bc, bool mask_in,
                                                      const T* __restrict__ x, T* y) {
-    __shared__ T us[81 * BS];
+    extern __shared__ __align__(16) unsigned char q2_smem[];
+    T* us = reinterpret_cast<T*>(q2_smem);
+    T* ws = us + 81 * BS;
     const int tid = threadIdx.x;
     const int64_t e = blockIdx.x * (int64_t)BS + tid;
     if (e >= g.n_el) return;
+#pragma unroll 5
+    for (int j = 0; j < 125; j++) q2_cp_async<sizeof(T)>(&ws[j * BS + tid], W + (int64_t)j * g.n_el + e);
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
     int ex[3];
     double h[3];
     q2e3(g, e, ex, h);
@@ -272,11 +292,11 @@ __global__ void __launch_bounds__(BS) k_applyK_q2_3d(uwg_lgeom g, const T* __res
             us[(A * 3 + c) * BS + tid] = (fx && mask_in) ? (T)0 : x[n * 3 + c];
         }
     }
-    const T* Wp = W + e;
-    const int64_t st = g.n_el;
-    q2_3d_apply_component<T, BS, 0>(g, us, Wp, st, sc, ex, fixbits[0], y);
-    q2_3d_apply_component<T, BS, 1>(g, us, Wp, st, sc, ex, fixbits[1], y);
-    q2_3d_apply_component<T, BS, 2>(g, us, Wp, st, sc, ex, fixbits[2], y);
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    const T* Wp = ws + tid;
+    q2_3d_apply_component<T, BS, 0>(g, us, Wp, BS, sc, ex, fixbits[0], y);
+    q2_3d_apply_component<T, BS, 1>(g, us, Wp, BS, sc, ex, fixbits[1], y);
+    q2_3d_apply_component<T, BS, 2>(g, us, Wp, BS, sc, ex, fixbits[2], y);
 }
 
 // ---------------------------------------------------------------------------
@@ -605,6 +625,11 @@ int uwg_q2_3d_init(uwg_ctx* c) {
 int uwg_q2_3d_assemble(uwg_ctx* c, const int32_t* off, const int32_t* list, const double* ip_xi, const double* ip_w,
                        const double* eta_p, const double* body_p) {
     uwg_lgeom g = uwg_level_geom(c, 0);
+    // the applies stage 105 KB per block (set here, before any solve is captured)
+    UWG_CUDA(c, cudaFuncSetAttribute(k_applyK_q2_3d<float, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)q2_3d_apply_smem<float, 128>()));
+    UWG_CUDA(c, cudaFuncSetAttribute(k_applyK_q2_3d<double, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)q2_3d_apply_smem<double, 64>()));
     vk_zero<double>(c->stream, c->n_vdof, c->f);
     k_assemble_q2_3d<<<nblk(c->n_el * 32, 128), 128, 0, c->stream>>>(g, off, list, ip_xi, ip_w, eta_p, body_p,
                                                                     c->lev[0].W64, c->lev[1].W64, c->f);
@@ -639,7 +664,8 @@ int uwg_q2_3d_applyK(uwg_ctx* c, const T* x, T* y, bool mask_in) {
     const T* W;
     if constexpr (sizeof(T) == 8) W = (const T*)L.W64; else W = (const T*)L.W32;
     constexpr int BS = sizeof(T) == 8 ? 64 : 128;
-    k_applyK_q2_3d<T, BS><<<nblk(L.n_el, BS), BS, 0, c->stream>>>(uwg_level_geom(c, 0), W, L.bc, mask_in, x, y);
+    k_applyK_q2_3d<T, BS><<<nblk(L.n_el, BS), BS, q2_3d_apply_smem<T, BS>(), c->stream>>>(uwg_level_geom(c, 0), W,
+                                                                                         L.bc, mask_in, x, y);
     UWG_CUDA(c, cudaGetLastError());
     return UWG_OK;
 }
