@@ -144,6 +144,13 @@ int uwg_assemble(uwg_ctx* ctx, int64_t np, const int32_t* cell_offsets, const in
                  const double* ip_xi, const double* ip_w, const double* eta_p,
                  const double* body_p, const double* lambda_p);
 
+/* Adds df[n_vdof] (device) to the assembled velocity right-hand side at free dofs:
+ * the traction (NeumannCondition) surface term VectorSurfaceAssemblyTerm_NA__Fn__ni
+ * (L/Underworld/Utils/src/VectorSurfaceAssemblyTerm_NA__Fn__ni.cpp:163-236), which the
+ * reference adds to the Stokes force vector (P/systems/_stokes.py:291-297).  Call after
+ * uwg_assemble, which rebuilds the right-hand side. */
+int uwg_add_force(uwg_ctx* ctx, const double* df);
+
 /* Element matrices of one element as assembled (host outputs, for checks):
  * Ke_h[(dim*nen)^2], fe_h[dim*nen], Ge_h[dim*nen*npn], Se_h[npn*npn]. */
 int uwg_element_matrices(uwg_ctx* ctx, int64_t el, double* Ke_h, double* fe_h, double* Ge_h,
@@ -290,10 +297,13 @@ int uwg_cnn_adam(uwg_ctx* ctx, int64_t n, float* w, const float* g, float* m, fl
  *   kappa_q   [n_el*3^dim] diffusivity at the 3-point Gauss points of each element
  *   source_q  same layout, or NULL
  *   bc        [n_nodes] 1 = Dirichlet node, with phi = bcval and phi-dot = bcdot (NULL: 0)
- *   phi, phidot [n_nodes] advanced in place; iterations (2) and gamma (0.5) as the reference */
+ *   phi, phidot [n_nodes] advanced in place; iterations (2) and gamma (0.5) as the reference
+ *   flux      [n_nodes] boundary-flux vector added to every residual (the NeumannCondition
+ *             surface term VectorSurfaceAssemblyTerm_NA__Fn__ni, L/Underworld/Utils/src/
+ *             VectorSurfaceAssemblyTerm_NA__Fn__ni.cpp:163-236), or NULL */
 int uwg_advdiff_step(uwg_ctx* ctx, double dt, const double* vel, const double* kappa_q, const double* source_q,
                      const uint8_t* bc, const double* bcval, const double* bcdot, double* phi, double* phidot,
-                     int iterations, double gamma);
+                     int iterations, double gamma, const double* flux);
 /* Time-step bound of AdvectionDiffusionSLE_CalculateDt (Timestep.c:31-117): courant *
  * min(advective, diffusive); the reference's SUPG system uses courant = 0.5. */
 int uwg_advdiff_max_dt(uwg_ctx* ctx, const double* vel, const double* kappa_q, double courant, double* dt_h);
@@ -311,9 +321,12 @@ int uwg_slcn_phistar(uwg_ctx* ctx, double dt, const double* vel, const double* p
  *   kappa_q, source_q [n_el*5^dim] at the 5-point Gauss points (source_q may be NULL)
  *   bc [n_nodes] 1 = Dirichlet node (its value is phi's current value)
  *   phi in: current field (initial guess), out: solution; CG to rtol (relative
- *   residual), its_out / res_out report the iterations and final residual. */
+ *   residual), its_out / res_out report the iterations and final residual.
+ *   flux [n_nodes] boundary-flux vector (dt times the NeumannCondition surface term,
+ *   P/systems/_advectiondiffusion.py:237-248) added to the right-hand side, or NULL. */
 int uwg_slcn_solve(uwg_ctx* ctx, double dt, const double* kappa_q, const double* source_q, const uint8_t* bc,
-                   const double* phistar, double* phi, double rtol, int max_its, int* its_out, double* res_out);
+                   const double* phistar, double* phi, double rtol, int max_its, int* its_out, double* res_out,
+                   const double* flux);
 
 #ifdef __cplusplus
 }

@@ -146,6 +146,10 @@ class Context:
         self._call("uwg_assemble", lst.shape[0], _ptr(off), _ptr(lst), _ptr(ip_xi), _ptr(ip_w), _ptr(eta),
                    _ptr(body), _ptr(one_on_lambda))
 
+    def add_force(self, df):
+        """f += df at free dofs (traction surface term; after assemble)."""
+        self._call("uwg_add_force", _ptr(df.contiguous()))
+
     def element_matrices(self, el):
         nd = self.dim * self.nen
         Ke = np.zeros((nd, nd))
@@ -227,10 +231,10 @@ class Context:
         return torch.from_numpy(out.reshape(-1, self.dim)).to(self.device)
 
     def advdiff_step(self, dt, vel, kappa_q, phi, phidot, bc, bcval, bcdot=None, source_q=None, iterations=2,
-                     gamma=0.5):
+                     gamma=0.5, flux=None):
         bc = bc.to(self.device, torch.uint8).contiguous()
         self._call("uwg_advdiff_step", float(dt), _ptr(vel), _ptr(kappa_q), _ptr(source_q), _ptr(bc), _ptr(bcval),
-                   _ptr(bcdot), _ptr(phi), _ptr(phidot), int(iterations), float(gamma))
+                   _ptr(bcdot), _ptr(phi), _ptr(phidot), int(iterations), float(gamma), _ptr(flux))
 
     def advdiff_max_dt(self, vel, kappa_q, courant=0.5):
         dt = ctypes.c_double(0.0)
@@ -243,11 +247,11 @@ class Context:
         self._call("uwg_slcn_phistar", float(dt), _ptr(vel), _ptr(phi), _ptr(out))
         return out
 
-    def slcn_solve(self, dt, kappa_q, bc, phistar, phi, source_q=None, rtol=1e-10, max_its=5000):
+    def slcn_solve(self, dt, kappa_q, bc, phistar, phi, source_q=None, rtol=1e-10, max_its=5000, flux=None):
         bc = bc.to(self.device, torch.uint8).contiguous()
         its, res = ctypes.c_int(0), ctypes.c_double(0.0)
         self._call("uwg_slcn_solve", float(dt), _ptr(kappa_q), _ptr(source_q), _ptr(bc), _ptr(phistar), _ptr(phi),
-                   float(rtol), int(max_its), ctypes.byref(its), ctypes.byref(res))
+                   float(rtol), int(max_its), ctypes.byref(its), ctypes.byref(res), _ptr(flux))
         return its.value, res.value
 
 

@@ -77,6 +77,7 @@ SIGNATURES = {
     "uwg_set_bcs": (_I, [_CTX, _P, _P]),
     "uwg_assemble": (_I, [_CTX, _I64, _P, _P, _P, _P, _P, _P, _P]),
     "uwg_element_matrices": (_I, [_CTX, _I64, _P, _P, _P, _P]),
+    "uwg_add_force": (_I, [_CTX, _P]),
     "uwg_solve_opts_default": (None, [ctypes.POINTER(SolveOpts)]),
     "uwg_stokes_solve": (_I, [_CTX, ctypes.POINTER(SolveOpts), _P, _P, ctypes.POINTER(SolveStats)]),
     "uwg_stokes_residuals": (_I, [_CTX, _P, _P, _P]),
@@ -87,7 +88,7 @@ SIGNATURES = {
     "uwg_rk2_advect": (_I, [_CTX, _I64, _D, _P, _P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
     "uwg_interpolate": (_I, [_CTX, _I64, _P, _P, _P]),
     "uwg_max_dt": (_I, [_CTX, _P, ctypes.POINTER(_D)]),
-    "uwg_advdiff_step": (_I, [_CTX, _D, _P, _P, _P, _P, _P, _P, _P, _P, _I, _D]),
+    "uwg_advdiff_step": (_I, [_CTX, _D, _P, _P, _P, _P, _P, _P, _P, _P, _I, _D, _P]),
     "uwg_advdiff_max_dt": (_I, [_CTX, _P, _P, _D, ctypes.POINTER(_D)]),
     "uwg_slcn_phistar": (_I, [_CTX, _D, _P, _P, _P]),
     "uwg_interpolate_field": (_I, [_CTX, ctypes.c_int64, _P, _P, _I, _P, _P]),
@@ -103,7 +104,7 @@ SIGNATURES = {
     "uwg_cnn_mse": (_I, [_CTX, _I64, _I, _I, _P, _P, _P, _P]),
     "uwg_cnn_adam": (_I, [_CTX, _I64, _P, _P, _P, _P, _P, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                           ctypes.c_float, _I]),
-    "uwg_slcn_solve": (_I, [_CTX, _D, _P, _P, _P, _P, _P, _D, _I, ctypes.POINTER(_I), ctypes.POINTER(_D)]),
+    "uwg_slcn_solve": (_I, [_CTX, _D, _P, _P, _P, _P, _P, _D, _I, ctypes.POINTER(_I), ctypes.POINTER(_D), _P]),
 }
 
 

@@ -1,4 +1,4 @@
-"""Dirichlet conditions (``uw.conditions`` subset, P/conditions/_conditions.py:63)."""
+"""Dirichlet and Neumann conditions (``uw.conditions`` subset, P/conditions/_conditions.py:63-170)."""
 import numpy as np
 
 
@@ -31,5 +31,29 @@ class DirichletCondition(SystemCondition):
 
 
 class NeumannCondition(SystemCondition):
-    def __init__(self, *args, **kwargs):
-        raise NotImplementedError("Neumann conditions are not part of the GPU PIC Stokes path")
+    """A flux (traction, for a velocity field) ``fn_flux`` on the nodes given
+    per dof of ``variable`` (P/conditions/_conditions.py:109-170).  The systems
+    add its surface integral to their right-hand side: Gauss points on the
+    element faces whose nodes all lie in the sets, weight times surface
+    Jacobian times flux times the shape function of each flagged dof."""
+
+    def __init__(self, variable, indexSetsPerDof=None, fn_flux=None):
+        from . import function as _fn
+        from .mesh import MeshVariable
+        if not isinstance(variable, MeshVariable):
+            raise TypeError("Provided 'variable' must be of 'MeshVariable' class.")
+        self.variable = variable
+        if indexSetsPerDof is None:
+            raise ValueError("'indexSetsPerDof' must be provided")
+        if not isinstance(indexSetsPerDof, (list, tuple)):
+            indexSetsPerDof = (indexSetsPerDof,)
+        if len(indexSetsPerDof) != variable.nodeDofCount:
+            raise ValueError("indexSetsPerDof needs one entry (or None) per dof of the variable")
+        self.indexSetsPerDof = tuple(indexSetsPerDof)
+        f = _fn.Function.convert(fn_flux)
+        if not isinstance(f, _fn.Function):
+            raise ValueError("Provided 'fn_flux' must be of or convertible to 'Function' class.")
+        self.fn_flux = f
+
+    def mask(self):
+        return DirichletCondition.mask(self)

@@ -256,6 +256,19 @@ extern "C" int uwg_assemble(uwg_ctx* c, int64_t np, const int32_t* off, const in
     return UWG_OK;
 }
 
+__global__ void k_add_free(int64_t n, const uint8_t* bc, const double* df, double* f) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n && !bc[i]) f[i] += df[i];
+}
+
+extern "C" int uwg_add_force(uwg_ctx* c, const double* df) {
+    if (!c || !df) return uwg_set_error(c, UWG_ERR_ARG, "uwg_add_force: bad argument");
+    if (!c->assembled) return uwg_set_error(c, UWG_ERR_STATE, "uwg_add_force before uwg_assemble");
+    k_add_free<<<(unsigned)((c->n_vdof + 255) / 256), 256, 0, c->stream>>>(c->n_vdof, c->bc, df, c->f);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
 extern "C" int uwg_element_matrices(uwg_ctx* c, int64_t el, double* Ke, double* fe, double* Ge, double* Se) {
     if (!c || el < 0 || el >= c->n_el) return uwg_set_error(c, UWG_ERR_ARG, "uwg_element_matrices: bad element");
     if (!c->assembled) return uwg_set_error(c, UWG_ERR_STATE, "element matrices before uwg_assemble");

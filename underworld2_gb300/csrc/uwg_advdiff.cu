@@ -245,11 +245,12 @@ __global__ void k_supg_predict(int64_t n, const uint8_t* bc, const double* bcval
     phidot[i] = 0.0;
 }
 
-__global__ void k_supg_correct(int64_t n, const uint8_t* bc, const double* R, const double* M, double f, double* phi,
-                               double* phidot) {
+// flux: the boundary-flux vector added to the residual, or NULL
+__global__ void k_supg_correct(int64_t n, const uint8_t* bc, const double* R, const double* flux, const double* M,
+                               double f, double* phi, double* phidot) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n || bc[i]) return;
-    const double d = R[i] / M[i];
+    const double d = (flux ? R[i] + flux[i] : R[i]) / M[i];
     phi[i] += f * d;
     phidot[i] += d;
 }
@@ -311,7 +312,7 @@ extern "C" int uwg_advdiff_max_dt(uwg_ctx* c, const double* vel, const double* k
 //   bc       [n_nodes] 1 = Dirichlet node; bcval, bcdot its phi and phi-dot values
 extern "C" int uwg_advdiff_step(uwg_ctx* c, double dt, const double* vel, const double* kappa_q,
                                 const double* source_q, const uint8_t* bc, const double* bcval, const double* bcdot,
-                                double* phi, double* phidot, int iterations, double gamma) {
+                                double* phi, double* phidot, int iterations, double gamma, const double* flux) {
     if (!c || !kappa_q || !bc || !bcval || !phi || !phidot || iterations < 0 || !(dt >= 0.0))
         return uwg_set_error(c, UWG_ERR_ARG, "uwg_advdiff_step: bad argument");
     if (c->order != 1) return uwg_set_error(c, UWG_ERR_ARG, "advection-diffusion is provided on Q1 meshes");
@@ -331,7 +332,7 @@ extern "C" int uwg_advdiff_step(uwg_ctx* c, double dt, const double* vel, const 
         else
             k_supg_residual<2><<<nblk(c->n_el, 128), 128, 0, c->stream>>>(g, vel, phi, phidot, kappa_q, source_q, bc,
                                                                           vel ? 0 : 1, R, it == 0 ? M : nullptr);
-        k_supg_correct<<<nblk(n), 256, 0, c->stream>>>(n, bc, R, M, dt * gamma, phi, phidot);
+        k_supg_correct<<<nblk(n), 256, 0, c->stream>>>(n, bc, R, flux, M, dt * gamma, phi, phidot);
         err = cudaGetLastError();
     }
     cudaFreeAsync(R, c->stream);

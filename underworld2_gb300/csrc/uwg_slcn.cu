@@ -298,9 +298,14 @@ int dots(uwg_ctx* c, int k, const double* const* a, const double* const* b, doub
 //   bc                 [n_nodes] 1 = Dirichlet node; its value is phi's current value
 //   phistar            [n_nodes] departure values
 //   phi                [n_nodes] in: current field (initial guess), out: solution
+__global__ void k_slcn_add_flux(int64_t n, const uint8_t* bc, const double* flux, double* f) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n && !bc[i]) f[i] += flux[i];
+}
+
 extern "C" int uwg_slcn_solve(uwg_ctx* c, double dt, const double* kappa_q, const double* source_q,
                               const uint8_t* bc, const double* phistar, double* phi, double rtol, int max_its,
-                              int* its_out, double* res_out) {
+                              int* its_out, double* res_out, const double* flux) {
     if (!c || !kappa_q || !bc || !phistar || !phi || !(dt >= 0.0) || !(rtol > 0.0) || max_its < 0)
         return uwg_set_error(c, UWG_ERR_ARG, "uwg_slcn_solve: bad argument");
     if (c->order != 1) return uwg_set_error(c, UWG_ERR_ARG, "SLCN diffusion is provided on Q1 meshes");
@@ -328,6 +333,10 @@ extern "C" int uwg_slcn_solve(uwg_ctx* c, double dt, const double* kappa_q, cons
         k_slcn_element<2><<<nblk(c->n_el, 128), 128, 0, c->stream>>>(g, 0.5 * dt, dt, kappa_q, source_q, phistar, phi,
                                                                       bc, Kp, f, diag);
     UWG_CUDA(c, cudaGetLastError());
+    if (flux) {
+        k_slcn_add_flux<<<nblk(n), 256, 0, c->stream>>>(n, bc, flux, f);
+        UWG_CUDA(c, cudaGetLastError());
+    }
     // r = f - K x0, z = D^-1 r, p = z
     if ((rc = slcn_apply(c, g, Kp, bc, phi, q))) return rc;
     vk_copy<double>(c->stream, n, f, r);

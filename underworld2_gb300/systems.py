@@ -50,7 +50,7 @@ class Stokes:
             if not isinstance(c, _cond.SystemCondition):
                 raise TypeError("Provided 'conditions' must be 'SystemCondition' objects.")
             if c.variable is not velocityField:
-                raise ValueError("Only Dirichlet conditions on the velocity field are supported.")
+                raise ValueError("Only conditions on the velocity field are supported.")
         self._conditions = list(conditions)
         if self._swarm is not None:
             self._swarm._voronoi_swarm.repopulate()
@@ -81,7 +81,8 @@ class Stokes:
     def _bc(self):
         m = np.zeros(self._velocityField.data.shape, np.uint8)
         for c in self._conditions:
-            m |= c.mask()
+            if isinstance(c, _cond.DirichletCondition):
+                m |= c.mask()
         return m
 
     def _integration_points(self):
@@ -146,6 +147,10 @@ class Stokes:
         vals = self._velocityField.data * (mask != 0)
         ctx.set_bcs(torch.from_numpy(mask.ravel()), torch.from_numpy(np.ascontiguousarray(vals).ravel()))
         ctx.assemble(off, lst, ip_xi, ip_w, eta, body, lam)
+        # tractions: the surface term on 3 Gauss points per face axis (P/systems/_stokes.py:291-297)
+        for c in self._conditions:
+            if isinstance(c, _cond.NeumannCondition):
+                ctx.add_force(_surface_flux(c, 3, ctx.device))
 
     @property
     def eqResiduals(self):
@@ -400,9 +405,109 @@ def _check_conditions(conditions, phiField):
     for c in conditions:
         if not isinstance(c, _cond.SystemCondition):
             raise TypeError("Provided 'conditions' must be a list 'SystemCondition' objects.")
-        if not isinstance(c, _cond.DirichletCondition):
+        if not isinstance(c, (_cond.DirichletCondition, _cond.NeumannCondition)):
             raise RuntimeError("Input condition type not recognised.")
+        if isinstance(c, _cond.NeumannCondition) and c.variable is not phiField:
+            raise ValueError("Neumann conditions must be given on the 'phiField'")
     return list(conditions)
+
+
+def _neumann_flux(conditions, n_gauss, device, scale=1.0):
+    """Sum of the surface terms of the Neumann conditions, or None."""
+    out = None
+    for c in conditions:
+        if isinstance(c, _cond.NeumannCondition):
+            v = _surface_flux(c, n_gauss, device)
+            out = v if out is None else out + v
+    return None if out is None else (out * scale).contiguous()
+
+
+# Faces of an element in the reference's border-layout numbering
+# (GaussBorderParticleLayout.c:300-320): faces 0, 1 lie at y = -1, +1, faces 2, 3
+# at x = -1, +1, faces 4, 5 at z = -1, +1 (even faces at -1, odd at +1).
+_FACE_AXIS = (1, 1, 0, 0, 2, 2)
+
+
+def _surface_geometry(cond, n_gauss, device):
+    """Points and weights of a NeumannCondition's surface integral, cached on
+    the condition: the Gauss points of every face of every element that holds a
+    condition node (GaussBorderParticleLayout.c:186-290), kept where the
+    interpolated node indicator exceeds 0.999 (the mask of
+    P/systems/sle/_assemblyterm.py:124-144), with weight x surface Jacobian
+    (ElementType.c:566-606: product of h_j / 2 over the face's axes)."""
+    key = (n_gauss, str(device))
+    cache = cond.__dict__.setdefault("_surface_cache", {})
+    if key in cache:
+        return cache[key]
+    var = cond.variable
+    mesh = var.mesh
+    if not isinstance(mesh, _mesh.FeMesh_Cartesian):
+        raise NotImplementedError("Neumann conditions are provided for velocity-mesh variables")
+    dim, o, ndof = mesh.dim, mesh._order, var.nodeDofCount
+    cm = cond.mask().astype(bool)
+    node_on = cm.any(1)
+    en = mesh.data_elementNodes.astype(np.int64)
+    flagged = np.nonzero(node_on[en].any(1))[0]
+    x1, w1 = np.polynomial.legendre.leggauss(n_gauss)
+    pts, wts, fax = [], [], []
+    for f in range(2 * dim):
+        k = _FACE_AXIS[f]
+        others = [a for a in range(dim) if a != k]
+        for idx in np.ndindex(*([n_gauss] * (dim - 1))):
+            xi = np.zeros(dim)
+            xi[k] = -1.0 if f % 2 == 0 else 1.0
+            w = 1.0
+            for a, i in zip(others, idx):
+                xi[a] = x1[i]
+                w *= w1[i]
+            pts.append(xi)
+            wts.append(w)
+            fax.append(k)
+    pts, wts, fax = np.array(pts), np.array(wts), np.array(fax)
+    kk = o + 1
+    loc = np.arange(kk ** dim)
+    li = [loc % kk, (loc // kk) % kk] + ([loc // (kk * kk)] if dim == 3 else [])
+    N = np.ones((len(pts), kk ** dim))
+    for d in range(dim):
+        s_ = pts[:, d]
+        b = np.stack([(1 - s_) / 2, (1 + s_) / 2], 1) if o == 1 else \
+            np.stack([0.5 * s_ * (s_ - 1), 1 - s_ * s_, 0.5 * s_ * (s_ + 1)], 1)
+        N *= b[:, li[d]]
+    r = mesh.elementRes
+    ei = [flagged % r[0], (flagged // r[0]) % r[1]] + ([flagged // (r[0] * r[1])] if dim == 3 else [])
+    det = np.ones((len(flagged), len(pts)))
+    for d in range(dim):
+        h = mesh._axes[d][(ei[d] + 1) * o] - mesh._axes[d][ei[d] * o]
+        det *= np.where(fax[None, :] == d, 1.0, (h / 2.0)[:, None])
+    enf = en[flagged]
+    delta = node_on.astype(np.float64)[enf] @ N.T
+    fe, pe = np.nonzero(delta > 0.999)
+    X = mesh.data
+    xg = np.einsum("qa,qad->qd", N[pe], X[enf[fe]])
+    to = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(device)
+    geo = (to(xg), to(wts[pe] * det[fe, pe]), to(N[pe]), to(enf[fe]), to(cm), ndof, mesh.nodesGlobal)
+    cache[key] = geo
+    return geo
+
+
+def _surface_flux(cond, n_gauss, device):
+    """The NeumannCondition surface term VectorSurfaceAssemblyTerm_NA__Fn__ni
+    (L/Underworld/Utils/src/VectorSurfaceAssemblyTerm_NA__Fn__ni.cpp:163-236):
+    f[(A, d)] += weight |J_s| flux_d(x) N_A(x) over the condition's surface
+    points, for the dofs (A, d) in the condition; [n_nodes * ndof] on device."""
+    xg, fac, N, nodes, cm, ndof, n_nodes = _surface_geometry(cond, n_gauss, device)
+    out = torch.zeros(n_nodes * ndof, dtype=torch.float64, device=device)
+    if xg.shape[0] == 0:
+        return out
+    ectx = _fn.EvalContext(torch.full((xg.shape[0],), -1, dtype=torch.int64, device=device), lambda: xg, device)
+    q = cond.fn_flux.evaluate_at(ectx).to(torch.float64)
+    if q.shape[1] != ndof:
+        raise ValueError("'fn_flux' returns %d components, the variable has %d" % (q.shape[1], ndof))
+    for d in range(ndof):
+        c = (fac * q[:, d])[:, None] * N
+        c = torch.where(cm[nodes, d], c, torch.zeros_like(c))
+        out.index_add_(0, (nodes * ndof + d).reshape(-1), c.reshape(-1))
+    return out
 
 
 class AdvectionDiffusion:
@@ -484,7 +589,10 @@ class _SUPG_AdvectionDiffusion:
         bcval = phi.clone()
         bcdot = phidot.clone()
         vel = self.velocityField._to_device()
-        ctx.advdiff_step(dt, vel, kappa, phi, phidot, torch.from_numpy(mask), bcval, bcdot, source_q=src)
+        # flux conditions: the surface term on 2 Gauss points per face axis, added to the
+        # residual (P/systems/_advectiondiffusion.py:978-991)
+        flux = _neumann_flux(self._conditions, 2, ctx.device)
+        ctx.advdiff_step(dt, vel, kappa, phi, phidot, torch.from_numpy(mask), bcval, bcdot, source_q=src, flux=flux)
         self.phiField._from_device()
         self._phidot._from_device()
 
@@ -534,7 +642,10 @@ class _SLCN_AdvectionDiffusion:
                 kappa = _gauss_eval(self.mesh, self.fn_diffusivity, 5)
                 src = _gauss_eval(self.mesh, self.fn_sourceTerm, 5) if self.fn_sourceTerm is not None else None
                 mask = torch.from_numpy(_dirichlet_mask(self._conditions, self.phiField))
-                its, res = ctx.slcn_solve(dts, kappa, mask, ps, phi, source_q=src, rtol=rtol)
+                # flux conditions: dt times the surface term on 2 Gauss points per face axis
+                # (P/systems/_advectiondiffusion.py:237-248)
+                flux = _neumann_flux(self._conditions, 2, ctx.device, scale=dts)
+                its, res = ctx.slcn_solve(dts, kappa, mask, ps, phi, source_q=src, rtol=rtol, flux=flux)
                 self.last_solve = {"iterations": its, "residual": res}
                 self.phiField._from_device()
 
