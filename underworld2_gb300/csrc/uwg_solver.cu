@@ -294,9 +294,11 @@ int velocity_solve(uwg_ctx* c, const SolveCfg& cfg, const double* b, double* x, 
     if (x_zero) vk_zero<double>(s, n, x);
     if (bn == 0.0) return UWG_OK;
     for (int step = 0; step < 30; step++) {
-        if ((rc = uwg_ops_applyK<double>(c, 0, x, w->ref_d))) return rc;
         vk_copy<double>(s, n, b, w->ref_r);
-        vk_axpy<double>(s, n, -1.0, w->ref_d, w->ref_r);
+        if (step > 0 || !x_zero) {   // from a zero start the first residual is b itself
+            if ((rc = uwg_ops_applyK<double>(c, 0, x, w->ref_d))) return rc;
+            vk_axpy<double>(s, n, -1.0, w->ref_d, w->ref_r);
+        }
         double rn;
         const double* ar[1] = {w->ref_r};
         if ((rc = dots<double>(c, n, 1, ar, ar, &rn))) return rc;
