@@ -29,6 +29,7 @@ workload, extrapolated to the full size and labelled as such.
 """
 import argparse
 import json
+import re
 import os
 import subprocess
 import sys
@@ -702,11 +703,14 @@ def count_launches(ctx, x0, owner0, off0, lst0, eta0, body0, mixed, opts, u, p):
         ctx.rk2(x, u, dt)
         ctx.update_owners(x, owner, off, lst)
         torch.cuda.synchronize()
+    # libuwg's kernels are named k_* / vk_*, some inside an anonymous namespace
+    # ("void (anonymous namespace)::k_applyK_q2_3d<...>(...)")
+    ours = re.compile(r"(^|[\s:])v?k_\w")
     n = 0
     for evt in prof.events():
         name = evt.name or ""
-        if evt.device_type.name == "CUDA" and (name.startswith("k_") or name.startswith("vk_") or "uwg" in name
-                                                or name.startswith("void k_") or name.startswith("void vk_")):
+        if evt.device_type.name == "CUDA" and (ours.search(name.split("(")[0] if "::" not in name else name)
+                                                or "uwg" in name):
             n += 1
     return n
 
