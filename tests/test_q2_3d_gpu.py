@@ -85,6 +85,10 @@ def test_q2_3d_element_matrices_and_operators(gpu):
     assert np.abs(y[free] - yo[free]).max() <= 1e-12 * np.abs(yo).max()
     y32 = c.apply_K(torch.tensor(xv, device="cuda", dtype=torch.float32)).cpu().numpy()
     assert np.abs(y32[free] - yo[free]).max() <= 1e-5 * np.abs(yo).max()
+    # refinement residuals: double-float element matrices, about 2^-48 relative
+    yr = c.apply_K_refine(torch.tensor(xv, device="cuda")).cpu().numpy()
+    assert np.abs(yr[free] - yo[free]).max() <= 1e-12 * np.abs(yo).max()
+    np.testing.assert_array_equal(yr[~free], xv[~free])
     pv = rng.standard_normal(m.n_el * 4)
     yg = c.apply_G(torch.tensor(pv, device="cuda")).cpu().numpy()
     assert np.abs(yg[free] - (sysd["G"] @ pv)[free]).max() <= 1e-12 * np.abs(yg).max()

@@ -181,6 +181,12 @@ class Context:
         self._call("uwg_apply_K64" if x.dtype == torch.float64 else "uwg_apply_K32", int(level), _ptr(x), _ptr(y))
         return y
 
+    def apply_K_refine(self, x):
+        """The refinement-residual operator (FP64 input and output)."""
+        y = torch.empty_like(x)
+        self._call("uwg_apply_K_refine", _ptr(x), _ptr(y))
+        return y
+
     def apply_G(self, p):
         y = self.zeros(self.n_vdof)
         self._call("uwg_apply_G", _ptr(p), _ptr(y))

@@ -82,6 +82,7 @@ SIGNATURES = {
     "uwg_stokes_solve": (_I, [_CTX, ctypes.POINTER(SolveOpts), _P, _P, ctypes.POINTER(SolveStats)]),
     "uwg_stokes_residuals": (_I, [_CTX, _P, _P, _P]),
     "uwg_apply_K64": (_I, [_CTX, _I, _P, _P]),
+    "uwg_apply_K_refine": (_I, [_CTX, _P, _P]),
     "uwg_apply_K32": (_I, [_CTX, _I, _P, _P]),
     "uwg_apply_G": (_I, [_CTX, _P, _P]),
     "uwg_apply_Gt": (_I, [_CTX, _P, _P]),

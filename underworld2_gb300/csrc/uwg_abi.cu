@@ -37,6 +37,7 @@ extern "C" void uwg_ctx_destroy(uwg_ctx* c) {
     if (c->slcn_ws) cudaFree(c->slcn_ws);
     uwg_pop_free(c);
     if (c->q2_ke) cudaFree(c->q2_ke);
+    if (c->q2_ke_df) cudaFree(c->q2_ke_df);
     if (c->red_host) cudaFreeHost(c->red_host);
     uwg_solver_free(c);
     delete c;
@@ -279,6 +280,14 @@ extern "C" int uwg_apply_K64(uwg_ctx* c, int level, const double* x, double* y) 
     if (!c || !x || !y || level < 0 || level >= c->nlev) return uwg_set_error(c, UWG_ERR_ARG, "uwg_apply_K64: bad argument");
     if (!c->assembled) return uwg_set_error(c, UWG_ERR_STATE, "apply before uwg_assemble");
     return uwg_ops_applyK<double>(c, level, x, y);
+}
+
+// The operator of the mixed solve's refinement residuals (double-float on 3D Q2
+// meshes with stored element matrices, else the FP64 apply).
+extern "C" int uwg_apply_K_refine(uwg_ctx* c, const double* x, double* y) {
+    if (!c || !x || !y) return uwg_set_error(c, UWG_ERR_ARG, "uwg_apply_K_refine: bad argument");
+    if (!c->assembled) return uwg_set_error(c, UWG_ERR_STATE, "apply before uwg_assemble");
+    return uwg_ops_applyK_refine(c, x, y);
 }
 
 extern "C" int uwg_apply_K32(uwg_ctx* c, int level, const float* x, float* y) {

@@ -66,6 +66,7 @@ struct uwg_ctx {
     double* slcn_ws;        // SLCN element matrices and CG vectors (grown on demand)
     void* pop;              // pending population plan (uwg_population.cu)
     double* q2_ke;          // 3D Q2: packed FP64 element matrices [n_el][3321] for the FP64 apply
+    float2* q2_ke_df;       // the same as double-float pairs (hi, lo), for the refinement residuals
     size_t slcn_ws_bytes;
 };
 

@@ -535,6 +535,15 @@ int uwg_ops_applyK_lift(uwg_ctx* c, const double* x, double* y) {
     UWG_CUDA(c, cudaGetLastError());
     return UWG_OK;
 }
+int uwg_ops_applyK_refine(uwg_ctx* c, const double* x, double* y) {
+    const uwg_level& L = c->lev[0];
+    if (L.order == 2 && c->dim == 3 && c->q2_ke_df) {
+        k_bc_copy<double><<<nblk(L.n_dof), 256, 0, c->stream>>>(L.n_dof, L.bc, x, y);
+        return uwg_q2_3d_applyK_df(c, x, y);
+    }
+    return uwg_ops_applyK<double>(c, 0, x, y);
+}
+
 template int uwg_ops_applyK<double>(uwg_ctx*, int, const double*, double*);
 template int uwg_ops_applyK<float>(uwg_ctx*, int, const float*, float*);
 

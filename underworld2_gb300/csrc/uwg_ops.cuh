@@ -63,6 +63,10 @@ int uwg_q2_3d_init(uwg_ctx* c);
 int uwg_q2_3d_assemble(uwg_ctx* c, const int32_t* off, const int32_t* list, const double* ip_xi, const double* ip_w,
                        const double* eta_p, const double* body_p);
 template <typename T> int uwg_q2_3d_applyK(uwg_ctx* c, const T* x, T* y, bool mask_in);
+int uwg_q2_3d_applyK_df(uwg_ctx* c, const double* x, double* y);
+// The velocity operator for refinement residuals: double-float on 3D Q2 meshes
+// with stored element matrices, else the FP64 apply.
+int uwg_ops_applyK_refine(uwg_ctx* c, const double* x, double* y);
 int uwg_q2_3d_diag(uwg_ctx* c, double* sinv);
 int uwg_q2_3d_applyG(uwg_ctx* c, const double* p, double* y);
 int uwg_q2_3d_applyGt(uwg_ctx* c, const double* u, double* q, int only_bc);

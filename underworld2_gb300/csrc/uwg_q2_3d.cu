@@ -415,6 +415,64 @@ __global__ void __launch_bounds__(128) k_applyK_q2_3d_em(uwg_lgeom g, const doub
     }
 }
 
+// ---------------------------------------------------------------------------
+// Refinement residuals in double-float arithmetic.  The mixed solve's FP64
+// refinement needs K x to a relative accuracy far below its 1e-8 target, not
+// to the last FP64 bit, and GB300 runs FP64 at 1/64 of the FP32 rate.  Each
+// element-matrix entry is stored as a pair of floats (hi, lo) with
+// hi + lo = K to about 2^-48, each x value is split the same way, and a row is
+// accumulated with the error-free transformations of Dekker (TwoProd, with
+// FMA) and Knuth (TwoSum) on the FP32 pipes.  The plain FP64 solve, the
+// right-hand side lifting and the reported residuals use the FP64 apply.
+// ---------------------------------------------------------------------------
+__global__ void k_split_df(int64_t n, const double* __restrict__ in, float2* __restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double v = in[i];
+        const float hi = (float)v;
+        out[i] = make_float2(hi, (float)(v - (double)hi));
+    }
+}
+
+// y += K x over free dofs from the double-float element matrices: one warp per
+// element, lane owns rows (the layout of k_applyK_q2_3d_em)
+__global__ void __launch_bounds__(128) k_applyK_q2_3d_df(uwg_lgeom g, const float2* __restrict__ Ke,
+                                                         const uint8_t* __restrict__ bc,
+                                                         const double* __restrict__ x, double* y) {
+    __shared__ float2 us[4][81];
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    const int64_t e = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (e >= g.n_el) return;   // warp-uniform
+    int ex[3];
+    double h[3];
+    q2e3(g, e, ex, h);
+    for (int k = lane; k < 81; k += 32) {
+        const int64_t dof = q2node3(g, ex, k / 3) * 3 + k % 3;
+        const double v = bc[dof] ? 0.0 : x[dof];
+        const float hi = (float)v;
+        us[wl][k] = make_float2(hi, (float)(v - (double)hi));
+    }
+    __syncwarp();
+    const float2* K = Ke + e * (int64_t)KE_N;
+    for (int rr = lane; rr < 81; rr += 32) {
+        float sh = 0.0f, sl = 0.0f;
+        for (int cc = 0; cc < 81; cc++) {
+            const float2 k = K[rr <= cc ? ke_idx(rr, cc) : ke_idx(cc, rr)];
+            const float2 u = us[wl][cc];
+            const float ph = k.x * u.x;                 // TwoProd: ph + pl = k.x u.x exactly
+            float pl = fmaf(k.x, u.x, -ph);
+            pl = fmaf(k.x, u.y, pl);                    // cross terms into the low part
+            pl = fmaf(k.y, u.x, pl);
+            const float s = sh + ph;                    // TwoSum: s + err = sh + ph exactly
+            const float bb = s - sh;
+            const float err = (sh - (s - bb)) + (ph - bb);
+            sh = s;
+            sl += err + pl;
+        }
+        const int64_t dof = q2node3(g, ex, rr / 3) * 3 + rr % 3;
+        if (!bc[dof]) atomicAdd(&y[dof], (double)sh + (double)sl);
+    }
+}
+
 // G_e[(A,i)][k] = -(prod_{j != i} h_j / 2) GR[i][A][k]
 __device__ __forceinline__ double q2_Ge3(const double* h, int A, int i, int k) {
     const double f = i == 0 ? (h[1] * 0.5) * (h[2] * 0.5) : (i == 1 ? (h[0] * 0.5) * (h[2] * 0.5) : (h[0] * 0.5) * (h[1] * 0.5));
@@ -646,6 +704,17 @@ int uwg_q2_3d_assemble(uwg_ctx* c, const int32_t* off, const int32_t* list, cons
     if (c->q2_ke) {
         k_elmat_q2_3d<<<(unsigned)c->n_el, 32, sizeof(ElmatScratch), c->stream>>>(g, c->lev[0].W64, c->q2_ke);
         UWG_CUDA(c, cudaGetLastError());
+        if (!c->q2_ke_df) {
+            cudaError_t e = cudaMalloc((void**)&c->q2_ke_df, sizeof(float2) * (size_t)KE_N * c->n_el);
+            if (e != cudaSuccess) {
+                c->q2_ke_df = nullptr;   // no room: refinement residuals use the FP64 apply
+                cudaGetLastError();
+            }
+        }
+        if (c->q2_ke_df) {
+            k_split_df<<<152 * 16, 256, 0, c->stream>>>((int64_t)KE_N * c->n_el, c->q2_ke, c->q2_ke_df);
+            UWG_CUDA(c, cudaGetLastError());
+        }
     }
     return UWG_OK;
 }
@@ -670,6 +739,16 @@ int uwg_q2_3d_applyK(uwg_ctx* c, const T* x, T* y, bool mask_in) {
     return UWG_OK;
 }
 template int uwg_q2_3d_applyK<double>(uwg_ctx*, const double*, double*, bool);
+
+// y += K x at free dofs in double-float arithmetic; UWG_ERR_STATE when the
+// double-float element matrices are absent (the caller then uses the FP64 apply)
+int uwg_q2_3d_applyK_df(uwg_ctx* c, const double* x, double* y) {
+    if (!c->q2_ke_df) return UWG_ERR_STATE;
+    const uwg_level& L = c->lev[0];
+    k_applyK_q2_3d_df<<<nblk(L.n_el * 32, 128), 128, 0, c->stream>>>(uwg_level_geom(c, 0), c->q2_ke_df, L.bc, x, y);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
 template int uwg_q2_3d_applyK<float>(uwg_ctx*, const float*, float*, bool);
 
 int uwg_q2_3d_diag(uwg_ctx* c, double* sinv) {

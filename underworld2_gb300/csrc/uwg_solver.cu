@@ -296,7 +296,7 @@ int velocity_solve(uwg_ctx* c, const SolveCfg& cfg, const double* b, double* x, 
     for (int step = 0; step < 30; step++) {
         vk_copy<double>(s, n, b, w->ref_r);
         if (step > 0 || !x_zero) {   // from a zero start the first residual is b itself
-            if ((rc = uwg_ops_applyK<double>(c, 0, x, w->ref_d))) return rc;
+            if ((rc = uwg_ops_applyK_refine(c, x, w->ref_d))) return rc;
             vk_axpy<double>(s, n, -1.0, w->ref_d, w->ref_r);
         }
         double rn;
