@@ -34,9 +34,12 @@ struct dvc_args {
     int nmax;            // particle slots per warp in shared memory (<= DVC_NMAX)
 };
 
-// Shared memory of one warp for a grid of RC cells and nmax particle slots.
+// Shared memory of one warp for a grid of RC cells and nmax particle slots:
+// coordinates, pool headers, FP32 coordinates, the boundary-list membership
+// bits (one per cell) and the owner byte of every cell.
 __host__ __device__ inline size_t dvc_warp_bytes(int RC, int nmax) {
-    size_t b = (size_t)RC * 2 + (size_t)nmax * 3 * 8 + (size_t)nmax * 4 * 4 + (size_t)nmax * 3 * 4;
+    size_t b = (size_t)nmax * 3 * 8 + (size_t)nmax * 4 * 4 + (size_t)nmax * 3 * 4 + (size_t)((RC + 31) / 32) * 4 +
+               (size_t)RC;
     return (b + 15) & ~(size_t)15;
 }
 
@@ -68,8 +71,8 @@ __global__ void __launch_bounds__(32 * DVC_WARPS) k_dvc(dvc_args a) {
     double* xs = (double*)wbase;                       // [NM][3]
     int32_t* hdr = (int32_t*)(xs + NM * 3);            // [2][NM][2] (offset, length) per pool
     float* xf = (float*)(hdr + NM * 4);                // [NM][3] FP32 copies (distance pre-test)
-    uint8_t* owner = (uint8_t*)(xf + NM * 3);          // [RC]
-    uint8_t* done = owner + RC;                        // [RC]
+    uint32_t* done = (uint32_t*)(xf + NM * 3);         // [(RC + 31) / 32] bit c: cell c already listed
+    uint8_t* owner = (uint8_t*)(done + (RC + 31) / 32); // [RC]
     if (threadIdx.x == 0) {
         double dx = (1.0 - -1.0) / R;
         double X = -1.0 - dx / 2.0;
@@ -98,7 +101,8 @@ __global__ void __launch_bounds__(32 * DVC_WARPS) k_dvc(dvc_args a) {
             xf[k * 3 + 1] = (float)xs[k * 3 + 1];
             xf[k * 3 + 2] = (float)xs[k * 3 + 2];
         }
-        for (int c = lane; c < RC; c += 32) { owner[c] = 0xFF; done[c] = 0; }
+        for (int c = lane; c < RC; c += 32) owner[c] = 0xFF;
+        for (int wd = lane; wd < (RC + 31) / 32; wd += 32) done[wd] = 0u;
         __syncwarp();
 
         int cur = 0;
@@ -124,13 +128,13 @@ __global__ void __launch_bounds__(32 * DVC_WARPS) k_dvc(dvc_args a) {
                         case 4: c1 = ck < R - 1 ? c0 + R * R : -1; break;
                         default: c1 = ck > 0 ? c0 - R * R : -1; break;
                     }
-                    ok = c1 >= 0 && owner[c1] != i && done[c1] == 0;
+                    ok = c1 >= 0 && owner[c1] != i && ((done[c1 >> 5] >> (c1 & 31)) & 1u) == 0u;
                 }
                 unsigned m = __match_any_sync(0xffffffffu, ok ? c1 : -2 - lane);
                 bool keep = ok && (__ffs(m) - 1 == lane);
                 unsigned kb = __ballot_sync(0xffffffffu, keep);
                 if (keep) {
-                    done[c1] = 1;
+                    atomicOr(&done[c1 >> 5], 1u << (c1 & 31));   // lanes may share a word
                     int64_t pos = start + cnt + __popc(kb & lt);
                     if (pos < a.pcap) pool[dst][pos] = (int16_t)c1;
                 }
@@ -138,7 +142,10 @@ __global__ void __launch_bounds__(32 * DVC_WARPS) k_dvc(dvc_args a) {
                 __syncwarp();
             }
             if (start + cnt > a.pcap) overflow = true;
-            for (int k = lane; k < cnt && start + k < a.pcap; k += 32) done[pool[dst][start + k]] = 0;
+            for (int k = lane; k < cnt && start + k < a.pcap; k += 32) {
+                const int c = pool[dst][start + k];
+                atomicAnd(&done[c >> 5], ~(1u << (c & 31)));
+            }
             if (lane == 0) {
                 hdr[(dst * NM + i) * 2 + 0] = (int32_t)start;
                 hdr[(dst * NM + i) * 2 + 1] = cnt;
