@@ -97,3 +97,21 @@ def test_steady_flux_profile(method):
     for _ in range(4000 if method == "SUPG" else 400):
         ad.integrate(dt)
     np.testing.assert_allclose(T.data[:, 0], q * (1.0 - m.data[:, 1]) / kappa, atol=1e-6)
+
+
+@pytest.mark.parametrize("et", ["Q1/dQ0", "Q2/dPc1"])
+def test_surface_term_exact_integrals(et):
+    """Pins the oracle and the product on a quadratic flux q = 1 + x + x^2 along
+    the bottom wall of [0, 2] x [0, 1]: the entries sum to the integral of q
+    (partition of unity) and their first moment to the integral of q x
+    (isoparametric coordinates), both exact with 3 Gauss points per face."""
+    m = uw.mesh.FeMesh_Cartesian(et, (4, 3), (0.0, 0.0), (2.0, 1.0))
+    T = m.add_variable(1)
+    x = uw.function.coord()
+    c = uw.conditions.NeumannCondition(T, (m.specialSets["MinJ_VertexSet"],), fn_flux=1.0 + x[0] + x[0] * x[0])
+    ref = surface_term(m._axes, m._order, c.mask().astype(bool), lambda p: [1.0 + p[0] + p[0] ** 2], 3)
+    got = systems._surface_flux(c, 3, "cpu").numpy()
+    for v in (ref, got):
+        assert abs(v.sum() - (2.0 + 2.0 + 8.0 / 3.0)) < 1e-13
+        assert abs((v * m.data[:, 0]).sum() - (2.0 + 8.0 / 3.0 + 4.0)) < 1e-13
+        assert np.all(v[m.data[:, 1] > 0] == 0.0)
