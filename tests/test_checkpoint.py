@@ -230,3 +230,43 @@ def test_swarm_and_variable_save_load(tmp_path):
     v19 = m19.add_variable(1)
     v19.load(str(tmp_path / "v.h5"), interpolate=True)
     np.testing.assert_allclose(v19.data[:, 0], 1.0 + 2.0 * m19.data[:, 0] - 0.5 * m19.data[:, 1], atol=1e-12)
+
+
+def _pad8(b):
+    return b + b"\0" * ((-len(b)) % 8)
+
+
+def test_h5_reader_continuation_and_vlen_strings():
+    """Reader paths that libhdf5-written files use: an object header whose
+    messages continue in a second block (continuation message 0x0010), and a
+    variable-length string attribute whose bytes live in a global heap
+    collection (how h5py stores Python str attributes).  Byte layouts follow
+    the HDF5 file-format specification."""
+    import struct
+    from underworld2_gb300.h5 import _Reader
+    # global heap collection at 256: object 1 = b"Q2"
+    text = b"Q2"
+    obj = struct.pack("<HH4xQ", 1, 1, len(text)) + _pad8(text)
+    gcol = b"GCOL" + bytes([1, 0, 0, 0]) + struct.pack("<Q", 16 + len(obj) + 16) + obj + b"\0" * 16
+    # attribute "elementType": class 9 (variable length), type 1 (string), size 16,
+    # base type: 1-byte string; scalar dataspace; value = (length, heap address, index)
+    base = bytes([0x10 | 3, 0, 0, 0]) + struct.pack("<I", 1)
+    dt = bytes([0x10 | 9, 0x01, 0, 0]) + struct.pack("<I", 16) + base
+    sp = bytes([1, 0, 0, 0]) + b"\0" * 4
+    name = b"elementType\0"
+    body = struct.pack("<BxHHH", 1, len(name), len(dt), len(sp)) + _pad8(name) + _pad8(dt) + _pad8(sp) + \
+        struct.pack("<IQI", len(text), 256, 1)
+    body = _pad8(body)
+    amsg = struct.pack("<HHB3x", 0x000C, len(body), 0) + body
+    # object header at 0: one continuation message pointing at the block at 64
+    cont = struct.pack("<HHB3x", 0x0010, 16, 0) + struct.pack("<QQ", 64, len(amsg))
+    hdr = struct.pack("<BxHII4x", 1, 2, 1, len(cont)) + cont
+    buf = bytearray(512)
+    buf[0:len(hdr)] = hdr
+    buf[64:64 + len(amsg)] = amsg
+    buf[256:256 + len(gcol)] = gcol
+    r = _Reader(bytes(buf))
+    msgs = r.messages(0)
+    assert [m[0] for m in msgs] == [0x0010, 0x000C]
+    name_out, value = r.attribute(msgs[1][1])
+    assert name_out == "elementType" and value == "Q2"
