@@ -107,3 +107,26 @@ def test_branching():
     np.testing.assert_array_equal(m.evaluate(x), [[10.0], [20.0], [30.0]])
     c = fn.branching.conditional([(fn.input()[0] < 0.5, -1.0), (True, 1.0)])
     np.testing.assert_array_equal(c.evaluate(x), [[-1.0], [1.0], [1.0]])
+
+
+def test_view_count_and_custom_exception():
+    """P/function/view.py:385-440 and P/function/exception.py:69-140 docstring behaviour."""
+    import underworld2_gb300.function as fn
+    c = fn.view.count(fn.input())
+    c.evaluate(5.0)
+    assert c.count() == 1
+    for _ in range(3):
+        c.evaluate(5.0)
+    assert c.count() == 4
+    c.reset()
+    c.evaluate(5.0)
+    c.evaluate(5.0)
+    assert c.count() == 2
+    c.evaluate(np.zeros((7, 2)))          # one count per point
+    assert c.count() == 9
+    one = fn.misc.constant(1.0)
+    np.testing.assert_array_equal(fn.exception.CustomException(one, one < 2.0).evaluate(), [[1.0]])
+    with pytest.raises(RuntimeError, match="evaluated to False"):
+        fn.exception.CustomException(one, one > 2.0).evaluate()
+    with pytest.raises(RuntimeError, match=r"\( 5 \)"):
+        fn.exception.CustomException(one, one * 5.0 > 20.0, one * 5.0).evaluate()

@@ -14,7 +14,7 @@ P/function/math.py, ``misc.min/max``, ``tensor.symmetric/antisymmetric/
 second_invariant/deviatoric`` (L/StgDomain/Geometry/src/TensorMath.c
 conventions: full tensors row-major, symmetric tensors [00, 11, (22,) 01,
 (02, 12)]), ``shape.Polygon``, ``branching.map/conditional``,
-``view.min_max``, ``exception.SafeMaths`` and
+``view.min_max``, ``view.count``, ``exception.SafeMaths``, ``exception.CustomException`` and
 ``rheology.stress_limiting_viscosity``.  ``Function.evaluate`` accepts
 coordinates, a mesh or a swarm, as the reference's.
 """
@@ -471,9 +471,42 @@ class _SafeMaths(Function):
         return v
 
 
+class _CustomException(Function):
+    """Pass-through of fn_input where fn_condition holds at every point; else a
+    RuntimeError carrying fn_print's values at the first failing point
+    (P/function/exception.py:69-140)."""
+
+    def __init__(self, fn_input, fn_condition, fn_print=None):
+        self.a = Function.convert(fn_input)
+        self.cond = Function.convert(fn_condition)
+        self.pr = Function.convert(fn_print) if fn_print is not None else None
+        if not isinstance(self.a, Function) or not isinstance(self.cond, Function):
+            raise ValueError("provided 'fn_input' and 'fn_condition' must be 'Function' or convertible.")
+        self._kind = self.a._kind
+
+    def _children(self):
+        return [self.a, self.cond] + ([self.pr] if self.pr is not None else [])
+
+    def _eval(self, ctx):
+        ok = self.cond.evaluate_at(ctx)[:, 0] != 0
+        if not bool(ok.all()):
+            msg = "CustomException condition function has evaluated to False for current input!"
+            if self.pr is not None:
+                bad = int(torch.nonzero(~ok)[0])
+                vals = self.pr.evaluate_at(ctx)[bad].to(torch.float64).tolist()
+                msg += ("\nPrint function returns the following values (cast to double precision):\n    ( %s )"
+                        % " ".join("%g" % v for v in vals))
+            raise RuntimeError(msg)
+        return self.a.evaluate_at(ctx)
+
+
 class exception:
     @staticmethod
     def SafeMaths(fn, *args, **kwargs): return _SafeMaths(fn)
+
+    @staticmethod
+    def CustomException(fn_input, fn_condition, fn_print=None, *args, **kwargs):
+        return _CustomException(fn_input, fn_condition, fn_print)
 
 
 class _StressLimit(Function):
@@ -526,12 +559,43 @@ class _MinMax(Function):
     def max_global(self): return self._max
 
 
+class _Count(Function):
+    """Pass-through that counts its evaluations, one per point
+    (P/function/view.py:385-440)."""
+
+    def __init__(self, fn):
+        self.a = Function.convert(fn)
+        if not isinstance(self.a, Function):
+            raise ValueError("provided 'fn' must a 'Function' or convertible.")
+        self._kind = self.a._kind
+        self._n = 0
+
+    def _children(self):
+        return [self.a]
+
+    def _eval(self, ctx):
+        v = self.a.evaluate_at(ctx)
+        self._n += int(ctx.n)
+        return v
+
+    def count(self):
+        return self._n
+
+    def reset(self):
+        self._n = 0
+
+
 class view:
     @staticmethod
     def min_max(fn, fn_norm=None, fn_auxiliary=None, *args, **kwargs):
         """Pass-through that records the extrema of its input (of fn_norm where
         given, of the magnitude for vectors) over every evaluation (P/function/view.py)."""
         return _MinMax(fn, fn_norm, fn_auxiliary)
+
+    @staticmethod
+    def count(fn):
+        """Pass-through that counts its evaluations (one per point)."""
+        return _Count(fn)
 
 
 def _input_context(inputData):
