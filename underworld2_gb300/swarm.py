@@ -473,5 +473,207 @@ class PerCellRandomLayout(_ParticleLayoutAbstract):
         self.swarm._set_particles(x, owner, off, lst)
 
 
+# ---------------------------------------------------------------------------
+# Host-side layouts.  The reference generates these positions serially on the
+# host at swarm set-up (no GPU counterpart is needed for a one-time fill); the
+# arithmetic below follows its expressions so that positions are bit-identical.
+# ---------------------------------------------------------------------------
+_PM_M = 2147483647
+
+# Sobol generators of the first three axes, from the reference's table
+# (L/StgDomain/Utils/src/SobolGenerator.c:288-321, the initialisation of Joe and
+# Kuo, ACM TOMS 29(1), 2003): polynomial degree, coefficient, initial direction
+# numbers.
+_SOBOL_TABLE = ((1, 0, (1,)), (2, 1, (1, 1)), (3, 1, (1, 3, 7)))
+_SOBOL_BITS = 30   # WORDLENGTH of SobolGenerator_GetNextNumber
+
+
+def _sobol_direction_numbers(axis):
+    """Direction numbers v_0..v_29 of an axis' generator by the recurrence of
+    SobolGenerator_GetDirectionalNumber (SobolGenerator.c:179-216)."""
+    deg, coef, init = _SOBOL_TABLE[axis]
+    v = list(init)
+    while len(v) < _SOBOL_BITS:
+        i = len(v)
+        r = last = 0
+        for c in range(deg):
+            if c == deg - 1 or (coef >> (deg - 2 - c)) & 1:
+                last = v[i - 1 - c]
+                r ^= ((1 << (c + 1)) * last) & 0xFFFFFFFF
+        v.append((r ^ last) & 0xFFFFFFFF)
+    return v
+
+
+def _sobol(axis, n):
+    """The n-th value (n >= 1, uint64 array) that successive
+    SobolGenerator_GetNextNumber calls return (SobolGenerator.c:218-241): the
+    Gray code of n selects the direction numbers XOR-ed into the 30-bit word."""
+    v = _sobol_direction_numbers(axis)
+    g = n ^ (n >> np.uint64(1))
+    word = np.zeros(n.shape, dtype=np.uint64)
+    for b in range(_SOBOL_BITS):
+        bit = (g >> np.uint64(b)) & np.uint64(1)
+        word ^= bit * np.uint64(v[b] << (_SOBOL_BITS - b - 1))
+    return word.astype(np.float64) / float(1 << _SOBOL_BITS)
+
+
+def _pm_draws(state, n):
+    """The next n states of the Park-Miller stream (Random.c:23-53) after
+    `state`, by jump-ahead powers of 16807, and the state after the last."""
+    if n == 0:
+        return np.zeros(0, dtype=np.uint64), state
+    M = np.uint64(_PM_M)
+    pw = np.empty(n, dtype=np.uint64)       # pw[j] = 16807^(j+1) mod M
+    pw[0] = 16807
+    m = 1
+    while m < n:
+        k = min(m, n - m)
+        pw[m:m + k] = (pw[:k] * pw[m - 1]) % M
+        m += k
+    st = (pw * np.uint64(state)) % M
+    return st, int(st[-1])
+
+
+def _shape_values(dim, order, xi):
+    """Shape functions at local coordinates xi[n, dim], lexicographic nodes, in
+    the expressions of BilinearElementType.c:179-211, TrilinearElementType.c:
+    215-274, Biquadratic.c:138-200 and Triquadratic.c:193-300."""
+    x = xi[:, 0]
+    y = xi[:, 1]
+    if dim == 2 and order == 1:
+        return np.stack([0.25 * (1.0 - x) * (1.0 - y), 0.25 * (1.0 + x) * (1.0 - y),
+                         0.25 * (1.0 - x) * (1.0 + y), 0.25 * (1.0 + x) * (1.0 + y)], 1)
+    if dim == 3 and order == 1:
+        z = xi[:, 2]
+        out = []
+        for c in range(2):
+            fz = (1.0 - z) if c == 0 else (1.0 + z)
+            for b in range(2):
+                fy = (1.0 - y) if b == 0 else (1.0 + y)
+                for a in range(2):
+                    fx = (1.0 - x) if a == 0 else (1.0 + x)
+                    out.append(0.125 * fx * fy * fz)
+        return np.stack(out, 1)
+    if dim == 2:
+        a0, b0 = x - 1.0, y - 1.0
+        a1, b1 = 1.0 - x * x, 1.0 - y * y
+        a2, b2 = x + 1.0, y + 1.0
+        m0, m1, m2 = 0.5 * x, 0.5 * y, 0.25 * x * y
+        return np.stack([m2 * a0 * b0, m1 * a1 * b0, m2 * a2 * b0, m0 * a0 * b1, a1 * b1, m0 * a2 * b1,
+                         m2 * a0 * b2, m1 * a1 * b2, m2 * a2 * b2], 1)
+    z = xi[:, 2]
+    A = (x - 1.0, 1.0 - x * x, x + 1.0)
+    B = (y - 1.0, 1.0 - y * y, y + 1.0)
+    C = (z - 1.0, 1.0 - z * z, z + 1.0)
+    m0, m1, m2 = 0.5 * x, 0.5 * y, 0.5 * z
+    m3, m4, m5 = 0.25 * x * y, 0.25 * x * z, 0.25 * y * z
+    m6 = 0.125 * x * y * z
+    mfull = (None, m2, m1, m5, m0, m4, m3, m6)   # by corner axes (x: 4, y: 2, z: 1)
+    out = []
+    for n in range(27):
+        a, b, c = n % 3, (n // 3) % 3, n // 9
+        sel = (a != 1) * 4 + (b != 1) * 2 + (c != 1)
+        out.append(mfull[sel] * A[a] * B[b] * C[c] if sel else A[a] * B[b] * C[c])
+    return np.stack(out, 1)
+
+
+def _local_to_global(mesh, el, xi):
+    """FeMesh_CoordLocalToGlobal (L/StgFEM/Discretisation/src/FeMesh.c:333-360):
+    x = sum over the element's nodes, in order, of N_A(xi) times the vertex."""
+    N = _shape_values(mesh.dim, mesh._order, xi)
+    X = mesh.data
+    en = mesh.data_elementNodes[el]
+    out = np.zeros((len(el), mesh.dim))
+    for a in range(N.shape[1]):
+        va = X[en[:, a]]
+        for d in range(mesh.dim):
+            out[:, d] += N[:, a] * va[:, d]
+    return out
+
+
+def _space_filler_positions(mesh, ppc, state, chunk=1 << 22):
+    """PerCellSpaceFillerLayout (L/StgFEM/Utils/src/MeshParticleLayout.c:194-230,
+    filltype 0): cells in order, particles in order; one draw of the shared
+    stream per particle, and when it exceeds 0.9 every axis' generator skips one
+    value; local coordinate = (1 - -1) * sobol + -1.  Returns (x, state)."""
+    n_el = mesh.elementsGlobal
+    total = n_el * ppc
+    out = np.empty((total, mesh.dim))
+    skipped = 0
+    for start in range(0, total, chunk):
+        n = min(chunk, total - start)
+        st, state = _pm_draws(state, n)
+        rnd = (1.0 - 0.0) * st.astype(np.float64) / float(_PM_M) + 0.0
+        skip = (rnd > 0.9).astype(np.uint64)
+        idx = np.arange(start + 1, start + n + 1, dtype=np.uint64) + np.uint64(skipped) + np.cumsum(skip)
+        skipped += int(skip.sum())
+        xi = np.stack([(1.0 - -1.0) * _sobol(d, idx) + -1.0 for d in range(mesh.dim)], 1)
+        out[start:start + n] = _local_to_global(mesh, np.arange(start, start + n) // ppc, xi)
+    return out, state
+
+
+def _gauss_positions(mesh, count):
+    """PerCellGaussLayout (L/StgFEM/Discretisation/src/IrregularMeshGaussLayout.c:
+    143-177): per cell count^dim particles at the Gauss-Legendre abscissae,
+    x index fastest."""
+    x1, _ = np.polynomial.legendre.leggauss(count)
+    per = count ** mesh.dim
+    p = np.arange(per)
+    loc = [x1[p % count], x1[(p // count) % count]] + ([x1[p // (count * count)]] if mesh.dim == 3 else [])
+    xi = np.tile(np.stack(loc, 1), (mesh.elementsGlobal, 1))
+    el = np.repeat(np.arange(mesh.elementsGlobal), per)
+    return _local_to_global(mesh, el, xi), per
+
+
+def _set_per_cell(swarm, x, per):
+    """Particles generated per cell in cell order: owner = generating cell."""
+    ctx = swarm.mesh.ctx
+    n_el = swarm.mesh.elementsGlobal
+    dev = ctx.device
+    xt = torch.from_numpy(np.ascontiguousarray(x)).to(dev)
+    owner = torch.arange(n_el, device=dev, dtype=torch.int32).repeat_interleave(per)
+    off = (torch.arange(n_el + 1, device=dev, dtype=torch.int64) * per).to(torch.int32)
+    lst = torch.arange(n_el * per, device=dev, dtype=torch.int32)
+    swarm._set_particles(xt, owner, off, lst)
+
+
+class PerCellSpaceFillerLayout(_ParticleLayoutAbstract):
+    """Per-element quasi-random (Sobol) layout (P/swarm/layouts.py:146-184,
+    L/StgFEM/Utils/src/MeshParticleLayout.c:194-230).  Constructing the layout
+    seeds the process-wide stream with 13, as _MeshParticleLayout_Init does."""
+
+    def __init__(self, swarm, particlesPerCell, **kwargs):
+        if not isinstance(particlesPerCell, int):
+            raise TypeError("'particlesPerCell' object passed in must be of type 'int'.")
+        if particlesPerCell < 1:
+            raise ValueError("'particlesPerCell' object passed in must take a value greater than zero.")
+        super().__init__(swarm)
+        self.particlesPerCell = particlesPerCell
+        _RNG["state"] = _core.rng_seed(13)
+
+    def _populate(self):
+        x, _RNG["state"] = _space_filler_positions(self.swarm.mesh, self.particlesPerCell, _RNG["state"])
+        _set_per_cell(self.swarm, x, self.particlesPerCell)
+
+
+class PerCellGaussLayout(_ParticleLayoutAbstract):
+    """Particles at the Gauss points of every element (P/swarm/layouts.py:53-108)."""
+
+    def __init__(self, swarm, gaussPointCount, **kwargs):
+        if not isinstance(gaussPointCount, int):
+            raise TypeError("'gaussPointCount' object passed in must be of type 'int'")
+        if gaussPointCount not in (1, 2, 3, 4, 5):
+            raise ValueError("'gaussPointCount' object passed in must take a value between \n between 1 and 5 "
+                             "inclusive.")
+        super().__init__(swarm)
+        self.gaussPointCount = gaussPointCount
+
+    def _populate(self):
+        x, per = _gauss_positions(self.swarm.mesh, self.gaussPointCount)
+        _set_per_cell(self.swarm, x, per)
+
+
 class layouts:
     PerCellRandomLayout = PerCellRandomLayout
+    PerCellSpaceFillerLayout = PerCellSpaceFillerLayout
+    PerCellGaussLayout = PerCellGaussLayout
