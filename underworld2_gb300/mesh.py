@@ -171,6 +171,11 @@ class FeMesh_Cartesian:
         self._axes = mesh._axes
         self._ctx = None
 
+    def integrate(self, fn):
+        """Volume integral of fn over the mesh (P/mesh/_mesh.py:1200-1226)."""
+        from .utils import Integral
+        return Integral(fn, mesh=self).evaluate()
+
     def _node_grid(self):
         n = [r * self._order + 1 for r in self.elementRes]
         idx = np.arange(self.nodesGlobal)
@@ -178,6 +183,82 @@ class FeMesh_Cartesian:
         if self.dim == 3:
             out.append(idx // (n[0] * n[1]))
         return out, n
+
+
+# Faces of an element in the reference's border-layout numbering
+# (GaussBorderParticleLayout.c:300-320): faces 0, 1 lie at y = -1, +1, faces 2, 3
+# at x = -1, +1, faces 4, 5 at z = -1, +1 (even faces at -1, odd at +1).
+_FACE_AXIS = (1, 1, 0, 0, 2, 2)
+
+
+def _border_points(mesh, node_on, n_gauss):
+    """Gauss points on the faces of the elements that hold a flagged node
+    (GaussBorderParticleLayout.c:186-290), kept where the interpolated node
+    indicator exceeds 0.999 (the mask of P/systems/sle/_assemblyterm.py:124-144
+    and P/utils/_utils.py:131-142).  Returns numpy arrays: global coordinates
+    [q, dim], weight x surface Jacobian [q] (ElementType.c:566-606: the product
+    of h_j / 2 over the face's axes), shape values [q, nen] and element nodes
+    [q, nen] of the kept points."""
+    dim, o = mesh.dim, mesh._order
+    en = mesh.data_elementNodes.astype(np.int64)
+    flagged = np.nonzero(node_on[en].any(1))[0]
+    x1, w1 = np.polynomial.legendre.leggauss(n_gauss)
+    pts, wts, fax = [], [], []
+    for f in range(2 * dim):
+        k = _FACE_AXIS[f]
+        others = [a for a in range(dim) if a != k]
+        for idx in np.ndindex(*([n_gauss] * (dim - 1))):
+            xi = np.zeros(dim)
+            xi[k] = -1.0 if f % 2 == 0 else 1.0
+            w = 1.0
+            for a, i in zip(others, idx):
+                xi[a] = x1[i]
+                w *= w1[i]
+            pts.append(xi)
+            wts.append(w)
+            fax.append(k)
+    pts, wts, fax = np.array(pts), np.array(wts), np.array(fax)
+    kk = o + 1
+    loc = np.arange(kk ** dim)
+    li = [loc % kk, (loc // kk) % kk] + ([loc // (kk * kk)] if dim == 3 else [])
+    N = np.ones((len(pts), kk ** dim))
+    for d in range(dim):
+        s_ = pts[:, d]
+        b = np.stack([(1 - s_) / 2, (1 + s_) / 2], 1) if o == 1 else \
+            np.stack([0.5 * s_ * (s_ - 1), 1 - s_ * s_, 0.5 * s_ * (s_ + 1)], 1)
+        N *= b[:, li[d]]
+    r = mesh.elementRes
+    ei = [flagged % r[0], (flagged // r[0]) % r[1]] + ([flagged // (r[0] * r[1])] if dim == 3 else [])
+    det = np.ones((len(flagged), len(pts)))
+    for d in range(dim):
+        h = mesh._axes[d][(ei[d] + 1) * o] - mesh._axes[d][ei[d] * o]
+        det *= np.where(fax[None, :] == d, 1.0, (h / 2.0)[:, None])
+    enf = en[flagged]
+    delta = node_on.astype(np.float64)[enf] @ N.T
+    fe, pe = np.nonzero(delta > 0.999)
+    xg = np.einsum("qa,qad->qd", N[pe], mesh.data[enf[fe]])
+    return xg, wts[pe] * det[fe, pe], N[pe], enf[fe]
+
+
+def _volume_points(mesh, n_gauss, first, count):
+    """Global coordinates [count * n^dim, dim] and weight x det J of the n^dim
+    Gauss points of elements first .. first+count-1 (x fastest, element-major)."""
+    dim, o = mesh.dim, mesh._order
+    x1, w1 = np.polynomial.legendre.leggauss(n_gauss)
+    q = np.arange(n_gauss ** dim)
+    qi = [q % n_gauss, (q // n_gauss) % n_gauss] + ([q // (n_gauss * n_gauss)] if dim == 3 else [])
+    w = np.prod([w1[qi[d]] for d in range(dim)], axis=0)
+    e = np.arange(first, first + count)
+    r = mesh.elementRes
+    ei = [e % r[0], (e // r[0]) % r[1]] + ([e // (r[0] * r[1])] if dim == 3 else [])
+    xg = np.empty((count, len(q), dim))
+    det = np.ones(count)
+    for d in range(dim):
+        lo = mesh._axes[d][ei[d] * o]
+        hi = mesh._axes[d][(ei[d] + 1) * o]
+        xg[:, :, d] = lo[:, None] + (x1[qi[d]][None, :] + 1.0) * 0.5 * (hi - lo)[:, None]
+        det *= (hi - lo) / 2.0
+    return xg.reshape(-1, dim), (det[:, None] * w[None, :]).reshape(-1)
 
 
 class _SubMesh:

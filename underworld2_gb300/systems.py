@@ -422,12 +422,6 @@ def _neumann_flux(conditions, n_gauss, device, scale=1.0):
     return None if out is None else (out * scale).contiguous()
 
 
-# Faces of an element in the reference's border-layout numbering
-# (GaussBorderParticleLayout.c:300-320): faces 0, 1 lie at y = -1, +1, faces 2, 3
-# at x = -1, +1, faces 4, 5 at z = -1, +1 (even faces at -1, odd at +1).
-_FACE_AXIS = (1, 1, 0, 0, 2, 2)
-
-
 def _surface_geometry(cond, n_gauss, device):
     """Points and weights of a NeumannCondition's surface integral, cached on
     the condition: the Gauss points of every face of every element that holds a
@@ -443,49 +437,11 @@ def _surface_geometry(cond, n_gauss, device):
     mesh = var.mesh
     if not isinstance(mesh, _mesh.FeMesh_Cartesian):
         raise NotImplementedError("Neumann conditions are provided for velocity-mesh variables")
-    dim, o, ndof = mesh.dim, mesh._order, var.nodeDofCount
+    ndof = var.nodeDofCount
     cm = cond.mask().astype(bool)
-    node_on = cm.any(1)
-    en = mesh.data_elementNodes.astype(np.int64)
-    flagged = np.nonzero(node_on[en].any(1))[0]
-    x1, w1 = np.polynomial.legendre.leggauss(n_gauss)
-    pts, wts, fax = [], [], []
-    for f in range(2 * dim):
-        k = _FACE_AXIS[f]
-        others = [a for a in range(dim) if a != k]
-        for idx in np.ndindex(*([n_gauss] * (dim - 1))):
-            xi = np.zeros(dim)
-            xi[k] = -1.0 if f % 2 == 0 else 1.0
-            w = 1.0
-            for a, i in zip(others, idx):
-                xi[a] = x1[i]
-                w *= w1[i]
-            pts.append(xi)
-            wts.append(w)
-            fax.append(k)
-    pts, wts, fax = np.array(pts), np.array(wts), np.array(fax)
-    kk = o + 1
-    loc = np.arange(kk ** dim)
-    li = [loc % kk, (loc // kk) % kk] + ([loc // (kk * kk)] if dim == 3 else [])
-    N = np.ones((len(pts), kk ** dim))
-    for d in range(dim):
-        s_ = pts[:, d]
-        b = np.stack([(1 - s_) / 2, (1 + s_) / 2], 1) if o == 1 else \
-            np.stack([0.5 * s_ * (s_ - 1), 1 - s_ * s_, 0.5 * s_ * (s_ + 1)], 1)
-        N *= b[:, li[d]]
-    r = mesh.elementRes
-    ei = [flagged % r[0], (flagged // r[0]) % r[1]] + ([flagged // (r[0] * r[1])] if dim == 3 else [])
-    det = np.ones((len(flagged), len(pts)))
-    for d in range(dim):
-        h = mesh._axes[d][(ei[d] + 1) * o] - mesh._axes[d][ei[d] * o]
-        det *= np.where(fax[None, :] == d, 1.0, (h / 2.0)[:, None])
-    enf = en[flagged]
-    delta = node_on.astype(np.float64)[enf] @ N.T
-    fe, pe = np.nonzero(delta > 0.999)
-    X = mesh.data
-    xg = np.einsum("qa,qad->qd", N[pe], X[enf[fe]])
+    xg, fac, Nq, nodes = _mesh._border_points(mesh, cm.any(1), n_gauss)
     to = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(device)
-    geo = (to(xg), to(wts[pe] * det[fe, pe]), to(N[pe]), to(enf[fe]), to(cm), ndof, mesh.nodesGlobal)
+    geo = (to(xg), to(fac), to(Nq), to(nodes), to(cm), ndof, mesh.nodesGlobal)
     cache[key] = geo
     return geo
 

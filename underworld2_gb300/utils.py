@@ -1,4 +1,4 @@
-"""Checkpoint handles and XDMF descriptions (``uw.utils`` subset).
+"""Integrals, checkpoint handles and XDMF descriptions (``uw.utils`` subset).
 
 ``SavedFileData`` is what every ``save`` returns (P/utils/_utils.py:207-222).
 The XDMF writers describe saved HDF5 files to visualisation tools in the
@@ -12,6 +12,93 @@ per-column hyperslabs.
 import os
 
 from . import h5
+
+
+class Integral:
+    """Volume or surface integral of a function over a mesh (P/utils/_utils.py:
+    38-206): Gauss points (3 per axis on Q1 meshes, 5 on Q2, as
+    GaussIntegrationSwarm), weight x det J, the function evaluated on the
+    device; a surface integral sums the Gauss points of the faces that lie in
+    ``surfaceIndexSet`` (the reference's border swarm and 0.999 indicator mask)
+    with the surface Jacobian.  ``evaluate()`` returns one value per function
+    component."""
+
+    def __init__(self, fn, mesh=None, integrationType="volume", surfaceIndexSet=None, integrationSwarm=None,
+                 **kwargs):
+        from .mesh import FeMesh_Cartesian
+        import numpy as np
+        if not mesh:
+            raise ValueError("A mesh object must be provided")
+        if not isinstance(mesh, FeMesh_Cartesian):
+            raise TypeError("'feMesh' object passed in must be of type 'FeMesh'")
+        if integrationType and integrationSwarm:
+            raise RuntimeError("Either an 'integrationType' or an 'integrationSwarm' may be provided, but not both.\n"
+                               "You may need to set 'integrationType' to None.")
+        if integrationSwarm is not None:
+            raise NotImplementedError("user integration swarms are not supported; use 'integrationType'")
+        if not isinstance(integrationType, str):
+            raise TypeError("'integrationType' provided must be a string.")
+        integrationType = integrationType.lower()
+        if integrationType not in ("volume", "surface"):
+            raise ValueError("'integrationType' string provided must be either 'volume' or 'surface'.")
+        self._mesh = mesh
+        self._surface = integrationType == "surface"
+        self._node_on = None
+        if self._surface:
+            if surfaceIndexSet is None:
+                raise RuntimeError("For surface integration, you must provide a 'surfaceIndexSet'.")
+            idx = np.asarray(surfaceIndexSet.data if hasattr(surfaceIndexSet, "data") else list(surfaceIndexSet),
+                             dtype=np.int64)
+            walls = set(mesh.specialSets["AllWalls_VertexSet"].data.tolist())
+            if any(int(i) not in walls for i in idx):
+                raise ValueError("Your surfaceIndexSet appears to contain node(s) which do not belong to the mesh "
+                                 "boundary. Surface integration across internal nodes is not currently supported.")
+            self._node_on = np.zeros(mesh.nodesGlobal, dtype=bool)
+            self._node_on[idx] = True
+        self.fn = fn
+
+    @property
+    def fn(self):
+        return self._fn
+
+    @fn.setter
+    def fn(self, fn):
+        from . import function as _fn
+        f = _fn.Function.convert(fn)
+        if not isinstance(f, _fn.Function):
+            raise TypeError("'fn' must be of or convertible to 'Function' class.")
+        if f.depends_on({"swarm"}):
+            raise ValueError("Gauss-point integration cannot evaluate swarm variables")
+        self._fn = f
+
+    def _eval(self, pts, wts, dev):
+        import torch
+        from . import function as _fn
+        xt = torch.from_numpy(pts).to(dev)
+        ectx = _fn.EvalContext(torch.full((xt.shape[0],), -1, dtype=torch.int64, device=dev), lambda: xt, dev)
+        v = self._fn.evaluate_at(ectx).to(torch.float64)
+        return (v * torch.from_numpy(wts).to(dev)[:, None]).sum(0)
+
+    def evaluate(self):
+        import numpy as np
+        import torch
+        from .mesh import _border_points, _volume_points
+        dev = torch.device("cuda") if torch.cuda.is_available() else torch.device("cpu")
+        m = self._mesh
+        ng = 3 if m._order == 1 else 5
+        if self._surface:
+            xg, fac, _, _ = _border_points(m, self._node_on, ng)
+            if len(xg) == 0:
+                return np.zeros(1)
+            return self._eval(xg, fac, dev).cpu().numpy()
+        total = None
+        step = max(1, (1 << 22) // ng ** m.dim)
+        for first in range(0, m.elementsGlobal, step):
+            cnt = min(step, m.elementsGlobal - first)
+            pts, wts = _volume_points(m, ng, first, cnt)
+            part = self._eval(pts, wts, dev)
+            total = part if total is None else total + part
+        return total.cpu().numpy()
 
 
 class SavedFileData:
