@@ -1,0 +1,18 @@
+"""Host-side parts of the uw-style API that need no GPU: solver options and
+statistics objects before a solve (P/systems/_bsscr.py:509-512,704-738)."""
+import underworld2_gb300 as uw
+
+
+def test_solver_option_setters_and_stats(capsys):
+    m = uw.mesh.FeMesh_Cartesian("Q1/dQ0", (4, 4), (0.0, 0.0), (1.0, 1.0))
+    v = m.add_variable(2)
+    p = m.subMesh.add_variable(1)
+    solver = uw.systems.Solver(uw.systems.Stokes(v, p, fn_viscosity=1.0))
+    a = solver.get_nonLinearStats()
+    assert a.picard_iterations == 0 and a.picard_residual == 0.0
+    solver.set_inner_method("mixed")
+    solver.set_inner_rtol(1e-9)
+    solver.set_outer_rtol(1e-8)
+    solver.print_petsc_options()
+    out = capsys.readouterr().out
+    assert "inner_method=mixed" in out and "inner_rtol=1e-09" in out and "outer_rtol=1e-08" in out

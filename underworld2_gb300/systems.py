@@ -307,6 +307,7 @@ class StokesSolver:
         nonlinear = self._check_linearity(nonLinearIterate) and bool(nonLinearIterate)
         its = nonLinearMaxIterations if nonlinear else 1
         prev = None
+        self._picard = (0, 0.0)
         for it in range(its):
             self._linear_solve(print_stats)
             if callback_post_solve is not None:
@@ -314,11 +315,31 @@ class StokesSolver:
             if not nonlinear:
                 break
             v = self._stokesSLE._velocityField.data.copy()
-            if prev is not None and it + 1 >= nonLinearMinIterations:
+            if prev is not None:
                 change = np.linalg.norm(v - prev) / max(np.linalg.norm(v), 1e-300)
-                if change < nonLinearTolerance:
+                self._picard = (it + 1, float(change))
+                if it + 1 >= nonLinearMinIterations and change < nonLinearTolerance:
                     break
+            else:
+                self._picard = (it + 1, 0.0)
             prev = v
+
+    def get_nonLinearStats(self):
+        """Picard iterations of the last nonlinear solve and the relative change
+        of the velocity in its last iteration (P/systems/_bsscr.py:728-738)."""
+        class _Stats:
+            pass
+        a = _Stats()
+        a.picard_iterations, a.picard_residual = getattr(self, "_picard", (0, 0.0))
+        return a
+
+    def print_petsc_options(self):
+        """Prints the solver options in use (the GPU solver's counterpart of the
+        reference's PETSc option string, P/systems/_bsscr.py:509-512)."""
+        o = self.options
+        print("Options: inner_method=%s inner_rtol=%g outer_rtol=%g mg_smooth=%d restart=%d max_inner=%d "
+              "max_outer=%d" % ("mixed" if o.A11._mixed else "mg", o.A11.ksp_rtol, o.scr.ksp_rtol,
+                                o.mg.smooth_steps, o.scr.restart, o.main.max_inner, o.main.max_outer))
 
     def _linear_solve(self, print_stats):
         s = self._stokesSLE
