@@ -16,3 +16,28 @@ def test_solver_option_setters_and_stats(capsys):
     solver.print_petsc_options()
     out = capsys.readouterr().out
     assert "inner_method=mixed" in out and "inner_rtol=1e-09" in out and "outer_rtol=1e-08" in out
+
+
+def test_property_members():
+    import numpy as np
+    m = uw.mesh.FeMesh_Cartesian("Q1/dQ0", (4, 4), (0.0, 0.0), (1.0, 1.0))
+    v = m.add_variable(2)
+    v.data[:, 0] = np.arange(v.data.shape[0])
+    c = v.copy()
+    assert c.nodeDofCount == 2 and c.mesh is m and np.all(c.data == 0.0)
+    d = v.copy(deepcopy=True)
+    np.testing.assert_array_equal(d.data, v.data)
+    assert v.dataType == "double" and v.syncronise() is None
+    p = m.subMesh.add_variable(1)
+    st = uw.systems.Stokes(v, p, fn_viscosity=1.0)
+    assert st.fn_one_on_lambda is None and st.fn_source is None
+    st.fn_one_on_lambda = 1e-3
+    assert isinstance(st.fn_one_on_lambda, uw.function.Function)
+    sw = uw.swarm.Swarm(m)
+    a = sw.add_variable("int", 1)
+    b = a.copy()
+    assert sw.variables == [a, b] and b.dataType == "int" and b.count == 1
+    adv = uw.systems.SwarmAdvector(v, sw)
+    assert adv.dt == 0.0 and adv.time == 0.0
+    adv.time = 2.5
+    assert adv.time == 2.5

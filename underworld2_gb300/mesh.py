@@ -328,6 +328,22 @@ class MeshVariable:
     def data(self, v):
         self._data[...] = v
 
+    @property
+    def dataType(self):
+        return "double"
+
+    def copy(self, deepcopy=False):
+        """A new variable on the same mesh with the same components; with
+        deepcopy the data too (P/mesh/_meshvariable.py:613-660)."""
+        new = MeshVariable(self.mesh, self.nodeDofCount, self.dataType)
+        if deepcopy:
+            new.data[...] = self._data
+        return new
+
+    def syncronise(self):
+        """Shadow-node synchronisation: a single-process mesh has no shadows."""
+        return None
+
     def _primary(self):
         return self.mesh if isinstance(self.mesh, FeMesh_Cartesian) else self.mesh.parent
 

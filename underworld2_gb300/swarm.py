@@ -44,6 +44,14 @@ class SwarmVariable:
         self._dirty = True
         return self._data
 
+    def copy(self, deepcopy=False):
+        """A new variable of the same type and count on the same swarm; with
+        deepcopy the data too (P/swarm/_swarmvariable.py)."""
+        new = self.swarm.add_variable(self.dataType, self.count)
+        if deepcopy:
+            new.data[...] = self._data
+        return new
+
     def _resize(self, n):
         old = self._data
         self._data = np.zeros((n, self.count), dtype=old.dtype)
@@ -199,6 +207,11 @@ class Swarm:
         v = SwarmVariable(self, dataType, count)
         self._variables.append(v)
         return v
+
+    @property
+    def variables(self):
+        """The swarm variables added to this swarm."""
+        return list(self._variables)
 
     # -- checkpointing (P/swarm/_swarm.py:226-420) ----------------------------
     def save(self, filename, collective=False, units=None, **kwargs):

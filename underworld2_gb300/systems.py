@@ -70,6 +70,25 @@ class Stokes:
         self._fn_viscosity = f
 
     @property
+    def fn_one_on_lambda(self):
+        """1/lambda of the compressible formulation, or None (P/systems/_stokes.py:356-372)."""
+        return self._fn_one_on_lambda
+
+    @fn_one_on_lambda.setter
+    def fn_one_on_lambda(self, value):
+        self._fn_one_on_lambda = _fn.Function.convert(value) if value is not None else None
+
+    @property
+    def fn_source(self):
+        """The continuity source term; not part of the GPU PIC Stokes path (always None)."""
+        return None
+
+    @fn_source.setter
+    def fn_source(self, value):
+        if value is not None:
+            raise NotImplementedError("fn_source is not part of the GPU PIC Stokes path")
+
+    @property
     def fn_bodyforce(self):
         return self._fn_bodyforce
 
@@ -652,6 +671,8 @@ class SwarmAdvector:
             raise ValueError("only order=2 (midpoint RK2) is provided")
         self._velocityField = velocityField
         self._swarm = swarm
+        self.dt = 0.0
+        self.time = 0.0
 
     def get_max_dt(self):
         """0.5 * minimum node separation / max |v| (SwarmAdvector_MaxDt)."""
@@ -659,6 +680,7 @@ class SwarmAdvector:
         return ctx.max_dt(self._velocityField._to_device())
 
     def integrate(self, dt, update_owners=True):
+        self.dt = dt     # the integrator's step, as TimeIntegration.integrate records it
         s = self._swarm
         ctx = s.mesh.ctx
         vel = self._velocityField._to_device()
