@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(32 * DVC_WARPS) k_dvc(dvc_args a) {
             if (k == R) k--;
             if (j == R) j--;
             if (DIM == 3 && l == R) l--;
-            hdr[(NM + i) * 2] = k + j * R + l * R * R;   // pool-1 headers are unused until round 1
+            hdr[(NM + i) * 2] = k + j * R + l * R * R;   // pool-1 headers stay unused until the first growth round
         }
         if (__any_sync(0xffffffffu, bad)) {
             if (lane == 0) dvc_fail(a.status, UWG_ERR_STATE, el);

@@ -12,7 +12,7 @@ accumulation in libuwg (``uwg_cnn_*``, hand-written forward and backward); the
 master weights, gradients and Adam moments are FP32.  PyTorch holds the device
 buffers and does the few gradient additions of the skip connections.
 
-The plain path stays the judge: a warm-started solve reports the same FP64
+The plain path decides every result: a warm-started solve reports the same FP64
 residual as any other, and ``solve_with_warm_start`` falls back to the plain
 FP64 solve when the warm-started mixed-precision solve does not reach the
 tolerance.
