@@ -104,16 +104,19 @@ int uwg_dvc_weights(uwg_ctx* ctx, int res, const int32_t* cell_offsets, double* 
 
 /* DVC weights without any device allocation and without a context.
  * No counterpart in the reference: it exists for callers that cannot allocate
- * device memory when they need the weights -- code running while a stream is
- * captured into a CUDA graph (cudaMalloc is not capturable) and host frameworks
- * that own all device memory -- and that therefore cannot create a context.
+ * device memory when they need the weights -- host frameworks that reserve the
+ * GPU's memory in their own pool at start-up and forbid later cudaMalloc calls,
+ * and plugin hosts that hand a plugin device buffers but no allocator -- and
+ * that therefore cannot create a context (creating one allocates).
  * Same inputs and outputs as uwg_dvc_weights (dim 2 or 3, res 1..16, at most
- * 128 particles per element), on `cuda_stream`; synchronises the stream.
+ * 128 particles per element), on `cuda_stream`; reads the status word back
+ * and synchronises the stream before it returns.
  * The boundary-list scratch is a fixed 32 MiB device array inside libuwg that
  * every GPU loading the library holds until exit; the first call on a device
- * looks its address up (cudaGetSymbolAddress) and should come before any
- * stream capture.  All calls share that array: calls that overlap on the GPU
- * (different streams or threads) race and must be serialised by the caller.
+ * looks its address up (cudaGetSymbolAddress) and keeps it, so a device must
+ * not be reset (cudaDeviceReset) between calls.  All calls share that array
+ * and its status word, which each call clears first: calls that overlap on the
+ * GPU (different streams or threads) race and must be serialised by the caller.
  * Returns 0, UWG_ERR_ARG, UWG_ERR_CUDA, UWG_ERR_EMPTY_CELL, UWG_ERR_CELL_FULL or UWG_ERR_STATE
  * (a listed particle's local coordinates lie outside [-1, 1]). */
 int uwg_dvc_weights_noalloc(int dim, int res, int64_t n_el, const int32_t* cell_offsets, double* ip_xi,

@@ -80,7 +80,9 @@ def petsc_matrix(root):
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python make_golden.py <root of the underworld2 source tree>")
+    root = sys.argv[1]
     g = {
         "dvc_suite": dvc_suite(root),
         "isoviscous_K": petsc_matrix(root),

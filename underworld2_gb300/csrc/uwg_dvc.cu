@@ -43,6 +43,12 @@ __host__ __device__ inline size_t dvc_warp_bytes(int RC, int nmax) {
     return (b + 15) & ~(size_t)15;
 }
 
+// Dynamic shared-memory limit set on k_dvc by both entry points: the size of the
+// largest launch either can make (res 16 in 3D, DVC_NMAX slots).  One fixed
+// value means a call on one thread never lowers the limit under a launch of
+// the other entry point on another thread.
+inline int dvc_smem_limit() { return (int)(192 + dvc_warp_bytes(16 * 16 * 16, DVC_NMAX) * DVC_WARPS); }
+
 __device__ __forceinline__ void dvc_fail(int32_t* status, int code, int64_t el) {
     if (atomicCAS(&status[0], 0, code) == 0) status[1] = (int32_t)el;
 }
@@ -332,7 +338,7 @@ extern "C" int uwg_dvc_weights(uwg_ctx* c, int res, const int32_t* cell_offsets,
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     void (*kern)(dvc_args) = dim == 3 ? k_dvc<3> : k_dvc<2>;
-    UWG_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+    UWG_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, dvc_smem_limit()));
     int per_sm = 0;
     UWG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * DVC_WARPS, shm));
     if (per_sm < 1) per_sm = 1;
@@ -376,13 +382,12 @@ extern "C" int uwg_dvc_weights(uwg_ctx* c, int res, const int32_t* cell_offsets,
 // Allocation-free variant of the DVC weights.
 //
 // Some callers cannot allocate device memory at the point where they need
-// the weights: code that runs while a CUDA stream is being captured into a
-// graph (cudaMalloc is not a capturable operation), and host frameworks that
-// hand out all device memory up front and forbid allocations afterwards.
-// They cannot create a uwg context either, because creating one allocates.
-// This entry point needs neither: the per-warp boundary lists live in the
-// fixed device array below, which every GPU that loads libuwg holds until the
-// process exits.
+// the weights: host frameworks that reserve the GPU's memory in their own pool
+// when they start and forbid (or cannot satisfy) any later cudaMalloc, and
+// plugin hosts that give a plugin device buffers but no allocator.  They cannot
+// create a uwg context either, because creating one allocates.  This entry
+// point needs neither: the per-warp boundary lists live in the fixed device
+// array below, which every GPU that loads libuwg holds until the process exits.
 // ---------------------------------------------------------------------------
 #include <mutex>
 
@@ -404,7 +409,9 @@ extern "C" int uwg_dvc_weights_noalloc(int dim, int res, int64_t n_el, const int
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= UWG_NOALLOC_MAX_DEVICES) return UWG_ERR_CUDA;
     unsigned char* base = nullptr;
     {
-        // once per device, with that device current: the device address of the array
+        // once per device, with that device current: the device address of the array.
+        // The cached address belongs to the device's primary context; it does not
+        // survive cudaDeviceReset (the caller must not reset a device between calls).
         std::lock_guard<std::mutex> lock(uwg_noalloc_mutex);
         if (!uwg_noalloc_ptr[dev]) {
             void* p = nullptr;
@@ -428,7 +435,7 @@ extern "C" int uwg_dvc_weights_noalloc(int dim, int res, int64_t n_el, const int
     int64_t max_blocks = max_warps / DVC_WARPS;
     if (max_blocks < 1) return UWG_ERR_ARG;   // grid too fine for the fixed scratch
     void (*kern)(dvc_args) = dim == 3 ? k_dvc<3> : k_dvc<2>;
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm) != cudaSuccess)
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, dvc_smem_limit()) != cudaSuccess)
         return UWG_ERR_CUDA;
     int nsm = 0, per_sm = 0;
     if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return UWG_ERR_CUDA;
