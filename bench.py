@@ -193,7 +193,7 @@ def run_gpu(args):
     u = ctx.zeros(ctx.n_vdof)
     p = ctx.zeros(ctx.n_pdof)
     opts = dict(rtol=1e-8, inner_rtol=args.inner_rtol, outer_rtol=args.outer_rtol, smooth_steps=2, restart=120,
-                schur_pc=args.schur_pc if cfg.get("porder", 0) == 0 else 0, schur_pc_rtol=args.bfbt_rtol, max_outer=args.max_outer)
+                schur_pc=args.schur_pc if cfg.get("porder", 0) == 0 else 0, schur_pc_rtol=args.bfbt_rtol, schur_pc_its=args.bfbt_its, max_outer=args.max_outer)
     ev = lambda: torch.cuda.Event(enable_timing=True)
 
     def solve_step(x, off, lst, eta, body, mixed, times):
@@ -680,7 +680,7 @@ def run_profile_solve(args):
     u, p = ctx.zeros(ctx.n_vdof), ctx.zeros(ctx.n_pdof)
     st = ctx.solve(u, p, mixed=1 if args.mode == "mixed" else 0, rtol=1e-8, inner_rtol=args.inner_rtol,
                    outer_rtol=args.outer_rtol, smooth_steps=2, restart=120, schur_pc=args.schur_pc if cfg.get("porder", 0) == 0 else 0,
-                   schur_pc_rtol=args.bfbt_rtol, max_outer=args.max_outer)
+                   schur_pc_rtol=args.bfbt_rtol, schur_pc_its=args.bfbt_its, max_outer=args.max_outer)
     torch.cuda.synchronize()
     print(json.dumps({"profile_solve": args.config, "particles_per_cell": ppc,
                       "pressure_its": st["pressure_its"], "schur_pc_its": st["schur_pc_its"],
@@ -763,6 +763,7 @@ def main():
     ap.add_argument("--outer-rtol", type=float, default=1e-9)
     ap.add_argument("--schur-pc", type=int, default=1, help="0: Uzawa S^ (reference), 1: scaled BFBt")
     ap.add_argument("--bfbt-rtol", type=float, default=3e-2)
+    ap.add_argument("--bfbt-its", type=int, default=0, help="> 0: fixed CG iterations per BFBt L-solve")
     ap.add_argument("--kernel", choices=["applyK32", "applyK64", "advdiff", "slcn"],
                     help="only launch one operator kernel, or time SUPG / SLCN advection-diffusion steps (profiling)")
     ap.add_argument("--kernel-ppc", type=int, default=0)

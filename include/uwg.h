@@ -154,6 +154,14 @@ int uwg_assemble(uwg_ctx* ctx, int64_t np, const int32_t* cell_offsets, const in
  * uwg_assemble, which rebuilds the right-hand side. */
 int uwg_add_force(uwg_ctx* ctx, const double* df);
 
+/* Adds the continuity source term to the assembled pressure right-hand side:
+ * h_e[b] += sum_q w_q detJ src_q M_b(xi_q) over the PIC points (slot order as
+ * uwg_assemble; src_p per particle).  Replaces the VectorAssemblyTerm_NA__Fn on the
+ * pressure vector (L/Underworld/Utils/src/VectorAssemblyTerm_NA__Fn.cpp:143-202) that
+ * P/systems/_stokes.py:284-288 builds for fn_source.  Call after uwg_assemble. */
+int uwg_add_source(uwg_ctx* ctx, const int32_t* cell_offsets, const int32_t* cell_list, const double* ip_xi,
+                   const double* ip_w, const double* src_p);
+
 /* Element matrices of one element as assembled (host outputs, for checks):
  * Ke_h[(dim*nen)^2], fe_h[dim*nen], Ge_h[dim*nen*npn], Se_h[npn*npn]. */
 int uwg_element_matrices(uwg_ctx* ctx, int64_t el, double* Ke_h, double* fe_h, double* Ge_h,
@@ -178,6 +186,16 @@ typedef struct {
     const double* p_dir;   /* device [n_pdof] or NULL: first search direction of the Schur FGMRES in
                               place of the first preconditioner application (a learned correction;
                               the least-squares step of the iteration chooses its weight) */
+    int null_space;        /* pressure null-space removal (KSPRemovePressureNullspace_BSSCR,
+                              L/Solvers/KSPSolvers/src/BSSCR/ksp_pressure_nullspace.c:28-183):
+                              0 none (the reference's default); 1 the constant
+                              (remove_constant_pressure_null_space); 2 the even-cell and odd-cell
+                              indicator vectors (-remove_checkerboard_pressure_null_space), which
+                              span the constant and the Q1/dQ0 checkerboard.  A vector is removed
+                              only if ||G t||/||t|| < 1e-7 ||G||_inf: from h (and h^) before the
+                              pressure solve and from p after it. */
+    int schur_pc_its;      /* > 0: each pressure-Laplacian solve inside BFBt runs this many CG
+                              iterations (rounded up to even) instead of stopping at schur_pc_rtol */
 } uwg_solve_opts;
 
 typedef struct {
@@ -194,6 +212,8 @@ typedef struct {
     int schur_pc_its;      /* CG iterations of the pressure-Laplacian solves inside BFBt */
     double schur_pc_time;  /* seconds in the Schur preconditioner */
     double schur_op_time;  /* seconds in Schur-operator applications (inner velocity solves) */
+    int schur_pc_used;     /* the Schur preconditioner applied: schur_pc, except that a compressible
+                              system (pressure block C) is preconditioned by the Uzawa term (0) */
 } uwg_solve_stats;
 
 void uwg_solve_opts_default(uwg_solve_opts* o);

@@ -65,6 +65,7 @@ def lib():
             "uwo_element_G": (None, [M, _P, _P, _P, ctypes.c_int, _I64, ctypes.c_int, _P, _P, _P]),
             "uwo_element_f": (None, [M, _P, _P, _P, _I64, ctypes.c_int, _P, _P, _P, _P]),
             "uwo_element_M": (None, [M, _P, _P, _P, ctypes.c_int, _I64, ctypes.c_int, _P, _P, _P, _P]),
+            "uwo_element_h": (None, [M, _P, _P, _P, ctypes.c_int, _I64, ctypes.c_int, _P, _P, _P, _P]),
             "uwo_element_S": (None, [ctypes.c_int, ctypes.c_int, _P, _P, _P]),
             "uwo_shape": (None, [ctypes.c_int, ctypes.c_int, _P, _P, _P]),
             "uwo_pressure_shape": (None, [ctypes.c_int, ctypes.c_int, _P, _P]),
@@ -218,6 +219,14 @@ class Mesh:
                              _p(np.ascontiguousarray(w, np.float64)),
                              _p(np.ascontiguousarray(Fq, np.float64)), _p(Me))
         return Me
+
+    def element_h(self, el, xi, w, Fq):
+        he = np.zeros(self.npn)
+        self.L.uwo_element_h(ctypes.byref(self._c), *self._ax(), self.porder, int(el), len(w),
+                             _p(np.ascontiguousarray(xi, np.float64)),
+                             _p(np.ascontiguousarray(w, np.float64)),
+                             _p(np.ascontiguousarray(Fq, np.float64)), _p(he))
+        return he
 
     def element_S(self, Ke, Ge):
         Se = np.zeros((self.npn, self.npn))

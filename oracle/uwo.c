@@ -766,6 +766,27 @@ void uwo_element_M(const uwo_mesh* m, const double* ax0, const double* ax1, cons
     }
 }
 
+/* h_e[B] = sum_q w detJ F N_B over the pressure basis: the continuity source term
+ * (VectorAssemblyTerm_NA__Fn on the pressure vector,
+ * L/Underworld/Utils/src/VectorAssemblyTerm_NA__Fn.cpp:143-202; detJ from the velocity
+ * geometry; added for fn_source at P/systems/_stokes.py:284-288). */
+void uwo_element_h(const uwo_mesh* m, const double* ax0, const double* ax1, const double* ax2,
+                   int porder, int64_t el, int nq, const double* xi, const double* wt, const double* Fq,
+                   double* he) {
+    const double* ax[3] = {ax0, ax1, ax2};
+    int64_t nodes[27];
+    double N[27], GNx[3][27], M[4];
+    int dim = m->dim, npn = uwo_pressure_nodes(dim, porder);
+    uwo_element_nodes(m, el, nodes);
+    memset(he, 0, sizeof(double) * npn);
+    for (int q = 0; q < nq; q++) {
+        double detJ = global_derivs(m, ax, nodes, xi + q * dim, N, GNx);
+        uwo_pressure_shape(dim, porder, xi + q * dim, M);
+        double factor = detJ * wt[q];
+        for (int b = 0; b < npn; b++) he[b] += factor * Fq[q] * M[b];
+    }
+}
+
 /* S_e = G_e^T diag(K_e)^-1 G_e
  * (L/StgFEM/SLE/ProvidedSystems/StokesFlow/src/UzawaPreconditionerTerm.c:124-207). */
 void uwo_element_S(int nv, int npn, const double* Ke, const double* Ge, double* Se) {

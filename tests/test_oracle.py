@@ -134,3 +134,22 @@ def test_cpu_solver_matches_direct(dim, res):
     free = mask == 0
     y = cpu.applyK(v)
     assert np.abs(y[free] - (sysd["K"] @ v)[free]).max() <= 1e-12 * np.abs(y).max()
+
+
+@pytest.mark.parametrize("dim,res,expect", [(2, (6, 6), 2), (2, (5, 4), 2), (3, (4, 4, 4), 11), (3, (6, 6, 6), 17)])
+def test_q1dq0_pressure_null_space_of_closed_box(dim, res, expect):
+    """With velocity fixed on every wall, the gradient of a Q1/dQ0 mesh loses
+    rank: in 2D the constant and the checkerboard (the two vectors the
+    reference's -remove_checkerboard_pressure_null_space removes); in 3D many
+    more (3N-1 on an N^3 mesh; planar checkerboards among them), which that
+    removal cannot cover."""
+    m = oracle.Mesh(dim, 1, res, (0.0,) * dim, (1.0,) * dim)
+    gxi, gw = m.gauss_points()
+    G = np.zeros((m.n_nodes * dim, m.n_el))
+    for e in range(m.n_el):
+        dofs = (m.element_nodes(e)[:, None] * dim + np.arange(dim)).ravel()
+        G[dofs, e] += m.element_G(e, gxi, gw)[:, 0]
+    nodes = m.node_coords()
+    free = np.repeat(~np.any(np.isclose(nodes, 0.0) | np.isclose(nodes, 1.0), axis=1), dim)
+    s = np.linalg.svd(G[free], compute_uv=False)
+    assert int(np.sum(s < 1e-10 * s.max())) == expect

@@ -150,6 +150,10 @@ class Context:
         """f += df at free dofs (traction surface term; after assemble)."""
         self._call("uwg_add_force", _ptr(df.contiguous()))
 
+    def add_source(self, off, lst, ip_xi, ip_w, src):
+        """h += the continuity source term from per-particle values (after assemble)."""
+        self._call("uwg_add_source", _ptr(off), _ptr(lst), _ptr(ip_xi), _ptr(ip_w), _ptr(src.contiguous()))
+
     def element_matrices(self, el):
         nd = self.dim * self.nen
         Ke = np.zeros((nd, nd))

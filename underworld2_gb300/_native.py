@@ -35,7 +35,8 @@ class SolveOpts(ctypes.Structure):
                 ("outer_rtol", ctypes.c_double), ("max_inner", ctypes.c_int), ("max_outer", ctypes.c_int),
                 ("mg_levels", ctypes.c_int), ("smooth_steps", ctypes.c_int), ("restart", ctypes.c_int),
                 ("zero_guess", ctypes.c_int), ("schur_pc", ctypes.c_int), ("schur_pc_rtol", ctypes.c_double),
-                ("relax_inner", ctypes.c_int), ("schur_pc_smooth", ctypes.c_int), ("p_dir", ctypes.c_void_p)]
+                ("relax_inner", ctypes.c_int), ("schur_pc_smooth", ctypes.c_int), ("p_dir", ctypes.c_void_p),
+                ("null_space", ctypes.c_int), ("schur_pc_its", ctypes.c_int)]
 
 
 class SolveStats(ctypes.Structure):
@@ -48,7 +49,8 @@ class SolveStats(ctypes.Structure):
                 ("vmin", ctypes.c_double), ("vmax", ctypes.c_double), ("pmin", ctypes.c_double),
                 ("pmax", ctypes.c_double), ("fhat_reason", ctypes.c_int), ("outer_reason", ctypes.c_int),
                 ("backsolve_reason", ctypes.c_int), ("schur_pc_its", ctypes.c_int),
-                ("schur_pc_time", ctypes.c_double), ("schur_op_time", ctypes.c_double)]
+                ("schur_pc_time", ctypes.c_double), ("schur_op_time", ctypes.c_double),
+                ("schur_pc_used", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -78,6 +80,7 @@ SIGNATURES = {
     "uwg_assemble": (_I, [_CTX, _I64, _P, _P, _P, _P, _P, _P, _P]),
     "uwg_element_matrices": (_I, [_CTX, _I64, _P, _P, _P, _P]),
     "uwg_add_force": (_I, [_CTX, _P]),
+    "uwg_add_source": (_I, [_CTX, _P, _P, _P, _P, _P]),
     "uwg_solve_opts_default": (None, [ctypes.POINTER(SolveOpts)]),
     "uwg_stokes_solve": (_I, [_CTX, ctypes.POINTER(SolveOpts), _P, _P, ctypes.POINTER(SolveStats)]),
     "uwg_stokes_residuals": (_I, [_CTX, _P, _P, _P]),

@@ -242,6 +242,7 @@ extern "C" int uwg_assemble(uwg_ctx* c, int64_t np, const int32_t* off, const in
     int rc = uwg_ops_assemble(c, off, list, ip_xi, ip_w, eta_p, body_p, lambda_p);
     if (rc) return rc;
     if (!lambda_p) UWG_CUDA(c, cudaMemsetAsync(c->Mp, 0, sizeof(double) * c->n_pdof, c->stream));
+    c->compressible = lambda_p != nullptr;
     UWG_CUDA(c, cudaMemsetAsync(c->h, 0, sizeof(double) * c->n_pdof, c->stream));
     // Dirichlet lifting: f -= K_fb g, h -= G_b^T g  (StiffnessMatrix.c:627-678)
     k_keep_bc<<<(unsigned)((c->n_vdof + 255) / 256), 256, 0, c->stream>>>(c->n_vdof, c->bc, c->bcval);
@@ -266,6 +267,60 @@ extern "C" int uwg_add_force(uwg_ctx* c, const double* df) {
     if (!c || !df) return uwg_set_error(c, UWG_ERR_ARG, "uwg_add_force: bad argument");
     if (!c->assembled) return uwg_set_error(c, UWG_ERR_STATE, "uwg_add_force before uwg_assemble");
     k_add_free<<<(unsigned)((c->n_vdof + 255) / 256), 256, 0, c->stream>>>(c->n_vdof, c->bc, df, c->f);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
+// Continuity source term h_e[b] += sum_q w_q detJ src_q M_b(xi_q) over the PIC
+// points of each element: VectorAssemblyTerm_NA__Fn on the pressure variable
+// (L/Underworld/Utils/src/VectorAssemblyTerm_NA__Fn.cpp:143-202; N = the pressure
+// basis, detJ from the velocity geometry), as P/systems/_stokes.py:284-288 adds
+// it for fn_source.  One thread per element; elements are affine, so detJ is
+// the product of the half-extents.  dPc1 bases: BilinearInnerElType.c:169-179,
+// TrilinearInnerElType.c:202-216 (the same expressions, term for term).
+template <int DIM>
+__global__ void k_add_source(int64_t n_el, int order, int npn, int rx, int ry, const double* ax0, const double* ax1,
+                             const double* ax2, const int32_t* off, const int32_t* list, const double* ip_xi,
+                             const double* ip_w, const double* src_p, double* h) {
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= n_el) return;
+    int64_t ie[3] = {e % rx, (e / rx) % ry, DIM == 3 ? e / ((int64_t)rx * ry) : 0};
+    const double* ax[3] = {ax0, ax1, ax2};
+    double detJ = 1.0;
+    for (int d = 0; d < DIM; d++) detJ *= 0.5 * (ax[d][order * ie[d] + order] - ax[d][order * ie[d]]);
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int32_t s = off[e]; s < off[e + 1]; s++) {
+        double fac = detJ * ip_w[s] * src_p[list[s]];
+        const double* xi = ip_xi + (int64_t)s * DIM;
+        if (npn == 1) {
+            acc[0] += fac;
+        } else if (DIM == 2) {
+            double x = xi[0], y = xi[1];
+            acc[0] += fac * (-x - 0.5 * y + 0.25);
+            acc[1] += fac * (x - 0.5 * y + 0.25);
+            acc[2] += fac * (y + 0.5);
+        } else {
+            double x = xi[0], y = xi[1], z = xi[DIM - 1], k = 1.0 / 9.0;
+            acc[0] += fac * (k * (-4.0 * x - 20.0 * y + 12.0 * z + 3.0));
+            acc[1] += fac * (k * (16.0 * x - 64.0 * y + 60.0 * z + 6.0));
+            acc[2] += fac * (k * (36.0 * y - 36.0 * z));
+            acc[3] += fac * (k * (-12.0 * x + 48.0 * y - 36.0 * z));
+        }
+    }
+    for (int b = 0; b < npn; b++) h[e * npn + b] += acc[b];
+}
+
+extern "C" int uwg_add_source(uwg_ctx* c, const int32_t* off, const int32_t* list, const double* ip_xi,
+                              const double* ip_w, const double* src_p) {
+    if (!c || !off || !list || !ip_xi || !ip_w || !src_p) return uwg_set_error(c, UWG_ERR_ARG, "uwg_add_source: bad argument");
+    if (!c->assembled) return uwg_set_error(c, UWG_ERR_STATE, "uwg_add_source before uwg_assemble");
+    unsigned nb = (unsigned)((c->n_el + 127) / 128);
+    if (c->dim == 3)
+        k_add_source<3><<<nb, 128, 0, c->stream>>>(c->n_el, c->order, c->npn, c->res[0], c->res[1], c->ax[0], c->ax[1],
+                                                   c->ax[2], off, list, ip_xi, ip_w, src_p, c->h);
+    else
+        k_add_source<2><<<nb, 128, 0, c->stream>>>(c->n_el, c->order, c->npn, c->res[0], c->res[1], c->ax[0], c->ax[1],
+                                                   c->ax[0], off, list, ip_xi, ip_w, src_p, c->h);
     UWG_CUDA(c, cudaGetLastError());
     return UWG_OK;
 }

@@ -58,6 +58,7 @@ struct uwg_ctx {
     uint8_t* bc;            // finest BC mask (alias of lev[0].bc)
     double* bcval;          // Dirichlet values [n_vdof]
     bool assembled;
+    bool compressible;      // the last assembly had a pressure block C (fn_one_on_lambda)
 
     // scratch
     void* red;              // reduction scratch (double[4096])

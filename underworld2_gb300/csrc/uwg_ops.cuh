@@ -88,7 +88,7 @@ int uwg_pmg_apply0_mf(uwg_ctx* c, const float* W0, const float* x, float* y);   
 int uwg_pmg_diag(uwg_ctx* c, int l, const float* st, float* d);
 int uwg_pmg_restrict(uwg_ctx* c, int lc, const float* rf, float* rc);
 int uwg_pmg_prolong_add(uwg_ctx* c, int lc, const float* xc, float* xf);
-int uwg_pmg_dense_inverse(uwg_ctx* c, int l, const float* st, float* inv32);
+int uwg_pmg_dense_inverse(uwg_ctx* c, int l, const float* st, int fix_checkerboard, float* inv32);
 
 // Vector kernels ---------------------------------------------------------------
 template <typename T> void vk_copy(cudaStream_t s, int64_t n, const T* x, T* y);

@@ -277,18 +277,26 @@ __global__ void k_pdense(uwg_lgeom g, const float* __restrict__ st, double* __re
     }
 }
 
-__global__ void k_pdense_fix(int64_t m, int64_t n, double* A) {
+// Rank-one terms tau 1 1^T on the smooth block (and, when the checkerboard is a
+// null mode of G as well, on the checkerboard block) make the singular coarse
+// operator invertible without changing its action on the range.
+__global__ void k_pdense_fix(int64_t m, int64_t n, int fix_checkerboard, double* A) {
     __shared__ double red[1024];
-    double mx = 0.0;
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) mx = fmax(mx, A[i * m + i]);
-    red[threadIdx.x] = mx;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if ((int)threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+    for (int blk = 0; blk < (fix_checkerboard && m == 2 * n ? 2 : 1); blk++) {
+        double* B = A + (int64_t)blk * n * m + (int64_t)blk * n;   // diagonal block blk
+        double mx = 0.0;
+        for (int64_t i = threadIdx.x; i < n; i += blockDim.x) mx = fmax(mx, B[i * m + i]);
+        red[threadIdx.x] = mx;
+        __syncthreads();
+        for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+            if ((int)threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+            __syncthreads();
+        }
+        const double tau = (red[0] > 0.0 ? red[0] : 1.0) / (double)n;
+        __syncthreads();
+        for (int64_t k = threadIdx.x; k < n * n; k += blockDim.x) B[(k / n) * m + (k % n)] += tau;
         __syncthreads();
     }
-    const double tau = (red[0] > 0.0 ? red[0] : 1.0) / (double)n;
-    for (int64_t k = threadIdx.x; k < n * n; k += blockDim.x) A[(k / n) * m + (k % n)] += tau;
 }
 
 
@@ -759,7 +767,7 @@ int uwg_pmg_prolong_add(uwg_ctx* c, int lc, const float* xc, float* xf) {
     return UWG_OK;
 }
 
-int uwg_pmg_dense_inverse(uwg_ctx* c, int l, const float* st, float* inv32) {
+int uwg_pmg_dense_inverse(uwg_ctx* c, int l, const float* st, int fix_checkerboard, float* inv32) {
     uwg_lgeom g = uwg_level_geom(c, l);
     int nc = uwg_pmg_ncomp(l);
     int64_t n = g.n_el, m = nc * n;
@@ -769,7 +777,7 @@ int uwg_pmg_dense_inverse(uwg_ctx* c, int l, const float* st, float* inv32) {
     UWG_CUDA(c, cudaMallocAsync((void**)&B, sizeof(double) * m * m, c->stream));
     UWG_CUDA(c, cudaMemsetAsync(A, 0, sizeof(double) * m * m, c->stream));
     PMG_DIM_NC(k_pdense, nc, nblk(n, 64), g, st, A);
-    k_pdense_fix<<<1, 1024, 0, c->stream>>>(m, n, A);
+    k_pdense_fix<<<1, 1024, 0, c->stream>>>(m, n, fix_checkerboard, A);
     int rc = uwg_ops_dense_invert(c, m, A, B);
     if (!rc) rc = uwg_ops_to_f32(c, m * m, B, inv32);
     cudaFreeAsync(A, c->stream);

@@ -66,6 +66,10 @@ struct Work {
     double* lcg_h = nullptr;                  // pinned host mirror of lcg_s
     int g_deg = 0;
     int pdeg = 2, g_pdeg = 0;                  // pressure smoother degree (in use / captured)
+    // pressure null space: even-cell / odd-cell indicator vectors, the constant, and
+    // whether the checkerboard lies in the null space of G (every velocity dof on the walls fixed)
+    double *ns_t = nullptr, *ns_v = nullptr, *ns_one = nullptr, *ns_tmp = nullptr;
+    bool cb_null = false;
 };
 
 Work* work_of(uwg_ctx* c) {
@@ -118,6 +122,8 @@ int work_init(uwg_ctx* c, int restart) {
         w->bf_r = dalloc<float>(c, np); w->bf_y = dalloc<float>(c, np);
         w->bf_m = dalloc<float>(c, np); w->bf_z = dalloc<float>(c, np);
         w->bf_v1 = dalloc<float>(c, nv); w->bf_v2 = dalloc<float>(c, nv);
+        w->ns_t = dalloc<double>(c, np); w->ns_v = dalloc<double>(c, np); w->ns_one = dalloc<double>(c, np);
+        w->ns_tmp = dalloc<double>(c, np);
     }
     while ((int)w->V.size() < restart + 1) w->V.push_back(dalloc<double>(c, np));
     while ((int)w->Z.size() < restart) w->Z.push_back(dalloc<double>(c, np));
@@ -270,9 +276,10 @@ struct SolveCfg {
     int schur_pc;
     double schur_pc_rtol;
     bool relax;
+    int schur_pc_its;   // > 0: fixed CG iterations per pressure-Laplacian solve (rtol ignored)
 };
 
-int bfbt(uwg_ctx* c, const double* r, double* z, double rtol);
+int bfbt(uwg_ctx* c, const double* r, double* z, double rtol, int its);
 
 // x = A^-1 b for the velocity operator A = PKP + (I-P), FP64 result.
 // x holds the initial guess unless x_zero.  Returns iterations through *its.
@@ -508,6 +515,7 @@ int lsolve(uwg_ctx* c, const float* b, float* x, double rtol, int maxit) {
         for (int it = 0; it < maxit; it += 2) {
             UWG_CUDA(c, cudaGraphLaunch(w->g_lcg, s));
             w->lsolve_its += 2;
+            if (!(rtol > 0.0)) continue;   // fixed iterations: no host round trip (breakdowns stop on the device)
             UWG_CUDA(c, cudaMemcpyAsync(w->lcg_h, w->lcg_s, sizeof(double) * 16, cudaMemcpyDeviceToHost, s));
             UWG_CUDA(c, cudaStreamSynchronize(s));
             if (w->lcg_h[9] != 0.0 || !(std::sqrt(w->lcg_h[5]) > rtol * bn)) break;
@@ -517,21 +525,126 @@ int lsolve(uwg_ctx* c, const float* b, float* x, double rtol, int maxit) {
     return UWG_OK;   // a preconditioner: an inexact solve is acceptable
 }
 
+// ---------------------------------------------------------------------------
+// Pressure null space (KSPBuildPressure_{Const,CB}_Nullspace_BSSCR and
+// KSPRemovePressureNullspace_BSSCR, L/Solvers/KSPSolvers/src/BSSCR/
+// ksp_pressure_nullspace.c:28-183).  Mode 1 is the constant vector; mode 2 is
+// the pair of indicator vectors of the even cells (i+j+k even) and the odd
+// cells, whose span holds both the constant and the checkerboard.  A vector
+// is removed only when it lies in the null space of G:
+// ||G t|| / ||t|| < nstol ||G||_inf with nstol = 1e-7 (BSSCR.c:428).
+// ---------------------------------------------------------------------------
+__global__ void k_ns_fill(int64_t n_el, int npn, int rx, int ry, double* t, double* v, double* one) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n_el * npn) return;
+    int64_t e = i / npn;
+    int64_t ex = e % rx, ey = (e / rx) % ry, ez = e / ((int64_t)rx * ry);
+    bool even = ((ex + ey + ez) & 1) == 0;
+    t[i] = even ? 1.0 : 0.0;
+    v[i] = even ? 0.0 : 1.0;
+    one[i] = 1.0;   // all pressure coefficients 1 is p = 1 for dQ0 and for dPc1 (its basis sums to 1)
+}
+
+int ns_fill(uwg_ctx* c) {
+    Work* w = work_of(c);
+    int64_t n = c->n_el * c->npn;
+    k_ns_fill<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->n_el, c->npn, c->res[0], c->res[1], w->ns_t,
+                                                                   w->ns_v, w->ns_one);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
+// ||G||_inf, the largest absolute row sum of the assembled gradient (MatNorm(G,
+// NORM_INFINITY) at auglag-driver-DGTGD.c:410).  Q1/dQ0: an interior velocity row
+// of component i couples to 2^dim cells with entries prod_{d != i} h_d / 2 (the
+// closed form of k_gradG_nodes).  Q2/dPc1: estimated as ||G z|| / ||z|| for a
+// fixed z, which is only used in the two threshold tests below.
+int g_norm_inf(uwg_ctx* c, double* out) {
+    Work* w = work_of(c);
+    cudaStream_t s = c->stream;
+    int rc;
+    if (c->order == 1) {
+        double hmax[3] = {1.0, 1.0, 1.0};
+        for (int d = 0; d < c->dim; d++) {
+            std::vector<double> ax(c->res[d] + 1);
+            UWG_CUDA(c, cudaMemcpyAsync(ax.data(), c->ax[d], sizeof(double) * ax.size(), cudaMemcpyDeviceToHost, s));
+            UWG_CUDA(c, cudaStreamSynchronize(s));
+            hmax[d] = 0.0;
+            for (int i = 0; i < c->res[d]; i++) hmax[d] = std::max(hmax[d], ax[i + 1] - ax[i]);
+        }
+        double best = 0.0;
+        for (int i = 0; i < c->dim; i++) {
+            double g = (double)(1 << c->dim);
+            for (int d = 0; d < c->dim; d++)
+                if (d != i) g *= 0.5 * hmax[d];
+            best = std::max(best, g);
+        }
+        *out = best;
+        return UWG_OK;
+    }
+    int64_t np = c->n_pdof;
+    std::vector<double> z(np);
+    for (int64_t i = 0; i < np; i++) z[i] = std::sin(1.37 * (double)i) + ((i & 1) ? 0.3 : -0.3);
+    UWG_CUDA(c, cudaMemcpyAsync(w->ns_tmp, z.data(), sizeof(double) * np, cudaMemcpyHostToDevice, s));
+    if ((rc = uwg_ops_applyG(c, w->ns_tmp, w->u_tmp))) return rc;
+    double d[2];
+    const double* a1[1] = {w->u_tmp};
+    if ((rc = dots<double>(c, c->n_vdof, 1, a1, a1, d))) return rc;
+    const double* a2[1] = {w->ns_tmp};
+    if ((rc = dots<double>(c, np, 1, a2, a2, d + 1))) return rc;   // synchronises: z outlives its copy
+    *out = d[1] > 0.0 ? std::sqrt(d[0] / d[1]) : 1.0;
+    return UWG_OK;
+}
+
+// Does t lie in the null space of G (free rows)?
+int ns_test(uwg_ctx* c, const double* t, double gnorm, bool* in_ns) {
+    Work* w = work_of(c);
+    int rc;
+    if ((rc = uwg_ops_applyG(c, t, w->u_tmp))) return rc;   // Dirichlet rows are zero
+    double d[2];
+    const double* a1[1] = {w->u_tmp};
+    if ((rc = dots<double>(c, c->n_vdof, 1, a1, a1, d))) return rc;
+    const double* a2[1] = {t};
+    if ((rc = dots<double>(c, c->n_pdof, 1, a2, a2, d + 1))) return rc;
+    *in_ns = d[1] > 0.0 && std::sqrt(d[0] / d[1]) < 1e-7 * gnorm;
+    return UWG_OK;
+}
+
+// x -= (t.x / t.t) t
+int ns_project(uwg_ctx* c, const double* t, double* x) {
+    double d[2];
+    const double* a[2] = {t, t};
+    const double* b[2] = {x, t};
+    int rc = dots<double>(c, c->n_pdof, 2, a, b, d);
+    if (rc) return rc;
+    if (d[1] > 0.0) vk_axpy<double>(c->stream, c->n_pdof, -d[0] / d[1], t, x);
+    return UWG_OK;
+}
+
 // z = -BFBt(r): the sign makes it approximate the inverse of C - G^T K^-1 G
-int bfbt(uwg_ctx* c, const double* r, double* z, double rtol) {
+int bfbt(uwg_ctx* c, const double* r, double* z, double rtol, int its) {
     Work* w = work_of(c);
     cudaStream_t s = c->stream;
     int64_t np = c->n_pdof, nv = c->n_vdof;
     int rc;
+    if (w->cb_null) {
+        // both null modes out of the input, so that the L-solves see consistent right-hand sides
+        vk_copy<double>(s, np, r, w->ns_tmp);
+        if ((rc = ns_project(c, w->ns_t, w->ns_tmp)) || (rc = ns_project(c, w->ns_v, w->ns_tmp))) return rc;
+        r = w->ns_tmp;
+    }
+    const int maxit = its > 0 ? its : 200;
+    if (its > 0) rtol = 0.0;   // a fixed number of iterations: flexible GMRES accepts the varying operator
     vk_convert<double, float>(s, np, r, w->bf_r);
-    if ((rc = lsolve(c, w->bf_r, w->bf_y, rtol, 200))) return rc;
+    if ((rc = lsolve(c, w->bf_r, w->bf_y, rtol, maxit))) return rc;
     if ((rc = uwg_ops_G32(c, 0, w->W0, w->bf_y, w->bf_v1))) return rc;             // W G y
     if ((rc = uwg_ops_applyK<float>(c, 0, w->bf_v1, w->bf_v2))) return rc;         // K W G y
     vk_pointwise_mul_mask(s, nv, w->W0, w->bf_v2);                                  // W K W G y
     if ((rc = uwg_ops_Gt32(c, 0, w->bf_v2, w->bf_m))) return rc;
-    if ((rc = lsolve(c, w->bf_m, w->bf_z, rtol, 200))) return rc;
+    if ((rc = lsolve(c, w->bf_m, w->bf_z, rtol, maxit))) return rc;
     vk_convert<float, double>(s, np, w->bf_z, z);
     vk_scale<double>(s, np, -1.0, z);
+    if (w->cb_null && ((rc = ns_project(c, w->ns_t, z)) || (rc = ns_project(c, w->ns_v, z)))) return rc;
     return UWG_OK;
 }
 
@@ -565,7 +678,7 @@ int bfbt_setup(uwg_ctx* c) {
         UWG_CUDA(c, cudaStreamSynchronize(s));   // the host vector must outlive its copy
         w->Lmax[l] = lam;
     }
-    return uwg_pmg_dense_inverse(c, c->nlev - 1, w->pst[c->nlev - 1], w->pcinv);
+    return uwg_pmg_dense_inverse(c, c->nlev - 1, w->pst[c->nlev - 1], w->cb_null ? 1 : 0, w->pcinv);
 }
 }  // namespace
 
@@ -626,6 +739,19 @@ int uwg_solver_setup(uwg_ctx* c) {
         if (l < c->nlev - 1 && (rc = uwg_solver_estimate(c, l))) return rc;
     }
     if ((rc = uwg_ops_dense_coarse(c, c->nlev - 1))) return rc;
+    // null-space vectors, and whether the checkerboard is a null mode of G (the
+    // BFBt pressure multigrid then needs a second rank-one term on its coarsest level)
+    {
+        Work* w = work_of(c);
+        if ((rc = ns_fill(c))) return rc;
+        double gn = 1.0;
+        if ((rc = g_norm_inf(c, &gn))) return rc;
+        vk_copy<double>(c->stream, c->n_pdof, w->ns_t, w->ns_tmp);
+        vk_axpy<double>(c->stream, c->n_pdof, -1.0, w->ns_v, w->ns_tmp);
+        bool cb = false;
+        if (c->porder == 0 && (rc = ns_test(c, w->ns_tmp, gn, &cb))) return rc;
+        w->cb_null = cb;
+    }
     if (c->porder == 0 && (rc = bfbt_setup(c))) return rc;
     return capture_cycles(c, work_of(c)->g_deg > 0 ? work_of(c)->g_deg : 3);
 }
@@ -647,6 +773,8 @@ extern "C" void uwg_solve_opts_default(uwg_solve_opts* o) {
     o->schur_pc = 1;
     o->schur_pc_rtol = 3e-2;
     o->p_dir = nullptr;
+    o->null_space = 0;
+    o->schur_pc_its = 0;
 }
 
 namespace {
@@ -708,7 +836,7 @@ int fgmres(uwg_ctx* c, const SolveCfg& cfg, const double* rhs, double* p, double
                 // a given first direction (the learned correction) in place of M^-1 V_0
                 vk_copy<double>(s, n, z0, w->Z[j]);
             } else if (cfg.schur_pc == 1) {
-                if ((rc = bfbt(c, w->V[j], w->Z[j], cfg.schur_pc_rtol))) return rc;
+                if ((rc = bfbt(c, w->V[j], w->Z[j], cfg.schur_pc_rtol, cfg.schur_pc_its))) return rc;
                 cudaStreamSynchronize(s);
                 w->t_pc += now() - tp0;
             } else {
@@ -854,8 +982,12 @@ extern "C" int uwg_stokes_solve(uwg_ctx* c, const uwg_solve_opts* o, double* u, 
     if (std::max(1, o->smooth_steps) != w->g_deg && (rc = capture_cycles(c, std::max(1, o->smooth_steps))))
         return rc;
     int64_t nv = c->n_vdof, np = c->n_pdof;
-    SolveCfg cfg{o->mixed != 0, o->inner_rtol, o->max_inner, std::max(1, o->smooth_steps), o->schur_pc,
-                 o->schur_pc_rtol > 0.0 ? o->schur_pc_rtol : 1e-2, o->relax_inner != 0};
+    // Scaled BFBt approximates (G^T K^-1 G)^-1 only: with a compressible block C the
+    // Schur complement C - G^T K^-1 G is preconditioned by the Uzawa term S^ (which holds -C).
+    const int schur_pc = (o->schur_pc == 1 && c->compressible) ? 0 : o->schur_pc;
+    SolveCfg cfg{o->mixed != 0, o->inner_rtol, o->max_inner, std::max(1, o->smooth_steps), schur_pc,
+                 o->schur_pc_rtol > 0.0 ? o->schur_pc_rtol : 1e-2, o->relax_inner != 0, o->schur_pc_its};
+    if (o->schur_pc_its < 0 || o->schur_pc_its > 200) return uwg_set_error(c, UWG_ERR_ARG, "schur_pc_its must be in [0, 200]");
     // b = f with Dirichlet values in BC rows
     vk_copy<double>(s, nv, c->f, w->bvec);
     {
@@ -876,9 +1008,30 @@ extern "C" int uwg_stokes_solve(uwg_ctx* c, const uwg_solve_opts* o, double* u, 
     vk_mask<double>(s, nv, c->bc, w->ftil);
     double t2 = now();
     S.presolve_time = t2 - t1;
+    // null-space vectors requested by the caller that lie in the null space of G
+    // (KSPBuildPressure_*_Nullspace_BSSCR + the test of KSPRemovePressureNullspace_BSSCR)
+    const double* nsv[2];
+    int n_ns = 0;
+    double gnorm = 1.0;
+    if ((rc = g_norm_inf(c, &gnorm))) return rc;
+    if (o->null_space < 0 || o->null_space > 2) return uwg_set_error(c, UWG_ERR_ARG, "null_space must be 0, 1 or 2");
+    if (o->null_space) {
+        const double* cand[2] = {o->null_space == 1 ? w->ns_one : w->ns_t, o->null_space == 1 ? nullptr : w->ns_v};
+        for (int k = 0; k < 2; k++) {
+            bool in_ns = false;
+            if (cand[k] && (rc = ns_test(c, cand[k], gnorm, &in_ns))) return rc;
+            if (in_ns) nsv[n_ns++] = cand[k];
+        }
+        // The components of h along them make the system inconsistent; they are
+        // dropped from h itself, so that the reported residual is the consistent system's.
+        for (int k = 0; k < n_ns; k++)
+            if ((rc = ns_project(c, nsv[k], c->h))) return rc;
+    }
     // 2. h^ = h - G^T f~
     if ((rc = uwg_ops_applyGt(c, w->ftil, w->hhat))) return rc;
     vk_axpby<double>(s, np, 1.0, c->h, -1.0, w->hhat);
+    for (int k = 0; k < n_ns; k++)
+        if ((rc = ns_project(c, nsv[k], w->hhat))) return rc;
     // 3. pressure solve: S p = h^, S = C - G^T A^-1 G
     w->lsolve_its = 0;
     w->t_pc = w->t_schur = 0.0;
@@ -895,10 +1048,28 @@ extern "C" int uwg_stokes_solve(uwg_ctx* c, const uwg_solve_opts* o, double* u, 
         if ((rc = dots<double>(c, np, 1, a2, a2, &fh2[1]))) return rc;
     }
     double atol = o->rtol > 0.0 ? 0.5 * o->rtol * std::sqrt(fh2[0] + fh2[1]) : 0.0;
+    // h^ scaling (auglag-driver-DGTGD.c:410-417): a small ||h^|| / ||G||_inf in
+    // (1e-20, 1e-6) is scaled to one for the pressure solve and p scaled back after.
+    double hscale = 1.0;
+    {
+        double hn;
+        const double* ah[1] = {w->hhat};
+        if ((rc = dots<double>(c, np, 1, ah, ah, &hn))) return rc;
+        hn = std::sqrt(hn) / gnorm;
+        if (hn < 1e-6 && hn > 1e-20) hscale = 1.0 / hn;
+    }
+    if (hscale != 1.0) {
+        vk_scale<double>(s, np, hscale, w->hhat);
+        if (o->zero_guess == 0) vk_scale<double>(s, np, hscale, p);
+        atol *= hscale;
+    }
     rc = fgmres(c, cfg, w->hhat, p, o->outer_rtol, atol, o->max_outer, std::max(2, o->restart), &outer, &inner_its,
                 &S.refinement_steps, o->zero_guess == 0, o->p_dir);
+    if (hscale != 1.0) vk_scale<double>(s, np, 1.0 / hscale, p);
+    for (int k = 0; !rc && k < n_ns; k++) rc = ns_project(c, nsv[k], p);
     S.pressure_its = outer;
     S.schur_pc_its = w->lsolve_its;
+    S.schur_pc_used = schur_pc;
     S.schur_pc_time = w->t_pc;
     S.schur_op_time = w->t_schur;
     S.velocity_pressuresolve_its = inner_its;

@@ -30,7 +30,7 @@ class Stokes:
         if pressureField.nodeDofCount != 1:
             raise ValueError("Provided 'pressureField' must be a scalar field (ie pressureField.nodeDofCount==1).")
         for name, v in (("_fn_viscosity2", _fn_viscosity2), ("_fn_director", _fn_director),
-                        ("fn_stresshistory", fn_stresshistory), ("fn_source", fn_source)):
+                        ("fn_stresshistory", fn_stresshistory)):
             if v is not None:
                 raise NotImplementedError("%s is not part of the GPU PIC Stokes path" % name)
         if voronoi_swarm is not None and not isinstance(voronoi_swarm, _swarm.Swarm):
@@ -43,6 +43,12 @@ class Stokes:
             fn_bodyforce = (0.0,) * self.mesh.dim
         self.fn_bodyforce = fn_bodyforce
         self._fn_one_on_lambda = _fn.Function.convert(fn_one_on_lambda) if fn_one_on_lambda is not None else None
+        self._fn_source = None
+        self._has_source_term = fn_source is not None
+        if fn_source is not None:
+            self._fn_source = _fn.Function.convert(fn_source)
+            if not isinstance(self._fn_source, _fn.Function):
+                raise ValueError("Provided 'fn_source' must be of, or convertible to, the 'Function' class.")
         self._swarm = voronoi_swarm
         if not isinstance(conditions, (list, tuple)):
             conditions = [conditions]
@@ -80,13 +86,19 @@ class Stokes:
 
     @property
     def fn_source(self):
-        """The continuity source term; not part of the GPU PIC Stokes path (always None)."""
-        return None
+        """The volumetric (continuity) source term H, integrated into h on the PIC
+        points (P/systems/_stokes.py:284-288, 375-393)."""
+        return self._fn_source
 
     @fn_source.setter
     def fn_source(self, value):
-        if value is not None:
-            raise NotImplementedError("fn_source is not part of the GPU PIC Stokes path")
+        # as the reference: the term exists only if the object was built with one
+        if self._has_source_term:
+            self._fn_source = _fn.Function.convert(value)
+        else:
+            import warnings
+            warnings.warn("Cannot add fn_source to existing stokes object. Instead you should build a new object "
+                          "with fn_source defined", RuntimeWarning)
 
     @property
     def fn_bodyforce(self):
@@ -166,6 +178,8 @@ class Stokes:
         vals = self._velocityField.data * (mask != 0)
         ctx.set_bcs(torch.from_numpy(mask.ravel()), torch.from_numpy(np.ascontiguousarray(vals).ravel()))
         ctx.assemble(off, lst, ip_xi, ip_w, eta, body, lam)
+        if self._fn_source is not None:
+            ctx.add_source(off, lst, ip_xi, ip_w, self._per_particle(self._fn_source, ectx, npart, 1).view(-1))
         # tractions: the surface term on 3 Gauss points per face axis (P/systems/_stokes.py:291-297)
         for c in self._conditions:
             if isinstance(c, _cond.NeumannCondition):
@@ -258,7 +272,11 @@ class _OptionsGroup:
     def __init__(self):
         self.A11 = _Options(ksp_rtol=1e-6, ksp_type="fgmres", _mixed=False)
         self.scr = _Options(ksp_rtol=1e-5, ksp_type="fgmres", restart=30)
-        self.main = _Options(penalty=0.0, Q22_pc_type="uw", ksp_k2_type="NULL", max_inner=500, max_outer=500)
+        # remove_constant_pressure_null_space (OptionsMain, P/systems/_bsscr.py:151,167) and the
+        # -remove_checkerboard_pressure_null_space switch of BSSCR (BSSCR.c:369-381)
+        self.main = _Options(penalty=0.0, Q22_pc_type="uw", ksp_k2_type="NULL", max_inner=500, max_outer=500,
+                             remove_constant_pressure_null_space=False,
+                             remove_checkerboard_pressure_null_space=False)
         self.mg = _Options(active=True, levels=0, smooth_steps=3)
 
 
@@ -372,7 +390,9 @@ class StokesSolver:
         st = ctx.solve(u, p, mixed=int(o.A11._mixed), rtol=min(o.A11.ksp_rtol, o.scr.ksp_rtol),
                        inner_rtol=o.A11.ksp_rtol, outer_rtol=o.scr.ksp_rtol, max_inner=o.main.max_inner,
                        max_outer=o.main.max_outer, smooth_steps=o.mg.smooth_steps, restart=o.scr.restart,
-                       schur_pc=1 if s.mesh._porder == 0 else 0)
+                       schur_pc=1 if s.mesh._porder == 0 else 0,
+                       null_space=2 if o.main.remove_checkerboard_pressure_null_space
+                       else (1 if o.main.remove_constant_pressure_null_space else 0))
         s._velocityField._from_device()
         s._pressureField._from_device()
         st["assembly_time"] = t1 - t0
