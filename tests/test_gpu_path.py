@@ -260,3 +260,33 @@ def test_initial_guess(gpu):
     dp = (p2 - p2.mean()) - (p0 - p0.mean())
     assert float((u2 - u0).abs().max()) <= 1e-6 * float(u0.abs().max())
     assert float(dp.abs().max()) <= 1e-6 * float(p0.abs().max())
+
+
+@pytest.mark.parametrize("res", [(64, 48, 40), (22, 18, 14)])
+def test_K32_tiled_apply_many_tiles(gpu, res):
+    """The FP32 3D apply (persistent, double-buffered tiles; 16-byte weight copies
+    when res_x % 4 == 0, else 4-byte) against the FP64 apply: 480 tiles (more
+    than the resident CTAs, so CTAs loop) and a mesh of partial tiles, with
+    free-slip walls and scattered interior Dirichlet dofs (tiles with and
+    without a Dirichlet flag)."""
+    from underworld2_gb300._core import Context, rng_seed
+    c = Context(3, res, (0.0,) * 3, (1.0,) * 3)
+    x, owner, off, lst, _ = c.layout_random(2, rng_seed(3))
+    ip_xi = c.pic_map(x, off, lst)
+    ip_w = c.dvc_weights(off, ip_xi, res=6)
+    xo = x.cpu().numpy()
+    eta = torch.tensor(np.exp(3.0 * np.sin(7.0 * xo[:, 0]) * np.cos(5.0 * xo[:, 2])), device="cuda")
+    nodes = np.stack(np.meshgrid(*[np.array(a) for a in reversed(c.axes)], indexing="ij")[::-1], -1).reshape(-1, 3)
+    mask = np.zeros((len(nodes), 3), np.uint8)
+    for d in range(3):
+        mask[:, d] = np.isclose(nodes[:, d], 0.0) | np.isclose(nodes[:, d], 1.0)
+    rng = np.random.default_rng(1)
+    mask.ravel()[rng.choice(mask.size, 40, replace=False)] = 1
+    c.set_bcs(torch.tensor(mask.ravel(), device="cuda"))
+    c.assemble(off, lst, ip_xi, ip_w, eta, torch.zeros((len(xo), 3), dtype=torch.float64, device="cuda"))
+    xv = rng.standard_normal(mask.size)
+    y64 = c.apply_K(torch.tensor(xv, device="cuda")).cpu().numpy()
+    y32 = c.apply_K(torch.tensor(xv, device="cuda", dtype=torch.float32)).cpu().numpy()
+    assert np.abs(y32 - y64).max() <= 2e-5 * np.abs(y64).max()
+    fixed = mask.ravel() != 0
+    np.testing.assert_array_equal(y64[fixed], xv[fixed])

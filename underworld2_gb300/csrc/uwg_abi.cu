@@ -30,6 +30,8 @@ extern "C" void uwg_ctx_destroy(uwg_ctx* c) {
         if (l > 0) for (int d = 0; d < 3; d++) if (L.ax[d]) cudaFree(L.ax[d]);
         cudaFree(L.W64); cudaFree(L.W32); cudaFree(L.bc); cudaFree(L.diag64); cudaFree(L.diag32);
         if (L.cinv64) cudaFree(L.cinv64);
+        if (L.tile_bc) cudaFree(L.tile_bc);
+        for (int d = 0; d < 3; d++) if (L.h2inv[d]) cudaFree(L.h2inv[d]);
         if (L.cinv32) cudaFree(L.cinv32);
     }
     cudaFree(c->f); cudaFree(c->h); cudaFree(c->Shat); cudaFree(c->Mp); cudaFree(c->bcval);
@@ -146,6 +148,19 @@ extern "C" int uwg_ctx_create(const uwg_mesh_desc* d, uwg_ctx** out) {
             for (int k = 0; k <= L.res[i]; k++) v[k] = hax[i][(size_t)k << l];
             L.ax[i] = (double*)dmalloc(sizeof(double) * v.size(), &ok);
             if (ok) cudaMemcpy(L.ax[i], v.data(), sizeof(double) * v.size(), cudaMemcpyHostToDevice);
+        }
+        for (int i = 0; i < 3; i++) {
+            // 2/h per element along each axis in FP32, as the tiled FP32 apply forms it
+            L.h2inv[i] = nullptr;
+            if (i >= c->dim || L.order != 1) continue;
+            std::vector<float> hv(L.res[i]);
+            for (int k = 0; k < L.res[i]; k++) {
+                double a = l == 0 ? hax[i][k] : hax[i][(size_t)k << l];
+                double b = l == 0 ? hax[i][k + 1] : hax[i][(size_t)(k + 1) << l];
+                hv[k] = 2.0f / (float)(b - a);
+            }
+            L.h2inv[i] = (float*)dmalloc(sizeof(float) * hv.size(), &ok);
+            if (ok) cudaMemcpy(L.h2inv[i], hv.data(), sizeof(float) * hv.size(), cudaMemcpyHostToDevice);
         }
         L.W64 = (double*)dmalloc(sizeof(double) * L.nq * ne, &ok);
         L.W32 = (float*)dmalloc(sizeof(float) * L.nq * ne, &ok);

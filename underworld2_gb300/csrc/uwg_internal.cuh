@@ -26,6 +26,8 @@ struct uwg_level {
     double* diag64;       // operator diagonal (BC rows = 1)
     float* diag32;
     double lmax64, lmax32; // Chebyshev upper bound for D^-1 K
+    uint8_t* tile_bc;     // 3D Q1: per 8x8x4 tile, 1 when the tile holds a Dirichlet dof (tiled apply)
+    float* h2inv[3];      // order-1 levels: 2 / (element size) per axis index, FP32 (tiled apply)
     // dense coarse solve (coarsest level only)
     double* cinv64;
     float* cinv32;

@@ -352,101 +352,280 @@ __global__ void __launch_bounds__(128) k_applyK_q1_3d(uwg_lgeom g, const T* __re
 }
 
 
-// Shared-memory tiled K apply (3D): a CTA owns an 8x8x4 tile of elements, stages
-// the tile's 9x9x5 nodal values in shared memory (row-contiguous loads), adds
-// the element results into a shared tile with shared-memory atomics, and then
-// writes nodes inside the tile with plain stores and nodes on the tile faces
-// (shared with neighbouring tiles) with global atomics: 8x fewer global
-// atomics than the element-per-thread kernel.  In FP32 the tile's 27 weight
-// planes are copied to shared memory with cp.async at the start, so their
-// DRAM latency overlaps the nodal staging instead of stalling the element
-// arithmetic.
+// Tiled K apply (3D): a CTA owns an 8x8x4 tile of elements.
+//  1. The tile's 9x9x5 nodal values are staged by cp.async row by row: one
+//     warp per row of 27 contiguous values, so a lane's node index is fixed
+//     and no per-slot integer division is left.  Dirichlet flags are staged
+//     only for tiles that hold a Dirichlet dof (a per-tile flag, built with
+//     the level); the other tiles never read the mask.
+//  2. One thread per element adds K_e u_e into a shared tile (shared atomics).
+//  3. Write-back, row by row: Dirichlet dofs y = x (the identity rows; every
+//     tile holding the node writes the same value), nodes inside the tile a
+//     plain store, nodes on the tile faces a global atomic add onto y, which
+//     the caller zeroes first (a memset rather than a masked copy pass).
+// Tiles without a Dirichlet dof take an element path without the mask.  A
+// persistent, double-buffered variant (the next tile's copies in flight while
+// computing the current one) measured slower: at 16 warps per SM the kernel is
+// bound by instruction issue and latency, not by DRAM.
 #define KT_X 8
 #define KT_Y 8
 #define KT_Z 4
 #define KT_N (KT_X * KT_Y * KT_Z)
 
-__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+template <int BYTES>
+__device__ __forceinline__ void cp_async_z(void* smem, const void* gmem, bool valid) {
     unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem));
+    if constexpr (BYTES == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(gmem), "r"(valid ? 16 : 0));
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(sa), "l"(gmem), "n"(BYTES),
+                     "r"(valid ? BYTES : 0));
 }
-__device__ __forceinline__ void cp_async4z(void* smem, const void* gmem, bool valid) {
-    unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sa), "l"(gmem), "r"(valid ? 4 : 0));
-}
-__device__ __forceinline__ void cp_async_wait_all() {
-    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;\n" ::: "memory");
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+int64_t uwg_ops_ktiles(const int* res) {
+    return (int64_t)((res[0] + KT_X - 1) / KT_X) * ((res[1] + KT_Y - 1) / KT_Y) * ((res[2] + KT_Z - 1) / KT_Z);
 }
 
-template <typename T, bool STAGE_W>
-__global__ void __launch_bounds__(KT_N, STAGE_W ? 3 : 1) k_applyK_q1_3d_tiled(uwg_lgeom g, const T* __restrict__ W,
-                                                            const uint8_t* __restrict__ bc,
-                                                            const T* __restrict__ x, T* y) {
+// Per-tile Dirichlet flag: 1 when any dof of the tile's nodes (halo included) is fixed.
+__global__ void k_tile_bc_flags(uwg_lgeom g, const uint8_t* __restrict__ bc, uint8_t* __restrict__ flags) {
     constexpr int NX = KT_X + 1, NY = KT_Y + 1, NZ = KT_Z + 1, NN = NX * NY * NZ;
-    __shared__ T xs[NN * 3];
-    __shared__ T ys[NN * 3];
-    __shared__ T ws[STAGE_W ? 27 * KT_N : 1];
-    __shared__ uint8_t bs[NN * 3];
     int ntx = (g.res[0] + KT_X - 1) / KT_X, nty = (g.res[1] + KT_Y - 1) / KT_Y;
     int tile = blockIdx.x;
     int tx0 = (tile % ntx) * KT_X, ty0 = ((tile / ntx) % nty) * KT_Y, tz0 = (tile / (ntx * nty)) * KT_Z;
-    int64_t gnx = g.nx[0], gny = g.nx[1];
-    int li = threadIdx.x % KT_X, lj = (threadIdx.x / KT_X) % KT_Y, lk = threadIdx.x / (KT_X * KT_Y);
-    int ex = tx0 + li, ey = ty0 + lj, ez = tz0 + lk;
+    int any = 0;
+    for (int k = threadIdx.x; k < NN * 3; k += blockDim.x) {
+        int nl = k / 3, c = k % 3;
+        int gi = tx0 + nl % NX, gj = ty0 + (nl / NX) % NY, gk = tz0 + nl / (NX * NY);
+        if (gi < g.nx[0] && gj < g.nx[1] && gk < g.nx[2])
+            any |= bc[(gi + (int64_t)g.nx[0] * (gj + (int64_t)g.nx[1] * gk)) * 3 + c] != 0;
+    }
+    any = __syncthreads_or(any);
+    if (threadIdx.x == 0) flags[tile] = (uint8_t)any;
+}
+
+constexpr int KT_NROW = (KT_Y + 1) * (KT_Z + 1), KT_ROW = 3 * (KT_X + 1);
+constexpr int KT_NN3 = KT_NROW * KT_ROW;
+constexpr int KT_NIT = (KT_NROW + KT_N / 32 - 1) / (KT_N / 32);
+static_assert(KT_ROW <= 32, "one warp per staged row");
+
+// Stage a tile's nodal values (cp.async) and, for a tile with a Dirichlet dof, its flags (plain loads).
+template <typename T>
+__device__ __forceinline__ void kt_stage_x(const uwg_lgeom& g, int tx0, int ty0, int tz0, const T* __restrict__ x,
+                                           T* xs) {
+    constexpr int NY = KT_Y + 1, NW = KT_N / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, gi = tx0 + lane / 3;
+    const int64_t gnx = g.nx[0], gny = g.nx[1];
+#pragma unroll
+    for (int it = 0; it < KT_NIT; it++) {
+        const int r = warp + it * NW;
+        if (r < KT_NROW && lane < KT_ROW) {
+            const int gj = ty0 + r % NY, gk = tz0 + r / NY;
+            const bool in = gi < g.nx[0] && gj < g.nx[1] && gk < g.nx[2];
+            const int64_t dof = in ? (tx0 + gnx * (gj + gny * (int64_t)gk)) * 3 + lane : 0;
+            cp_async_z<sizeof(T)>(&xs[r * KT_ROW + lane], x + dof, in);
+        }
+    }
+}
+__device__ __forceinline__ void kt_stage_bc(const uwg_lgeom& g, int tx0, int ty0, int tz0,
+                                            const uint8_t* __restrict__ bc, uint8_t* bs) {
+    constexpr int NY = KT_Y + 1, NW = KT_N / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, gi = tx0 + lane / 3;
+    const int64_t gnx = g.nx[0], gny = g.nx[1];
+#pragma unroll
+    for (int it = 0; it < KT_NIT; it++) {
+        const int r = warp + it * NW;
+        if (r < KT_NROW && lane < KT_ROW) {
+            const int gj = ty0 + r % NY, gk = tz0 + r / NY;
+            const bool in = gi < g.nx[0] && gj < g.nx[1] && gk < g.nx[2];
+            bs[r * KT_ROW + lane] = in ? bc[(tx0 + gnx * (gj + gny * (int64_t)gk)) * 3 + lane] : (uint8_t)1;
+        }
+    }
+}
+
+// One element: gather u from the staged tile (Dirichlet dofs as zero when
+// HAS_BC), K_e u_e, scatter into the shared accumulator (FP64), or return the
+// 24 outputs for the gather write-back (FP32, out != nullptr).
+template <typename T, bool HAS_BC>
+__device__ __forceinline__ void kt_element(const T* xs, const uint8_t* bs, T* ys, const T* ws, int64_t wstride, T hx,
+                                           T hy, T hz, T (*eo)[3] = nullptr) {
+    constexpr int NX = KT_X + 1, NY = KT_Y + 1;
+    const int li = threadIdx.x % KT_X, lj = (threadIdx.x / KT_X) % KT_Y, lk = threadIdx.x / (KT_X * KT_Y);
+    T u[8][3], out[8][3];
+#pragma unroll
+    for (int n = 0; n < 8; n++) {
+        const int sl = (li + (n & 1)) + NX * ((lj + ((n >> 1) & 1)) + NY * (lk + ((n >> 2) & 1)));
+#pragma unroll
+        for (int c = 0; c < 3; c++) u[n][c] = (HAS_BC && bs[sl * 3 + c]) ? (T)0 : xs[sl * 3 + c];
+    }
+    q1_3d_element<T>(ws, wstride, hx, hy, hz, u, out);
+    if (eo) {
+#pragma unroll
+        for (int n = 0; n < 8; n++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) eo[n][c] = out[n][c];
+        return;
+    }
+#pragma unroll
+    for (int n = 0; n < 8; n++) {
+        const int sl = (li + (n & 1)) + NX * ((lj + ((n >> 1) & 1)) + NY * (lk + ((n >> 2) & 1)));
+#pragma unroll
+        for (int c = 0; c < 3; c++) atomicAdd(&ys[sl * 3 + c], out[n][c]);
+    }
+}
+
+// Gather write-back (FP32): eo[(n * 3 + c) * KT_N + t] holds output (node n,
+// component c) of the element of thread t (zero for elements outside the
+// mesh); a node sums the outputs of the up to eight tile elements around it.
+__device__ __forceinline__ void kt_writeback_gather(const uwg_lgeom& g, int tx0, int ty0, int tz0, bool has_bc,
+                                                    const float* xs, const uint8_t* bs, const float* eo,
+                                                    float* __restrict__ y) {
+    constexpr int NY = KT_Y + 1, NW = KT_N / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, ni = lane / 3, c = lane - 3 * (lane / 3), gi = tx0 + ni;
+    const int64_t gnx = g.nx[0], gny = g.nx[1];
+#pragma unroll
+    for (int it = 0; it < KT_NIT; it++) {
+        const int r = warp + it * NW;
+        if (r < KT_NROW && lane < KT_ROW) {
+            const int nj = r % NY, nk = r / NY;
+            const int gj = ty0 + nj, gk = tz0 + nk;
+            if (gi < g.nx[0] && gj < g.nx[1] && gk < g.nx[2]) {
+                const int64_t dof = (tx0 + gnx * (gj + gny * (int64_t)gk)) * 3 + lane;
+                const int k = r * KT_ROW + lane;
+                if (has_bc && bs[k]) {
+                    y[dof] = xs[k];
+                } else {
+                    // element (ni - dx, nj - dy, nk - dz) holds this node as its corner n = dx + 2 dy + 4 dz:
+                    // one base address, constant offsets, validity from six per-axis tests
+                    const bool x0 = ni < KT_X, x1 = ni > 0, y0 = nj < KT_Y, y1 = nj > 0, z0 = nk < KT_Z, z1 = nk > 0;
+                    const float* b0 = eo + c * KT_N + ni + KT_X * (nj + KT_Y * nk);
+                    float v = 0.f;
+#pragma unroll
+                    for (int n = 0; n < 8; n++) {
+                        const int dx = n & 1, dy = (n >> 1) & 1, dz = n >> 2;
+                        const bool ok = (dx ? x1 : x0) && (dy ? y1 : y0) && (dz ? z1 : z0);
+                        if (ok) v += b0[n * 3 * KT_N - dx - KT_X * dy - KT_X * KT_Y * dz];
+                    }
+                    const bool interior = ni > 0 && ni < KT_X && nj > 0 && nj < KT_Y && nk > 0 && nk < KT_Z;
+                    if (interior) y[dof] = v;
+                    else atomicAdd(&y[dof], v);
+                }
+            }
+        }
+    }
+}
+
+// Write-back, row by row (see the comment above KT_X).
+template <typename T>
+__device__ __forceinline__ void kt_writeback(const uwg_lgeom& g, int tx0, int ty0, int tz0, bool has_bc, const T* xs,
+                                             const uint8_t* bs, const T* ys, T* __restrict__ y) {
+    constexpr int NY = KT_Y + 1, NW = KT_N / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, ni = lane / 3, gi = tx0 + ni;
+    const int64_t gnx = g.nx[0], gny = g.nx[1];
+#pragma unroll
+    for (int it = 0; it < KT_NIT; it++) {
+        const int r = warp + it * NW;
+        if (r < KT_NROW && lane < KT_ROW) {
+            const int nj = r % NY, nk = r / NY;
+            const int gj = ty0 + nj, gk = tz0 + nk;
+            const int k = r * KT_ROW + lane;
+            if (gi < g.nx[0] && gj < g.nx[1] && gk < g.nx[2]) {
+                const int64_t dof = (tx0 + gnx * (gj + gny * (int64_t)gk)) * 3 + lane;
+                if (has_bc && bs[k]) {
+                    y[dof] = xs[k];
+                } else {
+                    const bool interior = ni > 0 && ni < KT_X && nj > 0 && nj < KT_Y && nk > 0 && nk < KT_Z;
+                    if (interior) y[dof] = ys[k];
+                    else atomicAdd(&y[dof], ys[k]);
+                }
+            }
+        }
+    }
+}
+
+// One CTA per tile.  FP32 (STAGE_W): the tile's 27 weight planes go to shared
+// memory by cp.async (16-byte copies of 4-element rows when res_x % 4 == 0
+// and n_el % 4 == 0), 2/h comes from the level's FP32 table, 2 CTAs per SM.
+// FP64: weights straight from global memory, 2/h in FP64.
+template <typename T, bool STAGE_W, bool VEC_W>
+__global__ void __launch_bounds__(KT_N, STAGE_W ? 2 : 1) k_applyK_q1_3d_tiled(
+    uwg_lgeom g, const T* __restrict__ W, const uint8_t* __restrict__ bc, const uint8_t* __restrict__ tile_bc,
+    const float* __restrict__ h2x, const float* __restrict__ h2y, const float* __restrict__ h2z,
+    const T* __restrict__ x, T* __restrict__ y) {
+    __shared__ __align__(16) T xs[KT_NN3];
+    __shared__ T ys[STAGE_W ? 1 : KT_NN3];
+    __shared__ __align__(16) T ws[STAGE_W ? 27 * KT_N : 1];
+    __shared__ uint8_t bs[KT_NN3];
+    const int ntx = (g.res[0] + KT_X - 1) / KT_X, nty = (g.res[1] + KT_Y - 1) / KT_Y;
+    const int tile = blockIdx.x;
+    const int tx0 = (tile % ntx) * KT_X, ty0 = ((tile / ntx) % nty) * KT_Y, tz0 = (tile / (ntx * nty)) * KT_Z;
+    const int li = threadIdx.x % KT_X, lj = (threadIdx.x / KT_X) % KT_Y, lk = threadIdx.x / (KT_X * KT_Y);
+    const int ex = tx0 + li, ey = ty0 + lj, ez = tz0 + lk;
     const bool own = ex < g.res[0] && ey < g.res[1] && ez < g.res[2];
     const int64_t e = own ? ex + (int64_t)g.res[0] * (ey + (int64_t)g.res[1] * ez) : 0;
     if constexpr (STAGE_W) {
-        if (own) {
+        if constexpr (VEC_W) {
+            // 27 planes x 32 rows x 2 chunks of 16 bytes: thread t copies chunk (t & 63)
+            // of planes t/64, t/64 + 4, ...: one address computation, then a stride of n_el
+            static_assert(KT_X == 8 && KT_Y * KT_Z == 32 && KT_N == 256, "16-byte weight staging layout");
+            const int q = threadIdx.x & 63, j0 = threadIdx.x >> 6, ch = q & 1, lyz = q >> 1;
+            const int cx = tx0 + ch * 4, cy = ty0 + (lyz & (KT_Y - 1)), cz = tz0 + lyz / KT_Y;
+            const bool in = cx < g.res[0] && cy < g.res[1] && cz < g.res[2];
+            const float* src = (const float*)W + (in ? cx + (int64_t)g.res[0] * (cy + (int64_t)g.res[1] * cz) : 0) +
+                               (int64_t)j0 * g.n_el;
+            float* dst = (float*)ws + j0 * KT_N + KT_X * lyz + ch * 4;
+            const int64_t step = 4 * g.n_el;
 #pragma unroll
-            for (int j = 0; j < 27; j++) cp_async4(&ws[j * KT_N + threadIdx.x], W + (int64_t)j * g.n_el + e);
+            for (int j = j0; j < 27; j += 4, src += step, dst += 4 * KT_N) cp_async_z<16>(dst, src, in);
+        } else {
+#pragma unroll
+            for (int j = 0; j < 27; j++) cp_async_z<sizeof(T)>(&ws[j * KT_N + threadIdx.x], W + (int64_t)j * g.n_el + e, own);
         }
     }
-    // stage nodal values and Dirichlet flags, clear the accumulator (in FP32 the
-    // values arrive by cp.async, so no thread waits on a chain of loads)
-    for (int k = threadIdx.x; k < NN * 3; k += blockDim.x) {
-        int nl = k / 3, c = k % 3;
-        int ni = nl % NX, nj = (nl / NX) % NY, nk = nl / (NX * NY);
-        int gi = tx0 + ni, gj = ty0 + nj, gk = tz0 + nk;
-        const bool in = gi < g.nx[0] && gj < g.nx[1] && gk < g.nx[2];
-        const int64_t dof = in ? (gi + gnx * (gj + gny * (int64_t)gk)) * 3 + c : 0;
-        if constexpr (STAGE_W) cp_async4z(&xs[k], x + dof, in);
-        else xs[k] = in ? x[dof] : (T)0;
-        bs[k] = in ? bc[dof] : (uint8_t)1;
-        ys[k] = (T)0;
-    }
-    if constexpr (STAGE_W) cp_async_wait_all();
-    __syncthreads();
+    kt_stage_x<T>(g, tx0, ty0, tz0, x, xs);
+    cp_async_commit();
+    const bool has_bc = tile_bc[tile] != 0;
+    if (has_bc) kt_stage_bc(g, tx0, ty0, tz0, bc, bs);
+    if constexpr (!STAGE_W)
+        for (int k = threadIdx.x; k < KT_NN3; k += KT_N) ys[k] = (T)0;
+    T hx = (T)1, hy = (T)1, hz = (T)1;
     if (own) {
-        const T hx = (T)2 / (T)(g.ax[0][ex + 1] - g.ax[0][ex]);   // 2/h in the operator's precision
-        const T hy = (T)2 / (T)(g.ax[1][ey + 1] - g.ax[1][ey]);
-        const T hz = (T)2 / (T)(g.ax[2][ez + 1] - g.ax[2][ez]);
-        T u[8][3], out[8][3];
-#pragma unroll
-        for (int n = 0; n < 8; n++) {
-            int sl = (li + (n & 1)) + NX * ((lj + ((n >> 1) & 1)) + NY * (lk + ((n >> 2) & 1)));
-#pragma unroll
-            for (int c = 0; c < 3; c++) u[n][c] = bs[sl * 3 + c] ? (T)0 : xs[sl * 3 + c];
-        }
-        if constexpr (STAGE_W) q1_3d_element<T>(ws + threadIdx.x, KT_N, hx, hy, hz, u, out);
-        else q1_3d_element<T>(W + e, g.n_el, hx, hy, hz, u, out);
-#pragma unroll
-        for (int n = 0; n < 8; n++) {
-            int sl = (li + (n & 1)) + NX * ((lj + ((n >> 1) & 1)) + NY * (lk + ((n >> 2) & 1)));
-#pragma unroll
-            for (int c = 0; c < 3; c++) atomicAdd(&ys[sl * 3 + c], out[n][c]);
+        if constexpr (STAGE_W) {
+            hx = (T)__ldg(&h2x[ex]); hy = (T)__ldg(&h2y[ey]); hz = (T)__ldg(&h2z[ez]);
+        } else {
+            hx = (T)2 / (T)(g.ax[0][ex + 1] - g.ax[0][ex]);
+            hy = (T)2 / (T)(g.ax[1][ey + 1] - g.ax[1][ey]);
+            hz = (T)2 / (T)(g.ax[2][ez + 1] - g.ax[2][ez]);
         }
     }
+    cp_async_wait<0>();
     __syncthreads();
-    for (int k = threadIdx.x; k < NN * 3; k += blockDim.x) {
-        int nl = k / 3, c = k % 3;
-        int ni = nl % NX, nj = (nl / NX) % NY, nk = nl / (NX * NY);
-        int gi = tx0 + ni, gj = ty0 + nj, gk = tz0 + nk;
-        if (gi >= g.nx[0] || gj >= g.nx[1] || gk >= g.nx[2]) continue;
-        int64_t dof = (gi + gnx * (gj + gny * (int64_t)gk)) * 3 + c;
-        if (bs[k]) continue;
-        bool interior = ni > 0 && ni < KT_X && nj > 0 && nj < KT_Y && nk > 0 && nk < KT_Z;
-        if (interior) y[dof] = ys[k];
-        else atomicAdd(&y[dof], ys[k]);
+    if constexpr (STAGE_W) {
+        // outputs in registers, then (once every thread is done with the weights)
+        // into the weight buffer for the gather write-back: no shared atomics
+        T eo[8][3];
+#pragma unroll
+        for (int n = 0; n < 8; n++) eo[n][0] = eo[n][1] = eo[n][2] = (T)0;
+        if (own) {
+            if (has_bc) kt_element<T, true>(xs, bs, ys, ws + threadIdx.x, KT_N, hx, hy, hz, eo);
+            else kt_element<T, false>(xs, bs, ys, ws + threadIdx.x, KT_N, hx, hy, hz, eo);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int n = 0; n < 8; n++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) ws[(n * 3 + c) * KT_N + threadIdx.x] = eo[n][c];
+        __syncthreads();
+        kt_writeback_gather(g, tx0, ty0, tz0, has_bc, (const float*)xs, bs, (const float*)ws, (float*)y);
+    } else {
+        if (own) {
+            if (has_bc) kt_element<T, true>(xs, bs, ys, W + e, g.n_el, hx, hy, hz);
+            else kt_element<T, false>(xs, bs, ys, W + e, g.n_el, hx, hy, hz);
+        }
+        __syncthreads();
+        kt_writeback<T>(g, tx0, ty0, tz0, has_bc, xs, bs, ys, y);
     }
 }
 
@@ -510,12 +689,29 @@ int uwg_ops_applyK(uwg_ctx* c, int l, const T* x, T* y) {
     uwg_lgeom g = uwg_level_geom(c, l);
     const T* W;
     if constexpr (sizeof(T) == 8) W = (const T*)L.W64; else W = (const T*)L.W32;
+    if (L.order == 1 && c->dim == 3 && L.tile_bc) {
+        // y = 0, then the tiled kernel writes Dirichlet rows (y = x) and adds K x elsewhere
+        UWG_CUDA(c, cudaMemsetAsync(y, 0, sizeof(T) * L.n_dof, c->stream));
+        unsigned tiles = (unsigned)uwg_ops_ktiles(L.res);
+        bool vec = (L.res[0] % 4) == 0 && (L.n_el % 4) == 0;
+        if constexpr (sizeof(T) == 4) {
+            if (vec)
+                k_applyK_q1_3d_tiled<T, true, true><<<tiles, KT_N, 0, c->stream>>>(
+                    g, W, L.bc, L.tile_bc, L.h2inv[0], L.h2inv[1], L.h2inv[2], x, y);
+            else
+                k_applyK_q1_3d_tiled<T, true, false><<<tiles, KT_N, 0, c->stream>>>(
+                    g, W, L.bc, L.tile_bc, L.h2inv[0], L.h2inv[1], L.h2inv[2], x, y);
+        } else {
+            k_applyK_q1_3d_tiled<T, false, false><<<tiles, KT_N, 0, c->stream>>>(
+                g, W, L.bc, L.tile_bc, nullptr, nullptr, nullptr, x, y);
+        }
+        UWG_CUDA(c, cudaGetLastError());
+        return UWG_OK;
+    }
     k_bc_copy<T><<<nblk(L.n_dof), 256, 0, c->stream>>>(L.n_dof, L.bc, x, y);
     if (L.order == 2) return uwg_q2_applyK<T>(c, x, y, true);
     if (c->dim == 3) {
-        unsigned tiles = (unsigned)(((L.res[0] + KT_X - 1) / KT_X) * ((L.res[1] + KT_Y - 1) / KT_Y) *
-                                    ((L.res[2] + KT_Z - 1) / KT_Z));
-        k_applyK_q1_3d_tiled<T, sizeof(T) == 4><<<tiles, KT_N, 0, c->stream>>>(g, W, L.bc, x, y);
+        return uwg_set_error(c, UWG_ERR_STATE, "3D Q1 apply before the level's tile flags were built");
     } else {
         k_applyK_q1_2d<T><<<nblk(L.n_el, 128), 128, 0, c->stream>>>(g, W, L.bc, true, x, y);
     }
@@ -1106,6 +1302,13 @@ int uwg_ops_level_setup(uwg_ctx* c, int l) {
         k_to_f32<<<nblk(L.n_el * L.nq), 256, 0, c->stream>>>(L.n_el * L.nq, L.W64, L.W32);
         UWG_CUDA(c, cudaGetLastError());
         return UWG_OK;
+    }
+    if (c->dim == 3) {
+        // per-tile Dirichlet flags of the tiled apply (the mask of this level is final here)
+        int64_t nt = uwg_ops_ktiles(L.res);
+        if (!L.tile_bc) UWG_CUDA(c, cudaMalloc((void**)&L.tile_bc, nt));
+        k_tile_bc_flags<<<(unsigned)nt, 256, 0, c->stream>>>(g, L.bc, L.tile_bc);
+        UWG_CUDA(c, cudaGetLastError());
     }
     if (c->dim == 3) k_diag_q1<3><<<nblk(L.n_el), 256, 0, c->stream>>>(g, L.W64, L.bc, L.diag64, l == 0 ? c->Shat : nullptr, c->Mp);
     else k_diag_q1<2><<<nblk(L.n_el), 256, 0, c->stream>>>(g, L.W64, L.bc, L.diag64, l == 0 ? c->Shat : nullptr, c->Mp);

@@ -12,6 +12,7 @@ struct uwg_lgeom {
 };
 
 uwg_lgeom uwg_level_geom(const uwg_ctx* c, int l);
+int64_t uwg_ops_ktiles(const int* res);   // tiles of the 3D Q1 tiled apply
 
 // Assembly from the PIC swarm (finest level): W, f, Mp.
 int uwg_ops_assemble(uwg_ctx* c, const int32_t* off, const int32_t* list, const double* ip_xi,
