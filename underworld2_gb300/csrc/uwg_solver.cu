@@ -70,6 +70,7 @@ struct Work {
     // whether the checkerboard lies in the null space of G (every velocity dof on the walls fixed)
     double *ns_t = nullptr, *ns_v = nullptr, *ns_one = nullptr, *ns_tmp = nullptr;
     bool cb_null = false;
+    bool const_null = false;   // the constant pressure lies in the null space of G
 };
 
 Work* work_of(uwg_ctx* c) {
@@ -241,6 +242,8 @@ int pcg(uwg_ctx* c, const T* b, T* x, double bnorm, double tol, int maxit, int d
     const T* b2[2] = {z, r};
     if ((rc = dots<T>(c, n, 2, a2, b2, d2))) return rc;
     double rz = d2[0];
+    if (!std::isfinite(bnorm) || !std::isfinite(d2[1]))
+        return uwg_set_error(c, UWG_ERR_NAN, "velocity CG: non-finite right-hand side or residual");
     if (std::sqrt(d2[1]) <= tol * bnorm) return UWG_OK;
     for (int it = 1; it <= maxit; it++) {
         if ((rc = uwg_ops_applyK<T>(c, 0, p, q))) return rc;
@@ -261,6 +264,10 @@ int pcg(uwg_ctx* c, const T* b, T* x, double bnorm, double tol, int maxit, int d
         *its = it;
         if (!std::isfinite(d2[1])) return uwg_set_error(c, UWG_ERR_NAN, "non-finite residual in velocity CG");
         if (std::sqrt(d2[1]) <= tol * bnorm) return UWG_OK;
+        if (!(d2[0] > 0.0) || !std::isfinite(d2[0]))
+            return uwg_set_error(c, std::isfinite(d2[0]) ? UWG_ERR_NOT_CONVERGED : UWG_ERR_NAN,
+                                 "velocity CG: preconditioned residual r.z = " + std::to_string(d2[0]) +
+                                 " at ||r||/||b|| = " + std::to_string(std::sqrt(d2[1]) / bnorm));
         double beta = d2[0] / rz;
         rz = d2[0];
         vk_axpby<T>(s, n, (T)1, z, (T)beta, p);
@@ -644,7 +651,14 @@ int bfbt(uwg_ctx* c, const double* r, double* z, double rtol, int its) {
     if ((rc = lsolve(c, w->bf_m, w->bf_z, rtol, maxit))) return rc;
     vk_convert<float, double>(s, np, w->bf_z, z);
     vk_scale<double>(s, np, -1.0, z);
-    if (w->cb_null && ((rc = ns_project(c, w->ns_t, z)) || (rc = ns_project(c, w->ns_v, z)))) return rc;
+    // Null modes of S in z are arbitrary (L is singular on them) and S removes them
+    // again; left in, a direction that is almost a pure null mode would give the
+    // flexible GMRES a zero pivot near convergence.
+    if (w->cb_null) {
+        if ((rc = ns_project(c, w->ns_t, z)) || (rc = ns_project(c, w->ns_v, z))) return rc;
+    } else if (w->const_null && (rc = ns_project(c, w->ns_one, z))) {
+        return rc;
+    }
     return UWG_OK;
 }
 
@@ -748,9 +762,11 @@ int uwg_solver_setup(uwg_ctx* c) {
         if ((rc = g_norm_inf(c, &gn))) return rc;
         vk_copy<double>(c->stream, c->n_pdof, w->ns_t, w->ns_tmp);
         vk_axpy<double>(c->stream, c->n_pdof, -1.0, w->ns_v, w->ns_tmp);
-        bool cb = false;
+        bool cb = false, cn = false;
         if (c->porder == 0 && (rc = ns_test(c, w->ns_tmp, gn, &cb))) return rc;
+        if ((rc = ns_test(c, w->ns_one, gn, &cn))) return rc;
         w->cb_null = cb;
+        w->const_null = cn;
     }
     if (c->porder == 0 && (rc = bfbt_setup(c))) return rc;
     return capture_cycles(c, work_of(c)->g_deg > 0 ? work_of(c)->g_deg : 3);
@@ -837,7 +853,11 @@ int fgmres(uwg_ctx* c, const SolveCfg& cfg, const double* rhs, double* p, double
                 vk_copy<double>(s, n, z0, w->Z[j]);
             } else if (cfg.schur_pc == 1) {
                 if ((rc = bfbt(c, w->V[j], w->Z[j], cfg.schur_pc_rtol, cfg.schur_pc_its))) return rc;
-                cudaStreamSynchronize(s);
+                double zn;
+                const double* az[1] = {w->Z[j]};
+                if ((rc = dots<double>(c, n, 1, az, az, &zn))) return rc;
+                if (!std::isfinite(zn))
+                    return uwg_set_error(c, UWG_ERR_NAN, "non-finite value from the BFBt Schur preconditioner");
                 w->t_pc += now() - tp0;
             } else {
                 if ((rc = uwg_ops_schur_pc(c, w->V[j], w->Z[j]))) return rc;
@@ -894,11 +914,12 @@ int fgmres(uwg_ctx* c, const SolveCfg& cfg, const double* rhs, double* p, double
             if (hn > 0.0) vk_scale<double>(s, n, 1.0 / hn, w->V[j + 1]);
             if (std::fabs(g[j + 1]) <= tol || hn == 0.0) { j++; done = true; break; }
         }
-        // y = H^-1 g, p += Z y
+        // y = H^-1 g, p += Z y (a zero pivot -- a direction S maps to nothing -- is dropped)
         for (int i = j - 1; i >= 0; i--) {
             double t = g[i];
             for (int k = i + 1; k < j; k++) t -= H[i * m + k] * y[k];
-            y[i] = t / H[i * m + i];
+            y[i] = H[i * m + i] != 0.0 ? t / H[i * m + i] : 0.0;
+            if (!std::isfinite(y[i])) y[i] = 0.0;
         }
         UWG_CUDA(c, cudaMemcpyAsync(w->coef, y.data(), sizeof(double) * j, cudaMemcpyHostToDevice, s));
         for (int i0 = 0; i0 < j; i0 += 64)
