@@ -181,6 +181,10 @@ extern "C" int uwg_ctx_create(const uwg_mesh_desc* d, uwg_ctx** out) {
         }
     }
     c->bc = c->lev[0].bc;
+    // the pressure hierarchy ends at the first level of at most 512 cells (two unknowns
+    // each below level 0): a dense solve there replaces the tiny, launch-bound levels
+    c->pnlev = 1;
+    while (c->pnlev < nlev && (c->pnlev < 2 || c->lev[c->pnlev - 1].n_el > 512)) c->pnlev++;
     c->f = (double*)dmalloc(sizeof(double) * c->n_vdof, &ok);
     c->bcval = (double*)dmalloc(sizeof(double) * c->n_vdof, &ok);
     c->h = (double*)dmalloc(sizeof(double) * c->n_pdof, &ok);

@@ -51,6 +51,7 @@ struct uwg_ctx {
 
     // assembled state
     int nlev;
+    int pnlev;              // levels of the BFBt pressure multigrid (it stops at <= 512 cells, dense below)
     uwg_level lev[UWG_MAXLEV];
     double* f;              // velocity rhs [n_vdof] (BC lifted)
     double* h;              // pressure rhs [n_pdof]

@@ -279,9 +279,29 @@ __global__ void k_pdense(uwg_lgeom g, const float* __restrict__ st, double* __re
 
 // Rank-one terms tau 1 1^T on the smooth block (and, when the checkerboard is a
 // null mode of G as well, on the checkerboard block) make the singular coarse
-// operator invertible without changing its action on the range.
-__global__ void k_pdense_fix(int64_t m, int64_t n, int fix_checkerboard, double* A) {
+// operator invertible without changing its action on the range.  A one-unknown
+// level (m == n) gets the checkerboard term as tau s s^T, s_i = (-1)^(x+y+z).
+__global__ void k_pdense_fix(int64_t m, int64_t n, int fix_checkerboard, int rx, int ry, double* A) {
     __shared__ double red[1024];
+    if (fix_checkerboard && m == n) {
+        double mx = 0.0;
+        for (int64_t i = threadIdx.x; i < n; i += blockDim.x) mx = fmax(mx, A[i * m + i]);
+        red[threadIdx.x] = mx;
+        __syncthreads();
+        for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+            if ((int)threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+            __syncthreads();
+        }
+        const double tau = (red[0] > 0.0 ? red[0] : 1.0) / (double)n;
+        __syncthreads();
+        for (int64_t k = threadIdx.x; k < n * n; k += blockDim.x) {
+            const int64_t i = k / n, j = k % n;
+            const int si = (int)((i % rx) + (i / rx) % ry + i / ((int64_t)rx * ry)) & 1;
+            const int sj = (int)((j % rx) + (j / rx) % ry + j / ((int64_t)rx * ry)) & 1;
+            A[i * m + j] += si == sj ? tau : -tau;
+        }
+        __syncthreads();
+    }
     for (int blk = 0; blk < (fix_checkerboard && m == 2 * n ? 2 : 1); blk++) {
         double* B = A + (int64_t)blk * n * m + (int64_t)blk * n;   // diagonal block blk
         double mx = 0.0;
@@ -686,7 +706,7 @@ __global__ void k_pdiag1_tri(int64_t n, int center, int center5, const float* __
 int uwg_pmg_ncomp(int l) { return l == 0 ? 1 : 2; }
 
 // level 1 uses the smooth checkerboard interpolation when it is not the coarsest level
-static bool smooth1(const uwg_ctx* c) { return c->nlev >= 3; }
+static bool smooth1(const uwg_ctx* c) { return c->pnlev >= 3; }
 
 int64_t uwg_pmg_stencil_size(const uwg_ctx* c, int l) {
     int no = c->dim == 3 ? 27 : 9, n5 = c->dim == 3 ? 125 : 25;
@@ -777,7 +797,7 @@ int uwg_pmg_dense_inverse(uwg_ctx* c, int l, const float* st, int fix_checkerboa
     UWG_CUDA(c, cudaMallocAsync((void**)&B, sizeof(double) * m * m, c->stream));
     UWG_CUDA(c, cudaMemsetAsync(A, 0, sizeof(double) * m * m, c->stream));
     PMG_DIM_NC(k_pdense, nc, nblk(n, 64), g, st, A);
-    k_pdense_fix<<<1, 1024, 0, c->stream>>>(m, n, fix_checkerboard, A);
+    k_pdense_fix<<<1, 1024, 0, c->stream>>>(m, n, fix_checkerboard, g.res[0], g.res[1], A);
     int rc = uwg_ops_dense_invert(c, m, A, B);
     if (!rc) rc = uwg_ops_to_f32(c, m * m, B, inv32);
     cudaFreeAsync(A, c->stream);

@@ -55,6 +55,7 @@ struct Work {
     float* W0 = nullptr;                      // 1/sqrt(diag K) on level 0, 0 on Dirichlet dofs
     double Lmax[UWG_MAXLEV];
     float *pcg_r, *pcg_z, *pcg_p, *pcg_q, *bf_r, *bf_y, *bf_m, *bf_z, *bf_v1, *bf_v2;
+    float *pf1 = nullptr, *pf2 = nullptr;    // level-0 scratch of the level-1 Galerkin apply
     int lsolve_its = 0;
     double t_pc = 0.0, t_schur = 0.0;          // seconds in the Schur preconditioner / operator
     // CUDA graphs of the V-cycles (captured at setup, replayed by the Krylov loops)
@@ -105,13 +106,13 @@ int work_init(uwg_ctx* c, int restart) {
         w->ftil = dalloc<double>(c, nv); w->bvec = dalloc<double>(c, nv);
         w->p_tmp = dalloc<double>(c, np); w->p_tmp2 = dalloc<double>(c, np); w->hhat = dalloc<double>(c, np);
         w->coef = dalloc<double>(c, 512);
-        for (int l = 0; l < c->nlev && c->porder == 0; l++) {   // the BFBt pressure multigrid is dQ0 only
+        for (int l = 0; l < c->pnlev && c->porder == 0; l++) {   // the BFBt pressure multigrid is dQ0 only
             int64_t ne = uwg_pmg_ncomp(l) * c->lev[l].n_el;
             w->pv[l] = {dalloc<float>(c, ne), dalloc<float>(c, ne), dalloc<float>(c, ne), dalloc<float>(c, ne), dalloc<float>(c, ne)};
             w->pst[l] = dalloc<float>(c, uwg_pmg_stencil_size(c, l));
             w->pdg[l] = dalloc<float>(c, ne);
             w->Lmax[l] = 1.0;
-            if (l == c->nlev - 1) w->pcinv = dalloc<float>(c, ne * ne);
+            if (l == c->pnlev - 1) w->pcinv = dalloc<float>(c, ne * ne);
             if (!w->pst[l] || !w->pdg[l] || !w->pv[l].x) return uwg_set_error(c, UWG_ERR_CUDA, "out of device memory (pressure multigrid)");
         }
         w->W0 = dalloc<float>(c, nv);
@@ -123,6 +124,7 @@ int work_init(uwg_ctx* c, int restart) {
         w->bf_r = dalloc<float>(c, np); w->bf_y = dalloc<float>(c, np);
         w->bf_m = dalloc<float>(c, np); w->bf_z = dalloc<float>(c, np);
         w->bf_v1 = dalloc<float>(c, nv); w->bf_v2 = dalloc<float>(c, nv);
+        w->pf1 = dalloc<float>(c, np); w->pf2 = dalloc<float>(c, np);
         w->ns_t = dalloc<double>(c, np); w->ns_v = dalloc<double>(c, np); w->ns_one = dalloc<double>(c, np);
         w->ns_tmp = dalloc<double>(c, np);
     }
@@ -348,6 +350,16 @@ int velocity_solve(uwg_ctx* c, const SolveCfg& cfg, const double* b, double* x, 
 int papply(uwg_ctx* c, int l, const float* x, float* y) {
     Work* w = work_of(c);
     if (l == 0 && c->dim == 3) return uwg_pmg_apply0_mf(c, w->W0, x, y);
+    if (l == 1 && c->pnlev >= 3) {
+        // A_1 x = P^T (A_0 (P x)): the Galerkin product itself, applied through level 0.
+        // Its stored stencil (smooth-checkerboard block, 206 coefficients per cell) costs
+        // three times the bytes of the prolongation, level-0 apply and restriction.
+        int rc;
+        UWG_CUDA(c, cudaMemsetAsync(w->pf1, 0, sizeof(float) * c->lev[0].n_el, c->stream));
+        if ((rc = uwg_pmg_prolong_add(c, 1, x, w->pf1))) return rc;
+        if ((rc = papply(c, 0, w->pf1, w->pf2))) return rc;
+        return uwg_pmg_restrict(c, 1, w->pf2, y);
+    }
     return uwg_pmg_apply(c, l, w->pst[l], x, y);
 }
 
@@ -377,7 +389,7 @@ int pvcycle(uwg_ctx* c, int l, const float* b, float* x) {
     cudaStream_t s = c->stream;
     int64_t n = uwg_pmg_ncomp(l) * c->lev[l].n_el;
     int rc;
-    if (l == c->nlev - 1) return uwg_ops_dense_mv32(c, n, w->pcinv, b, x);
+    if (l == c->pnlev - 1) return uwg_ops_dense_mv32(c, n, w->pcinv, b, x);
     LevelVecs<float>& v = w->pv[l];
     LevelVecs<float>& vc = w->pv[l + 1];
     if ((rc = cheb_L(c, l, b, x, w->pdeg, true))) return rc;
@@ -667,10 +679,10 @@ int bfbt_setup(uwg_ctx* c) {
     cudaStream_t s = c->stream;
     int rc;
     if ((rc = uwg_ops_winv(c, 0, w->W0))) return rc;
-    for (int l = 0; l < c->nlev; l++) {
+    for (int l = 0; l < c->pnlev; l++) {
         if ((rc = uwg_pmg_stencil(c, l, w->W0, l ? w->pst[l - 1] : nullptr, w->pst[l]))) return rc;
         if ((rc = uwg_pmg_diag(c, l, w->pst[l], w->pdg[l]))) return rc;
-        if (l == c->nlev - 1) break;
+        if (l == c->pnlev - 1) break;
         // largest eigenvalue of D^-1 A by power iteration (Chebyshev interval)
         int64_t n = uwg_pmg_ncomp(l) * c->lev[l].n_el;
         LevelVecs<float>& v = w->pv[l];
@@ -692,7 +704,7 @@ int bfbt_setup(uwg_ctx* c) {
         UWG_CUDA(c, cudaStreamSynchronize(s));   // the host vector must outlive its copy
         w->Lmax[l] = lam;
     }
-    return uwg_pmg_dense_inverse(c, c->nlev - 1, w->pst[c->nlev - 1], w->cb_null ? 1 : 0, w->pcinv);
+    return uwg_pmg_dense_inverse(c, c->pnlev - 1, w->pst[c->pnlev - 1], w->cb_null ? 1 : 0, w->pcinv);
 }
 }  // namespace
 
