@@ -248,38 +248,24 @@ def run_gpu(args):
     torch.cuda.synchronize()
     clk = clocks.stop()
 
-    # plain FP64 solve on the same assembled system (one timed run)
+    # plain FP64 solve on the same assembled system (one timed run); the error of the
+    # mixed-precision solution against it (pressure modulo its constant null mode)
+    u_mix, p_mix = u.clone(), p.clone()
     fp64 = None
     if not args.skip_fp64 and mixed:
         x.copy_(x0); owner.copy_(owner0); off.copy_(off0); lst.copy_(lst0)
         t64 = {k: [] for k in ("map_dvc", "assemble", "solve")}
         st64 = solve_step(x, off, lst, eta0, body0, 0, t64)
+        pm, p64 = p_mix - p_mix.mean(), p - p.mean()
         fp64 = {"solve_s": t64["solve"][0], "pressure_its": st64["pressure_its"],
                 "velocity_total_its": st64["velocity_total_its"], "schur_pc_its": st64["schur_pc_its"],
-                "residual": st64["residual"]}
+                "residual": st64["residual"],
+                "mixed_vs_fp64": {"velocity": float(torch.linalg.norm(u_mix - u) / torch.linalg.norm(u)),
+                                  "pressure": float(torch.linalg.norm(pm - p64) / torch.linalg.norm(p64))}}
 
-    # end to end through host buffers
-    x_h = x0.cpu().pin_memory()
-    eta_h = eta0.cpu().pin_memory()
-    body_h = body0.cpu().pin_memory()
-    u_h = torch.empty(ctx.n_vdof, dtype=torch.float64).pin_memory()
-    p_h = torch.empty(ctx.n_pdof, dtype=torch.float64).pin_memory()
-    e2e_t = []
-    for it in range(1):
-        owner.copy_(owner0); off.copy_(off0); lst.copy_(lst0)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        x.copy_(x_h, non_blocking=True)
-        eta = eta_h.to(ctx.device, non_blocking=True)
-        body = body_h.to(ctx.device, non_blocking=True)
-        tt = {k: [] for k in ("map_dvc", "assemble", "solve")}
-        solve_step(x, off, lst, eta, body, mixed, tt)
-        u_h.copy_(u, non_blocking=True)
-        p_h.copy_(p, non_blocking=True)
-        torch.cuda.synchronize()
-        e2e_t.append(time.perf_counter() - t0)
-    h2d = x_h.numel() * 8 + eta_h.numel() * 8 + body_h.numel() * 8
-    d2h = u_h.numel() * 8 + p_h.numel() * 8
+    # end to end through the drop-in API from numpy host arrays, every step
+    e2e = e2e_api(args, cfg, x0.cpu().numpy(), eta0.cpu().numpy(), body0.cpu().numpy(), mixed)
+    del u_mix, p_mix
 
     # roofline of the dominant kernel class: the matrix-free K apply (FP32)
     kinfo = time_kernel_apply(ctx)
@@ -301,9 +287,8 @@ def run_gpu(args):
         "vs_baseline": None,
         "dtype": "f64" if not mixed else "f32+f64",
         "data": "synthetic",
-        "config": {"workload": workload_name(args.config), "mesh": "x".join(map(str, cfg["res"])) + (" Q2/dPc1" if cfg.get("order", 1) == 2 else " Q1/dQ0"),
-                   "particles": npart, "particles_per_cell": cfg["ppc"], "solve_mode": args.mode,
-                   "inputs_vs_L2": "particle arrays (%.1f GB) exceed the 129 MB L2" % (npart * 8 * (2 * dim + 1) / 1e9)},
+        "config": workload_config(args.config, npart),
+        "solve_mode": args.mode,
         "particles_per_s": npart / adv_s,
         "throughput": {"K_apply_mdof_per_s": ctx.n_vdof / kinfo["seconds"] / 1e6,
                        "stokes_solves_per_s": 1.0 / solve_s},
@@ -315,8 +300,7 @@ def run_gpu(args):
                    "backsolve_s": stats[-1]["backsolve_time"], "schur_pc_s": stats[-1]["schur_pc_time"],
                    "schur_op_s": stats[-1]["schur_op_time"]},
         "fp64_solve": fp64,
-        "e2e": {"value": float(np.mean(e2e_t)), "unit": "s/solve", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h)},
+        "e2e": e2e,
         "roofline": {"bound": "hbm", "kernel": kinfo["name"], "achieved": achieved, "peak": pk.get("hbm_gbs"),
                      "unit": "GB/s", "frac": achieved / pk.get("hbm_gbs", 6800.0),
                      "peak_source": "fallback" if pk.get("_fallback") else "measured",
@@ -326,8 +310,9 @@ def run_gpu(args):
     }
     if args.count_launches:
         line["gpu_launches"] = count_launches(ctx, x0, owner0, off0, lst0, eta0, body0, mixed, opts, u, p) * args.steps
+    line["pairings"] = gpu_pairings()
     if args.cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(args, quick=True)
+        line["cpu_baseline"] = cpu_baseline(args)
     return line
 
 
@@ -338,6 +323,114 @@ def workload_name(key):
             "rt2d_q2": "2D 256^2 Q2/dPc1 Rayleigh-Taylor, 40 ppc, viscosity x 10^U(-1,1), free-slip (config 2)",
             "conv3d_q2": "3D 96^3 Q2/dPc1 convection Stokes step, T = 1 - z + 1e-2 noise, viscosity exp(-9.2T), Ra=1e6, 30 ppc, free-slip (config 5 solve)",
             "conv3d_q2_small": "3D 32^3 Q2/dPc1 convection Stokes step, 30 ppc"}[key]
+
+
+def workload_config(key, npart=None):
+    """The `config` object of both arms' lines (identical keys and values)."""
+    import numpy as np
+    cfg = CONFIGS[key]
+    dim = cfg["dim"]
+    if npart is None:
+        npart = int(np.prod(cfg["res"])) * cfg["ppc"]
+    return {"workload": workload_name(key),
+            "mesh": "x".join(map(str, cfg["res"])) + (" Q2/dPc1" if cfg.get("order", 1) == 2 else " Q1/dQ0"),
+            "particles": int(npart), "particles_per_cell": cfg["ppc"],
+            "inputs_vs_L2": "particle arrays (%.1f GB) exceed the 129 MB L2" % (npart * 8 * (2 * dim + 1) / 1e9)}
+
+
+def e2e_api(args, cfg, x_h, eta_h, body_h, mixed):
+    """The same step through the drop-in API (uw.mesh / uw.swarm / uw.systems) from
+    numpy host arrays: every step sets the swarm's coordinates and the per-particle
+    viscosity and body force from host arrays, solves with Solver.solve() (PIC
+    mapping, DVC weights, assembly, BSSCR solve) and reads the velocity and
+    pressure fields back to host numpy arrays."""
+    import underworld2_gb300 as uw
+    dim = cfg["dim"]
+    mesh = uw.mesh.FeMesh_Cartesian(elementType="Q1/dQ0", elementRes=cfg["res"], minCoord=(0.0,) * dim,
+                                    maxCoord=(1.0,) * dim)
+    v = mesh.add_variable(nodeDofCount=dim)
+    pr = mesh.subMesh.add_variable(nodeDofCount=1)
+    swarm = uw.swarm.Swarm(mesh=mesh)
+    visc = swarm.add_variable(dataType="double", count=1)
+    force = swarm.add_variable(dataType="double", count=dim)
+    swarm.populate_using_layout(uw.swarm.layouts.PerCellRandomLayout(swarm=swarm, particlesPerCell=cfg["ppc"], seed=13))
+    axes = "IJK"[:dim]
+    walls = [mesh.specialSets["Min%s_VertexSet" % a] + mesh.specialSets["Max%s_VertexSet" % a] for a in axes]
+    bc = uw.conditions.DirichletCondition(variable=v, indexSetsPerDof=tuple(walls))
+    stokes = uw.systems.Stokes(velocityField=v, pressureField=pr, voronoi_swarm=swarm, conditions=[bc],
+                               fn_viscosity=visc, fn_bodyforce=force)
+    solver = uw.systems.Solver(stokes)
+    solver.set_inner_method("mixed" if mixed else "mg")
+    solver.set_inner_rtol(args.inner_rtol)
+    solver.set_outer_rtol(args.outer_rtol)
+    solver.options.mg.smooth_steps = 2
+    solver.options.scr.restart = 120
+    x_h = np.ascontiguousarray(x_h)
+    eta_h = np.ascontiguousarray(eta_h).reshape(-1)
+    body_h = np.ascontiguousarray(body_h).reshape(-1, dim)
+
+    def step():
+        t0 = time.perf_counter()
+        with swarm.deform_swarm():
+            swarm.data[:] = x_h
+        visc.data[:, 0] = eta_h
+        force.data[:] = body_h
+        solver.solve()
+        vel, p = v.data.copy(), pr.data.copy()
+        return time.perf_counter() - t0, vel, p
+
+    for _ in range(min(args.warmup, 1)):
+        step()
+    ts, out = [], None
+    for _ in range(args.steps):
+        t, vel, p = step()
+        ts.append(t)
+        out = (vel, p)
+    st = solver.get_stats()
+    return {"value": float(np.mean(ts)), "unit": "s/solve",
+            "h2d_bytes_per_step": int(x_h.nbytes + eta_h.nbytes + body_h.nbytes),
+            "d2h_bytes_per_step": int(out[0].nbytes + out[1].nbytes),
+            "api": "uw.systems.Stokes + uw.systems.Solver(...).solve(), swarm coordinates and swarm-variable "
+                   "data set from numpy every step, velocity/pressure .data read back",
+            "residual": float(st.residual), "pressure_its": int(st.pressure_its)}
+
+
+def gpu_pairings():
+    """GPU solves of the workloads the CPU baseline solves in full (see
+    oracle/cpu_reference.pairings): the 2D 64^2 sinker with both Schur
+    preconditioners and the 3D GRF workload on 32^3, plain FP64 and mixed."""
+    import torch
+    from underworld2_gb300._core import Context, rng_seed
+    out = {}
+    for key, res, pcs in (("sinker2d", (64, 64), ((1, "bfbt"), (0, "uzawa"))), ("grf3d", (32, 32, 32), ((1, "bfbt"),))):
+        cfg = dict(CONFIGS[key])
+        cfg["res"] = res
+        dim = cfg["dim"]
+        ctx = Context(dim, res, (0.0,) * dim, (1.0,) * dim)
+        ctx.set_bcs(freeslip_mask(ctx))
+        x, owner, off, lst, _ = ctx.layout_random(cfg["ppc"], rng_seed(13))
+        eta, body = material(cfg, x)
+        ip_xi = ctx.pic_map(x, off, lst)
+        ip_w = ctx.dvc_weights(off, ip_xi)
+        ctx.assemble(off, lst, ip_xi, ip_w, eta, body)
+        for pc, name in pcs:
+            for mixed in (0, 1):
+                best = None
+                for _ in range(3):
+                    u = ctx.zeros(ctx.n_vdof)
+                    p = ctx.zeros(ctx.n_pdof)
+                    torch.cuda.synchronize()
+                    t0 = time.perf_counter()
+                    st = ctx.solve(u, p, mixed=mixed, rtol=1e-8, inner_rtol=1e-10, outer_rtol=1e-9, smooth_steps=2,
+                                   restart=120, schur_pc=pc, max_outer=2000)
+                    torch.cuda.synchronize()
+                    t = time.perf_counter() - t0
+                    best = t if best is None else min(best, t)
+                out["%s_%s_%s_%s" % (key, "x".join(map(str, res)), name, "mixed" if mixed else "fp64")] = {
+                    "solve_s": best, "pressure_its": st["pressure_its"], "velocity_total_its": st["velocity_total_its"],
+                    "schur_pc_its": st["schur_pc_its"], "residual": st["residual"]}
+        del ctx
+    return out
 
 
 def dram_traffic(kernel_name, config):
@@ -718,18 +811,31 @@ def count_launches(ctx, x0, owner0, off0, lst0, eta0, body0, mixed, opts, u, p):
 # ---------------------------------------------------------------------------
 # CPU arm: the oracle (reference algorithms restated in C) on host cores
 # ---------------------------------------------------------------------------
-def cpu_baseline(args, quick=False):
+def cpu_baseline(args):
+    """The CPU port on this workload, one bounded sample (the `cpu_baseline` of our line)."""
     from oracle import cpu_reference
     try:
-        return cpu_reference.measure(CONFIGS[args.config], workload_name(args.config), quick=quick)
+        return cpu_reference.measure(CONFIGS[args.config], workload_name(args.config), steps=1)
     except NotImplementedError as e:
         return {"unavailable": str(e)}
 
 
 def run_reference(args):
-    res = cpu_baseline(args)
-    if "unavailable" in res:
-        return {"impl": "reference", "unavailable": res["unavailable"]}
+    """The reference arm: the CPU port of the path on all host cores (the reference
+    itself cannot be built here), set up once at full size, then `--warmup` +
+    `--steps` bounded samples; plus full CPU solves of the paired workloads."""
+    from oracle import cpu_reference
+    try:
+        b = cpu_reference.CPUBaseline(CONFIGS[args.config], workload_name(args.config))
+    except NotImplementedError as e:
+        return {"impl": "reference", "unavailable": str(e)}
+    for _ in range(args.warmup):
+        b.step()
+    t0 = time.perf_counter()
+    samples = [b.step() for _ in range(args.steps)]
+    wall = time.perf_counter() - t0
+    res = b.result(samples)
+    res["pairings"] = cpu_reference.pairings(CONFIGS)
     line = {
         "impl": "reference",
         "metric": "Stokes solve time @1e-8 resid (learned+FP32 vs FP64 GPU); particles/s advected",
@@ -743,7 +849,8 @@ def run_reference(args):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": workload_name(args.config)},
+        "ms_per_step": 1e3 * wall / max(args.steps, 1),
+        "config": workload_config(args.config),
         "particles_per_s": res.get("particles_per_s"),
         "cpu_baseline": res,
         "e2e": {"value": res["value"], "unit": "s/solve", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

@@ -78,6 +78,8 @@ def lib():
             "uwo_sys_set_bc": (None, [_P, _P, _P]),
             "uwo_sys_assemble_points": (None, [_P, _P, _P, _P, _P, _P, _P]),
             "uwo_sys_finish": (None, [_P]),
+            "uwo_sys_set_schur_pc": (None, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_double]),
+            "uwo_sys_time_iterations": (None, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P]),
             "uwo_sys_applyK": (None, [_P, ctypes.c_int, _P, _P]),
             "uwo_sys_solve": (ctypes.c_int, [_P, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                              ctypes.c_int, _P, _P, _P]),
@@ -312,12 +314,23 @@ class StokesCPU:
         values = None if values is None else np.ascontiguousarray(values, np.float64)
         self.mesh.L.uwo_sys_set_bc(self.h, _p(mask), _p(values))
 
+    def set_schur_pc(self, pc, deg=2, rtol=3e-2):
+        """0: the assembled Uzawa term (the reference's "uw"); 1: weighted scaled
+        BFBt with the GPU library's pressure multigrid.  Takes effect at assemble."""
+        self.mesh.L.uwo_sys_set_schur_pc(self.h, int(pc), int(deg), float(rtol))
+
     def assemble(self, off, lst, ip_xi, ip_w, eta, body):
         a = [np.ascontiguousarray(off, np.int32), np.ascontiguousarray(lst, np.int32),
              np.ascontiguousarray(ip_xi, np.float64), np.ascontiguousarray(ip_w, np.float64),
              np.ascontiguousarray(eta, np.float64), np.ascontiguousarray(body, np.float64)]
         self.mesh.L.uwo_sys_assemble_points(self.h, *[_p(x) for x in a])
         self.mesh.L.uwo_sys_finish(self.h)
+
+    def time_iterations(self, n_vel=2, n_l=2, deg=2):
+        """(seconds per velocity MG-CG iteration, seconds per pressure-Laplacian CG iteration)."""
+        out = np.zeros(2)
+        self.mesh.L.uwo_sys_time_iterations(self.h, int(n_vel), int(n_l), int(deg), _p(out))
+        return float(out[0]), float(out[1])
 
     def applyK(self, x, level=0):
         x = np.ascontiguousarray(x, np.float64)
@@ -333,4 +346,4 @@ class StokesCPU:
                                        _p(u), _p(p), _p(st))
         return u, p, {"rc": rc, "pressure_its": int(st[0]), "velocity_presolve_its": int(st[1]),
                       "velocity_pressuresolve_its": int(st[2]), "velocity_backsolve_its": int(st[3]),
-                      "residual": float(st[4])}
+                      "residual": float(st[4]), "schur_pc_its": int(st[5])}

@@ -1,27 +1,46 @@
 """CPU baseline of the PIC Stokes path (TEST/BENCHMARK INFRASTRUCTURE).
 
 Times the oracle -- the reference's algorithms restated in C (uwo.c) plus the
-CPU BSSCR solver (uwo_solve.c) -- with OpenMP on all host cores, on a bounded
-sample of the benchmark workload, and extrapolates to the full size:
+CPU BSSCR solver (uwo_solve.c) -- with OpenMP on all host cores.  The solver
+runs the GPU library's algorithm: velocity solves by multigrid-preconditioned
+CG (Chebyshev degree 2), flexible GMRES on the Schur complement with the
+weighted scaled BFBt preconditioner and its pressure multigrid (the CPU port
+in uwo_solve.c), FP64 vectors.
 
-* coincident mapping + DVC weights: a contiguous sample of elements, scaled
-  by the element count;
-* PIC assembly and owner update: the full workload;
-* Stokes solve: (CPU time of one multigrid-preconditioned CG iteration on the
-  full mesh) x (inner iterations of the same BSSCR algorithm run to the same
-  tolerance on an 8^d mesh of the same workload).  The outer iteration count
-  of the reference's Schur preconditioner grows with the resolution, so this
-  figure is a lower bound of the full-size CPU solve and is labelled so;
-* RK2 advection: a sample of particles, scaled by the particle count.
+Per workload (``CPUBaseline``), set up once at full size, then per step a
+bounded sample:
 
-Every extrapolated figure is labelled in the returned dict.
+* coincident mapping + DVC weights: a contiguous slice of elements, scaled by
+  the element count;
+* PIC assembly + solver setup: the full mesh, once (its time is reported);
+* Stokes solve: a converged solve where the mesh is small enough to finish in
+  seconds; otherwise (seconds per velocity MG-CG iteration on the full mesh) x
+  (velocity iterations) + (seconds per pressure-Laplacian CG iteration on the
+  full mesh) x (pressure-Laplacian iterations), the iteration counts taken
+  from the GPU's plain FP64 solve of the same algorithm and workload
+  (``GPU_FP64_ITS``), and labelled so;
+* RK2 advection: a sample of particles, scaled; owner update on all.
+
+``pairings()`` runs full converged CPU solves of the smaller workloads with
+both Schur preconditioners, for side-by-side comparison with the same GPU
+solves.
 """
+import ctypes
 import os
 import time
 
 import numpy as np
 
 import oracle
+
+# Iteration counts of the GPU's plain FP64 solve (weighted BFBt, pressure-
+# Laplacian tolerance 3e-2, smoother degree 2) of the 3D 128^3 GRF workload,
+# measured by bench.py on a GB300 (its "fp64_solve" entry): 25 outer, 360
+# velocity MG-CG, 1676 pressure-Laplacian CG iterations.
+GPU_FP64_ITS = {(3, (128, 128, 128)): {"pressure_its": 25, "velocity_total_its": 360, "schur_pc_its": 1676}}
+
+FULL_SOLVE_MAX_EL = 70000
+SMOOTH = 2
 
 
 def _threads():
@@ -30,7 +49,6 @@ def _threads():
 
 def _material(kind, x, dim):
     import torch
-    sys_path_bench = None
     if kind == "grf":
         import importlib
         bench = importlib.import_module("bench")
@@ -62,109 +80,150 @@ def _setup(cfg, res):
     return m, x, eta, body
 
 
-def _solve_counts(cfg, res):
-    """Converged CPU BSSCR on a coarser mesh: iteration counts."""
+def _grow(tbl, cnt, cap=64):
+    t = np.full((tbl.shape[0], cap), -1, np.int32)
+    t[:, : tbl.shape[1]] = tbl
+    return t
+
+
+def solve_full(cfg, res, schur_pc):
+    """A converged CPU solve (to a 1e-8 relative residual) of the workload on `res`."""
     m, x, eta, body = _setup(cfg, res)
     tbl, cnt, _ = m.initial_tables(cfg["ppc"], cfg["ppc"])
     ip_xi, ip_w = m.pic_map(x, tbl, cnt)
     s = oracle.StokesCPU(m)
     s.set_bc(_mask(m))
+    s.set_schur_pc(schur_pc, SMOOTH)
     off = np.concatenate([[0], np.cumsum(cnt)]).astype(np.int32)
     lst = tbl.ravel().astype(np.int32)
-    s.assemble(off, lst, ip_xi[lst], ip_w[lst], eta, body)
     t0 = time.perf_counter()
-    u, p, st = s.solve(inner_rtol=1e-10, outer_rtol=1e-9)
-    st["seconds"] = time.perf_counter() - t0
+    s.assemble(off, lst, ip_xi[lst], ip_w[lst], eta, body)
+    t_asm = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    u, p, st = s.solve(inner_rtol=1e-10, outer_rtol=1e-9, max_outer=2000, deg=SMOOTH)
+    st.update(solve_s=time.perf_counter() - t0, assemble_s=t_asm)
     return st
 
 
-def measure(cfg, workload, quick=False):
-    if cfg.get("order", 1) != 1:
-        raise NotImplementedError("the CPU solver port covers Q1/dQ0 only")
-    dim, ppc = cfg["dim"], cfg["ppc"]
-    res = cfg["res"]
-    L = oracle.lib()
-    out = {"kind": "port", "cores": _threads(), "workload": workload}
-    t_all = time.perf_counter()
-    m, x, eta, body = _setup(cfg, res)
-    n_el, npart = m.n_el, len(x)
-    tbl, cnt, owner = m.initial_tables(ppc, ppc)
+class CPUBaseline:
+    """The CPU port on one workload, set up once; `step()` times one bounded sample."""
 
-    # 1. mapping + DVC on a sample of elements
-    frac = 1.0 if n_el <= 8192 else 1.0 / 256
-    n_s = max(1, int(n_el * frac))
-    ip_xi = np.zeros((npart, dim))
-    ip_w = np.zeros(npart)
-    import ctypes
-    p = lambda a: ctypes.c_void_p(a.ctypes.data)
-    t0 = time.perf_counter()
-    L.uwo_pic_map(ctypes.byref(m._c), *m._ax(), p(x), p(tbl), p(cnt), tbl.shape[1], 0, n_s, 15, p(ip_xi), p(ip_w))
-    t_map = (time.perf_counter() - t0) * n_el / n_s
-    if n_s < n_el:   # the rest of the weights for assembly (untimed)
-        L.uwo_pic_map(ctypes.byref(m._c), *m._ax(), p(x), p(tbl), p(cnt), tbl.shape[1], n_s, n_el, 15,
-                      p(ip_xi), p(ip_w))
-
-    # 2. assembly + solver setup on the full mesh
-    s = oracle.StokesCPU(m)
-    s.set_bc(_mask(m))
-    off = np.concatenate([[0], np.cumsum(cnt)]).astype(np.int32)
-    lst = tbl.ravel().astype(np.int32)
-    xi_s, w_s = ip_xi[lst], ip_w[lst]
-    t0 = time.perf_counter()
-    s.assemble(off, lst, xi_s, w_s, eta, body)
-    t_asm = time.perf_counter() - t0
-
-    # 3. solve: per-iteration cost on the full mesh x converged iteration count
-    if n_el <= 70000:
+    def __init__(self, cfg, workload):
+        if cfg.get("order", 1) != 1:
+            raise NotImplementedError("the CPU solver port covers Q1/dQ0 only")
+        self.cfg, self.workload = cfg, workload
+        dim, ppc, res = cfg["dim"], cfg["ppc"], tuple(cfg["res"])
+        self.res = res
+        t_all = time.perf_counter()
+        self.m, self.x, eta, body = _setup(cfg, res)
+        m = self.m
+        self.n_el, self.npart = m.n_el, len(self.x)
+        self.tbl, self.cnt, self.owner = m.initial_tables(ppc, ppc)
+        self.frac = 1.0 if self.n_el <= 8192 else 1.0 / 256
+        self.n_s = max(1, int(self.n_el * self.frac))
+        self.ip_xi = np.zeros((self.npart, dim))
+        self.ip_w = np.zeros(self.npart)
+        self._map(0, self.n_el)
+        self.s = oracle.StokesCPU(m)
+        self.s.set_bc(_mask(m))
+        self.s.set_schur_pc(1, SMOOTH)
+        off = np.concatenate([[0], np.cumsum(self.cnt)]).astype(np.int32)
+        lst = self.tbl.ravel().astype(np.int32)
         t0 = time.perf_counter()
-        u, pr, st = s.solve(inner_rtol=1e-10, outer_rtol=1e-9)
-        t_solve = time.perf_counter() - t0
-        solve_note = "full converged solve"
-        its = st
-    else:
-        coarse = tuple(min(8, r) for r in res)
-        its = _solve_counts(cfg, coarse)
-        n_it = its["velocity_presolve_its"] + its["velocity_pressuresolve_its"] + its["velocity_backsolve_its"]
+        self.s.assemble(off, lst, self.ip_xi[lst], self.ip_w[lst], eta, body)
+        self.t_asm = time.perf_counter() - t0
+        self.full = None
+        if self.n_el <= FULL_SOLVE_MAX_EL:
+            t0 = time.perf_counter()
+            u, p, st = self.s.solve(inner_rtol=1e-10, outer_rtol=1e-9, max_outer=2000, deg=SMOOTH)
+            st["solve_s"] = time.perf_counter() - t0
+            self.full = st
+        elif (dim, res) not in GPU_FP64_ITS:
+            raise NotImplementedError("no GPU iteration counts recorded for %s" % (res,))
+        self.vel = np.zeros(m.n_nodes * dim)
+        self.vel[::dim] = 1e-3
+        self.n_p = self.npart if self.npart <= 2_000_000 else self.npart // 16
+        self.setup_s = time.perf_counter() - t_all
+
+    def _map(self, e0, e1):
+        p = lambda a: ctypes.c_void_p(a.ctypes.data)
+        m = self.m
+        oracle.lib().uwo_pic_map(ctypes.byref(m._c), *m._ax(), p(self.x), p(self.tbl), p(self.cnt),
+                                 self.tbl.shape[1], e0, e1, 15, p(self.ip_xi), p(self.ip_w))
+
+    def step(self):
+        """One bounded sample: mapping + DVC on a slice, one velocity and two
+        pressure-Laplacian iterations on the full mesh, RK2 on a sample."""
         t0 = time.perf_counter()
-        u, pr, st = s.solve(inner_rtol=1e-10, outer_rtol=1e-9, max_inner=3, max_outer=1)
-        dt = time.perf_counter() - t0
-        it_done = st["velocity_presolve_its"] + st["velocity_pressuresolve_its"] + st["velocity_backsolve_its"]
-        t_it = dt / max(it_done, 1)
-        t_solve = n_it * t_it
-        conv = "converged" if its.get("rc", 0) == 0 else "iteration-capped"
-        solve_note = ("solve extrapolated as a LOWER BOUND: %.3f s per MG-CG iteration on the full mesh x %d "
-                      "iterations of the %s %s solve (outer iterations of this preconditioner grow with "
-                      "resolution)" % (t_it, n_it, conv, "x".join(map(str, coarse))))
+        self._map(0, self.n_s)
+        t_map = (time.perf_counter() - t0) * self.n_el / self.n_s
+        tv, tl = self.s.time_iterations(1, 2, SMOOTH)
+        xs = self.x[: self.n_p].copy()
+        t0 = time.perf_counter()
+        self.m.rk2(self.vel, 0.1 / max(self.res), xs)
+        t_rk2 = (time.perf_counter() - t0) * self.npart / self.n_p
+        return {"map_dvc": t_map, "t_vel_it": tv, "t_l_it": tl, "rk2": t_rk2}
 
-    # 4. RK2 on a sample of particles + owner update on all
-    vel = np.zeros(m.n_nodes * dim)
-    vel[::dim] = 1e-3
-    n_p = npart if npart <= 2_000_000 else npart // 16
-    xs = x[:n_p].copy()
-    t0 = time.perf_counter()
-    m.rk2(vel, 0.1 / max(res), xs)
-    t_rk2 = (time.perf_counter() - t0) * npart / n_p
-    x2 = x.copy()
-    x2[:n_p] = xs
-    t0 = time.perf_counter()
-    m.update_owners(x2, owner, _grow(tbl, cnt), cnt)
-    t_mig = time.perf_counter() - t0
+    def result(self, samples):
+        med = {k: float(np.median([s[k] for s in samples])) for k in samples[0]}
+        dim = self.cfg["dim"]
+        if self.full is not None:
+            t_solve = self.full["solve_s"]
+            its = {k: v for k, v in self.full.items() if k not in ("rc", "solve_s")}
+            note = "full converged CPU solve"
+        else:
+            its = GPU_FP64_ITS[(dim, self.res)]
+            t_solve = med["t_vel_it"] * its["velocity_total_its"] + med["t_l_it"] * its["schur_pc_its"]
+            note = ("solve EXTRAPOLATED: %.3f s per velocity MG-CG iteration and %.4f s per pressure-Laplacian CG "
+                    "iteration, measured on the full mesh, x the %d and %d iterations of the GPU's plain FP64 "
+                    "solve of the same algorithm (weighted BFBt) and workload"
+                    % (med["t_vel_it"], med["t_l_it"], its["velocity_total_its"], its["schur_pc_its"]))
+        # owner update of all particles after the sampled RK2 move
+        x2 = self.x.copy()
+        xs = self.x[: self.n_p].copy()
+        self.m.rk2(self.vel, 0.1 / max(self.res), xs)
+        x2[: self.n_p] = xs
+        t0 = time.perf_counter()
+        self.m.update_owners(x2, self.owner.copy(), _grow(self.tbl, self.cnt), self.cnt.copy())
+        t_mig = time.perf_counter() - t0
+        total = med["map_dvc"] + self.t_asm + t_solve
+        return {
+            "kind": "port", "cores": _threads(), "workload": self.workload,
+            "value": total, "unit": "s/solve",
+            "particles_per_s": self.npart / (med["rk2"] + t_mig),
+            "phases_s": {"map_dvc": med["map_dvc"], "assemble": self.t_asm, "solve": t_solve, "rk2": med["rk2"],
+                         "migrate": t_mig},
+            "per_iteration_s": {"velocity_mg_cg": med["t_vel_it"], "pressure_laplacian_cg": med["t_l_it"]},
+            "solver_its": its,
+            "schur_pc": "weighted scaled BFBt (the GPU library's algorithm, CPU port)",
+            "sample": ("map+DVC on %d of %d elements (scaled); assembly and solver setup on the full mesh; %s; "
+                       "RK2 on %d of %d particles (scaled), owner update on all" %
+                       (self.n_s, self.n_el, note, self.n_p, self.npart)),
+            "setup_s": self.setup_s,
+        }
 
-    total = t_map + t_asm + t_solve
-    out.update({
-        "value": total,
-        "unit": "s/solve",
-        "particles_per_s": npart / (t_rk2 + t_mig),
-        "phases_s": {"map_dvc": t_map, "assemble": t_asm, "solve": t_solve, "rk2": t_rk2, "migrate": t_mig},
-        "sample": ("map+DVC on %d of %d elements (scaled); assembly and owner update on all %d particles; %s; "
-                   "RK2 on %d of %d particles (scaled)" % (n_s, n_el, npart, solve_note, n_p, npart)),
-        "solver_its": {k: v for k, v in its.items() if k != "rc"},
-        "wall_s": time.perf_counter() - t_all,
-    })
+
+def pairings(configs):
+    """Full converged CPU solves for side-by-side comparison: the 2D 64^2 sinker with
+    both Schur preconditioners and the 3D GRF workload on a 32^3 mesh with BFBt."""
+    out = {}
+    s2 = dict(configs["sinker2d"])
+    for pc, name in ((1, "bfbt"), (0, "uzawa")):
+        st = solve_full(s2, tuple(s2["res"]), pc)
+        out["sinker2d_64x64_%s" % name] = _brief(st)
+    g = dict(configs["grf3d"])
+    st = solve_full(g, (32, 32, 32), 1)
+    out["grf3d_32x32x32_bfbt"] = _brief(st)
     return out
 
 
-def _grow(tbl, cnt, cap=64):
-    t = np.full((tbl.shape[0], cap), -1, np.int32)
-    t[:, : tbl.shape[1]] = tbl
-    return t
+def _brief(st):
+    return {"solve_s": st["solve_s"], "assemble_s": st.get("assemble_s"), "pressure_its": st["pressure_its"],
+            "velocity_total_its": st["velocity_presolve_its"] + st["velocity_pressuresolve_its"] +
+            st["velocity_backsolve_its"], "schur_pc_its": st.get("schur_pc_its", 0), "residual": st["residual"]}
+
+
+def measure(cfg, workload, steps=1):
+    """Set up and time `steps` samples (the bench's cpu_baseline entry)."""
+    b = CPUBaseline(cfg, workload)
+    return b.result([b.step() for _ in range(max(1, steps))])
