@@ -214,17 +214,27 @@ def run_gpu(args):
         times["solve"].append(e[2].elapsed_time(e[3]) / 1e3)
         return st
 
-    def advect_step(x, owner, off, lst, times):
-        e = [ev() for _ in range(3)]
-        e[0].record()
-        dt = ctx.max_dt(u)
-        ctx.rk2(x, u, dt)
-        e[1].record()
-        ctx.update_owners(x, owner, off, lst)
-        e[2].record()
+    def advect(n_steps, times):
+        """Successive RK2 steps at the maximum stable dt with the owner update
+        (migration between elements) after each, particles stored in FP32 with the
+        arithmetic in FP64, from the reset swarm through the solved velocity field."""
+        x32 = x0.to(torch.float32)
+        own, of, ls = owner0.clone(), off0.clone(), lst0.clone()
         torch.cuda.synchronize()
-        times["rk2"].append(e[0].elapsed_time(e[1]) / 1e3)
-        times["migrate"].append(e[1].elapsed_time(e[2]) / 1e3)
+        for _ in range(n_steps):
+            e = [ev() for _ in range(3)]
+            e[0].record()
+            dt = ctx.max_dt(u)
+            ctx.rk2(x32, u, dt)
+            e[1].record()
+            ctx.update_owners(x32, own, of, ls)
+            e[2].record()
+            torch.cuda.synchronize()
+            times["rk2"].append(e[0].elapsed_time(e[1]) / 1e3)
+            times["migrate"].append(e[1].elapsed_time(e[2]) / 1e3)
+        moved = int((own != owner0).sum())
+        del x32
+        return moved
 
     mixed = 0 if args.mode == "fp64" else 1
     # state copies so every step starts from the same swarm
@@ -233,7 +243,7 @@ def run_gpu(args):
     for _ in range(args.warmup):
         x.copy_(x0); owner.copy_(owner0); off.copy_(off0); lst.copy_(lst0)
         solve_step(x, off, lst, eta0, body0, mixed, warm)
-        advect_step(x, owner, off, lst, warm)
+    advect(3, warm)
 
     clocks = Clocks()
     clocks.start()
@@ -244,8 +254,9 @@ def run_gpu(args):
         x.copy_(x0); owner.copy_(owner0); off.copy_(off0); lst.copy_(lst0)
         torch.cuda.synchronize()
         stats.append(solve_step(x, off, lst, eta0, body0, mixed, times))
-        advect_step(x, owner, off, lst, times)
     torch.cuda.synchronize()
+    # advection of the workload: ten successive steps (FP32 storage, FP64 arithmetic)
+    moved = advect(10, times)
     clk = clocks.stop()
 
     # plain FP64 solve on the same assembled system (one timed run); the error of the
@@ -273,7 +284,7 @@ def run_gpu(args):
     achieved = kinfo["bytes"] / kinfo["seconds"] / 1e9
     per_step = [times["map_dvc"][i] + times["assemble"][i] + times["solve"][i] for i in range(args.steps)]
     solve_s = float(np.mean(per_step))
-    adv_s = float(np.mean([times["rk2"][i] + times["migrate"][i] for i in range(args.steps)]))
+    adv_s = float(np.mean([times["rk2"][i] + times["migrate"][i] for i in range(len(times["rk2"]))]))
     line = {
         "metric": "Stokes solve time @1e-8 resid (learned+FP32 vs FP64 GPU); particles/s advected",
         "value": solve_s,
@@ -281,7 +292,7 @@ def run_gpu(args):
         "n_gpus": 1,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": 1e3 * (solve_s + adv_s),
+        "ms_per_step": 1e3 * solve_s,
         "higher_is_better": False,
         "scaling": "weak",
         "vs_baseline": None,
@@ -290,6 +301,8 @@ def run_gpu(args):
         "config": workload_config(args.config, npart),
         "solve_mode": args.mode,
         "particles_per_s": npart / adv_s,
+        "advection": {"steps": 10, "storage": "FP32 coordinates, FP64 arithmetic", "s_per_step": adv_s,
+                      "particles_changed_element": moved},
         "throughput": {"K_apply_mdof_per_s": ctx.n_vdof / kinfo["seconds"] / 1e6,
                        "stokes_solves_per_s": 1.0 / solve_s},
         "phases_s": {k: float(np.mean(v)) for k, v in times.items()},
@@ -309,7 +322,8 @@ def run_gpu(args):
         "clocks": clk,
     }
     if args.count_launches:
-        line["gpu_launches"] = count_launches(ctx, x0, owner0, off0, lst0, eta0, body0, mixed, opts, u, p) * args.steps
+        n_solve, n_adv = count_launches(ctx, x0, owner0, off0, lst0, eta0, body0, mixed, opts, u, p)
+        line["gpu_launches"] = n_solve * args.steps + n_adv * 10
     line["pairings"] = gpu_pairings()
     if args.cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args)
@@ -502,6 +516,39 @@ def run_kernel(args):
     torch.cuda.synchronize()
     print(json.dumps({"kernel": args.kernel, "config": args.config, "reps": args.reps,
                       "ms_per_launch": s.elapsed_time(e) / args.reps}))
+
+
+def run_rk2(args):
+    """`--reps` RK2 steps (FP32 coordinate storage, FP64 arithmetic) through a
+    cellular velocity field on the workload's mesh, with --kernel-ppc particles per
+    element (the target of the RK2 ncu capture): prints ms per step and particles/s."""
+    import torch
+    from underworld2_gb300._core import Context, rng_seed
+    cfg = CONFIGS[args.config]
+    dim = cfg["dim"]
+    ctx = Context(dim, cfg["res"], (0.0,) * dim, (1.0,) * dim)
+    x, owner, off, lst, _ = ctx.layout_random(args.kernel_ppc or cfg["ppc"], rng_seed(13))
+    xyz = torch.stack(torch.meshgrid(*[torch.tensor(a, device=ctx.device) for a in reversed(ctx.axes)],
+                                     indexing="ij")[::-1], dim=-1).reshape(-1, dim)
+    sn, cs = torch.sin(torch.pi * xyz), torch.cos(torch.pi * xyz)
+    vel = torch.zeros_like(xyz)
+    vel[:, 0] = sn[:, 0] * cs[:, dim - 1]
+    vel[:, dim - 1] = -cs[:, 0] * sn[:, dim - 1]
+    vel = vel.contiguous().reshape(-1)
+    dt = ctx.max_dt(vel)
+    x32 = x.to(torch.float32)
+    del x
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ctx.rk2(x32, vel, dt)
+    torch.cuda.synchronize()
+    s.record()
+    for _ in range(args.reps):
+        ctx.rk2(x32, vel, dt)
+    e.record()
+    torch.cuda.synchronize()
+    ms = s.elapsed_time(e) / args.reps
+    print(json.dumps({"kernel": "rk2", "config": args.config, "particles": x32.shape[0], "reps": args.reps,
+                      "ms_per_step": ms, "particles_per_s": x32.shape[0] / (ms / 1e3)}))
 
 
 def run_advdiff(args):
@@ -784,30 +831,39 @@ def run_profile_solve(args):
 
 
 def count_launches(ctx, x0, owner0, off0, lst0, eta0, body0, mixed, opts, u, p):
-    """Kernels launched by libuwg in one step, counted with the CUDA activity profiler."""
+    """Kernels launched by libuwg in one solve step and in one advection step,
+    counted with the CUDA activity profiler."""
     import torch
     from torch.profiler import ProfilerActivity, profile
     x, owner, off, lst = x0.clone(), owner0.clone(), off0.clone(), lst0.clone()
+    # libuwg's kernels are named k_* / vk_*, some inside an anonymous namespace
+    # ("void (anonymous namespace)::k_applyK_q2_3d<...>(...)")
+    ours = re.compile(r"(^|[\s:])v?k_\w")
+
+    def count(prof):
+        n = 0
+        for evt in prof.events():
+            name = evt.name or ""
+            if evt.device_type.name == "CUDA" and (ours.search(name.split("(")[0] if "::" not in name else name)
+                                                    or "uwg" in name):
+                n += 1
+        return n
+
     with profile(activities=[ProfilerActivity.CUDA]) as prof:
         ip_xi = ctx.pic_map(x, off, lst)
         ip_w = ctx.dvc_weights(off, ip_xi)
         ctx.assemble(off, lst, ip_xi, ip_w, eta0, body0)
         u.zero_(); p.zero_()
         ctx.solve(u, p, mixed=mixed, **opts)
-        dt = ctx.max_dt(u)
-        ctx.rk2(x, u, dt)
-        ctx.update_owners(x, owner, off, lst)
         torch.cuda.synchronize()
-    # libuwg's kernels are named k_* / vk_*, some inside an anonymous namespace
-    # ("void (anonymous namespace)::k_applyK_q2_3d<...>(...)")
-    ours = re.compile(r"(^|[\s:])v?k_\w")
-    n = 0
-    for evt in prof.events():
-        name = evt.name or ""
-        if evt.device_type.name == "CUDA" and (ours.search(name.split("(")[0] if "::" not in name else name)
-                                                or "uwg" in name):
-            n += 1
-    return n
+    n_solve = count(prof)
+    x32 = x0.to(torch.float32)
+    with profile(activities=[ProfilerActivity.CUDA]) as prof:
+        dt = ctx.max_dt(u)
+        ctx.rk2(x32, u, dt)
+        ctx.update_owners(x32, owner, off, lst)
+        torch.cuda.synchronize()
+    return n_solve, count(prof)
 
 
 # ---------------------------------------------------------------------------
@@ -873,7 +929,7 @@ def main():
     ap.add_argument("--schur-pc", type=int, default=1, help="0: Uzawa S^ (reference), 1: scaled BFBt")
     ap.add_argument("--bfbt-rtol", type=float, default=3e-2)
     ap.add_argument("--bfbt-its", type=int, default=0, help="> 0: fixed CG iterations per BFBt L-solve")
-    ap.add_argument("--kernel", choices=["applyK32", "applyK64", "advdiff", "slcn"],
+    ap.add_argument("--kernel", choices=["applyK32", "applyK64", "advdiff", "slcn", "rk2"],
                     help="only launch one operator kernel, or time SUPG / SLCN advection-diffusion steps (profiling)")
     ap.add_argument("--kernel-ppc", type=int, default=0)
     ap.add_argument("--profile-solve", action="store_true", help="one untimed solve (profiling target)")
@@ -892,6 +948,9 @@ def main():
     args = ap.parse_args()
     if args.kernel == "advdiff":
         run_advdiff(args)
+        return
+    if args.kernel == "rk2":
+        run_rk2(args)
         return
     if args.kernel == "slcn":
         run_slcn(args)

@@ -253,6 +253,16 @@ int uwg_apply_Gt(uwg_ctx* ctx, const double* u, double* q);
 int uwg_rk2_advect(uwg_ctx* ctx, int64_t np, double dt, const double* vel, double* x,
                    int64_t* n_fallback_h, int64_t* n_failed_h);
 
+/* uwg_rk2_advect / uwg_update_owners for particle coordinates stored in FP32:
+ * each stored coordinate is widened to FP64, the update is computed in FP64 as
+ * above, and the new position is rounded to FP32 once when stored (the same
+ * reference calls; the storage precision is this library's option for large
+ * swarms). */
+int uwg_rk2_advect_f32(uwg_ctx* ctx, int64_t np, double dt, const double* vel, float* x,
+                       int64_t* n_fallback_h, int64_t* n_failed_h);
+int uwg_update_owners_f32(uwg_ctx* ctx, int64_t np, const float* x, int32_t* owner,
+                          int32_t* cell_offsets, int32_t* cell_list, int64_t* n_lost_h);
+
 /* Velocity at arbitrary points (Mesh_SearchElements + Newton + basis);
  * points outside get NaN.  Replaces FieldVariable_InterpolateValueAt
  * (L/StgFEM/Discretisation/src/FeVariable.c:389-403). */

@@ -290,3 +290,39 @@ def test_K32_tiled_apply_many_tiles(gpu, res):
     assert np.abs(y32 - y64).max() <= 2e-5 * np.abs(y64).max()
     fixed = mask.ravel() != 0
     np.testing.assert_array_equal(y64[fixed], xv[fixed])
+
+
+@pytest.mark.parametrize("dim,res,ppc", [(2, (16, 16), 20), (3, (6, 5, 4), 8)])
+def test_rk2_fp32_storage_ten_steps(gpu, dim, res, ppc):
+    """FP32 particle storage with FP64 arithmetic: ten successive RK2 steps with
+    owner updates (migration between elements).  Each GPU step equals the
+    oracle's FP64 step from the same stored (widened) coordinates, rounded once
+    to FP32; owners and cell tables equal the oracle's after every step."""
+    c, m, (x, owner, off, lst), xo, eta, body, mask = _circle_problem(dim, res, ppc)
+    ip_xi = c.pic_map(x, off, lst)
+    ip_w = c.dvc_weights(off, ip_xi)
+    c.set_bcs(torch.tensor(mask, device="cuda"))
+    c.assemble(off, lst, ip_xi, ip_w, torch.tensor(eta, device="cuda"), torch.tensor(body, device="cuda"))
+    u = c.zeros(m.n_nodes * dim)
+    p = c.zeros(m.n_el)
+    c.solve(u, p, rtol=1e-8)
+    ug = u.cpu().numpy()
+    x32 = x.to(torch.float32)
+    xo32 = xo.astype(np.float32)
+    np.testing.assert_array_equal(x32.cpu().numpy(), xo32)
+    tbl, cnt, own_o = m.initial_tables(ppc, 64)
+    dt = 3.0 * c.max_dt(u)   # several elements over the ten steps
+    for _ in range(10):
+        c.rk2(x32, u, dt)
+        xn, _ = m.rk2(ug, dt, xo32.astype(np.float64))
+        xo32 = xn.astype(np.float32)
+        np.testing.assert_array_equal(x32.cpu().numpy(), xo32)
+        c.update_owners(x32, owner, off, lst)
+        m.update_owners(xo32.astype(np.float64), own_o, tbl, cnt)
+        np.testing.assert_array_equal(owner.cpu().numpy(), own_o)
+    moved = np.sum(own_o != m.cell_of(xo.astype(np.float32).astype(np.float64)))
+    assert moved > 0
+    o = off.cpu().numpy()
+    lst_h = lst.cpu().numpy()
+    for e in range(m.n_el):
+        np.testing.assert_array_equal(lst_h[o[e]:o[e + 1]], tbl[e, : cnt[e]])

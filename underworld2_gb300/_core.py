@@ -97,8 +97,10 @@ class Context:
         return owner
 
     def update_owners(self, x, owner, off, lst):
+        """Owner update; x may be stored in FP64 or FP32."""
         lost = ctypes.c_int64(0)
-        self._call("uwg_update_owners", x.shape[0], _ptr(x), _ptr(owner), _ptr(off), _ptr(lst), ctypes.byref(lost))
+        name = "uwg_update_owners_f32" if x.dtype == torch.float32 else "uwg_update_owners"
+        self._call(name, x.shape[0], _ptr(x), _ptr(owner), _ptr(off), _ptr(lst), ctypes.byref(lost))
         return lost.value
 
     def pic_map(self, x, off, lst):
@@ -203,8 +205,10 @@ class Context:
 
     # -- advection -------------------------------------------------------------
     def rk2(self, x, vel, dt):
+        """Midpoint RK2 in FP64; x may be stored in FP64 or FP32 (rounded once per step)."""
         fb, failed = ctypes.c_int64(0), ctypes.c_int64(0)
-        self._call("uwg_rk2_advect", x.shape[0], float(dt), _ptr(vel), _ptr(x), ctypes.byref(fb), ctypes.byref(failed))
+        name = "uwg_rk2_advect_f32" if x.dtype == torch.float32 else "uwg_rk2_advect"
+        self._call(name, x.shape[0], float(dt), _ptr(vel), _ptr(x), ctypes.byref(fb), ctypes.byref(failed))
         return fb.value, failed.value
 
     def interpolate(self, pts, vel):

@@ -73,6 +73,7 @@ SIGNATURES = {
     "uwg_layout_random": (_I, [_CTX, _I, ctypes.POINTER(_I64), _P, _P, _P, _P]),
     "uwg_locate": (_I, [_CTX, _I64, _P, _P]),
     "uwg_update_owners": (_I, [_CTX, _I64, _P, _P, _P, _P, ctypes.POINTER(_I64)]),
+    "uwg_update_owners_f32": (_I, [_CTX, _I64, _P, _P, _P, _P, ctypes.POINTER(_I64)]),
     "uwg_pic_map": (_I, [_CTX, _I64, _P, _P, _P, _P]),
     "uwg_dvc_weights": (_I, [_CTX, _I, _P, _P, _P]),
     "uwg_dvc_weights_noalloc": (_I, [_I, _I, _I64, _P, _P, _P, _P]),
@@ -90,6 +91,7 @@ SIGNATURES = {
     "uwg_apply_G": (_I, [_CTX, _P, _P]),
     "uwg_apply_Gt": (_I, [_CTX, _P, _P]),
     "uwg_rk2_advect": (_I, [_CTX, _I64, _D, _P, _P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
+    "uwg_rk2_advect_f32": (_I, [_CTX, _I64, _D, _P, _P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
     "uwg_interpolate": (_I, [_CTX, _I64, _P, _P, _P]),
     "uwg_max_dt": (_I, [_CTX, _P, ctypes.POINTER(_D)]),
     "uwg_advdiff_step": (_I, [_CTX, _D, _P, _P, _P, _P, _P, _P, _P, _P, _I, _D, _P]),

@@ -100,15 +100,17 @@ __global__ void k_locate(uwg_geom g, int64_t n_el, int64_t np, const double* x, 
 // new table.  Tables of different cells never interact, so each cell replays
 // its own events (removals and additions, in particle order) on one thread.
 // ---------------------------------------------------------------------------
-template <int DIM>
-__global__ void k_owner_events(uwg_geom g, int64_t n_el, int64_t np, const double* x,
+// X: the storage type of the particle coordinates (double, or float with the
+// arithmetic still in double).
+template <int DIM, typename X>
+__global__ void k_owner_events(uwg_geom g, int64_t n_el, int64_t np, const X* x,
                                const int32_t* owner, int32_t* newowner, int32_t* n_events,
                                int32_t* n_add, int32_t* n_rem, unsigned long long* n_lost) {
     int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (p >= np) return;
     double pt[3];
 #pragma unroll
-    for (int d = 0; d < DIM; d++) pt[d] = x[p * DIM + d];
+    for (int d = 0; d < DIM; d++) pt[d] = (double)x[p * DIM + d];
     int32_t nc = (int32_t)cell_of<DIM>(g, pt, n_el);
     int32_t oc = owner[p];
     newowner[p] = nc;
@@ -251,15 +253,18 @@ __device__ bool eval_velocity(const uwg_geom& g, const double* vel, const double
 }
 
 // TimeIntegrand_SecondOrder (L/StgDomain/Utils/src/TimeIntegrand.c:249-319) with
-// _TimeIntegrand_RewindToStartAndApplyFirstOrderUpdate (:441-468).
-template <int DIM, int ORDER>
-__global__ void k_rk2(uwg_geom g, int64_t np, double dt, const double* vel, double* x,
+// _TimeIntegrand_RewindToStartAndApplyFirstOrderUpdate (:441-468).  X is the
+// coordinate storage type: with float storage the stored values are widened to
+// double, every step of the update is done in double, and the result is
+// rounded once when it is stored.
+template <int DIM, int ORDER, typename X>
+__global__ void k_rk2(uwg_geom g, int64_t np, double dt, const double* vel, X* x,
                       unsigned long long* counts) {
     int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (p >= np) return;
     double x0[3], xm[3], v[3];
 #pragma unroll
-    for (int d = 0; d < DIM; d++) x0[d] = x[p * DIM + d];
+    for (int d = 0; d < DIM; d++) x0[d] = (double)x[p * DIM + d];
     if (!eval_velocity<DIM, ORDER>(g, vel, x0, v)) {
         atomicAdd(&counts[1], 1ull);
         return;
@@ -269,11 +274,11 @@ __global__ void k_rk2(uwg_geom g, int64_t np, double dt, const double* vel, doub
     double vm[3];
     if (eval_velocity<DIM, ORDER>(g, vel, xm, vm)) {
 #pragma unroll
-        for (int d = 0; d < DIM; d++) x[p * DIM + d] = x0[d] + dt * vm[d];
+        for (int d = 0; d < DIM; d++) x[p * DIM + d] = (X)(x0[d] + dt * vm[d]);
     } else {
         atomicAdd(&counts[0], 1ull);
 #pragma unroll
-        for (int d = 0; d < DIM; d++) x[p * DIM + d] = x0[d] + dt * v[d];
+        for (int d = 0; d < DIM; d++) x[p * DIM + d] = (X)(x0[d] + dt * v[d]);
     }
 }
 
@@ -358,8 +363,9 @@ struct uwg_dev_buf {
     ~uwg_dev_buf() { if (p) cudaFree(p); }
 };
 
-extern "C" int uwg_update_owners(uwg_ctx* c, int64_t np, const double* x, int32_t* owner,
-                                 int32_t* cell_offsets, int32_t* cell_list, int64_t* n_lost_h) {
+template <typename X>
+static int update_owners(uwg_ctx* c, int64_t np, const X* x, int32_t* owner, int32_t* cell_offsets,
+                         int32_t* cell_list, int64_t* n_lost_h) {
     if (!c || np < 0 || !cell_offsets || (np && (!x || !owner || !cell_list)))
         return uwg_set_error(c, UWG_ERR_ARG, "uwg_update_owners: bad argument");
     int64_t n_el = c->n_el;
@@ -384,9 +390,9 @@ extern "C" int uwg_update_owners(uwg_ctx* c, int64_t np, const double* x, int32_
     UWG_CUDA(c, cudaMemsetAsync(err, 0, 24, s));
     if (np) {
         if (c->dim == 2)
-            k_owner_events<2><<<nblk(np), 256, 0, s>>>(g, n_el, np, x, owner, newowner, n_events, n_add, n_rem, lost);
+            k_owner_events<2, X><<<nblk(np), 256, 0, s>>>(g, n_el, np, x, owner, newowner, n_events, n_add, n_rem, lost);
         else
-            k_owner_events<3><<<nblk(np), 256, 0, s>>>(g, n_el, np, x, owner, newowner, n_events, n_add, n_rem, lost);
+            k_owner_events<3, X><<<nblk(np), 256, 0, s>>>(g, n_el, np, x, owner, newowner, n_events, n_add, n_rem, lost);
         UWG_CUDA(c, cudaGetLastError());
     }
     // event offsets
@@ -437,6 +443,16 @@ extern "C" int uwg_update_owners(uwg_ctx* c, int64_t np, const double* x, int32_
     return UWG_OK;
 }
 
+extern "C" int uwg_update_owners(uwg_ctx* c, int64_t np, const double* x, int32_t* owner,
+                                 int32_t* cell_offsets, int32_t* cell_list, int64_t* n_lost_h) {
+    return update_owners<double>(c, np, x, owner, cell_offsets, cell_list, n_lost_h);
+}
+
+extern "C" int uwg_update_owners_f32(uwg_ctx* c, int64_t np, const float* x, int32_t* owner,
+                                     int32_t* cell_offsets, int32_t* cell_list, int64_t* n_lost_h) {
+    return update_owners<float>(c, np, x, owner, cell_offsets, cell_list, n_lost_h);
+}
+
 extern "C" int uwg_pic_map(uwg_ctx* c, int64_t np, const double* x, const int32_t* cell_offsets,
                            const int32_t* cell_list, double* ip_xi) {
     if (!c || np < 0 || !cell_offsets || (np && (!x || !cell_list || !ip_xi)))
@@ -450,14 +466,15 @@ extern "C" int uwg_pic_map(uwg_ctx* c, int64_t np, const double* x, const int32_
     return UWG_OK;
 }
 
-extern "C" int uwg_rk2_advect(uwg_ctx* c, int64_t np, double dt, const double* vel, double* x,
-                              int64_t* n_fallback_h, int64_t* n_failed_h) {
+template <typename X>
+static int rk2_advect(uwg_ctx* c, int64_t np, double dt, const double* vel, X* x, int64_t* n_fallback_h,
+                      int64_t* n_failed_h) {
     if (!c || np < 0 || !vel || (np && !x)) return uwg_set_error(c, UWG_ERR_ARG, "uwg_rk2_advect: bad argument");
     uwg_geom g = make_geom(c);
     unsigned long long* cnt = (unsigned long long*)c->red;
     UWG_CUDA(c, cudaMemsetAsync(cnt, 0, 16, c->stream));
     if (np) {
-#define L_(D, O) k_rk2<D, O><<<nblk(np), 256, 0, c->stream>>>(g, np, dt, vel, x, cnt)
+#define L_(D, O) k_rk2<D, O, X><<<nblk(np), 256, 0, c->stream>>>(g, np, dt, vel, x, cnt)
         UWG_DISPATCH(c, L_);
 #undef L_
         UWG_CUDA(c, cudaGetLastError());
@@ -470,6 +487,16 @@ extern "C" int uwg_rk2_advect(uwg_ctx* c, int64_t np, double dt, const double* v
         if (n_failed_h) *n_failed_h = (int64_t)h[1];
     }
     return UWG_OK;
+}
+
+extern "C" int uwg_rk2_advect(uwg_ctx* c, int64_t np, double dt, const double* vel, double* x,
+                              int64_t* n_fallback_h, int64_t* n_failed_h) {
+    return rk2_advect<double>(c, np, dt, vel, x, n_fallback_h, n_failed_h);
+}
+
+extern "C" int uwg_rk2_advect_f32(uwg_ctx* c, int64_t np, double dt, const double* vel, float* x,
+                                  int64_t* n_fallback_h, int64_t* n_failed_h) {
+    return rk2_advect<float>(c, np, dt, vel, x, n_fallback_h, n_failed_h);
 }
 
 extern "C" int uwg_interpolate(uwg_ctx* c, int64_t n, const double* pts, const double* vel, double* out) {
