@@ -60,6 +60,30 @@ int uwg_mesh_sizes(const uwg_ctx* ctx, int64_t* sizes_h);
 /* node coordinates per axis, copied to host arrays of length res*order+1 */
 int uwg_mesh_axis(const uwg_ctx* ctx, int axis, double* coords_h);
 
+/* ---- Function-graph evaluation at integration points --------------------------
+ * One op of a register program: r[dst] = f(r[a], r[b], imm) (opcodes in
+ * csrc/uwg_fn.cu; function.py compiles the graph).  An input is an array of
+ * `count` components per row, of dtype 0 f64, 1 f32, 2 i32, 3 i8, 4 i16, 5 i64,
+ * indexed by the point's particle id (by_particle = 1) or by the point index. */
+typedef struct {
+    int32_t op, dst, a, b;
+    double imm;
+} uwg_fn_op;
+typedef struct {
+    const void* ptr;
+    int32_t dtype, count, by_particle, pad;
+} uwg_fn_input;
+
+/* Evaluates the program at n points (pid[n]: particle of each point, or NULL)
+ * into out[n][nout], or into out[pid[i]][nout] with out_by_particle; *flags_h
+ * collects the program's error checks (bit k set by a failing check with
+ * code k).  Replaces the per-point virtual-call
+ * evaluation of the function graph behind the assembly terms
+ * (L/Underworld/Function/src/SwarmVariableFn.cpp:30-110, Map.cpp,
+ * Conditional.cpp, MathUnary.cpp, Arithmetic.cpp). */
+int uwg_fn_eval(uwg_ctx* ctx, int nops, const uwg_fn_op* ops_h, int ninputs, const uwg_fn_input* inputs_h,
+                int64_t n, const int32_t* pid, int nout, int out_by_particle, double* out, int32_t* flags_h);
+
 /* Seeded per-cell uniform-random particle layout: cells in order, particles
  * in order, dims in order, one Park-Miller stream seeded with seed^123459876.
  * Writes x[n_el*ppc][dim], owner[n_el*ppc] and the cell tables

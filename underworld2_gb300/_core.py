@@ -152,6 +152,18 @@ class Context:
         """f += df at free dofs (traction surface term; after assemble)."""
         self._call("uwg_add_force", _ptr(df.contiguous()))
 
+    def fn_eval(self, ops, inputs, n, pid32, nout, out, by_particle):
+        """Run a compiled function program (function.py) at n points; returns the check flags."""
+        from . import function as _fn
+        arr = (_native.FnOp * max(len(ops), 1))(*[_native.FnOp(*o) for o in ops])
+        ins = (_native.FnInput * max(len(inputs), 1))(
+            *[_native.FnInput(t.data_ptr(), _fn._DTYPES[t.dtype], t.shape[1], int(bp), 0) for t, bp in inputs])
+        flags = ctypes.c_int32(0)
+        self._call("uwg_fn_eval", len(ops), ctypes.cast(arr, ctypes.c_void_p), len(inputs),
+                   ctypes.cast(ins, ctypes.c_void_p), int(n), _ptr(pid32), int(nout), int(bool(by_particle)),
+                   _ptr(out), ctypes.byref(flags))
+        return flags.value
+
     def add_source(self, off, lst, ip_xi, ip_w, src):
         """h += the continuity source term from per-particle values (after assemble)."""
         self._call("uwg_add_source", _ptr(off), _ptr(lst), _ptr(ip_xi), _ptr(ip_w), _ptr(src.contiguous()))

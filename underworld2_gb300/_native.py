@@ -39,6 +39,16 @@ class SolveOpts(ctypes.Structure):
                 ("null_space", ctypes.c_int), ("schur_pc_its", ctypes.c_int)]
 
 
+class FnOp(ctypes.Structure):
+    _fields_ = [("op", ctypes.c_int32), ("dst", ctypes.c_int32), ("a", ctypes.c_int32), ("b", ctypes.c_int32),
+                ("imm", ctypes.c_double)]
+
+
+class FnInput(ctypes.Structure):
+    _fields_ = [("ptr", ctypes.c_void_p), ("dtype", ctypes.c_int32), ("count", ctypes.c_int32),
+                ("by_particle", ctypes.c_int32), ("pad", ctypes.c_int32)]
+
+
 class SolveStats(ctypes.Structure):
     _fields_ = [("pressure_its", ctypes.c_int), ("velocity_presolve_its", ctypes.c_int),
                 ("velocity_pressuresolve_its", ctypes.c_int), ("velocity_backsolve_its", ctypes.c_int),
@@ -82,6 +92,7 @@ SIGNATURES = {
     "uwg_element_matrices": (_I, [_CTX, _I64, _P, _P, _P, _P]),
     "uwg_add_force": (_I, [_CTX, _P]),
     "uwg_add_source": (_I, [_CTX, _P, _P, _P, _P, _P]),
+    "uwg_fn_eval": (_I, [_CTX, _I, _P, _I, _P, _I64, _P, _I, _I, _P, ctypes.POINTER(ctypes.c_int32)]),
     "uwg_solve_opts_default": (None, [ctypes.POINTER(SolveOpts)]),
     "uwg_stokes_solve": (_I, [_CTX, ctypes.POINTER(SolveOpts), _P, _P, ctypes.POINTER(SolveStats)]),
     "uwg_stokes_residuals": (_I, [_CTX, _P, _P, _P]),

@@ -29,11 +29,13 @@ class EvalContext:
     """Where to evaluate: integration points with their particle ids and
     global coordinates (coords computed on demand)."""
 
-    def __init__(self, particle_ids, coords_fn, device):
+    def __init__(self, particle_ids, coords_fn, device, lib_ctx=None, pid32=None):
         self.pid = particle_ids
         self._coords_fn = coords_fn
         self._coords = None
         self.device = device
+        self.lib_ctx = lib_ctx     # the mesh's libuwg context: compiled evaluation (uwg_fn_eval)
+        self.pid32 = pid32         # int32 particle id of each point
 
     @property
     def coords(self):
@@ -107,13 +109,13 @@ class Function:
     def __rtruediv__(self, o): return _Bin(torch.div, Function.convert(o), self)
     def __pow__(self, o): return _Bin(torch.pow, self, Function.convert(o))
     def __neg__(self): return _Un(torch.neg, self)
-    def __lt__(self, o): return _Bool(lambda a, b: a < b, self, Function.convert(o))
-    def __le__(self, o): return _Bool(lambda a, b: a <= b, self, Function.convert(o))
-    def __gt__(self, o): return _Bool(lambda a, b: a > b, self, Function.convert(o))
-    def __ge__(self, o): return _Bool(lambda a, b: a >= b, self, Function.convert(o))
-    def __and__(self, o): return _Bool(lambda a, b: (a != 0) & (b != 0), self, Function.convert(o))
-    def __or__(self, o): return _Bool(lambda a, b: (a != 0) | (b != 0), self, Function.convert(o))
-    def __xor__(self, o): return _Bool(lambda a, b: (a != 0) ^ (b != 0), self, Function.convert(o))
+    def __lt__(self, o): return _Bool(lambda a, b: a < b, self, Function.convert(o), "lt")
+    def __le__(self, o): return _Bool(lambda a, b: a <= b, self, Function.convert(o), "le")
+    def __gt__(self, o): return _Bool(lambda a, b: a > b, self, Function.convert(o), "gt")
+    def __ge__(self, o): return _Bool(lambda a, b: a >= b, self, Function.convert(o), "ge")
+    def __and__(self, o): return _Bool(lambda a, b: (a != 0) & (b != 0), self, Function.convert(o), "and")
+    def __or__(self, o): return _Bool(lambda a, b: (a != 0) | (b != 0), self, Function.convert(o), "or")
+    def __xor__(self, o): return _Bool(lambda a, b: (a != 0) ^ (b != 0), self, Function.convert(o), "xor")
 
     def __getitem__(self, i):
         return _Index(self, i)
@@ -159,8 +161,8 @@ class _Bin(Function):
 class _Bool(Function):
     _bool = True
 
-    def __init__(self, op, a, b):
-        self.op, self.a, self.b = op, a, b
+    def __init__(self, op, a, b, name=None):
+        self.op, self.a, self.b, self.name = op, a, b, name
 
     def _children(self):
         return [self.a, self.b]
@@ -274,7 +276,9 @@ class math:
 
     @staticmethod
     def dot(fn1, fn2):
-        return _Bin(lambda x, y: (x * y).sum(dim=1, keepdim=True), Function.convert(fn1), Function.convert(fn2))
+        f = _Bin(lambda x, y: (x * y).sum(dim=1, keepdim=True), Function.convert(fn1), Function.convert(fn2))
+        f.name = "dot"
+        return f
 
 
 class _Map(Function):
@@ -596,6 +600,187 @@ class view:
     def count(fn):
         """Pass-through that counts its evaluations (one per point)."""
         return _Count(fn)
+
+
+# ---------------------------------------------------------------------------
+# Compilation to a register program evaluated by one kernel (csrc/uwg_fn.cu)
+# ---------------------------------------------------------------------------
+_OPS = {"const": 0, "input": 1, "add": 2, "sub": 3, "mul": 4, "div": 5, "pow": 6, "max": 7, "min": 8,
+        "lt": 9, "le": 10, "gt": 11, "ge": 12, "and": 13, "or": 14, "xor": 15, "neg": 16, "abs": 17,
+        "exp": 18, "log": 19, "log2": 20, "log10": 21, "sqrt": 22, "sin": 23, "cos": 24, "tan": 25,
+        "asin": 26, "acos": 27, "atan": 28, "sinh": 29, "cosh": 30, "tanh": 31, "asinh": 32, "acosh": 33,
+        "atanh": 34, "erf": 35, "erfc": 36, "eqk": 37, "select": 38, "check": 39, "out": 40, "copy": 41,
+        "finite": 42}
+_BIN_OPS = {torch.add: "add", torch.sub: "sub", torch.mul: "mul", torch.div: "div", torch.pow: "pow",
+            torch.maximum: "max", torch.minimum: "min"}
+_UN_OPS = {torch.neg: "neg", torch.abs: "abs", torch.exp: "exp", torch.log: "log", torch.log2: "log2",
+           torch.log10: "log10", torch.sqrt: "sqrt", torch.sin: "sin", torch.cos: "cos", torch.tan: "tan",
+           torch.asin: "asin", torch.acos: "acos", torch.atan: "atan", torch.sinh: "sinh", torch.cosh: "cosh",
+           torch.tanh: "tanh", torch.asinh: "asinh", torch.acosh: "acosh", torch.atanh: "atanh",
+           torch.erf: "erf", torch.erfc: "erfc"}
+_DTYPES = {torch.float64: 0, torch.float32: 1, torch.int32: 2, torch.int8: 3, torch.int16: 4, torch.int64: 5}
+# error-check codes of the program and the exceptions they raise on the host
+_CHECKS = {0: (ValueError, "branching.map: a key has no mapping and no default is given"),
+           1: (RuntimeError, "branching.conditional: no clause evaluated true for some points"),
+           2: (RuntimeError, "Function evaluation produced a non-finite value (SafeMaths).")}
+
+
+class _Unsupported(Exception):
+    pass
+
+
+class _Program:
+    """A function graph lowered to register operations (memoised per node)."""
+
+    MAX_REG = 128
+
+    def __init__(self, ctx):
+        self.ctx = ctx
+        self.ops = []
+        self.inputs = []          # (tensor, by_particle)
+        self.nreg = 0
+        self.memo = {}
+
+    def reg(self):
+        if self.nreg >= self.MAX_REG:
+            raise _Unsupported("too many registers")
+        self.nreg += 1
+        return self.nreg - 1
+
+    def emit(self, op, dst=-1, a=-1, b=-1, imm=0.0):
+        self.ops.append((_OPS[op], dst, a, b, float(imm)))
+        return dst
+
+    def input(self, t, by_particle):
+        if t.dim() == 1:
+            t = t[:, None]
+        t = t.contiguous()
+        if t.dtype not in _DTYPES:
+            t = t.double()
+        self.inputs.append((t, by_particle))
+        slot = len(self.inputs) - 1
+        return [self.emit("input", self.reg(), slot, k) for k in range(t.shape[1])]
+
+    @staticmethod
+    def _broadcast(a, b):
+        if len(a) == len(b):
+            return a, b
+        if len(a) == 1:
+            return a * len(b), b
+        if len(b) == 1:
+            return a, b * len(a)
+        raise _Unsupported("component counts %d and %d" % (len(a), len(b)))
+
+    def node(self, f):
+        key = id(f)
+        if key not in self.memo:
+            self.memo[key] = self._node(f)
+        return self.memo[key]
+
+    def _node(self, f):
+        if isinstance(f, constant):
+            vals = np.atleast_1d(np.asarray(f.value, dtype=np.float64)).ravel()
+            return [self.emit("const", self.reg(), imm=v) for v in vals]
+        if isinstance(f, _Vector):
+            return [r for p in f.parts for r in self.node(p)]
+        if isinstance(f, _Bin):
+            name = getattr(f, "name", None) or _BIN_OPS.get(f.op)
+            if name is None:
+                raise _Unsupported("binary operation")
+            a, b = self.node(f.a), self.node(f.b)
+            if name == "dot":
+                a, b = self._broadcast(a, b)
+                acc = self.emit("mul", self.reg(), a[0], b[0])
+                for x, y in zip(a[1:], b[1:]):
+                    t = self.emit("mul", self.reg(), x, y)
+                    acc = self.emit("add", self.reg(), acc, t)
+                return [acc]
+            a, b = self._broadcast(a, b)
+            return [self.emit(name, self.reg(), x, y) for x, y in zip(a, b)]
+        if isinstance(f, _Bool):
+            if f.name is None:
+                raise _Unsupported("comparison")
+            a, b = self._broadcast(self.node(f.a), self.node(f.b))
+            return [self.emit(f.name, self.reg(), x, y) for x, y in zip(a, b)]
+        if isinstance(f, _Un):
+            name = _UN_OPS.get(f.op)
+            if name is None:
+                raise _Unsupported("unary operation")
+            return [self.emit(name, self.reg(), x) for x in self.node(f.a)]
+        if isinstance(f, _Index):
+            return [self.node(f.a)[f.i]]
+        if isinstance(f, input):
+            return self.input(self.ctx.coords, False)
+        if isinstance(f, _SwarmVar):
+            return self.input(f.var._device_data(), True)
+        if isinstance(f, _MeshVar):
+            return self.input(f._eval(self.ctx), False)      # sampled by the interpolation kernel
+        if isinstance(f, _MeshGrad):
+            return self.input(f._eval(self.ctx), False)
+        if isinstance(f, _Map):
+            key = self.node(f.key)[0]
+            entries = [(k, self.node(v)) for k, v in f.mapping.items()]
+            k = max([len(v) for _, v in entries] + ([len(self.node(f.default))] if f.default is not None else []))
+            if f.default is not None:
+                out = [self.emit("copy", self.reg(), r) for r in self._broadcast(self.node(f.default), [0] * k)[0]]
+                hit = None
+            else:
+                out = [self.emit("const", self.reg(), imm=float("nan")) for _ in range(k)]
+                hit = self.emit("const", self.reg(), imm=0.0)
+            for kv, v in entries:
+                eq = self.emit("eqk", self.reg(), key, imm=kv)
+                v = self._broadcast(v, [0] * k)[0]
+                out = [self.emit("select", self.reg(), x, o, imm=eq) for x, o in zip(v, out)]
+                if hit is not None:
+                    hit = self.emit("or", self.reg(), hit, eq)
+            if hit is not None:
+                self.emit("check", -1, hit, 0)
+            return out
+        if isinstance(f, _Conditional):
+            clauses = [(self.node(c)[0], self.node(v)) for c, v in f.clauses]
+            k = max(len(v) for _, v in clauses)
+            out = [self.emit("const", self.reg(), imm=float("nan")) for _ in range(k)]
+            done = self.emit("const", self.reg(), imm=0.0)
+            for c, v in reversed(clauses):
+                v = self._broadcast(v, [0] * k)[0]
+                out = [self.emit("select", self.reg(), x, o, imm=c) for x, o in zip(v, out)]
+                done = self.emit("or", self.reg(), done, c)
+            self.emit("check", -1, done, 1)
+            return out
+        if isinstance(f, _SafeMaths):
+            regs = self.node(f.a)
+            for r in regs:
+                self.emit("finite", -1, r, 2)
+            return regs
+        raise _Unsupported(type(f).__name__)
+
+
+def _eval_kernel(f, ctx, ncomp=None, out=None):
+    """Evaluate f at the points of ctx with one kernel launch; returns None when
+    the graph holds a node kind the program does not cover.  With `out` (a
+    per-particle [n_particles, k] float64 tensor) the values are scattered into
+    particle order by the kernel itself."""
+    lib_ctx = getattr(ctx, "lib_ctx", None)
+    if lib_ctx is None or getattr(ctx, "pid32", None) is None:
+        return None
+    prog = _Program(ctx)
+    try:
+        regs = prog.node(f)
+    except _Unsupported:
+        return None
+    k = len(regs)
+    if ncomp is not None and k not in (1, ncomp):
+        raise ValueError("function returns %d components, %d expected" % (k, ncomp))
+    nout = ncomp or k
+    regs = regs * nout if k == 1 else regs
+    for c, r in enumerate(regs):
+        prog.emit("out", c, r)
+    res = torch.empty((ctx.n, nout), dtype=torch.float64, device=ctx.device) if out is None else out
+    flags = lib_ctx.fn_eval(prog.ops, prog.inputs, ctx.n, ctx.pid32, nout, res, out is not None)
+    for code, (exc, msg) in _CHECKS.items():
+        if flags & (1 << code):
+            raise exc(msg)
+    return res
 
 
 def _input_context(inputData):

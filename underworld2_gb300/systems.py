@@ -124,7 +124,8 @@ class Stokes:
             vs.repopulate()
             s = self._swarm
             n = int(s._off[-1])
-            e = _fn.EvalContext(s._lst[:n].long(), vs.global_coords, ctx.device)
+            e = _fn.EvalContext(s._lst[:n].long(), vs.global_coords, ctx.device, lib_ctx=ctx,
+                                pid32=s._lst[:n].to(torch.int32).contiguous())
             return s._off, s._lst, vs.ip_xi, vs.ip_w, e
         # Gauss integration (3 points per axis), one "particle" per point
         x1, w1 = np.polynomial.legendre.leggauss(3)
@@ -155,9 +156,15 @@ class Stokes:
 
         if self._fn_viscosity.depends_on({"swarm"}) or self._fn_bodyforce.depends_on({"swarm"}):
             raise ValueError("swarm-variable functions need a voronoi_swarm")
-        return off, lst, ip_xi, ip_w, _fn.EvalContext(lst.long(), coords, ctx.device)
+        return off, lst, ip_xi, ip_w, _fn.EvalContext(lst.long(), coords, ctx.device, lib_ctx=ctx,
+                                                      pid32=lst.to(torch.int32).contiguous())
 
     def _per_particle(self, f, ectx, npart, ncomp):
+        # one kernel for the whole graph, writing straight into particle order
+        # (uwg_fn_eval); graphs with node kinds it does not cover use the tensor path
+        out = torch.zeros((npart, ncomp), dtype=torch.float64, device=ectx.device)
+        if _fn._eval_kernel(f, ectx, ncomp, out) is not None:
+            return out
         v = f.evaluate_at(ectx).to(torch.float64)
         if v.shape[1] != ncomp:
             raise ValueError("function returns %d components, %d expected" % (v.shape[1], ncomp))
