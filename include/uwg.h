@@ -327,11 +327,18 @@ int uwg_pop_apply(uwg_ctx* ctx, const double* ip_xi, const double* x_old, double
  * No counterpart in the reference.  Device pointers; BF16 buffers as uint16_t;
  * activations NHWC.  C[m][n] (+)= sum_k A(m,k) B(k,n) (+ bias[n]) (ReLU) with
  * A(m,k) = a_trans ? A[k*lda+m] : A[m*lda+k], B(k,n) = b_trans ? B[n*ldb+k] :
- * B[k*ldb+n], FP32 accumulation (mma.sync m16n8k16 bf16); Cf (FP32) and/or Cb
- * (BF16) outputs. */
+ * B[k*ldb+n], FP32 accumulation; Cf (FP32) and/or Cb (BF16) outputs.  K-major A
+ * and B (a_trans 0, b_trans 1) with K, lda, ldb multiples of 8 and 16-byte aligned
+ * A, B run on tcgen05.mma with the accumulator in tensor memory; the other
+ * layouts on mma.sync m16n8k16. */
 int uwg_cnn_gemm(uwg_ctx* ctx, int M, int N, int K, const uint16_t* A, int64_t lda, int a_trans, const uint16_t* B,
                  int64_t ldb, int b_trans, float* Cf, uint16_t* Cb, int64_t ldc, const float* bias, int relu,
                  int accumulate);
+/* path 0 (default): tcgen05 where the operands allow it; 1: mma.sync always. */
+int uwg_cnn_set_path(uwg_ctx* ctx, int path);
+/* Synchronises the stream; UWG_ERR_CUDA if a tensor-core GEMM since the last
+ * check gave up a bounded wait (its output tile is then incomplete). */
+int uwg_cnn_check(uwg_ctx* ctx);
 /* 3x3 im2col (BF16, zero padding) and its transpose col2im (FP32). */
 int uwg_cnn_im2col(uwg_ctx* ctx, int nb, int H, int W, int C, const uint16_t* x, uint16_t* col);
 int uwg_cnn_col2im(uwg_ctx* ctx, int nb, int H, int W, int C, const float* col, float* out);

@@ -42,6 +42,37 @@ def test_gemm_matches_torch(gpu, at, bt):
     assert torch.allclose(C2, torch.relu(C + Af @ Bf), rtol=1e-4, atol=1e-3 * ref.abs().max().item())
 
 
+@pytest.mark.parametrize("M,N,K", [(128, 64, 64), (300, 32, 72), (1000, 96, 288), (257, 128, 576),
+                                   (4096, 256, 1152), (77, 200, 1000), (130, 3, 288)])
+def test_tcgen05_gemm_matches_torch_fp32(gpu, M, N, K):
+    """The tcgen05 GEMM (K-major A and B, accumulator in tensor memory) against torch's
+    FP32 matmul and the mma.sync kernel on the same BF16 inputs: ragged M and N, K
+    not a multiple of the 64-wide chunk, bias, ReLU, accumulation and a BF16 copy."""
+    from underworld2_gb300.learned import _Ops
+    ops = _Ops(_ctx())
+    g = torch.Generator(device="cuda").manual_seed(M + N + K)
+    A = torch.randn((M, K), device="cuda", generator=g).to(torch.bfloat16)
+    B = torch.randn((N, K), device="cuda", generator=g).to(torch.bfloat16)
+    bias = torch.randn(N, device="cuda", generator=g)
+    ref = A.float() @ B.float().t() + bias
+    bound = 1e-5 * (A.float().abs() @ B.float().abs().t()).max().item()
+    C = torch.full((M, N), float("nan"), device="cuda")
+    Cb = torch.empty((M, N), device="cuda", dtype=torch.bfloat16)
+    ops.gemm(M, N, K, A, K, 0, B, K, 1, Cf=C, Cb=Cb, ldc=N, bias=bias)
+    ops.check()
+    assert (C - ref).abs().max().item() <= bound
+    assert torch.equal(Cb, C.to(torch.bfloat16))
+    ops.set_path(1)
+    C1 = torch.empty((M, N), device="cuda")
+    ops.gemm(M, N, K, A, K, 0, B, K, 1, Cf=C1, ldc=N, bias=bias)
+    ops.set_path(0)
+    assert (C - C1).abs().max().item() <= bound
+    C2 = C.clone()
+    ops.gemm(M, N, K, A, K, 0, B, K, 1, Cf=C2, ldc=N, relu=True, acc=True)
+    ops.check()
+    assert (C2 - torch.relu(C + A.float() @ B.float().t())).abs().max().item() <= 2 * bound
+
+
 def test_conv_forward_backward_matches_autograd(gpu):
     from underworld2_gb300.learned import Conv3x3, _Ops
     ops = _Ops(_ctx())

@@ -114,6 +114,8 @@ SIGNATURES = {
                                 ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
     "uwg_pop_apply": (_I, [_CTX, _P, _P, _P, _P, _P, _P, _P]),
     "uwg_cnn_gemm": (_I, [_CTX, _I, _I, _I, _P, _I64, _I, _P, _I64, _I, _P, _P, _I64, _P, _I, _I]),
+    "uwg_cnn_set_path": (_I, [_CTX, _I]),
+    "uwg_cnn_check": (_I, [_CTX]),
     "uwg_cnn_im2col": (_I, [_CTX, _I, _I, _I, _I, _P, _P]),
     "uwg_cnn_col2im": (_I, [_CTX, _I, _I, _I, _I, _P, _P]),
     "uwg_cnn_elementwise": (_I, [_CTX, _I, _I, _I, _I, _I, _P, _P, _P, _P, _P]),

@@ -40,6 +40,7 @@ extern "C" void uwg_ctx_destroy(uwg_ctx* c) {
     uwg_pop_free(c);
     if (c->q2_ke) cudaFree(c->q2_ke);
     if (c->q2_ke_df) cudaFree(c->q2_ke_df);
+    if (c->cnn_flag) cudaFree(c->cnn_flag);
     if (c->red_host) cudaFreeHost(c->red_host);
     uwg_solver_free(c);
     delete c;

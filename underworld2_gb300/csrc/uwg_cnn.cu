@@ -1,12 +1,15 @@
 // Kernels of the learned warm start: a small convolutional network trained on
 // solves of the Stokes path itself (no counterpart in the reference).
 //
-// Every convolution is a GEMM on BF16 tensor cores with FP32 accumulation
-// (mma.sync m16n8k16): forward C = im2col(x) W^T, data gradient
-// dcol = dZ W followed by col2im, weight gradient dW = dZ^T im2col(x).
-// Activations are NHWC so that the GEMM's K dimension (tap, channel) is
-// contiguous.  One generic GEMM with optional operand transposes, a fused
-// bias + ReLU epilogue and FP32 / BF16 outputs serves all three products.
+// Every convolution is a GEMM on BF16 tensor cores with FP32 accumulation:
+// forward C = im2col(x) W^T, data gradient dcol = dZ W followed by col2im,
+// weight gradient dW = dZ^T im2col(x).  Activations are NHWC so that the
+// GEMM's K dimension (tap, channel) is contiguous.  The forward product (both
+// operands K-major) runs on tcgen05.mma with the accumulator in tensor memory;
+// a generic mma.sync m16n8k16 GEMM with optional operand transposes serves the
+// two gradient products and operands whose rows are not 16-byte aligned (the
+// 3-channel input layer).  Both have a fused bias + ReLU epilogue and FP32 /
+// BF16 outputs.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -111,6 +114,187 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, const __
                 if (Cf) Cf[o] = v;
                 if (Cb) Cb[o] = __float2bfloat16(v);
             }
+}
+
+// ---------------------------------------------------------------------------
+// The same product on the 5th-generation tensor cores (tcgen05) for K-major A
+// and K-major B (A(m,k) = A[m*lda + k], B(k,n) = B[n*ldb + k]): the
+// convolution forward product im2col(x) W^T.
+//
+// One CTA of 128 threads computes a 128 x BN tile of C.  K advances in chunks
+// of 64; each chunk of A (128 x 64) and B (BN x 64) is staged by cp.async into
+// shared memory in the no-swizzle K-major core-matrix layout (8 rows x 16 bytes
+// per core matrix, 128 contiguous bytes; core matrix (row group g, k group j)
+// at (g * 8 + j) * 128 bytes, so the descriptor's leading (K) byte offset is
+// 128 and its stride (row-group) byte offset 1024).  Thread 0 issues four
+// tcgen05.mma (M 128, N BN, K 16) per chunk into an FP32 accumulator in tensor
+// memory and commits them to the chunk buffer's mbarrier; two buffers let the
+// next chunk's copies overlap the tensor-core work.  The epilogue reads the
+// accumulator back with tcgen05.ld (warp w owns lanes 32w..32w+31 = rows) and
+// applies accumulate / bias / ReLU as the mma.sync kernel does.
+//
+// Every mbarrier wait is bounded (about two seconds of SM clock); a wait that
+// gives up sets bit 0 of the status word, the CTA skips the remaining MMAs and
+// the epilogue, waits (bounded) for what it has issued, frees its tensor
+// memory and returns.
+// ---------------------------------------------------------------------------
+constexpr int TC_BM = 128, TC_BK = 64;
+constexpr long long TC_WAIT_CYCLES = 4000000000LL;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void tc_cp16(uint32_t dst, const void* src, bool valid) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(valid ? 16 : 0)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity) {
+    const long long t0 = clock64();
+    while (true) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (clock64() - t0 > TC_WAIT_CYCLES) return false;
+    }
+}
+
+// shared-memory matrix descriptor: start, leading (K) and stride (row group)
+// byte offsets in 16-byte units, fixed field 0b001 at bits 46-48, no swizzle
+__device__ __forceinline__ uint64_t tc_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
+}
+
+template <int BN>
+__global__ void __launch_bounds__(128) k_gemm_bf16_tc(int M, int N, int K, const __nv_bfloat16* __restrict__ A,
+                                                      int64_t lda, const __nv_bfloat16* __restrict__ B, int64_t ldb,
+                                                      float* Cf, __nv_bfloat16* Cb, int64_t ldc,
+                                                      const float* __restrict__ bias, int relu, int accumulate,
+                                                      int32_t* status) {
+    static_assert(BN % 16 == 0 && BN >= 32 && BN <= 256 && (BN & (BN - 1)) == 0, "tensor memory columns");
+    constexpr int A_BYTES = TC_BM * TC_BK * 2, B_BYTES = BN * TC_BK * 2, BUF = A_BYTES + B_BYTES;
+    // D F32 (bits 4-5 = 1), A BF16 (bits 7-9 = 1), B BF16 (bits 10-12 = 1), both K-major,
+    // N >> 3 at bits 17-22, M >> 4 at bits 24-28
+    constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                               ((uint32_t)(TC_BM >> 4) << 24);
+    extern __shared__ __align__(128) unsigned char tc_smem[];
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ uint32_t tmem_slot;
+    __shared__ int abort_all;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * BN;
+    const uint32_t sbase = smem_u32(tc_smem);
+    const uint32_t mb0 = smem_u32(&mbar[0]), mb1 = smem_u32(&mbar[1]);
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_slot)),
+                     "r"(BN)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mb0) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mb1) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        abort_all = 0;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+
+    const int nk = (K + TC_BK - 1) / TC_BK;
+    bool ok = true;
+    int committed = 0;  // chunks whose MMAs were issued and committed (uniform over the CTA)
+    for (int it = 0; it < nk; it++) {
+        const int buf = it & 1;
+        const uint32_t mb = buf ? mb1 : mb0;
+        // the buffer is free once the MMAs of chunk it - 2 have completed
+        if (it >= 2 && !tc_wait(mb, ((it - 2) >> 1) & 1)) ok = false;
+        if (__syncthreads_or(!ok)) { ok = false; break; }
+        committed = it + 1;
+        const int k0 = it * TC_BK;
+        const uint32_t sa = sbase + buf * BUF, sb = sa + A_BYTES;
+        for (int q = tid; q < TC_BM * 8; q += 128) {
+            const int r = q >> 3, j = q & 7, gm = m0 + r, gk = k0 + j * 8;
+            const bool v = gm < M && gk < K;
+            tc_cp16(sa + ((r >> 3) * 8 + j) * 128 + (r & 7) * 16, v ? (const void*)(A + (int64_t)gm * lda + gk) : A, v);
+        }
+        for (int q = tid; q < BN * 8; q += 128) {
+            const int r = q >> 3, j = q & 7, gn = n0 + r, gk = k0 + j * 8;
+            const bool v = gn < N && gk < K;
+            tc_cp16(sb + ((r >> 3) * 8 + j) * 128 + (r & 7) * 16, v ? (const void*)(B + (int64_t)gn * ldb + gk) : B, v);
+        }
+        asm volatile("cp.async.wait_all;\n" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+#pragma unroll
+            for (int s = 0; s < TC_BK / 16; s++) {
+                const uint64_t da = tc_desc(sa + s * 256, 128, 1024), db = tc_desc(sb + s * 256, 128, 1024);
+                const uint32_t acc = (it > 0 || s > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                    " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                    "l"(da), "l"(db), "r"(IDESC), "r"(acc)
+                    : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mb)
+                         : "memory");
+        }
+    }
+    // wait for the last commit on each buffer: every MMA this CTA issued has completed
+    bool fin = true;
+    if (committed >= 1 && !tc_wait((committed - 1) & 1 ? mb1 : mb0, ((committed - 1) >> 1) & 1)) fin = false;
+    if (committed >= 2 && !tc_wait((committed - 2) & 1 ? mb1 : mb0, ((committed - 2) >> 1) & 1)) fin = false;
+    if (tid == 0 && (!ok || !fin)) {
+        atomicOr(status, 1);
+        abort_all = 1;
+    }
+    __syncthreads();
+    if (!abort_all) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        const int row = m0 + warp * 32 + lane;
+#pragma unroll 1
+        for (int c0 = 0; c0 < BN; c0 += 16) {
+            uint32_t v[16];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                "[%16];\n"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                  "=r"(v[15])
+                : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0)
+                : "memory");
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            if (row >= M) continue;
+#pragma unroll
+            for (int j = 0; j < 16; j++) {
+                const int gn = n0 + c0 + j;
+                if (gn >= N) break;
+                float x = __uint_as_float(v[j]);
+                const int64_t o = (int64_t)row * ldc + gn;
+                if (accumulate && Cf) x += Cf[o];
+                if (bias) x += bias[gn];
+                if (relu) x = fmaxf(x, 0.f);
+                if (Cf) Cf[o] = x;
+                if (Cb) Cb[o] = __float2bfloat16(x);
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(BN) : "memory");
+    }
 }
 
 // col[p][tap*C + c] = x[pixel p shifted by tap][c] (zero outside), 3x3 taps, NHWC
@@ -276,10 +460,46 @@ extern "C" int uwg_cnn_gemm(uwg_ctx* c, int M, int N, int K, const uint16_t* A, 
     if (!c || M < 0 || N < 0 || K < 0 || !A || !B || (!Cf && !Cb) || (accumulate && !Cf))
         return uwg_set_error(c, UWG_ERR_ARG, "uwg_cnn_gemm: bad argument");
     if (!M || !N) return UWG_OK;
-    dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
     const __nv_bfloat16* a = reinterpret_cast<const __nv_bfloat16*>(A);
     const __nv_bfloat16* b = reinterpret_cast<const __nv_bfloat16*>(B);
     __nv_bfloat16* cb = reinterpret_cast<__nv_bfloat16*>(Cb);
+    // tcgen05 path: K-major A and B, 16-byte aligned rows (K, lda, ldb multiples of 8)
+    const bool tc = c->cnn_path == 0 && !a_trans && b_trans && K > 0 && K % 8 == 0 && lda % 8 == 0 &&
+                    ldb % 8 == 0 && ((uintptr_t)A & 15) == 0 && ((uintptr_t)B & 15) == 0;
+    if (tc) {
+        if (!c->cnn_flag) {
+            void* p = nullptr;
+            UWG_CUDA(c, cudaMalloc(&p, 16));
+            c->cnn_flag = static_cast<int32_t*>(p);   // freed by uwg_ctx_destroy
+            UWG_CUDA(c, cudaMemsetAsync(p, 0, 16, c->stream));
+        }
+        // shared memory per CTA: two chunk buffers (A 16 KB + B BN x 128 B each).  With BN 128 at most
+        // three CTAs fit an SM (384 of 512 tensor-memory columns), with BN 64 at most four (256).
+        if (N > 64) {
+            constexpr int SM = 2 * (TC_BM * TC_BK * 2 + 128 * TC_BK * 2);
+            static bool attr = false;
+            if (!attr) {
+                UWG_CUDA(c, cudaFuncSetAttribute(k_gemm_bf16_tc<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM));
+                attr = true;
+            }
+            dim3 g((N + 127) / 128, (M + TC_BM - 1) / TC_BM);
+            k_gemm_bf16_tc<128><<<g, 128, SM, c->stream>>>(M, N, K, a, lda, b, ldb, Cf, cb, ldc, bias, relu, accumulate,
+                                                           c->cnn_flag);
+        } else {
+            constexpr int SM = 2 * (TC_BM * TC_BK * 2 + 64 * TC_BK * 2);
+            static bool attr = false;
+            if (!attr) {
+                UWG_CUDA(c, cudaFuncSetAttribute(k_gemm_bf16_tc<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM));
+                attr = true;
+            }
+            dim3 g((N + 63) / 64, (M + TC_BM - 1) / TC_BM);
+            k_gemm_bf16_tc<64><<<g, 128, SM, c->stream>>>(M, N, K, a, lda, b, ldb, Cf, cb, ldc, bias, relu, accumulate,
+                                                          c->cnn_flag);
+        }
+        UWG_CUDA(c, cudaGetLastError());
+        return UWG_OK;
+    }
+    dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
 #define G_(AT, BT) k_gemm_bf16<AT, BT><<<grid, 128, 0, c->stream>>>(M, N, K, a, lda, b, ldb, Cf, cb, ldc, bias, relu, accumulate)
     if (a_trans && b_trans) G_(true, true);
     else if (a_trans) G_(true, false);
@@ -288,6 +508,23 @@ extern "C" int uwg_cnn_gemm(uwg_ctx* c, int M, int N, int K, const uint16_t* A, 
 #undef G_
     UWG_CUDA(c, cudaGetLastError());
     return UWG_OK;
+}
+
+extern "C" int uwg_cnn_set_path(uwg_ctx* c, int path) {
+    if (!c || path < 0 || path > 1) return uwg_set_error(c, UWG_ERR_ARG, "uwg_cnn_set_path: path 0 or 1");
+    c->cnn_path = path;
+    return UWG_OK;
+}
+
+extern "C" int uwg_cnn_check(uwg_ctx* c) {
+    if (!c) return uwg_set_error(c, UWG_ERR_ARG, "uwg_cnn_check: null context");
+    UWG_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (!c->cnn_flag) return UWG_OK;
+    int32_t f = 0;
+    UWG_CUDA(c, cudaMemcpy(&f, c->cnn_flag, 4, cudaMemcpyDeviceToHost));
+    if (!f) return UWG_OK;
+    UWG_CUDA(c, cudaMemset(c->cnn_flag, 0, 4));
+    return uwg_set_error(c, UWG_ERR_CUDA, "uwg_cnn_gemm: a tensor-core GEMM wait timed out (output incomplete)");
 }
 
 extern "C" int uwg_cnn_im2col(uwg_ctx* c, int nb, int H, int W, int C, const uint16_t* x, uint16_t* col) {

@@ -72,6 +72,8 @@ struct uwg_ctx {
     double* q2_ke;          // 3D Q2: packed FP64 element matrices [n_el][3321] for the FP64 apply
     float2* q2_ke_df;       // the same as double-float pairs (hi, lo), for the refinement residuals
     size_t slcn_ws_bytes;
+    int32_t* cnn_flag;      // CNN GEMM status word (device; set by a tensor-core GEMM whose wait gave up)
+    int cnn_path;           // CNN GEMM: 0 tcgen05 where the operands allow it, 1 always mma.sync
 };
 
 // Error helpers --------------------------------------------------------------

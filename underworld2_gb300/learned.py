@@ -8,7 +8,8 @@ velocity and pressure.  It is trained on solves of this library's own BSSCR path
 pressure is the initial guess of the Schur FGMRES (``zero_guess = 0``); the
 velocity channels are trained alongside but the BSSCR iteration only takes a
 pressure guess.  Every convolution runs as BF16 tensor-core GEMMs with FP32
-accumulation in libuwg (``uwg_cnn_*``, hand-written forward and backward); the
+accumulation in libuwg (``uwg_cnn_*``, hand-written forward and backward; the
+forward product on tcgen05 with the accumulator in tensor memory); the
 master weights, gradients and Adam moments are FP32.  PyTorch holds the device
 buffers and does the few gradient additions of the skip connections.
 
@@ -41,6 +42,14 @@ class _Ops:
     def gemm(self, M, N, K, A, lda, at, B, ldb, bt, Cf=None, Cb=None, ldc=None, bias=None, relu=False, acc=False):
         self.ctx._call("uwg_cnn_gemm", int(M), int(N), int(K), _p(A), int(lda), int(at), _p(B), int(ldb), int(bt),
                        _p(Cf), _p(Cb), int(ldc), _p(bias), int(relu), int(acc))
+
+    def check(self):
+        """Synchronise; raises if a tensor-core GEMM gave up a bounded wait."""
+        self.ctx._call("uwg_cnn_check")
+
+    def set_path(self, path):
+        """0: tcgen05 GEMM where the operands allow it (default); 1: mma.sync always."""
+        self.ctx._call("uwg_cnn_set_path", int(path))
 
     def im2col(self, nb, H, W, C, x, col):
         self.ctx._call("uwg_cnn_im2col", nb, H, W, C, _p(x), _p(col))
@@ -240,11 +249,13 @@ class WarmStartNet:
         self.step += 1
         for l in self.layers:
             l.adam(self.ops, self.step, lr)
+        self.ops.check()
         return float(loss.item())
 
     def predict(self, x):
         y = self.forward(x)
         self._acts = None
+        self.ops.check()
         return y
 
 
