@@ -264,9 +264,9 @@ def test_initial_guess(gpu):
 
 @pytest.mark.parametrize("res", [(64, 48, 40), (22, 18, 14)])
 def test_K32_tiled_apply_many_tiles(gpu, res):
-    """The FP32 3D apply (persistent, double-buffered tiles; 16-byte weight copies
-    when res_x % 4 == 0, else 4-byte) against the FP64 apply: 480 tiles (more
-    than the resident CTAs, so CTAs loop) and a mesh of partial tiles, with
+    """The FP32 3D apply (one CTA per 8x8x4 tile; 16-byte weight copies when
+    res_x % 4 == 0, else 4-byte) against the FP64 apply: 480 tiles (more than
+    the resident CTAs) and a mesh of partial tiles, with
     free-slip walls and scattered interior Dirichlet dofs (tiles with and
     without a Dirichlet flag)."""
     from underworld2_gb300._core import Context, rng_seed

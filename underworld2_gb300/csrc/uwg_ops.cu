@@ -363,9 +363,13 @@ __global__ void __launch_bounds__(128) k_applyK_q1_3d(uwg_lgeom g, const T* __re
 //     tile holding the node writes the same value), nodes inside the tile a
 //     plain store, nodes on the tile faces a global atomic add onto y, which
 //     the caller zeroes first (a memset rather than a masked copy pass).
-// Tiles without a Dirichlet dof take an element path without the mask.  A
-// persistent, double-buffered variant (the next tile's copies in flight while
-// computing the current one) measured slower: at 16 warps per SM the kernel is
+// Tiles without a Dirichlet dof take an element path without the mask.  Two
+// persistent variants measured slower on the 128^3 workload: one double-
+// buffering the next tile's copies behind the current tile's compute (0.272 ms
+// against 0.1875 ms per apply), and one with the per-tile index tables hoisted
+// out of the tile loop, element outputs in zero-haloed per-corner planes (a
+// node's value = 8 shared loads without validity tests) and the next tile's
+// copies behind the write-back (0.226 ms).  At 16 warps per SM the kernel is
 // bound by instruction issue and latency, not by DRAM.
 #define KT_X 8
 #define KT_Y 8
