@@ -220,6 +220,15 @@ typedef struct {
                               pressure solve and from p after it. */
     int schur_pc_its;      /* > 0: each pressure-Laplacian solve inside BFBt runs this many CG
                               iterations (rounded up to even) instead of stopping at schur_pc_rtol */
+    int coarse_agg;        /* > 0 (2D Q1/dQ0, BFBt, incompressible): coarse-level correction inside
+                              the flexible GMRES.  Pressure cells are aggregated in coarse_agg x
+                              coarse_agg blocks; the coarse Schur complement Sc = Gc^T Kc^-1 Gc is
+                              built from the velocity multigrid level whose elements are
+                              coarse_agg / 2 fine cells wide (Galerkin Kc, exact Gc) and inverted
+                              densely; each preconditioner application is the deflation step
+                              z = y + Q (r - S y), y = BFBt(r), Q = P Sc^-1 P^T (one extra Schur
+                              apply at coarse_rtol).  No counterpart in the reference. */
+    double coarse_rtol;    /* velocity tolerance of the extra Schur apply (default 1e-2) */
 } uwg_solve_opts;
 
 typedef struct {
@@ -238,6 +247,8 @@ typedef struct {
     double schur_op_time;  /* seconds in Schur-operator applications (inner velocity solves) */
     int schur_pc_used;     /* the Schur preconditioner applied: schur_pc, except that a compressible
                               system (pressure block C) is preconditioned by the Uzawa term (0) */
+    int coarse_dim;        /* dimension of the coarse space of the correction (0: not used) */
+    double coarse_setup_time; /* seconds building Sc^-1 */
 } uwg_solve_stats;
 
 void uwg_solve_opts_default(uwg_solve_opts* o);

@@ -139,13 +139,15 @@ def _check(st, u, p, uo, po, null_vectors=None, tol=TOL):
     return eu, ep
 
 
-@pytest.mark.parametrize("mixed", [0, 1])
-def test_config1_sinker_64(gpu, mixed):
-    """2D 64^2 Q1/dQ0 sinker, 20 particles per cell (81,920), free slip."""
+@pytest.mark.parametrize("mixed,coarse", [(0, 0), (1, 0), (1, 4)])
+def test_config1_sinker_64(gpu, mixed, coarse):
+    """2D 64^2 Q1/dQ0 sinker, 20 particles per cell (81,920), free slip; also with
+    the coarse-level correction of the Schur FGMRES (4 x 4 cell aggregates)."""
     case = Case(2, (64, 64), 20)
     eta, body = _sinker(case)
     mask = case.walls([[0], [1]])
-    st, u, p, uo, po = case.run(eta, body, mask, mixed=mixed)
+    st, u, p, uo, po = case.run(eta, body, mask, mixed=mixed, coarse_agg=coarse)
+    assert st["coarse_dim"] == (256 if coarse else 0)
     _check(st, u, p, uo, po, null_vectors=[np.ones(len(po))])
 
 

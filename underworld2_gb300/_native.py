@@ -36,7 +36,8 @@ class SolveOpts(ctypes.Structure):
                 ("mg_levels", ctypes.c_int), ("smooth_steps", ctypes.c_int), ("restart", ctypes.c_int),
                 ("zero_guess", ctypes.c_int), ("schur_pc", ctypes.c_int), ("schur_pc_rtol", ctypes.c_double),
                 ("relax_inner", ctypes.c_int), ("schur_pc_smooth", ctypes.c_int), ("p_dir", ctypes.c_void_p),
-                ("null_space", ctypes.c_int), ("schur_pc_its", ctypes.c_int)]
+                ("null_space", ctypes.c_int), ("schur_pc_its", ctypes.c_int), ("coarse_agg", ctypes.c_int),
+                ("coarse_rtol", ctypes.c_double)]
 
 
 class FnOp(ctypes.Structure):
@@ -60,7 +61,7 @@ class SolveStats(ctypes.Structure):
                 ("pmax", ctypes.c_double), ("fhat_reason", ctypes.c_int), ("outer_reason", ctypes.c_int),
                 ("backsolve_reason", ctypes.c_int), ("schur_pc_its", ctypes.c_int),
                 ("schur_pc_time", ctypes.c_double), ("schur_op_time", ctypes.c_double),
-                ("schur_pc_used", ctypes.c_int)]
+                ("schur_pc_used", ctypes.c_int), ("coarse_dim", ctypes.c_int), ("coarse_setup_time", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -275,6 +275,7 @@ extern "C" int uwg_assemble(uwg_ctx* c, int64_t np, const int32_t* off, const in
     if ((rc = uwg_solver_setup(c))) return rc;
     UWG_CUDA(c, cudaStreamSynchronize(c->stream));
     c->assembled = true;
+    c->asm_gen++;
     return UWG_OK;
 }
 

@@ -62,6 +62,7 @@ struct uwg_ctx {
     double* bcval;          // Dirichlet values [n_vdof]
     bool assembled;
     bool compressible;      // the last assembly had a pressure block C (fn_one_on_lambda)
+    int64_t asm_gen;        // assemblies so far (cached operator-derived data compares against it)
 
     // scratch
     void* red;              // reduction scratch (double[4096])

@@ -1451,6 +1451,18 @@ __global__ void k_dense_invert(int64_t n, double* A, double* B) {
     }
 }
 
+int uwg_ops_dense_matrix(uwg_ctx* c, int l, double* A) {
+    uwg_level& L = c->lev[l];
+    int64_t n = L.n_dof;
+    uwg_lgeom g = uwg_level_geom(c, l);
+    UWG_CUDA(c, cudaMemsetAsync(A, 0, sizeof(double) * n * n, c->stream));
+    if (c->dim == 3) k_dense_assemble<3><<<nblk(L.n_el, 64), 64, 0, c->stream>>>(g, L.W64, L.bc, n, A);
+    else k_dense_assemble<2><<<nblk(L.n_el, 64), 64, 0, c->stream>>>(g, L.W64, L.bc, n, A);
+    k_dense_bcdiag<<<nblk(n), 256, 0, c->stream>>>(n, L.bc, A);
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
 int uwg_ops_dense_coarse(uwg_ctx* c, int l) {
     uwg_level& L = c->lev[l];
     int64_t n = L.n_dof;
@@ -1513,6 +1525,9 @@ int uwg_ops_dense_invert(uwg_ctx* c, int64_t n, double* A, double* B) {
         UWG_CUDA(c, cudaGetLastError());
         return UWG_OK;
     }
+    return uwg_ops_dense_invert_grid(c, n, A, B);
+}
+int uwg_ops_dense_invert_grid(uwg_ctx* c, int64_t n, double* A, double* B) {
     double *A2 = nullptr, *B2 = nullptr;
     UWG_CUDA(c, cudaMallocAsync((void**)&A2, sizeof(double) * n * n, c->stream));
     UWG_CUDA(c, cudaMallocAsync((void**)&B2, sizeof(double) * n * n, c->stream));

@@ -22,6 +22,14 @@ int uwg_ops_level_setup(uwg_ctx* c, int l);
 int uwg_ops_coarsen(uwg_ctx* c, int l);          // W of level l+1 from level l
 int uwg_ops_bc_coarsen(uwg_ctx* c, int l);       // BC mask of level l+1 from level l
 int uwg_ops_dense_coarse(uwg_ctx* c, int l);     // dense inverse of level l
+int uwg_ops_dense_matrix(uwg_ctx* c, int l, double* A);   // dense operator of level l (Dirichlet rows: identity)
+// Coarse-level correction of the Schur FGMRES (uwg_coarse.cu): aggregates per
+// pressure multigrid / velocity level (0, or -1 not 2D Q1/dQ0, -2 bad agg, -3 no level),
+// Sc^-1 into sinv [npc^2], and z -= P Sc^-1 P^T (r - s).
+int uwg_cc_dims(const uwg_ctx* c, int agg, int* npc, int* lv);
+int uwg_cc_build(uwg_ctx* c, int agg, bool const_null, double* sinv);
+int uwg_cc_apply(uwg_ctx* c, int agg, const double* sinv, double* tc, double* zc, const double* r, const double* s,
+                 double* z);
 
 template <typename T> int uwg_ops_applyK(uwg_ctx* c, int l, const T* x, T* y);
 template <typename T> int uwg_ops_prolong_add(uwg_ctx* c, int lc, const T* xc, T* xf);   // xf += P xc
@@ -75,6 +83,7 @@ int uwg_q2_3d_schur_pc(uwg_ctx* c, const double* r, double* z);
 int uwg_q2_3d_element_matrices(uwg_ctx* c, int64_t el, double* Ke, double* Ge, double* Se);
 
 int uwg_ops_dense_invert(uwg_ctx* c, int64_t n, double* A, double* B);   // B = A^-1 (A destroyed)
+int uwg_ops_dense_invert_grid(uwg_ctx* c, int64_t n, double* A, double* B);   // the same, grid-wide steps
 int uwg_ops_to_f32(uwg_ctx* c, int64_t n, const double* a, float* b);
 int uwg_ops_dense_mv32(uwg_ctx* c, int64_t n, const float* Ainv, const float* b, float* x);
 

@@ -72,6 +72,10 @@ struct Work {
     double *ns_t = nullptr, *ns_v = nullptr, *ns_one = nullptr, *ns_tmp = nullptr;
     bool cb_null = false;
     bool const_null = false;   // the constant pressure lies in the null space of G
+    // coarse-level correction of the Schur FGMRES (uwg_coarse.cu)
+    double *cc_sinv = nullptr, *cc_tc = nullptr, *cc_zc = nullptr;
+    int cc_agg = 0, cc_cap = 0;               // aggregate size of cc_sinv, its capacity (aggregates)
+    int64_t cc_gen = -1;                      // assembly generation cc_sinv was built for
 };
 
 Work* work_of(uwg_ctx* c) {
@@ -286,6 +290,8 @@ struct SolveCfg {
     double schur_pc_rtol;
     bool relax;
     int schur_pc_its;   // > 0: fixed CG iterations per pressure-Laplacian solve (rtol ignored)
+    int cc_agg = 0;     // > 0: coarse-level correction with this aggregate size (Sc^-1 built)
+    double cc_rtol = 1e-2;
 };
 
 int bfbt(uwg_ctx* c, const double* r, double* z, double rtol, int its);
@@ -803,6 +809,8 @@ extern "C" void uwg_solve_opts_default(uwg_solve_opts* o) {
     o->p_dir = nullptr;
     o->null_space = 0;
     o->schur_pc_its = 0;
+    o->coarse_agg = 0;
+    o->coarse_rtol = 1e-2;
 }
 
 namespace {
@@ -865,6 +873,18 @@ int fgmres(uwg_ctx* c, const SolveCfg& cfg, const double* rhs, double* p, double
                 vk_copy<double>(s, n, z0, w->Z[j]);
             } else if (cfg.schur_pc == 1) {
                 if ((rc = bfbt(c, w->V[j], w->Z[j], cfg.schur_pc_rtol, cfg.schur_pc_its))) return rc;
+                if (cfg.cc_agg > 0) {
+                    // deflation step z = y + Q (r - A y) (uwg_coarse.cu); V[j+1] holds A y until
+                    // the iteration's own Schur apply overwrites it
+                    SolveCfg cl = cfg;
+                    cl.inner_rtol = cfg.cc_rtol;
+                    cl.relax = false;
+                    if ((rc = schur_apply(c, cl, w->Z[j], w->V[j + 1], inner_its, refine))) return rc;
+                    if ((rc = uwg_cc_apply(c, cfg.cc_agg, w->cc_sinv, w->cc_tc, w->cc_zc, w->V[j], w->V[j + 1],
+                                           w->Z[j])))
+                        return rc;
+                    if (w->const_null && (rc = ns_project(c, w->ns_one, w->Z[j]))) return rc;
+                }
                 double zn;
                 const double* az[1] = {w->Z[j]};
                 if ((rc = dots<double>(c, n, 1, az, az, &zn))) return rc;
@@ -1021,6 +1041,29 @@ extern "C" int uwg_stokes_solve(uwg_ctx* c, const uwg_solve_opts* o, double* u, 
     SolveCfg cfg{o->mixed != 0, o->inner_rtol, o->max_inner, std::max(1, o->smooth_steps), schur_pc,
                  o->schur_pc_rtol > 0.0 ? o->schur_pc_rtol : 1e-2, o->relax_inner != 0, o->schur_pc_its};
     if (o->schur_pc_its < 0 || o->schur_pc_its > 200) return uwg_set_error(c, UWG_ERR_ARG, "schur_pc_its must be in [0, 200]");
+    // coarse-level correction: BFBt, incompressible, no checkerboard null mode (its
+    // aggregates would not see it); Sc^-1 is rebuilt after each assembly
+    if (o->coarse_agg < 0) return uwg_set_error(c, UWG_ERR_ARG, "coarse_agg must be >= 0");
+    if (o->coarse_agg > 0 && schur_pc == 1 && !c->compressible && !w->cb_null) {
+        int npc = 0, lv = 0;
+        if (uwg_cc_dims(c, o->coarse_agg, &npc, &lv) == 0 && npc > w->cc_cap && npc <= 1024) {
+            if (!(w->cc_sinv = dalloc<double>(c, (int64_t)npc * npc)) || !(w->cc_tc = dalloc<double>(c, npc)) ||
+                !(w->cc_zc = dalloc<double>(c, npc)))
+                return uwg_set_error(c, UWG_ERR_CUDA, "coarse correction: out of device memory");
+            w->cc_cap = npc;
+            w->cc_gen = -1;
+        }
+        if (w->cc_gen != c->asm_gen || w->cc_agg != o->coarse_agg) {
+            double tc0 = now();
+            if ((rc = uwg_cc_build(c, o->coarse_agg, w->const_null, w->cc_sinv))) return rc;
+            w->cc_gen = c->asm_gen;
+            w->cc_agg = o->coarse_agg;
+            S.coarse_setup_time = now() - tc0;
+        }
+        cfg.cc_agg = o->coarse_agg;
+        cfg.cc_rtol = o->coarse_rtol > 0.0 ? o->coarse_rtol : 1e-2;
+        S.coarse_dim = npc;
+    }
     // b = f with Dirichlet values in BC rows
     vk_copy<double>(s, nv, c->f, w->bvec);
     {
