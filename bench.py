@@ -643,72 +643,99 @@ def run_slcn(args):
 
 
 def run_learned(args):
-    """Learned warm start on the 2D 128^2 Q1/dQ0 problem family of the training
-    set (log10 viscosity GRF with correlation length U[0.05, 0.2] and contrast
-    10^U[3,6], 0-8 inclusions of radius U[0.03, 0.1] with density +-1, 20
-    particles per element, free slip): generate `--train` solves with the plain
-    path, train the CNN, then on `--eval` held-out seeds compare outer (Schur
-    FGMRES) iterations and time to a 1e-8 residual of the plain FP64 solve, the
-    mixed-precision solve from zero and the mixed-precision solve from the
-    network's pressure as the first Schur search direction ("learned") and as
-    the initial guess ("guess"), prediction time included.  Problems without
-    buoyancy (no inclusions: zero solution) are left out of the means."""
+    """Learned warm start and coarse-level correction on the 2D 128^2 Q1/dQ0
+    problem family of the training set (log10 viscosity GRF with correlation
+    length U[0.05, 0.2] and contrast 10^U[3,6], 0-8 inclusions of radius
+    U[0.03, 0.1] with density +-1, 20 particles per element, free slip):
+    generate `--train` solves with the plain path and train the CNN (skipped
+    with --train 0), then on `--eval` held-out seeds compare outer (Schur
+    FGMRES) iterations and time to a 1e-8 residual of
+      fp64            the plain FP64 solve,
+      mixed           the mixed-precision solve from zero,
+      mixed_coarse    the same with the coarse-level correction (aggregates of
+                      --coarse-agg cells; its setup on a fresh assembly is timed),
+      learned         mixed, the network's pressure as the first search direction,
+      guess           mixed, the network's pressure as the initial guess,
+      learned_coarse  learned + the coarse-level correction,
+      hydro           mixed, the hydrostatic pressure (an input channel) as the
+                      first direction (control),
+    prediction time included in the learned arms.  Problems without buoyancy
+    (no inclusions: zero solution) are left out of the statistics."""
     import numpy as np
     import torch
     from underworld2_gb300 import learned
     ps = learned.ProblemSet(res=128, ppc=20)
-    t0 = time.perf_counter()
-    X, Y = learned.generate(ps, list(range(1000, 1000 + args.train)))
-    torch.cuda.synchronize()
-    t_gen = time.perf_counter() - t0
-    net = learned.WarmStartNet(ps.ctx, seed=0)
-    t0 = time.perf_counter()
-    losses = learned.train(net, X, Y, epochs=args.epochs, batch=8)
-    torch.cuda.synchronize()
-    t_train = time.perf_counter() - t0
+    net, t_gen, t_train, losses = None, 0.0, 0.0, []
+    if args.train > 0:
+        t0 = time.perf_counter()
+        X, Y = learned.generate(ps, list(range(1000, 1000 + args.train)))
+        torch.cuda.synchronize()
+        t_gen = time.perf_counter() - t0
+        net = learned.WarmStartNet(ps.ctx, seed=0)
+        t0 = time.perf_counter()
+        losses = learned.train(net, X, Y, epochs=args.epochs, batch=8)
+        torch.cuda.synchronize()
+        t_train = time.perf_counter() - t0
+        del X, Y
+    agg_c = args.coarse_agg
     rows = []
     ev = lambda: torch.cuda.Event(enable_timing=True)
     for s in range(900000, 900000 + args.eval):
         f, scales = ps.assemble(s)
-        u64, p64, st64 = ps.solve(0)
-        um, pm, stm = ps.solve(1)
-        e0, e1 = ev(), ev()
-        e0.record()
-        p0 = learned.predict_pressure(net, f, scales)
-        e1.record()
-        torch.cuda.synchronize()
-        t_pred = e0.elapsed_time(e1) / 1e3
-        ul, pl, stl, fb = learned.solve_with_warm_start(ps, net, f, scales, mode="direction")
-        ug, pg, stg, fbg = learned.solve_with_warm_start(ps, net, f, scales, mode="guess")
-        # control: the hydrostatic pressure alone (the third input channel) as the direction
-        ph = (f[:, :, 2].reshape(-1).double() * scales[1]).contiguous()
-        uh, phs, sth = ps.solve(1, p_dir=ph)
+        r = {}
+        u64, p64, st = ps.solve(0)
+        r.update(fp64_its=st["pressure_its"], fp64_s=st["total_time"], res=st["residual"])
+        _, _, st = ps.solve(1)
+        r.update(mixed_its=st["pressure_its"], mixed_s=st["total_time"], res=max(r["res"], st["residual"]))
+        ps.assemble(s)   # fresh assembly: the coarse operator is built (and timed) inside the solve
+        _, _, st = ps.solve(1, coarse_agg=agg_c)
+        r.update(mixed_coarse_its=st["pressure_its"], mixed_coarse_s=st["total_time"],
+                 coarse_setup_s=st["coarse_setup_time"], res=max(r["res"], st["residual"]))
         pt = p64 - p64.mean()
         nt = max(float(pt.norm()), 1e-300)
-        err = float((p0 - pt).norm() / nt)
-        err_h = float((ph - ph.mean() - pt).norm() / nt)
-        rows.append({"fp64_its": st64["pressure_its"], "fp64_s": st64["total_time"],
-                     "mixed_its": stm["pressure_its"], "mixed_s": stm["total_time"],
-                     "learned_its": stl["pressure_its"], "learned_s": stl["total_time"] + t_pred,
-                     "guess_its": stg["pressure_its"], "guess_s": stg["total_time"] + t_pred,
-                     "hydro_its": sth["pressure_its"], "hydro_p_rel_err": err_h,
-                     "predict_s": t_pred, "fallback": fb or fbg, "p_rel_err": err,
-                     "residual": max(stl["residual"], stg["residual"]), "trivial": float(pt.norm()) == 0.0})
-    rows_nt = [r for r in rows if not r["trivial"]]
-    agg = lambda k: float(np.mean([r[k] for r in rows_nt]))
-    med = lambda k: float(np.median([r[k] for r in rows_nt]))
-    print(json.dumps({
-        "learned": "CNN warm start (pressure initial guess of the Schur FGMRES)",
-        "params": net.n_params(), "train_solves": args.train, "eval_solves": args.eval, "epochs": args.epochs,
-        "generate_s": t_gen, "train_s": t_train, "loss_first_epoch": losses[0], "loss_last_epoch": losses[-1],
-        "mean": {k: agg(k) for k in ("fp64_its", "fp64_s", "mixed_its", "mixed_s", "learned_its", "learned_s",
-                                      "guess_its", "guess_s", "hydro_its", "hydro_p_rel_err", "predict_s",
-                                      "p_rel_err")},
-        "median_p_rel_err": med("p_rel_err"), "trivial_problems": int(sum(r["trivial"] for r in rows)),
-        "fallbacks": int(sum(r["fallback"] for r in rows)),
-        "max_residual": float(max(r["residual"] for r in rows)),
-        "speedup_learned_vs_fp64": agg("fp64_s") / agg("learned_s"),
-        "speedup_mixed_vs_fp64": agg("fp64_s") / agg("mixed_s")}))
+        r["trivial"] = float(pt.norm()) == 0.0
+        if net is not None:
+            e0, e1 = ev(), ev()
+            e0.record()
+            p0 = learned.predict_pressure(net, f, scales)
+            e1.record()
+            torch.cuda.synchronize()
+            t_pred = e0.elapsed_time(e1) / 1e3
+            _, _, stl, fb = learned.solve_with_warm_start(ps, net, f, scales, mode="direction")
+            _, _, stg, fbg = learned.solve_with_warm_start(ps, net, f, scales, mode="guess")
+            ps.assemble(s)
+            _, _, stc, fbc = learned.solve_with_warm_start(ps, net, f, scales, mode="direction", coarse_agg=agg_c)
+            ph = (f[:, :, 2].reshape(-1).double() * scales[1]).contiguous()
+            _, _, sth = ps.solve(1, p_dir=ph)
+            r.update(learned_its=stl["pressure_its"], learned_s=stl["total_time"] + t_pred,
+                     guess_its=stg["pressure_its"], guess_s=stg["total_time"] + t_pred,
+                     learned_coarse_its=stc["pressure_its"], learned_coarse_s=stc["total_time"] + t_pred,
+                     hydro_its=sth["pressure_its"], hydro_s=sth["total_time"], predict_s=t_pred,
+                     fallback=bool(fb or fbg or fbc), p_rel_err=float((p0 - pt).norm() / nt),
+                     hydro_p_rel_err=float((ph - ph.mean() - pt).norm() / nt),
+                     res=max(r["res"], stl["residual"], stg["residual"], stc["residual"], sth["residual"]))
+        rows.append(r)
+    nt_rows = [r for r in rows if not r["trivial"]]
+    arms = ["fp64", "mixed", "mixed_coarse"] + (["learned", "guess", "learned_coarse", "hydro"] if net else [])
+    stat = lambda k, f_: float(f_([r[k] for r in nt_rows]))
+    out = {
+        "workload": "2D 128^2 Q1/dQ0 learned-set problems, 20 particles per cell, free slip, rtol 1e-8",
+        "train_solves": args.train, "eval_solves": args.eval, "nontrivial": len(nt_rows), "epochs": args.epochs,
+        "coarse_agg": agg_c, "generate_s": t_gen, "train_s": t_train,
+        "loss_first_epoch": losses[0] if losses else None, "loss_last_epoch": losses[-1] if losses else None,
+        "params": net.n_params() if net else 0,
+        "its_mean": {a: stat(a + "_its", np.mean) for a in arms},
+        "s_mean": {a: stat(a + "_s", np.mean) for a in arms},
+        "s_median": {a: stat(a + "_s", np.median) for a in arms},
+        "coarse_setup_s_median": stat("coarse_setup_s", np.median),
+        "max_residual": float(max(r["res"] for r in rows)),
+        "faster_than_mixed": {a: int(sum(r[a + "_s"] < r["mixed_s"] for r in nt_rows)) for a in arms},
+    }
+    if net is not None:
+        out.update(p_rel_err_mean=stat("p_rel_err", np.mean), p_rel_err_median=stat("p_rel_err", np.median),
+                   hydro_p_rel_err_mean=stat("hydro_p_rel_err", np.mean), predict_s_mean=stat("predict_s", np.mean),
+                   fallbacks=int(sum(r["fallback"] for r in nt_rows)))
+    print(json.dumps(out))
 
 
 def run_convection(args):
@@ -969,6 +996,7 @@ def main():
     ap.add_argument("--train", type=int, default=800)
     ap.add_argument("--eval", type=int, default=100)
     ap.add_argument("--epochs", type=int, default=20)
+    ap.add_argument("--coarse-agg", type=int, default=8, help="aggregate size of the coarse-level correction")
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--max-outer", type=int, default=500)
     ap.add_argument("--skip-fp64", action="store_true")

@@ -7,10 +7,11 @@
 // farther away, :256-365), then rebuilds its boundary list from the cells it
 // just claimed (neighbours in the order S, N, E, W, U, D that it does not own,
 // each once, :388-486).  Within one particle's step the claims touch distinct
-// cells and are independent, and the boundary rebuild is an ordered,
-// de-duplicated expansion, so the warp performs each step in parallel with
-// ballots and prefix counts while keeping the reference's sequential order:
-// results are identical to the sequential algorithm.
+// cells and are independent, and the boundary rebuild is a de-duplicated
+// expansion whose order decides nothing (the next claim step again treats its
+// cells independently), so the warp performs each step in parallel with
+// ballots, prefix counts and atomic bit flags while keeping the reference's
+// sequential particle order: results are identical to the sequential algorithm.
 //
 // Per warp: owner/done bytes and particle coordinates in shared memory,
 // boundary lists (double-buffered per round) in a per-warp global scratch.
@@ -62,6 +63,11 @@ __global__ void k_max_count(int64_t n_el, const int32_t* off, int32_t* out) {
     if ((threadIdx.x & 31) == 0) atomicMax(out, m);
 }
 
+// c / R for 0 <= c < 4096 and 1 <= R <= 16 without an integer division: the
+// FP32 product c (1/R) is within 5e-4 of the exact quotient, whose fraction
+// is a multiple of 1/R >= 1/16, so adding 1e-3 and truncating gives floor(c / R).
+__device__ __forceinline__ int dvc_div(int c, float invR) { return (int)__fadd_rn(__fmul_rn((float)c, invR), 1e-3f); }
+
 template <int DIM>
 __global__ void __launch_bounds__(32 * DVC_WARPS) k_dvc(dvc_args a) {
     extern __shared__ unsigned char smem[];
@@ -87,6 +93,21 @@ __global__ void __launch_bounds__(32 * DVC_WARPS) k_dvc(dvc_args a) {
     __syncthreads();
     const double dx = (1.0 - -1.0) / R;
     const double da = DIM == 3 ? dx * dx * dx : dx * dx;
+    const float invR = 1.0f / (float)R;
+    // cell c -> (i, j, k) grid indices
+    auto cell_ijk = [&](int c) {
+        const int q = dvc_div(c, invR);
+        int3 r;
+        r.x = c - q * R;
+        if (DIM == 3) {
+            r.z = dvc_div(q, invR);
+            r.y = q - r.z * R;
+        } else {
+            r.y = q;
+            r.z = 0;
+        }
+        return r;
+    };
 
     int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -123,24 +144,28 @@ __global__ void __launch_bounds__(32 * DVC_WARPS) k_dvc(dvc_args a) {
                 int t = base + lane;
                 int c1 = -1;
                 bool ok = false;
+                bool keep = false;
                 if (t < total) {
                     int c0 = claimed[t / NNB], k = t % NNB;
-                    int ci = c0 % R, cj = (c0 / R) % R, ck = DIM == 3 ? c0 / (R * R) : 0;
-                    switch (k) {   // S, N, E, W, U, D
-                        case 0: c1 = cj > 0 ? c0 - R : -1; break;
-                        case 1: c1 = cj < R - 1 ? c0 + R : -1; break;
-                        case 2: c1 = ci < R - 1 ? c0 + 1 : -1; break;
-                        case 3: c1 = ci > 0 ? c0 - 1 : -1; break;
-                        case 4: c1 = ck < R - 1 ? c0 + R * R : -1; break;
-                        default: c1 = ck > 0 ? c0 - R * R : -1; break;
-                    }
+                    const int3 g = cell_ijk(c0);
+                    const int ci = g.x, cj = g.y, ck = g.z;
+                    // neighbour k in the order S, N, E, W, U, D, without a divergent switch
+                    const int coord = k < 2 ? cj : (k < 4 ? ci : ck);
+                    const int stride = k < 2 ? R : (k < 4 ? 1 : R * R);
+                    const bool up = k == 1 || k == 2 || k == 4;
+                    c1 = (up ? coord < R - 1 : coord > 0) ? c0 + (up ? stride : -stride) : -1;
                     ok = c1 >= 0 && owner[c1] != i && ((done[c1 >> 5] >> (c1 & 31)) & 1u) == 0u;
+                    // each cell once: the lane whose OR sets the cell's bit lists it.  The
+                    // order inside a boundary list is free: a particle's claims touch
+                    // distinct cells and its rebuilt list is a set, so no ownership
+                    // decision depends on it.
+                    if (ok) {
+                        const unsigned bit = 1u << (c1 & 31);
+                        keep = (atomicOr(&done[c1 >> 5], bit) & bit) == 0u;
+                    }
                 }
-                unsigned m = __match_any_sync(0xffffffffu, ok ? c1 : -2 - lane);
-                bool keep = ok && (__ffs(m) - 1 == lane);
                 unsigned kb = __ballot_sync(0xffffffffu, keep);
                 if (keep) {
-                    atomicOr(&done[c1 >> 5], 1u << (c1 & 31));   // lanes may share a word
                     int64_t pos = start + cnt + __popc(kb & lt);
                     if (pos < a.pcap) pool[dst][pos] = (int16_t)c1;
                 }
@@ -217,25 +242,27 @@ __global__ void __launch_bounds__(32 * DVC_WARPS) k_dvc(dvc_args a) {
                             // value is within 2e-5 of the exact one; only values near
                             // zero need the FP64 expression, whose sign is the result.
                             float fd;
+                            const int3 g = cell_ijk(c0);
+                            const int ci = g.x, cj = g.y, ck = g.z;
                             {
-                                const float fx0 = cenf[c0 % R], fy0 = cenf[(c0 / R) % R];
+                                const float fx0 = cenf[ci], fy0 = cenf[cj];
                                 const float fx1 = xf[o * 3 + 0], fy1 = xf[o * 3 + 1];
                                 fd = (fx1 + fpx - fx0 - fx0) * (fx1 - fpx) + (fy1 + fpy - fy0 - fy0) * (fy1 - fpy);
                                 if (DIM == 3) {
-                                    const float fz0 = cenf[c0 / (R * R)], fz1 = xf[o * 3 + 2];
+                                    const float fz0 = cenf[ck], fz1 = xf[o * 3 + 2];
                                     fd += (fz1 + fpz - fz0 - fz0) * (fz1 - fpz);
                                 }
                             }
                             if (fd > 1e-4f) take = true;
                             else if (fd < -1e-4f) take = false;
                             else {
-                            double x0 = cen[c0 % R], y0 = cen[(c0 / R) % R];
+                            double x0 = cen[ci], y0 = cen[cj];
                             double x1 = xs[o * 3 + 0], y1 = xs[o * 3 + 1];
                             double dist;
                             if (DIM == 2) {
                                 dist = (x1 + px - x0 - x0) * (x1 - px) + (y1 + py - y0 - y0) * (y1 - py);
                             } else {
-                                double z0 = cen[c0 / (R * R)], z1 = xs[o * 3 + 2];
+                                double z0 = cen[ck], z1 = xs[o * 3 + 2];
                                 dist = (x1 + px - x0 - x0) * (x1 - px) + (y1 + py - y0 - y0) * (y1 - py) +
                                        (z1 + pz - z0 - z0) * (z1 - pz);
                             }
@@ -302,10 +329,10 @@ __global__ void __launch_bounds__(32 * DVC_WARPS) k_dvc(dvc_args a) {
                 const int m = cnt[i], end = pos[i];
                 double sx = 0.0, sy = 0.0, sz = 0.0;
                 for (int k = end - m; k < end; k++) {
-                    const int c = claimed[k];
-                    sx += cen[c % R];
-                    sy += cen[(c / R) % R];
-                    if (DIM == 3) sz += cen[c / (R * R)];
+                    const int3 g = cell_ijk(claimed[k]);
+                    sx += cen[g.x];
+                    sy += cen[g.y];
+                    if (DIM == 3) sz += cen[g.z];
                 }
                 int64_t s = o0 + i;
                 a.ip_w[s] = m * da;

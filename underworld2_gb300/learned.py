@@ -383,16 +383,17 @@ class ProblemSet:
         f, scales = features(log_eta, rho, self.res, ctx.device)
         return f, scales
 
-    def solve(self, mixed, p0=None, p_dir=None, rtol=1e-8):
+    def solve(self, mixed, p0=None, p_dir=None, rtol=1e-8, coarse_agg=0):
         """Solve the assembled problem; p0: initial pressure, p_dir: first search
-        direction of the Schur FGMRES (both device tensors, or None)."""
+        direction of the Schur FGMRES (both device tensors, or None); coarse_agg > 0:
+        the coarse-level correction of the Schur FGMRES with that aggregate size."""
         ctx = self.ctx
         u = ctx.zeros(ctx.n_vdof)
         p = ctx.zeros(ctx.n_pdof) if p0 is None else p0.reshape(-1).to(torch.float64).contiguous().clone()
         d = None if p_dir is None else p_dir.reshape(-1).to(torch.float64).contiguous()
         st = ctx.solve(u, p, mixed=int(mixed), rtol=rtol, inner_rtol=1e-10, outer_rtol=1e-9, smooth_steps=2,
                        restart=120, schur_pc=1, max_outer=500, zero_guess=0 if p0 is not None else 1,
-                       p_dir=None if d is None else d.data_ptr())
+                       p_dir=None if d is None else d.data_ptr(), coarse_agg=int(coarse_agg))
         return u, p, st
 
 
@@ -440,19 +441,20 @@ def predict_pressure(net, f, scales):
     return p - p.mean()
 
 
-def solve_with_warm_start(ps, net, f, scales, rtol=1e-8, mode="direction"):
+def solve_with_warm_start(ps, net, f, scales, rtol=1e-8, mode="direction", coarse_agg=0):
     """Mixed-precision solve using the network's pressure -- as the first search
     direction of the Schur FGMRES (mode "direction": the iteration's least-squares
     step weighs it) or as the initial guess (mode "guess") -- and the plain FP64
-    solve if that does not reach rtol.  Returns (u, p, stats, fell_back)."""
+    solve if that does not reach rtol.  coarse_agg > 0 adds the coarse-level
+    correction of the Schur FGMRES.  Returns (u, p, stats, fell_back)."""
     p0 = predict_pressure(net, f, scales)
     try:
         if not bool(torch.isfinite(p0).all()):
             raise FloatingPointError("non-finite network output")
         if mode == "guess":
-            u, p, st = ps.solve(1, p0=p0, rtol=rtol)
+            u, p, st = ps.solve(1, p0=p0, rtol=rtol, coarse_agg=coarse_agg)
         else:
-            u, p, st = ps.solve(1, p_dir=p0, rtol=rtol)
+            u, p, st = ps.solve(1, p_dir=p0, rtol=rtol, coarse_agg=coarse_agg)
         if st["residual"] <= rtol:
             return u, p, st, False
     except (FloatingPointError, _native.UwgError):
