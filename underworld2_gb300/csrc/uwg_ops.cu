@@ -1493,31 +1493,36 @@ __global__ void k_dense_mv(int64_t n, const T* Ainv, const T* b, T* x) {
     if (lane == 0) x[i] = s;
 }
 
-// One Gauss-Jordan step on [A | B] over the whole grid (no pivoting: the coarse
-// matrices are symmetric positive definite once their null modes are fixed),
-// reading (Ai, Bi) and writing (Ao, Bo) so that row k is never read after it
-// is overwritten.
-__global__ void k_gj_step(int64_t n, int64_t k, const double* __restrict__ Ai, const double* __restrict__ Bi,
-                          double* __restrict__ Ao, double* __restrict__ Bo) {
-    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (idx >= n * n) return;
-    const int64_t i = idx / n, j = idx % n;
-    const double piv = Ai[k * n + k];
-    if (i == k) {
-        Ao[idx] = Ai[idx] / piv;
-        Bo[idx] = Bi[idx] / piv;
-    } else {
-        const double f = Ai[i * n + k] / piv;
-        Ao[idx] = j == k ? 0.0 : Ai[idx] - f * Ai[k * n + j];
-        Bo[idx] = Bi[idx] - f * Bi[k * n + j];
-    }
-}
-__global__ void k_identity(int64_t n, double* B) {
-    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (idx < n * n) B[idx] = (idx / n == idx % n) ? 1.0 : 0.0;
+// C = [A | I] (n x 2n, row-major) in both ping-pong buffers
+__global__ void k_gj_init(int64_t n, const double* __restrict__ A, double* __restrict__ C0, double* __restrict__ C1) {
+    const int64_t i = blockIdx.y, j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j >= 2 * n) return;
+    const double v = j < n ? A[i * n + j] : (j - n == i ? 1.0 : 0.0);
+    C0[i * 2 * n + j] = v;
+    C1[i * 2 * n + j] = v;
 }
 
-// B = A^-1 (A is overwritten).  Small matrices in one CTA; larger ones one
+// Gauss-Jordan pivot k on C = [A | B]: only columns k .. n + k change (A's
+// columns left of k are unit vectors, B's columns right of k are still the
+// identity's), so the grid covers that window; row i per blockIdx.y, one
+// reciprocal of the pivot per CTA.
+__global__ void k_gj_win(int64_t n, int64_t k, const double* __restrict__ Ci, double* __restrict__ Co) {
+    __shared__ double inv;
+    if (threadIdx.x == 0) inv = 1.0 / Ci[k * 2 * n + k];
+    __syncthreads();
+    const int64_t i = blockIdx.y, j = k + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j > n + k) return;
+    const int64_t ld = 2 * n;
+    const double rk = Ci[k * ld + j] * inv;
+    Co[i * ld + j] = (i == k) ? rk : Ci[i * ld + j] - Ci[i * ld + k] * rk;
+}
+
+__global__ void k_gj_extract(int64_t n, const double* __restrict__ C, double* __restrict__ B) {
+    const int64_t i = blockIdx.y, j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j < n) B[i * n + j] = C[i * 2 * n + n + j];
+}
+
+// B = A^-1 (the one-CTA path overwrites A).  Small matrices in one CTA; larger ones one
 // grid-wide launch per pivot (a single CTA took 0.6 s at n = 1024).
 int uwg_ops_dense_invert(uwg_ctx* c, int64_t n, double* A, double* B) {
     if (n <= 256) {
@@ -1528,19 +1533,20 @@ int uwg_ops_dense_invert(uwg_ctx* c, int64_t n, double* A, double* B) {
     return uwg_ops_dense_invert_grid(c, n, A, B);
 }
 int uwg_ops_dense_invert_grid(uwg_ctx* c, int64_t n, double* A, double* B) {
-    double *A2 = nullptr, *B2 = nullptr;
-    UWG_CUDA(c, cudaMallocAsync((void**)&A2, sizeof(double) * n * n, c->stream));
-    UWG_CUDA(c, cudaMallocAsync((void**)&B2, sizeof(double) * n * n, c->stream));
-    k_identity<<<nblk(n * n), 256, 0, c->stream>>>(n, B);
-    double *a = A, *b = B, *ao = A2, *bo = B2;
+    if (n < 1 || n > 65535) return uwg_set_error(c, UWG_ERR_ARG, "dense inverse: n out of range");
+    double *C0 = nullptr, *C1 = nullptr;
+    UWG_CUDA(c, cudaMallocAsync((void**)&C0, sizeof(double) * 2 * n * n, c->stream));
+    UWG_CUDA(c, cudaMallocAsync((void**)&C1, sizeof(double) * 2 * n * n, c->stream));
+    k_gj_init<<<dim3(nblk(2 * n), (unsigned)n), 256, 0, c->stream>>>(n, A, C0, C1);
+    double *ci = C0, *co = C1;
+    const dim3 grid(nblk(n + 1), (unsigned)n);
     for (int64_t k = 0; k < n; k++) {
-        k_gj_step<<<nblk(n * n), 256, 0, c->stream>>>(n, k, a, b, ao, bo);
-        std::swap(a, ao);
-        std::swap(b, bo);
+        k_gj_win<<<grid, 256, 0, c->stream>>>(n, k, ci, co);
+        std::swap(ci, co);
     }
-    if (b != B) UWG_CUDA(c, cudaMemcpyAsync(B, b, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, c->stream));
-    cudaFreeAsync(A2, c->stream);
-    cudaFreeAsync(B2, c->stream);
+    k_gj_extract<<<dim3(nblk(n), (unsigned)n), 256, 0, c->stream>>>(n, ci, B);
+    cudaFreeAsync(C0, c->stream);
+    cudaFreeAsync(C1, c->stream);
     UWG_CUDA(c, cudaGetLastError());
     return UWG_OK;
 }

@@ -141,6 +141,15 @@ int work_init(uwg_ctx* c, int restart) {
     return UWG_OK;
 }
 
+// Deterministic probe vectors (power-iteration starts, the ||G|| estimate),
+// filled on the device: x[i] = c0 + a sin(b i) + c (-1)^(i+1).  Dirichlet dofs
+// are zeroed by the caller.
+template <typename T>
+__global__ void k_power_start(int64_t n, double c0, double a, double b, double cterm, T* x) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) x[i] = (T)(c0 + a * sin(b * (double)i) + ((i & 1) ? cterm : -cterm));
+}
+
 // Host reductions through the context's pinned mirror.
 template <typename T>
 int dots(uwg_ctx* c, int64_t n, int k, const T* const* a, const T* const* b, double* out) {
@@ -608,15 +617,13 @@ int g_norm_inf(uwg_ctx* c, double* out) {
         return UWG_OK;
     }
     int64_t np = c->n_pdof;
-    std::vector<double> z(np);
-    for (int64_t i = 0; i < np; i++) z[i] = std::sin(1.37 * (double)i) + ((i & 1) ? 0.3 : -0.3);
-    UWG_CUDA(c, cudaMemcpyAsync(w->ns_tmp, z.data(), sizeof(double) * np, cudaMemcpyHostToDevice, s));
+    k_power_start<double><<<(unsigned)((np + 255) / 256), 256, 0, s>>>(np, 0.0, 1.0, 1.37, 0.3, w->ns_tmp);
     if ((rc = uwg_ops_applyG(c, w->ns_tmp, w->u_tmp))) return rc;
     double d[2];
     const double* a1[1] = {w->u_tmp};
     if ((rc = dots<double>(c, c->n_vdof, 1, a1, a1, d))) return rc;
     const double* a2[1] = {w->ns_tmp};
-    if ((rc = dots<double>(c, np, 1, a2, a2, d + 1))) return rc;   // synchronises: z outlives its copy
+    if ((rc = dots<double>(c, np, 1, a2, a2, d + 1))) return rc;
     *out = d[1] > 0.0 ? std::sqrt(d[0] / d[1]) : 1.0;
     return UWG_OK;
 }
@@ -692,9 +699,7 @@ int bfbt_setup(uwg_ctx* c) {
         // largest eigenvalue of D^-1 A by power iteration (Chebyshev interval)
         int64_t n = uwg_pmg_ncomp(l) * c->lev[l].n_el;
         LevelVecs<float>& v = w->pv[l];
-        std::vector<float> hv(n);
-        for (int64_t i = 0; i < n; i++) hv[i] = (float)(1.0 + 0.41 * std::sin(1.37 * (double)i) + ((i & 1) ? 0.3 : -0.3));
-        UWG_CUDA(c, cudaMemcpyAsync(v.x, hv.data(), sizeof(float) * n, cudaMemcpyHostToDevice, s));
+        k_power_start<float><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, 1.0, 0.41, 1.37, 0.3, v.x);
         double lam = 1.0;
         for (int it = 0; it < 30; it++) {
             if ((rc = papply(c, l, v.x, v.t))) return rc;
@@ -707,7 +712,6 @@ int bfbt_setup(uwg_ctx* c) {
             vk_copy<float>(s, n, v.d, v.x);
             vk_scale<float>(s, n, (float)(1.0 / std::sqrt(d2[0])), v.x);
         }
-        UWG_CUDA(c, cudaStreamSynchronize(s));   // the host vector must outlive its copy
         w->Lmax[l] = lam;
     }
     return uwg_pmg_dense_inverse(c, c->pnlev - 1, w->pst[c->pnlev - 1], w->cb_null ? 1 : 0, w->pcinv);
@@ -729,33 +733,33 @@ void uwg_solver_free(uwg_ctx* c) {
     c->ws.clear();
 }
 
-// Lanczos-free eigenvalue bound: power iteration on D^-1 K.
+// Lanczos-free eigenvalue bound: power iteration on D^-1 K with the FP32
+// operator (the Chebyshev interval [0.1, 1.2] lambda needs two digits; the FP64
+// apply costs 25x more on this GPU's FP64 pipe).
 int uwg_solver_estimate(uwg_ctx* c, int l) {
     uwg_level& L = c->lev[l];
     int rc = work_init(c, 30);
     if (rc) return rc;
     Work* w = work_of(c);
-    LevelVecs<double>& v = w->v64[l];
+    LevelVecs<float>& v = w->v32[l];
     cudaStream_t s = c->stream;
     int64_t n = L.n_dof;
     // deterministic start vector: 1 + small variation, BC dofs zero
-    std::vector<double> h(n);
-    for (int64_t i = 0; i < n; i++) h[i] = 1.0 + 0.37 * std::sin(0.731 * (double)i);
-    UWG_CUDA(c, cudaMemcpyAsync(v.x, h.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
-    vk_mask<double>(s, n, L.bc, v.x);
+    k_power_start<float><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, 1.0, 0.37, 0.731, 0.0, v.x);
+    vk_mask<float>(s, n, L.bc, v.x);
     double lam = 0.0;
     for (int it = 0; it < 30; it++) {
-        if ((rc = uwg_ops_applyK<double>(c, l, v.x, v.t))) return rc;
-        vk_mask<double>(s, n, L.bc, v.t);
-        vk_pointwise_div<double>(s, n, v.t, L.diag64, v.d);
+        if ((rc = uwg_ops_applyK<float>(c, l, v.x, v.t))) return rc;
+        vk_mask<float>(s, n, L.bc, v.t);
+        vk_pointwise_div<float>(s, n, v.t, L.diag32, v.d);
         double d2[2];
-        const double* a[2] = {v.d, v.x};
-        const double* b[2] = {v.d, v.x};
-        if ((rc = dots<double>(c, n, 2, a, b, d2))) return rc;
+        const float* a[2] = {v.d, v.x};
+        const float* b[2] = {v.d, v.x};
+        if ((rc = dots<float>(c, n, 2, a, b, d2))) return rc;
         if (d2[1] <= 0.0) break;
         lam = std::sqrt(d2[0] / d2[1]);
-        vk_copy<double>(s, n, v.d, v.x);
-        vk_scale<double>(s, n, 1.0 / std::sqrt(d2[0]), v.x);
+        vk_copy<float>(s, n, v.d, v.x);
+        vk_scale<float>(s, n, (float)(1.0 / std::sqrt(d2[0])), v.x);
     }
     L.lmax64 = L.lmax32 = lam > 0.0 ? lam : 1.0;
     return UWG_OK;
