@@ -518,6 +518,38 @@ def run_kernel(args):
                       "ms_per_launch": s.elapsed_time(e) / args.reps}))
 
 
+def run_gemm(args):
+    """The CNN's forward GEMM (BF16 operands, FP32 accumulation, BF16 output)
+    on the shape of a 128-channel 3x3 convolution over 16 problems of 128^2
+    cells: M = 262144 pixels, N = 128 output channels, K = 9 x 128, `--reps`
+    launches on the tcgen05 path and on the mma.sync path."""
+    import torch
+    from underworld2_gb300._core import Context
+    from underworld2_gb300.learned import _Ops
+    ops = _Ops(Context(2, (8, 8), (0.0, 0.0), (1.0, 1.0)))
+    M, N, K = 262144, 128, 1152
+    g = torch.Generator(device="cuda").manual_seed(0)
+    A = torch.randn((M, K), device="cuda", generator=g).to(torch.bfloat16)
+    B = torch.randn((N, K), device="cuda", generator=g).to(torch.bfloat16)
+    C = torch.empty((M, N), device="cuda", dtype=torch.bfloat16)
+    out = {"kernel": "cnn_gemm", "M": M, "N": N, "K": K, "reps": args.reps}
+    for path, name in ((0, "tcgen05"), (1, "mma_sync")):
+        ops.set_path(path)
+        ops.gemm(M, N, K, A, K, 0, B, K, 1, Cb=C, ldc=N)
+        ops.check()
+        s_, e_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s_.record()
+        for _ in range(args.reps):
+            ops.gemm(M, N, K, A, K, 0, B, K, 1, Cb=C, ldc=N)
+        e_.record()
+        ops.check()
+        ms = s_.elapsed_time(e_) / args.reps
+        out[name] = {"ms_per_launch": ms, "tflops": 2.0 * M * N * K / ms / 1e9,
+                     "hbm_gbs": 2.0 * (M * K + N * K + M * N) / ms / 1e6}
+    ops.set_path(0)
+    print(json.dumps(out))
+
+
 def run_rk2(args):
     """`--reps` RK2 steps (FP32 coordinate storage, FP64 arithmetic) through a
     cellular velocity field on the workload's mesh, with --kernel-ppc particles per
@@ -985,7 +1017,7 @@ def main():
     ap.add_argument("--schur-pc", type=int, default=1, help="0: Uzawa S^ (reference), 1: scaled BFBt")
     ap.add_argument("--bfbt-rtol", type=float, default=3e-2)
     ap.add_argument("--bfbt-its", type=int, default=0, help="> 0: fixed CG iterations per BFBt L-solve")
-    ap.add_argument("--kernel", choices=["applyK32", "applyK64", "advdiff", "slcn", "rk2"],
+    ap.add_argument("--kernel", choices=["applyK32", "applyK64", "advdiff", "slcn", "rk2", "cnn_gemm"],
                     help="only launch one operator kernel, or time SUPG / SLCN advection-diffusion steps (profiling)")
     ap.add_argument("--kernel-ppc", type=int, default=0)
     ap.add_argument("--profile-solve", action="store_true", help="one untimed solve (profiling target)")
@@ -1011,6 +1043,9 @@ def main():
         return
     if args.kernel == "slcn":
         run_slcn(args)
+        return
+    if args.kernel == "cnn_gemm":
+        run_gemm(args)
         return
     if args.kernel:
         run_kernel(args)
