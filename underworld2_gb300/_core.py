@@ -18,6 +18,16 @@ def _ptr(t):
     return ctypes.c_void_p(t.data_ptr()) if t is not None else None
 
 
+def host_array(shape, dtype):
+    """Zeroed numpy array in page-locked host memory when a GPU is visible (copies
+    to and from the device then run at DMA speed, without a staging copy), plain
+    numpy memory otherwise.  The array keeps its backing tensor alive."""
+    if torch.cuda.is_available():
+        t = torch.zeros(tuple(shape), dtype=torch.from_numpy(np.zeros(0, dtype=dtype)).dtype, pin_memory=True)
+        return t.numpy()
+    return np.zeros(shape, dtype=dtype)
+
+
 def _require_cuda():
     if not torch.cuda.is_available():
         raise RuntimeError("underworld2_gb300 needs a CUDA GPU (sm_103a); none is visible")

@@ -317,7 +317,7 @@ class MeshVariable:
             raise ValueError("only 'double' mesh variables are supported")
         self.mesh = mesh
         self.nodeDofCount = int(nodeDofCount)
-        self._data = np.zeros((mesh.nodesGlobal, self.nodeDofCount))
+        self._data = _core.host_array((mesh.nodesGlobal, self.nodeDofCount), np.float64)
         self._dev = None
 
     @property
@@ -349,15 +349,17 @@ class MeshVariable:
 
     def _to_device(self):
         ctx = self._primary().ctx
-        t = torch.from_numpy(np.ascontiguousarray(self._data).ravel()).to(ctx.device)
-        if self._dev is None or self._dev.shape != t.shape:
-            self._dev = t.clone()
-        else:
-            self._dev.copy_(t)
+        host = torch.from_numpy(np.ascontiguousarray(self._data).reshape(-1))
+        if self._dev is None or self._dev.shape != host.shape:
+            self._dev = torch.empty(host.shape, dtype=host.dtype, device=ctx.device)
+        self._dev.copy_(host)
         return self._dev
 
     def _from_device(self):
-        self._data[...] = self._dev.cpu().numpy().reshape(self._data.shape)
+        if self._data.flags.c_contiguous:
+            torch.from_numpy(self._data.reshape(-1)).copy_(self._dev)
+        else:
+            self._data[...] = self._dev.cpu().numpy().reshape(self._data.shape)
 
     def _as_function(self):
         return _fn._MeshVar(self)

@@ -35,7 +35,7 @@ class SwarmVariable:
         self.count = int(count)
         np_dt = {"double": np.float64, "float": np.float32, "int": np.int32, "char": np.int8,
                  "short": np.int16, "long": np.int64}[dataType]
-        self._data = np.zeros((swarm.particleLocalCount, self.count), dtype=np_dt)
+        self._data = _core.host_array((swarm.particleLocalCount, self.count), np_dt)
         self._dev = None
         self._dirty = True
 
@@ -54,13 +54,23 @@ class SwarmVariable:
 
     def _resize(self, n):
         old = self._data
-        self._data = np.zeros((n, self.count), dtype=old.dtype)
+        self._data = _core.host_array((n, self.count), old.dtype)
         self._data[: min(n, len(old))] = old[: min(n, len(old))]
+        self._dirty = True
+
+    def _set_rows(self, rows):
+        """Replace the data by the given rows (a population change), in page-locked memory."""
+        new = _core.host_array(rows.shape, self._data.dtype)
+        new[...] = rows
+        self._data = new
         self._dirty = True
 
     def _device_data(self):
         if self._dirty or self._dev is None:
-            self._dev = torch.from_numpy(np.ascontiguousarray(self._data)).to(self.swarm.mesh.ctx.device)
+            host = torch.from_numpy(np.ascontiguousarray(self._data))
+            if self._dev is None or self._dev.shape != host.shape or self._dev.dtype != host.dtype:
+                self._dev = torch.empty(host.shape, dtype=host.dtype, device=self.swarm.mesh.ctx.device)
+            self._dev.copy_(host)
             self._dirty = False
         return self._dev
 
@@ -177,7 +187,8 @@ class Swarm:
         self._lst = None
         self._variables = []
         self._state = 0
-        self._host_x = None
+        self._host_x = None          # page-locked host mirror of the coordinates (kept between uses)
+        self._host_valid = False     # the mirror equals the device coordinates
         self._writable = False
         self._voronoi = None
         self.particleCoordinates = _CoordVariable(self)
@@ -198,10 +209,16 @@ class Swarm:
 
     @property
     def data(self):
-        if self._host_x is None:
-            self._host_x = np.zeros((0, self.dim)) if self._x is None else np.array(self._x.cpu().numpy(), copy=True)
-        self._host_x.flags.writeable = self._writable
-        return self._host_x
+        if self._x is None:
+            self._host_x = np.zeros((0, self.dim))
+        elif not self._host_valid or self._host_x is None or self._host_x.shape != tuple(self._x.shape):
+            if self._host_x is None or self._host_x.shape != tuple(self._x.shape):
+                self._host_x = _core.host_array(tuple(self._x.shape), np.float64)
+            torch.from_numpy(self._host_x).copy_(self._x)
+            self._host_valid = True
+        view = self._host_x.view()   # the mirror itself stays writeable; views carry the flag
+        view.flags.writeable = self._writable
+        return view
 
     def add_variable(self, dataType, count):
         v = SwarmVariable(self, dataType, count)
@@ -313,7 +330,7 @@ class Swarm:
         self._owner, self._off, self._lst = owner, off, lst
         for v in self._variables:
             v._resize(self.particleLocalCount)
-        self._host_x = None
+        self._host_valid = False
         self._toggle_state()
 
     def _toggle_state(self):
@@ -330,8 +347,7 @@ class Swarm:
             yield
         finally:
             self._writable = False
-            self._x.copy_(torch.from_numpy(np.ascontiguousarray(self._host_x)).to(self._x.device))
-            self._host_x = None
+            self._x.copy_(torch.from_numpy(self._host_x))   # the mirror stays equal to the device copy
             if update_owners:
                 self.update_particle_owners()
 
@@ -344,7 +360,6 @@ class Swarm:
         if lost:
             np_new = ctx.pop_plan_escaped(self._owner, self._off, self._lst)
             self._apply_population(np_new, None)
-        self._host_x = None
         self._toggle_state()
         if lost and not self.particleEscape:
             raise RuntimeError("Particles appear to have left the domain, but swarm flag `particleEscape` is False. "
@@ -356,10 +371,9 @@ class Swarm:
         """Write the library's pending deletion/creation plan into the particle arrays."""
         x, owner, off, lst, src = self.mesh.ctx.pop_apply(ip_xi, self._x, np_new)
         for v in self._variables:
-            v._data = np.ascontiguousarray(v._data[src])
-            v._dirty = True
+            v._set_rows(v._data[src])
         self._x, self._owner, self._off, self._lst = x, owner, off, lst
-        self._host_x = None
+        self._host_valid = False
 
     # -- the PIC integration swarm ---------------------------------------------
     @property

@@ -719,7 +719,7 @@ class SwarmAdvector:
                                "outside the global domain." % failed)
         if not bool(torch.isfinite(s._x).all()):
             raise RuntimeError("particle coordinates are not finite after advection")
-        s._host_x = None
+        s._host_valid = False
         s._toggle_state()
         if update_owners:
             s.update_particle_owners()
