@@ -40,8 +40,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 CONFIGS = {
-    "grf3d": dict(dim=3, res=(128, 128, 128), ppc=20, kind="grf"),
-    "grf3d_small": dict(dim=3, res=(32, 32, 32), ppc=20, kind="grf"),
+    # smooth: Chebyshev degree of the velocity multigrid smoother (degree 1 is the
+    # fastest on the GRF workload: more but cheaper MG-CG iterations)
+    "grf3d": dict(dim=3, res=(128, 128, 128), ppc=20, kind="grf", smooth=1),
+    "grf3d_small": dict(dim=3, res=(32, 32, 32), ppc=20, kind="grf", smooth=1),
     "sinker2d": dict(dim=2, res=(64, 64), ppc=20, kind="sinker"),
     # 2D Q2/dPc1 Rayleigh-Taylor layering, 40 particles per element
     "rt2d_q2": dict(dim=2, res=(256, 256), ppc=40, kind="rt", order=2, porder=1),
@@ -192,7 +194,7 @@ def run_gpu(args):
     npart = x0.shape[0]
     u = ctx.zeros(ctx.n_vdof)
     p = ctx.zeros(ctx.n_pdof)
-    opts = dict(rtol=1e-8, inner_rtol=args.inner_rtol, outer_rtol=args.outer_rtol, smooth_steps=2, restart=120,
+    opts = dict(rtol=1e-8, inner_rtol=args.inner_rtol, outer_rtol=args.outer_rtol, smooth_steps=cfg.get("smooth", 2), restart=120,
                 schur_pc=args.schur_pc if cfg.get("porder", 0) == 0 else 0, schur_pc_rtol=args.bfbt_rtol, schur_pc_its=args.bfbt_its, max_outer=args.max_outer)
     ev = lambda: torch.cuda.Event(enable_timing=True)
 
@@ -378,7 +380,7 @@ def e2e_api(args, cfg, x_h, eta_h, body_h, mixed):
     solver.set_inner_method("mixed" if mixed else "mg")
     solver.set_inner_rtol(args.inner_rtol)
     solver.set_outer_rtol(1e-8)   # the metric's relative residual
-    solver.options.mg.smooth_steps = 2
+    solver.options.mg.smooth_steps = cfg.get("smooth", 2)
     solver.options.scr.restart = 120
     x_h = np.ascontiguousarray(x_h)
     eta_h = np.ascontiguousarray(eta_h).reshape(-1)
@@ -909,7 +911,7 @@ def run_profile_solve(args):
     ctx.assemble(off, lst, ip_xi, ip_w, eta, body)
     u, p = ctx.zeros(ctx.n_vdof), ctx.zeros(ctx.n_pdof)
     st = ctx.solve(u, p, mixed=1 if args.mode == "mixed" else 0, rtol=1e-8, inner_rtol=args.inner_rtol,
-                   outer_rtol=args.outer_rtol, smooth_steps=2, restart=120, schur_pc=args.schur_pc if cfg.get("porder", 0) == 0 else 0,
+                   outer_rtol=args.outer_rtol, smooth_steps=cfg.get("smooth", 2), restart=120, schur_pc=args.schur_pc if cfg.get("porder", 0) == 0 else 0,
                    schur_pc_rtol=args.bfbt_rtol, schur_pc_its=args.bfbt_its, max_outer=args.max_outer)
     torch.cuda.synchronize()
     print(json.dumps({"profile_solve": args.config, "particles_per_cell": ppc,

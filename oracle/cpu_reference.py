@@ -3,7 +3,8 @@
 Times the oracle -- the reference's algorithms restated in C (uwo.c) plus the
 CPU BSSCR solver (uwo_solve.c) -- with OpenMP on all host cores.  The solver
 runs the GPU library's algorithm: velocity solves by multigrid-preconditioned
-CG (Chebyshev degree 2), flexible GMRES on the Schur complement with the
+CG (Chebyshev smoother of the workload's degree: 1 for the 3D GRF workload,
+2 in the pairings), flexible GMRES on the Schur complement with the
 weighted scaled BFBt preconditioner and its pressure multigrid (the CPU port
 in uwo_solve.c), FP64 vectors.
 
@@ -34,10 +35,11 @@ import numpy as np
 import oracle
 
 # Iteration counts of the GPU's plain FP64 solve (weighted BFBt, pressure-
-# Laplacian tolerance 3e-2, smoother degree 2) of the 3D 128^3 GRF workload,
-# measured by bench.py on a GB300 (its "fp64_solve" entry): 25 outer, 360
+# Laplacian tolerance 3e-2 with pressure-smoother degree 2, velocity-smoother
+# degree 1 as the workload's configuration sets) of the 3D 128^3 GRF workload,
+# measured by bench.py on a GB300 (its "fp64_solve" entry): 25 outer, 485
 # velocity MG-CG, 1676 pressure-Laplacian CG iterations.
-GPU_FP64_ITS = {(3, (128, 128, 128)): {"pressure_its": 25, "velocity_total_its": 360, "schur_pc_its": 1676}}
+GPU_FP64_ITS = {(3, (128, 128, 128)): {"pressure_its": 25, "velocity_total_its": 485, "schur_pc_its": 1676}}
 
 FULL_SOLVE_MAX_EL = 70000
 SMOOTH = 2
@@ -135,7 +137,7 @@ class CPUBaseline:
         self.full = None
         if self.n_el <= FULL_SOLVE_MAX_EL:
             t0 = time.perf_counter()
-            u, p, st = self.s.solve(inner_rtol=1e-10, outer_rtol=1e-9, max_outer=2000, deg=SMOOTH)
+            u, p, st = self.s.solve(inner_rtol=1e-10, outer_rtol=1e-9, max_outer=2000, deg=self.cfg.get("smooth", SMOOTH))
             st["solve_s"] = time.perf_counter() - t0
             self.full = st
         elif (dim, res) not in GPU_FP64_ITS:
@@ -157,7 +159,7 @@ class CPUBaseline:
         t0 = time.perf_counter()
         self._map(0, self.n_s)
         t_map = (time.perf_counter() - t0) * self.n_el / self.n_s
-        tv, tl = self.s.time_iterations(1, 2, SMOOTH)
+        tv, tl = self.s.time_iterations(1, 2, self.cfg.get("smooth", SMOOTH))
         xs = self.x[: self.n_p].copy()
         t0 = time.perf_counter()
         self.m.rk2(self.vel, 0.1 / max(self.res), xs)
