@@ -165,15 +165,17 @@ def test_config2_rayleigh_taylor_q2_64(gpu):
     _check(st, u, p, uo, po, null_vectors=[np.ones(len(po))])
 
 
-def test_config3_grf_16(gpu):
-    """3D 16^3 Q1/dQ0, viscosity exp(-11.5 T) (contrast 1e5), body force Ra T z, 20 ppc."""
+@pytest.mark.parametrize("mixed", [0, 1])
+def test_config3_grf_16(gpu, mixed):
+    """3D 16^3 Q1/dQ0, viscosity exp(-11.5 T) (contrast 1e5), body force Ra T z, 20 ppc;
+    plain FP64 and mixed precision (FP32 inner solves, double-float refinement residuals)."""
     case = Case(3, (16, 16, 16), 20)
     T = grf_numpy(case.xo, seed=1234)
     eta = np.exp(-11.5 * T)
     body = np.zeros((len(T), 3))
     body[:, 2] = 1e6 * T
     mask = case.walls([[0], [1], [2]])
-    st, u, p, uo, po = case.run(eta, body, mask)
+    st, u, p, uo, po = case.run(eta, body, mask, mixed=mixed)
     _check(st, u, p, uo, po, null_vectors=[np.ones(len(po))])
 
 

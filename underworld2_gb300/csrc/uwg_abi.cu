@@ -31,6 +31,7 @@ extern "C" void uwg_ctx_destroy(uwg_ctx* c) {
         cudaFree(L.W64); cudaFree(L.W32); cudaFree(L.bc); cudaFree(L.diag64); cudaFree(L.diag32);
         if (L.cinv64) cudaFree(L.cinv64);
         if (L.tile_bc) cudaFree(L.tile_bc);
+        if (L.Wdf) cudaFree(L.Wdf);
         for (int d = 0; d < 3; d++) if (L.h2inv[d]) cudaFree(L.h2inv[d]);
         if (L.cinv32) cudaFree(L.cinv32);
     }

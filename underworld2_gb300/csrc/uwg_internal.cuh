@@ -28,6 +28,7 @@ struct uwg_level {
     double lmax64, lmax32; // Chebyshev upper bound for D^-1 K
     uint8_t* tile_bc;     // 3D Q1: per 8x8x4 tile, 1 when the tile holds a Dirichlet dof (tiled apply)
     float* h2inv[3];      // order-1 levels: 2 / (element size) per axis index, FP32 (tiled apply)
+    float2* Wdf;          // 3D Q1 level 0: W as double-float pairs (hi, lo) for the refinement residual
     // dense coarse solve (coarsest level only)
     double* cinv64;
     float* cinv32;

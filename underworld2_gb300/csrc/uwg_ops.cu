@@ -208,6 +208,38 @@ __global__ void k_diag_bc(int64_t n, const uint8_t* bc, double* diag, float* dia
 // Matrix-free K apply, sum-factorised on the 3-point rule.
 // y = P K P x + (I - P) x with P zeroing Dirichlet dofs.
 // ---------------------------------------------------------------------------
+// Double-float numbers: value = hi + lo with |lo| <= ulp(hi) / 2, about 48
+// significant bits from FP32 operations (Dekker's TwoProd through fmaf,
+// Knuth's TwoSum; the intrinsics keep the compiler from contracting them).
+// The element arithmetic of the FP64 refinement residual runs in it on the
+// FP32 pipe, which on this GPU issues far more than the FP64 one.
+struct dfl {
+    float hi, lo;
+    __device__ __forceinline__ dfl() {}
+    __device__ __forceinline__ dfl(double v) : hi((float)v), lo((float)(v - (double)(float)v)) {}
+    __device__ __forceinline__ dfl(float h, float l) : hi(h), lo(l) {}
+};
+__device__ __forceinline__ dfl operator+(dfl a, dfl b) {
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float bb = __fsub_rn(s, a.hi);
+    const float err = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+    const float t = __fadd_rn(err, __fadd_rn(a.lo, b.lo));
+    const float h = __fadd_rn(s, t);
+    return dfl(h, __fsub_rn(t, __fsub_rn(h, s)));
+}
+__device__ __forceinline__ dfl operator-(dfl a) { return dfl(-a.hi, -a.lo); }
+__device__ __forceinline__ dfl operator-(dfl a, dfl b) { return a + (-b); }
+__device__ __forceinline__ dfl operator*(dfl a, dfl b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    const float h = __fadd_rn(p, e);
+    return dfl(h, __fsub_rn(e, __fsub_rn(h, p)));
+}
+__device__ __forceinline__ dfl& operator+=(dfl& a, dfl b) { a = a + b; return a; }
+__device__ __forceinline__ dfl& operator-=(dfl& a, dfl b) { a = a - b; return a; }
+
 template <typename T>
 __device__ __forceinline__ void up3(T a, T b, T* o) { o[0] = a; o[1] = (T)0.5 * (a + b); o[2] = b; }
 
@@ -633,6 +665,67 @@ __global__ void __launch_bounds__(KT_N, STAGE_W ? 2 : 1) k_applyK_q1_3d_tiled(
     }
 }
 
+// The FP64 tiled apply (staging, Dirichlet rows, write-back as in
+// k_applyK_q1_3d_tiled<double>) with the element arithmetic in double-float:
+// nodal values converted on their way out of shared memory, W from its
+// double-float copy, outputs accumulated in FP64.  For the refinement
+// residual b - K x of the mixed-precision velocity solves.
+__global__ void __launch_bounds__(KT_N, 1) k_applyK_q1_3d_tiled_df(uwg_lgeom g, const dfl* __restrict__ Wd,
+                                                                   const uint8_t* __restrict__ bc,
+                                                                   const uint8_t* __restrict__ tile_bc,
+                                                                   const double* __restrict__ x, double* __restrict__ y) {
+    __shared__ __align__(16) double xs[KT_NN3];
+    __shared__ double ys[KT_NN3];
+    __shared__ uint8_t bs[KT_NN3];
+    constexpr int NX = KT_X + 1, NY = KT_Y + 1;
+    const int ntx = (g.res[0] + KT_X - 1) / KT_X, nty = (g.res[1] + KT_Y - 1) / KT_Y;
+    const int tile = blockIdx.x;
+    const int tx0 = (tile % ntx) * KT_X, ty0 = ((tile / ntx) % nty) * KT_Y, tz0 = (tile / (ntx * nty)) * KT_Z;
+    const int li = threadIdx.x % KT_X, lj = (threadIdx.x / KT_X) % KT_Y, lk = threadIdx.x / (KT_X * KT_Y);
+    const int ex = tx0 + li, ey = ty0 + lj, ez = tz0 + lk;
+    const bool own = ex < g.res[0] && ey < g.res[1] && ez < g.res[2];
+    const int64_t e = own ? ex + (int64_t)g.res[0] * (ey + (int64_t)g.res[1] * ez) : 0;
+    kt_stage_x<double>(g, tx0, ty0, tz0, x, xs);
+    cp_async_commit();
+    const bool has_bc = tile_bc[tile] != 0;
+    if (has_bc) kt_stage_bc(g, tx0, ty0, tz0, bc, bs);
+    for (int k = threadIdx.x; k < KT_NN3; k += KT_N) ys[k] = 0.0;
+    dfl hx(1.0), hy(1.0), hz(1.0);
+    if (own) {
+        hx = dfl(2.0 / (g.ax[0][ex + 1] - g.ax[0][ex]));
+        hy = dfl(2.0 / (g.ax[1][ey + 1] - g.ax[1][ey]));
+        hz = dfl(2.0 / (g.ax[2][ez + 1] - g.ax[2][ez]));
+    }
+    cp_async_wait<0>();
+    __syncthreads();
+    if (own) {
+        dfl u[8][3], out[8][3];
+#pragma unroll
+        for (int n = 0; n < 8; n++) {
+            const int sl = (li + (n & 1)) + NX * ((lj + ((n >> 1) & 1)) + NY * (lk + ((n >> 2) & 1)));
+#pragma unroll
+            for (int c = 0; c < 3; c++) u[n][c] = (has_bc && bs[sl * 3 + c]) ? dfl(0.f, 0.f) : dfl(xs[sl * 3 + c]);
+        }
+        q1_3d_element<dfl>(Wd + e, g.n_el, hx, hy, hz, u, out);
+#pragma unroll
+        for (int n = 0; n < 8; n++) {
+            const int sl = (li + (n & 1)) + NX * ((lj + ((n >> 1) & 1)) + NY * (lk + ((n >> 2) & 1)));
+#pragma unroll
+            for (int c = 0; c < 3; c++) atomicAdd(&ys[sl * 3 + c], (double)out[n][c].hi + (double)out[n][c].lo);
+        }
+    }
+    __syncthreads();
+    kt_writeback<double>(g, tx0, ty0, tz0, has_bc, xs, bs, ys, y);
+}
+
+__global__ void k_split_w_df(int64_t n, const double* __restrict__ w, float2* __restrict__ out) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) {
+        const float hi = (float)w[i];
+        out[i] = make_float2(hi, (float)(w[i] - (double)hi));
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(128) k_applyK_q1_2d(uwg_lgeom g, const T* __restrict__ W,
                                                       const uint8_t* __restrict__ bc, bool mask_in,
@@ -740,6 +833,13 @@ int uwg_ops_applyK_refine(uwg_ctx* c, const double* x, double* y) {
     if (L.order == 2 && c->dim == 3 && c->q2_ke_df) {
         k_bc_copy<double><<<nblk(L.n_dof), 256, 0, c->stream>>>(L.n_dof, L.bc, x, y);
         return uwg_q2_3d_applyK_df(c, x, y);
+    }
+    if (L.order == 1 && c->dim == 3 && L.Wdf && L.tile_bc) {
+        UWG_CUDA(c, cudaMemsetAsync(y, 0, sizeof(double) * L.n_dof, c->stream));
+        k_applyK_q1_3d_tiled_df<<<(unsigned)uwg_ops_ktiles(L.res), KT_N, 0, c->stream>>>(
+            uwg_level_geom(c, 0), reinterpret_cast<const dfl*>(L.Wdf), L.bc, L.tile_bc, x, y);
+        UWG_CUDA(c, cudaGetLastError());
+        return UWG_OK;
     }
     return uwg_ops_applyK<double>(c, 0, x, y);
 }
@@ -1313,6 +1413,17 @@ int uwg_ops_level_setup(uwg_ctx* c, int l) {
         if (!L.tile_bc) UWG_CUDA(c, cudaMalloc((void**)&L.tile_bc, nt));
         k_tile_bc_flags<<<(unsigned)nt, 256, 0, c->stream>>>(g, L.bc, L.tile_bc);
         UWG_CUDA(c, cudaGetLastError());
+        if (l == 0) {
+            // double-float copy of W for the refinement residual (without room for it the
+            // residual uses the FP64 apply)
+            const int64_t nw = (int64_t)27 * L.n_el;
+            if (!L.Wdf && cudaMalloc((void**)&L.Wdf, sizeof(float2) * nw) != cudaSuccess) {
+                cudaGetLastError();
+                L.Wdf = nullptr;
+            }
+            if (L.Wdf) k_split_w_df<<<nblk(nw), 256, 0, c->stream>>>(nw, L.W64, L.Wdf);
+            UWG_CUDA(c, cudaGetLastError());
+        }
     }
     if (c->dim == 3) k_diag_q1<3><<<nblk(L.n_el), 256, 0, c->stream>>>(g, L.W64, L.bc, L.diag64, l == 0 ? c->Shat : nullptr, c->Mp);
     else k_diag_q1<2><<<nblk(L.n_el), 256, 0, c->stream>>>(g, L.W64, L.bc, L.diag64, l == 0 ? c->Shat : nullptr, c->Mp);
