@@ -146,7 +146,11 @@ def test_config1_sinker_64(gpu, mixed, coarse):
     case = Case(2, (64, 64), 20)
     eta, body = _sinker(case)
     mask = case.walls([[0], [1]])
-    st, u, p, uo, po = case.run(eta, body, mask, mixed=mixed, coarse_agg=coarse)
+    # the solution error follows the outer tolerance along the Krylov path taken: with the
+    # coarse correction's path, 1e-11 left the pressure at 1.05e-10; 5e-12 is still above
+    # the residual floor
+    tight = dict(rtol=5e-12, outer_rtol=5e-12) if coarse else {}
+    st, u, p, uo, po = case.run(eta, body, mask, mixed=mixed, coarse_agg=coarse, **tight)
     assert st["coarse_dim"] == (256 if coarse else 0)
     _check(st, u, p, uo, po, null_vectors=[np.ones(len(po))])
 
