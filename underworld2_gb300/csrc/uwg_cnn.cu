@@ -460,6 +460,7 @@ extern "C" int uwg_cnn_gemm(uwg_ctx* c, int M, int N, int K, const uint16_t* A, 
     if (!c || M < 0 || N < 0 || K < 0 || !A || !B || (!Cf && !Cb) || (accumulate && !Cf))
         return uwg_set_error(c, UWG_ERR_ARG, "uwg_cnn_gemm: bad argument");
     if (!M || !N) return UWG_OK;
+    if ((M + BM - 1) / BM > 65535) return uwg_set_error(c, UWG_ERR_ARG, "uwg_cnn_gemm: M above 65535 x 64 rows");
     const __nv_bfloat16* a = reinterpret_cast<const __nv_bfloat16*>(A);
     const __nv_bfloat16* b = reinterpret_cast<const __nv_bfloat16*>(B);
     __nv_bfloat16* cb = reinterpret_cast<__nv_bfloat16*>(Cb);
@@ -477,21 +478,13 @@ extern "C" int uwg_cnn_gemm(uwg_ctx* c, int M, int N, int K, const uint16_t* A, 
         // three CTAs fit an SM (384 of 512 tensor-memory columns), with BN 64 at most four (256).
         if (N > 64) {
             constexpr int SM = 2 * (TC_BM * TC_BK * 2 + 128 * TC_BK * 2);
-            static bool attr = false;
-            if (!attr) {
-                UWG_CUDA(c, cudaFuncSetAttribute(k_gemm_bf16_tc<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM));
-                attr = true;
-            }
+            UWG_CUDA(c, cudaFuncSetAttribute(k_gemm_bf16_tc<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM));
             dim3 g((N + 127) / 128, (M + TC_BM - 1) / TC_BM);
             k_gemm_bf16_tc<128><<<g, 128, SM, c->stream>>>(M, N, K, a, lda, b, ldb, Cf, cb, ldc, bias, relu, accumulate,
                                                            c->cnn_flag);
         } else {
             constexpr int SM = 2 * (TC_BM * TC_BK * 2 + 64 * TC_BK * 2);
-            static bool attr = false;
-            if (!attr) {
-                UWG_CUDA(c, cudaFuncSetAttribute(k_gemm_bf16_tc<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM));
-                attr = true;
-            }
+            UWG_CUDA(c, cudaFuncSetAttribute(k_gemm_bf16_tc<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM));
             dim3 g((N + 63) / 64, (M + TC_BM - 1) / TC_BM);
             k_gemm_bf16_tc<64><<<g, 128, SM, c->stream>>>(M, N, K, a, lda, b, ldb, Cf, cb, ldc, bias, relu, accumulate,
                                                           c->cnn_flag);
