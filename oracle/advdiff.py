@@ -76,6 +76,7 @@ def residual(m, vel, phi, phidot, kappa_q, source_q, bc):
     R = np.zeros(m.n_nodes)
     M = np.zeros(m.n_nodes)
     N0, _ = _shape(m, np.zeros(dim))
+    shapes = [_shape(m, gxi[q]) for q in range(len(gw))]   # the same at every element
     for e in range(m.n_el):
         nodes = m.element_nodes(e)
         idx = [e % m.res[0], (e // m.res[0]) % m.res[1]] + ([e // (m.res[0] * m.res[1])] if dim == 3 else [])
@@ -92,7 +93,7 @@ def residual(m, vel, phi, phidot, kappa_q, source_q, bc):
         up *= ISQRT15
         detJ = float(np.prod([0.5 * hd for hd in h]))
         for q in range(len(gw)):
-            N, dN = _shape(m, gxi[q])
+            N, dN = shapes[q]
             GNx = dN * (2.0 / np.array(h))[:, None]
             vq = N @ v
             udotu = float(vq @ vq)
@@ -119,7 +120,11 @@ def residual(m, vel, phi, phidot, kappa_q, source_q, bc):
     return R, M
 
 
-def step(m, dt, vel, kappa_q, source_q, bc, bcval, bcdot, phi, phidot, iterations=2, gamma=0.5):
+def step(m, dt, vel, kappa_q, source_q, bc, bcval, bcdot, phi, phidot, iterations=2, gamma=0.5, flux=None):
+    """One predictor-multicorrector step.  flux [n_nodes] or None: the boundary-flux
+    vector of NeumannCondition terms (VectorSurfaceAssemblyTerm_NA__Fn__ni on the
+    residual force vector, P/systems/_advectiondiffusion.py:978-991), added to the
+    residual of every correction."""
     phi = phi.copy()
     phidot = phidot.copy()
     bc = bc.astype(bool)
@@ -133,6 +138,8 @@ def step(m, dt, vel, kappa_q, source_q, bc, bcval, bcdot, phi, phidot, iteration
         R, Mi = residual(m, vel, phi, phidot, kappa_q, source_q, bc)
         if M is None:
             M = Mi
+        if flux is not None:
+            R = R + flux
         d = np.zeros_like(phi)
         d[free] = R[free] / M[free]
         phi[free] += dt * gamma * d[free]

@@ -100,9 +100,13 @@ def system(m, dt, kappa_q, source_q, phistar):
     return K, f
 
 
-def solve(m, dt, kappa_q, source_q, bc, phistar, phi):
-    """Solution of the Crank-Nicolson system; Dirichlet nodes keep phi's values."""
+def solve(m, dt, kappa_q, source_q, bc, phistar, phi, flux=None):
+    """Solution of the Crank-Nicolson system; Dirichlet nodes keep phi's values.
+    flux [n_nodes] or None: dt times the NeumannCondition surface term, added to the
+    right-hand side (P/systems/_advectiondiffusion.py:237-248)."""
     K, f = system(m, dt, kappa_q, source_q, phistar)
+    if flux is not None:
+        f = f + flux
     bc = bc.astype(bool)
     free = ~bc
     out = phi.astype(np.float64).copy()
@@ -111,9 +115,9 @@ def solve(m, dt, kappa_q, source_q, bc, phistar, phi):
     return out
 
 
-def step(m, dt, vel, kappa_q, source_q, bc, phi):
+def step(m, dt, vel, kappa_q, source_q, bc, phi, flux=None):
     phistar = m.slcn_phistar(vel, phi, dt)
-    return solve(m, dt, kappa_q, source_q, bc, phistar, phi), phistar
+    return solve(m, dt, kappa_q, source_q, bc, phistar, phi, flux), phistar
 
 
 def max_dt(m, vel, kappa_nodes):
