@@ -1,0 +1,103 @@
+"""Known answers from the reference's function-module docstrings, restated as
+tests (CPU; no mesh or swarm needed).  Each case cites the docstring it
+follows; the asserted values and types are the ones printed there."""
+import numpy as np
+import pytest
+
+from underworld2_gb300 import function as fn
+
+
+def test_constants_keep_their_type():
+    """P/function/misc.py:27-46 and P/function/_function.py:210-214."""
+    a = fn.misc.constant(3).evaluate(0.)
+    assert a.dtype == np.int32 and a.tolist() == [[3]]
+    a = fn.misc.constant((3, 2, 1)).evaluate(0.)
+    assert a.dtype == np.int32 and a.tolist() == [[3, 2, 1]]
+    a = fn.misc.constant(3.).evaluate(0.)
+    assert a.dtype == np.float64 and a.tolist() == [[3.0]]
+    a = fn.misc.constant((3., 2., 1.)).evaluate(0.)
+    assert a.dtype == np.float64 and a.tolist() == [[3.0, 2.0, 1.0]]
+    a = fn.misc.constant(True).evaluate(0.)
+    assert a.dtype == bool and a.tolist() == [[True]]
+    a = fn.misc.constant((True, False, True)).evaluate(0.)
+    assert a.dtype == bool and a.tolist() == [[True, False, True]]
+    a = fn.Function.convert(3).evaluate(0.)
+    assert a.dtype == np.int32 and a.tolist() == [[3]]
+
+
+def test_vector_conversion():
+    """P/function/_function.py:220-227."""
+    fn1, fn2, fn3 = fn.input(), 10. * fn.input(), 100. * fn.input()
+    np.testing.assert_array_equal(fn.Function.convert((fn1, fn2, fn3)).evaluate([3.]), [[3., 30., 300.]])
+
+
+def test_arithmetic_on_constants():
+    """P/function/_function.py:282-437."""
+    two, three, four = fn.misc.constant(2.), fn.misc.constant(3.), fn.misc.constant(4.)
+    assert np.allclose((three + four).evaluate(0.), [[7.]])
+    assert np.allclose((three - four).evaluate(0.), [[-1.]])
+    assert np.allclose((5. - four).evaluate(0.), [[1.]])
+    assert np.allclose((-four).evaluate(0.), [[-4.]])
+    assert np.allclose((three * four).evaluate(0.), [[12.]])
+    assert np.allclose((four / two).evaluate(0.), [[2.]])
+    assert np.allclose((two ** four).evaluate(0.), [[16.]])
+
+
+def test_comparisons_and_logic():
+    """P/function/_function.py:455-620."""
+    two, four = fn.misc.constant(2.), fn.misc.constant(4.)
+    for f, expect in (((two < four), True), ((two <= two), True), ((two > four), False), ((two >= two), True)):
+        a = f.evaluate()
+        assert a.dtype == bool and a.tolist() == [[expect]]
+    t, f_ = fn.misc.constant(True), fn.misc.constant(False)
+    assert (t & f_).evaluate().tolist() == [[False]]
+    assert (t | f_).evaluate().tolist() == [[True]]
+    assert (t ^ f_).evaluate().tolist() == [[True]]
+    assert (t ^ t).evaluate().tolist() == [[False]]
+
+
+def test_component_and_input():
+    """P/function/_function.py:645-649, 1264-1281."""
+    assert np.allclose(fn.misc.constant((2., 3., 4.))[1].evaluate(0.), [[3.]])
+    assert np.allclose(fn.input().evaluate((1., 2., 3.)), [1., 2., 3.])
+    density = 1. - 0.01 * fn.input()[1]
+    assert np.allclose(density.evaluate((0.1, 0.4)), density.evaluate((0.9, 0.4)))
+
+
+def test_min_max_against_conditional():
+    """P/function/misc.py:150-166."""
+    testpoints = np.array([[0.0], [0.2], [0.4], [0.6], [0.8], [1.01], [1.2], [1.4], [1.6], [1.8], [2.0]])
+    x = fn.input()[0]
+    x_minus_one, one_minus_x = x - 1., 1. - x
+    fn_max = fn.misc.max(one_minus_x, x_minus_one)
+    fn_min = fn.misc.min(one_minus_x, x_minus_one)
+    cmax = fn.branching.conditional(((x <= 1., one_minus_x), (x > 1., x_minus_one)))
+    cmin = fn.branching.conditional(((x >= 1., one_minus_x), (x < 1., x_minus_one)))
+    assert np.allclose(fn_max.evaluate(testpoints), cmax.evaluate(testpoints))
+    assert np.allclose(fn_min.evaluate(testpoints), cmin.evaluate(testpoints))
+
+
+def test_view_count():
+    """P/function/view.py:396-423."""
+    fn_count = fn.view.count(fn.input())
+    fn_count.evaluate(5.)
+    assert fn_count.count() == 1
+    for _ in range(3):
+        fn_count.evaluate(5.)
+    assert fn_count.count() == 4
+    fn_count.reset()
+    fn_count.evaluate(5.)
+    fn_count.evaluate(5.)
+    assert fn_count.count() == 2
+
+
+def test_exceptions():
+    """P/function/exception.py:38-50 (SafeMaths on 1/0) and 95-115 (CustomException)."""
+    one, zero = fn.misc.constant(1.), fn.misc.constant(0.)
+    with pytest.raises(RuntimeError):
+        fn.exception.SafeMaths(one / zero).evaluate()
+    assert fn.exception.CustomException(one, (one < 2.)).evaluate().tolist() == [[1.0]]
+    with pytest.raises(RuntimeError):
+        fn.exception.CustomException(one, (one > 2.)).evaluate()
+    with pytest.raises(RuntimeError):
+        fn.exception.CustomException(one, (one * 5. > 20.), one * 5.).evaluate()

@@ -55,6 +55,7 @@ class Function:
 
     _kind = None
     _bool = False
+    _int = False      # integer results (integer constants): evaluate() returns int32
 
     @staticmethod
     def convert(obj):
@@ -93,10 +94,11 @@ class Function:
         nodes of a mesh or at the particles of a swarm (P/function/_function.py:808-930).
         Returns an [n, k] numpy array (bool for boolean functions)."""
         ctx = _input_context(inputData)
+        dt = bool if self._bool else (np.int32 if self._int else np.float64)
         if ctx.n == 0:
-            return np.zeros((0, 1), dtype=bool if self._bool else np.float64)
+            return np.zeros((0, 1), dtype=dt)
         v = self.evaluate_at(ctx).cpu().numpy()
-        return v != 0 if self._bool else np.array(v, dtype=np.float64)
+        return v != 0 if self._bool else np.array(v, dtype=dt)
 
     # arithmetic
     def __add__(self, o): return _Bin(torch.add, self, Function.convert(o))
@@ -124,6 +126,13 @@ class Function:
 class constant(Function):
     def __init__(self, value):
         self.value = value
+        # the reference keeps a constant's type: bools evaluate to bool, ints to int32
+        # (P/function/misc.py:13-67, P/function/_function.py:75-94)
+        flat = list(value) if isinstance(value, (tuple, list)) else [value]
+        if flat and all(isinstance(v, (bool, np.bool_)) for v in flat):
+            self._bool = True
+        elif flat and all(isinstance(v, (int, np.integer)) and not isinstance(v, (bool, np.bool_)) for v in flat):
+            self._int = True
 
     def _eval(self, ctx):
         t = torch.as_tensor(self.value, dtype=torch.float64, device=ctx.device)
