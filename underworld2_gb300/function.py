@@ -14,8 +14,9 @@ P/function/math.py, ``misc.min/max``, ``tensor.symmetric/antisymmetric/
 second_invariant/deviatoric`` (L/StgDomain/Geometry/src/TensorMath.c
 conventions: full tensors row-major, symmetric tensors [00, 11, (22,) 01,
 (02, 12)]), ``shape.Polygon``, ``branching.map/conditional``,
-``view.min_max``, ``view.count``, ``exception.SafeMaths``, ``exception.CustomException`` and
-``rheology.stress_limiting_viscosity``.  ``Function.evaluate`` accepts
+``view.min_max``, ``view.count``, ``exception.SafeMaths``, ``exception.CustomException``,
+``rheology.stress_limiting_viscosity`` and the fixed-wall analytic solutions
+``analytic.SolDB2d``/``SolDB3d``.  ``Function.evaluate`` accepts
 coordinates, a mesh or a swarm, as the reference's.
 """
 import math as _pymath
@@ -609,6 +610,141 @@ class view:
     def count(fn):
         """Pass-through that counts its evaluations (one per point)."""
         return _Count(fn)
+
+
+# ---------------------------------------------------------------------------
+# Analytic Stokes solutions with fixed velocity on every wall (P/function/analytic.py:568-656)
+# ---------------------------------------------------------------------------
+class _SolFixedBc:
+    """Fields of an analytic solution as function graphs of the coordinates:
+    fn_velocity, fn_pressure, fn_strainRate (symmetric-tensor order xx, yy[, zz], xy
+    [, xz, yz]), fn_stress (2 eta strain rate), fn_viscosity and fn_bodyforce, the
+    body force of -div(2 eta strain rate) + grad p = f."""
+
+    def _finish(self, eta, vel, p, e, div_e, grad_p, grad_eta):
+        """e: strain-rate components (matrix form, list of rows); div_e: the row
+        divergences of e; grad_eta: the viscosity gradient (None when constant)."""
+        d = self.dim
+        self.fn_velocity = Function.convert(tuple(vel))
+        self.fn_pressure = p
+        sym = [e[0][0], e[1][1]] + ([e[2][2]] if d == 3 else []) + [e[0][1]] + ([e[0][2], e[1][2]] if d == 3 else [])
+        self.fn_strainRate = Function.convert(tuple(sym))
+        self.fn_viscosity = eta
+        self.fn_stress = Function.convert(tuple(2.0 * eta * c for c in sym))
+        force = []
+        for i in range(d):
+            f = -2.0 * eta * div_e[i] + grad_p[i]
+            if grad_eta is not None:
+                for j in range(d):
+                    f = f - 2.0 * grad_eta[j] * e[i][j]
+            force.append(f)
+        self.fn_bodyforce = Function.convert(tuple(force))
+
+    def get_bcs(self, velVar):
+        """Velocity fixed on every wall at the analytic values, each wall's normal
+        component shifted by the difference between its numerical and analytic
+        fluxes (P/function/analytic.py:569-618).  The numerical flux is the exact
+        integral of the nodal interpolant, sum_A w_A v_A with the tensor-product
+        node weights of the wall (trapezoid on Q1, Simpson on Q2).  Returns the
+        DirichletCondition."""
+        from . import conditions as _cond
+        from . import utils as _utils
+        mesh = velVar.mesh
+        ss = mesh.specialSets
+        walls = ss["AllWalls_VertexSet"]
+        velVar.data[walls.data] = self.fn_velocity.evaluate(mesh.data[walls.data])
+        for ax, name in enumerate("IJK"[: self.dim]):
+            for side in ("Min", "Max"):
+                verts = ss["%s%s_VertexSet" % (side, name)]
+                idx = verts.data
+                num = float(np.dot(_wall_weights(mesh, idx, ax), velVar.data[idx, ax]))
+                ana = _utils.Integral(self.fn_velocity[ax], mesh, integrationType="surface",
+                                      surfaceIndexSet=verts).evaluate()
+                velVar.data[idx, ax] -= num - float(np.asarray(ana).ravel()[0])
+        return _cond.DirichletCondition(velVar, tuple(walls for _ in range(self.dim)))
+
+
+def _node_weights_1d(c, order):
+    """int N_i over an axis with node coordinates c: trapezoid (order 1), Simpson (order 2)."""
+    w = np.zeros(len(c))
+    for e in range((len(c) - 1) // order):
+        a, b = e * order, (e + 1) * order
+        h = c[b] - c[a]
+        if order == 1:
+            w[a] += 0.5 * h
+            w[b] += 0.5 * h
+        else:
+            w[a] += h / 6.0
+            w[a + 1] += 4.0 * h / 6.0
+            w[b] += h / 6.0
+    return w
+
+
+def _wall_weights(mesh, idx, ax):
+    """int N_A over the wall normal to axis ax for the wall's nodes idx."""
+    axes = [np.asarray(a) for a in mesh._axes]
+    nn = [len(a) for a in axes]
+    w = np.ones(len(idx))
+    rest = np.asarray(idx, dtype=np.int64)
+    for d in range(len(axes)):
+        i_d = rest % nn[d]
+        rest = rest // nn[d]
+        if d != ax:
+            w *= _node_weights_1d(axes[d], mesh._order)[i_d]
+    return w
+
+
+class analytic:
+    """The analytic Stokes solutions with fixed-velocity walls (P/function/analytic.py)."""
+
+    class SolDB2d(_SolFixedBc):
+        """Dohrmann & Bochev (Int. J. Numer. Meth. Fluids 46, 183-201, 2004), 2D, on the
+        unit square: viscosity 1,
+        u = (x + x^2 - 2xz + x^3 - 3xz^2 + x^2 z,  -z - 2xz + z^2 - 3x^2 z + z^3 - xz^2),
+        p = xz + x + z + x^3 z^2 - 4/3 (z the second coordinate)."""
+        eqn_viscosity = "1"
+
+        def __init__(self, *args, **kwargs):
+            self.dim = 2
+            x, z = input()[0], input()[1]
+            ux = x + x * x - 2.0 * x * z + x * x * x - 3.0 * x * z * z + x * x * z
+            uz = -z - 2.0 * x * z + z * z - 3.0 * x * x * z + z * z * z - x * z * z
+            p = x * z + x + z + x * x * x * z * z - 4.0 / 3.0
+            exx = 1.0 + 2.0 * x - 2.0 * z + 3.0 * x * x - 3.0 * z * z + 2.0 * x * z
+            exz = -x - z - 6.0 * x * z + 0.5 * x * x - 0.5 * z * z
+            e = [[exx, exz], [exz, -exx]]
+            div_e = [1.0 + z, 1.0 - x]
+            grad_p = [z + 1.0 + 3.0 * x * x * z * z, x + 1.0 + 2.0 * x * x * x * z]
+            self._finish(constant(1.0), [ux, uz], p, e, div_e, grad_p, None)
+
+    class SolDB3d(_SolFixedBc):
+        """Dohrmann & Bochev (2004), 3D, on the unit cube: viscosity
+        eta = exp(1 - Beta (x(1-x) + y(1-y) + z(1-z))),
+        u = (x + x^2 + xy + x^3 y,  y + xy + y^2 + x^2 y^2,  -2z - 3xz - 3yz - 5x^2 yz),
+        p = xyz + x^2 y^3 z - 5/32."""
+
+        def __init__(self, Beta=4., *args, **kwargs):
+            self.dim = 3
+            self.Beta = float(Beta)
+            x, y, z = input()[0], input()[1], input()[2]
+            b = self.Beta
+            eta = math.exp(1.0 - b * (x * (1.0 - x) + y * (1.0 - y) + z * (1.0 - z)))
+            u = [x + x * x + x * y + x * x * x * y,
+                 y + x * y + y * y + x * x * y * y,
+                 -2.0 * z - 3.0 * x * z - 3.0 * y * z - 5.0 * x * x * y * z]
+            p = x * y * z + x * x * y * y * y * z - 5.0 / 32.0
+            exx = 1.0 + 2.0 * x + y + 3.0 * x * x * y
+            eyy = 1.0 + x + 2.0 * y + 2.0 * x * x * y
+            ezz = -2.0 - 3.0 * x - 3.0 * y - 5.0 * x * x * y
+            exy = 0.5 * x + 0.5 * x * x * x + 0.5 * y + x * y * y
+            exz = -1.5 * z - 5.0 * x * y * z
+            eyz = -1.5 * z - 2.5 * x * x * z
+            e = [[exx, exy, exz], [exy, eyy, eyz], [exz, eyz, ezz]]
+            div_e = [1.0 + 3.0 * x * y, 1.0 + x * x + y * y, -5.0 * y * z]
+            grad_p = [y * z + 2.0 * x * y * y * y * z, x * z + 3.0 * x * x * y * y * z, x * y + x * x * y * y * y]
+            # grad eta = -Beta eta (1 - 2 x_i)
+            grad_eta = [-b * eta * (1.0 - 2.0 * c) for c in (x, y, z)]
+            self._finish(eta, u, p, e, div_e, grad_p, grad_eta)
 
 
 # ---------------------------------------------------------------------------
