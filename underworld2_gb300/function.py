@@ -615,11 +615,22 @@ class view:
 # ---------------------------------------------------------------------------
 # Analytic Stokes solutions with fixed velocity on every wall (P/function/analytic.py:568-656)
 # ---------------------------------------------------------------------------
-class _SolFixedBc:
+class _SolBase:
+    """Base of the analytic solutions: fn_velocity, fn_pressure, fn_stress,
+    fn_strainRate, fn_viscosity, fn_bodyforce, dim and nonlinear
+    (P/function/analytic.py:62-79)."""
+    eqn_bodyforce = None
+    eqn_viscosity = None
+    nonlinear = False
+
+
+class _SolFixedBc(_SolBase):
     """Fields of an analytic solution as function graphs of the coordinates:
     fn_velocity, fn_pressure, fn_strainRate (symmetric-tensor order xx, yy[, zz], xy
     [, xz, yz]), fn_stress (2 eta strain rate), fn_viscosity and fn_bodyforce, the
     body force of -div(2 eta strain rate) + grad p = f."""
+
+    fixed_walls = True
 
     def _finish(self, eta, vel, p, e, div_e, grad_p, grad_eta):
         """e: strain-rate components (matrix form, list of rows); div_e: the row
@@ -695,7 +706,11 @@ def _wall_weights(mesh, idx, ax):
 
 
 class analytic:
-    """The analytic Stokes solutions with fixed-velocity walls (P/function/analytic.py)."""
+    """The reference's analytic Stokes solutions (P/function/analytic.py): the
+    fixed-wall SolDB2d and SolDB3d here, and the free-slip solutions SolA, SolB,
+    SolC, SolCx, SolDA, SolH, SolKx, SolKz, SolM and the power-law SolNL
+    (module _analytic_series)."""
+    _SolBase = _SolBase
 
     class SolDB2d(_SolFixedBc):
         """Dohrmann & Bochev (Int. J. Numer. Meth. Fluids 46, 183-201, 2004), 2D, on the
@@ -947,3 +962,10 @@ def _input_context(inputData):
             pts = pts[None, :]
     t = torch.from_numpy(np.ascontiguousarray(pts)).to(dev)
     return EvalContext(torch.full((t.shape[0],), -1, dtype=torch.int64, device=dev), lambda: t, dev)
+
+
+from . import _analytic_series as _series  # noqa: E402  (it builds on the classes above)
+
+for _name in ("SolA", "SolB", "SolC", "SolCx", "SolDA", "SolH", "SolKx", "SolKz", "SolM", "SolNL"):
+    setattr(analytic, _name, getattr(_series, _name))
+del _name
