@@ -270,3 +270,24 @@ def test_h5_reader_continuation_and_vlen_strings():
     assert [m[0] for m in msgs] == [0x0010, 0x000C]
     name_out, value = r.attribute(msgs[1][1])
     assert name_out == "elementType" and value == "Q2"
+
+
+_REF_INPUT = os.path.join(os.environ.get("UW_REFERENCE_TREE", "/root/reference"), "docs", "examples", "input")
+
+
+@pytest.mark.skipif(not os.path.isdir(_REF_INPUT), reason="reference tree not present")
+def test_h5_reader_on_reference_swarm_files():
+    """The swarm checkpoints the reference ships with its shear-band example,
+    written by h5py/libhdf5 (docs/examples/input/07_ShearBandsPureShear): 28,800
+    particle coordinates in the example's [-2, 2] x [0, 1] box and their plastic
+    strain, each with the proc_offset attribute of a one-process save."""
+    d = os.path.join(_REF_INPUT, "07_ShearBandsPureShear")
+    f = h5.File(os.path.join(d, "particle_coords.h5"))
+    x = f["data"]
+    assert x.shape == (28800, 2) and x.dtype == np.float64
+    assert x[:, 0].min() > -2.0 and x[:, 0].max() < 2.0 and x[:, 1].min() > 0.0 and x[:, 1].max() < 1.0
+    assert f.attrs["proc_offset"].tolist() == [28800] and f.links == {}
+    g = h5.File(os.path.join(d, "plastic_strain.h5"))
+    e = g["data"]
+    assert e.shape == (28800, 1) and e.min() >= 0.0 and e.max() < 1.0
+    assert g.attrs["proc_offset"].tolist() == [28800]

@@ -12,8 +12,11 @@ table node and a local heap; contiguous datasets; attributes in the root
 object header) -- the layout libhdf5 produces with its default "earliest"
 format bounds.  The reader parses the same structures, plus what libhdf5 adds
 to such files: header continuation blocks, multi-node group B-trees, version 2
-dataspaces and variable-length string attributes in global heaps.  Chunked or
-filtered datasets are not supported and raise ``NotImplementedError``.
+dataspaces, variable-length string attributes in global heaps, and root groups
+in compact new-style storage (link-info and link messages: hard, soft and
+external links), which is how h5py stores a file holding an external link.
+Chunked or filtered datasets and dense link storage are not supported and
+raise ``NotImplementedError``.
 
 Values are little-endian.  Python ``bool`` attributes are stored as int8 and
 ``str`` attributes as fixed-length null-terminated ASCII strings (h5py returns
@@ -265,6 +268,38 @@ class _Reader:
             raise NotImplementedError("version 2 object headers")
         raise ValueError("bad object header at %d" % addr)
 
+    def link(self, off):
+        """(name, type, value) of a link message: type 0 (hard, value = object
+        header address), 1 (soft, value = ("", path)) or 64 (external, value =
+        (file name, object path))."""
+        ver, flags = self.u("BB", off)
+        if ver != 1:
+            raise NotImplementedError("link message version %d" % ver)
+        p = off + 2
+        kind = 0
+        if flags & 0x08:
+            kind = self.b[p]
+            p += 1
+        if flags & 0x04:
+            p += 8                                   # creation order
+        if flags & 0x10:
+            p += 1                                   # name character set
+        nlen_size = 1 << (flags & 0x03)
+        nlen = int.from_bytes(bytes(self.b[p:p + nlen_size]), "little")
+        p += nlen_size
+        name = bytes(self.b[p:p + nlen]).decode("utf-8")
+        p += nlen
+        if kind == 0:
+            return name, 0, self.u("Q", p)[0]
+        length = self.u("H", p)[0]
+        body = bytes(self.b[p + 2:p + 2 + length])
+        if kind == 1:
+            return name, 1, ("", body.rstrip(b"\0").decode("utf-8"))
+        if kind == 64:
+            parts = body[1:].split(b"\0")           # version/flags byte, file name, object path
+            return name, 64, (parts[0].decode("utf-8"), parts[1].decode("utf-8") if len(parts) > 1 else "/")
+        raise NotImplementedError("link type %d" % kind)
+
     def heap_string(self, heap_addr, off):
         assert self.b[heap_addr:heap_addr + 4] == b"HEAP"
         data = self.u("Q", heap_addr + 24)[0]
@@ -359,6 +394,7 @@ class File:
         root = r.u("Q", ent + 8)[0]
         self.attrs = {}
         self._entries = {}
+        self.links = {}          # soft and external links: name -> (file name or "", object path)
         for mtype, off, size in r.messages(root):
             if mtype == 0x0011:
                 bt, hp = r.u("QQ", off)
@@ -366,8 +402,17 @@ class File:
             elif mtype == 0x000C:
                 k, v = r.attribute(off)
                 self.attrs[k] = v
-            elif mtype in (0x0002, 0x0006):
-                raise NotImplementedError("new-style (link message) groups")
+            elif mtype == 0x0002:
+                flags = r.b[off + 1]
+                heap = r.u("Q", off + 2 + (8 if flags & 1 else 0))[0]
+                if heap != _UNDEF:
+                    raise NotImplementedError("dense link storage (fractal heap)")
+            elif mtype == 0x0006:
+                name, kind, value = r.link(off)
+                if kind == 0:
+                    self._entries[name] = value
+                else:
+                    self.links[name] = value
 
     def keys(self):
         return list(self._entries)

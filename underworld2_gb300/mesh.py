@@ -444,6 +444,10 @@ class MeshVariable:
         with _h5.File(filename) as f:
             d = f["data"]
             link = f.attrs.get("mesh")
+            if link is None and "mesh" in f.links:      # an external link, as h5py writes it
+                link = f.links["mesh"][0]
+                if not os.path.isabs(link):
+                    link = os.path.join(os.path.dirname(os.path.abspath(filename)), link)
         if d.ndim != 2 or d.shape[1] != self.nodeDofCount:
             raise RuntimeError("Can't load hdf5 '%s', incompatible data shape" % filename)
         if d.shape[0] == self._data.shape[0]:
