@@ -13,8 +13,11 @@ from the last Stokes solution (sigma_zz = 2 dw/dz - p minus its mean, scaled by
 eta0 kappa / h^2 / (rho g)).  Discretisation and solves are the oracle's
 (tests/oracle_system.py, oracle/advdiff.py); the notebook's tolerances apply:
 1e-2 for Nu, v_rms, q1, q2 and 1e-3 for the topography at both top corners and
-the x position of its zero.  The test reads the reference tree and is skipped
-where it is absent.
+the x position of its zero.  The first SUPG step is also held to the
+reference's own run as the notebook's saved output prints it (Nu before the
+loop to 6 decimals, v_rms to 3, the relative Nu change of the step to 4
+significant digits).  The test reads the reference tree and is skipped where
+it is absent.
 """
 import os
 
@@ -82,24 +85,42 @@ def test_blankenbach_case_a():
         sysd = osys.assemble(m, pts, np.ones(m.n_el * nq), body, mask, zero)
         return osys.solve(sysd, m.n_nodes * 2)
 
+    Tdot = np.zeros(m.n_nodes)                         # the notebook's temperatureDotField, kept across steps
+
     def supg(u, Tn):
+        nonlocal Tdot
         U = u.reshape(-1, 2)
         dt = advdiff.max_dt(m, U, kq)
-        Tn2, _ = advdiff.step(m, dt, U, kq, None, tbc, Tn.copy(), None, Tn.copy(), np.zeros(m.n_nodes))
+        Tn2, Tdot = advdiff.step(m, dt, U, kq, None, tbc, Tn.copy(), None, Tn.copy(), Tdot)
         return Tn2
 
+    h = 1.0 / res
+    rule3 = ac._Rule(m, 3)
+
+    def nusselt(Tn):
+        Tg = Tn.reshape(res + 1, res + 1)
+        dTdz = (Tg[-1] - Tg[-2]) / h                  # top row: linear in x along each element
+        return -np.sum(0.5 * (dTdz[1:] + dTdz[:-1]) * h) / np.sum(0.5 * (Tg[0, 1:] + Tg[0, :-1]) * h)
+
+    def v_rms(u):
+        uq = np.einsum("qn,eni->eqi", rule3.N, u.reshape(-1, 2)[rule3.nodes]).reshape(-1, 2)
+        return np.sqrt(np.tile(rule3.w * rule3.det, m.n_el) @ (uq ** 2).sum(1))
+
+    nu0 = nusselt(T)
     u, p = stokes(T)
+    vrms0 = v_rms(u)
     T = supg(u, T)
     u, p = stokes(T)
-    h = 1.0 / res
-    Tg = T.reshape(res + 1, res + 1)
-    dTdz = (Tg[-1] - Tg[-2]) / h                      # top row: linear in x along each element
-    nu = -np.sum(0.5 * (dTdz[1:] + dTdz[:-1]) * h) / np.sum(0.5 * (Tg[0, 1:] + Tg[0, :-1]) * h)
-    rule3 = ac._Rule(m, 3)
-    uq = np.einsum("qn,eni->eqi", rule3.N, u.reshape(-1, 2)[rule3.nodes]).reshape(-1, 2)
-    vrms = np.sqrt(np.tile(rule3.w * rule3.det, m.n_el) @ (uq ** 2).sum(1))
+    nu, vrms = nusselt(T), v_rms(u)
+    # the notebook's asserted values (the published benchmark), at its tolerances
     assert np.isclose(nu, 4.884, rtol=1e-2), nu
     assert np.isclose(vrms, 42.865, rtol=1e-2), vrms
+    # the reference's own run, as the notebook's saved output prints it:
+    # "Nusselt number = 4.856902" before the loop, then v_rms = 42.869 at steps
+    # 0 and 1 and a relative Nu change of 1.416e-03 over the first SUPG step
+    assert abs(nu0 - 4.856902) <= 5e-7, nu0
+    assert round(vrms0, 3) == 42.869 and round(vrms, 3) == 42.869, (vrms0, vrms)
+    assert abs(abs(nu - nu0) / nu - 1.416e-3) <= 5e-7, (nu - nu0) / nu
 
     Tg = supg(u, T).reshape(res + 1, res + 1)
     dTdz = (Tg[-1] - Tg[-2]) / h
