@@ -372,7 +372,11 @@ int uwg_cnn_adam(uwg_ctx* ctx, int64_t n, float* w, const float* g, float* m, fl
  *   kappa_q   [n_el*3^dim] diffusivity at the 3-point Gauss points of each element
  *   source_q  same layout, or NULL
  *   bc        [n_nodes] 1 = Dirichlet node, with phi = bcval and phi-dot = bcdot (NULL: 0)
- *   phi, phidot [n_nodes] advanced in place; iterations (2) and gamma (0.5) as the reference
+ *   phi, phidot [n_nodes] advanced in place; iterations (2) and gamma (0.5) as the reference.
+ *             As in the reference, the predictor phi += dt (1-gamma) phidot, phidot = 0 is
+ *             applied together with the first correction, whose residual is evaluated on
+ *             phi_n and phidot_n (the reference's residual reads the nodal fields, which its
+ *             predictor does not touch)
  *   flux      [n_nodes] boundary-flux vector added to every residual (the NeumannCondition
  *             surface term VectorSurfaceAssemblyTerm_NA__Fn__ni, L/Underworld/Utils/src/
  *             VectorSurfaceAssemblyTerm_NA__Fn__ni.cpp:163-236), or NULL */

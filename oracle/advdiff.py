@@ -4,10 +4,13 @@ INFRASTRUCTURE: the checker of libuwg's uwg_advdiff_step, never the product).
 Follows, element by element and point by point:
 * the explicit predictor-multicorrector,
   L/Underworld/Utils/AdvectionDiffusion/src/Multicorrector.c:166-300
-  (phi += dt (1-gamma) phidot, phidot = 0; then per iteration R = residual,
-  dphidot = R / M_lumped, phi += dt gamma dphidot, phidot += dphidot);
+  (phi += dt (1-gamma) phidot, phidot = 0 on the solution vectors; then per
+  iteration R = residual of the nodal values, dphidot = R / M_lumped,
+  phi += dt gamma dphidot, phidot += dphidot; the first residual sees the
+  nodal values from before the predictor, see ``step``);
 * the SUPG residual, Residual.cpp:213-341, with the upwind diffusivity of
-  Residual.cpp:416-506 and the "Exact" xi of :557-568;
+  Residual.cpp:416-506 and the doubly asymptotic xi of :580-587 (the choice
+  of P/systems/sle/_assemblyterm.py:388);
 * the lumped mass, LumpedMassMatrixForceTerm.c:139-172;
 * the time-step bound, Timestep.c:31-117;
 on Q1 meshes with the default Gauss swarm (3 points per axis).  Shape
@@ -60,63 +63,70 @@ def _shape(m, xi):
 
 
 def _upwind_xi(pe):
-    if abs(pe) < 1.0e-8:
-        return 0.33333333333333 * pe
-    if pe < -20.0:
-        return -1.0 - 1.0 / pe
-    if pe > 20.0:
-        return 1.0 - 1.0 / pe
-    return math.cosh(pe) / math.sinh(pe) - 1.0 / pe
+    """The doubly asymptotic upwind parameter (Residual.cpp:580-587), elementwise:
+    the reference's Python interface sets "UpwindXiFunction" to
+    "DoublyAsymptoticAssumption" (P/systems/sle/_assemblyterm.py:388)."""
+    pe = np.asarray(pe, dtype=np.float64)
+    return np.where(pe <= -3.0, -1.0, np.where(pe <= 3.0, 0.33333333333333 * pe, 1.0))
+
+
+def elements(m):
+    """Node lists [n_el, nen] and edge lengths [n_el, dim] of every element of a
+    regular Q1 mesh (cached on the mesh)."""
+    c = getattr(m, "_q1_elements", None)
+    if c is None:
+        nodes = np.array([m.element_nodes(e) for e in range(m.n_el)])
+        e = np.arange(m.n_el)
+        idx = [e % m.res[0], (e // m.res[0]) % m.res[1]] + ([e // (m.res[0] * m.res[1])] if m.dim == 3 else [])
+        h = np.stack([m.axes[d][idx[d] + 1] - m.axes[d][idx[d]] for d in range(m.dim)], 1)
+        c = m._q1_elements = (nodes, h)
+    return c
 
 
 def residual(m, vel, phi, phidot, kappa_q, source_q, bc):
-    """Assembled SUPG residual and lumped mass on the free nodes."""
+    """Assembled SUPG residual and lumped mass on the free nodes, every element at
+    once (the loops of Residual.cpp:213-341 over elements and points, vectorised
+    over the elements)."""
     dim, nen = m.dim, m.nen
     gxi, gw = gauss_points(dim)
+    nodes, h = elements(m)
+    ne = m.n_el
+    N0, _ = _shape(m, np.zeros(dim))
+    v = vel[nodes] if vel is not None else np.zeros((ne, nen, dim))            # [ne, nen, dim]
+    kavg = np.sum(kappa_q, axis=1) / len(gw)
+    kavg = np.where(kavg < SUPG_MIN_DIFFUSIVITY, SUPG_MIN_DIFFUSIVITY, kavg)
+    vc = np.einsum("a,ead->ed", N0, v)
+    L = np.abs(h)
+    up = np.sum(_upwind_xi(vc * L / (2.0 * kavg[:, None])) * vc * L, axis=1) * ISQRT15
+    plain = np.abs(up) < SUPG_MIN_DIFFUSIVITY
+    detJ = np.prod(0.5 * h, axis=1)
+    ph, pd = phi[nodes], phidot[nodes]
+    Re = np.zeros((ne, nen))
+    Me = np.zeros((ne, nen))
+    for q in range(len(gw)):
+        N, dN = _shape(m, gxi[q])
+        GNx = dN[None] * (2.0 / h)[:, :, None]                                 # [ne, dim, nen]
+        vq = np.einsum("a,ead->ed", N, v)
+        udotu = np.sum(vq * vq, axis=1)
+        grad = np.einsum("eda,ea->ed", GNx, ph)
+        total = pd @ N + np.sum(vq * grad, axis=1)
+        if source_q is not None:
+            total = total - source_q[:, q]
+        factor = gw[q] * detJ
+        with np.errstate(divide="ignore", invalid="ignore"):
+            supgN = N[None, :] + (up / udotu)[:, None] * np.einsum("ed,eda->ea", vq, GNx)
+        supgN = np.where(plain[:, None], N[None, :], supgN)
+        diff = kappa_q[:, q][:, None] * np.einsum("eda,ed->ea", GNx, grad)
+        if vel is None:
+            Re -= factor[:, None] * diff
+        else:
+            Re -= factor[:, None] * (supgN * total[:, None] + diff)
+        Me += N[None, :] * N.sum() * factor[:, None]
+    free = ~np.asarray(bc, dtype=bool)[nodes]
     R = np.zeros(m.n_nodes)
     M = np.zeros(m.n_nodes)
-    N0, _ = _shape(m, np.zeros(dim))
-    shapes = [_shape(m, gxi[q]) for q in range(len(gw))]   # the same at every element
-    for e in range(m.n_el):
-        nodes = m.element_nodes(e)
-        idx = [e % m.res[0], (e // m.res[0]) % m.res[1]] + ([e // (m.res[0] * m.res[1])] if dim == 3 else [])
-        h = [m.axes[d][idx[d] + 1] - m.axes[d][idx[d]] for d in range(dim)]
-        v = vel[nodes] if vel is not None else np.zeros((nen, dim))
-        kavg = float(np.sum(kappa_q[e])) / len(gw)
-        if kavg < SUPG_MIN_DIFFUSIVITY:
-            kavg = SUPG_MIN_DIFFUSIVITY
-        vc = N0 @ v
-        up = 0.0
-        for d in range(dim):
-            L = abs(h[d])
-            up += _upwind_xi(vc[d] * L / (2.0 * kavg)) * vc[d] * L
-        up *= ISQRT15
-        detJ = float(np.prod([0.5 * hd for hd in h]))
-        for q in range(len(gw)):
-            N, dN = shapes[q]
-            GNx = dN * (2.0 / np.array(h))[:, None]
-            vq = N @ v
-            udotu = float(vq @ vq)
-            grad = GNx @ phi[nodes]
-            total = float(N @ phidot[nodes]) + float(vq @ grad)
-            if source_q is not None:
-                total -= source_q[e, q]
-            factor = gw[q] * detJ
-            if abs(up) < SUPG_MIN_DIFFUSIVITY:
-                supgN = N
-            else:
-                with np.errstate(divide="ignore", invalid="ignore"):
-                    supgN = N + (up / udotu) * (vq @ GNx)
-            diff = kappa_q[e, q] * (GNx.T @ grad)
-            if vel is None:
-                Re = -factor * diff
-            else:
-                Re = -factor * (supgN * total + diff)
-            Me = N * N.sum() * factor
-            for a in range(nen):
-                if not bc[nodes[a]]:
-                    R[nodes[a]] += Re[a]
-                    M[nodes[a]] += Me[a]
+    np.add.at(R, nodes[free], Re[free])
+    np.add.at(M, nodes[free], Me[free])
     return R, M
 
 
@@ -124,15 +134,24 @@ def step(m, dt, vel, kappa_q, source_q, bc, bcval, bcdot, phi, phidot, iteration
     """One predictor-multicorrector step.  flux [n_nodes] or None: the boundary-flux
     vector of NeumannCondition terms (VectorSurfaceAssemblyTerm_NA__Fn__ni on the
     residual force vector, P/systems/_advectiondiffusion.py:978-991), added to the
-    residual of every correction."""
+    residual of every correction.
+
+    The order is the reference's (_AdvDiffMulticorrector_Solve, Multicorrector.c:
+    166-206): Dirichlet values go onto both fields; the predictor acts on the
+    solution vectors only, and the residual is assembled from the fields' nodal
+    values, which take the vectors' values after each corrector.  So the first
+    residual sees phi_n and phidot_n as they were before the predictor; with
+    d = R / M_lumped that correction gives phi = phi_n + dt (1 - gamma) phidot_n
+    + dt gamma d and phidot = d, and every later one phi += dt gamma d, phidot += d."""
     phi = phi.copy()
     phidot = phidot.copy()
     bc = bc.astype(bool)
     phi[bc] = bcval[bc]
     phidot[bc] = 0.0 if bcdot is None else bcdot[bc]
     free = ~bc
-    phi[free] += dt * (1.0 - gamma) * phidot[free]
-    phidot[free] = 0.0
+    if iterations == 0:
+        phi[free] += dt * (1.0 - gamma) * phidot[free]
+        phidot[free] = 0.0
     M = None
     for it in range(iterations):
         R, Mi = residual(m, vel, phi, phidot, kappa_q, source_q, bc)
@@ -142,8 +161,12 @@ def step(m, dt, vel, kappa_q, source_q, bc, bcval, bcdot, phi, phidot, iteration
             R = R + flux
         d = np.zeros_like(phi)
         d[free] = R[free] / M[free]
-        phi[free] += dt * gamma * d[free]
-        phidot[free] += d[free]
+        if it == 0:
+            phi[free] = (phi[free] + dt * (1.0 - gamma) * phidot[free]) + dt * gamma * d[free]
+            phidot[free] = d[free]
+        else:
+            phi[free] += dt * gamma * d[free]
+            phidot[free] += d[free]
     return phi, phidot
 
 

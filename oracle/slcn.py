@@ -73,30 +73,30 @@ def _shapes(m):
 
 
 def system(m, dt, kappa_q, source_q, phistar):
-    """Global (M + dt/2 D) and the right-hand side before Dirichlet elimination."""
+    """Global (M + dt/2 D) and the right-hand side before Dirichlet elimination
+    (the point loop of every element, vectorised over the elements)."""
+    from oracle.advdiff import elements
     N, dN, w = _shapes(m)
-    rows, cols, vals = [], [], []
+    nodes, h = elements(m)
+    ne, nen = m.n_el, m.nen
+    detJ = np.prod(0.5 * h, axis=1)
+    ps = phistar[nodes]
+    Ke = np.zeros((ne, nen, nen))
+    fe = np.zeros((ne, nen))
+    for q in range(len(w)):
+        G = dN[q][None] * (2.0 / h)[:, :, None]                     # [ne, dim, nen]
+        fac = w[q] * detJ
+        kq = kappa_q[:, q]
+        Ke += fac[:, None, None] * (np.outer(N[q], N[q])[None] + 0.5 * dt * kq[:, None, None]
+                                    * np.einsum("eda,edb->eab", G, G))
+        rhs = ps @ N[q] + (dt * source_q[:, q] if source_q is not None else 0.0)
+        Gps = np.einsum("eda,ea->ed", G, ps)
+        fe += fac[:, None] * (N[q][None, :] * rhs[:, None] - 0.5 * dt * kq[:, None] * np.einsum("eda,ed->ea", G, Gps))
+    rows = np.repeat(nodes, nen, axis=1).ravel()
+    cols = np.tile(nodes, (1, nen)).ravel()
+    K = sp.csr_matrix((Ke.ravel(), (rows, cols)), shape=(m.n_nodes, m.n_nodes))
     f = np.zeros(m.n_nodes)
-    for e in range(m.n_el):
-        nodes = m.element_nodes(e)
-        idx = _elem_index(m, e)
-        h = np.array([m.axes[d][idx[d] + 1] - m.axes[d][idx[d]] for d in range(m.dim)])
-        detJ = float(np.prod(0.5 * h))
-        Ke = np.zeros((m.nen, m.nen))
-        fe = np.zeros(m.nen)
-        ps = phistar[nodes]
-        for q in range(len(w)):
-            G = dN[q] * (2.0 / h)[:, None]
-            fac = w[q] * detJ
-            Ke += fac * (np.outer(N[q], N[q]) + 0.5 * dt * kappa_q[e, q] * (G.T @ G))
-            rhs = float(N[q] @ ps) + (dt * source_q[e, q] if source_q is not None else 0.0)
-            fe += fac * (N[q] * rhs - 0.5 * dt * kappa_q[e, q] * (G.T @ (G @ ps)))
-        rows.append(np.repeat(nodes, m.nen))
-        cols.append(np.tile(nodes, m.nen))
-        vals.append(Ke.ravel())
-        np.add.at(f, nodes, fe)
-    K = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
-                      shape=(m.n_nodes, m.n_nodes))
+    np.add.at(f, nodes.ravel(), fe.ravel())
     return K, f
 
 

@@ -32,3 +32,16 @@ def test_convergence_rate(name, order):
     assert np.isclose(v, order + 1, rtol=0.2), "velocity slope %.3f (errors %s)" % (v, ev)
     assert np.isclose(p, order, rtol=0.2), "pressure slope %.3f (errors %s)" % (p, ep)
     assert ev[-1] < 0.05 and ep[-1] < 0.2
+
+
+def test_solcx_vrms_known_answer():
+    """docs/examples/10_Analytic_Solutions.ipynb checks the standard SolCx case
+    (n_z = 1, eta_B = 1e5, Q2/dPc1, 32 x 32) for v_rms = 0.005578279626793198
+    within 1e-7 relative."""
+    sol = fn.analytic.SolCx(n_z=1, eta_B=100000.0)
+    m, u, p = ac.solve(sol, 2, 32)
+    rule = ac._Rule(m, 5)
+    wq = np.tile(rule.w * rule.det, m.n_el)
+    uq = np.einsum("qn,eni->eqi", rule.N, u.reshape(-1, 2)[rule.nodes]).reshape(-1, 2)
+    vrms = np.sqrt(wq @ (uq ** 2).sum(1) / wq.sum())
+    assert np.isclose(vrms, 0.005578279626793198, rtol=1e-7), vrms

@@ -13,10 +13,10 @@ from the last Stokes solution (sigma_zz = 2 dw/dz - p minus its mean, scaled by
 eta0 kappa / h^2 / (rho g)).  Discretisation and solves are the oracle's
 (tests/oracle_system.py, oracle/advdiff.py); the notebook's tolerances apply:
 1e-2 for Nu, v_rms, q1, q2 and 1e-3 for the topography at both top corners and
-the x position of its zero.  The first SUPG step is also held to the
-reference's own run as the notebook's saved output prints it (Nu before the
-loop to 6 decimals, v_rms to 3, the relative Nu change of the step to 4
-significant digits).  The test reads the reference tree and is skipped where
+the x position of its zero.  Both SUPG steps are also held to the reference's
+own run as the notebook's saved output prints it (Nu before the loop to 6
+decimals, v_rms to 3, the relative Nu change of the first step to 4
+significant digits, q1 and q2 after the second step to 3 decimals).  The test reads the reference tree and is skipped where
 it is absent.
 """
 import os
@@ -126,6 +126,8 @@ def test_blankenbach_case_a():
     dTdz = (Tg[-1] - Tg[-2]) / h
     assert np.isclose(-dTdz[0], 8.020, rtol=1e-2), -dTdz[0]
     assert np.isclose(-dTdz[-1], 0.589, rtol=1e-2), -dTdz[-1]
+    # the saved output of the reference's run: "q1 = 8.021; q2 = 0.589"
+    assert round(-dTdz[0], 3) == 8.021 and round(-dTdz[-1], 3) == 0.589, (-dTdz[0], -dTdz[-1])
 
     W = u.reshape(res + 1, res + 1, 2)[..., 1]
     dwdz = (W[-1] - W[-2]) / h                        # at the top nodes, per top element linear in x

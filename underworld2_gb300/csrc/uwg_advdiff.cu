@@ -2,8 +2,8 @@
 // explicit predictor-multicorrector of the reference's AdvDiffMulticorrector
 // (L/Underworld/Utils/AdvectionDiffusion/src/Multicorrector.c:166-300) with the
 // residual of AdvDiffResidualForceTerm (Residual.cpp:213-341), the upwind
-// diffusivity of Brooks & Hughes 1982 (Residual.cpp:416-506, "Exact" xi,
-// :557-568), the lumped mass of LumpedMassMatrixForceTerm.c:139-172 and the
+// diffusivity of Brooks & Hughes 1982 (Residual.cpp:416-506, the doubly
+// asymptotic xi of :580-587 that the Python interface selects), the lumped mass of LumpedMassMatrixForceTerm.c:139-172 and the
 // time-step bound of Timestep.c:31-117.  Integration is the default Gauss
 // swarm: 3 points per axis.
 //
@@ -11,6 +11,13 @@
 // tensor Gauss points) and scatters it with FP64 atomics; the vector updates
 // are element-free.  Dirichlet nodes are left out
 // of every update (the reference removes them from its equation numbering).
+//
+// Order of a step, as the reference's _AdvDiffMulticorrector_Solve runs it:
+// Dirichlet values go onto phi and phi-dot; the predictor acts on the
+// reference's solution vectors only while its residual reads the nodal fields,
+// so the first residual sees phi_n and phidot_n from before the predictor.  The
+// first correction therefore applies predictor and corrector together
+// (k_supg_predict_correct); later ones are plain correctors.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -30,12 +37,15 @@ inline unsigned nblk(int64_t n, int t = 256) { return (unsigned)((n + t - 1) / t
 __constant__ double c_gx[3] = {-0.7745966692414834, 0.0, 0.7745966692414834};
 __constant__ double c_gw[3] = {0.5555555555555556, 0.8888888888888888, 0.5555555555555556};
 
-// xi(alpha) = coth(alpha) - 1/alpha with the reference's asymptotic branches
-__device__ __forceinline__ double upwind_xi_exact(double pe) {
-    if (fabs(pe) < 1.0e-8) return 0.33333333333333 * pe;
-    if (pe < -20.0) return -1.0 - 1.0 / pe;
-    if (pe > 20.0) return +1.0 - 1.0 / pe;
-    return cosh(pe) / sinh(pe) - 1.0 / pe;
+// Upwind parameter xi(alpha): the doubly asymptotic approximation of
+// coth(alpha) - 1/alpha (Brooks & Hughes 1982, eq. 3.3.1), the one the reference's
+// Python interface selects for its SUPG term ("UpwindXiFunction" =
+// "DoublyAsymptoticAssumption", P/systems/sle/_assemblyterm.py:388;
+// Residual.cpp:580-587)
+__device__ __forceinline__ double upwind_xi(double pe) {
+    if (pe <= -3.0) return -1.0;
+    if (pe <= 3.0) return 0.33333333333333 * pe;
+    return 1.0;
 }
 
 template <int DIM>
@@ -103,7 +113,7 @@ __global__ void __launch_bounds__(128) k_supg_residual(uwg_lgeom g, const double
         for (int n = 0; n < NEN; n++) vc += v[n][d];
         vc *= 1.0 / NEN;
         const double L = fabs(h[d]);
-        upwind += upwind_xi_exact(vc * L / (2.0 * kavg)) * vc * L;
+        upwind += upwind_xi(vc * L / (2.0 * kavg)) * vc * L;
     }
     upwind *= SUPG_ISQRT15;
     const bool perturb = !pure_diffusion && !(fabs(upwind) < SUPG_MIN_DIFFUSIVITY);
@@ -245,6 +255,27 @@ __global__ void k_supg_predict(int64_t n, const uint8_t* bc, const double* bcval
     phidot[i] = 0.0;
 }
 
+// Dirichlet values onto both fields (FeVariable_ApplyBCs on phi and phi-dot)
+__global__ void k_supg_bc(int64_t n, const uint8_t* bc, const double* bcval, const double* bcdot, double* phi,
+                          double* phidot) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n || !bc[i]) return;
+    phi[i] = bcval[i];
+    phidot[i] = bcdot ? bcdot[i] : 0.0;
+}
+
+// First correction with the predictor: d = R / M,
+// phi = (phi_n + fp phidot_n) + fc d, phidot = d.  flux as k_supg_correct.
+__global__ void k_supg_predict_correct(int64_t n, const uint8_t* bc, const double* R, const double* flux,
+                                       const double* M, double fp, double fc, double* phi, double* phidot) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n || bc[i]) return;
+    const double d = (flux ? R[i] + flux[i] : R[i]) / M[i];
+    const double p = phi[i] + fp * phidot[i];
+    phi[i] = p + fc * d;
+    phidot[i] = d;
+}
+
 // flux: the boundary-flux vector added to the residual, or NULL
 __global__ void k_supg_correct(int64_t n, const uint8_t* bc, const double* R, const double* flux, const double* M,
                                double f, double* phi, double* phidot) {
@@ -321,7 +352,10 @@ extern "C" int uwg_advdiff_step(uwg_ctx* c, double dt, const double* vel, const 
     double *R = nullptr, *M = nullptr;
     UWG_CUDA(c, cudaMallocAsync((void**)&R, sizeof(double) * n, c->stream));
     UWG_CUDA(c, cudaMallocAsync((void**)&M, sizeof(double) * n, c->stream));
-    k_supg_predict<<<nblk(n), 256, 0, c->stream>>>(n, bc, bcval, bcdot, dt * (1.0 - gamma), phi, phidot);
+    if (iterations == 0)        // predictor only
+        k_supg_predict<<<nblk(n), 256, 0, c->stream>>>(n, bc, bcval, bcdot, dt * (1.0 - gamma), phi, phidot);
+    else
+        k_supg_bc<<<nblk(n), 256, 0, c->stream>>>(n, bc, bcval, bcdot, phi, phidot);
     cudaError_t err = cudaGetLastError();
     for (int it = 0; it < iterations && err == cudaSuccess; it++) {
         cudaMemsetAsync(R, 0, sizeof(double) * n, c->stream);
@@ -332,7 +366,11 @@ extern "C" int uwg_advdiff_step(uwg_ctx* c, double dt, const double* vel, const 
         else
             k_supg_residual<2><<<nblk(c->n_el, 128), 128, 0, c->stream>>>(g, vel, phi, phidot, kappa_q, source_q, bc,
                                                                           vel ? 0 : 1, R, it == 0 ? M : nullptr);
-        k_supg_correct<<<nblk(n), 256, 0, c->stream>>>(n, bc, R, flux, M, dt * gamma, phi, phidot);
+        if (it == 0)
+            k_supg_predict_correct<<<nblk(n), 256, 0, c->stream>>>(n, bc, R, flux, M, dt * (1.0 - gamma),
+                                                                   dt * gamma, phi, phidot);
+        else
+            k_supg_correct<<<nblk(n), 256, 0, c->stream>>>(n, bc, R, flux, M, dt * gamma, phi, phidot);
         err = cudaGetLastError();
     }
     cudaFreeAsync(R, c->stream);
