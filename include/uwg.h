@@ -101,6 +101,19 @@ int uwg_layout_random(uwg_ctx* ctx, int ppc, int64_t* rng_state_h, double* x, in
  * Mesh_RegularAlgorithms_SearchElements (L/StgDomain/Mesh/src/Mesh_RegularAlgorithms.c:174-205). */
 int uwg_locate(uwg_ctx* ctx, int64_t np, const double* x, int32_t* owner);
 
+/* Material particle of each Gauss integration point, for swarm-variable functions
+ * evaluated on a Gauss integration swarm.  Replaces GeneralSwarm_IntegrationPointMap
+ * (L/PICellerator/MaterialPoints/src/GeneralSwarm.cpp:319-431, called from
+ * SwarmVariableFn, L/Underworld/Function/src/SwarmVariableFn.cpp:73-101): the
+ * point's global position by FeMesh_CoordLocalToGlobal, then the first particle of
+ * its element's cell list at the least squared distance.
+ *   xi_q          [nq*dim] local coordinates of the element's points (device)
+ *   cell_offsets, cell_list, x   the swarm's cell tables and coordinates (device)
+ *   pid           [n_el*nq] out: particle index per point, element-major; -1 where
+ *                 the element holds no particle (the reference raises there) */
+int uwg_gauss_nearest(uwg_ctx* ctx, int nq, const double* xi_q, const int32_t* cell_offsets,
+                      const int32_t* cell_list, const double* x, int32_t* pid);
+
 /* Owner update with the reference's cell-table semantics: particles are
  * visited in index order, a leaver is removed from its old cell by
  * swap-with-last, an arrival is appended.  cell_offsets/cell_list are

@@ -189,6 +189,31 @@ class Mesh:
                            _p(tbl), _p(cnt), tbl.shape[1], 0, self.n_el, dvc_res, _p(ip_xi), _p(ip_w))
         return ip_xi, ip_w
 
+    def gauss_nearest(self, x, tbl, cnt, xi_q):
+        """Particle of every Gauss point, as GeneralSwarm_IntegrationPointMap finds it
+        (L/PICellerator/MaterialPoints/src/GeneralSwarm.cpp:319-431): the point's
+        global position (FeMesh_CoordLocalToGlobal), then the first particle of the
+        element's cell table at the least squared distance; -1 in empty elements.
+        Returns [n_el, nq]."""
+        xi_q = np.asarray(xi_q, dtype=np.float64)
+        key = xi_q.tobytes()
+        cache = self.__dict__.setdefault("_gauss_global", {})
+        if key not in cache:
+            cache[key] = np.array([[self.local_to_global(e, q) for q in xi_q] for e in range(self.n_el)])
+        G = cache[key]
+        out = np.full((self.n_el, len(xi_q)), -1, dtype=np.int64)
+        for e in range(self.n_el):
+            if cnt[e] == 0:
+                continue
+            ps = tbl[e, : cnt[e]]
+            g = G[e]
+            d2 = np.zeros((len(xi_q), len(ps)))
+            for d in range(self.dim):
+                dd = g[:, d][:, None] - x[ps, d][None, :]
+                d2 = d2 + dd * dd
+            out[e] = ps[np.argmin(d2, axis=1)]
+        return out
+
     # -- element terms ---------------------------------------------------
     def element_K(self, el, xi, w, eta):
         nd = self.dim * self.nen

@@ -1,0 +1,78 @@
+"""Swarm variables on a Gauss integration swarm (GPU, through the C ABI and the
+uw-style API): each Gauss point takes the value of the nearest particle of its
+element, as GeneralSwarm_IntegrationPointMap finds it
+(L/PICellerator/MaterialPoints/src/GeneralSwarm.cpp:319-431), checked against
+the oracle's restatement (oracle.Mesh.gauss_nearest); then a Stokes system
+without a voronoi swarm whose functions read a swarm variable, the case of the
+reference's Rayleigh-Taylor example, against the oracle's direct solve.  The
+same map drives tests/test_rayleigh_taylor_known_answer.py on the CPU."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from tests import analytic_convergence as ac
+from tests import oracle_system as osys
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("dim,order,res", [(2, 1, (6, 5)), (3, 1, (3, 3, 2)), (2, 2, (4, 3))])
+def test_gauss_nearest_matches_oracle(gpu, dim, order, res):
+    from underworld2_gb300._core import Context, rng_seed
+    c = Context(dim, res, (0.0,) * dim, (1.0,) * dim, order=order, porder=order - 1)
+    ppc = 7
+    x, owner, off, lst, _ = c.layout_random(ppc, rng_seed(13))
+    m = oracle.Mesh(dim, order, res, (0.0,) * dim, (1.0,) * dim, porder=order - 1)
+    xo, _ = m.layout_random(ppc, 13)
+    np.testing.assert_array_equal(x.cpu().numpy(), xo)
+    tbl, cnt, _ = m.initial_tables(ppc, ppc)
+    ng = 3 if order == 1 else 5
+    xi, _ = m.gauss_points(ng)
+    pid = c.gauss_nearest(torch.from_numpy(xi), off, lst, x).cpu().numpy().reshape(m.n_el, len(xi))
+    np.testing.assert_array_equal(pid, m.gauss_nearest(xo, tbl, cnt, xi))
+
+
+def test_stokes_on_gauss_swarm_with_swarm_variables(gpu):
+    import underworld2_gb300 as uw
+    res = (16, 16)
+    mesh = uw.mesh.FeMesh_Cartesian(elementType="Q1/dQ0", elementRes=res, minCoord=(0.0, 0.0), maxCoord=(1.0, 1.0))
+    velocityField = mesh.add_variable(nodeDofCount=2)
+    pressureField = mesh.subMesh.add_variable(nodeDofCount=1)
+    swarm = uw.swarm.Swarm(mesh=mesh)
+    material = swarm.add_variable(dataType="int", count=1)
+    swarm.populate_using_layout(layout=uw.swarm.layouts.PerCellRandomLayout(swarm=swarm, particlesPerCell=12, seed=13))
+    xy = swarm.particleCoordinates.data.copy()
+    material.data[:, 0] = (xy[:, 1] > 0.2 + 0.02 * np.cos(np.pi * xy[:, 0])).astype(np.int32)
+    fn_visc = uw.function.branching.map(fn_key=material, mapping={0: 0.1, 1: 1.0})
+    fn_dens = uw.function.branching.map(fn_key=material, mapping={0: 0.0, 1: 1.0})
+    iWalls = mesh.specialSets["MinI_VertexSet"] + mesh.specialSets["MaxI_VertexSet"]
+    jWalls = mesh.specialSets["MinJ_VertexSet"] + mesh.specialSets["MaxJ_VertexSet"]
+    bc = uw.conditions.DirichletCondition(variable=velocityField, indexSetsPerDof=(iWalls, jWalls))
+    stokes = uw.systems.Stokes(velocityField=velocityField, pressureField=pressureField, conditions=[bc],
+                               fn_viscosity=fn_visc, fn_bodyforce=fn_dens * (0.0, -1.0))
+    solver = uw.systems.Solver(stokes)
+    solver.set_inner_rtol(1e-11)
+    solver.set_outer_rtol(1e-10)
+    solver.solve()
+    # oracle: the same Gauss points, materials of the nearest particles, direct solve
+    m = oracle.Mesh(2, 1, res, (0.0, 0.0), (1.0, 1.0))
+    tbl, cnt, _ = m.initial_tables(12, 12)
+    g = ac._Rule(m, 3)
+    nq = len(g.w)
+    pid = m.gauss_nearest(xy, tbl, cnt, g.xi).ravel()
+    mat = material.data[:, 0][pid]
+    eta = np.where(mat == 1, 1.0, 0.1)
+    body = np.zeros((m.n_el * nq, 2))
+    body[:, 1] = -np.where(mat == 1, 1.0, 0.0)
+    X = m.node_coords()[:, :2]
+    mask = np.zeros(m.n_nodes * 2, np.uint8)
+    for d in range(2):
+        mask[np.flatnonzero(np.isclose(X[:, d], 0.0) | np.isclose(X[:, d], 1.0)) * 2 + d] = 1
+    pts = [(e * nq + np.arange(nq), g.xi, g.w) for e in range(m.n_el)]
+    uo, po = osys.solve(osys.assemble(m, pts, eta, body, mask, np.zeros(m.n_nodes * 2)), m.n_nodes * 2)
+    u = velocityField.data.ravel()
+    assert np.linalg.norm(u - uo) / np.linalg.norm(uo) < 1e-8
+    p = pressureField.data[:, 0]
+    p, po = p - p.mean(), po - po.mean()
+    assert np.linalg.norm(p - po) / np.linalg.norm(po) < 1e-8

@@ -106,6 +106,14 @@ class Context:
         self._call("uwg_locate", x.shape[0], _ptr(x), _ptr(owner))
         return owner
 
+    def gauss_nearest(self, xi_q, off, lst, x):
+        """Particle index of each Gauss point (element-major), -1 in empty elements."""
+        xi_q = xi_q.to(device=self.device, dtype=torch.float64).contiguous()
+        x = x.to(torch.float64).contiguous()
+        pid = self.zeros(self.n_el * xi_q.shape[0], dtype=torch.int32)
+        self._call("uwg_gauss_nearest", xi_q.shape[0], _ptr(xi_q), _ptr(off), _ptr(lst), _ptr(x), _ptr(pid))
+        return pid
+
     def update_owners(self, x, owner, off, lst):
         """Owner update; x may be stored in FP64 or FP32."""
         lost = ctypes.c_int64(0)

@@ -83,6 +83,7 @@ SIGNATURES = {
     "uwg_mesh_axis": (_I, [_CTX, _I, _P]),
     "uwg_layout_random": (_I, [_CTX, _I, ctypes.POINTER(_I64), _P, _P, _P, _P]),
     "uwg_locate": (_I, [_CTX, _I64, _P, _P]),
+    "uwg_gauss_nearest": (_I, [_CTX, _I, _P, _P, _P, _P, _P]),
     "uwg_update_owners": (_I, [_CTX, _I64, _P, _P, _P, _P, ctypes.POINTER(_I64)]),
     "uwg_update_owners_f32": (_I, [_CTX, _I64, _P, _P, _P, _P, ctypes.POINTER(_I64)]),
     "uwg_pic_map": (_I, [_CTX, _I64, _P, _P, _P, _P]),

@@ -348,6 +348,64 @@ extern "C" int uwg_layout_random(uwg_ctx* c, int ppc, int64_t* rng_state_h, doub
     return UWG_OK;
 }
 
+// Material particle of every Gauss integration point, as GeneralSwarm_IntegrationPointMap
+// finds it when a swarm variable is evaluated on a Gauss integration swarm
+// (L/PICellerator/MaterialPoints/src/GeneralSwarm.cpp:319-431): the point's global
+// position by FeMesh_CoordLocalToGlobal, then the first particle of its element's
+// list at the least squared distance.  pid = -1 where the element holds no particle.
+// One thread per (element, point); t = e * nq + q.
+template <int DIM, int ORDER>
+__global__ void k_gauss_nearest(uwg_geom g, int64_t n_el, int nq, const double* xi_q, const int32_t* off,
+                                const int32_t* lst, const double* x, int32_t* pid) {
+    constexpr int NEN = Shape<DIM, ORDER>::NEN;
+    int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= n_el * nq) return;
+    int64_t e = t / nq;
+    int q = (int)(t - e * nq);
+    int eidx[3];
+    el_index(g, e, eidx);
+    double N[NEN];
+    Shape<DIM, ORDER>::N(xi_q + q * DIM, N);
+    double pt[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int n = 0; n < NEN; n++)
+#pragma unroll
+        for (int d = 0; d < DIM; d++) pt[d] += N[n] * node_coord<DIM, ORDER>(g, eidx, n, d);
+    double best = 1.7976931348623157e308;
+    int32_t bi = -1;
+    for (int32_t k = off[e]; k < off[e + 1]; k++) {
+        const int32_t i = lst[k];
+        double d2 = 0.0;
+#pragma unroll
+        for (int d = 0; d < DIM; d++) {
+            const double dd = pt[d] - x[(int64_t)i * DIM + d];
+            d2 += dd * dd;
+        }
+        if (d2 < best) {
+            best = d2;
+            bi = i;
+        }
+    }
+    pid[t] = bi;
+}
+
+extern "C" int uwg_gauss_nearest(uwg_ctx* c, int nq, const double* xi_q, const int32_t* cell_offsets,
+                                 const int32_t* cell_list, const double* x, int32_t* pid) {
+    if (!c || nq < 1 || !xi_q || !cell_offsets || !cell_list || !x || !pid)
+        return uwg_set_error(c, UWG_ERR_ARG, "uwg_gauss_nearest: bad argument");
+    const int64_t n = c->n_el * (int64_t)nq;
+    uwg_geom g = make_geom(c);
+    if (c->dim == 2) {
+        if (c->order == 1) k_gauss_nearest<2, 1><<<nblk(n), 256, 0, c->stream>>>(g, c->n_el, nq, xi_q, cell_offsets, cell_list, x, pid);
+        else k_gauss_nearest<2, 2><<<nblk(n), 256, 0, c->stream>>>(g, c->n_el, nq, xi_q, cell_offsets, cell_list, x, pid);
+    } else {
+        if (c->order == 1) k_gauss_nearest<3, 1><<<nblk(n), 256, 0, c->stream>>>(g, c->n_el, nq, xi_q, cell_offsets, cell_list, x, pid);
+        else k_gauss_nearest<3, 2><<<nblk(n), 256, 0, c->stream>>>(g, c->n_el, nq, xi_q, cell_offsets, cell_list, x, pid);
+    }
+    UWG_CUDA(c, cudaGetLastError());
+    return UWG_OK;
+}
+
 extern "C" int uwg_locate(uwg_ctx* c, int64_t np, const double* x, int32_t* owner) {
     if (!c || np < 0 || (np && (!x || !owner))) return uwg_set_error(c, UWG_ERR_ARG, "uwg_locate: bad argument");
     if (!np) return UWG_OK;

@@ -58,7 +58,7 @@ class FeMesh_Cartesian:
         types = [t.upper() for t in elementType]
         if types[0] == "Q1" and (len(types) == 1 or types[1] == "DQ0"):
             order, porder = 1, 0
-        elif types[0] == "Q2" and len(types) > 1 and types[1] == "DPC1":
+        elif types[0] == "Q2" and (len(types) == 1 or types[1] == "DPC1"):
             order, porder = 2, 1
         else:
             raise ValueError("supported element types: 'Q1/dQ0' and 'Q2/dPc1' (got %s)" % "/".join(elementType))

@@ -127,15 +127,18 @@ class Stokes:
             e = _fn.EvalContext(s._lst[:n].long(), vs.global_coords, ctx.device, lib_ctx=ctx,
                                 pid32=s._lst[:n].to(torch.int32).contiguous())
             return s._off, s._lst, vs.ip_xi, vs.ip_w, e
-        # Gauss integration (3 points per axis), one "particle" per point
-        x1, w1 = np.polynomial.legendre.leggauss(3)
+        # Gauss integration, one "particle" per point: the default GaussIntegrationSwarm
+        # of the mesh, 3 points per axis on Q1 and 5 on Q2 (P/swarm/_integration_swarm.py:173-181)
+        ng = 5 if self.mesh.elementType.upper().startswith("Q2") else 3
+        x1, w1 = np.polynomial.legendre.leggauss(ng)
         dim = self.mesh.dim
+        r = range(ng)
         if dim == 2:
-            xi = np.array([[x1[i], x1[j]] for j in range(3) for i in range(3)])
-            w = np.array([w1[i] * w1[j] for j in range(3) for i in range(3)])
+            xi = np.array([[x1[i], x1[j]] for j in r for i in r])
+            w = np.array([w1[i] * w1[j] for j in r for i in r])
         else:
-            xi = np.array([[x1[i], x1[j], x1[k]] for k in range(3) for j in range(3) for i in range(3)])
-            w = np.array([w1[i] * w1[j] * w1[k] for k in range(3) for j in range(3) for i in range(3)])
+            xi = np.array([[x1[i], x1[j], x1[k]] for k in r for j in r for i in r])
+            w = np.array([w1[i] * w1[j] * w1[k] for k in r for j in r for i in r])
         nq = len(w)
         ne = ctx.n_el
         ip_xi = torch.from_numpy(np.tile(xi, (ne, 1))).to(ctx.device)
@@ -154,14 +157,40 @@ class Stokes:
                 out[:, d] = lo + (ip_xi[:, d] + 1.0) * 0.5 * (hi - lo)
             return out
 
-        if self._fn_viscosity.depends_on({"swarm"}) or self._fn_bodyforce.depends_on({"swarm"}):
-            raise ValueError("swarm-variable functions need a voronoi_swarm")
-        return off, lst, ip_xi, ip_w, _fn.EvalContext(lst.long(), coords, ctx.device, lib_ctx=ctx,
-                                                      pid32=lst.to(torch.int32).contiguous())
+        swarms = _swarms_in(self._fn_viscosity, self._fn_bodyforce, self._fn_one_on_lambda, self._fn_source)
+        if not swarms:
+            return off, lst, ip_xi, ip_w, _fn.EvalContext(lst.long(), coords, ctx.device, lib_ctx=ctx,
+                                                          pid32=lst.to(torch.int32).contiguous())
+        # swarm variables on the Gauss points: each point takes the value of the nearest
+        # particle of its element (SwarmVariableFn over GeneralSwarm_IntegrationPointMap,
+        # L/Underworld/Function/src/SwarmVariableFn.cpp:73-101)
+        if len(swarms) > 1:
+            raise NotImplementedError("swarm variables of more than one swarm on a Gauss integration swarm")
+        sw = swarms[0]
+        if sw._x is None or sw._off is None:
+            raise RuntimeError("Error occurred while trying to evaluate swarm variable. This can occur when there "
+                               "are no particles found in a given element.")
+        pid = ctx.gauss_nearest(torch.from_numpy(xi), sw._off, sw._lst, sw._x)
+        if bool((pid < 0).any()):
+            raise RuntimeError("Error occurred while trying to evaluate swarm variable. This can occur when there "
+                               "are no particles found in a given element. You may wish to add population "
+                               "control mechanisms.")
+        e = _fn.EvalContext(pid.long(), coords, ctx.device, lib_ctx=ctx, pid32=pid)
+        e.point_order = True          # rows are the Gauss points; pid only indexes the swarm's data
+        return off, lst, ip_xi, ip_w, e
 
     def _per_particle(self, f, ectx, npart, ncomp):
         # one kernel for the whole graph, writing straight into particle order
         # (uwg_fn_eval); graphs with node kinds it does not cover use the tensor path
+        if getattr(ectx, "point_order", False):
+            v = _fn._eval_kernel(f, ectx, ncomp)
+            if v is None:
+                v = f.evaluate_at(ectx).to(torch.float64)
+                if v.shape[1] == 1 and ncomp != 1:
+                    v = v.expand(v.shape[0], ncomp)
+            if v.shape[1] != ncomp:
+                raise ValueError("function returns %d components, %d expected" % (v.shape[1], ncomp))
+            return v.contiguous()
         out = torch.zeros((npart, ncomp), dtype=torch.float64, device=ectx.device)
         if _fn._eval_kernel(f, ectx, ncomp, out) is not None:
             return out
@@ -449,6 +478,21 @@ def _uses_swarm(f):
     if isinstance(f, _fn._SwarmVar):
         return True
     return any(_uses_swarm(c) for c in f._children())
+
+
+def _swarms_in(*fns):
+    """The swarms whose variables the function graphs read."""
+    found, seen = {}, set()
+    stack = [f for f in fns if f is not None]
+    while stack:
+        f = stack.pop()
+        if id(f) in seen:
+            continue
+        seen.add(id(f))
+        if isinstance(f, _fn._SwarmVar):
+            found[id(f.var.swarm)] = f.var.swarm
+        stack.extend(c for c in f._children() if c is not None)
+    return list(found.values())
 
 
 def _gauss_eval(mesh, f, n):
