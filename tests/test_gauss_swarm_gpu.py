@@ -76,3 +76,21 @@ def test_stokes_on_gauss_swarm_with_swarm_variables(gpu):
     p = pressureField.data[:, 0]
     p, po = p - p.mean(), po - po.mean()
     assert np.linalg.norm(p - po) / np.linalg.norm(po) < 1e-8
+
+
+def test_swarm_variable_at_coordinates_takes_nearest_particle(gpu):
+    """docs/user_guide/04_Functions.ipynb: a swarm variable evaluated at plain
+    coordinates returns its nearest particle's value (the guide expects particle 1
+    at (0.4, 0.4) for the point (0.5, 0.5)); integer variables stay integers."""
+    import underworld2_gb300 as uw
+    mesh = uw.mesh.FeMesh_Cartesian(maxCoord=(2.0, 1.0))
+    swarm = uw.swarm.Swarm(mesh)
+    swarm.add_particles_with_coordinates(np.array([(0.1, 0.1), (0.4, 0.4), (0.9, 0.9), (1.0, 0.1), (1.9, 0.1)]))
+    index_var = swarm.add_variable("int", 1)
+    index_var.data[:, 0] = np.arange(swarm.particleLocalCount)
+    result = index_var.evaluate((0.5, 0.5))
+    assert result.dtype == np.int32 and result.tolist() == [[1]]
+    pts = np.array([[1.8, 0.0], [0.1, 0.11], [0.95, 0.8]])
+    d2 = ((pts[:, None, :] - swarm.data[None, :, :]) ** 2).sum(-1)
+    np.testing.assert_array_equal(index_var.evaluate(pts)[:, 0], np.argmin(d2, axis=1))
+    np.testing.assert_array_equal(index_var.evaluate(swarm)[:, 0], np.arange(5))

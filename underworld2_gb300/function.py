@@ -220,15 +220,44 @@ coord = input
 class _SwarmVar(Function):
     def __init__(self, var):
         self.var = var
+        # integer swarm variables evaluate to integers (the reference's IO_int output)
+        self._int = getattr(var, "dataType", "double") in ("int", "char", "short", "long")
 
     def _eval(self, ctx):
         d = self.var._device_data()
         if d.dim() == 1:
             d = d[:, None]
-        return d[ctx.pid.long()].double()
+        pid = ctx.pid.long()
+        if pid.numel() and bool((pid < 0).any()):
+            pid = _closest_particles(self.var.swarm, ctx.coords, pid)
+        return d[pid].double()
 
     def depends_on(self, kinds):
         return "swarm" in kinds
+
+
+def _closest_particles(swarm, pts, pid, chunk_elems=1 << 24):
+    """Index of the closest particle of `swarm` to each point that has none yet
+    (pid < 0): a swarm variable evaluated at plain coordinates takes its nearest
+    particle's value (SwarmVariableFn, L/Underworld/Function/src/SwarmVariableFn.cpp:
+    129-171, over GeneralSwarm_GetClosestParticles).  Exhaustive search in chunks;
+    ties go to the lowest particle index."""
+    if pts.shape[1] != swarm.dim:
+        raise RuntimeError("Function input dimensionality (%d) does not appear to match swarm variable "
+                           "dimensionality (%d)." % (pts.shape[1], swarm.dim))
+    x = swarm._x
+    if x is None or x.shape[0] == 0:
+        raise RuntimeError("Unable to evaluate SwarmVariable: the swarm holds no particles.")
+    x = x.to(device=pts.device, dtype=torch.float64)
+    pid = pid.clone()
+    todo = torch.nonzero(pid < 0).flatten()
+    step = max(1, chunk_elems // x.shape[0])
+    for s in range(0, todo.numel(), step):
+        idx = todo[s:s + step]
+        q = pts[idx].to(torch.float64)
+        d2 = ((q[:, None, :] - x[None, :, :]) ** 2).sum(-1)
+        pid[idx] = torch.argmin(d2, dim=1)
+    return pid
 
 
 class _MeshVar(Function):

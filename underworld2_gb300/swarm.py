@@ -143,6 +143,16 @@ class SwarmVariable:
         with open(filename, "w") as fh:
             fh.write(text)
 
+    def evaluate(self, inputData=None, inputType=None):
+        """Values at the swarm's particles, at another swarm's or mesh's points or at
+        coordinates (the nearest particle's value), as a Function
+        (P/function/_function.py:808-930)."""
+        return self._as_function().evaluate(inputData, inputType)
+
+    def __getitem__(self, i): return self._as_function()[i]
+    def __neg__(self): return -self._as_function()
+    def __pow__(self, o): return self._as_function() ** o
+    def __rtruediv__(self, o): return o / self._as_function()
     def __add__(self, o): return self._as_function() + o
     def __radd__(self, o): return o + self._as_function()
     def __mul__(self, o): return self._as_function() * o
