@@ -1,4 +1,4 @@
-"""Known answers of two of the reference's Stokes test notebooks, restated on
+"""Known answers of the reference's Stokes test and example notebooks, restated on
 the oracle's discretisation (element terms of oracle/uwo.c, surface term of
 oracle/surface.py, direct solve of tests/oracle_system.py) -- CPU.
 
@@ -73,3 +73,34 @@ def test_compressible_extension_continuity():
     wq = rule.w * rule.det
     err = np.sum(np.abs(div + p[:, None] * one_on_lambda) * wq[None, :]) / (2.0 * 1.0)
     assert err < 1e-6, err
+
+
+def test_convection_example_vrms():
+    """docs/examples/02_Convection_Example.ipynb: a 32 x 16 Q1/dQ0 box [0, 2] x [0, 1],
+    Ra = 1e4, unit viscosity and diffusivity, T = 1 - y + 0.2 cos(pi x) sin(pi y)
+    clipped to [0, 1] with T = 1 / 0 on the bottom / top, free-slip walls; 20
+    steps of Stokes then SUPG at get_max_dt() (oracle/advdiff.py).  The notebook
+    checks the final v_rms against 8.70754e+01 with numpy's default isclose."""
+    from oracle import advdiff
+    m = oracle.Mesh(2, 1, (32, 16), (0.0, 0.0), (2.0, 1.0))
+    X = m.node_coords()[:, :2]
+    T = np.clip(1.0 - X[:, 1] + 0.2 * np.cos(np.pi * X[:, 0]) * np.sin(np.pi * X[:, 1]), 0.0, 1.0)
+    bot, top = np.isclose(X[:, 1], 0.0), np.isclose(X[:, 1], 1.0)
+    T[bot], T[top] = 1.0, 0.0
+    mask = np.zeros(m.n_nodes * 2, np.uint8)
+    mask[np.flatnonzero(np.isclose(X[:, 0], 0.0) | np.isclose(X[:, 0], 2.0)) * 2] = 1
+    mask[np.flatnonzero(bot | top) * 2 + 1] = 1
+    rule = ac._Rule(m, 3)
+    nq = len(rule.w)
+    pts = [(e * nq + np.arange(nq), rule.xi, rule.w) for e in range(m.n_el)]
+    kq, Tdot = np.ones((m.n_el, 9)), np.zeros(m.n_nodes)
+    for _ in range(20):
+        body = np.zeros((m.n_el * nq, 2))
+        body[:, 1] = 1.0e4 * np.einsum("qn,en->eq", rule.N, T[rule.nodes]).ravel()
+        u, _ = osys.solve(osys.assemble(m, pts, np.ones(m.n_el * nq), body, mask, np.zeros(m.n_nodes * 2)),
+                          m.n_nodes * 2)
+        U = u.reshape(-1, 2)
+        T, Tdot = advdiff.step(m, advdiff.max_dt(m, U, kq), U, kq, None, bot | top, T.copy(), None, T, Tdot)
+    wq = np.tile(rule.w * rule.det, m.n_el)
+    uq = np.einsum("qn,eni->eqi", rule.N, u.reshape(-1, 2)[rule.nodes]).reshape(-1, 2)
+    assert np.isclose(np.sqrt(wq @ (uq ** 2).sum(1) / wq.sum()), 8.70754e+01)
