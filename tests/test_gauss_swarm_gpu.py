@@ -94,3 +94,35 @@ def test_swarm_variable_at_coordinates_takes_nearest_particle(gpu):
     d2 = ((pts[:, None, :] - swarm.data[None, :, :]) ** 2).sum(-1)
     np.testing.assert_array_equal(index_var.evaluate(pts)[:, 0], np.argmin(d2, axis=1))
     np.testing.assert_array_equal(index_var.evaluate(swarm)[:, 0], np.arange(5))
+
+
+def test_swarm_variable_types_evaluate_and_checkpoint(gpu, tmp_path):
+    """docs/test/swarmvariable_types.ipynb: variables of every type hold their
+    type's largest value, evaluate to it at (0.5, 0.5) (nearest particle), and
+    survive a save / load onto a new swarm."""
+    import underworld2_gb300 as uw
+    mesh = uw.mesh.FeMesh_Cartesian()
+
+    def addvars(sw):
+        return ((sw.add_variable("char", 1), np.iinfo(np.int8).max), (sw.add_variable("short", 1), np.iinfo(np.int16).max),
+                (sw.add_variable("int", 1), np.iinfo(np.int32).max), (sw.add_variable("long", 1), np.iinfo(np.int64).max),
+                (sw.add_variable("float", 1), np.finfo(np.float32).max),
+                (sw.add_variable("double", 1), np.finfo(np.float64).max))
+
+    swarm = uw.swarm.Swarm(mesh)
+    vars1 = addvars(swarm)
+    swarm.populate_using_layout(uw.swarm.layouts.PerCellSpaceFillerLayout(swarm, 20))
+    for v, mx in vars1:
+        v.data[:] = mx
+    for v, mx in vars1:
+        res = v.evaluate((0.5, 0.5))
+        assert res.dtype == v.data.dtype and res.tolist() == [[mx]]
+    swarm.save(str(tmp_path / "swarm.h5"))
+    for i, (v, _) in enumerate(vars1):
+        v.save(str(tmp_path / ("var%d.h5" % i)))
+    swarm2 = uw.swarm.Swarm(mesh)
+    vars2 = addvars(swarm2)
+    swarm2.load(str(tmp_path / "swarm.h5"))
+    for i, (v, mx) in enumerate(vars2):
+        v.load(str(tmp_path / ("var%d.h5" % i)))
+        assert np.all(v.data == mx)

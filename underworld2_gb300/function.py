@@ -223,7 +223,14 @@ class _SwarmVar(Function):
         # integer swarm variables evaluate to integers (the reference's IO_int output)
         self._int = getattr(var, "dataType", "double") in ("int", "char", "short", "long")
 
+    def _check_swarm(self, ctx):
+        other = getattr(ctx, "swarm", None)
+        if other is not None and other is not self.var.swarm:
+            raise ValueError("'ParticleCoordinate' input and `SwarmVariableFn` function appear to be based on "
+                             "different swarms.")
+
     def _eval(self, ctx):
+        self._check_swarm(ctx)
         d = self.var._device_data()
         if d.dim() == 1:
             d = d[:, None]
@@ -231,6 +238,20 @@ class _SwarmVar(Function):
         if pid.numel() and bool((pid < 0).any()):
             pid = _closest_particles(self.var.swarm, ctx.coords, pid)
         return d[pid].double()
+
+    def evaluate(self, inputData=None, inputType=None):
+        """The variable's own values, in its own type (the reference's IO_char ...
+        IO_double outputs): at a swarm's particles, or the nearest particle's at
+        coordinates or a mesh's nodes."""
+        ctx = _input_context(inputData)
+        self._check_swarm(ctx)
+        data = self.var._data
+        if ctx.n == 0:
+            return np.zeros((0, data.shape[1]), dtype=data.dtype)
+        pid = ctx.pid.long()
+        if bool((pid < 0).any()):
+            pid = _closest_particles(self.var.swarm, ctx.coords, pid)
+        return np.array(data[pid.cpu().numpy()])
 
     def depends_on(self, kinds):
         return "swarm" in kinds
@@ -978,7 +999,9 @@ def _input_context(inputData):
     if hasattr(inputData, "particleCoordinates") and hasattr(inputData, "_x"):
         x = inputData._x if inputData._x is not None else torch.zeros((0, inputData.dim), dtype=torch.float64)
         dev = x.device
-        return EvalContext(torch.arange(x.shape[0], device=dev), lambda: x, dev)
+        ctx = EvalContext(torch.arange(x.shape[0], device=dev), lambda: x, dev)
+        ctx.swarm = inputData
+        return ctx
     if hasattr(inputData, "_axes") and hasattr(inputData, "elementRes"):
         pts = np.asarray(inputData.data, dtype=np.float64)
     elif inputData is None:
