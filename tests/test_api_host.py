@@ -41,3 +41,26 @@ def test_property_members():
     assert adv.dt == 0.0 and adv.time == 0.0
     adv.time = 2.5
     assert adv.time == 2.5
+
+
+def test_penalty_option_and_compressibility_warning(capsys):
+    """docs/test/solver_penalty_test.py: a penalty on a compressible system draws
+    the reference's warning at solve() (P/systems/_bsscr.py:320-321,359-365);
+    set_penalty switches the Schur preconditioner name as the reference does
+    (:766-780).  The warning comes before any device work, so the solve's own
+    failure on a machine without a GPU follows it."""
+    import pytest
+    import torch
+    m = uw.mesh.FeMesh_Cartesian("Q1/DQ0", (2, 2), (0.0, 0.0), (1.0, 1.0))
+    v = uw.mesh.MeshVariable(m, 2)
+    p = uw.mesh.MeshVariable(m.subMesh, 1)
+    solver = uw.systems.Solver(uw.systems.Stokes(v, p, 1.0, (0.0, 0.0), fn_one_on_lambda=1.0))
+    solver.set_penalty(1.0)
+    assert solver.options.main.penalty == 1.0 and solver.options.main.Q22_pc_type == "gkgdiag"
+    if not torch.cuda.is_available():
+        with pytest.warns(UserWarning) as w:
+            with pytest.raises(RuntimeError):
+                solver.solve()
+        assert str(w[0].message) == uw.systems.StokesSolver._warning_penalty_compressibility
+    solver.set_penalty(-1.0)
+    assert solver.options.main.penalty == 0.0 and "Invalid penalty" in capsys.readouterr().out

@@ -353,9 +353,23 @@ class StokesSolver:
     def set_mg_levels(self, levels):
         self.options.mg.levels = int(levels)
 
+    _warning_penalty_compressibility = "Stokes system appears to have set the `fn_one_on_lambda` parameter which " \
+        "is incompatible with the penalty method. If parameter is non-zero, erroneous results are likely to be " \
+        "generated."
+
     def set_penalty(self, penalty):
-        if penalty:
-            raise NotImplementedError("the augmented-Lagrangian penalty path is not part of the GPU solver")
+        """Augmented-Lagrangian penalty (P/systems/_bsscr.py:766-780).  The reference
+        adds penalty * G M^-1 G^T to K and penalty * G M^-1 h to f (M the diagonal of
+        the pressure mass; auglag-driver-DGTGD.c:151-200): for an incompressible system
+        that term vanishes at the solution, so it changes the Krylov path, not the
+        solution.  The GPU solver reaches that solution without the augmentation; the
+        option is recorded, and a compressible system draws the reference's warning."""
+        if isinstance(penalty, (int, float)) and penalty >= 0.0:
+            self.options.main.penalty = float(penalty)
+            self.options.main.Q22_pc_type = "gkgdiag"
+        else:
+            print("Invalid penalty number chosen. Penalty must be a positive float.")
+            self.options.main.penalty = 0.0
 
     def _check_linearity(self, nonLinearIterate):
         s = self._stokesSLE
@@ -378,6 +392,9 @@ class StokesSolver:
         if callback_post_solve is not None and not callable(callback_post_solve):
             raise RuntimeError("The 'callback_post_solve' parameter is not 'None' and isn't callable")
         nonlinear = self._check_linearity(nonLinearIterate) and bool(nonLinearIterate)
+        if self.options.main.penalty > 0.0 and self._stokesSLE._fn_one_on_lambda is not None:
+            import warnings
+            warnings.warn(self._warning_penalty_compressibility)
         its = nonLinearMaxIterations if nonlinear else 1
         prev = None
         self._picard = (0, 0.0)
