@@ -10,4 +10,4 @@ hand-written sm_103a CUDA kernels behind the C ABI in ``include/uwg.h``::
 """
 __version__ = "0.1.0"
 
-from . import conditions, function, mesh, swarm, systems, utils  # noqa: E402,F401
+from . import conditions, container, function, mesh, swarm, systems, utils  # noqa: E402,F401

@@ -1004,6 +1004,9 @@ def _input_context(inputData):
         return ctx
     if hasattr(inputData, "_axes") and hasattr(inputData, "elementRes"):
         pts = np.asarray(inputData.data, dtype=np.float64)
+    elif hasattr(inputData, "object") and hasattr(getattr(inputData, "object"), "_axes"):
+        # a mesh's vertex set: its vertices (FeMesh_IndexSet as a FunctionInput)
+        pts = np.asarray(inputData.object.data, dtype=np.float64)[inputData.data.astype(np.int64)]
     elif inputData is None:
         pts = np.zeros((1, 1))
     elif isinstance(inputData, numbers.Number):

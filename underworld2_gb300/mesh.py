@@ -7,6 +7,7 @@ node numbering x-fastest, element numbering x-fastest, node coordinates
 ``MeshVariable.data`` is a host numpy array; the library copies it to the
 device when a solve or an advection reads it and writes results back in place.
 """
+import copy
 import os
 import re
 
@@ -17,34 +18,30 @@ from . import _core
 from . import function as _fn
 from . import h5 as _h5
 from . import utils as _utils
+from . import container as _container
+from .container import ObjectifiedIndexSet
 
 
-class IndexSet:
-    """A set of node indices (``uw.container.IndexSet`` subset)."""
+class FeMesh_IndexSet(ObjectifiedIndexSet):
+    """Indices of a mesh's vertices (topologicalIndex 0), edges, faces or volumes,
+    tied to the mesh (P/mesh/_mesh.py:1228-1266); functions evaluate on it at
+    those vertices."""
 
-    def __init__(self, size, indices=()):
-        self.size = int(size)
-        self._set = np.unique(np.asarray(list(indices) if not isinstance(indices, np.ndarray) else indices,
-                                         dtype=np.int64))
+    def __init__(self, object, topologicalIndex=None, *args, **kwargs):
+        if topologicalIndex not in (0, 1, 2, 3):
+            raise ValueError("Topological index must be within [0,3].")
+        if not isinstance(object, FeMesh_Cartesian):
+            raise TypeError("'object' parameter must be of (sub)type 'FeMesh'.")
+        self._toplogicalIndex = topologicalIndex
+        super().__init__(object, *args, **kwargs)
 
     @property
-    def data(self):
-        return self._set.copy()
+    def topologicalIndex(self):
+        """0 vertex, 1 edge, 2 face, 3 volume."""
+        return self._toplogicalIndex
 
-    def __add__(self, other):
-        return IndexSet(max(self.size, other.size), np.union1d(self._set, other._set))
 
-    def __len__(self):
-        return len(self._set)
-
-    def __iter__(self):
-        return iter(self._set.tolist())
-
-    def __contains__(self, i):
-        return int(i) in set(self._set.tolist())
-
-    def __repr__(self):
-        return "IndexSet(%s)" % self._set.tolist()
+IndexSet = _container.IndexSet     # the plain container, kept under its earlier name here
 
 
 class FeMesh_Cartesian:
@@ -288,7 +285,9 @@ class _SubMesh:
 
 
 class _SpecialSets(dict):
-    """MinI/MaxI/MinJ/MaxJ(/MinK/MaxK) vertex sets and aliases (P/mesh/_mesh.py:1140-1158)."""
+    """MinI/MaxI/MinJ/MaxJ(/MinK/MaxK) vertex sets and aliases (P/mesh/_mesh.py:1140-1158).
+    Each lookup returns a new set, as the reference builds one per call, so that
+    editing a returned set leaves the mesh's own sets unchanged."""
 
     def __init__(self, mesh):
         super().__init__()
@@ -298,15 +297,18 @@ class _SpecialSets(dict):
                  ("MinJ_VertexSet", "Bottom_VertexSet", 1, 0), ("MaxJ_VertexSet", "Top_VertexSet", 1, 1)]
         if dim == 3:
             names += [("MinK_VertexSet", "Front_VertexSet", 2, 0), ("MaxK_VertexSet", "Back_VertexSet", 2, 1)]
-        allw = IndexSet(N)
+        allw = FeMesh_IndexSet(mesh, 0, N)
         for a, b, d, side in names:
             sel = np.where(ii[d] == (0 if side == 0 else nn[d] - 1))[0]
-            s = IndexSet(N, sel)
+            s = FeMesh_IndexSet(mesh, 0, N, sel)
             self[a] = s
             self[b] = s
             allw = allw + s
         self["AllWalls_VertexSet"] = allw
-        self["Empty"] = IndexSet(N)
+        self["Empty"] = FeMesh_IndexSet(mesh, 0, N)
+
+    def __getitem__(self, key):
+        return copy.deepcopy(dict.__getitem__(self, key))
 
 
 class MeshVariable:
