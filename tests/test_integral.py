@@ -52,3 +52,29 @@ def test_integral_argument_checks():
     inner = uw.mesh.IndexSet(m.nodesGlobal, [12])
     with pytest.raises(ValueError):
         uw.utils.Integral(1.0, mesh=m, integrationType="surface", surfaceIndexSet=inner)
+
+
+def test_gauss_integration_swarm():
+    """uw.swarm.GaussIntegrationSwarm (P/swarm/_integration_swarm.py:155-200): 3 points
+    per axis by default, 5 on Q2, 1..5 allowed; as an Integral's integrationSwarm
+    (with integrationType=None, as the reference's convergence notebook uses it)
+    its n-point rule integrates x^(2n-1) exactly and x^(2n) not."""
+    import pytest
+    m1 = uw.mesh.FeMesh_Cartesian("Q1/dQ0", (3, 2), (0.0, 0.0), (1.0, 1.0))
+    m2 = uw.mesh.FeMesh_Cartesian("Q2/dPc1", (3, 2), (0.0, 0.0), (1.0, 1.0))
+    assert uw.swarm.GaussIntegrationSwarm(m1).particleCount == 3
+    assert uw.swarm.GaussIntegrationSwarm(m2).particleCount == 5
+    assert uw.swarm.GaussIntegrationSwarm(m1, 2).particleLocalCount == 6 * 4
+    with pytest.raises(ValueError):
+        uw.swarm.GaussIntegrationSwarm(m1, 6)
+    with pytest.raises(ValueError):
+        uw.swarm.GaussIntegrationSwarm(m1, 2.0)
+    x = uw.function.input()[0]
+    for n in (1, 2, 3, 4, 5):
+        sw = uw.swarm.GaussIntegrationSwarm(m1, n)
+        odd = uw.utils.Integral(x ** (2 * n - 1), m1, integrationSwarm=sw, integrationType=None).evaluate()[0]
+        assert abs(odd - 1.0 / (2 * n)) < 1e-14
+        even = uw.utils.Integral(x ** (2 * n), m1, integrationSwarm=sw, integrationType=None).evaluate()[0]
+        assert abs(even - 1.0 / (2 * n + 1)) > 1e-13
+    with pytest.raises(RuntimeError):
+        uw.utils.Integral(1.0, m1, integrationSwarm=uw.swarm.GaussIntegrationSwarm(m1))

@@ -393,6 +393,31 @@ class Swarm:
         return self._voronoi
 
 
+class GaussIntegrationSwarm:
+    """Integration points at the tensor Gauss-Legendre points of every element
+    (P/swarm/_integration_swarm.py:155-200): particleCount points per axis,
+    3 by default (5 on Q2 meshes), from 1 to 5.  Systems and integrals that
+    take one integrate on those points."""
+
+    def __init__(self, mesh, particleCount=None, **kwargs):
+        if particleCount is None:
+            particleCount = 5 if mesh.elementType.upper().startswith("Q2") else 3
+        if not isinstance(particleCount, int) or isinstance(particleCount, bool):
+            raise ValueError("'particleCount' parameter must be of type 'int'.")
+        if particleCount not in (1, 2, 3, 4, 5):
+            raise ValueError("'particleCount' must take a value in [1,5].")
+        self.mesh = mesh
+        self._particleCount = particleCount
+
+    @property
+    def particleCount(self):
+        return self._particleCount
+
+    @property
+    def particleLocalCount(self):
+        return self.mesh.elementsGlobal * self._particleCount ** self.mesh.dim
+
+
 class VoronoiIntegrationSwarm:
     """Integration points coincident with the material particles, weighted by
     discrete Voronoi cells (P/swarm/_integration_swarm.py:118-145)."""

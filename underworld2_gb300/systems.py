@@ -50,6 +50,12 @@ class Stokes:
             if not isinstance(self._fn_source, _fn.Function):
                 raise ValueError("Provided 'fn_source' must be of, or convertible to, the 'Function' class.")
         self._swarm = voronoi_swarm
+        if gauss_swarm is not None:
+            if not isinstance(gauss_swarm, _swarm.GaussIntegrationSwarm):
+                raise RuntimeError("Provided 'gauss_swarm' must be a GaussIntegrationSwarm object")
+            if gauss_swarm.mesh is not self.mesh:
+                raise ValueError("Provided 'gauss_swarm' must live on the velocity field's mesh")
+        self._gauss_swarm = gauss_swarm
         if not isinstance(conditions, (list, tuple)):
             conditions = [conditions]
         for c in conditions:
@@ -129,7 +135,8 @@ class Stokes:
             return s._off, s._lst, vs.ip_xi, vs.ip_w, e
         # Gauss integration, one "particle" per point: the default GaussIntegrationSwarm
         # of the mesh, 3 points per axis on Q1 and 5 on Q2 (P/swarm/_integration_swarm.py:173-181)
-        ng = 5 if self.mesh.elementType.upper().startswith("Q2") else 3
+        ng = self._gauss_swarm.particleCount if self._gauss_swarm is not None else \
+            (5 if self.mesh.elementType.upper().startswith("Q2") else 3)
         x1, w1 = np.polynomial.legendre.leggauss(ng)
         dim = self.mesh.dim
         r = range(ng)
@@ -621,7 +628,12 @@ class AdvectionDiffusion:
             raise ValueError("The 'phiField' must be discretised on a Q1 mesh: advection-diffusion is provided "
                              "for Q1 elements only (allow_non_q1 is not supported on the GPU path)")
         if gauss_swarm is not None:
-            raise ValueError("the GPU path integrates on its own Gauss points (3 per axis for SUPG, 5 for SLCN)")
+            if not isinstance(gauss_swarm, _swarm.GaussIntegrationSwarm):
+                raise RuntimeError("Provided 'gauss_swarm' must be a GaussIntegrationSwarm object")
+            if gauss_swarm.particleCount != (3 if self.method == "SUPG" else 5):
+                raise NotImplementedError("the GPU %s kernels integrate on %d Gauss points per axis; a gauss_swarm "
+                                          "with %d is not supported" % (self.method, 3 if self.method == "SUPG" else 5,
+                                                                        gauss_swarm.particleCount))
         if self.method == "SUPG":
             self.system = _SUPG_AdvectionDiffusion(phiField, phiDotField, velocityField, fn_diffusivity,
                                                    fn_sourceTerm, conditions)

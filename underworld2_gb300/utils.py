@@ -34,8 +34,15 @@ class Integral:
         if integrationType and integrationSwarm:
             raise RuntimeError("Either an 'integrationType' or an 'integrationSwarm' may be provided, but not both.\n"
                                "You may need to set 'integrationType' to None.")
+        self._ng = None
         if integrationSwarm is not None:
-            raise NotImplementedError("user integration swarms are not supported; use 'integrationType'")
+            from .swarm import GaussIntegrationSwarm
+            if not isinstance(integrationSwarm, GaussIntegrationSwarm):
+                raise NotImplementedError("integration swarms other than GaussIntegrationSwarm are not supported")
+            if integrationSwarm.mesh is not mesh:
+                raise ValueError("The integration swarm must live on the provided mesh")
+            self._ng = integrationSwarm.particleCount
+            integrationType = "volume"
         if not isinstance(integrationType, str):
             raise TypeError("'integrationType' provided must be a string.")
         integrationType = integrationType.lower()
@@ -85,7 +92,7 @@ class Integral:
         from .mesh import _border_points, _volume_points
         dev = torch.device("cuda") if torch.cuda.is_available() else torch.device("cpu")
         m = self._mesh
-        ng = 3 if m._order == 1 else 5
+        ng = self._ng or (3 if m._order == 1 else 5)
         if self._surface:
             xg, fac, _, _ = _border_points(m, self._node_on, ng)
             if len(xg) == 0:
