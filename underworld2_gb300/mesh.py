@@ -101,6 +101,16 @@ class FeMesh_Cartesian:
     def elementsLocal(self):
         return self.elementsGlobal
 
+    @property
+    def nodesDomain(self):
+        """Local plus shadow nodes (P/mesh/_mesh.py:373-380); one process holds them all."""
+        return self.nodesGlobal
+
+    @property
+    def elementsDomain(self):
+        """Local plus shadow elements (P/mesh/_mesh.py:391-405)."""
+        return self.elementsGlobal
+
     def add_variable(self, nodeDofCount, dataType="double", **kwargs):
         return MeshVariable(self, nodeDofCount, dataType)
 
