@@ -15,7 +15,8 @@ import subprocess
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-_REF = os.environ.get("UW_REFERENCE_TREE", "/root/reference")
+REFERENCE_TREE = os.environ.get("UW_REFERENCE_TREE", "/root/reference")
+_REF = REFERENCE_TREE
 _LIBUW = os.path.join(_REF, "src", "underworld", "libUnderworld")
 _FNSRC = os.path.join(_LIBUW, "Underworld", "Function", "src")
 _VELIC = os.path.join(_LIBUW, "Underworld", "SysTest", "AnalyticPlugins")

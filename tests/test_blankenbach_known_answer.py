@@ -25,12 +25,13 @@ import numpy as np
 import pytest
 
 import oracle
+from oracle.ref_analytic import REFERENCE_TREE
 from oracle import advdiff
 from tests import analytic_convergence as ac
 from tests import oracle_system as osys
 import underworld2_gb300 as uw
 
-INPUT = os.path.join(os.environ.get("UW_REFERENCE_TREE", "/root/reference"), "docs", "examples", "input",
+INPUT = os.path.join(REFERENCE_TREE, "docs", "examples", "input",
                      "03_BlankenbachBenchmark")
 
 pytestmark = pytest.mark.skipif(not os.path.isdir(INPUT), reason="reference tree not present")

@@ -9,6 +9,7 @@ import xml.etree.ElementTree as ET
 import numpy as np
 import pytest
 
+from oracle.ref_analytic import REFERENCE_TREE
 from underworld2_gb300 import h5
 
 
@@ -272,7 +273,7 @@ def test_h5_reader_continuation_and_vlen_strings():
     assert name_out == "elementType" and value == "Q2"
 
 
-_REF_INPUT = os.path.join(os.environ.get("UW_REFERENCE_TREE", "/root/reference"), "docs", "examples", "input")
+_REF_INPUT = os.path.join(REFERENCE_TREE, "docs", "examples", "input")
 
 
 @pytest.mark.skipif(not os.path.isdir(_REF_INPUT), reason="reference tree not present")
