@@ -101,3 +101,13 @@ def test_exceptions():
         fn.exception.CustomException(one, (one > 2.)).evaluate()
     with pytest.raises(RuntimeError):
         fn.exception.CustomException(one, (one * 5. > 20.), one * 5.).evaluate()
+
+
+def test_conditional_integral_of_unit_disc():
+    """P/function/branching.py:189-197: the indicator of the unit disc,
+    integrated over [-1, 1]^2 on 16 x 16 Q1 elements, is pi within 1e-2."""
+    import underworld2_gb300 as uw
+    mesh = uw.mesh.FeMesh_Cartesian(elementRes=(16, 16), minCoord=(-1.0, -1.0), maxCoord=(1.0, 1.0))
+    circleFn = fn.coord()[0] ** 2 + fn.coord()[1] ** 2
+    fn_conditional = fn.branching.conditional([(circleFn < 1.0, 1.0), (True, 0.0)])
+    assert np.allclose(np.pi, uw.utils.Integral(fn_conditional, mesh).evaluate(), rtol=1e-2)

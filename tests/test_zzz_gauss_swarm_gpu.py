@@ -126,3 +126,23 @@ def test_swarm_variable_types_evaluate_and_checkpoint(gpu, tmp_path):
     for i, (v, mx) in enumerate(vars2):
         v.load(str(tmp_path / ("var%d.h5" % i)))
         assert np.all(v.data == mx)
+
+
+def test_integral_of_swarm_variable_map():
+    """P/function/branching.py:72-100: a swarm variable marking the particles in
+    the unit circle, mapped to 1 (and with a default), integrates to pi within 2 %
+    over [-1, 1]^2 (8 x 8 Q1, 20 space-filler particles per cell): the Gauss
+    points read their elements' nearest particles."""
+    import underworld2_gb300 as uw
+    fn = uw.function
+    mesh = uw.mesh.FeMesh_Cartesian(elementRes=(8, 8), minCoord=(-1.0, -1.0), maxCoord=(1.0, 1.0))
+    swarm = uw.swarm.Swarm(mesh)
+    svar = swarm.add_variable("int", 1)
+    swarm.populate_using_layout(uw.swarm.layouts.PerCellSpaceFillerLayout(swarm, 20))
+    svar.data[:] = 0
+    xy = swarm.particleCoordinates.data
+    svar.data[(xy ** 2).sum(1) < 1.0, 0] = 1
+    fn_map = fn.branching.map(fn_key=svar, mapping={0: 0.0, 1: 1.0})
+    assert np.allclose(np.pi, uw.utils.Integral(fn_map, mesh).evaluate(), rtol=2e-2)
+    fn_map = fn.branching.map(fn_key=svar, mapping={1: 1.0}, fn_default=0.0)
+    assert np.allclose(np.pi, uw.utils.Integral(fn_map, mesh).evaluate(), rtol=2e-2)

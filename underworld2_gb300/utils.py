@@ -74,17 +74,49 @@ class Integral:
         f = _fn.Function.convert(fn)
         if not isinstance(f, _fn.Function):
             raise TypeError("'fn' must be of or convertible to 'Function' class.")
-        if f.depends_on({"swarm"}):
-            raise ValueError("Gauss-point integration cannot evaluate swarm variables")
         self._fn = f
 
-    def _eval(self, pts, wts, dev):
+    def _eval(self, pts, wts, dev, pid=None):
         import torch
         from . import function as _fn
         xt = torch.from_numpy(pts).to(dev)
-        ectx = _fn.EvalContext(torch.full((xt.shape[0],), -1, dtype=torch.int64, device=dev), lambda: xt, dev)
+        if pid is None:
+            pid = torch.full((xt.shape[0],), -1, dtype=torch.int64, device=dev)
+        ectx = _fn.EvalContext(pid, lambda: xt, dev)
         v = self._fn.evaluate_at(ectx).to(torch.float64)
         return (v * torch.from_numpy(wts).to(dev)[:, None]).sum(0)
+
+    def _gauss_particles(self, ng):
+        """For swarm-variable integrands: the particle each Gauss point reads, the
+        nearest of its element (GeneralSwarm_IntegrationPointMap,
+        L/PICellerator/MaterialPoints/src/GeneralSwarm.cpp:319-431), element-major."""
+        import numpy as np
+        import torch
+        from .systems import _swarms_in
+        swarms = _swarms_in(self._fn)
+        if not swarms:
+            return None
+        if self._surface:
+            raise NotImplementedError("surface integrals of swarm variables are not supported")
+        if len(swarms) > 1:
+            raise NotImplementedError("swarm variables of more than one swarm in one integrand")
+        sw = swarms[0]
+        if sw.mesh is not self._mesh:
+            raise ValueError("the integrand's swarm lives on another mesh")
+        if sw._x is None or sw._off is None:
+            raise RuntimeError("Error occurred while trying to evaluate swarm variable. This can occur when there "
+                               "are no particles found in a given element.")
+        x1, _ = np.polynomial.legendre.leggauss(ng)
+        dim = self._mesh.dim
+        q = np.arange(ng ** dim)
+        xi = np.stack([x1[q % ng], x1[(q // ng) % ng]] + ([x1[q // (ng * ng)]] if dim == 3 else []), 1)
+        ctx = self._mesh.ctx
+        pid = ctx.gauss_nearest(torch.from_numpy(xi), sw._off, sw._lst, sw._x)
+        if bool((pid < 0).any()):
+            raise RuntimeError("Error occurred while trying to evaluate swarm variable. This can occur when there "
+                               "are no particles found in a given element. You may wish to add population "
+                               "control mechanisms.")
+        return pid.long()
 
     def evaluate(self):
         import numpy as np
@@ -98,12 +130,16 @@ class Integral:
             if len(xg) == 0:
                 return np.zeros(1)
             return self._eval(xg, fac, dev).cpu().numpy()
+        pid = self._gauss_particles(ng)
+        if pid is not None:
+            dev = pid.device
+        nq = ng ** m.dim
         total = None
-        step = max(1, (1 << 22) // ng ** m.dim)
+        step = max(1, (1 << 22) // nq)
         for first in range(0, m.elementsGlobal, step):
             cnt = min(step, m.elementsGlobal - first)
             pts, wts = _volume_points(m, ng, first, cnt)
-            part = self._eval(pts, wts, dev)
+            part = self._eval(pts, wts, dev, None if pid is None else pid[first * nq:(first + cnt) * nq])
             total = part if total is None else total + part
         return total.cpu().numpy()
 
