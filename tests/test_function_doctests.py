@@ -111,3 +111,34 @@ def test_conditional_integral_of_unit_disc():
     circleFn = fn.coord()[0] ** 2 + fn.coord()[1] ** 2
     fn_conditional = fn.branching.conditional([(circleFn < 1.0, 1.0), (True, 0.0)])
     assert np.allclose(np.pi, uw.utils.Integral(fn_conditional, mesh).evaluate(), rtol=1e-2)
+
+
+def test_view_min_max():
+    """P/function/view.py:52-121: min_max records the extremes over every
+    evaluation; a non-scalar function needs fn_norm; fn_auxiliary is recorded
+    at the extremes (P/function/view.py:150-245)."""
+    fn_simple = fn.input()[0] * 2.0
+    mm = fn.view.min_max(fn_simple)
+    assert mm.evaluate(5.0).tolist() == [[10.0]] and mm.min_global() == 10.0 and mm.max_global() == 10.0
+    assert mm.evaluate(-3.0).tolist() == [[-6.0]] and mm.min_global() == -6.0 and mm.max_global() == 10.0
+    assert fn_simple.evaluate(3000.0).tolist() == [[6000.0]] and mm.max_global() == 10.0
+    fn_vec = fn.input() * (1.0, 1.0)
+    with pytest.raises(RuntimeError, match="does not return scalar results"):
+        fn.view.min_max(fn_vec).evaluate(2.0)
+    vm = fn.view.min_max(fn_vec, fn_norm=fn.math.dot(fn_vec, fn_vec))
+    assert vm.evaluate(2.0).tolist() == [[2.0, 2.0]] and vm.max_global() == 8.0
+    assert vm.evaluate(-1.0).tolist() == [[-1.0, -1.0]] and vm.min_global() == 2.0 and vm.max_global() == 8.0
+    pts = np.array([[0.3, 0.1], [-0.2, 0.5], [0.05, 0.9], [0.7, -0.4]])
+    am = fn.view.min_max(fn.math.abs(fn.input()[0]), fn_auxiliary=fn.input())
+    am.evaluate(pts)
+    np.testing.assert_array_equal(am.min_global_auxiliary(), [[0.05, 0.9]])
+    np.testing.assert_array_equal(am.max_global_auxiliary(), [[0.7, -0.4]])
+    am.reset()
+    assert am.min_global() == float("inf") and am.min_global_auxiliary() is None
+
+
+def test_polygon_shape():
+    """P/function/shape.py:50-64: points inside a triangle."""
+    polyfn = fn.shape.Polygon(np.array([(0.0, 0.0), (0.5, 1.0), (1.0, 0.0)]))
+    res = polyfn.evaluate(np.array([(0.0, 0.9), (0.5, 0.5), (0.9, 0.2)]))
+    assert res.dtype == bool and res.tolist() == [[False], [True], [False]]

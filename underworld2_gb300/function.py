@@ -596,31 +596,60 @@ class rheology:
 
 
 class _MinMax(Function):
+    """Pass-through that records the extremes of its (scalar) function, or of
+    ``fn_norm`` for a non-scalar one, and the value of ``fn_auxiliary`` where they
+    occur (P/function/view.py:16-245): the first point that strictly improves
+    the record wins."""
+
     def __init__(self, fn, fn_norm=None, fn_auxiliary=None):
         self.a = Function.convert(fn)
         self.norm = Function.convert(fn_norm) if fn_norm is not None else None
+        self.aux = Function.convert(fn_auxiliary) if fn_auxiliary is not None else None
         self.reset()
 
     def _children(self):
-        return [self.a] + ([self.norm] if self.norm is not None else [])
+        return [self.a] + [f for f in (self.norm, self.aux) if f is not None]
 
     def reset(self):
         self._min, self._max = float("inf"), float("-inf")
+        self._min_aux = self._max_aux = None
 
     def _eval(self, ctx):
         v = self.a.evaluate_at(ctx)
-        q = self.norm.evaluate_at(ctx) if self.norm is not None else v
-        if q.shape[1] != 1:
-            q = torch.sqrt((q * q).sum(dim=1, keepdim=True))
+        if self.norm is not None:
+            q = self.norm.evaluate_at(ctx)
+            if q.shape[1] != 1:
+                raise RuntimeError("Norm function does not return scalar results.")
+        else:
+            if v.shape[1] != 1:
+                raise RuntimeError("Argument function does not return scalar results. You must also provide a "
+                                   "function which calculates the required norm like quantity via the `fn_norm` "
+                                   "parameter.")
+            q = v
         if q.shape[0]:
-            self._min = min(self._min, float(q.min()))
-            self._max = max(self._max, float(q.max()))
+            qv = q[:, 0]
+            i_min, i_max = int(torch.argmin(qv)), int(torch.argmax(qv))
+            lo, hi = float(qv[i_min]), float(qv[i_max])
+            aux = self.aux.evaluate_at(ctx) if self.aux is not None else None
+            if lo < self._min:
+                self._min = lo
+                if aux is not None:
+                    self._min_aux = aux[i_min:i_min + 1].cpu().numpy().copy()
+            if hi > self._max:
+                self._max = hi
+                if aux is not None:
+                    self._max_aux = aux[i_max:i_max + 1].cpu().numpy().copy()
         return v
 
     def min_local(self): return self._min
     def max_local(self): return self._max
     def min_global(self): return self._min
     def max_global(self): return self._max
+
+    def min_local_auxiliary(self): return self._min_aux
+    def max_local_auxiliary(self): return self._max_aux
+    def min_global_auxiliary(self): return self._min_aux
+    def max_global_auxiliary(self): return self._max_aux
 
 
 class _Count(Function):
