@@ -142,3 +142,23 @@ def test_polygon_shape():
     polyfn = fn.shape.Polygon(np.array([(0.0, 0.0), (0.5, 1.0), (1.0, 0.0)]))
     res = polyfn.evaluate(np.array([(0.0, 0.9), (0.5, 0.5), (0.9, 0.2)]))
     assert res.dtype == bool and res.tolist() == [[False], [True], [False]]
+
+
+def test_convert_identity_integrate_and_vector_input():
+    """P/function/_function.py:209-226, 793-799, 841-853: convert is the identity on
+    a Function and passes None; Function.integrate over a mesh; a unary math
+    function applies per component of a vector input; empty inputs give empty
+    results."""
+    import math as sysmath
+    import underworld2_gb300 as uw
+    fn_const = fn.Function.convert(3)
+    assert fn_const is fn.Function.convert(fn_const) and fn.Function.convert(None) is None
+    mesh = uw.mesh.FeMesh_Cartesian(minCoord=(0.0, 0.0), maxCoord=(1.0, 2.0))
+    assert np.allclose(fn.misc.constant(2.0).integrate(mesh)[0], 4)
+    assert np.allclose((fn.misc.constant(2.0) * (0.5, 1.0)).integrate(mesh), [2, 4])
+    sinfn = fn.math.sin()
+    assert np.allclose(sinfn.evaluate(sysmath.pi / 4.0), [[0.5 * sysmath.sqrt(2.0)]])
+    assert np.allclose(sinfn.evaluate((0.0, sysmath.pi / 4.0, 2.0 * sysmath.pi)), [[0.0, 0.5 * sysmath.sqrt(2.0), 0.0]])
+    var = uw.mesh.MeshVariable(uw.mesh.FeMesh_Cartesian(), 1)
+    assert var.evaluate(np.zeros((0, 2))).shape == (0, 1)
+    assert var.evaluate(var.mesh.specialSets["Empty"]).shape == (0, 1)

@@ -101,6 +101,11 @@ class Function:
         v = self.evaluate_at(ctx).cpu().numpy()
         return v != 0 if self._bool else np.array(v, dtype=dt)
 
+    def integrate(self, mesh):
+        """Volume integral over the mesh (P/function/_function.py:775-800)."""
+        from .utils import Integral
+        return Integral(self, mesh).evaluate()
+
     # arithmetic
     def __add__(self, o): return _Bin(torch.add, self, Function.convert(o))
     def __radd__(self, o): return _Bin(torch.add, Function.convert(o), self)
