@@ -301,3 +301,10 @@ def _swarmvar(saved_var, varname):
             raise RuntimeError("Can't find 'data' in file '%s'." % saved_var.filename)
         count = f["data"].shape[0]
     return _attribute(varname, _number_type(var.data.dtype), "Node", count, var.data.shape[1], ref)
+
+
+def _nps_2norm(v, comm=None):
+    """2-norm of a numpy vector (P/utils/_utils.py:645-672); one process holds it all."""
+    import numpy as np
+    v = np.asarray(v, dtype=np.float64)
+    return float(np.sqrt(np.sum(v * v)))
