@@ -28,7 +28,12 @@ import torch
 
 class EvalContext:
     """Where to evaluate: integration points with their particle ids and
-    global coordinates (coords computed on demand)."""
+    global coordinates (coords computed on demand).  ``swarm`` is set when the
+    points are a swarm's own particles; ``map_swarm`` when they are integration
+    points whose particle ids come from that swarm's integration-point map."""
+
+    swarm = None
+    map_swarm = None
 
     def __init__(self, particle_ids, coords_fn, device, lib_ctx=None, pid32=None):
         self.pid = particle_ids
@@ -284,6 +289,31 @@ def _closest_particles(swarm, pts, pid, chunk_elems=1 << 24):
         d2 = ((q[:, None, :] - x[None, :, :]) ** 2).sum(-1)
         pid[idx] = torch.argmin(d2, dim=1)
     return pid
+
+
+class _ParticleFound(Function):
+    """True where a particle of `swarm` serves the point (ParticleFound,
+    L/Underworld/Function/src/ParticleFound.cpp:26-95): at the swarm's own
+    particles; at integration points, when the point's element holds one of the
+    swarm's particles (the point's particle map found one); False at plain
+    coordinates."""
+    _bool = True
+
+    def __init__(self, swarm):
+        self.swarm = swarm
+
+    def _eval(self, ctx):
+        n = ctx.n
+        if getattr(ctx, "swarm", None) is not None:
+            v = torch.full((n, 1), 1.0 if ctx.swarm is self.swarm else 0.0, dtype=torch.float64, device=ctx.device)
+        elif getattr(ctx, "map_swarm", None) is self.swarm:
+            v = (ctx.pid >= 0).to(torch.float64)[:, None]
+        else:
+            v = torch.zeros((n, 1), dtype=torch.float64, device=ctx.device)
+        return v
+
+    def depends_on(self, kinds):
+        return "swarm" in kinds
 
 
 class _MeshVar(Function):
@@ -960,6 +990,8 @@ class _Program:
         if isinstance(f, _MeshVar):
             return self.input(f._eval(self.ctx), False)      # sampled by the interpolation kernel
         if isinstance(f, _MeshGrad):
+            return self.input(f._eval(self.ctx), False)
+        if isinstance(f, _ParticleFound):
             return self.input(f._eval(self.ctx), False)
         if isinstance(f, _Map):
             key = self.node(f.key)[0]

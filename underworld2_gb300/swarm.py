@@ -230,6 +230,13 @@ class Swarm:
         view.flags.writeable = self._writable
         return view
 
+    def fn_particle_found(self):
+        """A boolean Function: True where one of this swarm's particles serves
+        the point (P/swarm/_swarm.py:419-475)."""
+        if not hasattr(self, "_fn_particle_found"):
+            self._fn_particle_found = _fn._ParticleFound(self)
+        return self._fn_particle_found
+
     def add_variable(self, dataType, count):
         v = SwarmVariable(self, dataType, count)
         self._variables.append(v)

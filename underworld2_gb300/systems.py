@@ -132,6 +132,7 @@ class Stokes:
             n = int(s._off[-1])
             e = _fn.EvalContext(s._lst[:n].long(), vs.global_coords, ctx.device, lib_ctx=ctx,
                                 pid32=s._lst[:n].to(torch.int32).contiguous())
+            e.map_swarm = s
             return s._off, s._lst, vs.ip_xi, vs.ip_w, e
         # Gauss integration, one "particle" per point: the default GaussIntegrationSwarm
         # of the mesh, 3 points per axis on Q1 and 5 on Q2 (P/swarm/_integration_swarm.py:173-181)
@@ -178,12 +179,14 @@ class Stokes:
             raise RuntimeError("Error occurred while trying to evaluate swarm variable. This can occur when there "
                                "are no particles found in a given element.")
         pid = ctx.gauss_nearest(torch.from_numpy(xi), sw._off, sw._lst, sw._x)
-        if bool((pid < 0).any()):
+        if bool((pid < 0).any()) and _swarms_in(self._fn_viscosity, self._fn_bodyforce, self._fn_one_on_lambda,
+                                                 self._fn_source, variables_only=True):
             raise RuntimeError("Error occurred while trying to evaluate swarm variable. This can occur when there "
                                "are no particles found in a given element. You may wish to add population "
                                "control mechanisms.")
         e = _fn.EvalContext(pid.long(), coords, ctx.device, lib_ctx=ctx, pid32=pid)
         e.point_order = True          # rows are the Gauss points; pid only indexes the swarm's data
+        e.map_swarm = sw
         return off, lst, ip_xi, ip_w, e
 
     def _per_particle(self, f, ectx, npart, ncomp):
@@ -504,8 +507,9 @@ def _uses_swarm(f):
     return any(_uses_swarm(c) for c in f._children())
 
 
-def _swarms_in(*fns):
-    """The swarms whose variables the function graphs read."""
+def _swarms_in(*fns, variables_only=False):
+    """The swarms whose variables (and, unless variables_only, particle-found
+    tests) the function graphs read."""
     found, seen = {}, set()
     stack = [f for f in fns if f is not None]
     while stack:
@@ -515,6 +519,8 @@ def _swarms_in(*fns):
         seen.add(id(f))
         if isinstance(f, _fn._SwarmVar):
             found[id(f.var.swarm)] = f.var.swarm
+        elif isinstance(f, _fn._ParticleFound) and not variables_only:
+            found[id(f.swarm)] = f.swarm
         stack.extend(c for c in f._children() if c is not None)
     return list(found.values())
 

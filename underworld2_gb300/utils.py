@@ -80,9 +80,12 @@ class Integral:
         import torch
         from . import function as _fn
         xt = torch.from_numpy(pts).to(dev)
+        mapped = pid is not None
         if pid is None:
             pid = torch.full((xt.shape[0],), -1, dtype=torch.int64, device=dev)
         ectx = _fn.EvalContext(pid, lambda: xt, dev)
+        if mapped:
+            ectx.map_swarm = self._map_swarm
         v = self._fn.evaluate_at(ectx).to(torch.float64)
         return (v * torch.from_numpy(wts).to(dev)[:, None]).sum(0)
 
@@ -112,10 +115,11 @@ class Integral:
         xi = np.stack([x1[q % ng], x1[(q // ng) % ng]] + ([x1[q // (ng * ng)]] if dim == 3 else []), 1)
         ctx = self._mesh.ctx
         pid = ctx.gauss_nearest(torch.from_numpy(xi), sw._off, sw._lst, sw._x)
-        if bool((pid < 0).any()):
+        if bool((pid < 0).any()) and _swarms_in(self._fn, variables_only=True):
             raise RuntimeError("Error occurred while trying to evaluate swarm variable. This can occur when there "
                                "are no particles found in a given element. You may wish to add population "
                                "control mechanisms.")
+        self._map_swarm = sw
         return pid.long()
 
     def evaluate(self):
