@@ -88,9 +88,9 @@ def test_scatter_into_particle_order(gpu):
 def test_errors_match_the_tensor_path(gpu):
     fn, ctx, mat, T, T32, _ = _setup()
     nodef = fn.branching.map(fn_key=mat, mapping={0: 1.0, 1: 2.0})   # key 2 occurs, no default
-    with pytest.raises(ValueError):
+    with pytest.raises(RuntimeError, match="map"):
         fn._eval_kernel(nodef, ctx)
-    with pytest.raises(ValueError):
+    with pytest.raises(RuntimeError, match=r"key \(2\)"):
         nodef.evaluate_at(ctx)
     nocase = fn.branching.conditional([(fn.input()[0] < -1.0, 1.0)])
     with pytest.raises(RuntimeError):

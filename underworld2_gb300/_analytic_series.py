@@ -337,7 +337,7 @@ class SolA(_SeriesSolution):
         kx, kz = n_x * _PI, self.n_z * _PI
         self.modes = _ModeSet([_Mode(kx, [(0.0, 1.0, self.eta_0, 0.0)], fs_terms=_sin_terms(self.sigma_0, kz))], [1.0])
         x, z = input()[0], input()[1]
-        self.fn_viscosity = constant(self.eta_0)
+        self.fn_viscosity = constant(float(self.eta_0))
         self.fn_bodyforce = Function.convert((0.0, self.sigma_0 * _fmath.cos(kx * x) * _fmath.sin(kz * z)))
         self._finish()
 
@@ -361,7 +361,7 @@ class SolB(_SeriesSolution):
         fs = [(self.sigma_0 / 2.0, kz), (-self.sigma_0 / 2.0, -kz)]
         self.modes = _ModeSet([_Mode(kx, [(0.0, 1.0, self.eta_0, 0.0)], fs_terms=fs)], [1.0])
         x, z = input()[0], input()[1]
-        self.fn_viscosity = constant(self.eta_0)
+        self.fn_viscosity = constant(float(self.eta_0))
         self.fn_bodyforce = Function.convert((0.0, self.sigma_0 * _fmath.cos(kx * x) * _fmath.sinh(kz * z)))
         self._finish()
 
@@ -466,7 +466,7 @@ class SolC(_SeriesSolution):
         self._F0 = -self.sigma_0 * x_c
         self._p0 = 0.5
         x = input()[0]
-        self.fn_viscosity = constant(eta_0)
+        self.fn_viscosity = constant(float(eta_0))
         self.fn_bodyforce = Function.convert((0.0, _branching.conditional(((x < x_c, -self.sigma_0), (True, 0.0)))))
         self._finish()
 
@@ -550,7 +550,7 @@ class SolH(_SeriesSolution):
         self._F0 = -sigma_0 * x_c * y_c
         self._p0 = 0.5
         x, y = input()[0], input()[1]
-        self.fn_viscosity = constant(eta_0)
+        self.fn_viscosity = constant(float(eta_0))
         self.fn_bodyforce = Function.convert(
             (0.0, 0.0, _branching.conditional((((x <= x_c) & (y <= y_c), -sigma_0), (True, 0.0)))))
         self._finish()

@@ -69,10 +69,18 @@ class Function:
             return obj
         if isinstance(obj, numbers.Number):
             return constant(obj)
+        if isinstance(obj, np.generic):
+            return Function.convert(obj.item())
+        if isinstance(obj, np.ndarray):
+            return Function.convert(obj.tolist())
         if isinstance(obj, (tuple, list)):
             parts = [Function.convert(o) for o in obj]
-            if all(isinstance(p, constant) for p in parts):
-                return constant([p.value for p in parts])
+            if all(isinstance(p, constant) and p._sig[1] == 1 for p in parts):
+                tags = {p._sig[0] for p in parts}
+                if len(tags) == 1:
+                    return constant([p.value for p in parts])
+                if "bool" not in tags:      # ints and floats together: a float vector
+                    return constant([float(p.value) for p in parts])
             return _Vector(parts)
         if hasattr(obj, "_as_function"):
             return obj._as_function()
@@ -134,16 +142,68 @@ class Function:
         return _Index(self, i)
 
 
+def _const_tag(v):
+    if isinstance(v, (bool, np.bool_)):
+        return "bool"
+    if isinstance(v, numbers.Integral):
+        return "int"
+    if isinstance(v, numbers.Real):
+        return "double"
+    return None
+
+
+def _const_signature(value):
+    """(type, size) of a constant's value: a bool, int or float, or a non-empty
+    iterable of one of those types (P/function/misc.py:73-126)."""
+    tag = _const_tag(value)
+    if tag is not None:
+        return tag, 1
+    try:
+        items = tuple(iter(value))
+    except TypeError:
+        raise ValueError("'value' object provided to Constant Function constructor does not appear to be valid. "
+                         "Only python types 'int', 'float' and 'bool' are acceptable, or iterable objects "
+                         "homogeneous in these types. Provided object was of type '{}'."
+                         .format(type(value).__name__))
+    if not items:
+        raise ValueError("'value' object provided to Constant function appears to be an iterable, but seems to be "
+                         "of zero size. Iterable values must be of non-zero size.")
+    tag = _const_tag(items[0])
+    if tag is None:
+        raise ValueError("'value' object provided to Constant function appears to be an iterable, but does not "
+                         "appear to contain objects of python type 'int', 'float' or 'bool'.")
+    if any(_const_tag(v) != tag for v in items[1:]):
+        raise ValueError("'value' object provided to Constant function appears to be an iterable, but does not "
+                         "appear to be homogeneous in type. Objects in iterable must all be of python type 'int', "
+                         "'float' or 'bool'.")
+    return tag, len(items)
+
+
 class constant(Function):
+    """A constant value (P/function/misc.py:13-126).  The value keeps its type:
+    bools evaluate to bool, ints to int32, floats to float64; `value` may be
+    reset to another value of the same type and size."""
+
     def __init__(self, value):
-        self.value = value
-        # the reference keeps a constant's type: bools evaluate to bool, ints to int32
-        # (P/function/misc.py:13-67, P/function/_function.py:75-94)
-        flat = list(value) if isinstance(value, (tuple, list)) else [value]
-        if flat and all(isinstance(v, (bool, np.bool_)) for v in flat):
-            self._bool = True
-        elif flat and all(isinstance(v, (int, np.integer)) and not isinstance(v, (bool, np.bool_)) for v in flat):
-            self._int = True
+        self._sig = _const_signature(value)
+        self._value = value
+        self._bool = self._sig[0] == "bool"
+        self._int = self._sig[0] == "int"
+
+    @property
+    def value(self):
+        return self._value
+
+    @value.setter
+    def value(self, value):
+        tag, size = _const_signature(value)
+        if tag != self._sig[0]:
+            raise TypeError("'value' object passed in must be of identical type to that used in construction of "
+                            "this function.")
+        if size != self._sig[1]:
+            raise TypeError("'value' object passed in must be of identical size to that used in construction of "
+                            "this function.")
+        self._value = value
 
     def _eval(self, ctx):
         t = torch.as_tensor(self.value, dtype=torch.float64, device=ctx.device)
@@ -377,9 +437,24 @@ class math:
 
 
 class _Map(Function):
+    """branching.map (P/function/branching.py:102-140): keys are unsigned ints."""
+
     def __init__(self, fn_key, mapping, fn_default=None):
+        if not mapping:
+            raise ValueError("You must specify a mapping via the 'mapping' parameter.")
+        if not isinstance(mapping, dict):
+            raise TypeError("'mapping' object passed in must be of python type 'dict'")
+        if fn_key is None:
+            raise ValueError("You must specify a key function via the 'fn_key' parameter.")
         self.key = Function.convert(fn_key)
-        self.mapping = {int(k): Function.convert(v) for k, v in mapping.items()}
+        self.mapping = {}
+        for k, v in mapping.items():
+            if not isinstance(k, numbers.Integral) or isinstance(k, bool) or k < 0:
+                raise ValueError("Key '{}' not valid. Mapping keys must be unsigned integers.".format(k))
+            f = Function.convert(v)
+            if f is None:
+                raise ValueError("'None' is not valid for mapped functions.")
+            self.mapping[int(k)] = f
         self.default = Function.convert(fn_default)
 
     def _children(self):
@@ -401,13 +476,32 @@ class _Map(Function):
             v = self.default.evaluate_at(ctx)
             out[~hit] = v.expand(ctx.n, v.shape[1])[~hit]
         elif not bool(hit.all()):
-            raise ValueError("branching.map: a key has no mapping and no default is given")
+            k = int(key[~hit][0])
+            raise RuntimeError("Error evaluating 'map' function.\nKey function evaluates to key (%d) which\n"
+                               "does not appear to map to any functions, and no default function has been set." % k)
         return out
 
 
+_NO_CLAUSE = ("Reached end of conditional statement. At least one of the clause conditions must evaluate to "
+              "'True'.")
+_NO_KEY = ("Error evaluating 'map' function.\nKey function evaluates to a key which\n"
+           "does not appear to map to any functions, and no default function has been set.")
+
+
 class _Conditional(Function):
+    """branching.conditional (P/function/branching.py:143-230): the first clause
+    whose condition holds gives the value."""
+
     def __init__(self, clauses):
-        self.clauses = [(Function.convert(c), Function.convert(v)) for c, v in clauses]
+        if not isinstance(clauses, (list, tuple)):
+            raise TypeError("'clauses' object passed in must be of python type 'list' or 'tuple'")
+        self.clauses = []
+        for clause in clauses:
+            if not isinstance(clause, (list, tuple)):
+                raise TypeError("Clauses within the clause list must be of python type 'list' or 'tuple'")
+            if len(clause) != 2:
+                raise ValueError("Clauses tuples must be of length 2.")
+            self.clauses.append((Function.convert(clause[0]), Function.convert(clause[1])))
 
     def _children(self):
         return [f for cv in self.clauses for f in cv]
@@ -424,7 +518,7 @@ class _Conditional(Function):
             out[sel] = v.expand(ctx.n, v.shape[1])[sel]
             done |= sel
         if not bool(done.all()):
-            raise RuntimeError("branching.conditional: no clause evaluated true for some points")
+            raise RuntimeError(_NO_CLAUSE)
         return out
 
 
@@ -894,8 +988,8 @@ _UN_OPS = {torch.neg: "neg", torch.abs: "abs", torch.exp: "exp", torch.log: "log
            torch.erf: "erf", torch.erfc: "erfc"}
 _DTYPES = {torch.float64: 0, torch.float32: 1, torch.int32: 2, torch.int8: 3, torch.int16: 4, torch.int64: 5}
 # error-check codes of the program and the exceptions they raise on the host
-_CHECKS = {0: (ValueError, "branching.map: a key has no mapping and no default is given"),
-           1: (RuntimeError, "branching.conditional: no clause evaluated true for some points"),
+_CHECKS = {0: (RuntimeError, _NO_KEY),
+           1: (RuntimeError, _NO_CLAUSE),
            2: (RuntimeError, "Function evaluation produced a non-finite value (SafeMaths).")}
 
 
