@@ -84,7 +84,15 @@ class Function:
             return _Vector(parts)
         if hasattr(obj, "_as_function"):
             return obj._as_function()
-        raise TypeError("cannot convert %r to a Function" % (obj,))
+        try:
+            return constant(obj)
+        except ValueError as e:
+            # the reference converts through misc.constant and re-raises its error
+            # with this note prepended (P/function/_function.py:230-265)
+            raise ValueError("An exception was raised while try to convert an object to an Underworld2 function. "
+                             "Usually this occurs because you didn't pass in the correct object. Please check your "
+                             "function arguments! Note that only python types 'int', 'float' or 'bool' (and "
+                             "iterables of these types) are convertible to functions.\n\n" + str(e)) from None
 
     def _eval(self, ctx):
         raise NotImplementedError
