@@ -125,3 +125,21 @@ def test_numpy_values_convert():
     assert fn.Function.convert(np.array([1.0, 2.0])).evaluate(0.0).tolist() == [[1.0, 2.0]]
     assert fn.Function.convert(np.bool_(True)).evaluate(0.0).dtype == bool
     assert (fn.input()[0] * np.array((0.0, -1.0))).evaluate(2.0).tolist() == [[0.0, -2.0]]
+
+
+def test_exception_and_rheology_argument_checks():
+    """P/function/exception.py:57-60,131-145 and P/function/rheology.py:94-108:
+    missing functions are refused with ValueError."""
+    with pytest.raises(ValueError, match="'fn'"):
+        fn.exception.SafeMaths(None)
+    with pytest.raises(ValueError):
+        fn.exception.CustomException(None, True)
+    with pytest.raises(ValueError):
+        fn.exception.CustomException(1.0, None)
+    for args, name in (((None, 1.0, 1.0), "fn_stress"), ((1.0, None, 1.0), "fn_stresslimit"),
+                       ((1.0, 1.0, None), "fn_inputviscosity")):
+        with pytest.raises(ValueError, match=name):
+            fn.rheology.stress_limiting_viscosity(*args)
+    one = fn.misc.constant(1.0)
+    with pytest.raises(RuntimeError, match=r"\( 5 \)"):
+        fn.exception.CustomException(one, one * 5.0 > 20.0, one * 5.0).evaluate()

@@ -660,6 +660,8 @@ class shape:
 class _SafeMaths(Function):
     def __init__(self, fn):
         self.a = Function.convert(fn)
+        if not isinstance(self.a, Function):
+            raise ValueError("provided 'fn' must a 'Function' or convertible.")
         self._kind = self.a._kind
 
     def _children(self):
@@ -713,6 +715,9 @@ class exception:
 class _StressLimit(Function):
     def __init__(self, fn_stress, fn_stresslimit, fn_inputviscosity):
         self.s, self.lim, self.eta = (Function.convert(f) for f in (fn_stress, fn_stresslimit, fn_inputviscosity))
+        for f, name in ((self.s, "fn_stress"), (self.lim, "fn_stresslimit"), (self.eta, "fn_inputviscosity")):
+            if not isinstance(f, Function):
+                raise ValueError("Provided '%s' must a 'Function' or convertible type." % name)
 
     def _children(self):
         return [self.s, self.lim, self.eta]
