@@ -143,3 +143,31 @@ def test_exception_and_rheology_argument_checks():
     one = fn.misc.constant(1.0)
     with pytest.raises(RuntimeError, match=r"\( 5 \)"):
         fn.exception.CustomException(one, one * 5.0 > 20.0, one * 5.0).evaluate()
+
+
+def test_evaluate_global_single_process():
+    """P/function/_function.py:654-759 on one process: the root's result is the
+    plain evaluation; object inputs are refused."""
+    x = fn.input()
+    pts = np.array([[0.1, 0.2], [0.3, 0.4]])
+    np.testing.assert_array_equal((2.0 * x).evaluate_global(pts), (2.0 * x).evaluate(pts))
+    assert (x[0] + 1.0).evaluate_global(0.5).tolist() == [[1.5]]
+    mesh = uw.mesh.FeMesh_Cartesian(elementRes=(2, 2))
+    with pytest.raises(TypeError, match="not currently supported"):
+        x.evaluate_global(mesh)
+    with pytest.raises(TypeError, match="not currently supported"):
+        x.evaluate_global(mesh.specialSets["MinI_VertexSet"])
+
+
+def test_mesh_variable_outside_the_mesh():
+    """FeVariableFn.cpp:82-92: a mesh variable evaluated at a coordinate outside
+    its mesh raises ValueError naming the location (checked before any
+    interpolation, so this runs without a GPU)."""
+    mesh = uw.mesh.FeMesh_Cartesian(elementRes=(4, 4))
+    var = uw.mesh.MeshVariable(mesh, 1)
+    with pytest.raises(ValueError, match=r"location \(2, 0.5\) does not appear to be valid"):
+        var.evaluate((2.0, 0.5))
+    with pytest.raises(ValueError, match="outside local domain"):
+        (2.0 * var.fn_gradient[0]).evaluate(np.array([[0.5, 0.5], [0.5, -0.1]]))
+    with pytest.raises(RuntimeError, match="No results were found"):
+        var.evaluate_global(np.array([[1.5, 0.5], [-0.5, 0.5]]))

@@ -34,6 +34,7 @@ class EvalContext:
 
     swarm = None
     map_swarm = None
+    check_domain = False
 
     def __init__(self, particle_ids, coords_fn, device, lib_ctx=None, pid32=None):
         self.pid = particle_ids
@@ -121,6 +122,38 @@ class Function:
             return np.zeros((0, 1), dtype=dt)
         v = self.evaluate_at(ctx).cpu().numpy()
         return v != 0 if self._bool else np.array(v, dtype=dt)
+
+    def evaluate_global(self, inputData, inputType=None):
+        """Values at global coordinates, points outside the domain skipped
+        (P/function/_function.py:654-759).  One process holds the whole domain
+        here, so this process is the root and gets the [n, k] result; rows of
+        points that no evaluation found stay zero, and RuntimeError is raised
+        when none was found.  Mesh, swarm and index-set inputs are refused."""
+        from .container import ObjectifiedIndexSet
+        if hasattr(inputData, "particleCoordinates") or hasattr(inputData, "_axes") or \
+                isinstance(inputData, ObjectifiedIndexSet):
+            raise TypeError("This 'inputData' type is not currently supported for global function evaluation.")
+        if isinstance(inputData, np.ndarray):
+            pts = inputData
+        else:
+            pts = np.atleast_2d(np.asarray(inputData if not isinstance(inputData, float) else (inputData,),
+                                           dtype=np.float64))
+        try:
+            return self.evaluate(pts, inputType)
+        except ValueError:
+            pass                       # some point lies outside the domain: point by point
+        out = None
+        for i in range(len(pts)):
+            try:
+                v = self.evaluate(pts[i:i + 1], inputType)
+            except ValueError:
+                continue
+            if out is None:
+                out = np.zeros((len(pts), v.shape[1]), dtype=v.dtype)
+            out[i] = v[0]
+        if out is None:
+            raise RuntimeError("No results were found anywhere in the domain for provided input.")
+        return out
 
     def integrate(self, mesh):
         """Volume integral over the mesh (P/function/_function.py:775-800)."""
@@ -384,11 +417,30 @@ class _ParticleFound(Function):
         return "swarm" in kinds
 
 
+def _check_in_domain(var, ctx):
+    """At user-given coordinates, a mesh variable is defined only inside its
+    mesh: the reference raises for a point outside (FeVariableFn.cpp:82-92)."""
+    if not getattr(ctx, "check_domain", False):
+        return
+    m = var._primary()
+    x = ctx.coords
+    if x.shape[1] != m.dim:
+        return
+    lo = torch.tensor(m.minCoord, dtype=x.dtype, device=x.device)
+    hi = torch.tensor(m.maxCoord, dtype=x.dtype, device=x.device)
+    bad = ((x < lo) | (x > hi)).any(1)
+    if bool(bad.any()):
+        p = x[int(bad.nonzero()[0, 0])].tolist()
+        raise ValueError("FeVariable interpolation at location (%s) does not appear to be valid.\n"
+                         "Location is probably outside local domain." % ", ".join("%g" % v for v in p))
+
+
 class _MeshVar(Function):
     def __init__(self, var):
         self.var = var
 
     def _eval(self, ctx):
+        _check_in_domain(self.var, ctx)
         return self.var._interpolate(ctx.coords)
 
     def depends_on(self, kinds):
@@ -405,6 +457,7 @@ class _MeshGrad(Function):
         self._kind = "tensor" if var.nodeDofCount > 1 else None
 
     def _eval(self, ctx):
+        _check_in_domain(self.var, ctx)
         return self.var._interpolate_grad(ctx.coords)
 
     def depends_on(self, kinds):
@@ -1180,14 +1233,19 @@ def _input_context(inputData):
     elif hasattr(inputData, "object") and hasattr(getattr(inputData, "object"), "_axes"):
         # a mesh's vertex set: its vertices (FeMesh_IndexSet as a FunctionInput)
         pts = np.asarray(inputData.object.data, dtype=np.float64)[inputData.data.astype(np.int64)]
-    elif inputData is None:
-        pts = np.zeros((1, 1))
-    elif isinstance(inputData, numbers.Number):
-        pts = np.array([[float(inputData)]])
     else:
-        pts = np.asarray(inputData, dtype=np.float64)
-        if pts.ndim == 1:
-            pts = pts[None, :]
+        if inputData is None:
+            pts = np.zeros((1, 1))
+        elif isinstance(inputData, numbers.Number):
+            pts = np.array([[float(inputData)]])
+        else:
+            pts = np.asarray(inputData, dtype=np.float64)
+            if pts.ndim == 1:
+                pts = pts[None, :]
+        t = torch.from_numpy(np.ascontiguousarray(pts)).to(dev)
+        ctx = EvalContext(torch.full((t.shape[0],), -1, dtype=torch.int64, device=dev), lambda: t, dev)
+        ctx.check_domain = True      # user coordinates: mesh variables refuse points outside their mesh
+        return ctx
     t = torch.from_numpy(np.ascontiguousarray(pts)).to(dev)
     return EvalContext(torch.full((t.shape[0],), -1, dtype=torch.int64, device=dev), lambda: t, dev)
 

@@ -393,6 +393,9 @@ class MeshVariable:
     def evaluate(self, inputData=None, inputType=None):
         return self._as_function().evaluate(inputData, inputType)
 
+    def evaluate_global(self, inputData, inputType=None):
+        return self._as_function().evaluate_global(inputData, inputType)
+
     def _interpolate(self, coords):
         """Field values at global points (device tensor [n, dim] -> [n, k])."""
         ctx = self._primary().ctx

@@ -149,6 +149,9 @@ class SwarmVariable:
         (P/function/_function.py:808-930)."""
         return self._as_function().evaluate(inputData, inputType)
 
+    def evaluate_global(self, inputData, inputType=None):
+        return self._as_function().evaluate_global(inputData, inputType)
+
     def __getitem__(self, i): return self._as_function()[i]
     def __neg__(self): return -self._as_function()
     def __pow__(self, o): return self._as_function() ** o
